@@ -1,0 +1,193 @@
+/*
+ * sfmba.h - C ABI of the GB300 bundle adjuster (libsfmba_gb300.so).
+ *
+ * This is the drop-in boundary for the `sfm-ba` crate of sfmtory. Each entry
+ * point names the Rust item it replaces (paths are inside the sfmtory
+ * project). All arrays are plain caller-owned buffers in structure-of-arrays
+ * form; no entry point takes ownership of anything and none aborts: every
+ * call returns an `sfmba_status` and `sfmba_last_error()` gives the message
+ * of the last failure on the calling thread.
+ *
+ * Differences in shape from the Rust API, all mechanical:
+ *   - `Vec<CameraModel>` becomes a model id per camera plus a padded
+ *     [num_cameras][8] parameter table in `CameraModel::params()` order.
+ *   - `Pose` is 7 doubles: Hamilton quaternion (qw, qx, qy, qz) then t.
+ *   - `Vec<bool>` masks become uint8 arrays of full length, or NULL for
+ *     "all false" (the Rust code reads missing entries as false).
+ *   - `fixed_camera_params: Vec<Vec<bool>>` becomes a padded
+ *     [num_cameras][8] uint8 table (entries past a camera's parameter count,
+ *     or past the inner Vec's length, are 0).
+ *   - `BaOutput` is written into caller buffers named in `sfmba_result`.
+ */
+#ifndef SFMBA_H
+#define SFMBA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFMBA_MAX_CAMERA_PARAMS 8
+#define SFMBA_POSE_STRIDE 7
+
+/* COLMAP model ids, crates/sfm-core/src/camera.rs:74-83 (`model_id`). */
+typedef enum sfmba_camera_model {
+    SFMBA_SIMPLE_PINHOLE = 0, /* f, cx, cy                         */
+    SFMBA_PINHOLE = 1,        /* fx, fy, cx, cy                    */
+    SFMBA_SIMPLE_RADIAL = 2,  /* f, cx, cy, k                      */
+    SFMBA_RADIAL = 3,         /* f, cx, cy, k1, k2                 */
+    SFMBA_OPENCV = 4,         /* fx, fy, cx, cy, k1, k2, p1, p2    */
+    SFMBA_OPENCV_FISHEYE = 5  /* fx, fy, cx, cy, k1, k2, k3, k4    */
+} sfmba_camera_model;
+
+/* crates/sfm-ba/src/lib.rs:213-218 (`RobustLoss`). */
+typedef enum sfmba_robust_loss {
+    SFMBA_LOSS_NONE = 0,
+    SFMBA_LOSS_HUBER = 1,
+    SFMBA_LOSS_CAUCHY = 2
+} sfmba_robust_loss;
+
+/* Arithmetic of the residual/Jacobian/Schur/PCG kernels. The total cost,
+ * the step-acceptance test and the dense Cholesky are FP64 in both. */
+typedef enum sfmba_precision {
+    SFMBA_PRECISION_FP64 = 0,  /* plain all-FP64 path                      */
+    SFMBA_PRECISION_MIXED = 1  /* FP32 residual/Jacobian/Schur/PCG kernels  */
+} sfmba_precision;
+
+/* How the reduced camera system is solved. */
+typedef enum sfmba_solver {
+    SFMBA_SOLVER_AUTO = 0,   /* dense Cholesky up to a few thousand unknowns, else PCG */
+    SFMBA_SOLVER_DENSE = 1,  /* explicit Schur complement + FP64 blocked Cholesky (LU fallback) */
+    SFMBA_SOLVER_PCG = 2     /* matrix-free Schur PCG, block-Jacobi preconditioner */
+} sfmba_solver;
+
+typedef enum sfmba_status {
+    SFMBA_OK = 0,
+    SFMBA_ERR_INVALID_ARGUMENT = 1,
+    SFMBA_ERR_CUDA = 2,
+    SFMBA_ERR_OUT_OF_MEMORY = 3,
+    SFMBA_ERR_NO_DEVICE = 4,
+    SFMBA_ERR_UNSUPPORTED = 5,
+    SFMBA_ERR_INTERNAL = 6
+} sfmba_status;
+
+/* crates/sfm-ba/src/lib.rs:56-96 (`Observation`, `BaInput`). */
+typedef struct sfmba_problem {
+    int64_t num_images;
+    int64_t num_cameras;
+    int64_t num_points;
+    int64_t num_observations;
+    const int32_t *camera_of_image;      /* [num_images]                        */
+    const int32_t *camera_model;         /* [num_cameras] sfmba_camera_model    */
+    const double *camera_params;         /* [num_cameras][8]                    */
+    const double *poses;                 /* [num_images][7] qw qx qy qz tx ty tz */
+    const double *points;                /* [num_points][3]                     */
+    const int32_t *obs_image;            /* [num_observations]                  */
+    const int32_t *obs_point;            /* [num_observations]                  */
+    const double *obs_xy;                /* [num_observations][2] pixels        */
+    const uint8_t *fixed_poses;          /* [num_images] or NULL                */
+    const uint8_t *fixed_cameras;        /* [num_cameras] or NULL               */
+    const uint8_t *fixed_camera_params;  /* [num_cameras][8] or NULL            */
+} sfmba_problem;
+
+/* crates/sfm-ba/src/lib.rs:220-238 (`BaParams` and its Default), plus the
+ * GB300 solver controls. `sfmba_default_options` fills the reference
+ * defaults (50 iterations, lambda0 1e-3, Huber at 2 px). */
+typedef struct sfmba_options {
+    int32_t max_iterations;
+    double initial_lambda;
+    int32_t robust_loss;          /* sfmba_robust_loss */
+    double loss_scale_px;
+    int32_t precision;            /* sfmba_precision   */
+    int32_t solver;               /* sfmba_solver      */
+    int32_t pcg_max_iterations;   /* per damping retry (PCG solver)            */
+    double pcg_tolerance;         /* relative preconditioned-residual target   */
+    int32_t refinement_steps;     /* FP64 iterative-refinement steps (dense)   */
+    double target_cost;           /* > 0: also stop once cost <= target_cost   */
+    int32_t dense_max_dim;        /* AUTO picks dense up to this reduced dim   */
+    int32_t reserved[7];
+} sfmba_options;
+
+/* crates/sfm-ba/src/lib.rs:240-247 (`BaOutput`). Output buffers are caller
+ * owned and may be NULL to skip that copy-out. */
+typedef struct sfmba_result {
+    double *poses;                /* [num_images][7]  */
+    double *points;               /* [num_points][3]  */
+    double *camera_params;        /* [num_cameras][8] */
+    double initial_cost;
+    double final_cost;
+    int32_t iterations_run;
+    int32_t status;
+    int32_t damping_retries;      /* inner retries summed over outer iterations */
+    int32_t solver_used;          /* sfmba_solver actually run                 */
+    int64_t linear_iterations;    /* PCG iterations summed over all retries    */
+    int64_t reduced_dim;          /* size of the reduced camera system          */
+    int64_t valid_observations;   /* observations in front of their camera at the end */
+    double seconds;               /* wall time of the call, measured inside     */
+    double reserved[4];
+} sfmba_result;
+
+/* Reference defaults of BaParams (lib.rs:229-238) and of the GB300 controls. */
+void sfmba_default_options(sfmba_options *options);
+
+/* Replaces `pub fn bundle_adjust(input: BaInput, params: &BaParams) -> BaOutput`
+ * (crates/sfm-ba/src/lib.rs:747). All pointers are host pointers. */
+int sfmba_bundle_adjust(const sfmba_problem *problem, const sfmba_options *options,
+                        sfmba_result *result);
+
+/* Same solve with every problem and result pointer in device memory of the
+ * current CUDA device; runs on `stream` (a cudaStream_t, or NULL for the
+ * library's own stream) and returns after the solve has finished. */
+int sfmba_bundle_adjust_device(const sfmba_problem *problem, const sfmba_options *options,
+                               sfmba_result *result, void *stream);
+
+/* Replaces `pub fn mean_reprojection_error(input: &BaInput) -> f64`
+ * (crates/sfm-ba/src/lib.rs:708-725). Host pointers. */
+int sfmba_mean_reprojection_error(const sfmba_problem *problem, double *out_mean_px);
+
+/* The robust cost `bundle_adjust` minimises (lib.rs:727-745, `total_cost`,
+ * private in the crate): sum over observations of w * |r|^2. Host pointers. */
+int sfmba_total_cost(const sfmba_problem *problem, const sfmba_options *options,
+                     double *out_cost);
+
+/* Replaces `pub fn default_fixed_params_mask(&[CameraModel]) -> Vec<Vec<bool>>`
+ * (crates/sfm-ba/src/intrinsics.rs:49-61). Writes [num_cameras][8]. */
+int sfmba_default_fixed_params_mask(int64_t num_cameras, const int32_t *camera_model,
+                                    uint8_t *out_mask);
+
+/* Replaces `pub fn refine_intrinsics(...)` (crates/sfm-ba/src/intrinsics.rs:116-147)
+ * with IntrinsicsRefineParams mapped onto sfmba_options (max_iterations,
+ * initial_lambda, robust_loss, loss_scale_px). Updates problem->camera_params
+ * in place through `camera_params_inout` ([num_cameras][8], host). */
+int sfmba_refine_intrinsics(const sfmba_problem *problem, const sfmba_options *options,
+                            double *camera_params_inout);
+
+/* Many independent bundle adjustments (local BA windows, as
+ * sfm-reconstruction's BaScope::Local issues them one call at a time,
+ * crates/sfm-reconstruction/src/lib.rs:1287-1299) solved together, each
+ * with its own damping and stopping. Host pointers. */
+int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *windows,
+                                const sfmba_options *options, sfmba_result *results);
+
+/* Residual and Jacobian blocks of individual observations, computed on the
+ * GPU by the same device code the solver uses (crates/sfm-ba/src/lib.rs:327-590,
+ * `analytic_jacobians`). For observation o: r[o][2], j_pose[o][2][6],
+ * j_point[o][2][3], j_camera[o][2][8] (columns past the model's parameter
+ * count are 0), valid[o] = point in front of the camera (z > 1e-9).
+ * `precision` selects the FP64 or FP32 kernel. Host pointers. */
+int sfmba_residuals_jacobians(const sfmba_problem *problem, int32_t precision, double *r,
+                              double *j_pose, double *j_point, double *j_camera,
+                              uint8_t *valid);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *sfmba_last_error(void);
+
+/* Library version string. */
+const char *sfmba_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFMBA_H */

@@ -1,0 +1,198 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes loader for the CPU FP64 oracle
+(``oracle/sfmba_oracle.cpp``), a restatement of sfmtory's sfm-ba.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+leg may import this module, and only as the checker / CPU baseline. The
+product path (:mod:`sfmtory_gb300`) never imports it.
+
+Parity status: pinned by the reference's own known-answer tests (analytic vs
+central-difference Jacobians for all six camera models, convergence tests);
+the Rust reference cannot be built here and publishes no numeric golden
+outputs, so exact agreement with its binary is unpinned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+from sfmtory_gb300.abi import PackedProblem, ResultBuffers, SfmbaOptions, default_options
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "liboracle_sfmba.so")
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++ -fopenmp)."""
+    src = os.path.join(_HERE, "sfmba_oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-C", _HERE, "-B" if force else "liboracle_sfmba.so"], check=True,
+                       stdout=subprocess.DEVNULL)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(_LIB_PATH)
+            vp, dp, i32, i64 = C.c_void_p, C.POINTER(C.c_double), C.c_int32, C.c_int64
+            L.oracle_bundle_adjust.argtypes = [vp, vp, vp]
+            L.oracle_total_cost.argtypes = [vp, vp, dp]
+            L.oracle_mean_reprojection_error.argtypes = [vp, dp]
+            L.oracle_default_fixed_params_mask.argtypes = [i64, vp, vp]
+            L.oracle_refine_intrinsics.argtypes = [vp, vp, vp]
+            for f in (L.oracle_analytic_jacobians, L.oracle_numerical_jacobians):
+                f.argtypes = [vp, C.c_int, vp, vp, C.c_double, C.c_double, vp, vp, vp, vp]
+                f.restype = C.c_int
+            L.oracle_project.argtypes = [C.c_int, vp, vp, vp]
+            L.oracle_perturb_pose.argtypes = [vp, vp, vp]
+            L.oracle_transform_point.argtypes = [vp, vp, vp]
+            L.oracle_robust_weight.argtypes = [C.c_double, C.c_int, C.c_double]
+            L.oracle_robust_weight.restype = C.c_double
+            L.oracle_set_threads.argtypes = [C.c_int]
+            L.oracle_threads.restype = C.c_int
+            L.oracle_phase_seconds.argtypes = [vp]
+            _lib = L
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def threads() -> int:
+    return int(lib().oracle_threads())
+
+
+def phase_seconds() -> np.ndarray:
+    out = np.zeros(8)
+    lib().oracle_phase_seconds(out.ctypes.data)
+    return out
+
+
+def _opts(options=None, **kw):
+    if options is None:
+        options = default_options(**kw)
+    elif kw:
+        for k, v in kw.items():
+            setattr(options, k, v)
+    return options
+
+
+class OracleResult:
+    def __init__(self, buffers: ResultBuffers):
+        r = buffers.struct
+        self.poses = buffers.poses
+        self.points = buffers.points
+        self.camera_params = buffers.camera_params
+        self.initial_cost = r.initial_cost
+        self.final_cost = r.final_cost
+        self.iterations_run = r.iterations_run
+        self.damping_retries = r.damping_retries
+        self.reduced_dim = r.reduced_dim
+        self.seconds = r.seconds
+
+
+def bundle_adjust(problem, options: SfmbaOptions | None = None, **kw) -> OracleResult:
+    packed = PackedProblem(problem)
+    buf = ResultBuffers(packed)
+    o = _opts(options, **kw)
+    st = lib().oracle_bundle_adjust(C.byref(packed.struct), C.byref(o), C.byref(buf.struct))
+    if st != 0:
+        raise ValueError(f"oracle_bundle_adjust failed with status {st}")
+    return OracleResult(buf)
+
+
+def total_cost(problem, options: SfmbaOptions | None = None, **kw) -> float:
+    packed = PackedProblem(problem)
+    out = C.c_double()
+    st = lib().oracle_total_cost(C.byref(packed.struct), C.byref(_opts(options, **kw)), C.byref(out))
+    if st != 0:
+        raise ValueError(f"oracle_total_cost failed with status {st}")
+    return out.value
+
+
+def mean_reprojection_error(problem) -> float:
+    packed = PackedProblem(problem)
+    out = C.c_double()
+    st = lib().oracle_mean_reprojection_error(C.byref(packed.struct), C.byref(out))
+    if st != 0:
+        raise ValueError(f"oracle_mean_reprojection_error failed with status {st}")
+    return out.value
+
+
+def default_fixed_params_mask(models) -> np.ndarray:
+    models = np.ascontiguousarray(models, dtype=np.int32)
+    out = np.zeros((len(models), 8), dtype=np.uint8)
+    st = lib().oracle_default_fixed_params_mask(len(models), models.ctypes.data, out.ctypes.data)
+    if st != 0:
+        raise ValueError("invalid camera model")
+    return out.astype(bool)
+
+
+def refine_intrinsics(problem, options: SfmbaOptions | None = None, **kw) -> np.ndarray:
+    """intrinsics.rs refine_intrinsics defaults: 30 iterations, lambda 1e-3, Huber 2 px."""
+    base = dict(max_iterations=30)
+    base.update(kw)
+    packed = PackedProblem(problem)
+    cams = packed.camera_params.copy()
+    st = lib().oracle_refine_intrinsics(C.byref(packed.struct), C.byref(_opts(options, **base)),
+                                        cams.ctypes.data)
+    if st != 0:
+        raise ValueError(f"oracle_refine_intrinsics failed with status {st}")
+    return cams
+
+
+def _jac(fn, pose7, model, params, X, obs):
+    pose7 = np.ascontiguousarray(pose7, dtype=np.float64)
+    p = np.zeros(8)
+    p[: len(params)] = params
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    r, jp, jx, jc = np.zeros(2), np.zeros((2, 6)), np.zeros((2, 3)), np.zeros((2, 8))
+    ok = fn(pose7.ctypes.data, int(model), p.ctypes.data, X.ctypes.data, float(obs[0]), float(obs[1]),
+            r.ctypes.data, jp.ctypes.data, jx.ctypes.data, jc.ctypes.data)
+    if not ok:
+        return None
+    return r, jp, jx, jc
+
+
+def analytic_jacobians(pose7, model, params, X, obs):
+    """(r, J_pose 2x6, J_point 2x3, J_cam 2x8) or None (lib.rs:327-590)."""
+    return _jac(lib().oracle_analytic_jacobians, pose7, model, params, X, obs)
+
+
+def numerical_jacobians(pose7, model, params, X, obs):
+    """Central differences, step 1e-6 (lib.rs:600-670)."""
+    return _jac(lib().oracle_numerical_jacobians, pose7, model, params, X, obs)
+
+
+def perturb_pose(pose7, delta6) -> np.ndarray:
+    pose7 = np.ascontiguousarray(pose7, dtype=np.float64)
+    delta6 = np.ascontiguousarray(delta6, dtype=np.float64)
+    out = np.zeros(7)
+    lib().oracle_perturb_pose(pose7.ctypes.data, delta6.ctypes.data, out.ctypes.data)
+    return out
+
+
+def transform_point(pose7, X) -> np.ndarray:
+    pose7 = np.ascontiguousarray(pose7, dtype=np.float64)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    out = np.zeros(3)
+    lib().oracle_transform_point(pose7.ctypes.data, X.ctypes.data, out.ctypes.data)
+    return out
+
+
+def project(model, params, pc) -> np.ndarray:
+    p = np.zeros(8)
+    p[: len(params)] = params
+    pc = np.ascontiguousarray(pc, dtype=np.float64)
+    out = np.zeros(2)
+    lib().oracle_project(int(model), p.ctypes.data, pc.ctypes.data, out.ctypes.data)
+    return out

@@ -1,0 +1,160 @@
+"""The reference's own sfm-ba tests, run against the CPU FP64 oracle.
+
+These pin the oracle before it is trusted as the parity reference for the GPU
+path: crates/sfm-ba/src/lib.rs:1245-1592 (6 analytic-vs-numerical Jacobian
+tests, 2 convergence tests) and crates/sfm-ba/src/intrinsics.rs:252-383
+(3 intrinsics tests), with the reference's fixtures and tolerances.
+"""
+import numpy as np
+import pytest
+
+from sfmtory_gb300 import abi, scenes
+
+MODELS = list(scenes.JACOBIAN_TEST_CAMERAS)
+
+
+@pytest.mark.parametrize("model", MODELS, ids=[abi.MODEL_NAMES[m] for m in MODELS])
+def test_analytic_matches_numerical(oracle_lib, model):
+    """assert_analytic_matches_numerical (lib.rs:1252-1295): residual < 1e-9,
+    pose/point Jacobian Frobenius < 1e-5, camera Jacobian < 1e-4."""
+    pose, X, obs = scenes.jacobian_test_fixture()
+    params = scenes.JACOBIAN_TEST_CAMERAS[model]
+    num = oracle_lib.numerical_jacobians(pose, model, params, X, obs)
+    an = oracle_lib.analytic_jacobians(pose, model, params, X, obs)
+    assert num is not None and an is not None, "point in front of camera"
+    assert np.linalg.norm(num[0] - an[0]) < 1e-9
+    assert np.linalg.norm(num[1] - an[1]) < 1e-5
+    assert np.linalg.norm(num[2] - an[2]) < 1e-5
+    assert np.linalg.norm(num[3] - an[3]) < 1e-4
+    # Columns past the model's parameter count are zero.
+    assert np.all(an[3][:, abi.MODEL_DOF[model]:] == 0)
+
+
+def test_recovers_ground_truth_from_perturbed_initialization(oracle_lib):
+    """lib.rs:1368-1476."""
+    p = scenes.recovers_ground_truth_fixture()
+    out = oracle_lib.bundle_adjust(p, max_iterations=30)
+    assert out.final_cost < out.initial_cost * 0.01
+    mean_sq = out.final_cost / (len(out.poses) * 25)
+    assert np.sqrt(mean_sq) < 0.5
+    t = out.poses[1, 4:]
+    tt = p.meta["true_poses"][1, 4:]
+    cos = np.dot(t / np.linalg.norm(t), tt / np.linalg.norm(tt))
+    assert cos > 0.999
+    assert abs(np.linalg.norm(t) / np.linalg.norm(tt) - 1.0) < 0.1
+
+
+def test_joint_optimization_recovers_shared_camera_focal_length(oracle_lib):
+    """lib.rs:1487-1592: pre-converge with the wrong focal fixed, then solve
+    jointly with the shared camera free."""
+    p = scenes.shared_focal_fixture()
+    pre = oracle_lib.bundle_adjust(p, max_iterations=50)
+    joint = p.copy(poses=pre.poses, points=pre.points, fixed_cameras=np.array([False]))
+    out = oracle_lib.bundle_adjust(joint, max_iterations=50)
+    f = out.camera_params[0, 0]
+    assert abs(f - 1500.0) / 1500.0 < 0.02, f
+
+
+def test_recovers_true_focal_length_from_wrong_initial_guess(oracle_lib):
+    """intrinsics.rs:262-305."""
+    p = scenes.intrinsics_fixture()
+    cams = oracle_lib.refine_intrinsics(p)
+    assert abs(cams[0, 0] - 1500.0) < 1.0, cams[0, 0]
+
+
+def test_leaves_camera_unchanged_with_too_few_observations(oracle_lib):
+    """intrinsics.rs:307-340: one observation (< 8) leaves the camera as is."""
+    p = scenes.intrinsics_fixture(n_points=1)
+    p = p.copy(points=np.array([[0.1, 0.1, 3.0]]))
+    from sfmtory_gb300.problem import project
+
+    p.obs_xy = project(np.array([abi.SIMPLE_PINHOLE]), np.array([[1500.0, 500, 400, 0, 0, 0, 0, 0]]),
+                       p.points)
+    cams = oracle_lib.refine_intrinsics(p)
+    assert np.array_equal(cams, p.camera_params)
+
+
+def test_improves_overall_reprojection_cost_end_to_end(oracle_lib):
+    """intrinsics.rs:342-382: refinement cuts the camera cost 100x."""
+    p = scenes.intrinsics_fixture(n_points=30)
+    before = oracle_lib.total_cost(p)
+    cams = oracle_lib.refine_intrinsics(p)
+    after = oracle_lib.total_cost(p.copy(camera_params=cams))
+    assert after < before * 0.01
+
+
+def test_default_fixed_params_mask(oracle_lib):
+    """intrinsics.rs:33-61: principal point is [1,2] for SP/SR/R, [2,3] otherwise."""
+    m = oracle_lib.default_fixed_params_mask(list(range(6)))
+    expect = {0: [1, 2], 1: [2, 3], 2: [1, 2], 3: [1, 2], 4: [2, 3], 5: [2, 3]}
+    for model, idx in expect.items():
+        row = np.zeros(8, bool)
+        row[idx] = True
+        assert np.array_equal(m[model], row)
+
+
+def test_perturb_pose_left_multiplies(oracle_lib):
+    """perturb_pose (lib.rs:263-269) agrees with the numpy restatement used
+    by the scene generators, and zero delta leaves the pose bit-identical."""
+    from sfmtory_gb300.problem import perturb_pose
+
+    pose, _, _ = scenes.jacobian_test_fixture()
+    d = np.array([0.01, -0.02, 0.03, 0.1, 0.2, -0.3])
+    assert np.allclose(oracle_lib.perturb_pose(pose, d), perturb_pose(pose, d), atol=1e-15)
+    assert np.array_equal(oracle_lib.perturb_pose(pose, np.zeros(6)), pose)
+
+
+def test_projection_matches_numpy(oracle_lib):
+    from sfmtory_gb300.problem import project
+
+    rng = np.random.default_rng(1)
+    for m, params in scenes.JACOBIAN_TEST_CAMERAS.items():
+        for _ in range(5):
+            pc = rng.normal(size=3) + np.array([0, 0, 3.0])
+            p = np.zeros(8)
+            p[: len(params)] = params
+            a = oracle_lib.project(m, params, pc)
+            b = project(np.array([m]), p[None], pc[None])[0]
+            assert np.allclose(a, b, rtol=0, atol=1e-9)
+
+
+def test_total_cost_and_mean_error_semantics(oracle_lib):
+    """total_cost = sum w |r|^2 skipping z <= 1e-9 (lib.rs:727-745);
+    mean error = mean |r| over valid observations (lib.rs:708-725)."""
+    from sfmtory_gb300.problem import reprojection_residuals
+
+    p = scenes.ring16(seed=3, scale=0.05)
+    r, valid = reprojection_residuals(p)
+    n = np.linalg.norm(r[valid], axis=1)
+    assert np.isclose(oracle_lib.total_cost(p, robust_loss=abi.LOSS_NONE), np.sum(n**2), rtol=1e-12)
+    w = np.where(n <= 2.0, 1.0, 2.0 / n)
+    assert np.isclose(oracle_lib.total_cost(p), np.sum(w * n**2), rtol=1e-12)
+    s = 1.5
+    w = 1.0 / (1.0 + (n / s) ** 2)
+    assert np.isclose(oracle_lib.total_cost(p, robust_loss=abi.LOSS_CAUCHY, loss_scale_px=s),
+                      np.sum(w * n**2), rtol=1e-12)
+    assert np.isclose(oracle_lib.mean_reprojection_error(p), n.mean(), rtol=1e-12)
+    # A point pushed behind every camera drops out of both.
+    q = p.copy()
+    q.points[0] = np.array([50.0, 0.0, 0.0])
+    r2, v2 = reprojection_residuals(q)
+    assert v2.sum() < valid.sum()
+    assert np.isclose(oracle_lib.mean_reprojection_error(q), np.linalg.norm(r2[v2], axis=1).mean())
+
+
+def test_total_dim_zero_returns_initial_cost(oracle_lib):
+    """lib.rs:777-787: every pose and camera fixed -> no iterations."""
+    p = scenes.recovers_ground_truth_fixture().copy(fixed_poses=np.array([True, True]))
+    out = oracle_lib.bundle_adjust(p)
+    assert out.iterations_run == 0
+    assert out.final_cost == out.initial_cost
+    assert np.array_equal(out.points, p.points)
+
+
+def test_ring16_converges(oracle_lib):
+    p = scenes.ring16(seed=0, scale=0.1)
+    out = oracle_lib.bundle_adjust(p, robust_loss=abi.LOSS_NONE, max_iterations=50)
+    assert out.final_cost < 0.05 * out.initial_cost
+    n_obs = p.num_observations
+    # Noise sigma 0.5 px -> E|r|^2 ~ 2 * 0.25 per observation.
+    assert out.final_cost / n_obs < 0.6
