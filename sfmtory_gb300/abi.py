@@ -126,8 +126,10 @@ class PackedProblem:
         self.camera_of_image = np.ascontiguousarray(p.camera_of_image, dtype=np.int32)
         self.camera_model = np.ascontiguousarray(p.camera_model, dtype=np.int32)
         cp = np.zeros((len(self.camera_model), MAX_CAMERA_PARAMS), dtype=np.float64)
-        src = np.asarray(p.camera_params, dtype=np.float64).reshape(len(self.camera_model), -1)
-        cp[:, : src.shape[1]] = src
+        src = np.asarray(p.camera_params, dtype=np.float64)
+        if src.size:
+            src = src.reshape(len(self.camera_model), -1)
+            cp[:, : src.shape[1]] = src
         self.camera_params = cp
         self.poses = np.ascontiguousarray(p.poses, dtype=np.float64).reshape(-1, POSE_STRIDE)
         self.points = np.ascontiguousarray(p.points, dtype=np.float64).reshape(-1, 3)

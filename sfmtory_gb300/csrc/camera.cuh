@@ -1,0 +1,262 @@
+// Camera models (COLMAP names and parameter order) and the per-observation
+// residual with its hand-written adjoint Jacobian, for FP32 and FP64.
+//
+// Reference semantics: crates/sfm-core/src/camera.rs:204-244 (project),
+// crates/sfm-core/src/pose.rs:46-48 (transform_point),
+// crates/sfm-ba/src/lib.rs:249-261 (reprojection_residual),
+// crates/sfm-ba/src/lib.rs:282-590 (pose_point_jacobians, analytic_jacobians),
+// crates/sfm-ba/src/lib.rs:677-694 (robust_weight).
+#pragma once
+
+#include "common.cuh"
+
+namespace sfmba {
+
+template <typename T>
+__device__ __forceinline__ T dev_sqrt(T x);
+template <>
+__device__ __forceinline__ float dev_sqrt<float>(float x) { return sqrtf(x); }
+template <>
+__device__ __forceinline__ double dev_sqrt<double>(double x) { return sqrt(x); }
+
+template <typename T>
+__device__ __forceinline__ T dev_atan(T x);
+template <>
+__device__ __forceinline__ float dev_atan<float>(float x) { return atanf(x); }
+template <>
+__device__ __forceinline__ double dev_atan<double>(double x) { return atan(x); }
+
+// Per-image constants of one linearisation pass, in the kernel's precision:
+// rotation matrix and translation of the pose, the camera's parameters and
+// which columns of the image block are unknowns.
+template <typename T>
+struct __align__(16) ImageLin {
+    T R[9];
+    T t[3];
+    T c[8];
+    int model;
+    int active;  // bit r set: column r of the image block is an unknown
+    int pad[2];
+};
+
+// Forward projection of normalised coordinates plus the local derivatives
+// the adjoint pass needs: A = d(u,v)/d(xp,yp) (2x2) and the parameter
+// columns G = d(u,v)/d(params) (2x8, zero past the model's count).
+template <typename T>
+__device__ __forceinline__ void distort(int model, const T *c, T xp, T yp, T &u, T &v, T A[2][2],
+                                        T G[2][8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) { G[0][i] = T(0); G[1][i] = T(0); }
+    A[0][1] = T(0);
+    A[1][0] = T(0);
+    switch (model) {
+    case SFMBA_SIMPLE_PINHOLE: {
+        const T f = c[0];
+        u = f * xp + c[1];
+        v = f * yp + c[2];
+        A[0][0] = f; A[1][1] = f;
+        G[0][0] = xp; G[0][1] = T(1);
+        G[1][0] = yp; G[1][2] = T(1);
+        break;
+    }
+    case SFMBA_PINHOLE: {
+        u = c[0] * xp + c[2];
+        v = c[1] * yp + c[3];
+        A[0][0] = c[0]; A[1][1] = c[1];
+        G[0][0] = xp; G[0][2] = T(1);
+        G[1][1] = yp; G[1][3] = T(1);
+        break;
+    }
+    case SFMBA_SIMPLE_RADIAL:
+    case SFMBA_RADIAL: {
+        const bool two = model == SFMBA_RADIAL;
+        const T f = c[0], k1 = c[3], k2 = two ? c[4] : T(0);
+        const T r2 = xp * xp + yp * yp;
+        const T d = two ? T(1) + k1 * r2 + k2 * r2 * r2 : T(1) + k1 * r2;
+        const T dd = two ? k1 + T(2) * k2 * r2 : k1;  // d(d)/d(r2)
+        u = f * xp * d + c[1];
+        v = f * yp * d + c[2];
+        A[0][0] = f * (d + T(2) * dd * xp * xp);
+        A[0][1] = T(2) * f * dd * xp * yp;
+        A[1][0] = A[0][1];
+        A[1][1] = f * (d + T(2) * dd * yp * yp);
+        G[0][0] = xp * d; G[0][1] = T(1); G[0][3] = f * xp * r2;
+        G[1][0] = yp * d; G[1][2] = T(1); G[1][3] = f * yp * r2;
+        if (two) {
+            G[0][4] = f * xp * r2 * r2;
+            G[1][4] = f * yp * r2 * r2;
+        }
+        break;
+    }
+    case SFMBA_OPENCV: {
+        const T fx = c[0], fy = c[1], k1 = c[4], k2 = c[5], p1 = c[6], p2 = c[7];
+        const T r2 = xp * xp + yp * yp;
+        const T rad = T(1) + k1 * r2 + k2 * r2 * r2;
+        const T xd = xp * rad + T(2) * p1 * xp * yp + p2 * (r2 + T(2) * xp * xp);
+        const T yd = yp * rad + p1 * (r2 + T(2) * yp * yp) + T(2) * p2 * xp * yp;
+        u = fx * xd + c[2];
+        v = fy * yd + c[3];
+        const T kr = k1 + T(2) * k2 * r2;
+        const T dxx = rad + T(2) * kr * xp * xp + T(2) * p1 * yp + T(6) * p2 * xp;
+        const T dxy = T(2) * kr * xp * yp + T(2) * p1 * xp + T(2) * p2 * yp;
+        const T dyy = rad + T(2) * kr * yp * yp + T(6) * p1 * yp + T(2) * p2 * xp;
+        A[0][0] = fx * dxx; A[0][1] = fx * dxy;
+        A[1][0] = fy * dxy; A[1][1] = fy * dyy;
+        G[0][0] = xd; G[0][2] = T(1);
+        G[0][4] = fx * xp * r2; G[0][5] = fx * xp * r2 * r2;
+        G[0][6] = fx * T(2) * xp * yp; G[0][7] = fx * (r2 + T(2) * xp * xp);
+        G[1][1] = yd; G[1][3] = T(1);
+        G[1][4] = fy * yp * r2; G[1][5] = fy * yp * r2 * r2;
+        G[1][6] = fy * (r2 + T(2) * yp * yp); G[1][7] = fy * T(2) * xp * yp;
+        break;
+    }
+    default: {  // SFMBA_OPENCV_FISHEYE (equidistant)
+        const T fx = c[0], fy = c[1], k1 = c[4], k2 = c[5], k3 = c[6], k4 = c[7];
+        T r = dev_sqrt<T>(xp * xp + yp * yp);
+        r = r > T(1e-12) ? r : T(1e-12);
+        const T th = dev_atan<T>(r), t2 = th * th, t4 = t2 * t2, t6 = t4 * t2, t8 = t4 * t4;
+        const T poly = T(1) + k1 * t2 + k2 * t4 + k3 * t6 + k4 * t8;
+        const T thd = th * poly, s = thd / r;
+        u = fx * (xp * s) + c[2];
+        v = fy * (yp * s) + c[3];
+        const T dpoly = k1 + T(2) * k2 * t2 + T(3) * k3 * t4 + T(4) * k4 * t6;
+        const T dthd = poly + T(2) * t2 * dpoly;
+        const T ds_dr = (dthd / (T(1) + r * r) * r - thd) / (r * r);
+        const T dsx = ds_dr * (xp / r), dsy = ds_dr * (yp / r);
+        A[0][0] = fx * (s + xp * dsx); A[0][1] = fx * xp * dsy;
+        A[1][0] = fy * yp * dsx;       A[1][1] = fy * (s + yp * dsy);
+        G[0][0] = xp * s; G[0][2] = T(1);
+        G[1][1] = yp * s; G[1][3] = T(1);
+        const T tk[4] = {th * t2, th * t4, th * t6, th * t8};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            G[0][4 + i] = fx * xp * tk[i] / r;
+            G[1][4 + i] = fy * yp * tk[i] / r;
+        }
+        break;
+    }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T robust_weight(T n, int loss, T scale) {
+    const T s = scale > T(1e-9) ? scale : T(1e-9);
+    if (loss == SFMBA_LOSS_HUBER) return n <= s ? T(1) : s / n;
+    if (loss == SFMBA_LOSS_CAUCHY) {
+        const T q = n / s;
+        return T(1) / (T(1) + q * q);
+    }
+    return T(1);
+}
+
+// Residual and Jacobian of one observation, weighted by sqrt(w).
+//
+// Forward pass: pc = R X + t, (xp, yp) = (pc.x, pc.y) / pc.z, pixel = distort.
+// Adjoint pass, once per pixel row (u, then v): the row's sensitivity to the
+// normalised coordinates (row of A) is pulled back through the perspective
+// divide to the camera-frame point (pbar), then to the world point
+// (R^T pbar) and to the left rotation increment ((pc - t) x pbar) and the
+// translation (pbar). Camera-parameter columns come straight from G.
+// Returns false (and zeros) when pc.z <= 1e-9.
+template <typename T, int D>
+__device__ __forceinline__ bool linearize(const ImageLin<T> &im, T X0, T X1, T X2, T ox, T oy,
+                                          int loss, T scale, T rr[2], T jx[6], T jc[2 * D],
+                                          T *weight = nullptr) {
+    const T q0 = im.R[0] * X0 + im.R[1] * X1 + im.R[2] * X2;
+    const T q1 = im.R[3] * X0 + im.R[4] * X1 + im.R[5] * X2;
+    const T q2 = im.R[6] * X0 + im.R[7] * X1 + im.R[8] * X2;
+    const T pc0 = q0 + im.t[0], pc1 = q1 + im.t[1], pc2 = q2 + im.t[2];
+    if (!(pc2 > T(kMinDepth))) {
+        rr[0] = rr[1] = T(0);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) jx[i] = T(0);
+#pragma unroll
+        for (int i = 0; i < 2 * D; ++i) jc[i] = T(0);
+        if (weight) *weight = T(0);
+        return false;
+    }
+    const T iz = T(1) / pc2;
+    const T xp = pc0 * iz, yp = pc1 * iz;
+    T u, v, A[2][2], G[2][8];
+    distort<T>(im.model, im.c, xp, yp, u, v, A, G);
+    rr[0] = u - ox;
+    rr[1] = v - oy;
+    const T n = dev_sqrt<T>(rr[0] * rr[0] + rr[1] * rr[1]);
+    const T w = robust_weight<T>(n, loss, scale);
+    const T s = dev_sqrt<T>(w);
+    if (weight) *weight = w;
+    rr[0] *= s;
+    rr[1] *= s;
+#pragma unroll
+    for (int row = 0; row < 2; ++row) {
+        // pbar = d(pixel_row)/d(pc)
+        const T a0 = A[row][0] * s, a1 = A[row][1] * s;
+        const T pb0 = a0 * iz, pb1 = a1 * iz, pb2 = -(a0 * xp + a1 * yp) * iz;
+        jx[row * 3 + 0] = im.R[0] * pb0 + im.R[3] * pb1 + im.R[6] * pb2;
+        jx[row * 3 + 1] = im.R[1] * pb0 + im.R[4] * pb1 + im.R[7] * pb2;
+        jx[row * 3 + 2] = im.R[2] * pb0 + im.R[5] * pb1 + im.R[8] * pb2;
+        T *o = jc + row * D;
+        const bool pose_on = im.active & 1;
+        o[0] = pose_on ? q1 * pb2 - q2 * pb1 : T(0);
+        o[1] = pose_on ? q2 * pb0 - q0 * pb2 : T(0);
+        o[2] = pose_on ? q0 * pb1 - q1 * pb0 : T(0);
+        o[3] = pose_on ? pb0 : T(0);
+        o[4] = pose_on ? pb1 : T(0);
+        o[5] = pose_on ? pb2 : T(0);
+#pragma unroll
+        for (int k = 0; k < D - 6; ++k) o[6 + k] = ((im.active >> (6 + k)) & 1) ? G[row][k] * s : T(0);
+    }
+    return true;
+}
+
+// FP64 residual exactly as the reference's cost evaluates it: quaternion
+// rotation (pose.rs:46-48) and project() with a true division by z.
+__device__ __forceinline__ bool residual64(const double *pose7, int model, const double *c,
+                                           double X0, double X1, double X2, double ox, double oy,
+                                           double &rx, double &ry) {
+    const double w = pose7[0], x = pose7[1], y = pose7[2], z = pose7[3];
+    const double tx = 2.0 * (y * X2 - z * X1);
+    const double ty = 2.0 * (z * X0 - x * X2);
+    const double tz = 2.0 * (x * X1 - y * X0);
+    const double pc0 = X0 + w * tx + (y * tz - z * ty) + pose7[4];
+    const double pc1 = X1 + w * ty + (z * tx - x * tz) + pose7[5];
+    const double pc2 = X2 + w * tz + (x * ty - y * tx) + pose7[6];
+    if (!(pc2 > kMinDepth)) return false;
+    const double xn = pc0 / pc2, yn = pc1 / pc2;
+    double u, v;
+    switch (model) {
+    case SFMBA_SIMPLE_PINHOLE: u = c[0] * xn + c[1]; v = c[0] * yn + c[2]; break;
+    case SFMBA_PINHOLE: u = c[0] * xn + c[2]; v = c[1] * yn + c[3]; break;
+    case SFMBA_SIMPLE_RADIAL: {
+        const double r2 = xn * xn + yn * yn, d = 1.0 + c[3] * r2;
+        u = c[0] * (xn * d) + c[1]; v = c[0] * (yn * d) + c[2];
+        break;
+    }
+    case SFMBA_RADIAL: {
+        const double r2 = xn * xn + yn * yn, d = 1.0 + c[3] * r2 + c[4] * r2 * r2;
+        u = c[0] * (xn * d) + c[1]; v = c[0] * (yn * d) + c[2];
+        break;
+    }
+    case SFMBA_OPENCV: {
+        const double r2 = xn * xn + yn * yn, rad = 1.0 + c[4] * r2 + c[5] * r2 * r2;
+        const double xd = xn * rad + 2.0 * c[6] * xn * yn + c[7] * (r2 + 2.0 * xn * xn);
+        const double yd = yn * rad + c[6] * (r2 + 2.0 * yn * yn) + 2.0 * c[7] * xn * yn;
+        u = c[0] * xd + c[2]; v = c[1] * yd + c[3];
+        break;
+    }
+    default: {
+        double r = sqrt(xn * xn + yn * yn);
+        r = r > 1e-12 ? r : 1e-12;
+        const double th = atan(r), t2 = th * th;
+        const double thd = th * (1.0 + c[4] * t2 + c[5] * t2 * t2 + c[6] * t2 * t2 * t2 + c[7] * t2 * t2 * t2 * t2);
+        const double s = thd / r;
+        u = c[0] * (xn * s) + c[2]; v = c[1] * (yn * s) + c[3];
+        break;
+    }
+    }
+    rx = u - ox;
+    ry = v - oy;
+    return true;
+}
+
+}  // namespace sfmba

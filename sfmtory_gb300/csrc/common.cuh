@@ -1,0 +1,85 @@
+// Shared definitions of the GB300 bundle adjuster (device + host).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/sfmba.h"
+
+namespace sfmba {
+
+// Error carried from any CUDA call or validation failure up to the C ABI.
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+#define SFMBA_CUDA(call)                                                                       \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            (void)cudaGetLastError();                                                          \
+            throw ::sfmba::Error(e_ == cudaErrorMemoryAllocation ? SFMBA_ERR_OUT_OF_MEMORY     \
+                                                                 : SFMBA_ERR_CUDA,             \
+                                 std::string(#call) + ": " + cudaGetErrorString(e_) + " at " + \
+                                     __FILE__ + ":" + std::to_string(__LINE__));               \
+        }                                                                                      \
+    } while (0)
+
+#define SFMBA_LAUNCH_CHECK() SFMBA_CUDA(cudaGetLastError())
+
+constexpr int kMaxParams = SFMBA_MAX_CAMERA_PARAMS;
+constexpr double kMinDepth = 1e-9;            // crates/sfm-ba/src/lib.rs:256, 338
+constexpr double kFunctionTolerance = 1e-6;   // lib.rs:814
+constexpr int kMaxDampingRetries = 8;         // lib.rs:914
+
+__host__ __device__ inline int model_dof(int model) {
+    // crates/sfm-core/src/camera.rs:136-163 (params().len())
+    return model == 0 ? 3 : model == 1 ? 4 : model == 2 ? 4 : model == 3 ? 5 : (model == 4 || model == 5) ? 8 : 0;
+}
+
+// Width of the per-image variable block: 6 pose columns + the widest camera.
+__host__ __device__ constexpr int block_width_for(int kmax) {
+    return kmax == 0 ? 6 : kmax <= 3 ? 9 : kmax <= 4 ? 10 : kmax <= 5 ? 11 : 14;
+}
+
+// Per-observation linearisation record, array-of-structs, padded to 16 bytes:
+//   [0,2)   r~  = sqrt(w) r
+//   [2,8)   Jx~ = sqrt(w) d r / d point   (2 x 3, row major)
+//   [8,8+2D) Jc~ = sqrt(w) d r / d (pose | camera)  (2 x D, row major)
+// Columns of fixed poses/cameras, masked camera parameters and parameters
+// past the model's count are 0, so those variables drop out of every sum.
+template <int D>
+struct RecLayout {
+    static constexpr int kJx = 2;
+    static constexpr int kJc = 8;
+    static constexpr int kStride = ((8 + 2 * D) + 3) / 4 * 4;
+};
+
+// Device-resident state of the Levenberg-Marquardt loop. Kernels read the
+// damping from here, so captured graphs need no per-retry arguments.
+struct LMState {
+    double lambda;
+    double nu;
+    double cost;         // cost of the current (accepted) parameters
+    double trial_cost;
+    double cost_before;  // cost at the start of the outer iteration
+    int accepted;        // last retry accepted
+    int factor_failed;   // Cholesky failed in the last retry
+    int solve_failed;    // LU fallback also failed
+    int converged;
+    long long valid_obs;
+    long long trial_valid_obs;
+    int pcg_iterations;
+    int pad;
+    double pcg_rr0;
+    double pcg_rr;
+};
+
+inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace sfmba

@@ -1,0 +1,608 @@
+// Dense reduced camera system:
+//   * Schur reduction S_ij = [i==j] H_i - sum_p E_ip C_p^-1 E_jp^T, one warp
+//     per image pair, walking the pair list grouped by image pair (the
+//     visibility-sorted order), so every block is written exactly once and
+//     no global atomics are used (reference: lib.rs:114-211, :981-1043);
+//   * fold of the image-level system onto the reference's slot order with
+//     damping, per-parameter masks and symmetrisation (lib.rs:918-956,
+//     :1051-1074);
+//   * blocked right-looking FP64 Cholesky (64-wide panels) with triangular
+//     solves and one FP64 refinement step, and a partial-pivoting LU
+//     fallback (lib.rs:1081-1094).
+#include <type_traits>
+
+#include "kernels.cuh"
+
+namespace sfmba {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ void kahan_add(T &s, T &c, T x) {
+    if constexpr (std::is_same<T, float>::value) {
+        const T y = x - c;
+        const T t = s + y;
+        c = (t - s) - y;
+        s = t;
+    } else {
+        s += x;
+    }
+}
+
+constexpr int kSchurWarps = 2;
+
+template <typename T, int D>
+__global__ void __launch_bounds__(32 * kSchurWarps)
+    k_schur_pairs(const T *__restrict__ rec, const int2 *__restrict__ pairs,
+                  const int *__restrict__ group_start, const int2 *__restrict__ group_ij, int ngroups,
+                  const int *__restrict__ ob_pt, const T *__restrict__ pt_Cinv,
+                  const unsigned char *__restrict__ pt_ok, const double *__restrict__ img_H, int nID,
+                  double *__restrict__ S_img) {
+    constexpr int RS = RecLayout<D>::kStride;
+    constexpr int NE = (D * D + 31) / 32;
+    __shared__ T sM[kSchurWarps][32][4];
+    __shared__ T sA[kSchurWarps][32][2 * D];
+    __shared__ T sB[kSchurWarps][32][2 * D];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = blockIdx.x * kSchurWarps + wl;
+    if (g >= ngroups) return;
+    const int2 ij = group_ij[g];
+    const int gs = group_start[g], ge = group_start[g + 1];
+    T acc[NE], comp[NE];
+#pragma unroll
+    for (int k = 0; k < NE; ++k) acc[k] = comp[k] = T(0);
+    for (int base = gs; base < ge; base += 32) {
+        const int e = base + lane;
+        if (e < ge) {
+            const int2 ab = pairs[e];
+            const int p = ob_pt[ab.x];
+            const T *ra = rec + (size_t)ab.x * RS;
+            const T *rb = rec + (size_t)ab.y * RS;
+            if (pt_ok[p]) {
+                const T *Ci = pt_Cinv + 6 * (size_t)p;
+                const T c00 = Ci[0], c01 = Ci[1], c02 = Ci[2], c11 = Ci[3], c12 = Ci[4], c22 = Ci[5];
+                // U = Jx~_a C^-1 (2x3), M = U Jx~_b^T (2x2)
+                T U[2][3];
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const T x0 = ra[2 + 3 * r], x1 = ra[3 + 3 * r], x2 = ra[4 + 3 * r];
+                    U[r][0] = x0 * c00 + x1 * c01 + x2 * c02;
+                    U[r][1] = x0 * c01 + x1 * c11 + x2 * c12;
+                    U[r][2] = x0 * c02 + x1 * c12 + x2 * c22;
+                }
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+                        sM[wl][lane][2 * r + q] = U[r][0] * rb[2 + 3 * q] + U[r][1] * rb[3 + 3 * q] + U[r][2] * rb[4 + 3 * q];
+#pragma unroll
+                for (int f = 0; f < 2 * D; ++f) {
+                    sA[wl][lane][f] = ra[8 + f];
+                    sB[wl][lane][f] = rb[8 + f];
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sM[wl][lane][q] = T(0);
+#pragma unroll
+                for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = sB[wl][lane][f] = T(0);
+            }
+        }
+        __syncwarp();
+        const int cnt = min(32, ge - base);
+        for (int t = 0; t < cnt; ++t) {
+            const T m0 = sM[wl][t][0], m1 = sM[wl][t][1], m2 = sM[wl][t][2], m3 = sM[wl][t][3];
+#pragma unroll
+            for (int k = 0; k < NE; ++k) {
+                const int idx = lane + 32 * k;
+                if (idx < D * D) {
+                    const int r = idx / D, c = idx - r * D;
+                    const T b0 = sB[wl][t][c], b1 = sB[wl][t][D + c];
+                    kahan_add(acc[k], comp[k],
+                              sA[wl][t][r] * (m0 * b0 + m1 * b1) + sA[wl][t][D + r] * (m2 * b0 + m3 * b1));
+                }
+            }
+        }
+        __syncwarp();
+    }
+    const int i = ij.x, j = ij.y;
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+        const int idx = lane + 32 * k;
+        if (idx < D * D) {
+            const int r = idx / D, c = idx - r * D;
+            const double v = -((double)acc[k] - (double)comp[k]);
+            if (i == j) {
+                S_img[(size_t)(i * D + r) * nID + i * D + c] = img_H[(size_t)i * D * D + r * D + c] + v;
+            } else {
+                S_img[(size_t)(i * D + r) * nID + j * D + c] = v;
+                S_img[(size_t)(j * D + c) * nID + i * D + r] = v;
+            }
+        }
+    }
+}
+
+// S[a][b] = sym( sum_{u in pre(a), w in pre(b)} S_img[u][w] ) + [a==b] lambda diag(B)[a];
+// masked parameters become identity rows/columns (lib.rs:1051-1070).
+__global__ void k_fold(const double *__restrict__ S_img, int nID, const int *__restrict__ pre_start,
+                       const int *__restrict__ pre, const unsigned char *__restrict__ masked,
+                       const double *__restrict__ diagB, const LMState *__restrict__ st, int n,
+                       double *__restrict__ S, double *__restrict__ L) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = blockIdx.y;
+    if (b >= n || a >= n) return;
+    double v;
+    if (masked[a] || masked[b]) {
+        v = a == b ? 1.0 : 0.0;
+    } else {
+        double vab = 0.0, vba = 0.0;
+        const int as = pre_start[a], ae = pre_start[a + 1], bs = pre_start[b], be = pre_start[b + 1];
+        for (int x = as; x < ae; ++x)
+            for (int y = bs; y < be; ++y) {
+                vab += S_img[(size_t)pre[x] * nID + pre[y]];
+                vba += S_img[(size_t)pre[y] * nID + pre[x]];
+            }
+        v = 0.5 * (vab + vba);
+        if (a == b) v += diagB[a] * st->lambda;
+    }
+    S[(size_t)a * n + b] = v;
+    L[(size_t)a * n + b] = v;
+}
+
+__global__ void k_fold_rhs(const double *img_rhs, const int *pre_start, const int *pre,
+                           const unsigned char *masked, int n, double *rhs) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    double v = 0.0;
+    if (!masked[a])
+        for (int x = pre_start[a]; x < pre_start[a + 1]; ++x) v += img_rhs[pre[x]];
+    rhs[a] = v;
+}
+
+// ---------------------------------------------------------------- Cholesky
+
+constexpr int NB = kCholNB;
+constexpr int LD = NB + 1;
+
+// Factor the diagonal block k0 (in place, lower) and write the inverse of
+// its factor to Linv. Sets state->factor_failed when a pivot is not > 0
+// (nalgebra Cholesky::new semantics: 0, negative and NaN all fail).
+__global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, double *Linv, LMState *st) {
+    extern __shared__ double sm[];
+    double *A = sm;            // NB x LD
+    double *X = sm + NB * LD;  // NB x LD
+    __shared__ int fail;
+    if (st->factor_failed) return;
+    const int nb = min(NB, n - k0);
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        A[r * LD + c] = c <= r ? L[(size_t)(k0 + r) * n + k0 + c] : 0.0;
+    }
+    if (tid == 0) fail = 0;
+    __syncthreads();
+    for (int j = 0; j < nb; ++j) {
+        if (tid == 0) {
+            const double d = A[j * LD + j];
+            if (!(d > 0.0)) fail = 1;
+            else A[j * LD + j] = sqrt(d);
+        }
+        __syncthreads();
+        if (fail) break;
+        const double piv = A[j * LD + j];
+        for (int i = j + 1 + tid; i < nb; i += blockDim.x) A[i * LD + j] /= piv;
+        __syncthreads();
+        const int m = nb - j - 1;
+        for (int idx = tid; idx < m * m; idx += blockDim.x) {
+            const int i = j + 1 + idx / m, l = j + 1 + idx % m;
+            if (l <= i) A[i * LD + l] -= A[i * LD + j] * A[l * LD + j];
+        }
+        __syncthreads();
+    }
+    if (fail) {
+        if (tid == 0) st->factor_failed = 1;
+        return;
+    }
+    for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        if (c <= r) L[(size_t)(k0 + r) * n + k0 + c] = A[r * LD + c];
+    }
+    // Inverse of the lower-triangular factor, one column per thread.
+    if (tid < nb) {
+        const int c = tid;
+        for (int r = 0; r < c; ++r) X[r * LD + c] = 0.0;
+        for (int r = c; r < nb; ++r) {
+            double s = r == c ? 1.0 : 0.0;
+            for (int k = c; k < r; ++k) s -= A[r * LD + k] * X[k * LD + c];
+            X[r * LD + c] = s / A[r * LD + r];
+        }
+    }
+    __syncthreads();
+    double *out = Linv + (size_t)(k0 / NB) * NB * NB;
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+        const int r = idx / NB, c = idx - r * NB;
+        out[idx] = (r < nb && c < nb) ? X[r * LD + c] : 0.0;
+    }
+}
+
+// Panel below the diagonal block: A[r, k-block] <- A[r, k-block] Lkk^-T.
+constexpr int PANEL_ROWS = 32;
+__global__ void __launch_bounds__(256) k_chol_panel(double *L, int n, int k0, const double *Linv,
+                                                     const LMState *st) {
+    extern __shared__ double sm[];
+    double *Li = sm;             // NB x LD
+    double *R = sm + NB * LD;    // PANEL_ROWS x LD
+    if (st->factor_failed) return;
+    const int nb = min(NB, n - k0);
+    const int r0 = k0 + nb + blockIdx.x * PANEL_ROWS;
+    const int rows = min(PANEL_ROWS, n - r0);
+    if (rows <= 0) return;
+    const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Li[(idx / NB) * LD + idx % NB] = inv[idx];
+    for (int idx = threadIdx.x; idx < rows * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        R[r * LD + c] = L[(size_t)(r0 + r) * n + k0 + c];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < rows * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        double s = 0.0;
+        for (int t = 0; t <= c; ++t) s += R[r * LD + t] * Li[c * LD + t];
+        L[(size_t)(r0 + r) * n + k0 + c] = s;
+    }
+}
+
+// Trailing update of the lower triangle: A[I,J] -= P_I P_J^T for the 64x64
+// tiles (I >= J) right of the panel. Each thread owns a 4x4 register tile.
+__global__ void __launch_bounds__(256) k_chol_update(double *L, int n, int k0, const LMState *st) {
+    extern __shared__ double sm[];
+    double *Pi = sm;            // NB x LD
+    double *Pj = sm + NB * LD;  // NB x LD
+    if (st->factor_failed) return;
+    const int nb = min(NB, n - k0);
+    const int t0 = k0 + nb;
+    // tile index q -> (ti, tj), tj <= ti
+    const long long q = blockIdx.x;
+    int ti = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while ((long long)(ti + 1) * (ti + 2) / 2 <= q) ++ti;
+    while ((long long)ti * (ti + 1) / 2 > q) --ti;
+    const int tj = (int)(q - (long long)ti * (ti + 1) / 2);
+    const int ri = t0 + ti * NB, rj = t0 + tj * NB;
+    if (ri >= n || rj >= n) return;
+    const int mi = min(NB, n - ri), mj = min(NB, n - rj);
+    for (int idx = threadIdx.x; idx < NB * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        Pi[r * LD + c] = r < mi ? L[(size_t)(ri + r) * n + k0 + c] : 0.0;
+        Pj[r * LD + c] = r < mj ? L[(size_t)(rj + r) * n + k0 + c] : 0.0;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int t = 0; t < nb; ++t) {
+        double x[4], y[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) x[a] = Pi[(ty * 4 + a) * LD + t];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) y[b] = Pj[(tx + 16 * b) * LD + t];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] += x[a] * y[b];
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int r = ty * 4 + a;
+        if (r >= mi) continue;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int c = tx + 16 * b;
+            if (c >= mj) continue;
+            if (ti == tj && c > r) continue;
+            L[(size_t)(ri + r) * n + rj + c] -= acc[a][b];
+        }
+    }
+}
+
+// Forward step k of L y = b: y_k = Lkk^-1 b_k, then b_r -= L[r, k-block] y_k
+// for the rows below (one warp per row).
+__global__ void __launch_bounds__(256) k_trsv_fwd(const double *L, int n, int k0, const double *Linv,
+                                                   double *b, double *y, const LMState *st) {
+    __shared__ double yk[NB];
+    __shared__ double bk[NB];
+    if (st->factor_failed) return;
+    const int nb = min(NB, n - k0);
+    const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
+    if (threadIdx.x < nb) bk[threadIdx.x] = b[k0 + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < nb) {
+        const int r = threadIdx.x;
+        double s = 0.0;
+        for (int t = 0; t <= r; ++t) s += inv[r * NB + t] * bk[t];
+        yk[r] = s;
+        if (blockIdx.x == 0) y[k0 + r] = s;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rows_per_block = blockDim.x >> 5;
+    const int r = k0 + nb + blockIdx.x * rows_per_block + warp;
+    if (r >= n) return;
+    double s = 0.0;
+    for (int t = lane; t < nb; t += 32) s += L[(size_t)r * n + k0 + t] * yk[t];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) b[r] -= s;
+}
+
+// Backward step k of L^T x = y: x_k = Lkk^-T y_k, then y_r -= L[k-block, r]^T x_k
+// for the rows above (one thread per row, coalesced over r).
+__global__ void __launch_bounds__(256) k_trsv_bwd(const double *L, int n, int k0, const double *Linv,
+                                                   double *y, double *x, const LMState *st) {
+    __shared__ double xk[NB];
+    __shared__ double yk[NB];
+    if (st->factor_failed) return;
+    const int nb = min(NB, n - k0);
+    const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
+    if (threadIdx.x < nb) yk[threadIdx.x] = y[k0 + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < nb) {
+        const int c = threadIdx.x;
+        double s = 0.0;
+        for (int r = c; r < nb; ++r) s += inv[r * NB + c] * yk[r];
+        xk[c] = s;
+        if (blockIdx.x == 0) x[k0 + c] = s;
+    }
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k0) return;
+    double s = 0.0;
+    for (int t = 0; t < nb; ++t) s += L[(size_t)(k0 + t) * n + r] * xk[t];
+    y[r] -= s;
+}
+
+// res = rhs - S x (one warp per row).
+__global__ void k_residual(const double *S, int n, const double *x, const double *rhs, double *res,
+                           const LMState *st) {
+    if (st->factor_failed) return;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    double s = 0.0;
+    for (int c = lane; c < n; c += 32) s += S[(size_t)warp * n + c] * x[c];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) res[warp] = rhs[warp] - s;
+}
+
+__global__ void k_axpy_inplace(int n, const double *c, double *x, const LMState *st) {
+    if (st->factor_failed) return;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) x[a] += c[a];
+}
+
+// ---------------------------------------------------------------- LU fallback
+
+// Column k: pivot on max |a| (first maximum), swap rows, scale the
+// multipliers. A zero column is skipped (no swap, no elimination).
+__global__ void __launch_bounds__(1024) k_lu_pivot(double *A, int n, int k, int *perm, const LMState *st) {
+    __shared__ double bv[1024];
+    __shared__ int bi[1024];
+    if (!st->factor_failed || st->solve_failed) return;
+    double best = -1.0;
+    int besti = k;
+    for (int r = k + threadIdx.x; r < n; r += blockDim.x) {
+        const double v = fabs(A[(size_t)r * n + k]);
+        if (v > best) { best = v; besti = r; }
+    }
+    bv[threadIdx.x] = best;
+    bi[threadIdx.x] = besti;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            const double o = bv[threadIdx.x + w];
+            const int oi = bi[threadIdx.x + w];
+            if (o > bv[threadIdx.x] || (o == bv[threadIdx.x] && oi < bi[threadIdx.x])) {
+                bv[threadIdx.x] = o;
+                bi[threadIdx.x] = oi;
+            }
+        }
+        __syncthreads();
+    }
+    const int piv = bi[0];
+    const double diag = A[(size_t)piv * n + k];
+    if (diag == 0.0) {
+        if (threadIdx.x == 0) perm[k] = -1;  // zero column: skipped
+        return;
+    }
+    if (piv != k)
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            const double t = A[(size_t)k * n + c];
+            A[(size_t)k * n + c] = A[(size_t)piv * n + c];
+            A[(size_t)piv * n + c] = t;
+        }
+    if (threadIdx.x == 0) perm[k] = piv;
+    __syncthreads();
+    for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) A[(size_t)r * n + k] /= diag;
+}
+
+__global__ void k_lu_update(double *A, int n, int k, const int *perm, const LMState *st) {
+    if (!st->factor_failed || st->solve_failed) return;
+    if (perm[k] < 0) return;
+    const int c = k + 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = k + 1 + blockIdx.y;
+    if (c >= n || r >= n) return;
+    A[(size_t)r * n + c] -= A[(size_t)r * n + k] * A[(size_t)k * n + c];
+}
+
+// Apply the row swaps to rhs, solve unit-lower then upper. A zero diagonal
+// of U fails the solve (lambda then grows); success clears factor_failed so
+// the back-substitution and trial kernels run.
+__global__ void __launch_bounds__(1024) k_lu_solve(const double *A, int n, const int *perm,
+                                                    const double *rhs, double *x, LMState *st) {
+    __shared__ double red[1024];
+    __shared__ int bad;
+    if (!st->factor_failed || st->solve_failed) return;
+    if (threadIdx.x == 0) bad = 0;
+    for (int a = threadIdx.x; a < n; a += blockDim.x) x[a] = rhs[a];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < n; ++k)
+            if (perm[k] >= 0 && perm[k] != k) {
+                const double t = x[k];
+                x[k] = x[perm[k]];
+                x[perm[k]] = t;
+            }
+    __syncthreads();
+    for (int i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int k = threadIdx.x; k < i; k += blockDim.x) s += A[(size_t)i * n + k] * x[k];
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) x[i] -= red[0];
+        __syncthreads();
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double s = 0.0;
+        for (int k = i + 1 + threadIdx.x; k < n; k += blockDim.x) s += A[(size_t)i * n + k] * x[k];
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            const double d = A[(size_t)i * n + i];
+            if (d == 0.0) bad = 1;
+            else x[i] = (x[i] - red[0]) / d;
+        }
+        __syncthreads();
+        if (bad) break;
+    }
+    if (threadIdx.x == 0) {
+        if (bad) st->solve_failed = 1;
+        else st->factor_failed = 0;
+    }
+}
+
+template <typename F>
+void dispatch_D(int D, F &&f) {
+    switch (D) {
+    case 6: f(std::integral_constant<int, 6>()); break;
+    case 9: f(std::integral_constant<int, 9>()); break;
+    case 10: f(std::integral_constant<int, 10>()); break;
+    case 11: f(std::integral_constant<int, 11>()); break;
+    case 14: f(std::integral_constant<int, 14>()); break;
+    default: throw Error(SFMBA_ERR_INTERNAL, "unsupported image block width");
+    }
+}
+
+const size_t kSmemTwoTiles = 2 * NB * LD * sizeof(double);
+const size_t kSmemPanel = (NB + PANEL_ROWS) * LD * sizeof(double);
+
+void set_smem_limits() {
+    static bool done = false;
+    if (done) return;
+    SFMBA_CUDA(cudaFuncSetAttribute(k_chol_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTwoTiles));
+    SFMBA_CUDA(cudaFuncSetAttribute(k_chol_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTwoTiles));
+    SFMBA_CUDA(cudaFuncSetAttribute(k_chol_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPanel));
+    done = true;
+}
+
+}  // namespace
+
+void launch_schur_pairs(const Bufs &b, cudaStream_t s) {
+    if (b.ngroups == 0) return;
+    dispatch_D(b.D, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        const int grid = div_up(b.ngroups, kSchurWarps);
+        if (b.mixed)
+            k_schur_pairs<float, D><<<grid, 32 * kSchurWarps, 0, s>>>(
+                (const float *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
+                (const float *)b.pt_Cinv, b.pt_ok, b.img_H, b.nID, b.S_img);
+        else
+            k_schur_pairs<double, D><<<grid, 32 * kSchurWarps, 0, s>>>(
+                (const double *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
+                (const double *)b.pt_Cinv, b.pt_ok, b.img_H, b.nID, b.S_img);
+    });
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_fold_system(const Bufs &b, cudaStream_t s) {
+    if (b.n == 0) return;
+    dim3 grid(div_up(b.n, 128), b.n);
+    k_fold<<<grid, 128, 0, s>>>(b.S_img, b.nID, b.slot_pre_start, b.slot_pre, b.slot_masked, b.diagB,
+                                b.state, b.n, b.S, b.L);
+    SFMBA_LAUNCH_CHECK();
+    k_fold_rhs<<<div_up(b.n, 256), 256, 0, s>>>(b.img_rhs, b.slot_pre_start, b.slot_pre, b.slot_masked,
+                                                b.n, b.rhs);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_cholesky(const Bufs &b, cudaStream_t s) {
+    set_smem_limits();
+    const int n = b.n;
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        k_chol_diag<<<1, 256, kSmemTwoTiles, s>>>(b.L, n, k0, b.Linv, b.state);
+        SFMBA_LAUNCH_CHECK();
+        const int rem = n - k0 - NB;
+        if (rem <= 0) break;
+        k_chol_panel<<<div_up(rem, PANEL_ROWS), 256, kSmemPanel, s>>>(b.L, n, k0, b.Linv, b.state);
+        SFMBA_LAUNCH_CHECK();
+        const long long tiles = div_up(rem, NB);
+        k_chol_update<<<(unsigned)(tiles * (tiles + 1) / 2), 256, kSmemTwoTiles, s>>>(b.L, n, k0, b.state);
+        SFMBA_LAUNCH_CHECK();
+    }
+}
+
+void launch_cholesky_solve(const Bufs &b, const double *rhs, double *x, cudaStream_t s) {
+    const int n = b.n;
+    // forward: work <- rhs (updated in place), y -> work2
+    SFMBA_CUDA(cudaMemcpyAsync(b.work, rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int rem = n - k0 - NB;
+        const int grid = rem > 0 ? div_up(rem, 8) : 1;
+        k_trsv_fwd<<<grid, 256, 0, s>>>(b.L, n, k0, b.Linv, b.work, b.work2, b.state);
+        SFMBA_LAUNCH_CHECK();
+    }
+    const int last = ((n - 1) / NB) * NB;
+    for (int k0 = last; k0 >= 0; k0 -= NB) {
+        const int grid = k0 > 0 ? div_up(k0, 256) : 1;
+        k_trsv_bwd<<<grid, 256, 0, s>>>(b.L, n, k0, b.Linv, b.work2, x, b.state);
+        SFMBA_LAUNCH_CHECK();
+    }
+}
+
+void launch_refine(const Bufs &b, cudaStream_t s) {
+    // One FP64 iterative-refinement step: res = rhs - S delta, solve, delta += c.
+    k_residual<<<div_up((long long)b.n * 32, 256), 256, 0, s>>>(b.S, b.n, b.delta, b.rhs, b.ref_res, b.state);
+    SFMBA_LAUNCH_CHECK();
+    launch_cholesky_solve(b, b.ref_res, b.ref_corr, s);
+    k_axpy_inplace<<<div_up(b.n, 256), 256, 0, s>>>(b.n, b.ref_corr, b.delta, b.state);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_lu_factor(const Bufs &b, cudaStream_t s) {
+    const int n = b.n;
+    SFMBA_CUDA(cudaMemcpyAsync(b.L, b.S, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s));
+    for (int k = 0; k < n; ++k) {
+        k_lu_pivot<<<1, 1024, 0, s>>>(b.L, n, k, b.lu_perm, b.state);
+        SFMBA_LAUNCH_CHECK();
+        if (k + 1 < n) {
+            dim3 grid(div_up(n - k - 1, 128), n - k - 1);
+            k_lu_update<<<grid, 128, 0, s>>>(b.L, n, k, b.lu_perm, b.state);
+            SFMBA_LAUNCH_CHECK();
+        }
+    }
+}
+
+void launch_lu_solve(const Bufs &b, cudaStream_t s) {
+    k_lu_solve<<<1, 1024, 0, s>>>(b.L, b.n, b.lu_perm, b.rhs, b.delta, b.state);
+    SFMBA_LAUNCH_CHECK();
+}
+
+}  // namespace sfmba

@@ -1,0 +1,143 @@
+// Launchers of the GB300 bundle-adjustment kernels. Each launcher picks the
+// template instance (precision, image block width D) at run time; templates
+// stay inside their .cu file.
+#pragma once
+
+#include "common.cuh"
+
+namespace sfmba {
+
+// Device buffers of one solve (all owned by the workspace arena).
+struct Bufs {
+    // sizes
+    int nI = 0, nC = 0, nP = 0;
+    long long nO = 0;
+    int n = 0;        // reduced-system dimension (reference slotting)
+    int D = 6;        // image block width: 6 pose columns + widest camera
+    int nID = 0;      // nI * D
+    int mixed = 0;    // 1: FP32 linearisation/Schur/PCG, 0: FP64
+    int loss = 0;
+    double loss_scale = 1.0;
+    // problem, solver layout
+    const int *cam_model = nullptr;     // [nC]
+    const int *cam_of_img = nullptr;    // [nI]
+    double *cams = nullptr, *cams_trial = nullptr;      // [nC*8]
+    double *poses = nullptr, *poses_trial = nullptr;    // [nI*7]
+    double *points = nullptr, *points_trial = nullptr;  // [nP*3]
+    float4 *points32 = nullptr;                         // [nP] FP32 copy (mixed)
+    int *ob_img = nullptr, *ob_pt = nullptr;            // [nO] point-sorted
+    double2 *ob_xy = nullptr;                           // [nO]
+    int *pt_start = nullptr;                            // [nP+1]
+    int *img_start = nullptr;                           // [nI+1]
+    int *img_obs = nullptr;                             // [nO] image-sorted -> point-sorted index
+    int *img_slot = nullptr;      // [nI*D] slot of column r of image i, -1 if not an unknown
+    int *img_active = nullptr;    // [nI] bit r: column r is an unknown
+    int *img_free = nullptr;      // [nI] pose free or camera free
+    int *cam_slot = nullptr;      // [nC] first slot of the camera, -1 if fixed
+    int *pose_slot = nullptr;     // [nI] first slot of the pose, -1 if fixed
+    int *slot_pre_start = nullptr;  // [n+1]
+    int *slot_pre = nullptr;        // image-level indices i*D+r mapped onto each slot
+    unsigned char *slot_masked = nullptr;  // [n]
+    // linearisation (element type float or double by `mixed`)
+    void *img_lin = nullptr;      // [nI] ImageLin<T>
+    void *rec = nullptr;          // [nO * stride] records
+    unsigned char *ob_valid = nullptr;  // [nO]
+    void *pt_C = nullptr;         // [nP*6] symmetric 3x3 (00 01 02 11 12 22)
+    void *pt_g = nullptr;         // [nP*3]
+    int *pt_nfree = nullptr;      // [nP]
+    void *pt_Cinv = nullptr;      // [nP*6]
+    void *pt_h = nullptr;         // [nP*3] Cinv g
+    unsigned char *pt_ok = nullptr;  // [nP]
+    double *img_H = nullptr;      // [nI*D*D]
+    double *img_b = nullptr;      // [nI*D]
+    double *img_rhs = nullptr;    // [nI*D]
+    void *img_delta = nullptr;    // [nI*D] step of the image block (T)
+    // dense reduced system
+    int2 *pairs = nullptr;        // [npairs] (obs a, obs b), grouped by image pair
+    int *group_start = nullptr;   // [ngroups+1]
+    int2 *group_ij = nullptr;     // [ngroups]
+    long long npairs = 0;
+    int ngroups = 0;
+    double *S_img = nullptr;      // [nID*nID]
+    double *S = nullptr;          // [n*n] symmetric reduced system
+    double *L = nullptr;          // [n*n] Cholesky / LU factors
+    double *Linv = nullptr;       // [nblocks*64*64] inverses of diagonal blocks
+    int *lu_perm = nullptr;       // [n]
+    double *rhs = nullptr, *delta = nullptr, *diagB = nullptr, *work = nullptr, *work2 = nullptr;  // [n]
+    double *ref_res = nullptr, *ref_corr = nullptr;  // [n] refinement residual and correction
+    // LM bookkeeping
+    LMState *state = nullptr;
+    double *partials = nullptr;   // [kCostBlocks*2]
+    long long *count_partials = nullptr;
+    // PCG (matrix-free) vectors, [nI*D] each, element type T
+    void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
+    void *pcg_u = nullptr;        // [nP*4] per-point Cinv E^T p
+    void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
+    double *pcg_dots = nullptr;   // [kDotSlots]
+};
+
+constexpr int kCostBlocks = 1024;
+constexpr int kDotSlots = 16;
+constexpr int kCholNB = 64;
+
+// Inputs/outputs of the per-observation Jacobian probe (original order).
+struct JacProbe {
+    long long nO = 0;
+    double *poses = nullptr, *cams = nullptr, *points = nullptr, *obs_xy = nullptr;
+    int *cam_of_img = nullptr, *cam_model = nullptr, *obs_img = nullptr, *obs_pt = nullptr;
+    double *r = nullptr, *jp = nullptr, *jx = nullptr, *jc = nullptr;
+    unsigned char *valid = nullptr;
+};
+
+// ---- setup (k_setup.cu)
+size_t sort_temp_bytes(long long nO, int nP, int nI);
+void sort_observations(const int *obs_point_in, const int *obs_image_in, const double *obs_xy_in,
+                       long long nO, int nP, int nI, Bufs &b, void *temp, size_t temp_bytes,
+                       int *keys_tmp, int *vals_tmp, int *keys_tmp2, int *vals_tmp2,
+                       cudaStream_t s);
+size_t pairs_temp_bytes(long long npairs, int nI);
+long long count_pairs(const Bufs &b, long long *d_count_scan, void *temp, size_t temp_bytes,
+                      cudaStream_t s);
+void build_pairs(Bufs &b, const long long *d_count_scan, unsigned *keys_a, unsigned *keys_b,
+                 int2 *vals_b, void *temp, size_t temp_bytes, int *d_ngroups, cudaStream_t s);
+void validate_problem_device(const int *cam_of_img, const int *cam_model, const int *obs_image,
+                             const int *obs_point, long long nO, int nI, int nC, int nP,
+                             int *d_bad, cudaStream_t s);
+
+// ---- linearisation and LM bookkeeping (k_lin.cu)
+void launch_prepare_images(const Bufs &b, cudaStream_t s);
+void launch_linearize(const Bufs &b, cudaStream_t s);
+void launch_point_reduce(const Bufs &b, cudaStream_t s);
+void launch_image_reduce(const Bufs &b, cudaStream_t s);
+void launch_diag_fold(const Bufs &b, cudaStream_t s);
+void launch_point_inverse(const Bufs &b, cudaStream_t s);
+void launch_image_rhs(const Bufs &b, cudaStream_t s);
+void launch_gather_delta(const Bufs &b, const double *delta_slot, cudaStream_t s);
+void launch_backsub_update(const Bufs &b, const double *delta_slot, cudaStream_t s);
+// cost of (poses, cams, points) or of the trial buffers, into state->cost/trial_cost
+void launch_cost(const Bufs &b, bool trial, bool into_trial, cudaStream_t s);
+void launch_mean_error(const Bufs &b, cudaStream_t s);  // -> partials; host finalises
+void launch_accept(const Bufs &b, cudaStream_t s);
+void launch_commit(const Bufs &b, cudaStream_t s);
+void launch_reject(const Bufs &b, cudaStream_t s);
+void launch_refresh_points32(const Bufs &b, cudaStream_t s);
+void launch_begin_outer(const Bufs &b, cudaStream_t s);
+void launch_begin_retry(const Bufs &b, cudaStream_t s);
+void launch_count_valid(const Bufs &b, cudaStream_t s);
+void launch_jacobian_probe(const JacProbe &q, bool fp32, cudaStream_t s);
+
+// ---- dense reduced system (k_dense.cu)
+void launch_schur_pairs(const Bufs &b, cudaStream_t s);
+void launch_fold_system(const Bufs &b, cudaStream_t s);
+void launch_cholesky(const Bufs &b, cudaStream_t s);
+void launch_cholesky_solve(const Bufs &b, const double *rhs, double *x, cudaStream_t s);
+void launch_refine(const Bufs &b, cudaStream_t s);
+void launch_lu_factor(const Bufs &b, cudaStream_t s);
+void launch_lu_solve(const Bufs &b, cudaStream_t s);
+
+// ---- matrix-free Schur PCG (k_pcg.cu)
+void launch_pcg_setup(const Bufs &b, cudaStream_t s);
+void launch_pcg_iteration(const Bufs &b, cudaStream_t s);
+void launch_pcg_finish(const Bufs &b, cudaStream_t s);
+
+}  // namespace sfmba

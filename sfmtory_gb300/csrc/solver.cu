@@ -1,0 +1,758 @@
+// Host driver of the GB300 bundle adjuster and the C ABI (include/sfmba.h).
+//
+// The Levenberg-Marquardt loop follows crates/sfm-ba/src/lib.rs:747-1232:
+// slots for free poses then free cameras; per outer iteration one
+// linearisation; up to 8 damping retries, each building the reduced system,
+// solving it, back-substituting the points and evaluating the trial cost;
+// accept iff the FP64 trial cost is finite and lower; stop when no retry is
+// accepted or the relative decrease drops below 1e-6. Damping, acceptance
+// and all parameters live on the device; the host reads a 100-byte state
+// record once per retry to decide whether to launch another one.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cub/cub.cuh>
+
+#include "camera.cuh"
+#include "kernels.cuh"
+
+namespace sfmba {
+
+namespace {
+
+thread_local std::string g_last_error;
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Bump allocator over one device allocation that grows on demand and is
+// kept across calls on the same thread.
+class Arena {
+  public:
+    ~Arena() { release(); }
+    void release() {
+        if (base_) cudaFree(base_);
+        base_ = nullptr;
+        cap_ = 0;
+    }
+    void begin_sizing() { sizing_ = true; off_ = 0; }
+    void commit() {
+        if (off_ > cap_) {
+            release();
+            size_t want = off_ + (off_ >> 3) + (1 << 20);
+            SFMBA_CUDA(cudaMalloc(&base_, want));
+            cap_ = want;
+        }
+        sizing_ = false;
+        off_ = 0;
+    }
+    template <typename T>
+    T *take(size_t count) {
+        size_t bytes = ((count * sizeof(T)) + 255) / 256 * 256;
+        if (bytes == 0) bytes = 256;
+        char *p = sizing_ ? nullptr : base_ + off_;
+        off_ += bytes;
+        return reinterpret_cast<T *>(p);
+    }
+    size_t capacity() const { return cap_; }
+
+  private:
+    char *base_ = nullptr;
+    size_t cap_ = 0, off_ = 0;
+    bool sizing_ = false;
+};
+
+struct Context {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    Arena main, pairs;
+    LMState *h_state = nullptr;  // pinned mirror
+    ~Context() {
+        if (h_state) cudaFreeHost(h_state);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+Context &context() {
+    thread_local std::unique_ptr<Context> ctx;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw Error(SFMBA_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    int count = 0;
+    e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        (void)cudaGetLastError();
+        throw Error(SFMBA_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (!ctx || ctx->device != dev) {
+        ctx.reset(new Context());
+        ctx->device = dev;
+        SFMBA_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        SFMBA_CUDA(cudaMallocHost(&ctx->h_state, sizeof(LMState)));
+    }
+    return *ctx;
+}
+
+// Host view of the slot structure (lib.rs:753-776) and the image blocks.
+struct Layout {
+    int nI = 0, nC = 0, nP = 0;
+    long long nO = 0;
+    int n = 0, D = 6;
+    std::vector<int> pose_slot, cam_slot, img_slot, img_active, img_free;
+    std::vector<int> slot_pre_start, slot_pre;
+    std::vector<unsigned char> slot_masked;
+    bool injective = true;
+};
+
+Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> &cam_of_img,
+                   const std::vector<int> &model, const std::vector<unsigned char> &fixed_pose,
+                   const std::vector<unsigned char> &fixed_cam, const std::vector<unsigned char> &fixed_cp) {
+    Layout L;
+    L.nI = nI; L.nC = nC; L.nP = nP; L.nO = nO;
+    L.pose_slot.assign(nI, -1);
+    L.cam_slot.assign(nC, -1);
+    int n = 0;
+    for (int i = 0; i < nI; ++i)
+        if (!fixed_pose[i]) { L.pose_slot[i] = n; n += 6; }
+    int kmax = 0;
+    for (int c = 0; c < nC; ++c)
+        if (!fixed_cam[c]) {
+            L.cam_slot[c] = n;
+            n += model_dof(model[c]);
+            kmax = std::max(kmax, model_dof(model[c]));
+        }
+    L.n = n;
+    L.D = block_width_for(kmax);
+    const int D = L.D;
+    L.img_slot.assign((size_t)nI * D, -1);
+    L.img_active.assign(nI, 0);
+    L.img_free.assign(nI, 0);
+    L.slot_masked.assign(n, 0);
+    for (int c = 0; c < nC; ++c) {
+        if (L.cam_slot[c] < 0) continue;
+        for (int k = 0; k < model_dof(model[c]); ++k)
+            if (fixed_cp[(size_t)c * 8 + k]) L.slot_masked[L.cam_slot[c] + k] = 1;
+    }
+    std::vector<std::vector<int>> pre(n);
+    std::vector<int> cam_users(nC, 0);
+    for (int i = 0; i < nI; ++i) {
+        const int c = cam_of_img[i];
+        int act = 0;
+        if (L.pose_slot[i] >= 0)
+            for (int r = 0; r < 6; ++r) {
+                L.img_slot[(size_t)i * D + r] = L.pose_slot[i] + r;
+                pre[L.pose_slot[i] + r].push_back(i * D + r);
+                act |= 1 << r;
+            }
+        if (L.cam_slot[c] >= 0) {
+            cam_users[c] += 1;
+            for (int k = 0; k < model_dof(model[c]); ++k) {
+                const int slot = L.cam_slot[c] + k;
+                if (L.slot_masked[slot]) continue;
+                L.img_slot[(size_t)i * D + 6 + k] = slot;
+                pre[slot].push_back(i * D + 6 + k);
+                act |= 1 << (6 + k);
+            }
+        }
+        L.img_active[i] = act;
+        L.img_free[i] = (L.pose_slot[i] >= 0 || L.cam_slot[c] >= 0) ? 1 : 0;
+    }
+    for (int c = 0; c < nC; ++c)
+        if (cam_users[c] > 1) L.injective = false;
+    L.slot_pre_start.assign(n + 1, 0);
+    for (int a = 0; a < n; ++a) L.slot_pre_start[a + 1] = L.slot_pre_start[a] + (int)pre[a].size();
+    L.slot_pre.reserve(L.slot_pre_start[n]);
+    for (int a = 0; a < n; ++a) L.slot_pre.insert(L.slot_pre.end(), pre[a].begin(), pre[a].end());
+    return L;
+}
+
+void check_options(const sfmba_options *o) {
+    if (!o) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "options is NULL");
+    if (o->max_iterations < 0) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "max_iterations < 0");
+    if (o->robust_loss < 0 || o->robust_loss > 2) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "unknown robust_loss");
+    if (o->precision < 0 || o->precision > 1) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (o->solver < 0 || o->solver > 2) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "unknown solver");
+    if (!(o->initial_lambda >= 0.0) || !std::isfinite(o->initial_lambda))
+        throw Error(SFMBA_ERR_INVALID_ARGUMENT, "initial_lambda must be finite and >= 0");
+}
+
+void check_problem_shape(const sfmba_problem *p) {
+    if (!p) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "problem is NULL");
+    if (p->num_images < 0 || p->num_cameras < 0 || p->num_points < 0 || p->num_observations < 0)
+        throw Error(SFMBA_ERR_INVALID_ARGUMENT, "negative size");
+    if (p->num_images > (1 << 20) || p->num_cameras > (1 << 20) || p->num_points > (1LL << 30) ||
+        p->num_observations > (1LL << 31) - 1)
+        throw Error(SFMBA_ERR_INVALID_ARGUMENT, "problem too large for 32-bit indices");
+    auto need = [](const void *ptr, long long count, const char *name) {
+        if (count > 0 && !ptr) throw Error(SFMBA_ERR_INVALID_ARGUMENT, std::string(name) + " is NULL");
+    };
+    need(p->camera_of_image, p->num_images, "camera_of_image");
+    need(p->poses, p->num_images, "poses");
+    need(p->camera_model, p->num_cameras, "camera_model");
+    need(p->camera_params, p->num_cameras, "camera_params");
+    need(p->points, p->num_points, "points");
+    need(p->obs_image, p->num_observations, "obs_image");
+    need(p->obs_point, p->num_observations, "obs_point");
+    need(p->obs_xy, p->num_observations, "obs_xy");
+}
+
+void check_problem_host(const sfmba_problem *p) {
+    for (long long c = 0; c < p->num_cameras; ++c)
+        if (model_dof(p->camera_model[c]) == 0)
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "camera " + std::to_string(c) + " has an unknown model id");
+    for (long long i = 0; i < p->num_images; ++i)
+        if (p->camera_of_image[i] < 0 || p->camera_of_image[i] >= p->num_cameras)
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "camera_of_image[" + std::to_string(i) + "] out of range");
+    for (long long o = 0; o < p->num_observations; ++o) {
+        if (p->obs_image[o] < 0 || p->obs_image[o] >= p->num_images)
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "obs_image[" + std::to_string(o) + "] out of range");
+        if (p->obs_point[o] < 0 || p->obs_point[o] >= p->num_points)
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "obs_point[" + std::to_string(o) + "] out of range");
+    }
+}
+
+template <typename T>
+std::vector<T> fetch(const T *src, size_t count, bool device, cudaStream_t s) {
+    std::vector<T> v(count);
+    if (count == 0) return v;
+    if (device) {
+        SFMBA_CUDA(cudaMemcpyAsync(v.data(), src, sizeof(T) * count, cudaMemcpyDeviceToHost, s));
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+    } else {
+        std::memcpy(v.data(), src, sizeof(T) * count);
+    }
+    return v;
+}
+
+template <typename T>
+void put(T *dst, const T *src, size_t count, bool src_device, cudaStream_t s) {
+    if (count == 0) return;
+    SFMBA_CUDA(cudaMemcpyAsync(dst, src, sizeof(T) * count,
+                               src_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+}
+
+template <typename T>
+void put_vec(T *dst, const std::vector<T> &v, cudaStream_t s) {
+    if (v.empty()) return;
+    SFMBA_CUDA(cudaMemcpyAsync(dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+}
+
+struct SolveOutput {
+    double initial_cost = 0, final_cost = 0;
+    int iterations = 0, retries = 0, solver = SFMBA_SOLVER_DENSE;
+    long long linear_iterations = 0, valid_obs = 0;
+    int n = 0;
+};
+
+class Solver {
+  public:
+    Solver(Context &ctx, cudaStream_t s) : ctx_(ctx), s_(s) {}
+
+    void read_state() {
+        SFMBA_CUDA(cudaMemcpyAsync(ctx_.h_state, b_.state, sizeof(LMState), cudaMemcpyDeviceToHost, s_));
+        SFMBA_CUDA(cudaStreamSynchronize(s_));
+    }
+
+    // Copies the problem into solver layout and builds all device structures.
+    void setup(const sfmba_problem *p, const sfmba_options *o, bool device, bool need_system) {
+        const int nI = (int)p->num_images, nC = (int)p->num_cameras, nP = (int)p->num_points;
+        const long long nO = p->num_observations;
+        std::vector<int> cam_of_img = fetch(p->camera_of_image, nI, device, s_);
+        std::vector<int> model = fetch(p->camera_model, nC, device, s_);
+        for (int c = 0; c < nC; ++c)
+            if (model_dof(model[c]) == 0)
+                throw Error(SFMBA_ERR_INVALID_ARGUMENT, "camera " + std::to_string(c) + " has an unknown model id");
+        for (int i = 0; i < nI; ++i)
+            if (cam_of_img[i] < 0 || cam_of_img[i] >= nC)
+                throw Error(SFMBA_ERR_INVALID_ARGUMENT, "camera_of_image[" + std::to_string(i) + "] out of range");
+        std::vector<unsigned char> fp(nI, 0), fc(nC, 0), fcp((size_t)nC * 8, 0);
+        if (p->fixed_poses) fp = fetch(p->fixed_poses, nI, device, s_);
+        if (p->fixed_cameras) fc = fetch(p->fixed_cameras, nC, device, s_);
+        if (p->fixed_camera_params) fcp = fetch(p->fixed_camera_params, (size_t)nC * 8, device, s_);
+        lay_ = make_layout(nI, nC, nP, nO, cam_of_img, model, fp, fc, fcp);
+        const int n = lay_.n, D = lay_.D;
+        const bool mixed = o->precision == SFMBA_PRECISION_MIXED;
+        solver_ = SFMBA_SOLVER_DENSE;
+        if (o->solver == SFMBA_SOLVER_PCG) solver_ = SFMBA_SOLVER_PCG;
+        else if (o->solver == SFMBA_SOLVER_AUTO)
+            solver_ = (n <= std::max(1, o->dense_max_dim)) ? SFMBA_SOLVER_DENSE : SFMBA_SOLVER_PCG;
+        if (solver_ == SFMBA_SOLVER_PCG && !lay_.injective)
+            throw Error(SFMBA_ERR_UNSUPPORTED,
+                        "the PCG solver needs every free camera to belong to one image; use the dense solver");
+        if (solver_ == SFMBA_SOLVER_DENSE && n > 16384)
+            throw Error(SFMBA_ERR_UNSUPPORTED, "dense reduced system above 16384 unknowns; use the PCG solver");
+        if (solver_ == SFMBA_SOLVER_DENSE && nI > 65535)
+            throw Error(SFMBA_ERR_UNSUPPORTED, "dense solver supports at most 65535 images; use the PCG solver");
+        const int nID = nI * D;
+        const size_t tsz = mixed ? sizeof(float) : sizeof(double);
+        const size_t RS = (size_t)((8 + 2 * D) + 3) / 4 * 4;
+        size_t sort_tmp = nO > 0 ? sort_temp_bytes(nO, nP, nI) : 0;
+        {
+            size_t scan_bytes = 0;
+            SFMBA_CUDA(cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, (long long *)nullptr,
+                                                     (long long *)nullptr, std::max(nP, 1)));
+            sort_tmp = std::max(sort_tmp, scan_bytes);
+        }
+
+        Arena &A = ctx_.main;
+        int *in_img = nullptr, *in_pt = nullptr;
+        double *in_xy = nullptr;
+        void *sort_temp = nullptr;
+        int *k1 = nullptr, *v1 = nullptr, *k2 = nullptr, *v2 = nullptr;
+        long long *pair_scan = nullptr;
+        int *d_bad = nullptr;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            Bufs &b = b_;
+            b = Bufs();
+            b.nI = nI; b.nC = nC; b.nP = nP; b.nO = nO; b.n = n; b.D = D; b.nID = nID;
+            b.mixed = mixed; b.loss = o->robust_loss; b.loss_scale = o->loss_scale_px;
+            b.cam_model = A.take<int>(nC);
+            b.cam_of_img = A.take<int>(nI);
+            b.cams = A.take<double>((size_t)nC * 8);
+            b.cams_trial = A.take<double>((size_t)nC * 8);
+            b.poses = A.take<double>((size_t)nI * 7);
+            b.poses_trial = A.take<double>((size_t)nI * 7);
+            b.points = A.take<double>((size_t)nP * 3);
+            b.points_trial = A.take<double>((size_t)nP * 3);
+            b.points32 = mixed ? A.take<float4>(nP) : nullptr;
+            b.ob_img = A.take<int>(nO);
+            b.ob_pt = A.take<int>(nO);
+            b.ob_xy = A.take<double2>(nO);
+            b.pt_start = A.take<int>((size_t)nP + 1);
+            b.img_start = A.take<int>((size_t)nI + 1);
+            b.img_obs = A.take<int>(nO);
+            b.img_slot = A.take<int>((size_t)nID);
+            b.img_active = A.take<int>(nI);
+            b.img_free = A.take<int>(nI);
+            b.cam_slot = A.take<int>(nC);
+            b.pose_slot = A.take<int>(nI);
+            b.slot_pre_start = A.take<int>((size_t)n + 1);
+            b.slot_pre = A.take<int>(lay_.slot_pre.size());
+            b.slot_masked = A.take<unsigned char>(n);
+            b.state = A.take<LMState>(1);
+            b.partials = A.take<double>(kCostBlocks);
+            b.count_partials = A.take<long long>(kCostBlocks);
+            d_bad = A.take<int>(1);
+            if (!device) {
+                in_img = A.take<int>(nO);
+                in_pt = A.take<int>(nO);
+                in_xy = A.take<double>((size_t)nO * 2);
+            }
+            if (need_system) {
+                b.img_lin = A.take<char>((size_t)nI * (mixed ? sizeof(ImageLin<float>) : sizeof(ImageLin<double>)));
+                b.rec = A.take<char>((size_t)nO * RS * tsz);
+                b.ob_valid = A.take<unsigned char>(nO);
+                b.pt_C = A.take<char>((size_t)nP * 6 * tsz);
+                b.pt_g = A.take<char>((size_t)nP * 3 * tsz);
+                b.pt_nfree = A.take<int>(nP);
+                b.pt_Cinv = A.take<char>((size_t)nP * 6 * tsz);
+                b.pt_h = A.take<char>((size_t)nP * 3 * tsz);
+                b.pt_ok = A.take<unsigned char>(nP);
+                b.img_H = A.take<double>((size_t)nID * D);
+                b.img_b = A.take<double>((size_t)nID);
+                b.img_rhs = A.take<double>((size_t)nID);
+                b.img_delta = A.take<char>((size_t)nID * tsz);
+                b.rhs = A.take<double>(n);
+                b.delta = A.take<double>(n);
+                b.diagB = A.take<double>(n);
+                b.work = A.take<double>(n);
+                b.work2 = A.take<double>(n);
+                b.ref_res = A.take<double>(n);
+                b.ref_corr = A.take<double>(n);
+                if (solver_ == SFMBA_SOLVER_DENSE) {
+                    b.S_img = A.take<double>((size_t)nID * nID);
+                    b.S = A.take<double>((size_t)n * n);
+                    b.L = A.take<double>((size_t)n * n);
+                    b.Linv = A.take<double>((size_t)div_up(n, kCholNB) * kCholNB * kCholNB);
+                    b.lu_perm = A.take<int>(n);
+                    pair_scan = A.take<long long>(nP);
+                } else {
+                    b.pcg_x = A.take<char>((size_t)nID * tsz);
+                    b.pcg_r = A.take<char>((size_t)nID * tsz);
+                    b.pcg_z = A.take<char>((size_t)nID * tsz);
+                    b.pcg_p = A.take<char>((size_t)nID * tsz);
+                    b.pcg_q = A.take<char>((size_t)nID * tsz);
+                    b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
+                    b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
+                    b.pcg_dots = A.take<double>(kDotSlots);
+                }
+            }
+            sort_temp = A.take<char>(sort_tmp);
+            k1 = A.take<int>(nO);
+            v1 = A.take<int>(nO);
+            k2 = A.take<int>(nO);
+            v2 = A.take<int>(nO);
+        }
+        Bufs &b = b_;
+        // Problem arrays.
+        put(const_cast<int *>(b.cam_model), p->camera_model, nC, device, s_);
+        put(const_cast<int *>(b.cam_of_img), p->camera_of_image, nI, device, s_);
+        put(b.cams, p->camera_params, (size_t)nC * 8, device, s_);
+        put(b.poses, p->poses, (size_t)nI * 7, device, s_);
+        put(b.points, p->points, (size_t)nP * 3, device, s_);
+        const int *src_img = p->obs_image, *src_pt = p->obs_point;
+        const double *src_xy = p->obs_xy;
+        if (!device) {
+            put(in_img, p->obs_image, nO, false, s_);
+            put(in_pt, p->obs_point, nO, false, s_);
+            put(in_xy, p->obs_xy, (size_t)nO * 2, false, s_);
+            src_img = in_img; src_pt = in_pt; src_xy = in_xy;
+        } else {
+            SFMBA_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), s_));
+            validate_problem_device(b.cam_of_img, b.cam_model, src_img, src_pt, nO, nI, nC, nP, d_bad, s_);
+            int bad = 0;
+            SFMBA_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s_));
+            SFMBA_CUDA(cudaStreamSynchronize(s_));
+            if (bad) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "observation, image or camera index out of range");
+        }
+        put_vec(b.img_slot, lay_.img_slot, s_);
+        put_vec(b.img_active, lay_.img_active, s_);
+        put_vec(b.img_free, lay_.img_free, s_);
+        put_vec(b.cam_slot, lay_.cam_slot, s_);
+        put_vec(b.pose_slot, lay_.pose_slot, s_);
+        put_vec(b.slot_pre_start, lay_.slot_pre_start, s_);
+        put_vec(b.slot_pre, lay_.slot_pre, s_);
+        put_vec(b.slot_masked, lay_.slot_masked, s_);
+        sort_observations(src_pt, src_img, src_xy, nO, nP, nI, b, sort_temp, sort_tmp, k1, v1, k2, v2, s_);
+        SFMBA_CUDA(cudaMemsetAsync(b.state, 0, sizeof(LMState), s_));
+        if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
+            size_t scan_need = 0;
+            // pair count scan uses the sort temp (cub scan needs little)
+            b.npairs = count_pairs(b, pair_scan, sort_temp, sort_tmp, s_);
+            if (b.npairs > (1LL << 31) - 1)
+                throw Error(SFMBA_ERR_UNSUPPORTED, "too many observation pairs for the dense Schur path");
+            (void)scan_need;
+            const size_t ptemp = pairs_temp_bytes(b.npairs, nI);
+            Arena &P = ctx_.pairs;
+            unsigned *ka = nullptr, *kb = nullptr;
+            int2 *vb = nullptr;
+            void *pt = nullptr;
+            int *d_ng = nullptr;
+            for (int pass = 0; pass < 2; ++pass) {
+                if (pass == 0) P.begin_sizing(); else P.commit();
+                b.pairs = P.take<int2>(b.npairs);
+                b.group_start = P.take<int>(b.npairs + 1);
+                b.group_ij = P.take<int2>(b.npairs);
+                ka = P.take<unsigned>(b.npairs);
+                kb = P.take<unsigned>(b.npairs);
+                vb = P.take<int2>(b.npairs + 1);
+                pt = P.take<char>(ptemp);
+                d_ng = P.take<int>(1);
+            }
+            build_pairs(b, pair_scan, ka, kb, vb, pt, ptemp, d_ng, s_);
+            SFMBA_CUDA(cudaMemsetAsync(b.S_img, 0, sizeof(double) * (size_t)nID * nID, s_));
+        }
+        if (mixed) launch_refresh_points32(b, s_);
+    }
+
+    SolveOutput run(const sfmba_options *o) {
+        SolveOutput out;
+        Bufs &b = b_;
+        out.n = b.n;
+        out.solver = solver_;
+        LMState &hs = *ctx_.h_state;
+        // initial cost (lib.rs:794)
+        launch_cost(b, false, false, s_);
+        {
+            LMState init{};
+            init.lambda = o->initial_lambda;
+            init.nu = 2.0;
+            // cost and valid_obs were just written by launch_cost; keep them
+            read_state();
+            init.cost = hs.cost;
+            init.valid_obs = hs.valid_obs;
+            SFMBA_CUDA(cudaMemcpyAsync(b.state, &init, sizeof(LMState), cudaMemcpyHostToDevice, s_));
+            SFMBA_CUDA(cudaStreamSynchronize(s_));
+            out.initial_cost = init.cost;
+            out.final_cost = init.cost;
+            out.valid_obs = init.valid_obs;
+        }
+        if (b.n == 0) return out;  // lib.rs:777-787
+        const bool mixed = b.mixed;
+        for (int outer = 0; outer < o->max_iterations; ++outer) {
+            ++out.iterations;
+            launch_begin_outer(b, s_);
+            launch_prepare_images(b, s_);
+            launch_linearize(b, s_);
+            launch_point_reduce(b, s_);
+            launch_image_reduce(b, s_);
+            launch_diag_fold(b, s_);
+            read_state();
+            // lib.rs:855-857: no observation in front of its camera
+            if (hs.valid_obs == 0) break;
+            bool accepted = false;
+            for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
+                ++out.retries;
+                launch_begin_retry(b, s_);
+                launch_point_inverse(b, s_);
+                launch_image_rhs(b, s_);
+                if (solver_ == SFMBA_SOLVER_DENSE) {
+                    launch_schur_pairs(b, s_);
+                    launch_fold_system(b, s_);
+                    launch_cholesky(b, s_);
+                    launch_cholesky_solve(b, b.rhs, b.delta, s_);
+                    if (mixed)
+                        for (int k = 0; k < o->refinement_steps; ++k) launch_refine(b, s_);
+                } else {
+                    throw Error(SFMBA_ERR_UNSUPPORTED, "PCG solver not available");
+                }
+                launch_backsub_update(b, b.delta, s_);
+                launch_cost(b, true, true, s_);
+                launch_accept(b, s_);
+                launch_commit(b, s_);
+                read_state();
+                if (hs.factor_failed) {
+                    // LU fallback on the symmetrised system (lib.rs:1084-1092)
+                    launch_lu_factor(b, s_);
+                    launch_lu_solve(b, s_);
+                    launch_backsub_update(b, b.delta, s_);
+                    launch_cost(b, true, true, s_);
+                    launch_accept(b, s_);
+                    launch_commit(b, s_);
+                    launch_reject(b, s_);
+                    read_state();
+                }
+                if (hs.accepted) {
+                    accepted = true;
+                    break;
+                }
+            }
+            if (!accepted) break;
+            out.final_cost = hs.cost;
+            out.valid_obs = hs.valid_obs;
+            const double rel = (hs.cost_before - hs.cost) / std::max(hs.cost_before, 1e-12);
+            if (rel < kFunctionTolerance) break;
+            if (o->target_cost > 0.0 && hs.cost <= o->target_cost) break;
+        }
+        read_state();
+        out.final_cost = hs.cost;
+        out.valid_obs = hs.valid_obs;
+        return out;
+    }
+
+    void copy_out(sfmba_result *r, bool device) {
+        const cudaMemcpyKind k = device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (r->poses && b_.nI)
+            SFMBA_CUDA(cudaMemcpyAsync(r->poses, b_.poses, sizeof(double) * 7 * (size_t)b_.nI, k, s_));
+        if (r->points && b_.nP)
+            SFMBA_CUDA(cudaMemcpyAsync(r->points, b_.points, sizeof(double) * 3 * (size_t)b_.nP, k, s_));
+        if (r->camera_params && b_.nC)
+            SFMBA_CUDA(cudaMemcpyAsync(r->camera_params, b_.cams, sizeof(double) * 8 * (size_t)b_.nC, k, s_));
+        SFMBA_CUDA(cudaStreamSynchronize(s_));
+    }
+
+    const Bufs &bufs() const { return b_; }
+    cudaStream_t stream() const { return s_; }
+    Context &ctx() { return ctx_; }
+
+  private:
+    Context &ctx_;
+    cudaStream_t s_;
+    Bufs b_;
+    Layout lay_;
+    int solver_ = SFMBA_SOLVER_DENSE;
+};
+
+int fail(const Error &e) {
+    g_last_error = e.what();
+    return e.status;
+}
+
+template <typename F>
+int guarded(F &&f) {
+    try {
+        g_last_error.clear();
+        f();
+        return SFMBA_OK;
+    } catch (const Error &e) {
+        return fail(e);
+    } catch (const std::exception &e) {
+        g_last_error = e.what();
+        return SFMBA_ERR_INTERNAL;
+    }
+}
+
+int bundle_adjust_impl(const sfmba_problem *p, const sfmba_options *o, sfmba_result *r, bool device,
+                       void *stream) {
+    return guarded([&] {
+        const double t0 = now_s();
+        if (!r) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "result is NULL");
+        check_options(o);
+        check_problem_shape(p);
+        if (!device) check_problem_host(p);
+        Context &ctx = context();
+        cudaStream_t s = (device && stream) ? (cudaStream_t)stream : ctx.stream;
+        Solver solver(ctx, s);
+        solver.setup(p, o, device, true);
+        SolveOutput out = solver.run(o);
+        solver.copy_out(r, device);
+        r->initial_cost = out.initial_cost;
+        r->final_cost = out.final_cost;
+        r->iterations_run = out.iterations;
+        r->damping_retries = out.retries;
+        r->solver_used = out.solver;
+        r->linear_iterations = out.linear_iterations;
+        r->reduced_dim = out.n;
+        r->valid_observations = out.valid_obs;
+        r->status = SFMBA_OK;
+        r->seconds = now_s() - t0;
+    });
+}
+
+}  // namespace
+
+}  // namespace sfmba
+
+using namespace sfmba;
+
+extern "C" {
+
+void sfmba_default_options(sfmba_options *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->max_iterations = 50;
+    o->initial_lambda = 1e-3;
+    o->robust_loss = SFMBA_LOSS_HUBER;
+    o->loss_scale_px = 2.0;
+    o->precision = SFMBA_PRECISION_FP64;
+    o->solver = SFMBA_SOLVER_AUTO;
+    o->pcg_max_iterations = 100;
+    o->pcg_tolerance = 1e-6;
+    o->refinement_steps = 1;
+    o->target_cost = 0.0;
+    o->dense_max_dim = 6000;
+}
+
+int sfmba_bundle_adjust(const sfmba_problem *p, const sfmba_options *o, sfmba_result *r) {
+    int st = bundle_adjust_impl(p, o, r, false, nullptr);
+    if (r) r->status = st;
+    return st;
+}
+
+int sfmba_bundle_adjust_device(const sfmba_problem *p, const sfmba_options *o, sfmba_result *r,
+                               void *stream) {
+    int st = bundle_adjust_impl(p, o, r, true, stream);
+    if (r) r->status = st;
+    return st;
+}
+
+static int cost_entry(const sfmba_problem *p, const sfmba_options *o, double *out, int mode) {
+    return guarded([&] {
+        if (!out) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "output is NULL");
+        check_problem_shape(p);
+        check_problem_host(p);
+        sfmba_options opt;
+        sfmba_default_options(&opt);
+        if (o) opt = *o;
+        check_options(&opt);
+        Context &ctx = context();
+        Solver solver(ctx, ctx.stream);
+        solver.setup(p, &opt, false, false);
+        const Bufs &b = solver.bufs();
+        if (mode == 0) launch_cost(b, false, false, ctx.stream);
+        else launch_mean_error(b, ctx.stream);
+        solver.read_state();
+        const LMState &hs = *ctx.h_state;
+        if (mode == 0) *out = hs.cost;
+        else *out = hs.trial_valid_obs == 0 ? 0.0 : hs.trial_cost / (double)hs.trial_valid_obs;
+    });
+}
+
+int sfmba_total_cost(const sfmba_problem *p, const sfmba_options *o, double *out) {
+    return cost_entry(p, o, out, 0);
+}
+
+int sfmba_mean_reprojection_error(const sfmba_problem *p, double *out) {
+    return cost_entry(p, nullptr, out, 1);
+}
+
+int sfmba_default_fixed_params_mask(int64_t n, const int32_t *models, uint8_t *out) {
+    return guarded([&] {
+        if (n < 0 || (n > 0 && (!models || !out))) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "bad arguments");
+        for (int64_t c = 0; c < n; ++c) {
+            const int m = models[c];
+            if (model_dof(m) == 0) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "unknown camera model id");
+            std::memset(out + c * 8, 0, 8);
+            // intrinsics.rs:33-43: principal point is (1,2) for the f-only models, (2,3) otherwise
+            const int a = (m == SFMBA_SIMPLE_PINHOLE || m == SFMBA_SIMPLE_RADIAL || m == SFMBA_RADIAL) ? 1 : 2;
+            out[c * 8 + a] = 1;
+            out[c * 8 + a + 1] = 1;
+        }
+    });
+}
+
+int sfmba_residuals_jacobians(const sfmba_problem *p, int32_t precision, double *r, double *j_pose,
+                              double *j_point, double *j_camera, uint8_t *valid) {
+    return guarded([&] {
+        check_problem_shape(p);
+        check_problem_host(p);
+        if (precision != SFMBA_PRECISION_FP64 && precision != SFMBA_PRECISION_MIXED)
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "unknown precision");
+        const long long nO = p->num_observations;
+        const int nI = (int)p->num_images, nC = (int)p->num_cameras, nP = (int)p->num_points;
+        Context &ctx = context();
+        cudaStream_t s = ctx.stream;
+        Arena &A = ctx.main;
+        JacProbe q{};
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            q.poses = A.take<double>((size_t)nI * 7);
+            q.cams = A.take<double>((size_t)nC * 8);
+            q.cam_of_img = A.take<int>(nI);
+            q.cam_model = A.take<int>(nC);
+            q.points = A.take<double>((size_t)nP * 3);
+            q.obs_img = A.take<int>(nO);
+            q.obs_pt = A.take<int>(nO);
+            q.obs_xy = A.take<double>((size_t)nO * 2);
+            q.r = A.take<double>((size_t)nO * 2);
+            q.jp = A.take<double>((size_t)nO * 12);
+            q.jx = A.take<double>((size_t)nO * 6);
+            q.jc = A.take<double>((size_t)nO * 16);
+            q.valid = A.take<unsigned char>(nO);
+        }
+        q.nO = nO;
+        put(q.poses, p->poses, (size_t)nI * 7, false, s);
+        put(q.cams, p->camera_params, (size_t)nC * 8, false, s);
+        put(q.cam_of_img, p->camera_of_image, nI, false, s);
+        put(q.cam_model, p->camera_model, nC, false, s);
+        put(q.points, p->points, (size_t)nP * 3, false, s);
+        put(q.obs_img, p->obs_image, nO, false, s);
+        put(q.obs_pt, p->obs_point, nO, false, s);
+        put(q.obs_xy, p->obs_xy, (size_t)nO * 2, false, s);
+        launch_jacobian_probe(q, precision == SFMBA_PRECISION_MIXED, s);
+        auto get = [&](void *dst, const void *src, size_t bytes) {
+            if (dst && bytes) SFMBA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+        };
+        get(r, q.r, sizeof(double) * 2 * nO);
+        get(j_pose, q.jp, sizeof(double) * 12 * nO);
+        get(j_point, q.jx, sizeof(double) * 6 * nO);
+        get(j_camera, q.jc, sizeof(double) * 16 * nO);
+        get(valid, q.valid, nO);
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int sfmba_refine_intrinsics(const sfmba_problem *p, const sfmba_options *o, double *cams) {
+    return guarded([&] { throw Error(SFMBA_ERR_UNSUPPORTED, "refine_intrinsics: not built yet"); });
+}
+
+int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *windows,
+                                const sfmba_options *o, sfmba_result *results) {
+    return guarded([&] { throw Error(SFMBA_ERR_UNSUPPORTED, "batched solve: not built yet"); });
+}
+
+const char *sfmba_last_error(void) { return g_last_error.c_str(); }
+
+const char *sfmba_version(void) { return "sfmba-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

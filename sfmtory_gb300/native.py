@@ -1,0 +1,191 @@
+"""ctypes binding of libsfmba_gb300.so (the C ABI in include/sfmba.h).
+
+There is no fallback: if the CUDA library is missing or no GPU is present,
+every call raises. Build the library with ``python -m sfmtory_gb300.build``
+(or ``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from .abi import (
+    STATUS_NAMES,
+    PackedProblem,
+    ResultBuffers,
+    SfmbaOptions,
+    SfmbaProblem,
+    SfmbaResult,
+    default_options,
+)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsfmba_gb300.so")
+_lock = threading.Lock()
+_lib = None
+
+#: Every entry point declared in include/sfmba.h.
+EXPORTED_SYMBOLS = (
+    "sfmba_default_options",
+    "sfmba_bundle_adjust",
+    "sfmba_bundle_adjust_device",
+    "sfmba_mean_reprojection_error",
+    "sfmba_total_cost",
+    "sfmba_default_fixed_params_mask",
+    "sfmba_refine_intrinsics",
+    "sfmba_bundle_adjust_batched",
+    "sfmba_residuals_jacobians",
+    "sfmba_last_error",
+    "sfmba_version",
+)
+
+
+class SfmbaError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def load(path: str | None = None):
+    """Load the library (no compute call). Raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(
+                f"{p} is missing: the CUDA bundle adjuster has not been built "
+                "(run `python -m sfmtory_gb300.build`); there is no CPU fallback")
+        L = C.CDLL(p)
+        vp = C.c_void_p
+        L.sfmba_default_options.argtypes = [vp]
+        L.sfmba_default_options.restype = None
+        for name in ("sfmba_bundle_adjust",):
+            getattr(L, name).argtypes = [vp, vp, vp]
+        L.sfmba_bundle_adjust_device.argtypes = [vp, vp, vp, vp]
+        L.sfmba_mean_reprojection_error.argtypes = [vp, vp]
+        L.sfmba_total_cost.argtypes = [vp, vp, vp]
+        L.sfmba_default_fixed_params_mask.argtypes = [C.c_int64, vp, vp]
+        L.sfmba_refine_intrinsics.argtypes = [vp, vp, vp]
+        L.sfmba_bundle_adjust_batched.argtypes = [C.c_int32, vp, vp, vp]
+        L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
+        L.sfmba_last_error.restype = C.c_char_p
+        L.sfmba_version.restype = C.c_char_p
+        _lib = L
+        return L
+
+
+def _check(status: int):
+    if status != 0:
+        msg = load().sfmba_last_error().decode(errors="replace")
+        raise SfmbaError(status, msg)
+
+
+def options(**kw) -> SfmbaOptions:
+    return default_options(**kw)
+
+
+class Result:
+    """Outputs of one solve (the fields of sfm-ba's BaOutput plus solver stats)."""
+
+    def __init__(self, buf: ResultBuffers):
+        r = buf.struct
+        self.poses = buf.poses
+        self.points = buf.points
+        self.camera_params = buf.camera_params
+        self.initial_cost = r.initial_cost
+        self.final_cost = r.final_cost
+        self.iterations_run = r.iterations_run
+        self.damping_retries = r.damping_retries
+        self.solver_used = r.solver_used
+        self.linear_iterations = r.linear_iterations
+        self.reduced_dim = r.reduced_dim
+        self.valid_observations = r.valid_observations
+        self.seconds = r.seconds
+
+
+def bundle_adjust_arrays(problem, opts: SfmbaOptions | None = None, **kw) -> Result:
+    """Solve a :class:`~sfmtory_gb300.problem.Problem` through sfmba_bundle_adjust."""
+    L = load()
+    packed = PackedProblem(problem)
+    buf = ResultBuffers(packed)
+    o = opts if opts is not None else default_options(**kw)
+    if opts is not None and kw:
+        for k, v in kw.items():
+            setattr(o, k, v)
+    _check(L.sfmba_bundle_adjust(C.byref(packed.struct), C.byref(o), C.byref(buf.struct)))
+    return Result(buf)
+
+
+def total_cost(problem, opts: SfmbaOptions | None = None, **kw) -> float:
+    L = load()
+    packed = PackedProblem(problem)
+    out = C.c_double()
+    o = opts if opts is not None else default_options(**kw)
+    _check(L.sfmba_total_cost(C.byref(packed.struct), C.byref(o), C.byref(out)))
+    return out.value
+
+
+def mean_reprojection_error_arrays(problem) -> float:
+    L = load()
+    packed = PackedProblem(problem)
+    out = C.c_double()
+    _check(L.sfmba_mean_reprojection_error(C.byref(packed.struct), C.byref(out)))
+    return out.value
+
+
+def default_fixed_params_mask_arrays(models) -> np.ndarray:
+    L = load()
+    models = np.ascontiguousarray(models, dtype=np.int32)
+    out = np.zeros((len(models), 8), dtype=np.uint8)
+    _check(L.sfmba_default_fixed_params_mask(len(models), models.ctypes.data, out.ctypes.data))
+    return out.astype(bool)
+
+
+def refine_intrinsics_arrays(problem, opts: SfmbaOptions | None = None, **kw) -> np.ndarray:
+    L = load()
+    packed = PackedProblem(problem)
+    cams = packed.camera_params.copy()
+    base = dict(max_iterations=30)
+    base.update(kw)
+    o = opts if opts is not None else default_options(**base)
+    _check(L.sfmba_refine_intrinsics(C.byref(packed.struct), C.byref(o), cams.ctypes.data))
+    return cams
+
+
+def residuals_jacobians(problem, fp32: bool = False):
+    """(r [n,2], J_pose [n,2,6], J_point [n,2,3], J_cam [n,2,8], valid [n]) from the GPU kernels."""
+    L = load()
+    packed = PackedProblem(problem)
+    n = len(packed.obs_image)
+    r = np.zeros((n, 2))
+    jp = np.zeros((n, 2, 6))
+    jx = np.zeros((n, 2, 3))
+    jc = np.zeros((n, 2, 8))
+    valid = np.zeros(n, np.uint8)
+    _check(L.sfmba_residuals_jacobians(C.byref(packed.struct), 1 if fp32 else 0, r.ctypes.data,
+                                       jp.ctypes.data, jx.ctypes.data, jc.ctypes.data, valid.ctypes.data))
+    return r, jp, jx, jc, valid.astype(bool)
+
+
+def bundle_adjust_batched_arrays(problems, opts: SfmbaOptions | None = None, **kw) -> list[Result]:
+    L = load()
+    packs = [PackedProblem(p) for p in problems]
+    bufs = [ResultBuffers(p) for p in packs]
+    arr = (SfmbaProblem * len(packs))(*[p.struct for p in packs])
+    res = (SfmbaResult * len(bufs))(*[b.struct for b in bufs])
+    o = opts if opts is not None else default_options(**kw)
+    _check(L.sfmba_bundle_adjust_batched(len(packs), arr, C.byref(o), res))
+    out = []
+    for k, b in enumerate(bufs):
+        b.struct = res[k]
+        out.append(Result(b))
+    return out
+
+
+def version() -> str:
+    return load().sfmba_version().decode()

@@ -1,0 +1,200 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU FP64 oracle.
+
+Bars (written in each test): FP64 path - initial cost 1e-12 relative,
+final cost / parameters 1e-6 relative, same iteration count; FP32 path -
+residuals/Jacobians to FP32 accuracy, final cost 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+from sfmtory_gb300 import abi, native, scenes
+
+pytestmark = pytest.mark.gpu
+
+MODELS = list(scenes.JACOBIAN_TEST_CAMERAS)
+
+
+def _single_obs_problem(model, params, pose, X, obs):
+    from sfmtory_gb300.problem import Problem
+
+    cp = np.zeros((1, 8))
+    cp[0, : len(params)] = params
+    return Problem(
+        camera_of_image=np.array([0], np.int32), camera_model=np.array([model], np.int32), camera_params=cp,
+        poses=np.asarray(pose)[None], points=np.asarray(X)[None], obs_image=np.array([0], np.int32),
+        obs_point=np.array([0], np.int32), obs_xy=np.array([obs], np.float64))
+
+
+@pytest.mark.parametrize("model", MODELS, ids=[abi.MODEL_NAMES[m] for m in MODELS])
+def test_jacobians_match_oracle_and_fd(oracle_lib, model):
+    """Device adjoint Jacobians on the reference fixture (lib.rs:1252-1295):
+    FP64 equals the oracle's analytic Jacobian to 1e-9 relative and meets the
+    reference's FD tolerances; FP32 is within 1e-4 relative of it."""
+    pose, X, obs = scenes.jacobian_test_fixture()
+    params = scenes.JACOBIAN_TEST_CAMERAS[model]
+    p = _single_obs_problem(model, params, pose, X, obs)
+    an = oracle_lib.analytic_jacobians(pose, model, params, X, obs)
+    num = oracle_lib.numerical_jacobians(pose, model, params, X, obs)
+    r, jp, jx, jc, valid = native.residuals_jacobians(p, fp32=False)
+    assert valid[0]
+    scale = max(1.0, np.abs(an[1]).max(), np.abs(an[3]).max())
+    assert np.abs(r[0] - an[0]).max() < 1e-9
+    assert np.abs(jp[0] - an[1]).max() < 1e-9 * scale
+    assert np.abs(jx[0] - an[2]).max() < 1e-9 * scale
+    assert np.abs(jc[0] - an[3]).max() < 1e-9 * scale
+    assert np.linalg.norm(jp[0] - num[1]) < 1e-5
+    assert np.linalg.norm(jx[0] - num[2]) < 1e-5
+    assert np.linalg.norm(jc[0] - num[3]) < 1e-4
+    r32, jp32, jx32, jc32, v32 = native.residuals_jacobians(p, fp32=True)
+    assert v32[0]
+    for a, b in ((jp32[0], an[1]), (jx32[0], an[2]), (jc32[0], an[3])):
+        assert np.abs(a - b).max() <= 1e-4 * max(1.0, np.abs(b).max())
+    # pixel residual: FP32 rounding of ~1e3 px coordinates
+    assert np.abs(r32[0] - an[0]).max() < 2e-3
+
+
+def test_jacobians_random_observations(oracle_lib):
+    """Many random poses/points per model, FP64 device vs oracle (1e-9 rel)."""
+    rng = np.random.default_rng(7)
+    from sfmtory_gb300.problem import Problem, quat_from_scaled_axis
+
+    for model, params in scenes.JACOBIAN_TEST_CAMERAS.items():
+        n = 64
+        cp = np.zeros((n, 8))
+        cp[:, : len(params)] = params
+        q = quat_from_scaled_axis(rng.normal(0, 0.3, (n, 3)))
+        poses = np.concatenate([q, rng.normal(0, 0.5, (n, 3))], 1)
+        pts = rng.normal(0, 0.5, (n, 3)) + np.array([0, 0, 4.0])
+        obs = rng.uniform(0, 600, (n, 2))
+        p = Problem(camera_of_image=np.arange(n, dtype=np.int32), camera_model=np.full(n, model, np.int32),
+                    camera_params=cp, poses=poses, points=pts, obs_image=np.arange(n, dtype=np.int32),
+                    obs_point=np.arange(n, dtype=np.int32), obs_xy=obs)
+        r, jp, jx, jc, valid = native.residuals_jacobians(p)
+        for k in range(n):
+            an = oracle_lib.analytic_jacobians(poses[k], model, params, pts[k], obs[k])
+            assert (an is not None) == bool(valid[k])
+            if an is None:
+                continue
+            s = max(1.0, np.abs(an[1]).max(), np.abs(an[3]).max())
+            assert np.abs(r[k] - an[0]).max() < 1e-8
+            assert np.abs(jp[k] - an[1]).max() < 1e-9 * s
+            assert np.abs(jx[k] - an[2]).max() < 1e-9 * s
+            assert np.abs(jc[k] - an[3]).max() < 1e-9 * s
+
+
+@pytest.mark.parametrize("loss", [abi.LOSS_NONE, abi.LOSS_HUBER, abi.LOSS_CAUCHY])
+def test_total_cost_and_mean_error(oracle_lib, loss):
+    p = scenes.opencv47(seed=1, scale=0.1)
+    a = native.total_cost(p, robust_loss=loss, loss_scale_px=1.0)
+    b = oracle_lib.total_cost(p, robust_loss=loss, loss_scale_px=1.0)
+    assert abs(a - b) <= 1e-12 * abs(b)
+    assert abs(native.mean_reprojection_error_arrays(p) - oracle_lib.mean_reprojection_error(p)) < 1e-12
+
+
+def _compare(gpu, ref, *, cost_rtol=1e-6, param_rtol=1e-6, same_iters=True):
+    assert abs(gpu.initial_cost - ref.initial_cost) <= 1e-12 * abs(ref.initial_cost) + 1e-300
+    assert abs(gpu.final_cost - ref.final_cost) <= cost_rtol * abs(ref.final_cost) + 1e-12
+    if same_iters:
+        assert gpu.iterations_run == ref.iterations_run
+    for a, b in ((gpu.points, ref.points), (gpu.poses, ref.poses), (gpu.camera_params, ref.camera_params)):
+        err = np.abs(a - b) / np.maximum(np.abs(b), 1.0)
+        assert err.max() <= param_rtol, err.max()
+
+
+def test_fp64_recovers_ground_truth_matches_oracle(oracle_lib):
+    p = scenes.recovers_ground_truth_fixture()
+    g = native.bundle_adjust_arrays(p, max_iterations=30)
+    r = oracle_lib.bundle_adjust(p, max_iterations=30)
+    # noiseless problem: final cost ~1e-25, compare the absolute level
+    assert g.final_cost < 1e-12 and r.final_cost < 1e-12
+    assert g.final_cost < 0.01 * g.initial_cost
+    assert abs(g.initial_cost - r.initial_cost) < 1e-10 * r.initial_cost
+    assert np.allclose(g.poses, r.poses, atol=1e-8)
+    assert np.allclose(g.points, r.points, atol=1e-8)
+
+
+def test_fp64_shared_focal_joint_matches_oracle(oracle_lib):
+    """A camera shared by four images (slot fold with several pre-images)."""
+    p = scenes.shared_focal_fixture()
+    pre_g = native.bundle_adjust_arrays(p, max_iterations=50)
+    pre_r = oracle_lib.bundle_adjust(p, max_iterations=50)
+    assert np.allclose(pre_g.points, pre_r.points, atol=1e-7)
+    joint = p.copy(poses=pre_r.poses, points=pre_r.points, fixed_cameras=np.array([False]))
+    g = native.bundle_adjust_arrays(joint, max_iterations=50)
+    r = oracle_lib.bundle_adjust(joint, max_iterations=50)
+    assert abs(g.camera_params[0, 0] - 1500.0) / 1500.0 < 0.02
+    assert abs(g.camera_params[0, 0] - r.camera_params[0, 0]) < 1e-6 * 1500
+
+
+@pytest.mark.parametrize("scale", [0.05, 0.25])
+def test_fp64_ring16_matches_oracle(oracle_lib, scale):
+    p = scenes.ring16(seed=2, scale=scale)
+    kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=50)
+    g = native.bundle_adjust_arrays(p, **kw)
+    r = oracle_lib.bundle_adjust(p, **kw)
+    _compare(g, r)
+
+
+def test_fp64_opencv47_huber_matches_oracle(oracle_lib):
+    p = scenes.opencv47(seed=3, scale=0.05)
+    kw = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=1.0, max_iterations=30)
+    g = native.bundle_adjust_arrays(p, **kw)
+    r = oracle_lib.bundle_adjust(p, **kw)
+    _compare(g, r)
+
+
+def test_mixed_ring16_reaches_oracle_cost(oracle_lib):
+    """FP32 linearisation + Schur, FP64 cost and Cholesky: final cost within
+    1e-6 relative and RMS within 1e-4 px of the FP64 oracle."""
+    from sfmtory_gb300.problem import rms_reprojection_error
+
+    p = scenes.ring16(seed=4, scale=0.25)
+    kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=50)
+    g = native.bundle_adjust_arrays(p, precision=abi.PRECISION_MIXED, **kw)
+    r = oracle_lib.bundle_adjust(p, **kw)
+    assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost
+    rg = rms_reprojection_error(p.copy(poses=g.poses, points=g.points, camera_params=g.camera_params))
+    rr = rms_reprojection_error(p.copy(poses=r.poses, points=r.points, camera_params=r.camera_params))
+    assert abs(rg - rr) < 1e-4
+
+
+def test_total_dim_zero(oracle_lib):
+    p = scenes.recovers_ground_truth_fixture().copy(fixed_poses=np.array([True, True]))
+    g = native.bundle_adjust_arrays(p)
+    assert g.iterations_run == 0
+    assert g.final_cost == g.initial_cost
+    assert np.array_equal(g.points, p.points)
+
+
+def test_no_valid_observations_stops(oracle_lib):
+    """Every point behind its camera: total_cost 0, loop exits at once (lib.rs:855-857)."""
+    p = scenes.recovers_ground_truth_fixture()
+    p = p.copy(points=p.points * np.array([1, 1, -1.0]))
+    g = native.bundle_adjust_arrays(p)
+    r = oracle_lib.bundle_adjust(p)
+    assert g.initial_cost == 0.0 and r.initial_cost == 0.0
+    assert g.iterations_run == r.iterations_run == 1
+    assert np.array_equal(g.points, p.points)
+
+
+def test_empty_problem():
+    from sfmtory_gb300.problem import Problem
+
+    p = Problem(camera_of_image=np.zeros(0, np.int32), camera_model=np.zeros(0, np.int32),
+                camera_params=np.zeros((0, 8)), poses=np.zeros((0, 7)), points=np.zeros((0, 3)),
+                obs_image=np.zeros(0, np.int32), obs_point=np.zeros(0, np.int32), obs_xy=np.zeros((0, 2)))
+    g = native.bundle_adjust_arrays(p)
+    assert g.iterations_run == 0 and g.final_cost == 0.0
+
+
+def test_shuffled_observation_order_same_result(oracle_lib):
+    """The device sorts observations by point; input order must not matter."""
+    p = scenes.ring16(seed=5, scale=0.05)
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(p.num_observations)
+    q = p.copy(obs_image=p.obs_image[perm], obs_point=p.obs_point[perm], obs_xy=p.obs_xy[perm])
+    kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=20)
+    a = native.bundle_adjust_arrays(p, **kw)
+    b = native.bundle_adjust_arrays(q, **kw)
+    assert abs(a.final_cost - b.final_cost) <= 1e-9 * a.final_cost
+    assert np.allclose(a.points, b.points, rtol=0, atol=1e-9)
