@@ -1,0 +1,480 @@
+#!/usr/bin/env python
+"""Bundle-adjustment benchmark on one GB300 (per rank).
+
+Workload (default): ``radial2000`` - 2000 RADIAL cameras on a smooth loop,
+1M points, ~5.96M observations with power-law track lengths (exponent 2.5,
+2..200), sigma = 0.5 px, squared loss, pose 0 fixed, principal points
+masked, seeded synthetic data. Solver: matrix-free Schur PCG with block
+Jacobi.
+
+One step = one complete ``bundle_adjust`` of that problem from its initial
+guess on the FP32+adjoint path (FP32 residual/Jacobian/Schur/PCG kernels,
+FP64 cost and step acceptance), stopped at the tolerance target: the plain
+all-FP64 GPU path's final cost x (1 + 1e-6). ``value`` is observations x LM
+iterations per second of that solve with the problem already in HBM;
+``e2e`` is the same solve through ``sfmba_bundle_adjust`` with host buffers
+(pinned), host->device upload and result download inside the timed region.
+
+``--impl reference`` times the reference algorithm on the host cores (the
+C++ FP64 restatement of sfm-ba in oracle/, one LM iteration per step, its
+Schur accumulation and dense Cholesky timed on samples and scaled).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "BA time-to-tolerance (s) & obs/s: FP32+adjoint vs plain FP64 GPU, same final RMS"
+UNIT = "obs/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="radial2000")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--max-iterations", type=int, default=50)
+    ap.add_argument("--pcg-tol", type=float, default=1e-6)
+    ap.add_argument("--pcg-max", type=int, default=100)
+    ap.add_argument("--skip-fp64", action="store_true", help="skip the FP64 comparison solves")
+    ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def make_problem(args, rank):
+    from sfmtory_gb300 import scenes
+
+    return scenes.WORKLOADS[args.workload](seed=args.seed + rank, scale=args.scale)
+
+
+def workload_config(args, p):
+    counts = np.bincount(p.obs_point, minlength=p.num_points)
+    return {
+        "workload": f"{args.workload}: {p.num_images} {_model_name(p)} cameras, {p.num_points} points, "
+                    f"{p.num_observations} observations, track length mean {counts.mean():.2f} max {counts.max()}",
+        "reduced_dim": p.reduced_dim(),
+        "solver": "matrix-free Schur PCG, block-Jacobi, tol %g, max %d it/retry" % (args.pcg_tol, args.pcg_max),
+        "loss": "squared",
+        "max_lm_iterations": args.max_iterations,
+        "seed": args.seed,
+        "scale": args.scale,
+        "l2": "inputs larger than L2 (observation arrays + per-observation Jacobian records > 129 MB)",
+    }
+
+
+def _model_name(p):
+    from sfmtory_gb300.abi import MODEL_NAMES
+
+    ms = sorted(set(int(m) for m in p.camera_model))
+    return "/".join(MODEL_NAMES[m] for m in ms)
+
+
+def solver_options(args, precision, target_cost=0.0):
+    from sfmtory_gb300 import abi
+
+    return abi.default_options(
+        max_iterations=args.max_iterations, robust_loss=abi.LOSS_NONE, precision=precision,
+        solver=abi.SOLVER_PCG, pcg_tolerance=args.pcg_tol, pcg_max_iterations=args.pcg_max,
+        target_cost=target_cost)
+
+
+# ------------------------------------------------------------------ clocks
+
+CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={CLOCK_QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() in ("active", "1"):
+                    reasons.add(nm)
+        os.remove(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------- device problem
+
+class DeviceProblem:
+    """The problem's arrays in HBM (torch tensors used as plain device
+    buffers) and an sfmba_problem / sfmba_result pointing at them."""
+
+    def __init__(self, p, device):
+        import torch
+
+        from sfmtory_gb300.abi import PackedProblem, SfmbaProblem, SfmbaResult
+
+        pk = PackedProblem(p)
+        self.keep = []
+
+        def dev(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).to(device)
+            self.keep.append(t)
+            return t.data_ptr()
+
+        s = SfmbaProblem()
+        s.num_images, s.num_cameras = pk.struct.num_images, pk.struct.num_cameras
+        s.num_points, s.num_observations = pk.struct.num_points, pk.struct.num_observations
+        s.camera_of_image = dev(pk.camera_of_image)
+        s.camera_model = dev(pk.camera_model)
+        s.camera_params = dev(pk.camera_params)
+        s.poses = dev(pk.poses)
+        s.points = dev(pk.points)
+        s.obs_image = dev(pk.obs_image)
+        s.obs_point = dev(pk.obs_point)
+        s.obs_xy = dev(pk.obs_xy)
+        s.fixed_poses = dev(pk.fixed_poses) if pk.fixed_poses is not None else None
+        s.fixed_cameras = dev(pk.fixed_cameras) if pk.fixed_cameras is not None else None
+        s.fixed_camera_params = dev(pk.fixed_camera_params) if pk.fixed_camera_params is not None else None
+        self.struct = s
+        self.out_poses = torch.zeros_like(self.keep[3])
+        self.out_points = torch.zeros_like(self.keep[4])
+        self.out_cams = torch.zeros_like(self.keep[2])
+        r = SfmbaResult()
+        r.poses, r.points, r.camera_params = (self.out_poses.data_ptr(), self.out_points.data_ptr(),
+                                              self.out_cams.data_ptr())
+        self.result = r
+
+
+def solve_device(L, dp, opts, stream):
+    """One device-resident solve; returns (result struct copy, device ms)."""
+    import ctypes as C
+
+    import torch
+
+    from sfmtory_gb300 import native
+
+    r = type(dp.result).from_buffer_copy(dp.result)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st = L.sfmba_bundle_adjust_device(C.byref(dp.struct), C.byref(opts), C.byref(r), C.c_void_p(stream.cuda_stream))
+    e1.record(stream)
+    stream.synchronize()
+    if st != 0:
+        raise native.SfmbaError(st, L.sfmba_last_error().decode())
+    return r, e0.elapsed_time(e1)
+
+
+def pinned_problem(p):
+    """Copy of the problem whose arrays live in pinned host memory."""
+    import torch
+
+    def pin(a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0]).dtype, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    from sfmtory_gb300.abi import MAX_CAMERA_PARAMS
+
+    cp = np.zeros((p.num_cameras, MAX_CAMERA_PARAMS))
+    cp[:, : p.camera_params.shape[1]] = p.camera_params
+    return p.copy(camera_of_image=pin(p.camera_of_image, np.int32), camera_model=pin(p.camera_model, np.int32),
+                  camera_params=pin(cp, np.float64), poses=pin(p.poses, np.float64),
+                  points=pin(p.points, np.float64), obs_image=pin(p.obs_image, np.int32),
+                  obs_point=pin(p.obs_point, np.int32), obs_xy=pin(p.obs_xy, np.float64))
+
+
+def e2e_solve(L, pp, opts):
+    """Host-buffer solve through sfmba_bundle_adjust (pinned in and out)."""
+    import ctypes as C
+
+    import torch
+
+    from sfmtory_gb300 import native
+    from sfmtory_gb300.abi import PackedProblem, ResultBuffers
+
+    pk = PackedProblem(pp)
+    rb = ResultBuffers(pk)
+    for name in ("poses", "points", "camera_params"):
+        a = getattr(rb, name)
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        setattr(rb, name, t.numpy())
+    rb.struct.poses, rb.struct.points, rb.struct.camera_params = (rb.poses.ctypes.data, rb.points.ctypes.data,
+                                                                  rb.camera_params.ctypes.data)
+    t0 = time.perf_counter()
+    st = L.sfmba_bundle_adjust(C.byref(pk.struct), C.byref(opts), C.byref(rb.struct))
+    t1 = time.perf_counter()
+    if st != 0:
+        raise native.SfmbaError(st, L.sfmba_last_error().decode())
+    h2d = (pk.obs_image.nbytes + pk.obs_point.nbytes + pk.obs_xy.nbytes + pk.points.nbytes + pk.poses.nbytes
+           + pk.camera_params.nbytes + pk.camera_of_image.nbytes + pk.camera_model.nbytes
+           + sum(a.nbytes for a in (pk.fixed_poses, pk.fixed_cameras, pk.fixed_camera_params) if a is not None))
+    d2h = rb.poses.nbytes + rb.points.nbytes + rb.camera_params.nbytes
+    return rb.struct, t1 - t0, h2d, d2h
+
+
+# -------------------------------------------------------------- roofline
+
+def algorithmic_bytes(phase, nO, nP, nI, D, t):
+    """Compulsory bytes one launch of the phase's kernel moves (each array
+    touched once; per-observation Jacobian records read without padding)."""
+    jac = (6 + 2 * D) * t          # Jx~ (2x3) and Jc~ (2xD) of one observation
+    if phase == "pcg_images":     # q = (H + lam diag H) p - sum Jc~^T (Jx~ u)
+        return nO * (4 + 4 + jac + 3 * t) + nI * (D * D * 8 + 2 * D * t + 8 + 4 + 8)
+    if phase == "pcg_points":     # u_p = C^-1 sum Jx~^T (Jc~ p)
+        return nO * (4 + jac) + nP * (8 + 6 * t + 1 + 3 * t) + nI * D * t
+    if phase == "linearize":      # residual + adjoint Jacobian records
+        return nO * (4 + 4 + 16 + (8 + 2 * D) * t + 1) + nP * (16 if t == 4 else 24) + nI * (24 * t + 16)
+    if phase == "image_reduce":
+        return nO * (4 + (2 + 2 * D) * t) + nI * (D * D * 8 + D * 8 + 8)
+    if phase == "cost":
+        return nO * (4 + 4 + 16) + nP * 24 + nI * 56
+    return None
+
+
+def roofline(profile, p, D, t, peaks):
+    phases = {k: v for k, v in profile.items() if isinstance(v, dict) and v.get("launches")}
+    top = max(phases, key=lambda k: phases[k]["ms"])
+    order = sorted(phases, key=lambda k: -phases[k]["ms"])
+    for name in order:  # the heaviest phase with a one-kernel byte model
+        if algorithmic_bytes(name, p.num_observations, p.num_points, p.num_images, D, t) is not None:
+            top = name
+            break
+    ms_per = phases[top]["ms"] / phases[top]["launches"]
+    by = algorithmic_bytes(top, p.num_observations, p.num_points, p.num_images, D, t)
+    peak = peaks.get("hbm_gbs")
+    achieved = by / (ms_per * 1e-3) / 1e9
+    return {
+        "kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 4) if peak else None, "traffic": None,
+        "algorithmic_bytes_per_launch": int(by), "avg_launch_ms": round(ms_per, 4),
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peak else "fallback",
+    }
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return json.load(open(path))
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_baseline_sample(p, point_stride, chol_dim):
+    import oracle
+
+    t0 = time.perf_counter()
+    s = oracle.lm_iteration_sample(p, point_stride=point_stride, chol_dim=chol_dim)
+    wall = time.perf_counter() - t0
+    v = p.num_observations / s["seconds_per_iteration"]
+    sample = (f"one LM iteration of the C++ FP64 restatement of sfm-ba on the full problem: Jacobians, "
+              f"assembly, back-substitution and trial cost of all {p.num_observations} observations timed; "
+              f"Schur accumulation timed on {s['schur_points']} points and scaled x{s['schur_scale']:.1f} "
+              f"(ideal {s['threads']}-thread speed-up, per-thread accumulator reduction not counted); unblocked "
+              f"dense LL^T timed at n={s['chol_dim']} and scaled by (n/{s['chol_dim']})^3 to n={s['reduced_dim']}; "
+              f"extrapolated {s['seconds_per_iteration']:.1f} s/iteration from {wall:.1f} s measured")
+    return v, s, sample
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+
+    p = make_problem(args, 0)
+    stride = max(1, p.num_points // 20000)
+    chol_dim = min(2000, p.reduced_dim())
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        v, s, sample = cpu_baseline_sample(p, stride, chol_dim)
+        if k >= args.warmup:
+            vals.append(v)
+            info = (s, sample)
+    v = statistics.mean(vals)
+    s, sample = info
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": s["seconds_per_iteration"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, p),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": s["threads"], "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "phases_s": {k: s[k] for k in ("jacobians_s", "assembly_s", "schur_sample_s", "cholesky_sample_s",
+                                        "backsub_update_s", "trial_cost_s")},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ ours
+
+def run_ours(args):
+    import torch
+
+    from sfmtory_gb300 import abi, native
+    from sfmtory_gb300.problem import rms_reprojection_error
+
+    rank, world, local = dist_env()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    L = native.load()
+    p = make_problem(args, rank)
+    nO = p.num_observations
+    dp = DeviceProblem(p, device)
+    stream = torch.cuda.Stream(device=device)
+
+    # Plain all-FP64 GPU path: its final cost defines the tolerance target.
+    fp64 = {}
+    target = 0.0
+    if not args.skip_fp64:
+        r64, ms64_full = solve_device(L, dp, solver_options(args, abi.PRECISION_FP64), stream)
+        target = r64.final_cost * (1.0 + 1e-6)
+        r64t, ms64 = solve_device(L, dp, solver_options(args, abi.PRECISION_FP64, target), stream)
+        fp64 = {"final_cost": r64.final_cost, "iterations": r64.iterations_run, "full_solve_s": ms64_full / 1e3,
+                "time_to_tolerance_s": ms64 / 1e3, "iterations_to_tolerance": r64t.iterations_run,
+                "pcg_iterations": r64.linear_iterations}
+
+    opts32 = solver_options(args, abi.PRECISION_MIXED, target)
+    for _ in range(max(3, args.warmup)):
+        solve_device(L, dp, opts32, stream)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    native.profile_enable(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    times, iters, results = [], [], []
+    for _ in range(args.steps):
+        r, ms = solve_device(L, dp, opts32, stream)
+        times.append(ms / 1e3)
+        iters.append(r.iterations_run)
+        results.append(r)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    prof = native.profile_report()
+    native.profile_enable(False)
+    step_s = statistics.mean(times)
+    if world > 1:
+        t = torch.tensor([max(times)], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_max = float(t.item())
+    else:
+        step_max = max(times)
+    obs_per_step = nO * statistics.mean(iters)
+    value = obs_per_step * world / (step_s if world == 1 else step_max)
+    last = results[-1]
+
+    # End to end through the host API (pinned buffers).
+    pp = pinned_problem(p)
+    e2e_times, e2e_iters, h2d, d2h = [], [], 0, 0
+    e2e_solve(L, pp, opts32)
+    for _ in range(max(1, args.e2e_steps)):
+        r, s, h2d, d2h = e2e_solve(L, pp, opts32)
+        e2e_times.append(s)
+        e2e_iters.append(r.iterations_run)
+    e2e_value = nO * statistics.mean(e2e_iters) / statistics.mean(e2e_times) * world
+
+    out_points = dp.out_points.cpu().numpy()
+    out_poses = dp.out_poses.cpu().numpy()
+    out_cams = dp.out_cams.cpu().numpy()
+    rms32 = rms_reprojection_error(p.copy(points=out_points, poses=out_poses, camera_params=out_cams))
+
+    if rank != 0:
+        return
+    D = p.block_width()
+    roof = roofline(prof, p, D, 4, measured_peaks())
+    cpu = None
+    if not args.skip_cpu and world == 1:
+        stride = max(1, p.num_points // 20000)
+        v, s, sample = cpu_baseline_sample(p, stride, min(2000, p.reduced_dim()))
+        import oracle
+
+        cpu = {"value": v, "unit": UNIT, "cores": s["threads"], "kind": "port", "sample": sample}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(args, p),
+        "time_to_tolerance_s": step_s, "lm_iterations": statistics.mean(iters),
+        "lm_iterations_per_s": statistics.mean(iters) / step_s, "pcg_iterations": last.linear_iterations,
+        "final_cost": last.final_cost, "initial_cost": last.initial_cost,
+        "reached_tolerance": (last.final_cost <= target) if target else None, "rms_px": rms32,
+        "fp64_gpu": fp64, "speedup_vs_fp64_gpu": (fp64["time_to_tolerance_s"] / step_s) if fp64 else None,
+        "roofline": roof, "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "seconds_per_step": statistics.mean(e2e_times)},
+        "gpu_launches": int(prof.get("kernel_launches", 0) // max(1, args.steps)),
+        "clocks": clk,
+        "phase_ms_per_step": {k: round(v["ms"] / args.steps, 3) for k, v in prof.items()
+                              if isinstance(v, dict) and v.get("launches")},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -180,6 +180,15 @@ int sfmba_residuals_jacobians(const sfmba_problem *problem, int32_t precision, d
                               double *j_pose, double *j_point, double *j_camera,
                               uint8_t *valid);
 
+/* Benchmarking aid (no counterpart in the reference): when enabled, every
+ * kernel phase of the solves made on this thread is bracketed by CUDA events
+ * on its launch stream. Enabling or disabling clears the totals. */
+int sfmba_profile_enable(int32_t on);
+
+/* JSON object {phase: {"ms": total device ms, "launches": n}} of the
+ * profiled phases since the last sfmba_profile_enable, into buf[len]. */
+int sfmba_profile_report(char *buf, int64_t len);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char *sfmba_last_error(void);
 

@@ -59,6 +59,7 @@ def lib():
             L.oracle_set_threads.argtypes = [C.c_int]
             L.oracle_threads.restype = C.c_int
             L.oracle_phase_seconds.argtypes = [vp]
+            L.oracle_lm_iteration_sample.argtypes = [vp, vp, C.c_int, C.c_int, vp]
             _lib = L
     return _lib
 
@@ -196,3 +197,29 @@ def project(model, params, pc) -> np.ndarray:
     out = np.zeros(2)
     lib().oracle_project(int(model), p.ctypes.data, pc.ctypes.data, out.ctypes.data)
     return out
+
+
+def lm_iteration_sample(problem, point_stride: int, chol_dim: int, options: SfmbaOptions | None = None, **kw):
+    """Phase times of one reference LM iteration on the full problem, with the
+    Schur accumulation and the dense Cholesky timed on samples (see
+    oracle_lm_iteration_sample). Returns a dict with the raw times and the
+    extrapolated seconds per LM iteration."""
+    packed = PackedProblem(problem)
+    out = np.zeros(8)
+    st = lib().oracle_lm_iteration_sample(C.byref(packed.struct), C.byref(_opts(options, **kw)),
+                                          int(point_stride), int(chol_dim), out.ctypes.data)
+    if st != 0:
+        raise ValueError(f"oracle_lm_iteration_sample failed with status {st}")
+    n = problem.reduced_dim()
+    threads_used = max(1.0, out[7])
+    n_pts_free = max(out[6], 1.0)
+    schur_scale = (problem.num_points / point_stride) / n_pts_free * point_stride / threads_used
+    chol_scale = (n / max(1, min(chol_dim, n))) ** 3
+    est = out[0] + out[1] + out[2] * schur_scale + out[3] * chol_scale + out[4] + out[5]
+    return {
+        "jacobians_s": out[0], "assembly_s": out[1], "schur_sample_s": out[2], "schur_points": int(out[6]),
+        "cholesky_sample_s": out[3], "chol_dim": int(min(chol_dim, n)), "backsub_update_s": out[4],
+        "trial_cost_s": out[5], "threads": int(out[7]), "reduced_dim": n,
+        "schur_scale": schur_scale, "cholesky_scale": chol_scale, "seconds_per_iteration": est,
+        "measured_s": float(out[:6].sum()),
+    }

@@ -893,6 +893,134 @@ int oracle_bundle_adjust(const sfmba_problem *p, const sfmba_options *opt, sfmba
     return finish(initial_cost, cost, iterations_run);
 }
 
+
+// CPU baseline sample of ONE Levenberg-Marquardt iteration of the reference
+// algorithm on the full problem (lib.rs:816-1176), for problems whose dense
+// reduced system is too large to run whole in a bounded time. Phases:
+//   out[0] Jacobians of every observation (parallel, lib.rs:832-853)
+//   out[1] serial normal-equation assembly of every observation (:859-909)
+//   out[2] Schur accumulation of every `point_stride`-th point into the dense
+//          n x n system, one thread (:114-211); scale by stride / threads
+//   out[3] unblocked LL^T of a chol_dim x chol_dim SPD matrix, one thread
+//          like nalgebra (:1081); scale by (n / chol_dim)^3
+//   out[4] point back-substitution + trial update of every point (:1100-1164)
+//   out[5] trial cost of every observation (parallel, :1176)
+//   out[6] points in the Schur sample, out[7] threads used.
+int oracle_lm_iteration_sample(const sfmba_problem *p, const sfmba_options *opt, int point_stride,
+                               int chol_dim, double *out) {
+    Problem P;
+    if (!load(p, P) || !opt || !out || point_stride < 1 || chol_dim < 1) return SFMBA_ERR_INVALID_ARGUMENT;
+    const int loss = opt->robust_loss;
+    const double scale = opt->loss_scale_px;
+    const int nthreads = oracle_threads();
+    std::vector<long> pose_slot(P.nI, -1), cam_slot(P.nC, -1);
+    long n = 0;
+    for (long i = 0; i < P.nI; ++i)
+        if (!P.fixed_pose[i]) { pose_slot[i] = n; n += 6; }
+    for (long c = 0; c < P.nC; ++c)
+        if (!P.fixed_cam[c]) { cam_slot[c] = n; n += model_dof(P.model[c]); }
+    for (int k = 0; k < 8; ++k) out[k] = 0.0;
+    double t0 = now_s();
+    std::vector<Jac> J(P.nO);
+    std::vector<double> W(P.nO);
+    std::vector<char> ok(P.nO);
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (long o = 0; o < P.nO; ++o) {
+        int i = P.ob_img[o], c = P.cam_of_img[i];
+        ok[o] = analytic(load_pose(&P.poses[i * 7]), P.model[c], &P.cam[c * 8], &P.points[P.ob_pt[o] * 3],
+                         P.ob_xy[2 * o], P.ob_xy[2 * o + 1], J[o]);
+        if (ok[o]) W[o] = robust_weight(std::sqrt(J[o].r[0] * J[o].r[0] + J[o].r[1] * J[o].r[1]), loss, scale);
+    }
+    double t1 = now_s();
+    out[0] = t1 - t0;
+    std::vector<double> Cd(P.nP * 9, 0.0), Cg(P.nP * 3, 0.0);
+    std::vector<std::vector<EBlock>> p2o(P.nP);
+    std::vector<double> Bp(P.nI * 36, 0.0), bc(P.nC * 8, 0.0);
+    for (long o = 0; o < P.nO; ++o) {
+        if (!ok[o]) continue;
+        const Jac &q = J[o];
+        const double w = W[o];
+        const int i = P.ob_img[o], c = P.cam_of_img[i], pt = P.ob_pt[o], k = model_dof(P.model[c]);
+        for (int a = 0; a < 3; ++a) {
+            for (int b = 0; b < 3; ++b) Cd[pt * 9 + a * 3 + b] += w * (q.jx[0][a] * q.jx[0][b] + q.jx[1][a] * q.jx[1][b]);
+            Cg[pt * 3 + a] += w * (q.jx[0][a] * q.r[0] + q.jx[1][a] * q.r[1]);
+        }
+        if (pose_slot[i] >= 0) {
+            EBlock e;
+            e.slot = (int)pose_slot[i]; e.rows = 6;
+            for (int a = 0; a < 6; ++a) {
+                for (int b = 0; b < 6; ++b) Bp[i * 36 + a * 6 + b] += w * (q.jp[0][a] * q.jp[0][b] + q.jp[1][a] * q.jp[1][b]);
+                for (int b = 0; b < 3; ++b) e.E[a * 3 + b] = w * (q.jp[0][a] * q.jx[0][b] + q.jp[1][a] * q.jx[1][b]);
+            }
+            p2o[pt].push_back(e);
+        }
+        if (cam_slot[c] >= 0) {
+            EBlock e;
+            e.slot = (int)cam_slot[c]; e.rows = k;
+            for (int a = 0; a < k; ++a) {
+                bc[c * 8 + a] += w * (q.jc[0][a] * q.r[0] + q.jc[1][a] * q.r[1]);
+                for (int b = 0; b < 3; ++b) e.E[a * 3 + b] = w * (q.jc[0][a] * q.jx[0][b] + q.jc[1][a] * q.jx[1][b]);
+            }
+            p2o[pt].push_back(e);
+        }
+    }
+    double t2 = now_s();
+    out[1] = t2 - t1;
+    {
+        std::vector<double> S((size_t)n * n, 0.0), rhs(n, 0.0);
+        std::vector<double> Ci(9);
+        long sampled = 0;
+        double ts = now_s();
+        for (long q = 0; q < P.nP; q += point_stride) {
+            if (p2o[q].empty()) continue;
+            double m[9];
+            for (int a = 0; a < 9; ++a) m[a] = Cd[q * 9 + a];
+            for (int a = 0; a < 3; ++a) m[a * 4] += Cd[q * 9 + a * 4] * opt->initial_lambda;
+            if (!inverse3(m, Ci.data())) continue;
+            accumulate_point(Ci.data(), p2o[q], &Cg[q * 3], S.data(), rhs.data(), n);
+            ++sampled;
+        }
+        out[2] = now_s() - ts;
+        out[6] = (double)sampled;
+    }
+    {
+        const long m = std::min<long>(chol_dim, std::max<long>(n, 1));
+        std::vector<double> A((size_t)m * m);
+        for (long a = 0; a < m; ++a)
+            for (long b = 0; b < m; ++b) A[a * m + b] = (a == b ? (double)m : 0.0) + 1.0 / (1.0 + (double)(a > b ? a - b : b - a));
+        double tc = now_s();
+        cholesky(A, m);
+        out[3] = now_s() - tc;
+    }
+    double t4 = now_s();
+    std::vector<double> delta(n, 1e-9), tpts = P.points, tposes = P.poses, tcams = P.cam;
+    for (long q = 0; q < P.nP; ++q) {
+        if (p2o[q].empty()) continue;
+        double m[9], ci[9];
+        for (int a = 0; a < 9; ++a) m[a] = Cd[q * 9 + a];
+        for (int a = 0; a < 3; ++a) m[a * 4] += Cd[q * 9 + a * 4] * opt->initial_lambda;
+        if (!inverse3(m, ci)) continue;
+        double acc[3] = {Cg[q * 3], Cg[q * 3 + 1], Cg[q * 3 + 2]};
+        for (const EBlock &e : p2o[q])
+            for (int r = 0; r < e.rows; ++r)
+                for (int c = 0; c < 3; ++c) acc[c] += e.E[r * 3 + c] * delta[e.slot + r];
+        for (int a = 0; a < 3; ++a) tpts[q * 3 + a] -= ci[a * 3] * acc[0] + ci[a * 3 + 1] * acc[1] + ci[a * 3 + 2] * acc[2];
+    }
+    for (long i = 0; i < P.nI; ++i) {
+        double d[6] = {0, 0, 0, 0, 0, 0};
+        if (pose_slot[i] >= 0)
+            for (int a = 0; a < 6; ++a) d[a] = delta[pose_slot[i] + a];
+        store_pose(perturb_pose(load_pose(&P.poses[i * 7]), d), &tposes[i * 7]);
+    }
+    double t5 = now_s();
+    out[4] = t5 - t4;
+    volatile double c = total_cost(P, tposes, tcams, tpts, loss, scale);
+    (void)c;
+    out[5] = now_s() - t5;
+    out[7] = nthreads;
+    return SFMBA_OK;
+}
+
 // intrinsics.rs:116-238 (refine_intrinsics, refine_one_camera): per-camera
 // dense LM over that camera's own parameters with central-difference
 // Jacobians; cameras with fewer than 8 observations are left untouched.

@@ -30,7 +30,14 @@ struct Error : std::runtime_error {
         }                                                                                      \
     } while (0)
 
-#define SFMBA_LAUNCH_CHECK() SFMBA_CUDA(cudaGetLastError())
+// Kernel launches of this library on the calling thread (benchmark bookkeeping).
+extern thread_local long long g_kernel_launches;
+
+#define SFMBA_LAUNCH_CHECK()                \
+    do {                                    \
+        ++::sfmba::g_kernel_launches;       \
+        SFMBA_CUDA(cudaGetLastError());     \
+    } while (0)
 
 constexpr int kMaxParams = SFMBA_MAX_CAMERA_PARAMS;
 constexpr double kMinDepth = 1e-9;            // crates/sfm-ba/src/lib.rs:256, 338
@@ -74,10 +81,15 @@ struct LMState {
     int converged;
     long long valid_obs;
     long long trial_valid_obs;
-    int pcg_iterations;
-    int pad;
-    double pcg_rr0;
-    double pcg_rr;
+    int pcg_iterations;  // iterations of the current solve
+    int pcg_done;        // converged or broke down
+    double pcg_rz;       // r . z
+    double pcg_bb;       // |b|^2 of the current solve
+    double pcg_rr;       // |r|^2
+    double pcg_alpha;
+    double pcg_beta;
+    double pcg_tol2;     // stop when |r|^2 <= tol2 |b|^2
+    long long pcg_total;  // iterations summed over the whole solve
 };
 
 inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }

@@ -73,7 +73,8 @@ struct Bufs {
     void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
     void *pcg_u = nullptr;        // [nP*4] per-point Cinv E^T p
     void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
-    double *pcg_dots = nullptr;   // [kDotSlots]
+    double *pcg_part = nullptr;   // [3*nI] per-image partial dot products
+    double pcg_tol = 1e-6;
 };
 
 constexpr int kCostBlocks = 1024;
@@ -136,8 +137,15 @@ void launch_lu_factor(const Bufs &b, cudaStream_t s);
 void launch_lu_solve(const Bufs &b, cudaStream_t s);
 
 // ---- matrix-free Schur PCG (k_pcg.cu)
+// Preconditioner and start vectors (x = 0, r = rhs, p = z = M^-1 r).
 void launch_pcg_setup(const Bufs &b, cudaStream_t s);
-void launch_pcg_iteration(const Bufs &b, cudaStream_t s);
-void launch_pcg_finish(const Bufs &b, cudaStream_t s);
+// One PCG iteration: q = S p (two passes), x/r update, z = M^-1 r, new p.
+// One PCG iteration in three launch groups: q = S p is the point pass then
+// the image pass; the vector group updates x, r, z = M^-1 r and p.
+void launch_pcg_points(const Bufs &b, cudaStream_t s);
+void launch_pcg_images(const Bufs &b, cudaStream_t s);
+void launch_pcg_vector(const Bufs &b, cudaStream_t s);
+// Scatter the image-level solution to the slot-level delta.
+void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
 
 }  // namespace sfmba

@@ -23,13 +23,92 @@
 
 namespace sfmba {
 
+thread_local long long g_kernel_launches = 0;
+
 namespace {
+
+constexpr int kPcgPollEvery = 8;  // PCG iterations between host convergence polls
 
 thread_local std::string g_last_error;
 
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
+
+
+// Per-phase device timing: CUDA events on the launch stream around each
+// kernel phase, resolved after the solve's final synchronisation.
+const char *const kPhaseNames[] = {"setup",        "linearize",   "point_reduce", "image_reduce",
+                                   "point_inverse", "image_rhs",  "schur_pairs",  "fold",
+                                   "cholesky",     "trsv",        "refine",       "pcg_precond",
+                                   "pcg_points",   "pcg_images",  "pcg_vector",   "backsub_update",
+                                   "cost",         "lu",          "lm_bookkeeping"};
+enum Phase {
+    PH_SETUP, PH_LINEARIZE, PH_POINT_REDUCE, PH_IMAGE_REDUCE, PH_POINT_INVERSE, PH_IMAGE_RHS,
+    PH_SCHUR, PH_FOLD, PH_CHOLESKY, PH_TRSV, PH_REFINE, PH_PCG_PRECOND, PH_PCG_POINTS,
+    PH_PCG_IMAGES, PH_PCG_VECTOR, PH_BACKSUB, PH_COST, PH_LU, PH_LM, PH_COUNT
+};
+
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    double ms[PH_COUNT] = {0};
+    long long launches[PH_COUNT] = {0};
+    cudaEvent_t take() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            SFMBA_CUDA(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    void resolve() {
+        for (auto &p : pending) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, p.second.first, p.second.second) == cudaSuccess) {
+                ms[p.first] += t;
+                launches[p.first] += 1;
+            } else {
+                (void)cudaGetLastError();
+            }
+        }
+        pending.clear();
+        used = 0;
+    }
+    void reset() {
+        resolve();
+        for (int k = 0; k < PH_COUNT; ++k) { ms[k] = 0; launches[k] = 0; }
+    }
+};
+
+Profiler &profiler() {
+    thread_local Profiler p;
+    return p;
+}
+
+// Brackets the launches of one phase with events when profiling is on.
+struct PhaseScope {
+    Profiler &p;
+    int ph;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    PhaseScope(int phase, cudaStream_t stream) : p(profiler()), ph(phase), s(stream) {
+        if (p.on) {
+            a = p.take();
+            SFMBA_CUDA(cudaEventRecord(a, s));
+        }
+    }
+    ~PhaseScope() {
+        if (p.on && a) {
+            cudaEvent_t b = p.take();
+            if (cudaEventRecord(b, s) == cudaSuccess) p.pending.push_back({ph, {a, b}});
+            else (void)cudaGetLastError();
+        }
+    }
+};
+#define SFMBA_PHASE(ph) PhaseScope phase_scope_##__LINE__(ph, s_)
 
 // Bump allocator over one device allocation that grows on demand and is
 // kept across calls on the same thread.
@@ -316,6 +395,7 @@ class Solver {
             b = Bufs();
             b.nI = nI; b.nC = nC; b.nP = nP; b.nO = nO; b.n = n; b.D = D; b.nID = nID;
             b.mixed = mixed; b.loss = o->robust_loss; b.loss_scale = o->loss_scale_px;
+            b.pcg_tol = o->pcg_tolerance > 0.0 ? o->pcg_tolerance : 1e-6;
             b.cam_model = A.take<int>(nC);
             b.cam_of_img = A.take<int>(nI);
             b.cams = A.take<double>((size_t)nC * 8);
@@ -384,7 +464,7 @@ class Solver {
                     b.pcg_q = A.take<char>((size_t)nID * tsz);
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
                     b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
-                    b.pcg_dots = A.take<double>(kDotSlots);
+                    b.pcg_part = A.take<double>((size_t)3 * nI);
                 }
             }
             sort_temp = A.take<char>(sort_tmp);
@@ -462,7 +542,7 @@ class Solver {
         out.solver = solver_;
         LMState &hs = *ctx_.h_state;
         // initial cost (lib.rs:794)
-        launch_cost(b, false, false, s_);
+        { SFMBA_PHASE(PH_COST); launch_cost(b, false, false, s_); }
         {
             LMState init{};
             init.lambda = o->initial_lambda;
@@ -481,45 +561,53 @@ class Solver {
         const bool mixed = b.mixed;
         for (int outer = 0; outer < o->max_iterations; ++outer) {
             ++out.iterations;
-            launch_begin_outer(b, s_);
-            launch_prepare_images(b, s_);
-            launch_linearize(b, s_);
-            launch_point_reduce(b, s_);
-            launch_image_reduce(b, s_);
-            launch_diag_fold(b, s_);
+            { SFMBA_PHASE(PH_LM); launch_begin_outer(b, s_); }
+            { SFMBA_PHASE(PH_LINEARIZE); launch_prepare_images(b, s_); launch_linearize(b, s_); }
+            { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
+            { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
             read_state();
             // lib.rs:855-857: no observation in front of its camera
             if (hs.valid_obs == 0) break;
             bool accepted = false;
             for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
                 ++out.retries;
-                launch_begin_retry(b, s_);
-                launch_point_inverse(b, s_);
-                launch_image_rhs(b, s_);
+                { SFMBA_PHASE(PH_LM); launch_begin_retry(b, s_); }
+                { SFMBA_PHASE(PH_POINT_INVERSE); launch_point_inverse(b, s_); }
+                { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); }
                 if (solver_ == SFMBA_SOLVER_DENSE) {
-                    launch_schur_pairs(b, s_);
-                    launch_fold_system(b, s_);
-                    launch_cholesky(b, s_);
-                    launch_cholesky_solve(b, b.rhs, b.delta, s_);
-                    if (mixed)
+                    { SFMBA_PHASE(PH_SCHUR); launch_schur_pairs(b, s_); }
+                    { SFMBA_PHASE(PH_FOLD); launch_fold_system(b, s_); }
+                    { SFMBA_PHASE(PH_CHOLESKY); launch_cholesky(b, s_); }
+                    { SFMBA_PHASE(PH_TRSV); launch_cholesky_solve(b, b.rhs, b.delta, s_); }
+                    if (mixed) {
+                        SFMBA_PHASE(PH_REFINE);
                         for (int k = 0; k < o->refinement_steps; ++k) launch_refine(b, s_);
+                    }
                 } else {
-                    throw Error(SFMBA_ERR_UNSUPPORTED, "PCG solver not available");
+                    { SFMBA_PHASE(PH_PCG_PRECOND); launch_pcg_setup(b, s_); }
+                    const int maxit = std::max(1, o->pcg_max_iterations);
+                    for (int it = 0; it < maxit; it += kPcgPollEvery) {
+                        const int m = std::min(kPcgPollEvery, maxit - it);
+                        for (int k = 0; k < m; ++k) {
+                            { SFMBA_PHASE(PH_PCG_POINTS); launch_pcg_points(b, s_); }
+                            { SFMBA_PHASE(PH_PCG_IMAGES); launch_pcg_images(b, s_); }
+                            { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_); }
+                        }
+                        read_state();
+                        if (hs.pcg_done) break;
+                    }
+                    { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_finish(b, b.delta, s_); }
                 }
-                launch_backsub_update(b, b.delta, s_);
-                launch_cost(b, true, true, s_);
-                launch_accept(b, s_);
-                launch_commit(b, s_);
+                { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
+                { SFMBA_PHASE(PH_COST); launch_cost(b, true, true, s_); }
+                { SFMBA_PHASE(PH_LM); launch_accept(b, s_); launch_commit(b, s_); }
                 read_state();
                 if (hs.factor_failed) {
                     // LU fallback on the symmetrised system (lib.rs:1084-1092)
-                    launch_lu_factor(b, s_);
-                    launch_lu_solve(b, s_);
-                    launch_backsub_update(b, b.delta, s_);
-                    launch_cost(b, true, true, s_);
-                    launch_accept(b, s_);
-                    launch_commit(b, s_);
-                    launch_reject(b, s_);
+                    { SFMBA_PHASE(PH_LU); launch_lu_factor(b, s_); launch_lu_solve(b, s_); }
+                    { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
+                    { SFMBA_PHASE(PH_COST); launch_cost(b, true, true, s_); }
+                    { SFMBA_PHASE(PH_LM); launch_accept(b, s_); launch_commit(b, s_); launch_reject(b, s_); }
                     read_state();
                 }
                 if (hs.accepted) {
@@ -537,6 +625,7 @@ class Solver {
         read_state();
         out.final_cost = hs.cost;
         out.valid_obs = hs.valid_obs;
+        out.linear_iterations = hs.pcg_total;
         return out;
     }
 
@@ -593,9 +682,13 @@ int bundle_adjust_impl(const sfmba_problem *p, const sfmba_options *o, sfmba_res
         Context &ctx = context();
         cudaStream_t s = (device && stream) ? (cudaStream_t)stream : ctx.stream;
         Solver solver(ctx, s);
-        solver.setup(p, o, device, true);
+        {
+            PhaseScope ps(PH_SETUP, s);
+            solver.setup(p, o, device, true);
+        }
         SolveOutput out = solver.run(o);
         solver.copy_out(r, device);
+        profiler().resolve();
         r->initial_cost = out.initial_cost;
         r->final_cost = out.final_cost;
         r->iterations_run = out.iterations;
@@ -749,6 +842,34 @@ int sfmba_refine_intrinsics(const sfmba_problem *p, const sfmba_options *o, doub
 int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *windows,
                                 const sfmba_options *o, sfmba_result *results) {
     return guarded([&] { throw Error(SFMBA_ERR_UNSUPPORTED, "batched solve: not built yet"); });
+}
+
+int sfmba_profile_enable(int32_t on) {
+    return guarded([&] {
+        Profiler &p = profiler();
+        p.reset();
+        p.on = on != 0;
+        g_kernel_launches = 0;
+    });
+}
+
+int sfmba_profile_report(char *buf, int64_t len) {
+    return guarded([&] {
+        Profiler &p = profiler();
+        p.resolve();
+        std::string js = "{";
+        for (int k = 0; k < PH_COUNT; ++k) {
+            if (k) js += ",";
+            char tmp[160];
+            std::snprintf(tmp, sizeof(tmp), "\"%s\":{\"ms\":%.6f,\"launches\":%lld}", kPhaseNames[k], p.ms[k],
+                          p.launches[k]);
+            js += tmp;
+        }
+        js += ",\"kernel_launches\":" + std::to_string(g_kernel_launches) + "}";
+        if (!buf || len <= (int64_t)js.size())
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "profile buffer too small (need " + std::to_string(js.size() + 1) + ")");
+        std::memcpy(buf, js.c_str(), js.size() + 1);
+    });
 }
 
 const char *sfmba_last_error(void) { return g_last_error.c_str(); }

@@ -38,6 +38,8 @@ EXPORTED_SYMBOLS = (
     "sfmba_refine_intrinsics",
     "sfmba_bundle_adjust_batched",
     "sfmba_residuals_jacobians",
+    "sfmba_profile_enable",
+    "sfmba_profile_report",
     "sfmba_last_error",
     "sfmba_version",
 )
@@ -73,6 +75,8 @@ def load(path: str | None = None):
         L.sfmba_refine_intrinsics.argtypes = [vp, vp, vp]
         L.sfmba_bundle_adjust_batched.argtypes = [C.c_int32, vp, vp, vp]
         L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
+        L.sfmba_profile_enable.argtypes = [C.c_int32]
+        L.sfmba_profile_report.argtypes = [C.c_char_p, C.c_int64]
         L.sfmba_last_error.restype = C.c_char_p
         L.sfmba_version.restype = C.c_char_p
         _lib = L
@@ -185,6 +189,20 @@ def bundle_adjust_batched_arrays(problems, opts: SfmbaOptions | None = None, **k
         b.struct = res[k]
         out.append(Result(b))
     return out
+
+
+def profile_enable(on: bool = True) -> None:
+    """Per-phase CUDA-event timing of later solves on this thread (clears totals)."""
+    _check(load().sfmba_profile_enable(1 if on else 0))
+
+
+def profile_report() -> dict:
+    """{phase: {"ms": device milliseconds, "launches": count}} since profile_enable."""
+    import json
+
+    buf = C.create_string_buffer(8192)
+    _check(load().sfmba_profile_report(buf, len(buf)))
+    return json.loads(buf.value.decode())
 
 
 def version() -> str:

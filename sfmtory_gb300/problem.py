@@ -72,6 +72,17 @@ class Problem:
         )
         return replace(base, **changes) if changes else base
 
+    def block_width(self) -> int:
+        """Width D of the solver's per-image block: 6 pose columns plus the
+        widest free camera, rounded to the widths the kernels are built for."""
+        fc = np.zeros(self.num_cameras, bool)
+        if self.fixed_cameras is not None:
+            m = np.asarray(self.fixed_cameras, bool)[: self.num_cameras]
+            fc[: len(m)] = m
+        ks = [MODEL_DOF[m] for c, m in enumerate(self.camera_model) if not fc[c]]
+        k = max(ks) if ks else 0
+        return 6 if k == 0 else 9 if k <= 3 else 10 if k <= 4 else 11 if k <= 5 else 14
+
     def reduced_dim(self) -> int:
         """Size of the reduced camera system under the reference's slotting
         (crates/sfm-ba/src/lib.rs:753-776)."""

@@ -198,3 +198,44 @@ def test_shuffled_observation_order_same_result(oracle_lib):
     b = native.bundle_adjust_arrays(q, **kw)
     assert abs(a.final_cost - b.final_cost) <= 1e-9 * a.final_cost
     assert np.allclose(a.points, b.points, rtol=0, atol=1e-9)
+
+
+def test_pcg_fp64_matches_oracle(oracle_lib):
+    """Matrix-free PCG solved tightly follows the dense reference trajectory."""
+    p = scenes.ring16(seed=6, scale=0.1)
+    kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=50)
+    g = native.bundle_adjust_arrays(p, solver=abi.SOLVER_PCG, pcg_tolerance=1e-12, pcg_max_iterations=1000, **kw)
+    r = oracle_lib.bundle_adjust(p, **kw)
+    assert g.solver_used == abi.SOLVER_PCG and g.linear_iterations > 0
+    assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost
+    assert abs(g.initial_cost - r.initial_cost) <= 1e-12 * r.initial_cost
+
+
+def test_pcg_mixed_radial_reaches_oracle_cost(oracle_lib):
+    """FP32 PCG on a scaled-down power-law RADIAL scene reaches the FP64
+    oracle's final cost to 1e-6 relative."""
+    p = scenes.radial2000(seed=1, scale=0.002)
+    kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=50)
+    r = oracle_lib.bundle_adjust(p, **kw)
+    g = native.bundle_adjust_arrays(p, solver=abi.SOLVER_PCG, precision=abi.PRECISION_MIXED,
+                                    pcg_tolerance=1e-6, pcg_max_iterations=200, **kw)
+    assert g.final_cost <= r.final_cost * (1 + 1e-6)
+    g64 = native.bundle_adjust_arrays(p, solver=abi.SOLVER_PCG, pcg_tolerance=1e-8, pcg_max_iterations=400, **kw)
+    assert abs(g64.final_cost - r.final_cost) <= 1e-6 * r.final_cost
+
+
+def test_pcg_rejects_shared_free_camera():
+    p = scenes.shared_focal_fixture().copy(fixed_cameras=np.array([False]))
+    with pytest.raises(native.SfmbaError) as e:
+        native.bundle_adjust_arrays(p, solver=abi.SOLVER_PCG)
+    assert e.value.status == 5
+
+
+def test_profile_report_counts_phases():
+    p = scenes.ring16(seed=7, scale=0.05)
+    native.profile_enable(True)
+    native.bundle_adjust_arrays(p, robust_loss=abi.LOSS_NONE, max_iterations=3)
+    rep = native.profile_report()
+    native.profile_enable(False)
+    assert rep["linearize"]["launches"] >= 1 and rep["cholesky"]["ms"] > 0
+    assert rep["kernel_launches"] > 10
