@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--max-iterations", type=int, default=50)
-    ap.add_argument("--pcg-tol", type=float, default=1e-6)
+    ap.add_argument("--pcg-tol", type=float, default=0.1)
     ap.add_argument("--pcg-max", type=int, default=100)
     ap.add_argument("--skip-fp64", action="store_true", help="skip the FP64 comparison solves")
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU-baseline sample")

@@ -102,7 +102,7 @@ typedef struct sfmba_options {
     int32_t precision;            /* sfmba_precision   */
     int32_t solver;               /* sfmba_solver      */
     int32_t pcg_max_iterations;   /* per damping retry (PCG solver)            */
-    double pcg_tolerance;         /* relative preconditioned-residual target   */
+    double pcg_tolerance;         /* stop PCG at |r| <= tol |b| (default 0.1)  */
     int32_t refinement_steps;     /* FP64 iterative-refinement steps (dense)   */
     double target_cost;           /* > 0: also stop once cost <= target_cost   */
     int32_t dense_max_dim;        /* AUTO picks dense up to this reduced dim   */

@@ -103,7 +103,7 @@ def default_options(**overrides) -> SfmbaOptions:
     o.precision = PRECISION_FP64
     o.solver = SOLVER_AUTO
     o.pcg_max_iterations = 100
-    o.pcg_tolerance = 1e-6
+    o.pcg_tolerance = 0.1
     o.refinement_steps = 1
     o.target_cost = 0.0
     o.dense_max_dim = 6000

@@ -214,88 +214,239 @@ __global__ void k_pcg_scalar_init(const double *part, int nI, double tol2, LMSta
     }
 }
 
-// Point pass: u_p = C_p^-1 sum_o Jx~_o^T (Jc~_o p_img(o)).
+// Jx~ (2x3) and Jc~ (2xD) of observation o, read with 16-byte vector loads.
 template <typename T, int D>
-__global__ void __launch_bounds__(128) k_pcg_points(const T *rec, const int *pt_start, const int *ob_img,
-                                                    const T *pt_Cinv, const unsigned char *pt_ok,
-                                                    const T *p, const LMState *st, int nP, T *u) {
+__device__ __forceinline__ void load_jac(const T *__restrict__ rec, long long o, T jx[6], T jc[2 * D]) {
     constexpr int RS = RecLayout<D>::kStride;
+    constexpr int NV = 8 + 2 * D;  // elements [0, NV) cover r~, Jx~, Jc~
+    T v[(NV + 3) / 4 * 4];
+    if constexpr (std::is_same<T, float>::value) {
+        const float4 *q = reinterpret_cast<const float4 *>(rec + (size_t)o * RS);
+#pragma unroll
+        for (int k = 0; k < (NV + 3) / 4; ++k) {
+            const float4 t = __ldg(q + k);
+            v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
+        }
+    } else {
+        const double2 *q = reinterpret_cast<const double2 *>(rec + (size_t)o * RS);
+#pragma unroll
+        for (int k = 0; k < (NV + 1) / 2; ++k) {
+            const double2 t = __ldg(q + k);
+            v[2 * k] = t.x; v[2 * k + 1] = t.y;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) jx[k] = v[2 + k];
+#pragma unroll
+    for (int k = 0; k < 2 * D; ++k) jc[k] = v[8 + k];
+}
+
+// Point pass over point-aligned chunks of kChunkObs observations, one warp
+// per chunk: each lane takes one observation, contributions
+// Jx~^T (Jc~ p_img) are summed per point by a segmented warp scan (a point's
+// observations are contiguous and never straddle chunks; the running sum is
+// carried across the chunk's 32-observation rounds), and the lane ending a
+// point writes u_p = C_p^-1 t_p. No atomics; a track of 200 observations
+// costs its own lanes, not a whole warp's.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_pcg_points(const T *__restrict__ rec, const int *__restrict__ ob_pt,
+                                                    const int *__restrict__ ob_img, const int *__restrict__ pchunk,
+                                                    int nchunks, const T *__restrict__ pt_Cinv,
+                                                    const unsigned char *__restrict__ pt_ok, const T *__restrict__ p,
+                                                    const LMState *__restrict__ st, T *__restrict__ u) {
     if (st->pcg_done) return;
-    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pt >= nP) return;
-    T t0 = 0, t1 = 0, t2 = 0;
-    if (pt_ok[pt]) {
-        for (int o = pt_start[pt]; o < pt_start[pt + 1]; ++o) {
-            const T *r = rec + (size_t)o * RS;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nchunks) return;
+    const int cs = pchunk[warp], ce = pchunk[warp + 1];
+    T carry0 = 0, carry1 = 0, carry2 = 0;
+    int carry_pt = -1;
+    for (int base = cs; base < ce; base += 32) {
+        const int o = base + lane;
+        const bool valid = o < ce;
+        const int pt = valid ? ob_pt[o] : -1;
+        T c0 = 0, c1 = 0, c2 = 0;
+        if (valid) {
+            T jx[6], jc[2 * D];
+            load_jac<T, D>(rec, o, jx, jc);
             const T *pv = p + (size_t)ob_img[o] * D;
             T s0 = 0, s1 = 0;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 const T v = pv[c];
-                s0 += r[8 + c] * v;
-                s1 += r[8 + D + c] * v;
+                s0 += jc[c] * v;
+                s1 += jc[D + c] * v;
             }
-            t0 += r[2] * s0 + r[5] * s1;
-            t1 += r[3] * s0 + r[6] * s1;
-            t2 += r[4] * s0 + r[7] * s1;
+            c0 = jx[0] * s0 + jx[3] * s1;
+            c1 = jx[1] * s0 + jx[4] * s1;
+            c2 = jx[2] * s0 + jx[5] * s1;
+            if (lane == 0 && pt == carry_pt) { c0 += carry0; c1 += carry1; c2 += carry2; }
         }
-        const T *Ci = pt_Cinv + 6 * (size_t)pt;
-        const T u0 = Ci[0] * t0 + Ci[1] * t1 + Ci[2] * t2;
-        const T u1 = Ci[1] * t0 + Ci[3] * t1 + Ci[4] * t2;
-        const T u2 = Ci[2] * t0 + Ci[4] * t1 + Ci[5] * t2;
-        t0 = u0; t1 = u1; t2 = u2;
+        const int prev = __shfl_up_sync(0xffffffffu, pt, 1);
+        bool head = lane == 0 || pt != prev;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const T a0 = __shfl_up_sync(0xffffffffu, c0, off);
+            const T a1 = __shfl_up_sync(0xffffffffu, c1, off);
+            const T a2 = __shfl_up_sync(0xffffffffu, c2, off);
+            const bool hf = __shfl_up_sync(0xffffffffu, head, off);
+            if (lane >= off) {
+                if (!head) { c0 += a0; c1 += a1; c2 += a2; }
+                head = head || hf;
+            }
+        }
+        int next = __shfl_down_sync(0xffffffffu, pt, 1);
+        if (lane == 31) next = (o + 1 < ce) ? ob_pt[o + 1] : -1;
+        const bool tail = valid && next != pt;
+        if (tail) {
+            T u0 = 0, u1 = 0, u2 = 0;
+            if (pt_ok[pt]) {
+                const T *Ci = pt_Cinv + 6 * (size_t)pt;
+                u0 = Ci[0] * c0 + Ci[1] * c1 + Ci[2] * c2;
+                u1 = Ci[1] * c0 + Ci[3] * c1 + Ci[4] * c2;
+                u2 = Ci[2] * c0 + Ci[4] * c1 + Ci[5] * c2;
+            }
+            T *uo = u + 4 * (size_t)pt;
+            uo[0] = u0; uo[1] = u1; uo[2] = u2;
+        }
+        const bool cont = valid && !tail;  // segment continues into the next round (lane 31 only matters)
+        carry0 = __shfl_sync(0xffffffffu, c0, 31);
+        carry1 = __shfl_sync(0xffffffffu, c1, 31);
+        carry2 = __shfl_sync(0xffffffffu, c2, 31);
+        carry_pt = __shfl_sync(0xffffffffu, cont ? pt : -1, 31);
     }
-    T *uo = u + 4 * (size_t)pt;
-    uo[0] = t0; uo[1] = t1; uo[2] = t2; uo[3] = T(0);
 }
 
-// Image pass: q_i = (H_i + lambda diag H_i) p_i - sum_o Jc~^T (Jx~ u_p); part[i] = p_i . q_i.
+// Image pass over fixed chunks of kChunkObs image-major observations, one
+// warp per chunk: lanes accumulate Jc~^T (Jx~ u_p) for the chunk's current
+// image; at an image change the warp reduces and writes one partial sum for
+// (chunk, image). A second kernel adds an image's partials (deterministic,
+// no atomics).
 template <typename T, int D>
-__global__ void __launch_bounds__(128) k_pcg_images(const T *rec, const int *img_start, const int *img_obs,
-                                                    const int *ob_pt, const T *u, const double *img_H,
-                                                    const int *img_active, const T *p, const LMState *st,
-                                                    int nI, T *q, double *part) {
-    constexpr int RS = RecLayout<D>::kStride;
+__global__ void __launch_bounds__(256) k_pcg_images(const T *__restrict__ rec, const int *__restrict__ img_obs,
+                                                    const int *__restrict__ isort_img,
+                                                    const int *__restrict__ isort_pt, long long nO,
+                                                    const int *__restrict__ img_start,
+                                                    const int *__restrict__ ipart_off, const T *__restrict__ u,
+                                                    const LMState *__restrict__ st, T *__restrict__ ipart) {
+    if (st->pcg_done) return;
+    const long long chunk = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long cs = chunk * kChunkObs;
+    if (cs >= nO) return;
+    const long long ce = cs + kChunkObs < nO ? cs + kChunkObs : nO;
+    T acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = T(0);
+    int cur = isort_img[cs];
+    auto flush = [&](int img) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            T v = acc[c];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            acc[c] = v;
+        }
+        if (lane == 0) {
+            const int slot = ipart_off[img] + (int)(chunk - img_start[img] / kChunkObs);
+            T *dst = ipart + (size_t)slot * D;
+#pragma unroll
+            for (int c = 0; c < D; ++c) dst[c] = acc[c];
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] = T(0);
+    };
+    for (long long base = cs; base < ce; base += 32) {
+        const long long k = base + lane;
+        const bool valid = k < ce;
+        const int img = valid ? isort_img[k] : 0x7fffffff;
+        T cv[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) cv[c] = T(0);
+        if (valid) {
+            const int o = img_obs[k];
+            const float4 *up4 = nullptr;
+            T u0, u1, u2;
+            if constexpr (std::is_same<T, float>::value) {
+                up4 = reinterpret_cast<const float4 *>(u) + isort_pt[k];
+                const float4 t = __ldg(up4);
+                u0 = t.x; u1 = t.y; u2 = t.z;
+            } else {
+                const T *up = u + 4 * (size_t)isort_pt[k];
+                u0 = up[0]; u1 = up[1]; u2 = up[2];
+            }
+            T jx[6], jc[2 * D];
+            load_jac<T, D>(rec, o, jx, jc);
+            const T z0 = jx[0] * u0 + jx[1] * u1 + jx[2] * u2;
+            const T z1 = jx[3] * u0 + jx[4] * u1 + jx[5] * u2;
+#pragma unroll
+            for (int c = 0; c < D; ++c) cv[c] = jc[c] * z0 + jc[D + c] * z1;
+        }
+        while (true) {
+            if (valid && img == cur) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) acc[c] += cv[c];
+            }
+            const unsigned rest = __ballot_sync(0xffffffffu, valid && img > cur);
+            if (!rest) break;
+            flush(cur);
+            cur = __shfl_sync(0xffffffffu, img, __ffs(rest) - 1);
+        }
+    }
+    flush(cur);
+}
+
+// q_i = (H_i + lambda diag H_i) p_i - sum of the image's partials; part[i] = p_i . q_i.
+template <typename T, int D>
+__global__ void __launch_bounds__(128) k_pcg_images_finish(const T *__restrict__ ipart,
+                                                           const int *__restrict__ ipart_off,
+                                                           const double *__restrict__ img_H,
+                                                           const int *__restrict__ img_active,
+                                                           const T *__restrict__ p, const LMState *__restrict__ st,
+                                                           int nI, T *__restrict__ q, double *__restrict__ part) {
     if (st->pcg_done) return;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= nI) return;
-    T acc[D], comp[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) acc[c] = comp[c] = T(0);
-    const int s = img_start[i], e = img_start[i + 1];
-    for (int k = s + lane; k < e; k += 32) {
-        const int o = img_obs[k];
-        const T *r = rec + (size_t)o * RS;
-        const T *up = u + 4 * (size_t)ob_pt[o];
-        const T u0 = up[0], u1 = up[1], u2 = up[2];
-        const T z0 = r[2] * u0 + r[3] * u1 + r[4] * u2;
-        const T z1 = r[5] * u0 + r[6] * u1 + r[7] * u2;
-#pragma unroll
-        for (int c = 0; c < D; ++c) kahan_add(acc[c], comp[c], r[8 + c] * z0 + r[8 + D + c] * z1);
-    }
     const double lam = st->lambda;
     const int act = img_active[i];
     const double *H = img_H + (size_t)i * D * D;
     const T *pv = p + (size_t)i * D;
     double pq = 0.0;
+    if (lane < D) {
+        const int c = lane;
+        double sch = 0.0;
+        for (int k = ipart_off[i]; k < ipart_off[i + 1]; ++k) sch += (double)ipart[(size_t)k * D + c];
+        double hp = 0.0;
 #pragma unroll
-    for (int c = 0; c < D; ++c) {
-        double v = (double)acc[c] - (double)comp[c];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == c) {
-            double hp = 0.0;
-            for (int d = 0; d < D; ++d) hp += H[c * D + d] * (double)pv[d];
-            hp += lam * H[c * D + c] * (double)pv[c];
-            const double qc = ((act >> c) & 1) ? hp - v : 0.0;
-            q[(size_t)i * D + c] = (T)qc;
-            pq = (double)pv[c] * (double)(T)qc;
-        }
+        for (int d = 0; d < D; ++d) hp += H[c * D + d] * (double)pv[d];
+        hp += lam * H[c * D + c] * (double)pv[c];
+        const double qc = ((act >> c) & 1) ? hp - sch : 0.0;
+        q[(size_t)i * D + c] = (T)qc;
+        pq = (double)pv[c] * (double)(T)qc;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
     if (lane == 0) part[i] = pq;
+}
+
+__global__ void k_point_chunks(const int *pt_start, int nP, long long nO, int nchunks, int *pchunk) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > nchunks) return;
+    long long t = (long long)k * kChunkObs;
+    if (t > nO) t = nO;
+    int lo = 0, hi = nP;  // first point whose start is >= t (pt_start[nP] == nO)
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (pt_start[mid] < t) lo = mid + 1;
+        else hi = mid;
+    }
+    pchunk[k] = k == nchunks ? (int)nO : pt_start[lo];
+}
+
+__global__ void k_isort_pt(const int *img_obs, const int *ob_pt, long long nO, int *isort_pt) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k < nO) isort_pt[k] = ob_pt[img_obs[k]];
 }
 
 __global__ void k_pcg_scalar_alpha(const double *part, int nI, LMState *st) {
@@ -417,19 +568,25 @@ void setup_t(const Bufs &b, cudaStream_t s) {
 
 template <typename T, int D>
 void points_t(const Bufs &b, cudaStream_t s) {
-    if (b.nP == 0) return;
-    k_pcg_points<T, D><<<div_up(b.nP, 128), 128, 0, s>>>((const T *)b.rec, b.pt_start, b.ob_img,
-                                                         (const T *)b.pt_Cinv, b.pt_ok, (const T *)b.pcg_p,
-                                                         b.state, b.nP, (T *)b.pcg_u);
+    if (b.nP == 0 || b.npchunks == 0) return;
+    k_pcg_points<T, D><<<div_up((long long)b.npchunks * 32, 256), 256, 0, s>>>(
+        (const T *)b.rec, b.ob_pt, b.ob_img, b.pchunk, b.npchunks, (const T *)b.pt_Cinv, b.pt_ok,
+        (const T *)b.pcg_p, b.state, (T *)b.pcg_u);
     SFMBA_LAUNCH_CHECK();
 }
 
 template <typename T, int D>
 void images_t(const Bufs &b, cudaStream_t s) {
-    k_pcg_images<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.rec, b.img_start, b.img_obs, b.ob_pt,
-                                                       (const T *)b.pcg_u, b.img_H, b.img_active,
-                                                       (const T *)b.pcg_p, b.state, b.nI, (T *)b.pcg_q,
-                                                       b.pcg_part);
+    if (b.nO > 0) {
+        const long long chunks = (b.nO + kChunkObs - 1) / kChunkObs;
+        k_pcg_images<T, D><<<div_up(chunks * 32, 256), 256, 0, s>>>(
+            (const T *)b.rec, b.img_obs, b.isort_img, b.isort_pt, b.nO, b.img_start, b.ipart_off,
+            (const T *)b.pcg_u, b.state, (T *)b.ipart);
+        SFMBA_LAUNCH_CHECK();
+    }
+    k_pcg_images_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart, b.ipart_off, b.img_H,
+                                                              b.img_active, (const T *)b.pcg_p, b.state, b.nI,
+                                                              (T *)b.pcg_q, b.pcg_part);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -469,6 +626,18 @@ SFMBA_PCG_LAUNCHER(launch_pcg_points, points_t)
 SFMBA_PCG_LAUNCHER(launch_pcg_images, images_t)
 SFMBA_PCG_LAUNCHER(launch_pcg_vector, vector_t)
 #undef SFMBA_PCG_LAUNCHER
+
+void launch_pcg_partition(Bufs &b, const int *img_keys_sorted, cudaStream_t s) {
+    b.npchunks = (int)((b.nO + kChunkObs - 1) / kChunkObs);
+    k_point_chunks<<<div_up(b.npchunks + 1, 256), 256, 0, s>>>(b.pt_start, b.nP, b.nO, b.npchunks, b.pchunk);
+    SFMBA_LAUNCH_CHECK();
+    if (b.nO > 0) {
+        SFMBA_CUDA(cudaMemcpyAsync(b.isort_img, img_keys_sorted, sizeof(int) * (size_t)b.nO,
+                                   cudaMemcpyDeviceToDevice, s));
+        k_isort_pt<<<div_up(b.nO, 256), 256, 0, s>>>(b.img_obs, b.ob_pt, b.nO, b.isort_pt);
+        SFMBA_LAUNCH_CHECK();
+    }
+}
 
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s) {
     if (b.n == 0) return;

@@ -75,11 +75,20 @@ struct Bufs {
     void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
     double *pcg_part = nullptr;   // [3*nI] per-image partial dot products
     double pcg_tol = 1e-6;
+    // Work partition of the matrix-free passes (fixed-size observation chunks).
+    int *pchunk = nullptr;        // [npchunks+1] point-aligned chunk starts (point-major order)
+    int npchunks = 0;
+    int *isort_img = nullptr;     // [nO] image of the k-th image-major observation
+    int *isort_pt = nullptr;      // [nO] point of the k-th image-major observation
+    int *ipart_off = nullptr;     // [nI+1] first partial slot of each image
+    void *ipart = nullptr;        // [nparts*D] per-(chunk, image) partial sums
+    int nparts = 0;
 };
 
 constexpr int kCostBlocks = 1024;
 constexpr int kDotSlots = 16;
 constexpr int kCholNB = 64;
+constexpr int kChunkObs = 256;  // observations per warp in the matrix-free passes
 
 // Inputs/outputs of the per-observation Jacobian probe (original order).
 struct JacProbe {
@@ -145,6 +154,8 @@ void launch_pcg_setup(const Bufs &b, cudaStream_t s);
 void launch_pcg_points(const Bufs &b, cudaStream_t s);
 void launch_pcg_images(const Bufs &b, cudaStream_t s);
 void launch_pcg_vector(const Bufs &b, cudaStream_t s);
+// Work partition of the matrix-free passes (after sort_observations).
+void launch_pcg_partition(Bufs &b, const int *img_keys_sorted, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
 

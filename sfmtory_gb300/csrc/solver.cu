@@ -395,7 +395,7 @@ class Solver {
             b = Bufs();
             b.nI = nI; b.nC = nC; b.nP = nP; b.nO = nO; b.n = n; b.D = D; b.nID = nID;
             b.mixed = mixed; b.loss = o->robust_loss; b.loss_scale = o->loss_scale_px;
-            b.pcg_tol = o->pcg_tolerance > 0.0 ? o->pcg_tolerance : 1e-6;
+            b.pcg_tol = o->pcg_tolerance > 0.0 ? o->pcg_tolerance : 0.1;
             b.cam_model = A.take<int>(nC);
             b.cam_of_img = A.take<int>(nI);
             b.cams = A.take<double>((size_t)nC * 8);
@@ -465,6 +465,12 @@ class Solver {
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
                     b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
                     b.pcg_part = A.take<double>((size_t)3 * nI);
+                    const long long nchunks = (nO + kChunkObs - 1) / kChunkObs;
+                    b.pchunk = A.take<int>((size_t)nchunks + 1);
+                    b.isort_img = A.take<int>(nO);
+                    b.isort_pt = A.take<int>(nO);
+                    b.ipart_off = A.take<int>((size_t)nI + 1);
+                    b.ipart = A.take<char>((size_t)(nI + nchunks + 1) * D * tsz);
                 }
             }
             sort_temp = A.take<char>(sort_tmp);
@@ -505,6 +511,18 @@ class Solver {
         put_vec(b.slot_masked, lay_.slot_masked, s_);
         sort_observations(src_pt, src_img, src_xy, nO, nP, nI, b, sort_temp, sort_tmp, k1, v1, k2, v2, s_);
         SFMBA_CUDA(cudaMemsetAsync(b.state, 0, sizeof(LMState), s_));
+        if (need_system && solver_ == SFMBA_SOLVER_PCG) {
+            launch_pcg_partition(b, k2, s_);
+            // Partial-sum slots of the image pass: one per (chunk, image) overlap.
+            std::vector<int> img_start = fetch(b.img_start, (size_t)nI + 1, true, s_);
+            std::vector<int> off(nI + 1, 0);
+            for (int i = 0; i < nI; ++i) {
+                const int a = img_start[i], e = img_start[i + 1];
+                off[i + 1] = off[i] + (e > a ? (e - 1) / kChunkObs - a / kChunkObs + 1 : 0);
+            }
+            b.nparts = off[nI];
+            put_vec(b.ipart_off, off, s_);
+        }
         if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
             size_t scan_need = 0;
             // pair count scan uses the sort temp (cub scan needs little)
@@ -720,7 +738,7 @@ void sfmba_default_options(sfmba_options *o) {
     o->precision = SFMBA_PRECISION_FP64;
     o->solver = SFMBA_SOLVER_AUTO;
     o->pcg_max_iterations = 100;
-    o->pcg_tolerance = 1e-6;
+    o->pcg_tolerance = 0.1;
     o->refinement_steps = 1;
     o->target_cost = 0.0;
     o->dense_max_dim = 6000;

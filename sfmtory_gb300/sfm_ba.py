@@ -156,7 +156,7 @@ class BaParams:
     precision: int = abi.PRECISION_FP64
     solver: int = abi.SOLVER_AUTO
     pcg_max_iterations: int = 100
-    pcg_tolerance: float = 1e-6
+    pcg_tolerance: float = 0.1
     refinement_steps: int = 1
     target_cost: float = 0.0
 
