@@ -82,7 +82,7 @@ def workload_config(args, p):
         "max_lm_iterations": args.max_iterations,
         "seed": args.seed,
         "scale": args.scale,
-        "l2": "inputs larger than L2 (observation arrays + per-observation Jacobian records > 129 MB)",
+        "l2": "inputs larger than L2: observation arrays (index, pixel) and points, 5.96M x 24 B + 1M x 40 B",
     }
 
 
@@ -265,33 +265,37 @@ def e2e_solve(L, pp, opts):
 
 # -------------------------------------------------------------- roofline
 
-def algorithmic_bytes(phase, nO, nP, nI, D, t):
+def algorithmic_bytes(phase, nO, nP, nI, D, t, recompute):
     """Compulsory bytes one launch of the phase's kernel moves (each array
-    touched once; per-observation Jacobian records read without padding)."""
-    jac = (6 + 2 * D) * t          # Jx~ (2x3) and Jc~ (2xD) of one observation
-    if phase == "pcg_images":     # q = (H + lam diag H) p - sum Jc~^T (Jx~ u)
+    touched once). With ``recompute`` (the FP32 path) the Jacobian of an
+    observation is rebuilt from its pixel, point and image constants, so an
+    observation costs 16 bytes of input instead of a stored record."""
+    img_const = 24 * t + 16       # rotation, translation, camera, model/mask words
+    nchunks = (nO + 255) // 256
+    if recompute:
+        if phase == "pcg_points":  # u_p = C^-1 sum Jx~^T (Jc~ p)
+            return nO * 16 + nP * (16 + 6 * t + 1 + 3 * t) + nI * (img_const + D * t) + nchunks * 4
+        if phase == "pcg_images":  # partials of sum Jc~^T (Jx~ u)
+            return nO * 16 + nP * (16 + 3 * t) + nI * img_const + (nI + nchunks) * D * t
+        return None
+    jac = (6 + 2 * D) * t          # Jx~ (2x3) and Jc~ (2xD) of one stored record
+    if phase == "pcg_images":
         return nO * (4 + 4 + jac + 3 * t) + nI * (D * D * 8 + 2 * D * t + 8 + 4 + 8)
-    if phase == "pcg_points":     # u_p = C^-1 sum Jx~^T (Jc~ p)
+    if phase == "pcg_points":
         return nO * (4 + jac) + nP * (8 + 6 * t + 1 + 3 * t) + nI * D * t
-    if phase == "linearize":      # residual + adjoint Jacobian records
-        return nO * (4 + 4 + 16 + (8 + 2 * D) * t + 1) + nP * (16 if t == 4 else 24) + nI * (24 * t + 16)
-    if phase == "image_reduce":
-        return nO * (4 + (2 + 2 * D) * t) + nI * (D * D * 8 + D * 8 + 8)
-    if phase == "cost":
-        return nO * (4 + 4 + 16) + nP * 24 + nI * 56
     return None
 
 
-def roofline(profile, p, D, t, peaks):
+def roofline(profile, p, D, t, peaks, recompute=True):
     phases = {k: v for k, v in profile.items() if isinstance(v, dict) and v.get("launches")}
     top = max(phases, key=lambda k: phases[k]["ms"])
     order = sorted(phases, key=lambda k: -phases[k]["ms"])
     for name in order:  # the heaviest phase with a one-kernel byte model
-        if algorithmic_bytes(name, p.num_observations, p.num_points, p.num_images, D, t) is not None:
+        if algorithmic_bytes(name, p.num_observations, p.num_points, p.num_images, D, t, recompute) is not None:
             top = name
             break
     ms_per = phases[top]["ms"] / phases[top]["launches"]
-    by = algorithmic_bytes(top, p.num_observations, p.num_points, p.num_images, D, t)
+    by = algorithmic_bytes(top, p.num_observations, p.num_points, p.num_images, D, t, recompute)
     peak = peaks.get("hbm_gbs")
     achieved = by / (ms_per * 1e-3) / 1e9
     return {
@@ -299,6 +303,8 @@ def roofline(profile, p, D, t, peaks):
         "frac": round(achieved / peak, 4) if peak else None, "traffic": None,
         "algorithmic_bytes_per_launch": int(by), "avg_launch_ms": round(ms_per, 4),
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peak else "fallback",
+        "byte_model": "recomputed Jacobians: 16 B/observation + per-point/per-image terms" if recompute
+                      else "stored Jacobian records",
     }
 
 

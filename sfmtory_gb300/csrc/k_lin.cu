@@ -657,6 +657,10 @@ void launch_backsub_update(const Bufs &b, const double *delta_slot, cudaStream_t
         });
         SFMBA_LAUNCH_CHECK();
     }
+    launch_update_images(b, delta_slot, s);
+}
+
+void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t s) {
     const int m = b.nI > b.nC ? b.nI : b.nC;
     if (m > 0) {
         k_update_images<<<div_up(m, 128), 128, 0, s>>>(b.poses, b.cams, b.pose_slot, b.cam_slot,

@@ -82,7 +82,10 @@ struct Bufs {
     int *isort_pt = nullptr;      // [nO] point of the k-th image-major observation
     int *ipart_off = nullptr;     // [nI+1] first partial slot of each image
     void *ipart = nullptr;        // [nparts*D] per-(chunk, image) partial sums
+    void *ipart2 = nullptr;       // [nparts*(D(D+1)/2+D)] block partials of the image passes
     int nparts = 0;
+    float2 *ob_xy32 = nullptr;    // [nO] point-major pixels (FP32 recompute)
+    float2 *isort_xy32 = nullptr; // [nO] image-major pixels (FP32 recompute)
 };
 
 constexpr int kCostBlocks = 1024;
@@ -124,6 +127,7 @@ void launch_point_inverse(const Bufs &b, cudaStream_t s);
 void launch_image_rhs(const Bufs &b, cudaStream_t s);
 void launch_gather_delta(const Bufs &b, const double *delta_slot, cudaStream_t s);
 void launch_backsub_update(const Bufs &b, const double *delta_slot, cudaStream_t s);
+void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t s);
 // cost of (poses, cams, points) or of the trial buffers, into state->cost/trial_cost
 void launch_cost(const Bufs &b, bool trial, bool into_trial, cudaStream_t s);
 void launch_mean_error(const Bufs &b, cudaStream_t s);  // -> partials; host finalises
@@ -145,14 +149,21 @@ void launch_refine(const Bufs &b, cudaStream_t s);
 void launch_lu_factor(const Bufs &b, cudaStream_t s);
 void launch_lu_solve(const Bufs &b, cudaStream_t s);
 
-// ---- matrix-free Schur PCG (k_pcg.cu)
-// Preconditioner and start vectors (x = 0, r = rhs, p = z = M^-1 r).
-void launch_pcg_setup(const Bufs &b, cudaStream_t s);
-// One PCG iteration: q = S p (two passes), x/r update, z = M^-1 r, new p.
-// One PCG iteration in three launch groups: q = S p is the point pass then
-// the image pass; the vector group updates x, r, z = M^-1 r and p.
-void launch_pcg_points(const Bufs &b, cudaStream_t s);
-void launch_pcg_images(const Bufs &b, cudaStream_t s);
+// ---- matrix-free observation passes (k_matfree.cu)
+void launch_mf_prepare(const Bufs &b, cudaStream_t s);          // FP32 pixel copies
+void launch_mf_point_reduce(const Bufs &b, cudaStream_t s);     // C_p, g_p, free count
+void launch_mf_image_blocks(const Bufs &b, cudaStream_t s);     // H_i, b_i
+void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PCG start vectors
+void launch_mf_points(const Bufs &b, cudaStream_t s);           // u = C^-1 E^T p
+void launch_mf_images(const Bufs &b, cudaStream_t s);           // partials of E u
+void launch_mf_backsub(const Bufs &b, const double *delta_slot, cudaStream_t s);
+
+// ---- matrix-free Schur PCG, vector side (k_pcg.cu)
+// Scalars of a new solve (after launch_mf_precond).
+void launch_pcg_start(const Bufs &b, cudaStream_t s);
+// One PCG iteration is launch_mf_points, launch_mf_images, then
+// launch_pcg_images_finish (q = S p) and launch_pcg_vector (x, r, z, p).
+void launch_pcg_images_finish(const Bufs &b, cudaStream_t s);
 void launch_pcg_vector(const Bufs &b, cudaStream_t s);
 // Work partition of the matrix-free passes (after sort_observations).
 void launch_pcg_partition(Bufs &b, const int *img_keys_sorted, cudaStream_t s);

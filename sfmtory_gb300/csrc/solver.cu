@@ -108,7 +108,9 @@ struct PhaseScope {
         }
     }
 };
-#define SFMBA_PHASE(ph) PhaseScope phase_scope_##__LINE__(ph, s_)
+#define SFMBA_PHASE_CAT2(a, b) a##b
+#define SFMBA_PHASE_CAT(a, b) SFMBA_PHASE_CAT2(a, b)
+#define SFMBA_PHASE(ph) PhaseScope SFMBA_PHASE_CAT(phase_scope_, __LINE__)(ph, s_)
 
 // Bump allocator over one device allocation that grows on demand and is
 // kept across calls on the same thread.
@@ -429,8 +431,10 @@ class Solver {
                 in_xy = A.take<double>((size_t)nO * 2);
             }
             if (need_system) {
+                const bool records = solver_ == SFMBA_SOLVER_DENSE || !mixed;
+                const long long nchunks = (nO + kChunkObs - 1) / kChunkObs;
                 b.img_lin = A.take<char>((size_t)nI * (mixed ? sizeof(ImageLin<float>) : sizeof(ImageLin<double>)));
-                b.rec = A.take<char>((size_t)nO * RS * tsz);
+                b.rec = records ? A.take<char>((size_t)nO * RS * tsz) : nullptr;
                 b.ob_valid = A.take<unsigned char>(nO);
                 b.pt_C = A.take<char>((size_t)nP * 6 * tsz);
                 b.pt_g = A.take<char>((size_t)nP * 3 * tsz);
@@ -465,12 +469,16 @@ class Solver {
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
                     b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
                     b.pcg_part = A.take<double>((size_t)3 * nI);
-                    const long long nchunks = (nO + kChunkObs - 1) / kChunkObs;
                     b.pchunk = A.take<int>((size_t)nchunks + 1);
                     b.isort_img = A.take<int>(nO);
                     b.isort_pt = A.take<int>(nO);
                     b.ipart_off = A.take<int>((size_t)nI + 1);
                     b.ipart = A.take<char>((size_t)(nI + nchunks + 1) * D * tsz);
+                    b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * (D * (D + 1) / 2 + D) * tsz);
+                    if (mixed) {
+                        b.ob_xy32 = A.take<float2>(nO);
+                        b.isort_xy32 = A.take<float2>(nO);
+                    }
                 }
             }
             sort_temp = A.take<char>(sort_tmp);
@@ -522,6 +530,7 @@ class Solver {
             }
             b.nparts = off[nI];
             put_vec(b.ipart_off, off, s_);
+            launch_mf_prepare(b, s_);
         }
         if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
             size_t scan_need = 0;
@@ -580,9 +589,18 @@ class Solver {
         for (int outer = 0; outer < o->max_iterations; ++outer) {
             ++out.iterations;
             { SFMBA_PHASE(PH_LM); launch_begin_outer(b, s_); }
-            { SFMBA_PHASE(PH_LINEARIZE); launch_prepare_images(b, s_); launch_linearize(b, s_); }
-            { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
-            { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
+            {
+                SFMBA_PHASE(PH_LINEARIZE);
+                launch_prepare_images(b, s_);
+                if (b.rec) launch_linearize(b, s_);
+            }
+            if (solver_ == SFMBA_SOLVER_DENSE) {
+                { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
+                { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
+            } else {
+                { SFMBA_PHASE(PH_POINT_REDUCE); launch_mf_point_reduce(b, s_); }
+                { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_mf_image_blocks(b, s_); }
+            }
             read_state();
             // lib.rs:855-857: no observation in front of its camera
             if (hs.valid_obs == 0) break;
@@ -591,8 +609,8 @@ class Solver {
                 ++out.retries;
                 { SFMBA_PHASE(PH_LM); launch_begin_retry(b, s_); }
                 { SFMBA_PHASE(PH_POINT_INVERSE); launch_point_inverse(b, s_); }
-                { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); }
                 if (solver_ == SFMBA_SOLVER_DENSE) {
+                    { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); }
                     { SFMBA_PHASE(PH_SCHUR); launch_schur_pairs(b, s_); }
                     { SFMBA_PHASE(PH_FOLD); launch_fold_system(b, s_); }
                     { SFMBA_PHASE(PH_CHOLESKY); launch_cholesky(b, s_); }
@@ -601,22 +619,23 @@ class Solver {
                         SFMBA_PHASE(PH_REFINE);
                         for (int k = 0; k < o->refinement_steps; ++k) launch_refine(b, s_);
                     }
+                    { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
                 } else {
-                    { SFMBA_PHASE(PH_PCG_PRECOND); launch_pcg_setup(b, s_); }
+                    { SFMBA_PHASE(PH_PCG_PRECOND); launch_mf_precond(b, s_); launch_pcg_start(b, s_); }
                     const int maxit = std::max(1, o->pcg_max_iterations);
                     for (int it = 0; it < maxit; it += kPcgPollEvery) {
                         const int m = std::min(kPcgPollEvery, maxit - it);
                         for (int k = 0; k < m; ++k) {
-                            { SFMBA_PHASE(PH_PCG_POINTS); launch_pcg_points(b, s_); }
-                            { SFMBA_PHASE(PH_PCG_IMAGES); launch_pcg_images(b, s_); }
+                            { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_); }
+                            { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_); launch_pcg_images_finish(b, s_); }
                             { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_); }
                         }
                         read_state();
                         if (hs.pcg_done) break;
                     }
                     { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_finish(b, b.delta, s_); }
+                    { SFMBA_PHASE(PH_BACKSUB); launch_mf_backsub(b, b.delta, s_); }
                 }
-                { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
                 { SFMBA_PHASE(PH_COST); launch_cost(b, true, true, s_); }
                 { SFMBA_PHASE(PH_LM); launch_accept(b, s_); launch_commit(b, s_); }
                 read_state();
