@@ -180,6 +180,22 @@ int sfmba_residuals_jacobians(const sfmba_problem *problem, int32_t precision, d
                               double *j_pose, double *j_point, double *j_camera,
                               uint8_t *valid);
 
+/* No counterpart in the reference. The robust cost of sfmba_total_cost for
+ * a problem whose arrays are all in device memory, computed without
+ * allocating any memory, for callers that cannot let a library allocate
+ * (a fixed per-component slice of the GPU, or a thread that must not pay
+ * for cudaFree's device-wide synchronisation). The result is written to
+ * `out_cost_device` (device memory) on `stream` (NULL: the default stream);
+ * the call returns once it is there. Scratch is a fixed 64 KB array inside
+ * the library, held on every device the library is used on until exit;
+ * at most SFMBA_NOALLOC_MAX_OBSERVATIONS observations (larger problems are
+ * rejected with SFMBA_ERR_INVALID_ARGUMENT). The first call on a device
+ * looks up the array's device address - make it before any stream capture.
+ * Calls share the array: calls that overlap on one GPU race. */
+#define SFMBA_NOALLOC_MAX_OBSERVATIONS 16777216
+int sfmba_total_cost_noalloc(const sfmba_problem *problem, const sfmba_options *options,
+                             double *out_cost_device, void *stream);
+
 /* Benchmarking aid (no counterpart in the reference): when enabled, every
  * kernel phase of the solves made on this thread is bracketed by CUDA events
  * on its launch stream. Enabling or disabling clears the totals. */

@@ -741,6 +741,9 @@ int bundle_adjust_impl(const sfmba_problem *p, const sfmba_options *o, sfmba_res
 
 }  // namespace
 
+// Sets the message sfmba_last_error() returns on this thread.
+void record_error(const char *message) { g_last_error = message; }
+
 }  // namespace sfmba
 
 using namespace sfmba;

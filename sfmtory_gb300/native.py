@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "sfmba_refine_intrinsics",
     "sfmba_bundle_adjust_batched",
     "sfmba_residuals_jacobians",
+    "sfmba_total_cost_noalloc",
     "sfmba_profile_enable",
     "sfmba_profile_report",
     "sfmba_last_error",
@@ -75,6 +76,7 @@ def load(path: str | None = None):
         L.sfmba_refine_intrinsics.argtypes = [vp, vp, vp]
         L.sfmba_bundle_adjust_batched.argtypes = [C.c_int32, vp, vp, vp]
         L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
+        L.sfmba_total_cost_noalloc.argtypes = [vp, vp, vp, vp]
         L.sfmba_profile_enable.argtypes = [C.c_int32]
         L.sfmba_profile_report.argtypes = [C.c_char_p, C.c_int64]
         L.sfmba_last_error.restype = C.c_char_p
