@@ -209,6 +209,62 @@ __device__ __forceinline__ bool linearize(const ImageLin<T> &im, T X0, T X1, T X
     return true;
 }
 
+// Compact linearisation of one observation: everything needed to apply its
+// Jacobian and transpose without forming them. With q = R X, the pixel-row
+// sensitivities d_row = d(pixel_row)/d(pc) and the camera-parameter rows
+// g_row (all weighted by sqrt(w)):
+//   pose rotation columns of row  = q x d_row, translation columns = d_row,
+//   point columns of row          = R^T d_row, camera columns = g_row.
+template <typename T, int D>
+struct LinCompact {
+    static constexpr int K = D > 6 ? D - 6 : 1;
+    T q[3];
+    T d[2][3];
+    T g[2][K];
+    T r[2];
+    bool pose_on;
+};
+
+template <typename T, int D>
+__device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T X1, T X2, T ox, T oy, int loss,
+                                                  T scale, LinCompact<T, D> &L) {
+    L.q[0] = im.R[0] * X0 + im.R[1] * X1 + im.R[2] * X2;
+    L.q[1] = im.R[3] * X0 + im.R[4] * X1 + im.R[5] * X2;
+    L.q[2] = im.R[6] * X0 + im.R[7] * X1 + im.R[8] * X2;
+    L.pose_on = im.active & 1;
+    const T pc0 = L.q[0] + im.t[0], pc1 = L.q[1] + im.t[1], pc2 = L.q[2] + im.t[2];
+    if (!(pc2 > T(kMinDepth))) {
+#pragma unroll
+        for (int row = 0; row < 2; ++row) {
+            L.r[row] = T(0);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) L.d[row][c] = T(0);
+#pragma unroll
+            for (int k = 0; k < LinCompact<T, D>::K; ++k) L.g[row][k] = T(0);
+        }
+        return false;
+    }
+    const T iz = T(1) / pc2;
+    const T xp = pc0 * iz, yp = pc1 * iz;
+    T u, v, A[2][2], G[2][8];
+    distort<T>(im.model, im.c, xp, yp, u, v, A, G);
+    const T r0 = u - ox, r1 = v - oy;
+    const T s = loss == SFMBA_LOSS_NONE ? T(1) : dev_sqrt<T>(robust_weight<T>(dev_sqrt<T>(r0 * r0 + r1 * r1), loss, scale));
+    L.r[0] = r0 * s;
+    L.r[1] = r1 * s;
+#pragma unroll
+    for (int row = 0; row < 2; ++row) {
+        const T a0 = A[row][0] * s, a1 = A[row][1] * s;
+        L.d[row][0] = a0 * iz;
+        L.d[row][1] = a1 * iz;
+        L.d[row][2] = -(a0 * xp + a1 * yp) * iz;
+#pragma unroll
+        for (int k = 0; k < LinCompact<T, D>::K; ++k)
+            L.g[row][k] = (D > 6 && ((im.active >> (6 + k)) & 1)) ? G[row][k] * s : T(0);
+    }
+    return true;
+}
+
 // FP64 residual exactly as the reference's cost evaluates it: quaternion
 // rotation (pose.rs:46-48) and project() with a true division by z.
 __device__ __forceinline__ bool residual64(const double *pose7, int model, const double *c,

@@ -83,7 +83,7 @@ struct LMState {
     long long trial_valid_obs;
     int pcg_iterations;  // iterations of the current solve
     int pcg_done;        // converged or broke down
-    double pcg_rz;       // r . z
+    double pcg_rzbuf[2]; // r . z, double-buffered by iteration parity
     double pcg_bb;       // |b|^2 of the current solve
     double pcg_rr;       // |r|^2
     double pcg_alpha;

@@ -27,11 +27,12 @@ __device__ __forceinline__ void seg_scan(T (&v)[N], bool head, int lane) {
     }
 }
 
-// Walks one point-aligned chunk: contrib(o, img, pt, v) fills the lane's N
-// values; consume(pt, v) runs on the lane holding a point's complete sum.
+// Walks one point-aligned chunk: contrib(o, rc, v) fills the lane's N
+// values from observation o with packed record rc = {image, point, x, y};
+// consume(pt, v) runs on the lane holding a point's complete sum.
 template <typename T, int N, typename Contrib, typename Consume>
-__device__ __forceinline__ void point_chunk(const int *__restrict__ ob_pt, const int *__restrict__ ob_img, int cs,
-                                            int ce, int lane, Contrib contrib, Consume consume) {
+__device__ __forceinline__ void point_chunk(const int4 *__restrict__ obrec, int cs, int ce, int lane,
+                                            Contrib contrib, Consume consume) {
     T carry[N];
 #pragma unroll
     for (int n = 0; n < N; ++n) carry[n] = T(0);
@@ -39,12 +40,14 @@ __device__ __forceinline__ void point_chunk(const int *__restrict__ ob_pt, const
     for (int base = cs; base < ce; base += 32) {
         const int o = base + lane;
         const bool valid = o < ce;
-        const int pt = valid ? ob_pt[o] : -1;
+        int4 rc = make_int4(0, -1, 0, 0);
+        if (valid) rc = __ldg(obrec + o);
+        const int pt = rc.y;
         T v[N];
 #pragma unroll
         for (int n = 0; n < N; ++n) v[n] = T(0);
         if (valid) {
-            contrib(o, ob_img[o], pt, v);
+            contrib(o, rc, v);
             if (lane == 0 && pt == carry_pt) {
 #pragma unroll
                 for (int n = 0; n < N; ++n) v[n] += carry[n];
@@ -53,7 +56,7 @@ __device__ __forceinline__ void point_chunk(const int *__restrict__ ob_pt, const
         const int prev = __shfl_up_sync(0xffffffffu, pt, 1);
         seg_scan<T, N>(v, lane == 0 || pt != prev, lane);
         int next = __shfl_down_sync(0xffffffffu, pt, 1);
-        if (lane == 31) next = (o + 1 < ce) ? ob_pt[o + 1] : -1;
+        if (lane == 31) next = (o + 1 < ce) ? __ldg(obrec + o + 1).y : -1;
         const bool tail = valid && next != pt;
         if (tail) consume(pt, v);
 #pragma unroll
@@ -73,16 +76,20 @@ __global__ void __launch_bounds__(256) k_mf_point_reduce(JacSrc<T> J, const unsi
     const int lane = threadIdx.x & 31;
     if (warp >= nchunks) return;
     point_chunk<T, 10>(
-        J.ob_pt, J.ob_img, pchunk[warp], pchunk[warp + 1], lane,
-        [&](int o, int img, int pt, T (&v)[10]) {
-            T rr[2], jx[6], jc[2 * D];
-            bool ok = jac_point_major<T, D, RC>(J, o, img, pt, rr, jx, jc);
+        J.obrec, pchunk[warp], pchunk[warp + 1], lane,
+        [&](int o, int4 rc, T (&v)[10]) {
+            ObsOp<T, D, RC> op;
+            make_op_point_major<T, D, RC>(J, o, rc, op);
+            bool ok = op.valid;
             if constexpr (!RC) ok = ob_valid[o] != 0;
+            T jx[6];
+            op.jx_rows(jx);
+            const T r0 = op.r(0), r1 = op.r(1);
             const T a0 = jx[0], a1 = jx[1], a2 = jx[2], b0 = jx[3], b1 = jx[4], b2 = jx[5];
             v[0] = a0 * a0 + b0 * b0; v[1] = a0 * a1 + b0 * b1; v[2] = a0 * a2 + b0 * b2;
             v[3] = a1 * a1 + b1 * b1; v[4] = a1 * a2 + b1 * b2; v[5] = a2 * a2 + b2 * b2;
-            v[6] = a0 * rr[0] + b0 * rr[1]; v[7] = a1 * rr[0] + b1 * rr[1]; v[8] = a2 * rr[0] + b2 * rr[1];
-            v[9] = (ok && img_free[img]) ? T(1) : T(0);
+            v[6] = a0 * r0 + b0 * r1; v[7] = a1 * r0 + b1 * r1; v[8] = a2 * r0 + b2 * r1;
+            v[9] = (ok && img_free[rc.x]) ? T(1) : T(0);
         },
         [&](int pt, const T (&v)[10]) {
             T *C = pt_C + 6 * (size_t)pt;
@@ -100,8 +107,7 @@ __global__ void __launch_bounds__(256) k_mf_point_reduce(JacSrc<T> J, const unsi
 //   MODE 0: W = I, v = r~                 -> H_i, b_i
 //   MODE 1: W = Jx~ C^-1 Jx~^T, v = Jx~ h -> Schur diagonal block, rhs term
 template <typename T, int D, bool RC, int MODE>
-__global__ void __launch_bounds__(128) k_mf_image_accum(JacSrc<T> J, const int *__restrict__ isort_img,
-                                                        const int *__restrict__ isort_pt, long long nO,
+__global__ void __launch_bounds__(128) k_mf_image_accum(JacSrc<T> J, long long nO,
                                                         const int *__restrict__ img_start,
                                                         const int *__restrict__ ipart_off,
                                                         const T *__restrict__ pt_Cinv, const T *__restrict__ pt_h,
@@ -137,7 +143,7 @@ __global__ void __launch_bounds__(128) k_mf_image_accum(JacSrc<T> J, const int *
     T acc[NE];
 #pragma unroll
     for (int j = 0; j < NE; ++j) acc[j] = T(0);
-    int cur = isort_img[cs];
+    int cur = __ldg(J.isrec + cs).x;
     auto flush = [&](int img) {
         T *dst = part + (size_t)partial_slot(ipart_off, img_start, img, chunk) * NV;
 #pragma unroll
@@ -150,18 +156,22 @@ __global__ void __launch_bounds__(128) k_mf_image_accum(JacSrc<T> J, const int *
     for (long long base = cs; base < ce; base += 32) {
         const long long k = base + lane;
         const bool valid = k < ce;
-        T rr[2] = {0, 0}, jx[6] = {0, 0, 0, 0, 0, 0}, jc[2 * D];
+        T jx[6] = {0, 0, 0, 0, 0, 0}, jc[2 * D];
 #pragma unroll
         for (int c = 0; c < 2 * D; ++c) jc[c] = T(0);
         T w00 = 0, w01 = 0, w11 = 0, v0 = 0, v1 = 0;
         int img = 0x7fffffff;
         if (valid) {
-            img = isort_img[k];
-            const int pt = isort_pt[k];
-            jac_image_major<T, D, RC>(J, k, img, pt, rr, jx, jc);
+            const int4 rc = __ldg(J.isrec + k);
+            img = rc.x;
+            const int pt = rc.y;
+            ObsOp<T, D, RC> op;
+            make_op_image_major<T, D, RC>(J, k, rc, op);
+            op.jc_rows(jc);
+            op.jx_rows(jx);
             if constexpr (MODE == 0) {
                 w00 = T(1); w11 = T(1);
-                v0 = rr[0]; v1 = rr[1];
+                v0 = op.r(0); v1 = op.r(1);
             } else if (pt_ok[pt]) {
                 const T *Ci = pt_Cinv + 6 * (size_t)pt;
                 T U[2][3];
@@ -241,6 +251,8 @@ __global__ void __launch_bounds__(128) k_mf_image_finish0(const T *__restrict__ 
 // Block-Jacobi preconditioner (exact image diagonal block of the Schur
 // complement, Cholesky-inverted), reduced rhs and the PCG start vectors
 // (x = 0, r = rhs, p = z = M^-1 r) of image i, from its MODE-1 partials.
+// One warp per image: warp-cooperative Cholesky, one lane per column of the
+// inverse with the triangular solves unrolled into registers.
 template <typename T, int D>
 __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__ part,
                                                            const int *__restrict__ ipart_off,
@@ -253,113 +265,124 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
                                                            T *__restrict__ p, double *__restrict__ dots) {
     constexpr int NH = D * (D + 1) / 2;
     constexpr int NV = NH + D;
-    __shared__ double sum[NV];
-    __shared__ double blk[D][D + 1];
-    __shared__ double Mi[D][D + 1];
-    __shared__ double rv[D];
-    __shared__ double dg[D];
-    __shared__ int fallback;
-    const int i = blockIdx.x;
+    constexpr int WPB = 4;
+    __shared__ double Ls[WPB][D][D + 1];
+    __shared__ double Ms[WPB][D][D + 1];
+    __shared__ double rvs[WPB][D];
+    __shared__ double invd_s[WPB][D];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * WPB + wl;
     if (i >= nI) return;
-    const int tid = threadIdx.x;
-    for (int e = tid; e < NV; e += blockDim.x) {
-        double s = 0.0;
-        for (int k = ipart_off[i]; k < ipart_off[i + 1]; ++k) s += (double)part[(size_t)k * NV + e];
-        sum[e] = s;
-    }
-    __syncthreads();
+    double(&L)[D][D + 1] = Ls[wl];
+    double(&Mi)[D][D + 1] = Ms[wl];
+    double *rv = rvs[wl];
+    double *invd = invd_s[wl];
     const double lam = st->lambda;
     const int act = img_active[i];
     const double *H = img_H + (size_t)i * D * D;
-    for (int e = tid; e < NH; e += blockDim.x) {
-        int t = e, a = 0;
-        while (t >= D - a) { t -= D - a; ++a; }
-        const int b = a + t;
-        double v = H[a * D + b] - sum[e];
-        if (a == b) v += H[a * D + a] * lam;
-        const bool on = ((act >> a) & 1) && ((act >> b) & 1);
-        if (!on) v = a == b ? 1.0 : 0.0;
-        blk[a][b] = v;
-        blk[b][a] = v;
-        if (a == b) dg[a] = v;
-    }
-    if (tid < D) {
-        const double rhs = ((act >> tid) & 1) ? -img_b[(size_t)i * D + tid] + sum[NH + tid] : 0.0;
-        rv[tid] = rhs;
-        img_rhs[(size_t)i * D + tid] = rhs;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        fallback = 0;
-        for (int j = 0; j < D && !fallback; ++j) {
-            double d = blk[j][j];
-            for (int k = 0; k < j; ++k) d -= blk[j][k] * blk[j][k];
-            if (!(d > 0.0)) { fallback = 1; break; }
-            d = sqrt(d);
-            blk[j][j] = d;
-            for (int q = j + 1; q < D; ++q) {
-                double v = blk[q][j];
-                for (int k = 0; k < j; ++k) v -= blk[q][k] * blk[j][k];
-                blk[q][j] = v / d;
-            }
-        }
-        if (!fallback) {
-            for (int c = 0; c < D; ++c) {
-                double y[D];
-                for (int q = 0; q < D; ++q) {
-                    double v = q == c ? 1.0 : 0.0;
-                    for (int k = 0; k < q; ++k) v -= blk[q][k] * y[k];
-                    y[q] = v / blk[q][q];
-                }
-                for (int q = D - 1; q >= 0; --q) {
-                    double v = y[q];
-                    for (int k = q + 1; k < D; ++k) v -= blk[k][q] * Mi[k][c];
-                    Mi[q][c] = v / blk[q][q];
-                }
-            }
+    const int p0 = ipart_off[i], p1 = ipart_off[i + 1];
+    for (int e = lane; e < NV; e += 32) {
+        double sum = 0.0;
+        for (int k = p0; k < p1; ++k) sum += (double)part[(size_t)k * NV + e];
+        if (e < NH) {
+            int t = e, a = 0;
+            while (t >= D - a) { t -= D - a; ++a; }
+            const int b = a + t;
+            double v = H[a * D + b] - sum;
+            if (a == b) v += H[a * D + a] * lam;
+            const bool on = ((act >> a) & 1) && ((act >> b) & 1);
+            if (!on) v = a == b ? 1.0 : 0.0;
+            L[a][b] = v;
+            L[b][a] = v;
+            if (a == b) Mi[a][a] = v;  // keeps the diagonal for the Jacobi fallback
+        } else {
+            const int a = e - NH;
+            const double rhs = ((act >> a) & 1) ? -img_b[(size_t)i * D + a] + sum : 0.0;
+            rv[a] = rhs;
+            img_rhs[(size_t)i * D + a] = rhs;
         }
     }
-    __syncthreads();
-    if (fallback) {
+    __syncwarp();
+    // Right-looking Cholesky of the D x D block, lower triangle in place.
+    bool ok = true;
+    for (int j = 0; j < D; ++j) {
+        const double d = L[j][j];
+        if (!(d > 0.0)) { ok = false; break; }
+        const double sd = sqrt(d);
+        const double id = 1.0 / sd;
+        __syncwarp();
+        if (lane == 0) { L[j][j] = sd; invd[j] = id; }
+        if (lane > j && lane < D) L[lane][j] *= id;
+        __syncwarp();
+        const int m = D - j - 1;
+        for (int idx = lane; idx < m * m; idx += 32) {
+            const int q = j + 1 + idx / m, c = j + 1 + idx % m;
+            if (c <= q) L[q][c] -= L[q][j] * L[c][j];
+        }
+        __syncwarp();
+    }
+    if (ok) {
+        // Column c of the inverse: L y = e_c, then L^T x = y.
+        double col[D];
+        if (lane < D) {
+            const int c = lane;
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                double v = q == c ? 1.0 : 0.0;
+#pragma unroll
+                for (int k = 0; k < q; ++k) v -= L[q][k] * col[k];
+                col[q] = q < c ? 0.0 : v * invd[q];
+            }
+#pragma unroll
+            for (int q = D - 1; q >= 0; --q) {
+                double v = col[q];
+#pragma unroll
+                for (int k = q + 1; k < D; ++k) v -= L[k][q] * col[k];
+                col[q] = v * invd[q];
+            }
+        }
+        __syncwarp();
+        if (lane < D)
+#pragma unroll
+            for (int q = 0; q < D; ++q) Mi[q][lane] = col[q];
+    } else {
         // Not SPD in the kernel precision: Jacobi on the block's diagonal.
-        for (int idx = tid; idx < D * D; idx += blockDim.x) {
-            const int a = idx / D, c = idx - a * D;
-            Mi[a][c] = (a == c && dg[a] > 0.0) ? 1.0 / dg[a] : 0.0;
-        }
-        __syncthreads();
+        double dl = 0.0;
+        if (lane < D) dl = Mi[lane][lane];
+        __syncwarp();
+        if (lane < D)
+            for (int q = 0; q < D; ++q) Mi[q][lane] = (q == lane && dl > 0.0) ? 1.0 / dl : 0.0;
     }
-    for (int idx = tid; idx < D * D; idx += blockDim.x) {
+    __syncwarp();
+    for (int idx = lane; idx < D * D; idx += 32) {
         const int a = idx / D, c = idx - a * D;
         const bool on = ((act >> a) & 1) && ((act >> c) & 1);
-        const double v = on ? Mi[a][c] : 0.0;
-        Minv_out[(size_t)i * D * D + idx] = (T)v;
+        if (!on) Mi[a][c] = 0.0;
+        Minv_out[(size_t)i * D * D + idx] = (T)Mi[a][c];
     }
-    __syncthreads();
-    if (tid < 32) {
-        double rz = 0.0, rr = 0.0;
-        if (tid < D) {
-            const bool on_r = (act >> tid) & 1;
-            double zc = 0.0;
-            for (int d = 0; d < D; ++d)
-                if (on_r && ((act >> d) & 1)) zc += Mi[tid][d] * rv[d];
-            const size_t u = (size_t)i * D + tid;
-            const T rt = (T)rv[tid], zt = (T)zc;
-            x[u] = T(0);
-            r[u] = rt;
-            z[u] = zt;
-            p[u] = zt;
-            rz = (double)rt * (double)zt;
-            rr = (double)rt * (double)rt;
-        }
+    __syncwarp();
+    double rz = 0.0, rr = 0.0;
+    if (lane < D) {
+        double zc = 0.0;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            rz += __shfl_xor_sync(0xffffffffu, rz, off);
-            rr += __shfl_xor_sync(0xffffffffu, rr, off);
-        }
-        if (tid == 0) {
-            dots[i] = rz;
-            dots[nI + i] = rr;
-        }
+        for (int d = 0; d < D; ++d) zc += Mi[lane][d] * rv[d];
+        const size_t u = (size_t)i * D + lane;
+        const T rt = (T)rv[lane], zt = (T)zc;
+        x[u] = T(0);
+        r[u] = rt;
+        z[u] = zt;
+        p[u] = zt;
+        rz = (double)rt * (double)zt;
+        rr = (double)rt * (double)rt;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        rz += __shfl_xor_sync(0xffffffffu, rz, off);
+        rr += __shfl_xor_sync(0xffffffffu, rr, off);
+    }
+    if (lane == 0) {
+        dots[i] = rz;
+        dots[nI + i] = rr;
     }
 }
 
@@ -374,21 +397,16 @@ __global__ void __launch_bounds__(256) k_mf_points(JacSrc<T> J, const int *__res
     const int lane = threadIdx.x & 31;
     if (warp >= nchunks) return;
     point_chunk<T, 3>(
-        J.ob_pt, J.ob_img, pchunk[warp], pchunk[warp + 1], lane,
-        [&](int o, int img, int pt, T (&v)[3]) {
-            T rr[2], jx[6], jc[2 * D];
-            jac_point_major<T, D, RC>(J, o, img, pt, rr, jx, jc);
-            const T *pv = p + (size_t)img * D;
-            T s0 = 0, s1 = 0;
+        J.obrec, pchunk[warp], pchunk[warp + 1], lane,
+        [&](int o, int4 rc, T (&v)[3]) {
+            ObsOp<T, D, RC> op;
+            make_op_point_major<T, D, RC>(J, o, rc, op);
+            T pv[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                const T w = pv[c];
-                s0 += jc[c] * w;
-                s1 += jc[D + c] * w;
-            }
-            v[0] = jx[0] * s0 + jx[3] * s1;
-            v[1] = jx[1] * s0 + jx[4] * s1;
-            v[2] = jx[2] * s0 + jx[5] * s1;
+            for (int c = 0; c < D; ++c) pv[c] = p[(size_t)rc.x * D + c];
+            T s0, s1;
+            op.jc_dot(pv, s0, s1);
+            op.jx_t(s0, s1, v);
         },
         [&](int pt, const T (&v)[3]) {
             T u0 = 0, u1 = 0, u2 = 0;
@@ -405,8 +423,7 @@ __global__ void __launch_bounds__(256) k_mf_points(JacSrc<T> J, const int *__res
 
 // PCG image pass: partial sums of Jc~^T (Jx~ u_p) per (chunk, image).
 template <typename T, int D, bool RC>
-__global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, const int *__restrict__ isort_img,
-                                                   const int *__restrict__ isort_pt, long long nO,
+__global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, long long nO,
                                                    const int *__restrict__ img_start,
                                                    const int *__restrict__ ipart_off, const T *__restrict__ u,
                                                    const LMState *__restrict__ st, T *__restrict__ ipart) {
@@ -419,7 +436,7 @@ __global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, const int *__res
     T acc[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) acc[c] = T(0);
-    int cur = isort_img[cs];
+    int cur = __ldg(J.isrec + cs).x;
     auto flush = [&](int img) {
 #pragma unroll
         for (int c = 0; c < D; ++c) {
@@ -439,12 +456,14 @@ __global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, const int *__res
     for (long long base = cs; base < ce; base += 32) {
         const long long k = base + lane;
         const bool valid = k < ce;
-        const int img = valid ? isort_img[k] : 0x7fffffff;
+        int4 rc = make_int4(0x7fffffff, 0, 0, 0);
+        if (valid) rc = __ldg(J.isrec + k);
+        const int img = rc.x;
         T cv[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) cv[c] = T(0);
         if (valid) {
-            const int pt = isort_pt[k];
+            const int pt = rc.y;
             T u0, u1, u2;
             if constexpr (std::is_same<T, float>::value) {
                 const float4 t = __ldg(reinterpret_cast<const float4 *>(u) + pt);
@@ -453,12 +472,11 @@ __global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, const int *__res
                 const T *up = u + 4 * (size_t)pt;
                 u0 = up[0]; u1 = up[1]; u2 = up[2];
             }
-            T rr[2], jx[6], jc[2 * D];
-            jac_image_major<T, D, RC>(J, k, img, pt, rr, jx, jc);
-            const T z0 = jx[0] * u0 + jx[1] * u1 + jx[2] * u2;
-            const T z1 = jx[3] * u0 + jx[4] * u1 + jx[5] * u2;
-#pragma unroll
-            for (int c = 0; c < D; ++c) cv[c] = jc[c] * z0 + jc[D + c] * z1;
+            ObsOp<T, D, RC> op;
+            make_op_image_major<T, D, RC>(J, k, rc, op);
+            T z0, z1;
+            op.jx(u0, u1, u2, z0, z1);
+            op.jc_t(z0, z1, cv);
         }
         while (true) {
             if (valid && img == cur) {
@@ -487,20 +505,16 @@ __global__ void __launch_bounds__(256) k_mf_backsub(JacSrc<T> J, const int *__re
     const int lane = threadIdx.x & 31;
     if (warp >= nchunks) return;
     point_chunk<T, 3>(
-        J.ob_pt, J.ob_img, pchunk[warp], pchunk[warp + 1], lane,
-        [&](int o, int img, int pt, T (&v)[3]) {
-            T rr[2], jx[6], jc[2 * D];
-            jac_point_major<T, D, RC>(J, o, img, pt, rr, jx, jc);
-            const T *d = img_delta + (size_t)img * D;
-            T t0 = 0, t1 = 0;
+        J.obrec, pchunk[warp], pchunk[warp + 1], lane,
+        [&](int o, int4 rc, T (&v)[3]) {
+            ObsOp<T, D, RC> op;
+            make_op_point_major<T, D, RC>(J, o, rc, op);
+            T dv[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                t0 += jc[c] * d[c];
-                t1 += jc[D + c] * d[c];
-            }
-            v[0] = jx[0] * t0 + jx[3] * t1;
-            v[1] = jx[1] * t0 + jx[4] * t1;
-            v[2] = jx[2] * t0 + jx[5] * t1;
+            for (int c = 0; c < D; ++c) dv[c] = img_delta[(size_t)rc.x * D + c];
+            T t0, t1;
+            op.jc_dot(dv, t0, t1);
+            op.jx_t(t0, t1, v);
         },
         [&](int pt, const T (&v)[3]) {
             if (!pt_ok[pt]) return;
@@ -518,14 +532,16 @@ __global__ void __launch_bounds__(256) k_mf_backsub(JacSrc<T> J, const int *__re
         });
 }
 
-__global__ void k_isort_xy32(const int *img_obs, const double2 *ob_xy, long long nO, float2 *ob_xy32,
-                             float2 *isort_xy32) {
+// Packed {image, point, x, y} records of both observation orders.
+__global__ void k_pack_records(const int *img_obs, const int *ob_img, const int *ob_pt, const double2 *ob_xy,
+                               long long nO, int4 *obrec, int4 *isrec) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= nO) return;
     const double2 a = ob_xy[k];
-    ob_xy32[k] = make_float2((float)a.x, (float)a.y);
-    const double2 b = ob_xy[img_obs[k]];
-    isort_xy32[k] = make_float2((float)b.x, (float)b.y);
+    obrec[k] = make_int4(ob_img[k], ob_pt[k], __float_as_int((float)a.x), __float_as_int((float)a.y));
+    const int o = img_obs[k];
+    const double2 b = ob_xy[o];
+    isrec[k] = make_int4(ob_img[o], ob_pt[o], __float_as_int((float)b.x), __float_as_int((float)b.y));
 }
 
 template <typename F>
@@ -557,11 +573,8 @@ JacSrc<T> jac_src(const Bufs &b) {
     J.img_lin = (const ImageLin<T> *)b.img_lin;
     J.points32 = b.points32;
     J.points64 = b.points;
-    J.ob_xy32 = b.ob_xy32;
-    J.ob_xy64 = b.ob_xy;
-    J.isort_xy32 = b.isort_xy32;
-    J.ob_img = b.ob_img;
-    J.ob_pt = b.ob_pt;
+    J.obrec = b.obrec;
+    J.isrec = b.isrec;
     J.img_obs = b.img_obs;
     J.loss = b.loss;
     J.scale = (T)b.loss_scale;
@@ -573,8 +586,8 @@ int warps_grid(long long warps, int threads) { return div_up(warps * 32, threads
 }  // namespace
 
 void launch_mf_prepare(const Bufs &b, cudaStream_t s) {
-    if (b.mixed && b.nO > 0) {
-        k_isort_xy32<<<div_up(b.nO, 256), 256, 0, s>>>(b.img_obs, b.ob_xy, b.nO, b.ob_xy32, b.isort_xy32);
+    if (b.nO > 0) {
+        k_pack_records<<<div_up(b.nO, 256), 256, 0, s>>>(b.img_obs, b.ob_img, b.ob_pt, b.ob_xy, b.nO, b.obrec, b.isrec);
         SFMBA_LAUNCH_CHECK();
     }
 }
@@ -597,7 +610,7 @@ void launch_mf_image_blocks(const Bufs &b, cudaStream_t s) {
         if (b.nO > 0) {
             const long long chunks = (b.nO + kChunkObs - 1) / kChunkObs;
             k_mf_image_accum<T, D, decltype(rc)::value, 0><<<warps_grid(chunks, 128), 128, 0, s>>>(
-                jac_src<T>(b), b.isort_img, b.isort_pt, b.nO, b.img_start, b.ipart_off, (const T *)b.pt_Cinv,
+                jac_src<T>(b), b.nO, b.img_start, b.ipart_off, (const T *)b.pt_Cinv,
                 (const T *)b.pt_h, b.pt_ok, (T *)b.ipart2);
             SFMBA_LAUNCH_CHECK();
         }
@@ -614,11 +627,11 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s) {
         if (b.nO > 0) {
             const long long chunks = (b.nO + kChunkObs - 1) / kChunkObs;
             k_mf_image_accum<T, D, decltype(rc)::value, 1><<<warps_grid(chunks, 128), 128, 0, s>>>(
-                jac_src<T>(b), b.isort_img, b.isort_pt, b.nO, b.img_start, b.ipart_off, (const T *)b.pt_Cinv,
+                jac_src<T>(b), b.nO, b.img_start, b.ipart_off, (const T *)b.pt_Cinv,
                 (const T *)b.pt_h, b.pt_ok, (T *)b.ipart2);
             SFMBA_LAUNCH_CHECK();
         }
-        k_mf_precond_finish<T, D><<<b.nI, 128, 0, s>>>((const T *)b.ipart2, b.ipart_off, b.img_H, b.img_b,
+        k_mf_precond_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.ipart_off, b.img_H, b.img_b,
                                                        b.img_active, b.state, b.nI, b.img_rhs, (T *)b.pcg_Minv,
                                                        (T *)b.pcg_x, (T *)b.pcg_r, (T *)b.pcg_z, (T *)b.pcg_p,
                                                        b.pcg_part);
@@ -645,7 +658,7 @@ void launch_mf_images(const Bufs &b, cudaStream_t s) {
         constexpr int D = decltype(dc)::value;
         const long long chunks = (b.nO + kChunkObs - 1) / kChunkObs;
         k_mf_images<T, D, decltype(rc)::value><<<warps_grid(chunks, 256), 256, 0, s>>>(
-            jac_src<T>(b), b.isort_img, b.isort_pt, b.nO, b.img_start, b.ipart_off, (const T *)b.pcg_u, b.state,
+            jac_src<T>(b), b.nO, b.img_start, b.ipart_off, (const T *)b.pcg_u, b.state,
             (T *)b.ipart);
     });
     SFMBA_LAUNCH_CHECK();

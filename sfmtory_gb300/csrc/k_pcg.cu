@@ -49,7 +49,8 @@ __global__ void k_pcg_scalar_init(const double *part, int nI, double tol2, LMSta
     a = block_sum(a, sh);
     b = block_sum(b, sh);
     if (threadIdx.x == 0) {
-        st->pcg_rz = a;
+        st->pcg_rzbuf[0] = a;
+        st->pcg_rzbuf[1] = 0.0;
         st->pcg_bb = b;
         st->pcg_rr = b;
         st->pcg_tol2 = tol2;
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(128) k_pcg_images_finish(const T *__restrict__
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
-    if (lane == 0) part[i] = pq;
+    if (lane == 0) part[2 * nI + i] = pq;
 }
 
 __global__ void k_point_chunks(const int *pt_start, int nP, long long nO, int nchunks, int *pchunk) {
@@ -108,36 +109,31 @@ __global__ void k_point_chunks(const int *pt_start, int nP, long long nO, int nc
     pchunk[k] = k == nchunks ? (int)nO : pt_start[lo];
 }
 
-__global__ void k_isort_pt(const int *img_obs, const int *ob_pt, long long nO, int *isort_pt) {
-    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (k < nO) isort_pt[k] = ob_pt[img_obs[k]];
-}
 
-__global__ void k_pcg_scalar_alpha(const double *part, int nI, LMState *st) {
+// x += alpha p; r -= alpha q; z = M^-1 r; per-image partials of r.z and
+// r.r. alpha = (r.z) / (p.q) with p.q reduced from the image pass's
+// partials by every block in the same order (no separate scalar kernel).
+// One warp per image, 8 images per block.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_pcg_update(const T *Minv, const T *p, const T *q, LMState *st, int nI,
+                                                    int parity, T *x, T *r, T *z, double *part) {
     __shared__ double sh[256];
     if (st->pcg_done) return;
     double a = 0.0;
-    for (int k = threadIdx.x; k < nI; k += blockDim.x) a += part[k];
+    for (int k = threadIdx.x; k < nI; k += blockDim.x) a += part[2 * nI + k];
     a = block_sum(a, sh);
-    if (threadIdx.x == 0) {
-        if (!(a > 0.0) || !isfinite(a)) {
-            st->pcg_done = 1;  // breakdown: keep the current iterate
+    if (!(a > 0.0) || !isfinite(a)) {  // breakdown: keep the current iterate
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st->pcg_done = 1;
             st->pcg_alpha = 0.0;
-        } else {
-            st->pcg_alpha = st->pcg_rz / a;
         }
+        return;
     }
-}
-
-// x += alpha p; r -= alpha q; z = M^-1 r; part = (r.z, r.r) per image. One warp per image.
-template <typename T, int D>
-__global__ void __launch_bounds__(128) k_pcg_update(const T *Minv, const T *p, const T *q, const LMState *st,
-                                                    int nI, T *x, T *r, T *z, double *part) {
-    if (st->pcg_done) return;
+    const double alpha = st->pcg_rzbuf[parity] / a;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->pcg_alpha = alpha;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= nI) return;
-    const double alpha = st->pcg_alpha;
     const size_t base = (size_t)i * D;
     T rc = T(0);
     if (lane < D) {
@@ -169,32 +165,35 @@ __global__ void __launch_bounds__(128) k_pcg_update(const T *Minv, const T *p, c
     }
 }
 
-__global__ void k_pcg_scalar_beta(const double *part, int nI, LMState *st) {
+// Convergence test and p = z + beta p, beta = (r.z)_new / (r.z)_old. Every
+// block reduces the partials itself; block 0 records the new r.z in the
+// other parity slot (read by the next iteration only) and the counters.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const double *part, int nI, int nID,
+                                                 int parity, T *p) {
     __shared__ double sh[256];
     if (st->pcg_done) return;
     double a = 0.0, b = 0.0;
     for (int k = threadIdx.x; k < nI; k += blockDim.x) { a += part[k]; b += part[nI + k]; }
     a = block_sum(a, sh);
     b = block_sum(b, sh);
-    if (threadIdx.x == 0) {
+    const bool stop = b <= st->pcg_tol2 * st->pcg_bb || !(a > 0.0) || !isfinite(a);
+    const double beta = stop ? 0.0 : a / st->pcg_rzbuf[parity];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         st->pcg_iterations += 1;
         st->pcg_total += 1;
         st->pcg_rr = b;
-        if (b <= st->pcg_tol2 * st->pcg_bb || !(a > 0.0) || !isfinite(a)) {
+        if (stop) {
             st->pcg_done = 1;
         } else {
-            st->pcg_beta = a / st->pcg_rz;
-            st->pcg_rz = a;
+            st->pcg_beta = beta;
+            st->pcg_rzbuf[parity ^ 1] = a;
         }
     }
-}
-
-template <typename T>
-__global__ void k_pcg_dir(const T *z, const LMState *st, int nID, T *p) {
-    if (st->pcg_done) return;
+    if (stop) return;
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= nID) return;
-    p[u] = (T)((double)z[u] + st->pcg_beta * (double)p[u]);
+    p[u] = (T)((double)z[u] + beta * (double)p[u]);
 }
 
 template <typename T>
@@ -228,16 +227,13 @@ void images_finish_t(const Bufs &b, cudaStream_t s) {
 }
 
 template <typename T, int D>
-void vector_t(const Bufs &b, cudaStream_t s) {
-    k_pcg_scalar_alpha<<<1, 256, 0, s>>>(b.pcg_part, b.nI, b.state);
-    SFMBA_LAUNCH_CHECK();
-    k_pcg_update<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.pcg_Minv, (const T *)b.pcg_p,
-                                                       (const T *)b.pcg_q, b.state, b.nI, (T *)b.pcg_x,
+void vector_t(const Bufs &b, cudaStream_t s, int parity) {
+    k_pcg_update<T, D><<<div_up(b.nI, 8), 256, 0, s>>>((const T *)b.pcg_Minv, (const T *)b.pcg_p,
+                                                       (const T *)b.pcg_q, b.state, b.nI, parity, (T *)b.pcg_x,
                                                        (T *)b.pcg_r, (T *)b.pcg_z, b.pcg_part);
     SFMBA_LAUNCH_CHECK();
-    k_pcg_scalar_beta<<<1, 256, 0, s>>>(b.pcg_part, b.nI, b.state);
-    SFMBA_LAUNCH_CHECK();
-    k_pcg_dir<T><<<div_up(b.nID, 256), 256, 0, s>>>((const T *)b.pcg_z, b.state, b.nID, (T *)b.pcg_p);
+    k_pcg_dir<T><<<div_up(b.nID, 256), 256, 0, s>>>((const T *)b.pcg_z, b.state, b.pcg_part, b.nI, b.nID, parity,
+                                                    (T *)b.pcg_p);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -257,19 +253,20 @@ void launch_pcg_start(const Bufs &b, cudaStream_t s) {
         });                                                      \
     }
 SFMBA_PCG_LAUNCHER(launch_pcg_images_finish, images_finish_t)
-SFMBA_PCG_LAUNCHER(launch_pcg_vector, vector_t)
 #undef SFMBA_PCG_LAUNCHER
 
-void launch_pcg_partition(Bufs &b, const int *img_keys_sorted, cudaStream_t s) {
+void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity) {
+    dispatch_D(b.D, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        if (b.mixed) vector_t<float, D>(b, s, parity);
+        else vector_t<double, D>(b, s, parity);
+    });
+}
+
+void launch_pcg_partition(Bufs &b, cudaStream_t s) {
     b.npchunks = (int)((b.nO + kChunkObs - 1) / kChunkObs);
     k_point_chunks<<<div_up(b.npchunks + 1, 256), 256, 0, s>>>(b.pt_start, b.nP, b.nO, b.npchunks, b.pchunk);
     SFMBA_LAUNCH_CHECK();
-    if (b.nO > 0) {
-        SFMBA_CUDA(cudaMemcpyAsync(b.isort_img, img_keys_sorted, sizeof(int) * (size_t)b.nO,
-                                   cudaMemcpyDeviceToDevice, s));
-        k_isort_pt<<<div_up(b.nO, 256), 256, 0, s>>>(b.img_obs, b.ob_pt, b.nO, b.isort_pt);
-        SFMBA_LAUNCH_CHECK();
-    }
 }
 
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s) {

@@ -99,6 +99,44 @@ __global__ void k_group_decode(const unsigned *unique_keys, const int *d_ngroups
     group_ij[g] = make_int2((int)(k / (unsigned)nI), (int)(k % (unsigned)nI));
 }
 
+__global__ void k_fill(int *a, long long n, int v) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) a[t] = v;
+}
+
+__global__ void k_min_image(const int *obs_point, const int *obs_image, long long nO, int *key) {
+    const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (o < nO) atomicMin(key + obs_point[o], obs_image[o]);
+}
+
+__global__ void k_invert(const int *perm, int n, int *inv) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) inv[perm[k]] = k;
+}
+
+__global__ void k_remap(const int *in, const int *map, long long n, int *out) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) out[t] = map[in[t]];
+}
+
+__global__ void k_gather_points(const double *src, const int *perm, int nP, double *dst) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nP) return;
+    const int o = perm[k];
+    dst[3 * (size_t)k] = src[3 * (size_t)o];
+    dst[3 * (size_t)k + 1] = src[3 * (size_t)o + 1];
+    dst[3 * (size_t)k + 2] = src[3 * (size_t)o + 2];
+}
+
+__global__ void k_scatter_points(const double *src, const int *old2new, int nP, double *dst) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nP) return;
+    const int k = old2new[o];
+    dst[3 * (size_t)o] = src[3 * (size_t)k];
+    dst[3 * (size_t)o + 1] = src[3 * (size_t)k + 1];
+    dst[3 * (size_t)o + 2] = src[3 * (size_t)k + 2];
+}
+
 int bits_for(long long v) {
     int b = 1;
     while ((1LL << b) <= v) ++b;
@@ -120,12 +158,50 @@ void validate_problem_device(const int *cam_of_img, const int *cam_model, const 
 }
 
 size_t sort_temp_bytes(long long nO, int nP, int nI) {
-    size_t a = 0, b = 0;
+    size_t a = 0, b = 0, c = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, a, (int *)nullptr, (int *)nullptr, (int *)nullptr,
                                     (int *)nullptr, (int)nO, 0, bits_for(nP));
     cub::DeviceRadixSort::SortPairs(nullptr, b, (int *)nullptr, (int *)nullptr, (int *)nullptr,
                                     (int *)nullptr, (int)nO, 0, bits_for(nI));
-    return a > b ? a : b;
+    cub::DeviceRadixSort::SortPairs(nullptr, c, (int *)nullptr, (int *)nullptr, (int *)nullptr,
+                                    (int *)nullptr, nP, 0, bits_for((long long)nI + 1));
+    size_t m = a > b ? a : b;
+    return m > c ? m : c;
+}
+
+void order_points(const int *obs_point_in, const int *obs_image_in, long long nO, int nP, int nI, int *key,
+                  int *key_sorted, int *iota_tmp, int *perm, int *old2new, int *obs_point_out, void *temp,
+                  size_t temp_bytes, cudaStream_t s) {
+    if (nP == 0) return;
+    k_fill<<<div_up(nP, 256), 256, 0, s>>>(key, nP, nI);  // points without observations go last
+    SFMBA_LAUNCH_CHECK();
+    if (nO > 0) {
+        k_min_image<<<div_up(nO, 256), 256, 0, s>>>(obs_point_in, obs_image_in, nO, key);
+        SFMBA_LAUNCH_CHECK();
+    }
+    k_iota<<<div_up(nP, 256), 256, 0, s>>>(iota_tmp, nP);
+    SFMBA_LAUNCH_CHECK();
+    size_t tb = temp_bytes;
+    SFMBA_CUDA(cub::DeviceRadixSort::SortPairs(temp, tb, key, key_sorted, iota_tmp, perm, nP, 0,
+                                               bits_for((long long)nI + 1), s));
+    k_invert<<<div_up(nP, 256), 256, 0, s>>>(perm, nP, old2new);
+    SFMBA_LAUNCH_CHECK();
+    if (nO > 0) {
+        k_remap<<<div_up(nO, 256), 256, 0, s>>>(obs_point_in, old2new, nO, obs_point_out);
+        SFMBA_LAUNCH_CHECK();
+    }
+}
+
+void gather_points(const double *src, const int *perm, int nP, double *dst, cudaStream_t s) {
+    if (nP == 0) return;
+    k_gather_points<<<div_up(nP, 256), 256, 0, s>>>(src, perm, nP, dst);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void scatter_points(const double *src, const int *old2new, int nP, double *dst, cudaStream_t s) {
+    if (nP == 0) return;
+    k_scatter_points<<<div_up(nP, 256), 256, 0, s>>>(src, old2new, nP, dst);
+    SFMBA_LAUNCH_CHECK();
 }
 
 void sort_observations(const int *obs_point_in, const int *obs_image_in, const double *obs_xy_in,

@@ -30,6 +30,8 @@ struct Bufs {
     int *pt_start = nullptr;                            // [nP+1]
     int *img_start = nullptr;                           // [nI+1]
     int *img_obs = nullptr;                             // [nO] image-sorted -> point-sorted index
+    int *pt_perm = nullptr;       // [nP] solver point index -> caller's point index
+    int *pt_old2new = nullptr;    // [nP] caller's point index -> solver point index
     int *img_slot = nullptr;      // [nI*D] slot of column r of image i, -1 if not an unknown
     int *img_active = nullptr;    // [nI] bit r: column r is an unknown
     int *img_free = nullptr;      // [nI] pose free or camera free
@@ -78,14 +80,12 @@ struct Bufs {
     // Work partition of the matrix-free passes (fixed-size observation chunks).
     int *pchunk = nullptr;        // [npchunks+1] point-aligned chunk starts (point-major order)
     int npchunks = 0;
-    int *isort_img = nullptr;     // [nO] image of the k-th image-major observation
-    int *isort_pt = nullptr;      // [nO] point of the k-th image-major observation
     int *ipart_off = nullptr;     // [nI+1] first partial slot of each image
     void *ipart = nullptr;        // [nparts*D] per-(chunk, image) partial sums
     void *ipart2 = nullptr;       // [nparts*(D(D+1)/2+D)] block partials of the image passes
     int nparts = 0;
-    float2 *ob_xy32 = nullptr;    // [nO] point-major pixels (FP32 recompute)
-    float2 *isort_xy32 = nullptr; // [nO] image-major pixels (FP32 recompute)
+    int4 *obrec = nullptr;        // [nO] point-major {image, point, x, y (float bits)}
+    int4 *isrec = nullptr;        // [nO] image-major {image, point, x, y (float bits)}
 };
 
 constexpr int kCostBlocks = 1024;
@@ -104,6 +104,14 @@ struct JacProbe {
 
 // ---- setup (k_setup.cu)
 size_t sort_temp_bytes(long long nO, int nP, int nI);
+// Visibility order of the points: sorted by the first image observing them
+// (ties by index), so points seen by the same cameras sit together. Writes
+// perm (new -> old), old2new and the observations' point indices renumbered.
+void order_points(const int *obs_point_in, const int *obs_image_in, long long nO, int nP, int nI, int *key,
+                  int *key_sorted, int *iota_tmp, int *perm, int *old2new, int *obs_point_out, void *temp,
+                  size_t temp_bytes, cudaStream_t s);
+void gather_points(const double *src, const int *perm, int nP, double *dst, cudaStream_t s);
+void scatter_points(const double *src, const int *old2new, int nP, double *dst, cudaStream_t s);
 void sort_observations(const int *obs_point_in, const int *obs_image_in, const double *obs_xy_in,
                        long long nO, int nP, int nI, Bufs &b, void *temp, size_t temp_bytes,
                        int *keys_tmp, int *vals_tmp, int *keys_tmp2, int *vals_tmp2,
@@ -150,7 +158,7 @@ void launch_lu_factor(const Bufs &b, cudaStream_t s);
 void launch_lu_solve(const Bufs &b, cudaStream_t s);
 
 // ---- matrix-free observation passes (k_matfree.cu)
-void launch_mf_prepare(const Bufs &b, cudaStream_t s);          // FP32 pixel copies
+void launch_mf_prepare(const Bufs &b, cudaStream_t s);          // packed observation records
 void launch_mf_point_reduce(const Bufs &b, cudaStream_t s);     // C_p, g_p, free count
 void launch_mf_image_blocks(const Bufs &b, cudaStream_t s);     // H_i, b_i
 void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PCG start vectors
@@ -164,9 +172,9 @@ void launch_pcg_start(const Bufs &b, cudaStream_t s);
 // One PCG iteration is launch_mf_points, launch_mf_images, then
 // launch_pcg_images_finish (q = S p) and launch_pcg_vector (x, r, z, p).
 void launch_pcg_images_finish(const Bufs &b, cudaStream_t s);
-void launch_pcg_vector(const Bufs &b, cudaStream_t s);
+void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity);  // parity = iteration & 1
 // Work partition of the matrix-free passes (after sort_observations).
-void launch_pcg_partition(Bufs &b, const int *img_keys_sorted, cudaStream_t s);
+void launch_pcg_partition(Bufs &b, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
 

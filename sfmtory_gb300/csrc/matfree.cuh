@@ -10,8 +10,10 @@
 //     image by a finishing kernel.
 // The Jacobian of an observation comes either from the stored record
 // (RC = false) or is recomputed from the per-image constants, the point and
-// the pixel (RC = true): 16-32 bytes of input instead of a 128-256 byte
-// record, for the cost of ~200 flops.
+// the pixel (RC = true): a 16-byte packed observation record instead of a
+// 128-256 byte Jacobian record, for ~150 flops. The recomputed form applies
+// the Jacobian and its transpose in structured form (rotation columns
+// q x d, translation d, point R^T d) without materialising it.
 #pragma once
 
 #include <type_traits>
@@ -27,17 +29,14 @@ struct JacSrc {
     const ImageLin<T> *img_lin = nullptr;    // per-image constants (RC = true)
     const float4 *points32 = nullptr;        // T = float
     const double *points64 = nullptr;        // T = double
-    const float2 *ob_xy32 = nullptr;         // point-major pixels, T = float
-    const double2 *ob_xy64 = nullptr;        // point-major pixels, T = double
-    const float2 *isort_xy32 = nullptr;      // image-major pixels, T = float
-    const int *ob_img = nullptr;
-    const int *ob_pt = nullptr;
-    const int *img_obs = nullptr;
+    const int4 *obrec = nullptr;             // point-major {image, point, x, y}
+    const int4 *isrec = nullptr;             // image-major {image, point, x, y}
+    const int *img_obs = nullptr;            // image-major -> point-major index
     int loss = 0;
     T scale = T(1);
 };
 
-// Jx~ (2x3), Jc~ (2xD) and r~ of a stored record, 16-byte vector loads.
+// Jr~, Jx~ (2x3), Jc~ (2xD) of a stored record, 16-byte vector loads.
 template <typename T, int D>
 __device__ __forceinline__ void load_record(const T *__restrict__ rec, long long o, T rr[2], T jx[6],
                                             T jc[2 * D]) {
@@ -66,61 +65,148 @@ __device__ __forceinline__ void load_record(const T *__restrict__ rec, long long
     for (int k = 0; k < 2 * D; ++k) jc[k] = v[8 + k];
 }
 
-template <typename T>
-__device__ __forceinline__ void load_point_T(const JacSrc<T> &J, int p, T &X0, T &X1, T &X2) {
-    if constexpr (std::is_same<T, float>::value) {
-        const float4 v = __ldg(J.points32 + p);
-        X0 = v.x; X1 = v.y; X2 = v.z;
-    } else {
-        X0 = J.points64[3 * (size_t)p]; X1 = J.points64[3 * (size_t)p + 1]; X2 = J.points64[3 * (size_t)p + 2];
+// The Jacobian of one observation as an operator. Two forms with one
+// interface: recomputed from the pixel, point and image constants (RC), or
+// read from a stored record. Image blocks are D wide: 3 rotation, 3
+// translation, then the camera's parameters.
+template <typename T, int D, bool RC>
+struct ObsOp;
+
+template <typename T, int D>
+struct ObsOp<T, D, true> {
+    static constexpr int K = LinCompact<T, D>::K;
+    LinCompact<T, D> L;
+    T R[9];
+    bool valid;
+
+    __device__ __forceinline__ void build(const JacSrc<T> &J, int img, int pt, int4 rc) {
+        const ImageLin<T> im = J.img_lin[img];
+        T X0, X1, X2;
+        if constexpr (std::is_same<T, float>::value) {
+            const float4 v = __ldg(J.points32 + pt);
+            X0 = v.x; X1 = v.y; X2 = v.z;
+        } else {
+            X0 = J.points64[3 * (size_t)pt]; X1 = J.points64[3 * (size_t)pt + 1]; X2 = J.points64[3 * (size_t)pt + 2];
+        }
+        valid = linearize_compact<T, D>(im, X0, X1, X2, (T)__int_as_float(rc.z), (T)__int_as_float(rc.w), J.loss,
+                                        J.scale, L);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) R[k] = im.R[k];
     }
+    __device__ __forceinline__ T r(int row) const { return L.r[row]; }
+    // (s0, s1) = Jc~ v for an image-block vector v.
+    __device__ __forceinline__ void jc_dot(const T *v, T &s0, T &s1) const {
+        T w0 = T(0), w1 = T(0), w2 = T(0);
+        if (L.pose_on) {  // omega x q + dt
+            w0 = v[1] * L.q[2] - v[2] * L.q[1] + v[3];
+            w1 = v[2] * L.q[0] - v[0] * L.q[2] + v[4];
+            w2 = v[0] * L.q[1] - v[1] * L.q[0] + v[5];
+        }
+        s0 = L.d[0][0] * w0 + L.d[0][1] * w1 + L.d[0][2] * w2;
+        s1 = L.d[1][0] * w0 + L.d[1][1] * w1 + L.d[1][2] * w2;
+        if constexpr (D > 6) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                s0 += L.g[0][k] * v[6 + k];
+                s1 += L.g[1][k] * v[6 + k];
+            }
+        }
+    }
+    // out = Jx~^T (a0, a1) = R^T (a0 d0 + a1 d1)
+    __device__ __forceinline__ void jx_t(T a0, T a1, T out[3]) const {
+        const T e0 = a0 * L.d[0][0] + a1 * L.d[1][0];
+        const T e1 = a0 * L.d[0][1] + a1 * L.d[1][1];
+        const T e2 = a0 * L.d[0][2] + a1 * L.d[1][2];
+        out[0] = R[0] * e0 + R[3] * e1 + R[6] * e2;
+        out[1] = R[1] * e0 + R[4] * e1 + R[7] * e2;
+        out[2] = R[2] * e0 + R[5] * e1 + R[8] * e2;
+    }
+    // (z0, z1) = Jx~ u = d_row . (R u)
+    __device__ __forceinline__ void jx(T u0, T u1, T u2, T &z0, T &z1) const {
+        const T a = R[0] * u0 + R[1] * u1 + R[2] * u2;
+        const T b = R[3] * u0 + R[4] * u1 + R[5] * u2;
+        const T c = R[6] * u0 + R[7] * u1 + R[8] * u2;
+        z0 = L.d[0][0] * a + L.d[0][1] * b + L.d[0][2] * c;
+        z1 = L.d[1][0] * a + L.d[1][1] * b + L.d[1][2] * c;
+    }
+    // out = Jc~^T (z0, z1) = [q x e, e, z0 g0 + z1 g1], e = z0 d0 + z1 d1
+    __device__ __forceinline__ void jc_t(T z0, T z1, T out[D]) const {
+        const T e0 = z0 * L.d[0][0] + z1 * L.d[1][0];
+        const T e1 = z0 * L.d[0][1] + z1 * L.d[1][1];
+        const T e2 = z0 * L.d[0][2] + z1 * L.d[1][2];
+        const T on = L.pose_on ? T(1) : T(0);
+        out[0] = on * (L.q[1] * e2 - L.q[2] * e1);
+        out[1] = on * (L.q[2] * e0 - L.q[0] * e2);
+        out[2] = on * (L.q[0] * e1 - L.q[1] * e0);
+        out[3] = on * e0;
+        out[4] = on * e1;
+        out[5] = on * e2;
+#pragma unroll
+        for (int k = 0; k < D - 6; ++k) out[6 + k] = z0 * L.g[0][k] + z1 * L.g[1][k];
+    }
+    __device__ __forceinline__ void jx_rows(T jx[6]) const {
+        jx_t(T(1), T(0), jx);
+        jx_t(T(0), T(1), jx + 3);
+    }
+    __device__ __forceinline__ void jc_rows(T jc[2 * D]) const {
+        jc_t(T(1), T(0), jc);
+        jc_t(T(0), T(1), jc + D);
+    }
+};
+
+template <typename T, int D>
+struct ObsOp<T, D, false> {
+    T rr[2], jxm[6], jcm[2 * D];
+    bool valid;
+
+    __device__ __forceinline__ void build_record(const T *rec, long long o) {
+        load_record<T, D>(rec, o, rr, jxm, jcm);
+        valid = true;
+    }
+    __device__ __forceinline__ T r(int row) const { return rr[row]; }
+    __device__ __forceinline__ void jc_dot(const T *v, T &s0, T &s1) const {
+        s0 = T(0);
+        s1 = T(0);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            s0 += jcm[c] * v[c];
+            s1 += jcm[D + c] * v[c];
+        }
+    }
+    __device__ __forceinline__ void jx_t(T a0, T a1, T out[3]) const {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[c] = a0 * jxm[c] + a1 * jxm[3 + c];
+    }
+    __device__ __forceinline__ void jx(T u0, T u1, T u2, T &z0, T &z1) const {
+        z0 = jxm[0] * u0 + jxm[1] * u1 + jxm[2] * u2;
+        z1 = jxm[3] * u0 + jxm[4] * u1 + jxm[5] * u2;
+    }
+    __device__ __forceinline__ void jc_t(T z0, T z1, T out[D]) const {
+#pragma unroll
+        for (int c = 0; c < D; ++c) out[c] = z0 * jcm[c] + z1 * jcm[D + c];
+    }
+    __device__ __forceinline__ void jx_rows(T jx[6]) const {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) jx[c] = jxm[c];
+    }
+    __device__ __forceinline__ void jc_rows(T jc[2 * D]) const {
+#pragma unroll
+        for (int c = 0; c < 2 * D; ++c) jc[c] = jcm[c];
+    }
+};
+
+// Operator of point-major observation o with packed record rc.
+template <typename T, int D, bool RC>
+__device__ __forceinline__ void make_op_point_major(const JacSrc<T> &J, int o, int4 rc, ObsOp<T, D, RC> &op) {
+    if constexpr (RC) op.build(J, rc.x, rc.y, rc);
+    else op.build_record(J.rec, o);
 }
 
-// Point-major observation o (image i, point p). Returns whether it is in
-// front of its camera (stored path: the record of a culled observation is 0).
+// Operator of image-major observation k with packed record rc.
 template <typename T, int D, bool RC>
-__device__ __forceinline__ bool jac_point_major(const JacSrc<T> &J, int o, int i, int p, T rr[2], T jx[6],
-                                                T jc[2 * D]) {
-    if constexpr (RC) {
-        const ImageLin<T> im = J.img_lin[i];
-        T X0, X1, X2;
-        load_point_T<T>(J, p, X0, X1, X2);
-        T ox, oy;
-        if constexpr (std::is_same<T, float>::value) {
-            const float2 xy = __ldg(J.ob_xy32 + o);
-            ox = xy.x; oy = xy.y;
-        } else {
-            const double2 xy = J.ob_xy64[o];
-            ox = xy.x; oy = xy.y;
-        }
-        return linearize<T, D>(im, X0, X1, X2, ox, oy, J.loss, J.scale, rr, jx, jc);
-    } else {
-        load_record<T, D>(J.rec, o, rr, jx, jc);
-        return true;
-    }
-}
-
-// Image-major observation k (image i, point p).
-template <typename T, int D, bool RC>
-__device__ __forceinline__ bool jac_image_major(const JacSrc<T> &J, long long k, int i, int p, T rr[2], T jx[6],
-                                                T jc[2 * D]) {
-    if constexpr (RC) {
-        const ImageLin<T> im = J.img_lin[i];
-        T X0, X1, X2;
-        load_point_T<T>(J, p, X0, X1, X2);
-        T ox, oy;
-        if constexpr (std::is_same<T, float>::value) {
-            const float2 xy = __ldg(J.isort_xy32 + k);
-            ox = xy.x; oy = xy.y;
-        } else {
-            const double2 xy = J.ob_xy64[J.img_obs[k]];
-            ox = xy.x; oy = xy.y;
-        }
-        return linearize<T, D>(im, X0, X1, X2, ox, oy, J.loss, J.scale, rr, jx, jc);
-    } else {
-        load_record<T, D>(J.rec, J.img_obs[k], rr, jx, jc);
-        return true;
-    }
+__device__ __forceinline__ void make_op_image_major(const JacSrc<T> &J, long long k, int4 rc, ObsOp<T, D, RC> &op) {
+    if constexpr (RC) op.build(J, rc.x, rc.y, rc);
+    else op.build_record(J.rec, J.img_obs[k]);
 }
 
 template <typename T>

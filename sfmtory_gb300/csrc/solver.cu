@@ -376,7 +376,7 @@ class Solver {
         const int nID = nI * D;
         const size_t tsz = mixed ? sizeof(float) : sizeof(double);
         const size_t RS = (size_t)((8 + 2 * D) + 3) / 4 * 4;
-        size_t sort_tmp = nO > 0 ? sort_temp_bytes(nO, nP, nI) : 0;
+        size_t sort_tmp = sort_temp_bytes(std::max<long long>(nO, 1), std::max(nP, 1), nI);
         {
             size_t scan_bytes = 0;
             SFMBA_CUDA(cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, (long long *)nullptr,
@@ -391,6 +391,7 @@ class Solver {
         int *k1 = nullptr, *v1 = nullptr, *k2 = nullptr, *v2 = nullptr;
         long long *pair_scan = nullptr;
         int *d_bad = nullptr;
+        int *pkey = nullptr, *pkey2 = nullptr, *piota = nullptr, *obs_pt_new = nullptr;
         for (int pass = 0; pass < 2; ++pass) {
             if (pass == 0) A.begin_sizing(); else A.commit();
             Bufs &b = b_;
@@ -468,18 +469,22 @@ class Solver {
                     b.pcg_q = A.take<char>((size_t)nID * tsz);
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
                     b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
-                    b.pcg_part = A.take<double>((size_t)3 * nI);
+                    b.pcg_part = A.take<double>((size_t)3 * nI);  // r.z, r.r, p.q per image
                     b.pchunk = A.take<int>((size_t)nchunks + 1);
-                    b.isort_img = A.take<int>(nO);
-                    b.isort_pt = A.take<int>(nO);
                     b.ipart_off = A.take<int>((size_t)nI + 1);
                     b.ipart = A.take<char>((size_t)(nI + nchunks + 1) * D * tsz);
                     b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * (D * (D + 1) / 2 + D) * tsz);
-                    if (mixed) {
-                        b.ob_xy32 = A.take<float2>(nO);
-                        b.isort_xy32 = A.take<float2>(nO);
-                    }
+                    b.obrec = A.take<int4>(nO);
+                    b.isrec = A.take<int4>(nO);
                 }
+            }
+            if (need_system) {
+                b.pt_perm = A.take<int>(nP);
+                b.pt_old2new = A.take<int>(nP);
+                pkey = A.take<int>(nP);
+                pkey2 = A.take<int>(nP);
+                piota = A.take<int>(nP);
+                obs_pt_new = A.take<int>(nO);
             }
             sort_temp = A.take<char>(sort_tmp);
             k1 = A.take<int>(nO);
@@ -493,7 +498,7 @@ class Solver {
         put(const_cast<int *>(b.cam_of_img), p->camera_of_image, nI, device, s_);
         put(b.cams, p->camera_params, (size_t)nC * 8, device, s_);
         put(b.poses, p->poses, (size_t)nI * 7, device, s_);
-        put(b.points, p->points, (size_t)nP * 3, device, s_);
+        if (!need_system) put(b.points, p->points, (size_t)nP * 3, device, s_);
         const int *src_img = p->obs_image, *src_pt = p->obs_point;
         const double *src_xy = p->obs_xy;
         if (!device) {
@@ -517,10 +522,18 @@ class Solver {
         put_vec(b.slot_pre_start, lay_.slot_pre_start, s_);
         put_vec(b.slot_pre, lay_.slot_pre, s_);
         put_vec(b.slot_masked, lay_.slot_masked, s_);
+        if (need_system) {
+            // Solver point order: by first observing image (see order_points).
+            order_points(src_pt, src_img, nO, nP, nI, pkey, pkey2, piota, b.pt_perm, b.pt_old2new, obs_pt_new,
+                         sort_temp, sort_tmp, s_);
+            put(b.points_trial, p->points, (size_t)nP * 3, device, s_);
+            gather_points(b.points_trial, b.pt_perm, nP, b.points, s_);
+            src_pt = obs_pt_new;
+        }
         sort_observations(src_pt, src_img, src_xy, nO, nP, nI, b, sort_temp, sort_tmp, k1, v1, k2, v2, s_);
         SFMBA_CUDA(cudaMemsetAsync(b.state, 0, sizeof(LMState), s_));
         if (need_system && solver_ == SFMBA_SOLVER_PCG) {
-            launch_pcg_partition(b, k2, s_);
+            launch_pcg_partition(b, s_);
             // Partial-sum slots of the image pass: one per (chunk, image) overlap.
             std::vector<int> img_start = fetch(b.img_start, (size_t)nI + 1, true, s_);
             std::vector<int> off(nI + 1, 0);
@@ -628,7 +641,7 @@ class Solver {
                         for (int k = 0; k < m; ++k) {
                             { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_); }
                             { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_); launch_pcg_images_finish(b, s_); }
-                            { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_); }
+                            { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, (it + k) & 1); }
                         }
                         read_state();
                         if (hs.pcg_done) break;
@@ -670,8 +683,14 @@ class Solver {
         const cudaMemcpyKind k = device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         if (r->poses && b_.nI)
             SFMBA_CUDA(cudaMemcpyAsync(r->poses, b_.poses, sizeof(double) * 7 * (size_t)b_.nI, k, s_));
-        if (r->points && b_.nP)
-            SFMBA_CUDA(cudaMemcpyAsync(r->points, b_.points, sizeof(double) * 3 * (size_t)b_.nP, k, s_));
+        if (r->points && b_.nP) {
+            const double *src = b_.points;
+            if (b_.pt_old2new) {  // back to the caller's point order
+                scatter_points(b_.points, b_.pt_old2new, b_.nP, b_.points_trial, s_);
+                src = b_.points_trial;
+            }
+            SFMBA_CUDA(cudaMemcpyAsync(r->points, src, sizeof(double) * 3 * (size_t)b_.nP, k, s_));
+        }
         if (r->camera_params && b_.nC)
             SFMBA_CUDA(cudaMemcpyAsync(r->camera_params, b_.cams, sizeof(double) * 8 * (size_t)b_.nC, k, s_));
         SFMBA_CUDA(cudaStreamSynchronize(s_));
