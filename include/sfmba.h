@@ -106,7 +106,9 @@ typedef struct sfmba_options {
     int32_t refinement_steps;     /* FP64 iterative-refinement steps (dense)   */
     double target_cost;           /* > 0: also stop once cost <= target_cost   */
     int32_t dense_max_dim;        /* AUTO picks dense up to this reduced dim   */
-    int32_t reserved[7];
+    int32_t fp64_polish;          /* mixed path: when the FP32 loop would stop,
+                                     continue the same LM loop in FP64 (default 1) */
+    int32_t reserved[6];
 } sfmba_options;
 
 /* crates/sfm-ba/src/lib.rs:240-247 (`BaOutput`). Output buffers are caller
@@ -121,6 +123,8 @@ typedef struct sfmba_result {
     int32_t status;
     int32_t damping_retries;      /* inner retries summed over outer iterations */
     int32_t solver_used;          /* sfmba_solver actually run                 */
+    int32_t polish_iteration;     /* outer iteration where the FP64 polish began, -1 if none */
+    int32_t reserved_i;
     int64_t linear_iterations;    /* PCG iterations summed over all retries    */
     int64_t reduced_dim;          /* size of the reduced camera system          */
     int64_t valid_observations;   /* observations in front of their camera at the end */

@@ -69,7 +69,8 @@ class SfmbaOptions(C.Structure):
         ("refinement_steps", C.c_int32),
         ("target_cost", C.c_double),
         ("dense_max_dim", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("fp64_polish", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -84,6 +85,8 @@ class SfmbaResult(C.Structure):
         ("status", C.c_int32),
         ("damping_retries", C.c_int32),
         ("solver_used", C.c_int32),
+        ("polish_iteration", C.c_int32),
+        ("reserved_i", C.c_int32),
         ("linear_iterations", C.c_int64),
         ("reduced_dim", C.c_int64),
         ("valid_observations", C.c_int64),
@@ -107,6 +110,7 @@ def default_options(**overrides) -> SfmbaOptions:
     o.refinement_steps = 1
     o.target_cost = 0.0
     o.dense_max_dim = 6000
+    o.fp64_polish = 1
     for k, v in overrides.items():
         if not hasattr(o, k):
             raise AttributeError(f"sfmba_options has no field {k!r}")

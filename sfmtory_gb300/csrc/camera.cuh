@@ -265,8 +265,8 @@ __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T
     return true;
 }
 
-// FP64 residual exactly as the reference's cost evaluates it: quaternion
-// rotation (pose.rs:46-48) and project() with a true division by z.
+// FP64 residual as the reference's cost evaluates it: quaternion rotation
+// (pose.rs:46-48) and project() (the perspective divide as one reciprocal).
 __device__ __forceinline__ bool residual64(const double *pose7, int model, const double *c,
                                            double X0, double X1, double X2, double ox, double oy,
                                            double &rx, double &ry) {
@@ -278,7 +278,8 @@ __device__ __forceinline__ bool residual64(const double *pose7, int model, const
     const double pc1 = X1 + w * ty + (z * tx - x * tz) + pose7[5];
     const double pc2 = X2 + w * tz + (x * ty - y * tx) + pose7[6];
     if (!(pc2 > kMinDepth)) return false;
-    const double xn = pc0 / pc2, yn = pc1 / pc2;
+    const double iz = 1.0 / pc2;
+    const double xn = pc0 * iz, yn = pc1 * iz;
     double u, v;
     switch (model) {
     case SFMBA_SIMPLE_PINHOLE: u = c[0] * xn + c[1]; v = c[0] * yn + c[2]; break;

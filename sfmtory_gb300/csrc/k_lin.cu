@@ -380,10 +380,18 @@ __global__ void __launch_bounds__(256) k_cost(const double *poses, const double 
         double rx, ry;
         if (residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2],
                        xy.x, xy.y, rx, ry)) {
-            const double n = sqrt(rx * rx + ry * ry);
-            if (mode == 0) sum += robust_weight<double>(n, loss, scale) * n * n;
-            else if (mode == 1) sum += n;
-            else sum += n * n;
+            const double n2 = rx * rx + ry * ry;
+            if (mode == 0) {
+                if (loss == SFMBA_LOSS_NONE) sum += n2;
+                else {
+                    const double n = sqrt(n2);
+                    sum += robust_weight<double>(n, loss, scale) * n * n;
+                }
+            } else if (mode == 1) {
+                sum += sqrt(n2);
+            } else {
+                sum += n2;
+            }
             ++cnt;
         }
     }

@@ -329,7 +329,7 @@ void put_vec(T *dst, const std::vector<T> &v, cudaStream_t s) {
 
 struct SolveOutput {
     double initial_cost = 0, final_cost = 0;
-    int iterations = 0, retries = 0, solver = SFMBA_SOLVER_DENSE;
+    int iterations = 0, retries = 0, solver = SFMBA_SOLVER_DENSE, polish_iteration = -1;
     long long linear_iterations = 0, valid_obs = 0;
     int n = 0;
 };
@@ -374,7 +374,10 @@ class Solver {
         if (solver_ == SFMBA_SOLVER_DENSE && nI > 65535)
             throw Error(SFMBA_ERR_UNSUPPORTED, "dense solver supports at most 65535 images; use the PCG solver");
         const int nID = nI * D;
-        const size_t tsz = mixed ? sizeof(float) : sizeof(double);
+        // The mixed path may finish in FP64 (fp64_polish): its typed buffers
+        // are sized for doubles so the same allocation serves both precisions.
+        const bool polish = mixed && o->fp64_polish;
+        const size_t tsz = (mixed && !polish) ? sizeof(float) : sizeof(double);
         const size_t RS = (size_t)((8 + 2 * D) + 3) / 4 * 4;
         size_t sort_tmp = sort_temp_bytes(std::max<long long>(nO, 1), std::max(nP, 1), nI);
         {
@@ -432,9 +435,9 @@ class Solver {
                 in_xy = A.take<double>((size_t)nO * 2);
             }
             if (need_system) {
-                const bool records = solver_ == SFMBA_SOLVER_DENSE || !mixed;
+                const bool records = solver_ == SFMBA_SOLVER_DENSE || !mixed || polish;
                 const long long nchunks = (nO + kChunkObs - 1) / kChunkObs;
-                b.img_lin = A.take<char>((size_t)nI * (mixed ? sizeof(ImageLin<float>) : sizeof(ImageLin<double>)));
+                b.img_lin = A.take<char>((size_t)nI * sizeof(ImageLin<double>));
                 b.rec = records ? A.take<char>((size_t)nO * RS * tsz) : nullptr;
                 b.ob_valid = A.take<unsigned char>(nO);
                 b.pt_C = A.take<char>((size_t)nP * 6 * tsz);
@@ -598,14 +601,14 @@ class Solver {
             out.valid_obs = init.valid_obs;
         }
         if (b.n == 0) return out;  // lib.rs:777-787
-        const bool mixed = b.mixed;
+        bool polish_pending = b.mixed && o->fp64_polish;
         for (int outer = 0; outer < o->max_iterations; ++outer) {
             ++out.iterations;
             { SFMBA_PHASE(PH_LM); launch_begin_outer(b, s_); }
             {
                 SFMBA_PHASE(PH_LINEARIZE);
                 launch_prepare_images(b, s_);
-                if (b.rec) launch_linearize(b, s_);
+                if (solver_ == SFMBA_SOLVER_DENSE || !b.mixed) launch_linearize(b, s_);
             }
             if (solver_ == SFMBA_SOLVER_DENSE) {
                 { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
@@ -617,6 +620,7 @@ class Solver {
             read_state();
             // lib.rs:855-857: no observation in front of its camera
             if (hs.valid_obs == 0) break;
+            const double lambda_start = hs.lambda, nu_start = hs.nu;
             bool accepted = false;
             for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
                 ++out.retries;
@@ -628,7 +632,7 @@ class Solver {
                     { SFMBA_PHASE(PH_FOLD); launch_fold_system(b, s_); }
                     { SFMBA_PHASE(PH_CHOLESKY); launch_cholesky(b, s_); }
                     { SFMBA_PHASE(PH_TRSV); launch_cholesky_solve(b, b.rhs, b.delta, s_); }
-                    if (mixed) {
+                    if (b.mixed) {
                         SFMBA_PHASE(PH_REFINE);
                         for (int k = 0; k < o->refinement_steps; ++k) launch_refine(b, s_);
                     }
@@ -665,12 +669,30 @@ class Solver {
                     break;
                 }
             }
-            if (!accepted) break;
-            out.final_cost = hs.cost;
-            out.valid_obs = hs.valid_obs;
-            const double rel = (hs.cost_before - hs.cost) / std::max(hs.cost_before, 1e-12);
-            if (rel < kFunctionTolerance) break;
-            if (o->target_cost > 0.0 && hs.cost <= o->target_cost) break;
+            bool stop = !accepted;
+            if (accepted) {
+                out.final_cost = hs.cost;
+                out.valid_obs = hs.valid_obs;
+                const double rel = (hs.cost_before - hs.cost) / std::max(hs.cost_before, 1e-12);
+                if (o->target_cost > 0.0 && hs.cost <= o->target_cost) break;
+                stop = rel < kFunctionTolerance;
+            }
+            if (!stop) continue;
+            if (polish_pending && std::isfinite(hs.cost)) {
+                // The FP32 loop would stop here (lib.rs:1215-1221 rules): continue the
+                // same loop in FP64. A failed iteration's damping growth is undone.
+                polish_pending = false;
+                b.mixed = 0;
+                out.polish_iteration = outer + 1;
+                if (!accepted) {
+                    SFMBA_CUDA(cudaMemcpyAsync(&b.state->lambda, &lambda_start, sizeof(double),
+                                               cudaMemcpyHostToDevice, s_));
+                    SFMBA_CUDA(cudaMemcpyAsync(&b.state->nu, &nu_start, sizeof(double), cudaMemcpyHostToDevice, s_));
+                    SFMBA_CUDA(cudaStreamSynchronize(s_));
+                }
+                continue;
+            }
+            break;
         }
         read_state();
         out.final_cost = hs.cost;
@@ -750,6 +772,7 @@ int bundle_adjust_impl(const sfmba_problem *p, const sfmba_options *o, sfmba_res
         r->iterations_run = out.iterations;
         r->damping_retries = out.retries;
         r->solver_used = out.solver;
+        r->polish_iteration = out.polish_iteration;
         r->linear_iterations = out.linear_iterations;
         r->reduced_dim = out.n;
         r->valid_observations = out.valid_obs;
@@ -783,6 +806,7 @@ void sfmba_default_options(sfmba_options *o) {
     o->refinement_steps = 1;
     o->target_cost = 0.0;
     o->dense_max_dim = 6000;
+    o->fp64_polish = 1;
 }
 
 int sfmba_bundle_adjust(const sfmba_problem *p, const sfmba_options *o, sfmba_result *r) {

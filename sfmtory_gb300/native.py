@@ -108,6 +108,7 @@ class Result:
         self.iterations_run = r.iterations_run
         self.damping_retries = r.damping_retries
         self.solver_used = r.solver_used
+        self.polish_iteration = r.polish_iteration
         self.linear_iterations = r.linear_iterations
         self.reduced_dim = r.reduced_dim
         self.valid_observations = r.valid_observations

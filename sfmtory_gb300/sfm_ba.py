@@ -159,6 +159,7 @@ class BaParams:
     pcg_tolerance: float = 0.1
     refinement_steps: int = 1
     target_cost: float = 0.0
+    fp64_polish: bool = True
 
     def to_options(self) -> abi.SfmbaOptions:
         return abi.default_options(
@@ -166,7 +167,8 @@ class BaParams:
             robust_loss=int(self.robust_loss), loss_scale_px=float(self.loss_scale_px),
             precision=int(self.precision), solver=int(self.solver),
             pcg_max_iterations=int(self.pcg_max_iterations), pcg_tolerance=float(self.pcg_tolerance),
-            refinement_steps=int(self.refinement_steps), target_cost=float(self.target_cost))
+            refinement_steps=int(self.refinement_steps), target_cost=float(self.target_cost),
+            fp64_polish=int(bool(self.fp64_polish)))
 
 
 @dataclass

@@ -1,0 +1,65 @@
+"""GPU path against the committed golden fixtures (through the C ABI).
+
+Bars: FP64 dense - initial cost 1e-12, final cost and parameters 1e-6
+relative, same iteration count; FP32 (mixed) - final cost 1e-6 relative;
+FP64 PCG with a tight tolerance - final cost 1e-6 relative; Jacobians FP64
+1e-9 relative.
+"""
+import numpy as np
+import pytest
+
+import golden_util as G
+from sfmtory_gb300 import abi, native, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_fp64_dense_matches_golden(name):
+    p, kw, exp = G.load(name)
+    r = native.bundle_adjust_arrays(p, solver=abi.SOLVER_DENSE, **kw)
+    assert abs(r.initial_cost - exp["initial_cost"]) <= 1e-12 * abs(exp["initial_cost"])
+    assert r.iterations_run == exp["iterations_run"]
+    if exp["final_cost"] > 1e-12:
+        assert abs(r.final_cost - exp["final_cost"]) <= 1e-6 * exp["final_cost"]
+        assert G.rel_err(r.points, exp["points"]) < 1e-6
+        assert G.rel_err(r.poses, exp["poses"]) < 1e-6
+        assert G.rel_err(r.camera_params, exp["camera_params"]) < 1e-6
+    else:  # noiseless fixture: compare the converged geometry
+        assert r.final_cost < 1e-12
+        assert np.allclose(r.points, exp["points"], atol=1e-8)
+
+
+@pytest.mark.parametrize("name", [n for n in G.CASES if n != "recovers_ground_truth"])
+def test_mixed_reaches_golden_cost(name):
+    """The mixed path (FP32 linearisation and Schur, FP64 cost, Cholesky and
+    polish) reaches the FP64 oracle's final cost to 1e-6 relative."""
+    p, kw, exp = G.load(name)
+    r = native.bundle_adjust_arrays(p, precision=abi.PRECISION_MIXED, solver=abi.SOLVER_DENSE, **kw)
+    assert r.final_cost <= exp["final_cost"] * (1 + 1e-6), (r.final_cost, exp["final_cost"], r.polish_iteration)
+
+
+@pytest.mark.parametrize("name", ["ring16_s005", "radial2000_s0005", "window_mixed_models"])
+def test_pcg_reaches_golden_cost(name):
+    p, kw, exp = G.load(name)
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        r = native.bundle_adjust_arrays(p, precision=prec, solver=abi.SOLVER_PCG, pcg_tolerance=1e-10,
+                                        pcg_max_iterations=2000, **kw)
+        assert r.final_cost <= exp["final_cost"] * (1 + 1e-6), (prec, r.final_cost, exp["final_cost"])
+
+
+def test_gpu_jacobians_match_golden():
+    z = G.jacobians()
+    from sfmtory_gb300.problem import Problem
+
+    for m, params in scenes.JACOBIAN_TEST_CAMERAS.items():
+        cp = np.zeros((1, 8))
+        cp[0, : len(params)] = params
+        p = Problem(camera_of_image=np.array([0], np.int32), camera_model=np.array([m], np.int32),
+                    camera_params=cp, poses=z["pose"][None], points=z["point"][None],
+                    obs_image=np.array([0], np.int32), obs_point=np.array([0], np.int32),
+                    obs_xy=np.array(z["obs"], np.float64)[None])
+        r, jp, jx, jc, valid = native.residuals_jacobians(p)
+        assert valid[0]
+        for got, key in ((r[0], "r"), (jp[0], "jp"), (jx[0], "jx"), (jc[0], "jc")):
+            assert G.rel_err(got, z[f"m{m}_{key}"]) < 1e-9
