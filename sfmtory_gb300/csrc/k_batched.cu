@@ -1,0 +1,937 @@
+// Batched local bundle adjustment: many independent windows concatenated
+// into one block-diagonal problem. Observation, point and image kernels are
+// shared with the single-problem path; this file holds what is per window:
+// the LM state, the damped point inverses, the dense reduced systems (Schur
+// reduction into per-window image-level blocks, fold to slot order, blocked
+// FP64 Cholesky and triangular solves, refinement), the per-window cost and
+// the accept / commit rules (crates/sfm-ba/src/lib.rs:914-1221, applied to
+// each window independently as sfm-reconstruction's BaScope::Local calls
+// would, lib.rs:1287-1299 there).
+#include <type_traits>
+
+#include "camera.cuh"
+#include "kernels.cuh"
+
+namespace sfmba {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ void kahan_add(T &s, T &c, T x) {
+    if constexpr (std::is_same<T, float>::value) {
+        const T y = x - c;
+        const T t = s + y;
+        c = (t - s) - y;
+        s = t;
+    } else {
+        s += x;
+    }
+}
+
+constexpr int NB = kCholNB;
+constexpr int LD = NB + 1;
+
+__global__ void k_wb_window_of_points(const int *win_in, const int *perm, int nP, int *pt_win) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < nP) pt_win[p] = win_in[perm[p]];
+}
+
+// After the initial cost: damping lambda0, nu = 2 (lib.rs:801-802); a window
+// without unknowns returns at once (lib.rs:777-787).
+__global__ void k_wb_init(WinState *ws, const int *n_w, int W, double lambda0) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    s.lambda = lambda0;
+    s.nu = 2.0;
+    s.initial_cost = s.cost;
+    s.cost_before = s.cost;
+    s.lambda_start = lambda0;
+    s.nu_start = 2.0;
+    s.iterations = s.retries = s.retries_outer = 0;
+    s.accepted = s.accepted_outer = s.active = 0;
+    s.factor_failed = s.solve_failed = 0;
+    s.done = n_w[w] == 0 ? 1 : 0;
+    s.wants_polish = s.polished = 0;
+    s.polish_iteration = -1;
+}
+
+__global__ void k_wb_begin_outer(WinState *ws, int W, int max_iterations) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    s.accepted_outer = 0;
+    s.retries_outer = 0;
+    if (s.done) return;
+    if (s.iterations >= max_iterations) {
+        s.done = 1;
+        return;
+    }
+    s.iterations += 1;
+    s.cost_before = s.cost;
+    s.lambda_start = s.lambda;
+    s.nu_start = s.nu;
+    if (s.valid_obs == 0) s.done = 1;  // lib.rs:855-857
+}
+
+__global__ void k_wb_begin_retry(WinState *ws, int W) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    s.accepted = 0;
+    s.factor_failed = 0;
+    s.solve_failed = 0;
+    s.active = (!s.done && !s.accepted_outer && s.retries_outer < kMaxDampingRetries) ? 1 : 0;
+    if (s.active) {
+        s.retries += 1;
+        s.retries_outer += 1;
+    }
+}
+
+// Damped point inverses with the damping of the point's window.
+template <typename T>
+__global__ void k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_nfree, const int *pt_win,
+                                   const WinState *ws, int nP, T *pt_Cinv, T *pt_h, unsigned char *pt_ok) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nP) return;
+    const double lam = ws[pt_win[p]].lambda;
+    const T *C = pt_C + 6 * (size_t)p;
+    double m00 = C[0], m01 = C[1], m02 = C[2], m11 = C[3], m12 = C[4], m22 = C[5];
+    m00 = m00 + m00 * lam; m11 = m11 + m11 * lam; m22 = m22 + m22 * lam;
+    const double c00 = m11 * m22 - m12 * m12;
+    const double c01 = m12 * m02 - m01 * m22;
+    const double c02 = m01 * m12 - m11 * m02;
+    const double det = m00 * c00 + m01 * c01 + m02 * c02;
+    const bool ok = pt_nfree[p] > 0 && det != 0.0;
+    T *Ci = pt_Cinv + 6 * (size_t)p;
+    T *h = pt_h + 3 * (size_t)p;
+    if (!ok) {
+        for (int k = 0; k < 6; ++k) Ci[k] = T(0);
+        h[0] = h[1] = h[2] = T(0);
+        pt_ok[p] = 0;
+        return;
+    }
+    const double id = 1.0 / det;
+    const double i00 = c00 * id, i01 = c01 * id, i02 = c02 * id;
+    const double i11 = (m00 * m22 - m02 * m02) * id;
+    const double i12 = (m02 * m01 - m00 * m12) * id;
+    const double i22 = (m00 * m11 - m01 * m01) * id;
+    Ci[0] = (T)i00; Ci[1] = (T)i01; Ci[2] = (T)i02; Ci[3] = (T)i11; Ci[4] = (T)i12; Ci[5] = (T)i22;
+    const T *g = pt_g + 3 * (size_t)p;
+    const double g0 = g[0], g1 = g[1], g2 = g[2];
+    h[0] = (T)(i00 * g0 + i01 * g1 + i02 * g2);
+    h[1] = (T)(i01 * g0 + i11 * g1 + i12 * g2);
+    h[2] = (T)(i02 * g0 + i12 * g1 + i22 * g2);
+    pt_ok[p] = 1;
+}
+
+constexpr int kWarps = 2;
+
+// Schur reduction of the image pairs of every window (one warp per pair),
+// written into the window's image-level block matrix. Pairs of windows that
+// are not retrying are skipped.
+template <typename T, int D>
+__global__ void __launch_bounds__(32 * kWarps)
+    k_wb_schur_pairs(const T *__restrict__ rec, const int2 *__restrict__ pairs, const int *__restrict__ group_start,
+                     const int2 *__restrict__ group_ij, int ngroups, const int *__restrict__ ob_pt,
+                     const T *__restrict__ pt_Cinv, const unsigned char *__restrict__ pt_ok,
+                     const double *__restrict__ img_H, const int *__restrict__ img_win,
+                     const int *__restrict__ img_base, const int *__restrict__ nid_w,
+                     const long long *__restrict__ simg_off, const WinState *__restrict__ ws,
+                     double *__restrict__ S_img) {
+    constexpr int RS = RecLayout<D>::kStride;
+    constexpr int NE = (D * D + 31) / 32;
+    __shared__ T sM[kWarps][32][4];
+    __shared__ T sA[kWarps][32][2 * D];
+    __shared__ T sB[kWarps][32][2 * D];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = blockIdx.x * kWarps + wl;
+    if (g >= ngroups) return;
+    const int2 ij = group_ij[g];
+    const int w = img_win[ij.x];
+    if (!ws[w].active) return;
+    const int gs = group_start[g], ge = group_start[g + 1];
+    T acc[NE], comp[NE];
+#pragma unroll
+    for (int k = 0; k < NE; ++k) acc[k] = comp[k] = T(0);
+    for (int base = gs; base < ge; base += 32) {
+        const int e = base + lane;
+        if (e < ge) {
+            const int2 ab = pairs[e];
+            const int p = ob_pt[ab.x];
+            const T *ra = rec + (size_t)ab.x * RS;
+            const T *rb = rec + (size_t)ab.y * RS;
+            if (pt_ok[p]) {
+                const T *Ci = pt_Cinv + 6 * (size_t)p;
+                T U[2][3];
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const T x0 = ra[2 + 3 * r], x1 = ra[3 + 3 * r], x2 = ra[4 + 3 * r];
+                    U[r][0] = x0 * Ci[0] + x1 * Ci[1] + x2 * Ci[2];
+                    U[r][1] = x0 * Ci[1] + x1 * Ci[3] + x2 * Ci[4];
+                    U[r][2] = x0 * Ci[2] + x1 * Ci[4] + x2 * Ci[5];
+                }
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+                        sM[wl][lane][2 * r + q] = U[r][0] * rb[2 + 3 * q] + U[r][1] * rb[3 + 3 * q] + U[r][2] * rb[4 + 3 * q];
+#pragma unroll
+                for (int f = 0; f < 2 * D; ++f) {
+                    sA[wl][lane][f] = ra[8 + f];
+                    sB[wl][lane][f] = rb[8 + f];
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sM[wl][lane][q] = T(0);
+#pragma unroll
+                for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = sB[wl][lane][f] = T(0);
+            }
+        }
+        __syncwarp();
+        const int cnt = min(32, ge - base);
+        for (int t = 0; t < cnt; ++t) {
+            const T m0 = sM[wl][t][0], m1 = sM[wl][t][1], m2 = sM[wl][t][2], m3 = sM[wl][t][3];
+#pragma unroll
+            for (int k = 0; k < NE; ++k) {
+                const int idx = lane + 32 * k;
+                if (idx < D * D) {
+                    const int r = idx / D, c = idx - r * D;
+                    const T b0 = sB[wl][t][c], b1 = sB[wl][t][D + c];
+                    kahan_add(acc[k], comp[k],
+                              sA[wl][t][r] * (m0 * b0 + m1 * b1) + sA[wl][t][D + r] * (m2 * b0 + m3 * b1));
+                }
+            }
+        }
+        __syncwarp();
+    }
+    const int li = ij.x - img_base[w], lj = ij.y - img_base[w];
+    const int nid = nid_w[w];
+    double *Sw = S_img + simg_off[w];
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+        const int idx = lane + 32 * k;
+        if (idx < D * D) {
+            const int r = idx / D, c = idx - r * D;
+            const double v = -((double)acc[k] - (double)comp[k]);
+            if (li == lj) {
+                Sw[(size_t)(li * D + r) * nid + li * D + c] = img_H[(size_t)ij.x * D * D + r * D + c] + v;
+            } else {
+                Sw[(size_t)(li * D + r) * nid + lj * D + c] = v;
+                Sw[(size_t)(lj * D + c) * nid + li * D + r] = v;
+            }
+        }
+    }
+}
+
+// Window w's slot-order system: S[a][b] from its image-level blocks, damping
+// with the window's lambda, masks, symmetrisation. Grid: (column blocks, row, window).
+__global__ void k_wb_fold(const double *__restrict__ S_img, const long long *__restrict__ simg_off,
+                          const int *__restrict__ nid_w, const int *__restrict__ n_w,
+                          const int *__restrict__ slot_base, const long long *__restrict__ s_off,
+                          const int *__restrict__ img_base, int D, const int *__restrict__ pre_start,
+                          const int *__restrict__ pre, const unsigned char *__restrict__ masked,
+                          const double *__restrict__ diagB, const WinState *__restrict__ ws,
+                          double *__restrict__ S, double *__restrict__ L) {
+    const int w = blockIdx.z;
+    if (!ws[w].active) return;
+    const int n = n_w[w];
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = blockIdx.y;
+    if (a >= n || b >= n) return;
+    const int ga = slot_base[w] + a, gb = slot_base[w] + b;
+    const int nid = nid_w[w];
+    const int ub = img_base[w] * D;  // first image-level index of the window
+    const double *Sw = S_img + simg_off[w];
+    double v;
+    if (masked[ga] || masked[gb]) {
+        v = a == b ? 1.0 : 0.0;
+    } else {
+        double vab = 0.0, vba = 0.0;
+        for (int x = pre_start[ga]; x < pre_start[ga + 1]; ++x)
+            for (int y = pre_start[gb]; y < pre_start[gb + 1]; ++y) {
+                const int ux = pre[x] - ub, uy = pre[y] - ub;
+                vab += Sw[(size_t)ux * nid + uy];
+                vba += Sw[(size_t)uy * nid + ux];
+            }
+        v = 0.5 * (vab + vba);
+        if (a == b) v += diagB[ga] * ws[w].lambda;
+    }
+    S[s_off[w] + (size_t)a * n + b] = v;
+    L[s_off[w] + (size_t)a * n + b] = v;
+}
+
+// ---- batched blocked Cholesky (one matrix per window, leading dim n_w)
+
+__global__ void __launch_bounds__(256) k_wb_chol_diag(double *Lall, const long long *s_off, const int *n_w,
+                                                       double *Linv_all, const long long *linv_off, int k0,
+                                                       WinState *ws) {
+    extern __shared__ double sm[];
+    double *A = sm;
+    double *X = sm + NB * LD;
+    __shared__ int fail;
+    const int w = blockIdx.x;
+    const int n = n_w[w];
+    if (!ws[w].active || ws[w].factor_failed || k0 >= n) return;
+    double *L = Lall + s_off[w];
+    const int nb = min(NB, n - k0);
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        A[r * LD + c] = c <= r ? L[(size_t)(k0 + r) * n + k0 + c] : 0.0;
+    }
+    if (tid == 0) fail = 0;
+    __syncthreads();
+    for (int j = 0; j < nb; ++j) {
+        if (tid == 0) {
+            const double d = A[j * LD + j];
+            if (!(d > 0.0)) fail = 1;
+            else A[j * LD + j] = sqrt(d);
+        }
+        __syncthreads();
+        if (fail) break;
+        const double piv = A[j * LD + j];
+        for (int i = j + 1 + tid; i < nb; i += blockDim.x) A[i * LD + j] /= piv;
+        __syncthreads();
+        const int m = nb - j - 1;
+        for (int idx = tid; idx < m * m; idx += blockDim.x) {
+            const int i = j + 1 + idx / m, l = j + 1 + idx % m;
+            if (l <= i) A[i * LD + l] -= A[i * LD + j] * A[l * LD + j];
+        }
+        __syncthreads();
+    }
+    if (fail) {
+        if (tid == 0) ws[w].factor_failed = 1;
+        return;
+    }
+    for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        if (c <= r) L[(size_t)(k0 + r) * n + k0 + c] = A[r * LD + c];
+    }
+    if (tid < nb) {
+        const int c = tid;
+        for (int r = 0; r < c; ++r) X[r * LD + c] = 0.0;
+        for (int r = c; r < nb; ++r) {
+            double s = r == c ? 1.0 : 0.0;
+            for (int k = c; k < r; ++k) s -= A[r * LD + k] * X[k * LD + c];
+            X[r * LD + c] = s / A[r * LD + r];
+        }
+    }
+    __syncthreads();
+    double *out = Linv_all + linv_off[w] + (size_t)(k0 / NB) * NB * NB;
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+        const int r = idx / NB, c = idx - r * NB;
+        out[idx] = (r < nb && c < nb) ? X[r * LD + c] : 0.0;
+    }
+}
+
+constexpr int PANEL_ROWS = 32;
+
+__global__ void __launch_bounds__(256) k_wb_chol_panel(double *Lall, const long long *s_off, const int *n_w,
+                                                        const double *Linv_all, const long long *linv_off, int k0,
+                                                        const WinState *ws) {
+    extern __shared__ double sm[];
+    double *Li = sm;
+    double *R = sm + NB * LD;
+    const int w = blockIdx.y;
+    const int n = n_w[w];
+    if (!ws[w].active || ws[w].factor_failed || k0 >= n) return;
+    double *L = Lall + s_off[w];
+    const int nb = min(NB, n - k0);
+    const int r0 = k0 + nb + blockIdx.x * PANEL_ROWS;
+    const int rows = min(PANEL_ROWS, n - r0);
+    if (rows <= 0) return;
+    const double *inv = Linv_all + linv_off[w] + (size_t)(k0 / NB) * NB * NB;
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Li[(idx / NB) * LD + idx % NB] = inv[idx];
+    for (int idx = threadIdx.x; idx < rows * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        R[r * LD + c] = L[(size_t)(r0 + r) * n + k0 + c];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < rows * nb; idx += blockDim.x) {
+        const int r = idx / nb, c = idx - r * nb;
+        double s = 0.0;
+        for (int t = 0; t <= c; ++t) s += R[r * LD + t] * Li[c * LD + t];
+        L[(size_t)(r0 + r) * n + k0 + c] = s;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_wb_chol_update(double *Lall, const long long *s_off, const int *n_w, int k0,
+                                                         const WinState *ws) {
+    extern __shared__ double sm[];
+    double *Pi = sm;
+    double *Pj = sm + NB * LD;
+    const int w = blockIdx.y;
+    const int n = n_w[w];
+    if (!ws[w].active || ws[w].factor_failed || k0 + NB >= n) return;
+    double *L = Lall + s_off[w];
+    const int t0 = k0 + NB;
+    const long long q = blockIdx.x;
+    int ti = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while ((long long)(ti + 1) * (ti + 2) / 2 <= q) ++ti;
+    while ((long long)ti * (ti + 1) / 2 > q) --ti;
+    const int tj = (int)(q - (long long)ti * (ti + 1) / 2);
+    const int ri = t0 + ti * NB, rj = t0 + tj * NB;
+    if (ri >= n || rj >= n) return;
+    const int mi = min(NB, n - ri), mj = min(NB, n - rj);
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+        const int r = idx / NB, c = idx - r * NB;
+        Pi[r * LD + c] = r < mi ? L[(size_t)(ri + r) * n + k0 + c] : 0.0;
+        Pj[r * LD + c] = r < mj ? L[(size_t)(rj + r) * n + k0 + c] : 0.0;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int t = 0; t < NB; ++t) {
+        double x[4], y[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) x[a] = Pi[(ty * 4 + a) * LD + t];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) y[b] = Pj[(tx + 16 * b) * LD + t];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] += x[a] * y[b];
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int r = ty * 4 + a;
+        if (r >= mi) continue;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int c = tx + 16 * b;
+            if (c >= mj) continue;
+            if (ti == tj && c > r) continue;
+            L[(size_t)(ri + r) * n + rj + c] -= acc[a][b];
+        }
+    }
+}
+
+// Whole triangular solve L L^T x = b of window w in one CTA (windows are at
+// most a few hundred unknowns): forward with the diagonal-block inverses,
+// then backward; b and x are the window's slices of the slot vectors.
+__global__ void __launch_bounds__(256) k_wb_chol_solve(const double *Lall, const long long *s_off, const int *n_w,
+                                                        const double *Linv_all, const long long *linv_off,
+                                                        const int *slot_base, const double *rhs, double *work,
+                                                        double *x, const WinState *ws) {
+    __shared__ double yk[NB];
+    const int w = blockIdx.x;
+    if (!ws[w].active || ws[w].factor_failed) return;
+    const int n = n_w[w];
+    if (n == 0) return;
+    const double *L = Lall + s_off[w];
+    const double *Linv = Linv_all + linv_off[w];
+    double *b = work + slot_base[w];
+    double *xo = x + slot_base[w];
+    for (int a = threadIdx.x; a < n; a += blockDim.x) b[a] = rhs[slot_base[w] + a];
+    __syncthreads();
+    // forward: y_k = Lkk^-1 b_k; b_r -= L[r, k] y_k for r below
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int nb = min(NB, n - k0);
+        const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
+        if (threadIdx.x < nb) {
+            double s = 0.0;
+            for (int t = 0; t <= (int)threadIdx.x; ++t) s += inv[threadIdx.x * NB + t] * b[k0 + t];
+            yk[threadIdx.x] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x < nb) b[k0 + threadIdx.x] = yk[threadIdx.x];
+        for (int r = k0 + nb + threadIdx.x; r < n; r += blockDim.x) {
+            double s = 0.0;
+            for (int t = 0; t < nb; ++t) s += L[(size_t)r * n + k0 + t] * yk[t];
+            b[r] -= s;
+        }
+        __syncthreads();
+    }
+    // backward: x_k = Lkk^-T y_k; y_r -= L[k, r]^T x_k for r above
+    for (int k0 = ((n - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
+        const int nb = min(NB, n - k0);
+        const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
+        if (threadIdx.x < nb) {
+            double s = 0.0;
+            for (int r = threadIdx.x; r < nb; ++r) s += inv[r * NB + threadIdx.x] * b[k0 + r];
+            yk[threadIdx.x] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x < nb) xo[k0 + threadIdx.x] = yk[threadIdx.x];
+        for (int r = threadIdx.x; r < k0; r += blockDim.x) {
+            double s = 0.0;
+            for (int t = 0; t < nb; ++t) s += L[(size_t)(k0 + t) * n + r] * yk[t];
+            b[r] -= s;
+        }
+        __syncthreads();
+    }
+}
+
+// res = rhs - S x for window w (one CTA per window), the FP64 residual of
+// one refinement step.
+__global__ void __launch_bounds__(256) k_wb_residual(const double *Sall, const long long *s_off, const int *n_w,
+                                                      const int *slot_base, const double *x, const double *rhs,
+                                                      double *res, const WinState *ws) {
+    const int w = blockIdx.x;
+    if (!ws[w].active || ws[w].factor_failed) return;
+    const int n = n_w[w];
+    const double *S = Sall + s_off[w];
+    const double *xw = x + slot_base[w];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r < n; r += blockDim.x >> 5) {
+        double s = 0.0;
+        for (int c = lane; c < n; c += 32) s += S[(size_t)r * n + c] * xw[c];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) res[slot_base[w] + r] = rhs[slot_base[w] + r] - s;
+    }
+}
+
+__global__ void k_wb_axpy(const int *slot_win, int n, const double *c, double *x, const WinState *ws) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const WinState &s = ws[slot_win[a]];
+    if (s.active && !s.factor_failed) x[a] += c[a];
+}
+
+// Per-window FP64 cost: one CTA per window over its observations (windows
+// are contiguous in point-major order). mode 0 -> cost, 1 -> trial_cost.
+__global__ void __launch_bounds__(256) k_wb_cost(const double *poses, const double *cams, const double *points,
+                                                  const int *cam_of_img, const int *cam_model, const int *ob_img,
+                                                  const int *ob_pt, const double2 *ob_xy, const long long *obs_off,
+                                                  int loss, double scale, int into_trial, WinState *ws) {
+    __shared__ double ssum[256];
+    __shared__ long long scnt[256];
+    const int w = blockIdx.x;
+    if (into_trial && !(ws[w].active && !ws[w].factor_failed)) return;
+    double sum = 0.0;
+    long long cnt = 0;
+    for (long long o = obs_off[w] + threadIdx.x; o < obs_off[w + 1]; o += blockDim.x) {
+        const int i = ob_img[o], p = ob_pt[o];
+        const int c = cam_of_img[i];
+        const double *X = points + 3 * (size_t)p;
+        const double2 xy = ob_xy[o];
+        double rx, ry;
+        if (residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2], xy.x, xy.y,
+                       rx, ry)) {
+            const double n2 = rx * rx + ry * ry;
+            if (loss == SFMBA_LOSS_NONE) sum += n2;
+            else {
+                const double nn = sqrt(n2);
+                sum += robust_weight<double>(nn, loss, scale) * nn * nn;
+            }
+            ++cnt;
+        }
+    }
+    ssum[threadIdx.x] = sum;
+    scnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            ssum[threadIdx.x] += ssum[threadIdx.x + s];
+            scnt[threadIdx.x] += scnt[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (into_trial) {
+            ws[w].trial_cost = ssum[0];
+            ws[w].trial_valid_obs = scnt[0];
+        } else {
+            ws[w].cost = ssum[0];
+            ws[w].valid_obs = scnt[0];
+        }
+    }
+}
+
+// Accept / reject per retrying window (lib.rs:1188-1212); a window decided
+// here leaves the retry round.
+__global__ void k_wb_accept(WinState *ws, int W) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    if (!s.active || s.factor_failed) return;
+    const double t = s.trial_cost;
+    if (isfinite(t) && t < s.cost) {
+        s.accepted = 1;
+        s.accepted_outer = 1;
+        s.cost = t;
+        s.valid_obs = s.trial_valid_obs;
+        s.lambda = fmax(s.lambda / 3.0, 1e-12);
+        s.nu = 2.0;
+    } else {
+        s.lambda *= s.nu;
+        s.nu *= 2.0;
+    }
+    s.active = 0;
+}
+
+// Windows whose Cholesky and LU both failed: grow the damping (lib.rs:1089-1091).
+__global__ void k_wb_reject_failed(WinState *ws, int W) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    if (!s.active || !s.factor_failed) return;
+    s.lambda *= s.nu;
+    s.nu *= 2.0;
+    s.active = 0;
+}
+
+// Trial parameters of the windows accepted in this retry become current.
+__global__ void k_wb_commit(const WinState *ws, const int *pt_win, const int *img_win, const int *cam_win, int nI,
+                            int nC, int nP, const double *poses_trial, const double *cams_trial,
+                            const double *points_trial, double *poses, double *cams, double *points,
+                            float4 *points32) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < nP && ws[pt_win[t]].accepted) {
+        const double x = points_trial[3 * t], y = points_trial[3 * t + 1], z = points_trial[3 * t + 2];
+        points[3 * t] = x; points[3 * t + 1] = y; points[3 * t + 2] = z;
+        if (points32) points32[t] = make_float4((float)x, (float)y, (float)z, 0.f);
+    }
+    if (t < 7LL * nI && ws[img_win[t / 7]].accepted) poses[t] = poses_trial[t];
+    if (t < 8LL * nC && ws[cam_win[t / 8]].accepted) cams[t] = cams_trial[t];
+}
+
+// End of an outer iteration (lib.rs:1215-1221): a window with no accepted
+// retry, or a relative decrease below 1e-6, stops. On the mixed path with
+// the FP64 polish it is parked instead (damping of a failed iteration
+// restored) until the whole batch continues in FP64.
+__global__ void k_wb_end_outer(WinState *ws, int W, int max_iterations, int polish_allowed, double target_cost) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    if (s.done) return;
+    bool stop;
+    if (!s.accepted_outer) {
+        stop = true;
+    } else {
+        if (target_cost > 0.0 && s.cost <= target_cost) {
+            s.done = 1;
+            return;
+        }
+        const double rel = (s.cost_before - s.cost) / fmax(s.cost_before, 1e-12);
+        stop = rel < kFunctionTolerance;
+    }
+    if (stop && polish_allowed && !s.polished && isfinite(s.cost) && s.iterations < max_iterations) {
+        s.wants_polish = 1;
+        s.polish_iteration = s.iterations;
+        if (!s.accepted_outer) {
+            s.lambda = s.lambda_start;
+            s.nu = s.nu_start;
+        }
+        s.done = 1;
+        return;
+    }
+    if (stop || s.iterations >= max_iterations) s.done = 1;
+}
+
+__global__ void k_wb_start_polish(WinState *ws, int W) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    s.polished = 1;
+    if (s.wants_polish) {
+        s.wants_polish = 0;
+        s.done = 0;
+    }
+}
+
+// Batch summary for the host (one block); clears the per-retry accept flags
+// once the commit has consumed them.
+__global__ void __launch_bounds__(256) k_wb_summary(WinState *ws, int W, int *counts) {
+    __shared__ int red[4][256];
+    int c[4] = {0, 0, 0, 0};
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+        WinState &s = ws[w];
+        s.accepted = 0;
+        c[WB_NOT_DONE] += !s.done;
+        c[WB_RETRY_PENDING] += (!s.done && !s.accepted_outer && s.retries_outer < kMaxDampingRetries);
+        c[WB_FACTOR_FAILED] += (s.active && s.factor_failed);
+        c[WB_WANTS_POLISH] += s.wants_polish;
+    }
+    for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = c[k];
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h)
+            for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) counts[threadIdx.x] = red[threadIdx.x][0];
+}
+
+// Partial-pivoting LU of the windows whose Cholesky failed (lib.rs:1084-1092),
+// one block per window, then the solve. Column k pivots on the first
+// maximum |a|; a zero column is skipped and leaves a zero on U's diagonal,
+// which fails the solve (lambda then grows). Success clears factor_failed.
+__global__ void __launch_bounds__(1024) k_wb_lu(const double *Sall, double *Lall, const long long *s_off,
+                                                 const int *n_w, const int *slot_base, int *perm_all,
+                                                 const double *rhs, double *x, WinState *ws) {
+    __shared__ double bv[1024];
+    __shared__ int bi[1024];
+    __shared__ double red[32];
+    __shared__ int bad;
+    const int w = blockIdx.x;
+    WinState &st = ws[w];
+    if (!st.active || !st.factor_failed || st.solve_failed) return;
+    const int n = n_w[w];
+    const double *S = Sall + s_off[w];
+    double *A = Lall + s_off[w];
+    int *perm = perm_all + slot_base[w];
+    const double *b = rhs + slot_base[w];
+    double *xo = x + slot_base[w];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (long long i = tid; i < (long long)n * n; i += blockDim.x) A[i] = S[i];
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        double best = -1.0;
+        int besti = k;
+        for (int r = k + tid; r < n; r += blockDim.x) {
+            const double v = fabs(A[(size_t)r * n + k]);
+            if (v > best) { best = v; besti = r; }
+        }
+        bv[tid] = best;
+        bi[tid] = besti;
+        __syncthreads();
+        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+            if (tid < h) {
+                const double o = bv[tid + h];
+                const int oi = bi[tid + h];
+                if (o > bv[tid] || (o == bv[tid] && oi < bi[tid])) { bv[tid] = o; bi[tid] = oi; }
+            }
+            __syncthreads();
+        }
+        const int piv = bi[0];
+        const double diag = A[(size_t)piv * n + k];
+        __syncthreads();
+        if (diag == 0.0) {
+            if (tid == 0) perm[k] = -1;
+            continue;
+        }
+        if (piv != k)
+            for (int c = tid; c < n; c += blockDim.x) {
+                const double t = A[(size_t)k * n + c];
+                A[(size_t)k * n + c] = A[(size_t)piv * n + c];
+                A[(size_t)piv * n + c] = t;
+            }
+        if (tid == 0) perm[k] = piv;
+        __syncthreads();
+        for (int r = k + 1 + tid; r < n; r += blockDim.x) A[(size_t)r * n + k] /= diag;
+        __syncthreads();
+        const int m = n - k - 1;
+        for (long long idx = tid; idx < (long long)m * m; idx += blockDim.x) {
+            const int r = k + 1 + (int)(idx / m), c = k + 1 + (int)(idx % m);
+            A[(size_t)r * n + c] -= A[(size_t)r * n + k] * A[(size_t)k * n + c];
+        }
+        __syncthreads();
+    }
+    for (int a = tid; a < n; a += blockDim.x) xo[a] = b[a];
+    __syncthreads();
+    if (tid == 0)
+        for (int k = 0; k < n; ++k)
+            if (perm[k] >= 0 && perm[k] != k) {
+                const double t = xo[k];
+                xo[k] = xo[perm[k]];
+                xo[perm[k]] = t;
+            }
+    __syncthreads();
+    // forward (unit lower), then backward (upper); block reductions per row
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int q = 0; q < n; ++q) {
+            const int i = pass == 0 ? q : n - 1 - q;
+            const int lo = pass == 0 ? 0 : i + 1, hi = pass == 0 ? i : n;
+            double sum = 0.0;
+            for (int k = lo + tid; k < hi; k += blockDim.x) sum += A[(size_t)i * n + k] * xo[k];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+            if (lane == 0) red[warp] = sum;
+            __syncthreads();
+            if (tid == 0) {
+                double t = 0.0;
+                for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+                if (pass == 0) {
+                    xo[i] -= t;
+                } else {
+                    const double d = A[(size_t)i * n + i];
+                    if (d == 0.0) bad = 1;
+                    else xo[i] = (xo[i] - t) / d;
+                }
+            }
+            __syncthreads();
+            if (bad) break;
+        }
+    }
+    if (tid == 0) {
+        if (bad) st.solve_failed = 1;
+        else st.factor_failed = 0;
+    }
+}
+
+template <typename F>
+void dispatch_D(int D, F &&f) {
+    switch (D) {
+    case 6: f(std::integral_constant<int, 6>()); break;
+    case 9: f(std::integral_constant<int, 9>()); break;
+    case 10: f(std::integral_constant<int, 10>()); break;
+    case 11: f(std::integral_constant<int, 11>()); break;
+    case 14: f(std::integral_constant<int, 14>()); break;
+    default: throw Error(SFMBA_ERR_INTERNAL, "unsupported image block width");
+    }
+}
+
+const size_t kSmemTwoTiles = 2 * NB * LD * sizeof(double);
+const size_t kSmemPanel = (NB + PANEL_ROWS) * LD * sizeof(double);
+
+void set_smem_limits() {
+    static bool done = false;
+    if (done) return;
+    SFMBA_CUDA(cudaFuncSetAttribute(k_wb_chol_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTwoTiles));
+    SFMBA_CUDA(cudaFuncSetAttribute(k_wb_chol_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTwoTiles));
+    SFMBA_CUDA(cudaFuncSetAttribute(k_wb_chol_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPanel));
+    done = true;
+}
+
+int grid1(int n) { return div_up(n > 0 ? n : 1, 128); }
+
+}  // namespace
+
+void launch_wb_window_of_points(const int *win_of_input_point, const int *perm, int nP, int *pt_win,
+                                cudaStream_t s) {
+    if (nP == 0) return;
+    k_wb_window_of_points<<<div_up(nP, 256), 256, 0, s>>>(win_of_input_point, perm, nP, pt_win);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_init(const WinBufs &w, double initial_lambda, cudaStream_t s) {
+    k_wb_init<<<grid1(w.W), 128, 0, s>>>(w.ws, w.n_w, w.W, initial_lambda);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_begin_outer(const WinBufs &w, int max_iterations, cudaStream_t s) {
+    k_wb_begin_outer<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W, max_iterations);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_begin_retry(const WinBufs &w, cudaStream_t s) {
+    k_wb_begin_retry<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    if (b.nP == 0) return;
+    if (b.mixed)
+        k_wb_point_inverse<float><<<div_up(b.nP, 256), 256, 0, s>>>((const float *)b.pt_C, (const float *)b.pt_g,
+                                                                    b.pt_nfree, w.pt_win, w.ws, b.nP,
+                                                                    (float *)b.pt_Cinv, (float *)b.pt_h, b.pt_ok);
+    else
+        k_wb_point_inverse<double><<<div_up(b.nP, 256), 256, 0, s>>>((const double *)b.pt_C, (const double *)b.pt_g,
+                                                                     b.pt_nfree, w.pt_win, w.ws, b.nP,
+                                                                     (double *)b.pt_Cinv, (double *)b.pt_h, b.pt_ok);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    if (b.ngroups == 0) return;
+    dispatch_D(b.D, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        const int grid = div_up(b.ngroups, kWarps);
+        if (b.mixed)
+            k_wb_schur_pairs<float, D><<<grid, 32 * kWarps, 0, s>>>(
+                (const float *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt, (const float *)b.pt_Cinv,
+                b.pt_ok, b.img_H, w.img_win, w.img_base, w.nid_w, w.simg_off, w.ws, b.S_img);
+        else
+            k_wb_schur_pairs<double, D><<<grid, 32 * kWarps, 0, s>>>(
+                (const double *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
+                (const double *)b.pt_Cinv, b.pt_ok, b.img_H, w.img_win, w.img_base, w.nid_w, w.simg_off, w.ws,
+                b.S_img);
+    });
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_fold(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    if (w.max_n == 0) return;
+    dim3 grid(div_up(w.max_n, 128), w.max_n, w.W);
+    k_wb_fold<<<grid, 128, 0, s>>>(b.S_img, w.simg_off, w.nid_w, w.n_w, w.slot_base, w.s_off, w.img_base, b.D,
+                                   b.slot_pre_start, b.slot_pre, b.slot_masked, b.diagB, w.ws, b.S, b.L);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_cholesky(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    set_smem_limits();
+    for (int k0 = 0; k0 < w.max_n; k0 += NB) {
+        k_wb_chol_diag<<<w.W, 256, kSmemTwoTiles, s>>>(b.L, w.s_off, w.n_w, b.Linv, w.linv_off, k0, w.ws);
+        SFMBA_LAUNCH_CHECK();
+        const int rem = w.max_n - k0 - NB;
+        if (rem <= 0) break;
+        dim3 gp(div_up(rem, PANEL_ROWS), w.W);
+        k_wb_chol_panel<<<gp, 256, kSmemPanel, s>>>(b.L, w.s_off, w.n_w, b.Linv, w.linv_off, k0, w.ws);
+        SFMBA_LAUNCH_CHECK();
+        const long long tiles = div_up(rem, NB);
+        dim3 gu((unsigned)(tiles * (tiles + 1) / 2), w.W);
+        k_wb_chol_update<<<gu, 256, kSmemTwoTiles, s>>>(b.L, w.s_off, w.n_w, k0, w.ws);
+        SFMBA_LAUNCH_CHECK();
+    }
+}
+
+void launch_wb_solve(const Bufs &b, const WinBufs &w, const double *rhs, double *x, cudaStream_t s) {
+    k_wb_chol_solve<<<w.W, 256, 0, s>>>(b.L, w.s_off, w.n_w, b.Linv, w.linv_off, w.slot_base, rhs, b.work, x, w.ws);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_refine(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    k_wb_residual<<<w.W, 256, 0, s>>>(b.S, w.s_off, w.n_w, w.slot_base, b.delta, b.rhs, b.ref_res, w.ws);
+    SFMBA_LAUNCH_CHECK();
+    launch_wb_solve(b, w, b.ref_res, b.ref_corr, s);
+    if (b.n > 0) {
+        k_wb_axpy<<<div_up(b.n, 256), 256, 0, s>>>(w.slot_win, b.n, b.ref_corr, b.delta, w.ws);
+        SFMBA_LAUNCH_CHECK();
+    }
+}
+
+void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s) {
+    k_wb_cost<<<w.W, 256, 0, s>>>(trial ? b.poses_trial : b.poses, trial ? b.cams_trial : b.cams,
+                                  trial ? b.points_trial : b.points, b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt,
+                                  b.ob_xy, w.obs_off, b.loss, b.loss_scale, trial ? 1 : 0, w.ws);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_accept_commit(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    k_wb_accept<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W);
+    SFMBA_LAUNCH_CHECK();
+    long long m = b.nP;
+    if (7LL * b.nI > m) m = 7LL * b.nI;
+    if (8LL * b.nC > m) m = 8LL * b.nC;
+    if (m == 0) return;
+    k_wb_commit<<<div_up(m, 256), 256, 0, s>>>(w.ws, w.pt_win, w.img_win, w.cam_win, b.nI, b.nC, b.nP, b.poses_trial,
+                                               b.cams_trial, b.points_trial, b.poses, b.cams, b.points,
+                                               b.mixed ? b.points32 : nullptr);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_reject_failed(const WinBufs &w, cudaStream_t s) {
+    k_wb_reject_failed<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_end_outer(const WinBufs &w, int max_iterations, bool polish_allowed, double target_cost,
+                         cudaStream_t s) {
+    k_wb_end_outer<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W, max_iterations, polish_allowed ? 1 : 0, target_cost);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_start_polish(const WinBufs &w, cudaStream_t s) {
+    k_wb_start_polish<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_summary(const WinBufs &w, cudaStream_t s) {
+    k_wb_summary<<<1, 256, 0, s>>>(w.ws, w.W, w.counts);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_wb_lu(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    k_wb_lu<<<w.W, 1024, 0, s>>>(b.S, b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm, b.rhs, b.delta, w.ws);
+    SFMBA_LAUNCH_CHECK();
+}
+
+}  // namespace sfmba

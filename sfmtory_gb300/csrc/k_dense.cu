@@ -543,6 +543,13 @@ void launch_fold_system(const Bufs &b, cudaStream_t s) {
     SFMBA_LAUNCH_CHECK();
 }
 
+void launch_fold_rhs(const Bufs &b, cudaStream_t s) {
+    if (b.n == 0) return;
+    k_fold_rhs<<<div_up(b.n, 256), 256, 0, s>>>(b.img_rhs, b.slot_pre_start, b.slot_pre, b.slot_masked, b.n,
+                                                b.rhs);
+    SFMBA_LAUNCH_CHECK();
+}
+
 void launch_cholesky(const Bufs &b, cudaStream_t s) {
     set_smem_limits();
     const int n = b.n;

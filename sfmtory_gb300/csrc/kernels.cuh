@@ -88,6 +88,44 @@ struct Bufs {
     int4 *isrec = nullptr;        // [nO] image-major {image, point, x, y (float bits)}
 };
 
+// Levenberg-Marquardt state of one window of a batched solve.
+struct WinState {
+    double lambda, nu;
+    double cost, trial_cost, cost_before, initial_cost;
+    double lambda_start, nu_start;  // damping at the start of the outer iteration
+    long long valid_obs, trial_valid_obs;
+    int iterations, retries, retries_outer;
+    int accepted;        // accepted in the current retry, not yet committed
+    int accepted_outer;  // some retry of this outer iteration was accepted
+    int active;          // takes part in the current retry
+    int factor_failed, solve_failed;
+    int done;            // stopped (or parked until the FP64 polish)
+    int wants_polish, polished, polish_iteration;
+};
+
+// Window structure of a batched solve. The windows are concatenated into
+// one block-diagonal problem (images, cameras, points, slots in window
+// order); these arrays map the concatenation back to windows and locate
+// each window's dense reduced system.
+struct WinBufs {
+    int W = 0;
+    int max_n = 0;                 // largest window system
+    WinState *ws = nullptr;        // [W]
+    int *pt_win = nullptr;         // [nP] window of each point (solver order)
+    int *img_win = nullptr;        // [nI]
+    int *cam_win = nullptr;        // [nC]
+    int *slot_win = nullptr;       // [n]
+    int *img_base = nullptr;       // [W] first image of the window
+    int *nid_w = nullptr;          // [W] images of the window * D
+    int *n_w = nullptr;            // [W] reduced-system dimension
+    int *slot_base = nullptr;      // [W] first slot
+    long long *s_off = nullptr;    // [W] offset of the window's n_w^2 system in S and L
+    long long *simg_off = nullptr; // [W] offset of its nid_w^2 image-level blocks in S_img
+    long long *linv_off = nullptr; // [W] offset of its diagonal-block inverses in Linv
+    long long *obs_off = nullptr;  // [W+1] observation range (point-major order)
+    int *counts = nullptr;         // [4] summary read by the host each retry
+};
+
 constexpr int kCostBlocks = 1024;
 constexpr int kDotSlots = 16;
 constexpr int kCholNB = 64;
@@ -151,6 +189,7 @@ void launch_jacobian_probe(const JacProbe &q, bool fp32, cudaStream_t s);
 // ---- dense reduced system (k_dense.cu)
 void launch_schur_pairs(const Bufs &b, cudaStream_t s);
 void launch_fold_system(const Bufs &b, cudaStream_t s);
+void launch_fold_rhs(const Bufs &b, cudaStream_t s);  // slot-order rhs only
 void launch_cholesky(const Bufs &b, cudaStream_t s);
 void launch_cholesky_solve(const Bufs &b, const double *rhs, double *x, cudaStream_t s);
 void launch_refine(const Bufs &b, cudaStream_t s);
@@ -177,5 +216,28 @@ void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity);  // parity = 
 void launch_pcg_partition(Bufs &b, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
+
+// ---- batched windows (k_batched.cu)
+// Summary counts written by launch_wb_summary.
+enum { WB_NOT_DONE = 0, WB_RETRY_PENDING = 1, WB_FACTOR_FAILED = 2, WB_WANTS_POLISH = 3 };
+void launch_wb_window_of_points(const int *win_of_input_point, const int *perm, int nP, int *pt_win,
+                                cudaStream_t s);
+void launch_wb_init(const WinBufs &w, double initial_lambda, cudaStream_t s);
+void launch_wb_begin_outer(const WinBufs &w, int max_iterations, cudaStream_t s);
+void launch_wb_begin_retry(const WinBufs &w, cudaStream_t s);
+void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s);
+void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s);
+void launch_wb_fold(const Bufs &b, const WinBufs &w, cudaStream_t s);
+void launch_wb_cholesky(const Bufs &b, const WinBufs &w, cudaStream_t s);
+void launch_wb_solve(const Bufs &b, const WinBufs &w, const double *rhs, double *x, cudaStream_t s);
+void launch_wb_refine(const Bufs &b, const WinBufs &w, cudaStream_t s);
+void launch_wb_lu(const Bufs &b, const WinBufs &w, cudaStream_t s);
+void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s);
+void launch_wb_accept_commit(const Bufs &b, const WinBufs &w, cudaStream_t s);
+void launch_wb_reject_failed(const WinBufs &w, cudaStream_t s);
+void launch_wb_end_outer(const WinBufs &w, int max_iterations, bool polish_allowed, double target_cost,
+                         cudaStream_t s);
+void launch_wb_start_polish(const WinBufs &w, cudaStream_t s);
+void launch_wb_summary(const WinBufs &w, cudaStream_t s);
 
 }  // namespace sfmba

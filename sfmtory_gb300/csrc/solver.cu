@@ -154,8 +154,10 @@ struct Context {
     cudaStream_t stream = nullptr;
     Arena main, pairs;
     LMState *h_state = nullptr;  // pinned mirror
+    int *h_counts = nullptr;     // pinned batch summary
     ~Context() {
         if (h_state) cudaFreeHost(h_state);
+        if (h_counts) cudaFreeHost(h_counts);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -179,6 +181,7 @@ Context &context() {
         ctx->device = dev;
         SFMBA_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
         SFMBA_CUDA(cudaMallocHost(&ctx->h_state, sizeof(LMState)));
+        SFMBA_CUDA(cudaMallocHost(&ctx->h_counts, 4 * sizeof(int)));
     }
     return *ctx;
 }
@@ -196,7 +199,8 @@ struct Layout {
 
 Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> &cam_of_img,
                    const std::vector<int> &model, const std::vector<unsigned char> &fixed_pose,
-                   const std::vector<unsigned char> &fixed_cam, const std::vector<unsigned char> &fixed_cp) {
+                   const std::vector<unsigned char> &fixed_cam, const std::vector<unsigned char> &fixed_cp,
+                   int force_D = 0) {
     Layout L;
     L.nI = nI; L.nC = nC; L.nP = nP; L.nO = nO;
     L.pose_slot.assign(nI, -1);
@@ -212,7 +216,7 @@ Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> 
             kmax = std::max(kmax, model_dof(model[c]));
         }
     L.n = n;
-    L.D = block_width_for(kmax);
+    L.D = std::max(block_width_for(kmax), force_D);
     const int D = L.D;
     L.img_slot.assign((size_t)nI * D, -1);
     L.img_active.assign(nI, 0);
@@ -254,6 +258,133 @@ Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> 
     L.slot_pre.reserve(L.slot_pre_start[n]);
     for (int a = 0; a < n; ++a) L.slot_pre.insert(L.slot_pre.end(), pre[a].begin(), pre[a].end());
     return L;
+}
+
+// A batch of independent windows concatenated into one problem: images,
+// cameras, points and observations in window order, indices offset, and a
+// slot layout that keeps each window's unknowns contiguous (each window
+// slotted as its own problem, lib.rs:753-776), with one image block width
+// for the whole batch.
+struct Batch {
+    int W = 0;
+    Layout lay;
+    int max_n = 0;
+    std::vector<int> img_base, cam_base, pt_base, slot_base, n_w, nid_w;
+    std::vector<long long> obs_off, s_off, simg_off, linv_off;
+    long long s_total = 0, simg_total = 0, linv_total = 0;
+    std::vector<int> img_win, cam_win, slot_win, win_of_point;
+    // concatenated problem arrays
+    std::vector<int> cam_of_img, model, obs_image, obs_point;
+    std::vector<double> cams, poses, points, obs_xy;
+    std::vector<unsigned char> fixed_pose, fixed_cam, fixed_cp;
+    sfmba_problem problem{};
+    const sfmba_problem *windows = nullptr;
+    const sfmba_problem &window(int w) const { return windows[w]; }
+};
+
+void build_batch(int W, const sfmba_problem *win, Batch &B) {
+    // the window index is a grid dimension (y or z) of the per-window kernels
+    if (W > 65535) throw Error(SFMBA_ERR_UNSUPPORTED, "at most 65535 windows per batch");
+    B.W = W;
+    B.windows = win;
+    long long nI = 0, nC = 0, nP = 0, nO = 0;
+    int kmax = 0;
+    for (int w = 0; w < W; ++w) {
+        const sfmba_problem &p = win[w];
+        for (long long c = 0; c < p.num_cameras; ++c)
+            if (!(p.fixed_cameras && p.fixed_cameras[c])) kmax = std::max(kmax, model_dof(p.camera_model[c]));
+        nI += p.num_images; nC += p.num_cameras; nP += p.num_points; nO += p.num_observations;
+    }
+    if (nI > 65535) throw Error(SFMBA_ERR_UNSUPPORTED, "batched solve supports at most 65535 images in total");
+    if (nC > (1 << 20) || nP > (1LL << 30) || nO > (1LL << 31) - 1)
+        throw Error(SFMBA_ERR_INVALID_ARGUMENT, "batch too large for 32-bit indices");
+    const int D = block_width_for(kmax);
+    Layout &L = B.lay;
+    L.nI = (int)nI; L.nC = (int)nC; L.nP = (int)nP; L.nO = nO; L.D = D;
+    B.img_base.resize(W); B.cam_base.resize(W); B.pt_base.resize(W); B.slot_base.resize(W);
+    B.n_w.resize(W); B.nid_w.resize(W);
+    B.obs_off.assign(W + 1, 0); B.s_off.resize(W); B.simg_off.resize(W); B.linv_off.resize(W);
+    B.cam_of_img.reserve(nI); B.model.reserve(nC); B.obs_image.reserve(nO); B.obs_point.reserve(nO);
+    B.cams.reserve(nC * 8); B.poses.reserve(nI * 7); B.points.reserve(nP * 3); B.obs_xy.reserve(nO * 2);
+    B.fixed_pose.reserve(nI); B.fixed_cam.reserve(nC); B.fixed_cp.reserve(nC * 8);
+    B.img_win.reserve(nI); B.cam_win.reserve(nC); B.win_of_point.reserve(nP);
+    int ib = 0, cb = 0, pb = 0, sb = 0;
+    long long ob = 0, so = 0, sio = 0, lo = 0;
+    for (int w = 0; w < W; ++w) {
+        const sfmba_problem &p = win[w];
+        const int wi = (int)p.num_images, wc = (int)p.num_cameras, wp = (int)p.num_points;
+        const long long wo = p.num_observations;
+        std::vector<int> coi(p.camera_of_image, p.camera_of_image + wi);
+        std::vector<int> mod(p.camera_model, p.camera_model + wc);
+        std::vector<unsigned char> fp(wi, 0), fc(wc, 0), fcp((size_t)wc * 8, 0);
+        if (p.fixed_poses) fp.assign(p.fixed_poses, p.fixed_poses + wi);
+        if (p.fixed_cameras) fc.assign(p.fixed_cameras, p.fixed_cameras + wc);
+        if (p.fixed_camera_params) fcp.assign(p.fixed_camera_params, p.fixed_camera_params + (size_t)wc * 8);
+        Layout lw = make_layout(wi, wc, wp, wo, coi, mod, fp, fc, fcp, D);
+        if (lw.n > 16384)
+            throw Error(SFMBA_ERR_UNSUPPORTED, "window " + std::to_string(w) + " has more than 16384 unknowns");
+        B.img_base[w] = ib; B.cam_base[w] = cb; B.pt_base[w] = pb; B.slot_base[w] = sb;
+        B.n_w[w] = lw.n; B.nid_w[w] = wi * D;
+        B.max_n = std::max(B.max_n, lw.n);
+        B.s_off[w] = so; B.simg_off[w] = sio; B.linv_off[w] = lo;
+        so += (long long)lw.n * lw.n;
+        sio += (long long)wi * D * wi * D;
+        lo += (long long)div_up(lw.n, kCholNB) * kCholNB * kCholNB;
+        for (int i = 0; i < wi; ++i) {
+            B.cam_of_img.push_back(coi[i] + cb);
+            L.pose_slot.push_back(lw.pose_slot[i] >= 0 ? lw.pose_slot[i] + sb : -1);
+            L.img_active.push_back(lw.img_active[i]);
+            L.img_free.push_back(lw.img_free[i]);
+            B.img_win.push_back(w);
+            for (int r = 0; r < D; ++r) {
+                const int sl = lw.img_slot[(size_t)i * D + r];
+                L.img_slot.push_back(sl >= 0 ? sl + sb : -1);
+            }
+        }
+        for (int c = 0; c < wc; ++c) {
+            B.model.push_back(mod[c]);
+            L.cam_slot.push_back(lw.cam_slot[c] >= 0 ? lw.cam_slot[c] + sb : -1);
+            B.cam_win.push_back(w);
+        }
+        const int pre_base = L.slot_pre_start.empty() ? 0 : L.slot_pre_start.back();
+        if (L.slot_pre_start.empty()) L.slot_pre_start.push_back(0);
+        for (int a = 0; a < lw.n; ++a) {
+            L.slot_pre_start.push_back(pre_base + lw.slot_pre_start[a + 1]);
+            L.slot_masked.push_back(lw.slot_masked[a]);
+            B.slot_win.push_back(w);
+        }
+        for (int v : lw.slot_pre) L.slot_pre.push_back(v + ib * D);
+        B.cams.insert(B.cams.end(), p.camera_params, p.camera_params + (size_t)wc * 8);
+        B.poses.insert(B.poses.end(), p.poses, p.poses + (size_t)wi * 7);
+        B.points.insert(B.points.end(), p.points, p.points + (size_t)wp * 3);
+        B.win_of_point.insert(B.win_of_point.end(), wp, w);
+        for (long long o = 0; o < wo; ++o) {
+            B.obs_image.push_back(p.obs_image[o] + ib);
+            B.obs_point.push_back(p.obs_point[o] + pb);
+        }
+        B.obs_xy.insert(B.obs_xy.end(), p.obs_xy, p.obs_xy + (size_t)wo * 2);
+        B.fixed_pose.insert(B.fixed_pose.end(), fp.begin(), fp.end());
+        B.fixed_cam.insert(B.fixed_cam.end(), fc.begin(), fc.end());
+        B.fixed_cp.insert(B.fixed_cp.end(), fcp.begin(), fcp.end());
+        ib += wi; cb += wc; pb += wp; sb += lw.n; ob += wo;
+        B.obs_off[w + 1] = ob;
+    }
+    if (L.slot_pre_start.empty()) L.slot_pre_start.push_back(0);
+    L.n = sb;
+    B.s_total = so; B.simg_total = sio; B.linv_total = lo;
+    sfmba_problem &q = B.problem;
+    q.num_images = nI; q.num_cameras = nC; q.num_points = nP; q.num_observations = nO;
+    q.camera_of_image = B.cam_of_img.data();
+    q.camera_model = B.model.data();
+    q.camera_params = B.cams.data();
+    q.poses = B.poses.data();
+    q.points = B.points.data();
+    q.obs_image = B.obs_image.data();
+    q.obs_point = B.obs_point.data();
+    q.obs_xy = B.obs_xy.data();
+    q.fixed_poses = B.fixed_pose.data();
+    q.fixed_cameras = B.fixed_cam.data();
+    q.fixed_camera_params = B.fixed_cp.data();
 }
 
 void check_options(const sfmba_options *o) {
@@ -344,7 +475,8 @@ class Solver {
     }
 
     // Copies the problem into solver layout and builds all device structures.
-    void setup(const sfmba_problem *p, const sfmba_options *o, bool device, bool need_system) {
+    void setup(const sfmba_problem *p, const sfmba_options *o, bool device, bool need_system,
+               const Batch *batch = nullptr) {
         const int nI = (int)p->num_images, nC = (int)p->num_cameras, nP = (int)p->num_points;
         const long long nO = p->num_observations;
         std::vector<int> cam_of_img = fetch(p->camera_of_image, nI, device, s_);
@@ -359,17 +491,19 @@ class Solver {
         if (p->fixed_poses) fp = fetch(p->fixed_poses, nI, device, s_);
         if (p->fixed_cameras) fc = fetch(p->fixed_cameras, nC, device, s_);
         if (p->fixed_camera_params) fcp = fetch(p->fixed_camera_params, (size_t)nC * 8, device, s_);
-        lay_ = make_layout(nI, nC, nP, nO, cam_of_img, model, fp, fc, fcp);
+        lay_ = batch ? batch->lay : make_layout(nI, nC, nP, nO, cam_of_img, model, fp, fc, fcp);
         const int n = lay_.n, D = lay_.D;
         const bool mixed = o->precision == SFMBA_PRECISION_MIXED;
         solver_ = SFMBA_SOLVER_DENSE;
-        if (o->solver == SFMBA_SOLVER_PCG) solver_ = SFMBA_SOLVER_PCG;
+        if (batch) {
+            // every window is solved densely; its own size limit was checked
+        } else if (o->solver == SFMBA_SOLVER_PCG) solver_ = SFMBA_SOLVER_PCG;
         else if (o->solver == SFMBA_SOLVER_AUTO)
             solver_ = (n <= std::max(1, o->dense_max_dim)) ? SFMBA_SOLVER_DENSE : SFMBA_SOLVER_PCG;
         if (solver_ == SFMBA_SOLVER_PCG && !lay_.injective)
             throw Error(SFMBA_ERR_UNSUPPORTED,
                         "the PCG solver needs every free camera to belong to one image; use the dense solver");
-        if (solver_ == SFMBA_SOLVER_DENSE && n > 16384)
+        if (!batch && solver_ == SFMBA_SOLVER_DENSE && n > 16384)
             throw Error(SFMBA_ERR_UNSUPPORTED, "dense reduced system above 16384 unknowns; use the PCG solver");
         if (solver_ == SFMBA_SOLVER_DENSE && nI > 65535)
             throw Error(SFMBA_ERR_UNSUPPORTED, "dense solver supports at most 65535 images; use the PCG solver");
@@ -395,10 +529,32 @@ class Solver {
         long long *pair_scan = nullptr;
         int *d_bad = nullptr;
         int *pkey = nullptr, *pkey2 = nullptr, *piota = nullptr, *obs_pt_new = nullptr;
+        int *win_in = nullptr;
         for (int pass = 0; pass < 2; ++pass) {
             if (pass == 0) A.begin_sizing(); else A.commit();
             Bufs &b = b_;
             b = Bufs();
+            w_ = WinBufs();
+            if (batch) {
+                const int W = batch->W;
+                w_.W = W;
+                w_.max_n = batch->max_n;
+                w_.ws = A.take<WinState>(W);
+                w_.pt_win = A.take<int>(nP);
+                w_.img_win = A.take<int>(nI);
+                w_.cam_win = A.take<int>(nC);
+                w_.slot_win = A.take<int>(n);
+                w_.img_base = A.take<int>(W);
+                w_.nid_w = A.take<int>(W);
+                w_.n_w = A.take<int>(W);
+                w_.slot_base = A.take<int>(W);
+                w_.s_off = A.take<long long>(W);
+                w_.simg_off = A.take<long long>(W);
+                w_.linv_off = A.take<long long>(W);
+                w_.obs_off = A.take<long long>((size_t)W + 1);
+                w_.counts = A.take<int>(4);
+                win_in = A.take<int>(nP);
+            }
             b.nI = nI; b.nC = nC; b.nP = nP; b.nO = nO; b.n = n; b.D = D; b.nID = nID;
             b.mixed = mixed; b.loss = o->robust_loss; b.loss_scale = o->loss_scale_px;
             b.pcg_tol = o->pcg_tolerance > 0.0 ? o->pcg_tolerance : 0.1;
@@ -457,7 +613,14 @@ class Solver {
                 b.work2 = A.take<double>(n);
                 b.ref_res = A.take<double>(n);
                 b.ref_corr = A.take<double>(n);
-                if (solver_ == SFMBA_SOLVER_DENSE) {
+                if (batch) {
+                    b.S_img = A.take<double>((size_t)batch->simg_total);
+                    b.S = A.take<double>((size_t)batch->s_total);
+                    b.L = A.take<double>((size_t)batch->s_total);
+                    b.Linv = A.take<double>((size_t)batch->linv_total);
+                    b.lu_perm = A.take<int>(n);
+                    pair_scan = A.take<long long>(nP);
+                } else if (solver_ == SFMBA_SOLVER_DENSE) {
                     b.S_img = A.take<double>((size_t)nID * nID);
                     b.S = A.take<double>((size_t)n * n);
                     b.L = A.take<double>((size_t)n * n);
@@ -573,7 +736,24 @@ class Solver {
                 d_ng = P.take<int>(1);
             }
             build_pairs(b, pair_scan, ka, kb, vb, pt, ptemp, d_ng, s_);
-            SFMBA_CUDA(cudaMemsetAsync(b.S_img, 0, sizeof(double) * (size_t)nID * nID, s_));
+            const size_t simg = batch ? (size_t)batch->simg_total : (size_t)nID * nID;
+            SFMBA_CUDA(cudaMemsetAsync(b.S_img, 0, sizeof(double) * simg, s_));
+        }
+        if (batch) {
+            WinBufs &w = w_;
+            put_vec(w.img_win, batch->img_win, s_);
+            put_vec(w.cam_win, batch->cam_win, s_);
+            put_vec(w.slot_win, batch->slot_win, s_);
+            put_vec(w.img_base, batch->img_base, s_);
+            put_vec(w.nid_w, batch->nid_w, s_);
+            put_vec(w.n_w, batch->n_w, s_);
+            put_vec(w.slot_base, batch->slot_base, s_);
+            put_vec(w.s_off, batch->s_off, s_);
+            put_vec(w.simg_off, batch->simg_off, s_);
+            put_vec(w.linv_off, batch->linv_off, s_);
+            put_vec(w.obs_off, batch->obs_off, s_);
+            put_vec(win_in, batch->win_of_point, s_);
+            launch_wb_window_of_points(win_in, b.pt_perm, nP, w.pt_win, s_);
         }
         if (mixed) launch_refresh_points32(b, s_);
     }
@@ -701,6 +881,103 @@ class Solver {
         return out;
     }
 
+    // The LM loop of every window of a batch (lib.rs:794-1232 per window).
+    // Each kernel covers all windows; the windows that take part in a retry
+    // are flagged on the device, and the host only reads four counts per
+    // retry to decide whether another round is needed.
+    std::vector<WinState> run_batched(const sfmba_options *o) {
+        Bufs &b = b_;
+        WinBufs &w = w_;
+        int *hc = ctx_.h_counts;
+        auto counts = [&] {
+            launch_wb_summary(w, s_);
+            SFMBA_CUDA(cudaMemcpyAsync(hc, w.counts, 4 * sizeof(int), cudaMemcpyDeviceToHost, s_));
+            SFMBA_CUDA(cudaStreamSynchronize(s_));
+        };
+        { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, false, s_); }
+        launch_wb_init(w, o->initial_lambda, s_);
+        counts();
+        const bool polish = b.mixed && o->fp64_polish;
+        const int max_rounds = 2 * std::max(o->max_iterations, 0) + 2;
+        for (int round = 0; round < max_rounds; ++round) {
+            if (hc[WB_NOT_DONE] == 0) {
+                if (!(polish && b.mixed && hc[WB_WANTS_POLISH] > 0)) break;
+                // Every window has stopped in FP32: the parked ones continue in FP64.
+                b.mixed = 0;
+                launch_wb_start_polish(w, s_);
+            }
+            { SFMBA_PHASE(PH_LM); launch_wb_begin_outer(w, o->max_iterations, s_); }
+            counts();
+            if (hc[WB_NOT_DONE] == 0) continue;
+            {
+                SFMBA_PHASE(PH_LINEARIZE);
+                launch_prepare_images(b, s_);
+                launch_linearize(b, s_);
+            }
+            { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
+            { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
+            for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
+                { SFMBA_PHASE(PH_LM); launch_wb_begin_retry(w, s_); }
+                { SFMBA_PHASE(PH_POINT_INVERSE); launch_wb_point_inverse(b, w, s_); }
+                { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); launch_fold_rhs(b, s_); }
+                { SFMBA_PHASE(PH_SCHUR); launch_wb_schur(b, w, s_); }
+                { SFMBA_PHASE(PH_FOLD); launch_wb_fold(b, w, s_); }
+                { SFMBA_PHASE(PH_CHOLESKY); launch_wb_cholesky(b, w, s_); }
+                { SFMBA_PHASE(PH_TRSV); launch_wb_solve(b, w, b.rhs, b.delta, s_); }
+                if (b.mixed) {
+                    SFMBA_PHASE(PH_REFINE);
+                    for (int k = 0; k < o->refinement_steps; ++k) launch_wb_refine(b, w, s_);
+                }
+                { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
+                { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, true, s_); }
+                { SFMBA_PHASE(PH_LM); launch_wb_accept_commit(b, w, s_); }
+                counts();
+                if (hc[WB_FACTOR_FAILED] > 0) {
+                    // LU fallback for the windows whose Cholesky failed (lib.rs:1084-1092)
+                    { SFMBA_PHASE(PH_LU); launch_wb_lu(b, w, s_); }
+                    { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
+                    { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, true, s_); }
+                    { SFMBA_PHASE(PH_LM); launch_wb_accept_commit(b, w, s_); launch_wb_reject_failed(w, s_); }
+                    counts();
+                }
+                if (hc[WB_RETRY_PENDING] == 0) break;
+            }
+            { SFMBA_PHASE(PH_LM); launch_wb_end_outer(w, o->max_iterations, polish && b.mixed, o->target_cost, s_); }
+            counts();
+        }
+        std::vector<WinState> ws(w.W);
+        SFMBA_CUDA(cudaMemcpyAsync(ws.data(), w.ws, sizeof(WinState) * w.W, cudaMemcpyDeviceToHost, s_));
+        SFMBA_CUDA(cudaStreamSynchronize(s_));
+        return ws;
+    }
+
+    // Window results in the callers' buffers (host), points back in each
+    // window's own order.
+    void copy_out_batched(const Batch &B, sfmba_result *res) {
+        const Bufs &b = b_;
+        scatter_points(b.points, b.pt_old2new, b.nP, b.points_trial, s_);
+        std::vector<double> poses((size_t)b.nI * 7), points((size_t)b.nP * 3), cams((size_t)b.nC * 8);
+        if (!poses.empty())
+            SFMBA_CUDA(cudaMemcpyAsync(poses.data(), b.poses, sizeof(double) * poses.size(), cudaMemcpyDeviceToHost, s_));
+        if (!points.empty())
+            SFMBA_CUDA(cudaMemcpyAsync(points.data(), b.points_trial, sizeof(double) * points.size(),
+                                       cudaMemcpyDeviceToHost, s_));
+        if (!cams.empty())
+            SFMBA_CUDA(cudaMemcpyAsync(cams.data(), b.cams, sizeof(double) * cams.size(), cudaMemcpyDeviceToHost, s_));
+        SFMBA_CUDA(cudaStreamSynchronize(s_));
+        for (int w = 0; w < B.W; ++w) {
+            const sfmba_problem &p = B.window(w);
+            sfmba_result &r = res[w];
+            if (r.poses && p.num_images)
+                std::memcpy(r.poses, poses.data() + (size_t)B.img_base[w] * 7, sizeof(double) * 7 * p.num_images);
+            if (r.points && p.num_points)
+                std::memcpy(r.points, points.data() + (size_t)B.pt_base[w] * 3, sizeof(double) * 3 * p.num_points);
+            if (r.camera_params && p.num_cameras)
+                std::memcpy(r.camera_params, cams.data() + (size_t)B.cam_base[w] * 8,
+                            sizeof(double) * 8 * p.num_cameras);
+        }
+    }
+
     void copy_out(sfmba_result *r, bool device) {
         const cudaMemcpyKind k = device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         if (r->poses && b_.nI)
@@ -726,6 +1003,7 @@ class Solver {
     Context &ctx_;
     cudaStream_t s_;
     Bufs b_;
+    WinBufs w_;
     Layout lay_;
     int solver_ = SFMBA_SOLVER_DENSE;
 };
@@ -924,7 +1202,49 @@ int sfmba_refine_intrinsics(const sfmba_problem *p, const sfmba_options *o, doub
 
 int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *windows,
                                 const sfmba_options *o, sfmba_result *results) {
-    return guarded([&] { throw Error(SFMBA_ERR_UNSUPPORTED, "batched solve: not built yet"); });
+    const int st = guarded([&] {
+        const double t0 = now_s();
+        if (num_windows < 0) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "num_windows < 0");
+        if (num_windows > 0 && (!windows || !results))
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "windows or results is NULL");
+        check_options(o);
+        if (num_windows == 0) return;
+        for (int w = 0; w < num_windows; ++w) {
+            check_problem_shape(&windows[w]);
+            check_problem_host(&windows[w]);
+        }
+        Batch B;
+        build_batch(num_windows, windows, B);
+        Context &ctx = context();
+        cudaStream_t s = ctx.stream;
+        Solver solver(ctx, s);
+        {
+            PhaseScope ps(PH_SETUP, s);
+            solver.setup(&B.problem, o, false, true, &B);
+        }
+        std::vector<WinState> ws = solver.run_batched(o);
+        solver.copy_out_batched(B, results);
+        profiler().resolve();
+        const double secs = now_s() - t0;
+        for (int w = 0; w < num_windows; ++w) {
+            sfmba_result &r = results[w];
+            const WinState &x = ws[w];
+            r.initial_cost = x.initial_cost;
+            r.final_cost = x.cost;
+            r.iterations_run = x.iterations;
+            r.damping_retries = x.retries;
+            r.solver_used = SFMBA_SOLVER_DENSE;
+            r.polish_iteration = x.polished && x.polish_iteration >= 0 ? x.polish_iteration : -1;
+            r.linear_iterations = 0;
+            r.reduced_dim = B.n_w[w];
+            r.valid_observations = x.valid_obs;
+            r.seconds = secs;
+            r.status = SFMBA_OK;
+        }
+    });
+    if (st != SFMBA_OK && results && num_windows > 0)
+        for (int w = 0; w < num_windows; ++w) results[w].status = st;
+    return st;
 }
 
 int sfmba_profile_enable(int32_t on) {

@@ -224,6 +224,24 @@ def bundle_adjust(input: BaInput, params: BaParams = BaParams()) -> BaOutput:
                     r.initial_cost, r.final_cost, r.iterations_run)
 
 
+def bundle_adjust_batched(inputs: Sequence[BaInput], params: BaParams = BaParams()) -> List[BaOutput]:
+    """Many independent windows (sfm-reconstruction's BaScope::Local calls,
+    crates/sfm-reconstruction/src/lib.rs:1287-1299) in one GPU solve, each
+    window with its own damping and stopping; one BaOutput per window, as
+    ``bundle_adjust`` would return it."""
+    problems = [inp.to_problem() for inp in inputs]
+    res = native.bundle_adjust_batched_arrays(problems, params.to_options())
+    out = []
+    for inp, r in zip(inputs, res):
+        cams = [CameraModel(c.model_id, tuple(float(x) for x in r.camera_params[k, : len(c.param_values)]))
+                for k, c in enumerate(inp.cameras)]
+        poses = [Pose(tuple(map(float, r.poses[i, :4])), tuple(map(float, r.poses[i, 4:])))
+                 for i in range(len(inp.poses))]
+        out.append(BaOutput(poses, [r.points[k].copy() for k in range(len(r.points))], cams,
+                            r.initial_cost, r.final_cost, r.iterations_run))
+    return out
+
+
 def mean_reprojection_error(input: BaInput) -> float:
     """crates/sfm-ba/src/lib.rs:708-725."""
     return native.mean_reprojection_error_arrays(input.to_problem())

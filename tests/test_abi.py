@@ -73,3 +73,27 @@ def test_null_result_is_an_error():
     st = L.sfmba_bundle_adjust(C.byref(packed.struct), C.byref(o), None)
     assert st == 1
     assert b"NULL" in L.sfmba_last_error()
+
+
+def test_batched_rejects_invalid_input_before_device():
+    """The batched entry validates every window on the host first: a bad
+    index in any window, a negative count or NULL arrays are errors, and the
+    failing status is written into every window's result."""
+    good = scenes.recovers_ground_truth_fixture()
+    bad = scenes.recovers_ground_truth_fixture()
+    arr = bad.obs_point.copy()
+    arr[0] = 10**6
+    bad.obs_point = arr
+    with pytest.raises(native.SfmbaError) as e:
+        native.bundle_adjust_batched_arrays([good, bad])
+    assert e.value.status == 1
+    L = native.load()
+    o = abi.default_options()
+    assert L.sfmba_bundle_adjust_batched(-1, None, C.byref(o), None) == 1
+    assert L.sfmba_bundle_adjust_batched(2, None, C.byref(o), None) == 1
+    packed = abi.PackedProblem(good)
+    res = (abi.SfmbaResult * 1)()
+    bad_opts = abi.default_options(robust_loss=9)
+    assert L.sfmba_bundle_adjust_batched(1, C.byref(packed.struct), C.byref(bad_opts), res) == 1
+    assert res[0].status == 1
+    assert L.sfmba_bundle_adjust_batched(0, None, C.byref(o), None) == 0
