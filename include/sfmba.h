@@ -107,7 +107,9 @@ typedef struct sfmba_options {
     double target_cost;           /* > 0: also stop once cost <= target_cost   */
     int32_t dense_max_dim;        /* AUTO picks dense up to this reduced dim   */
     int32_t fp64_polish;          /* mixed path: when the FP32 loop would stop,
-                                     continue the same LM loop in FP64 (default 1) */
+                                     continue the same LM loop in FP64 (default 0:
+                                     the FP32 path already forms its gradient from
+                                     FP64 residuals and stops where FP64 does) */
     int32_t reserved[6];
 } sfmba_options;
 

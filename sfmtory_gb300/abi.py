@@ -110,7 +110,7 @@ def default_options(**overrides) -> SfmbaOptions:
     o.refinement_steps = 1
     o.target_cost = 0.0
     o.dense_max_dim = 6000
-    o.fp64_polish = 1
+    o.fp64_polish = 0
     for k, v in overrides.items():
         if not hasattr(o, k):
             raise AttributeError(f"sfmba_options has no field {k!r}")

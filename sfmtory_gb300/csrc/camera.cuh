@@ -149,6 +149,18 @@ __device__ __forceinline__ T robust_weight(T n, int loss, T scale) {
     return T(1);
 }
 
+// Optional FP64 residual of an observation. The FP32 path computes the
+// pixel residual u - obs from ~1e3 px quantities, which leaves ~1e-4 px of
+// rounding: far above what the gradient near the minimum can tolerate. The
+// kernels that form gradient terms pass the FP64 residual here; the robust
+// weight then comes from it too.
+struct Res64 {
+    bool use = false;
+    bool ok = false;
+    double r0 = 0.0, r1 = 0.0;  // unweighted residual
+    double s = -1.0;            // sqrt of the robust weight; < 0: from (r0, r1)
+};
+
 // Residual and Jacobian of one observation, weighted by sqrt(w).
 //
 // Forward pass: pc = R X + t, (xp, yp) = (pc.x, pc.y) / pc.z, pixel = distort.
@@ -161,12 +173,12 @@ __device__ __forceinline__ T robust_weight(T n, int loss, T scale) {
 template <typename T, int D>
 __device__ __forceinline__ bool linearize(const ImageLin<T> &im, T X0, T X1, T X2, T ox, T oy,
                                           int loss, T scale, T rr[2], T jx[6], T jc[2 * D],
-                                          T *weight = nullptr) {
+                                          T *weight = nullptr, const Res64 &rin = Res64()) {
     const T q0 = im.R[0] * X0 + im.R[1] * X1 + im.R[2] * X2;
     const T q1 = im.R[3] * X0 + im.R[4] * X1 + im.R[5] * X2;
     const T q2 = im.R[6] * X0 + im.R[7] * X1 + im.R[8] * X2;
     const T pc0 = q0 + im.t[0], pc1 = q1 + im.t[1], pc2 = q2 + im.t[2];
-    if (!(pc2 > T(kMinDepth))) {
+    if (!(pc2 > T(kMinDepth)) || (rin.use && !rin.ok)) {
         rr[0] = rr[1] = T(0);
 #pragma unroll
         for (int i = 0; i < 6; ++i) jx[i] = T(0);
@@ -179,14 +191,26 @@ __device__ __forceinline__ bool linearize(const ImageLin<T> &im, T X0, T X1, T X
     const T xp = pc0 * iz, yp = pc1 * iz;
     T u, v, A[2][2], G[2][8];
     distort<T>(im.model, im.c, xp, yp, u, v, A, G);
-    rr[0] = u - ox;
-    rr[1] = v - oy;
-    const T n = dev_sqrt<T>(rr[0] * rr[0] + rr[1] * rr[1]);
-    const T w = robust_weight<T>(n, loss, scale);
-    const T s = dev_sqrt<T>(w);
-    if (weight) *weight = w;
-    rr[0] *= s;
-    rr[1] *= s;
+    T s;
+    if (rin.use) {
+        const double w = rin.s >= 0.0 ? rin.s * rin.s
+                                      : robust_weight<double>(sqrt(rin.r0 * rin.r0 + rin.r1 * rin.r1), loss,
+                                                              (double)scale);
+        const double sd = rin.s >= 0.0 ? rin.s : sqrt(w);
+        rr[0] = (T)(rin.r0 * sd);
+        rr[1] = (T)(rin.r1 * sd);
+        s = (T)sd;
+        if (weight) *weight = (T)w;
+    } else {
+        rr[0] = u - ox;
+        rr[1] = v - oy;
+        const T n = dev_sqrt<T>(rr[0] * rr[0] + rr[1] * rr[1]);
+        const T w = robust_weight<T>(n, loss, scale);
+        s = dev_sqrt<T>(w);
+        if (weight) *weight = w;
+        rr[0] *= s;
+        rr[1] *= s;
+    }
 #pragma unroll
     for (int row = 0; row < 2; ++row) {
         // pbar = d(pixel_row)/d(pc)
@@ -227,13 +251,13 @@ struct LinCompact {
 
 template <typename T, int D>
 __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T X1, T X2, T ox, T oy, int loss,
-                                                  T scale, LinCompact<T, D> &L) {
+                                                  T scale, LinCompact<T, D> &L, const Res64 &rin = Res64()) {
     L.q[0] = im.R[0] * X0 + im.R[1] * X1 + im.R[2] * X2;
     L.q[1] = im.R[3] * X0 + im.R[4] * X1 + im.R[5] * X2;
     L.q[2] = im.R[6] * X0 + im.R[7] * X1 + im.R[8] * X2;
     L.pose_on = im.active & 1;
     const T pc0 = L.q[0] + im.t[0], pc1 = L.q[1] + im.t[1], pc2 = L.q[2] + im.t[2];
-    if (!(pc2 > T(kMinDepth))) {
+    if (!(pc2 > T(kMinDepth)) || (rin.use && !rin.ok)) {
 #pragma unroll
         for (int row = 0; row < 2; ++row) {
             L.r[row] = T(0);
@@ -248,10 +272,22 @@ __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T
     const T xp = pc0 * iz, yp = pc1 * iz;
     T u, v, A[2][2], G[2][8];
     distort<T>(im.model, im.c, xp, yp, u, v, A, G);
-    const T r0 = u - ox, r1 = v - oy;
-    const T s = loss == SFMBA_LOSS_NONE ? T(1) : dev_sqrt<T>(robust_weight<T>(dev_sqrt<T>(r0 * r0 + r1 * r1), loss, scale));
-    L.r[0] = r0 * s;
-    L.r[1] = r1 * s;
+    T s;
+    if (rin.use) {
+        const double sd = rin.s >= 0.0 ? rin.s
+                          : loss == SFMBA_LOSS_NONE
+                              ? 1.0
+                              : sqrt(robust_weight<double>(sqrt(rin.r0 * rin.r0 + rin.r1 * rin.r1), loss,
+                                                           (double)scale));
+        L.r[0] = (T)(rin.r0 * sd);
+        L.r[1] = (T)(rin.r1 * sd);
+        s = (T)sd;
+    } else {
+        const T r0 = u - ox, r1 = v - oy;
+        s = loss == SFMBA_LOSS_NONE ? T(1) : dev_sqrt<T>(robust_weight<T>(dev_sqrt<T>(r0 * r0 + r1 * r1), loss, scale));
+        L.r[0] = r0 * s;
+        L.r[1] = r1 * s;
+    }
 #pragma unroll
     for (int row = 0; row < 2; ++row) {
         const T a0 = A[row][0] * s, a1 = A[row][1] * s;
@@ -265,22 +301,9 @@ __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T
     return true;
 }
 
-// FP64 residual as the reference's cost evaluates it: quaternion rotation
-// (pose.rs:46-48) and project() (the perspective divide as one reciprocal).
-__device__ __forceinline__ bool residual64(const double *pose7, int model, const double *c,
-                                           double X0, double X1, double X2, double ox, double oy,
-                                           double &rx, double &ry) {
-    const double w = pose7[0], x = pose7[1], y = pose7[2], z = pose7[3];
-    const double tx = 2.0 * (y * X2 - z * X1);
-    const double ty = 2.0 * (z * X0 - x * X2);
-    const double tz = 2.0 * (x * X1 - y * X0);
-    const double pc0 = X0 + w * tx + (y * tz - z * ty) + pose7[4];
-    const double pc1 = X1 + w * ty + (z * tx - x * tz) + pose7[5];
-    const double pc2 = X2 + w * tz + (x * ty - y * tx) + pose7[6];
-    if (!(pc2 > kMinDepth)) return false;
-    const double iz = 1.0 / pc2;
-    const double xn = pc0 * iz, yn = pc1 * iz;
-    double u, v;
+// Pixel of normalised coordinates (xn, yn) under `model` in FP64
+// (crates/sfm-core/src/camera.rs:204-244).
+__device__ __forceinline__ void project64(int model, const double *c, double xn, double yn, double &u, double &v) {
     switch (model) {
     case SFMBA_SIMPLE_PINHOLE: u = c[0] * xn + c[1]; v = c[0] * yn + c[2]; break;
     case SFMBA_PINHOLE: u = c[0] * xn + c[2]; v = c[1] * yn + c[3]; break;
@@ -311,6 +334,44 @@ __device__ __forceinline__ bool residual64(const double *pose7, int model, const
         break;
     }
     }
+}
+
+// FP64 residual as the reference's cost evaluates it: quaternion rotation
+// (pose.rs:46-48) and project() (the perspective divide as one reciprocal).
+__device__ __forceinline__ bool residual64(const double *pose7, int model, const double *c,
+                                           double X0, double X1, double X2, double ox, double oy,
+                                           double &rx, double &ry) {
+    const double w = pose7[0], x = pose7[1], y = pose7[2], z = pose7[3];
+    const double tx = 2.0 * (y * X2 - z * X1);
+    const double ty = 2.0 * (z * X0 - x * X2);
+    const double tz = 2.0 * (x * X1 - y * X0);
+    const double pc0 = X0 + w * tx + (y * tz - z * ty) + pose7[4];
+    const double pc1 = X1 + w * ty + (z * tx - x * tz) + pose7[5];
+    const double pc2 = X2 + w * tz + (x * ty - y * tx) + pose7[6];
+    if (!(pc2 > kMinDepth)) return false;
+    const double iz = 1.0 / pc2;
+    double u, v;
+    project64(model, c, pc0 * iz, pc1 * iz, u, v);
+    rx = u - ox;
+    ry = v - oy;
+    return true;
+}
+
+// FP64 residual for the gradient terms of the FP32 path, from an image's
+// FP64 rotation matrix: 12 FMAs for R X + t, and 1/z from the FP32
+// reciprocal refined by one Newton-Raphson step x' = x (2 - z x), which
+// squares the relative error (2^-23 -> ~2^-46), instead of an FP64 divide.
+__device__ __forceinline__ bool residual64_lin(const ImageLin<double> &im, double X0, double X1, double X2,
+                                               double ox, double oy, double &rx, double &ry) {
+    const double pc0 = im.R[0] * X0 + im.R[1] * X1 + im.R[2] * X2 + im.t[0];
+    const double pc1 = im.R[3] * X0 + im.R[4] * X1 + im.R[5] * X2 + im.t[1];
+    const double pc2 = im.R[6] * X0 + im.R[7] * X1 + im.R[8] * X2 + im.t[2];
+    if (!(pc2 > kMinDepth)) return false;
+    const float izf = __frcp_rn((float)pc2);
+    double iz = (double)izf;
+    iz = isfinite(izf) ? iz * (2.0 - pc2 * iz) : 1.0 / pc2;
+    double u, v;
+    project64(im.model, im.c, pc0 * iz, pc1 * iz, u, v);
     rx = u - ox;
     ry = v - oy;
     return true;

@@ -11,25 +11,30 @@
 
 #include "camera.cuh"
 #include "kernels.cuh"
+#include "schur.cuh"
 
 namespace sfmba {
 
 namespace {
 
-template <typename T>
-__device__ __forceinline__ void kahan_add(T &s, T &c, T x) {
-    if constexpr (std::is_same<T, float>::value) {
-        const T y = x - c;
-        const T t = s + y;
-        c = (t - s) - y;
-        s = t;
-    } else {
-        s += x;
-    }
-}
-
 constexpr int NB = kCholNB;
 constexpr int LD = NB + 1;
+
+// Which images and points take part in the current phase: outer-iteration
+// kernels (linearisation, reductions) run for windows not done, retry
+// kernels (point inverse, rhs, back-substitution) for windows retrying.
+__global__ void k_wb_live(const WinState *ws, const int *img_win, const int *pt_win, int nI, int nP, int retry,
+                          unsigned char *img_live, unsigned char *pt_live) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < nI) {
+        const WinState &s = ws[img_win[t]];
+        img_live[t] = retry ? (unsigned char)(s.active != 0) : (unsigned char)(s.done == 0);
+    }
+    if (t < nP) {
+        const WinState &s = ws[pt_win[t]];
+        pt_live[t] = retry ? (unsigned char)(s.active != 0) : (unsigned char)(s.done == 0);
+    }
+}
 
 __global__ void k_wb_window_of_points(const int *win_in, const int *perm, int nP, int *pt_win) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -91,9 +96,11 @@ __global__ void k_wb_begin_retry(WinState *ws, int W) {
 // Damped point inverses with the damping of the point's window.
 template <typename T>
 __global__ void k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_nfree, const int *pt_win,
-                                   const WinState *ws, int nP, T *pt_Cinv, T *pt_h, unsigned char *pt_ok) {
+                                   const WinState *ws, int nP, T *pt_Cinv, T *pt_h, unsigned char *pt_ok,
+                                   const unsigned char *pt_live) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nP) return;
+    if (!pt_live[p]) return;
     const double lam = ws[pt_win[p]].lambda;
     const T *C = pt_C + 6 * (size_t)p;
     double m00 = C[0], m01 = C[1], m02 = C[2], m11 = C[3], m12 = C[4], m22 = C[5];
@@ -125,13 +132,13 @@ __global__ void k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_n
     pt_ok[p] = 1;
 }
 
-constexpr int kWarps = 2;
+template <typename T>
+constexpr int schur_warps() { return sizeof(T) == 4 ? 4 : 2; }
 
-// Schur reduction of the image pairs of every window (one warp per pair),
-// written into the window's image-level block matrix. Pairs of windows that
-// are not retrying are skipped.
+// Schur reduction of the image pairs of every retrying window (one warp per
+// pair, schur.cuh), written into the window's image-level block matrix.
 template <typename T, int D>
-__global__ void __launch_bounds__(32 * kWarps)
+__global__ void __launch_bounds__(32 * schur_warps<T>())
     k_wb_schur_pairs(const T *__restrict__ rec, const int2 *__restrict__ pairs, const int *__restrict__ group_start,
                      const int2 *__restrict__ group_ij, int ngroups, const int *__restrict__ ob_pt,
                      const T *__restrict__ pt_Cinv, const unsigned char *__restrict__ pt_ok,
@@ -139,81 +146,31 @@ __global__ void __launch_bounds__(32 * kWarps)
                      const int *__restrict__ img_base, const int *__restrict__ nid_w,
                      const long long *__restrict__ simg_off, const WinState *__restrict__ ws,
                      double *__restrict__ S_img) {
-    constexpr int RS = RecLayout<D>::kStride;
-    constexpr int NE = (D * D + 31) / 32;
-    __shared__ T sM[kWarps][32][4];
-    __shared__ T sA[kWarps][32][2 * D];
-    __shared__ T sB[kWarps][32][2 * D];
+    constexpr int W = schur_warps<T>();
+    using Tile = SchurTile<T, D>;
+    __shared__ T sA[W][32][Tile::LDS];
+    __shared__ T sP[W][32][Tile::LDS];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = blockIdx.x * kWarps + wl;
+    const int g = blockIdx.x * W + wl;
     if (g >= ngroups) return;
     const int2 ij = group_ij[g];
     const int w = img_win[ij.x];
     if (!ws[w].active) return;
-    const int gs = group_start[g], ge = group_start[g + 1];
-    T acc[NE], comp[NE];
-#pragma unroll
-    for (int k = 0; k < NE; ++k) acc[k] = comp[k] = T(0);
-    for (int base = gs; base < ge; base += 32) {
-        const int e = base + lane;
-        if (e < ge) {
-            const int2 ab = pairs[e];
-            const int p = ob_pt[ab.x];
-            const T *ra = rec + (size_t)ab.x * RS;
-            const T *rb = rec + (size_t)ab.y * RS;
-            if (pt_ok[p]) {
-                const T *Ci = pt_Cinv + 6 * (size_t)p;
-                T U[2][3];
-#pragma unroll
-                for (int r = 0; r < 2; ++r) {
-                    const T x0 = ra[2 + 3 * r], x1 = ra[3 + 3 * r], x2 = ra[4 + 3 * r];
-                    U[r][0] = x0 * Ci[0] + x1 * Ci[1] + x2 * Ci[2];
-                    U[r][1] = x0 * Ci[1] + x1 * Ci[3] + x2 * Ci[4];
-                    U[r][2] = x0 * Ci[2] + x1 * Ci[4] + x2 * Ci[5];
-                }
-#pragma unroll
-                for (int r = 0; r < 2; ++r)
-#pragma unroll
-                    for (int q = 0; q < 2; ++q)
-                        sM[wl][lane][2 * r + q] = U[r][0] * rb[2 + 3 * q] + U[r][1] * rb[3 + 3 * q] + U[r][2] * rb[4 + 3 * q];
-#pragma unroll
-                for (int f = 0; f < 2 * D; ++f) {
-                    sA[wl][lane][f] = ra[8 + f];
-                    sB[wl][lane][f] = rb[8 + f];
-                }
-            } else {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) sM[wl][lane][q] = T(0);
-#pragma unroll
-                for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = sB[wl][lane][f] = T(0);
-            }
-        }
-        __syncwarp();
-        const int cnt = min(32, ge - base);
-        for (int t = 0; t < cnt; ++t) {
-            const T m0 = sM[wl][t][0], m1 = sM[wl][t][1], m2 = sM[wl][t][2], m3 = sM[wl][t][3];
-#pragma unroll
-            for (int k = 0; k < NE; ++k) {
-                const int idx = lane + 32 * k;
-                if (idx < D * D) {
-                    const int r = idx / D, c = idx - r * D;
-                    const T b0 = sB[wl][t][c], b1 = sB[wl][t][D + c];
-                    kahan_add(acc[k], comp[k],
-                              sA[wl][t][r] * (m0 * b0 + m1 * b1) + sA[wl][t][D + r] * (m2 * b0 + m3 * b1));
-                }
-            }
-        }
-        __syncwarp();
-    }
+    double out[Tile::RH][Tile::CQ];
+    schur_group<T, D>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl], lane,
+                      out);
+    if (lane >= 8) return;
     const int li = ij.x - img_base[w], lj = ij.y - img_base[w];
     const int nid = nid_w[w];
     double *Sw = S_img + simg_off[w];
+    const int r0 = (lane >> 2) * Tile::RH, c0 = (lane & 3) * Tile::CQ;
 #pragma unroll
-    for (int k = 0; k < NE; ++k) {
-        const int idx = lane + 32 * k;
-        if (idx < D * D) {
-            const int r = idx / D, c = idx - r * D;
-            const double v = -((double)acc[k] - (double)comp[k]);
+    for (int a = 0; a < Tile::RH; ++a)
+#pragma unroll
+        for (int b = 0; b < Tile::CQ; ++b) {
+            const int r = r0 + a, c = c0 + b;
+            if (r >= D || c >= D) continue;
+            const double v = out[a][b];
             if (li == lj) {
                 Sw[(size_t)(li * D + r) * nid + li * D + c] = img_H[(size_t)ij.x * D * D + r * D + c] + v;
             } else {
@@ -221,44 +178,83 @@ __global__ void __launch_bounds__(32 * kWarps)
                 Sw[(size_t)(lj * D + c) * nid + li * D + r] = v;
             }
         }
-    }
 }
 
-// Window w's slot-order system: S[a][b] from its image-level blocks, damping
-// with the window's lambda, masks, symmetrisation. Grid: (column blocks, row, window).
-__global__ void k_wb_fold(const double *__restrict__ S_img, const long long *__restrict__ simg_off,
-                          const int *__restrict__ nid_w, const int *__restrict__ n_w,
-                          const int *__restrict__ slot_base, const long long *__restrict__ s_off,
-                          const int *__restrict__ img_base, int D, const int *__restrict__ pre_start,
-                          const int *__restrict__ pre, const unsigned char *__restrict__ masked,
-                          const double *__restrict__ diagB, const WinState *__restrict__ ws,
-                          double *__restrict__ S, double *__restrict__ L) {
+// Window systems are factored in a permuted slot order (slot_perm: position
+// -> slot, each image's pose slots followed by its camera's), in which the
+// co-visibility of nearby images makes S banded. row_first[a] is the first
+// nonzero column of row a of the permuted system; Cholesky keeps L inside
+// that envelope, so the factorisation skips the tiles outside it.
+__global__ void k_wb_envelope_init(const int *slot_win, const int *slot_base, int n, const WinState *ws,
+                                   int *row_first) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const int w = slot_win[a];
+    if (ws[w].active) row_first[a] = a - slot_base[w];
+}
+
+__global__ void k_wb_gather_rhs(const int *slot_perm, const int *slot_win, int n, const double *rhs, double *rhs_p,
+                                const WinState *ws) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    if (ws[slot_win[a]].active) rhs_p[a] = rhs[slot_perm[a]];
+}
+
+__global__ void k_wb_scatter_delta(const int *slot_perm, const int *slot_win, int n, const double *x_p,
+                                   double *delta, const WinState *ws) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const WinState &s = ws[slot_win[a]];
+    if (s.active && !s.factor_failed) delta[slot_perm[a]] = x_p[a];
+}
+
+// Window w's system in permuted slot order: S[a][b] from its image-level
+// blocks, damping with the window's lambda, masks, symmetrisation, and the
+// envelope. Grid: (column blocks, row, window).
+__global__ void __launch_bounds__(128) k_wb_fold(const double *__restrict__ S_img,
+                                                 const long long *__restrict__ simg_off,
+                                                 const int *__restrict__ nid_w, const int *__restrict__ n_w,
+                                                 const int *__restrict__ slot_base, const long long *__restrict__ s_off,
+                                                 const int *__restrict__ img_base, int D,
+                                                 const int *__restrict__ slot_perm,
+                                                 const int *__restrict__ pre_start, const int *__restrict__ pre,
+                                                 const unsigned char *__restrict__ masked,
+                                                 const double *__restrict__ diagB, const WinState *__restrict__ ws,
+                                                 double *__restrict__ S, double *__restrict__ L,
+                                                 int *__restrict__ row_first) {
     const int w = blockIdx.z;
     if (!ws[w].active) return;
     const int n = n_w[w];
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int a = blockIdx.y;
-    if (a >= n || b >= n) return;
-    const int ga = slot_base[w] + a, gb = slot_base[w] + b;
-    const int nid = nid_w[w];
-    const int ub = img_base[w] * D;  // first image-level index of the window
-    const double *Sw = S_img + simg_off[w];
-    double v;
-    if (masked[ga] || masked[gb]) {
-        v = a == b ? 1.0 : 0.0;
-    } else {
-        double vab = 0.0, vba = 0.0;
-        for (int x = pre_start[ga]; x < pre_start[ga + 1]; ++x)
-            for (int y = pre_start[gb]; y < pre_start[gb + 1]; ++y) {
-                const int ux = pre[x] - ub, uy = pre[y] - ub;
-                vab += Sw[(size_t)ux * nid + uy];
-                vba += Sw[(size_t)uy * nid + ux];
-            }
-        v = 0.5 * (vab + vba);
-        if (a == b) v += diagB[ga] * ws[w].lambda;
+    if (a >= n || (int)(blockIdx.x * blockDim.x) >= n) return;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sb = slot_base[w];
+    int first = 0x7fffffff;
+    if (b < n) {
+        const int ga = slot_perm[sb + a], gb = slot_perm[sb + b];
+        const int nid = nid_w[w];
+        const int ub = img_base[w] * D;  // first image-level index of the window
+        const double *Sw = S_img + simg_off[w];
+        double v;
+        if (masked[ga] || masked[gb]) {
+            v = a == b ? 1.0 : 0.0;
+        } else {
+            double vab = 0.0, vba = 0.0;
+            for (int x = pre_start[ga]; x < pre_start[ga + 1]; ++x)
+                for (int y = pre_start[gb]; y < pre_start[gb + 1]; ++y) {
+                    const int ux = pre[x] - ub, uy = pre[y] - ub;
+                    vab += Sw[(size_t)ux * nid + uy];
+                    vba += Sw[(size_t)uy * nid + ux];
+                }
+            v = 0.5 * (vab + vba);
+            if (a == b) v += diagB[ga] * ws[w].lambda;
+        }
+        S[s_off[w] + (size_t)a * n + b] = v;
+        L[s_off[w] + (size_t)a * n + b] = v;
+        if (b < a && v != 0.0) first = b;
     }
-    S[s_off[w] + (size_t)a * n + b] = v;
-    L[s_off[w] + (size_t)a * n + b] = v;
+    first = __reduce_min_sync(0xffffffffu, first);
+    if ((threadIdx.x & 31) == 0 && first < a) atomicMin(row_first + sb + a, first);
 }
 
 // ---- batched blocked Cholesky (one matrix per window, leading dim n_w)
@@ -329,7 +325,8 @@ constexpr int PANEL_ROWS = 32;
 
 __global__ void __launch_bounds__(256) k_wb_chol_panel(double *Lall, const long long *s_off, const int *n_w,
                                                         const double *Linv_all, const long long *linv_off, int k0,
-                                                        const WinState *ws) {
+                                                        const WinState *ws, const int *row_first,
+                                                        const int *slot_base) {
     extern __shared__ double sm[];
     double *Li = sm;
     double *R = sm + NB * LD;
@@ -341,6 +338,10 @@ __global__ void __launch_bounds__(256) k_wb_chol_panel(double *Lall, const long 
     const int r0 = k0 + nb + blockIdx.x * PANEL_ROWS;
     const int rows = min(PANEL_ROWS, n - r0);
     if (rows <= 0) return;
+    // rows whose envelope starts right of this column block stay zero
+    const int *rf = row_first + slot_base[w];
+    const bool outside = (int)threadIdx.x >= rows || rf[r0 + threadIdx.x] > k0 + nb - 1;
+    if (__syncthreads_and(outside)) return;
     const double *inv = Linv_all + linv_off[w] + (size_t)(k0 / NB) * NB * NB;
     for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Li[(idx / NB) * LD + idx % NB] = inv[idx];
     for (int idx = threadIdx.x; idx < rows * nb; idx += blockDim.x) {
@@ -357,7 +358,8 @@ __global__ void __launch_bounds__(256) k_wb_chol_panel(double *Lall, const long 
 }
 
 __global__ void __launch_bounds__(256) k_wb_chol_update(double *Lall, const long long *s_off, const int *n_w, int k0,
-                                                         const WinState *ws) {
+                                                         const WinState *ws, const int *row_first,
+                                                         const int *slot_base) {
     extern __shared__ double sm[];
     double *Pi = sm;
     double *Pj = sm + NB * LD;
@@ -374,6 +376,14 @@ __global__ void __launch_bounds__(256) k_wb_chol_update(double *Lall, const long
     const int ri = t0 + ti * NB, rj = t0 + tj * NB;
     if (ri >= n || rj >= n) return;
     const int mi = min(NB, n - ri), mj = min(NB, n - rj);
+    // a panel tile whose rows all start right of this column block is zero
+    const int *rf = row_first + slot_base[w];
+    const int tr = threadIdx.x;
+    const bool nzi = tr < mi && rf[ri + tr] <= k0 + NB - 1;
+    const bool nzj = tr < mj && rf[rj + tr] <= k0 + NB - 1;
+    const int any_i = __syncthreads_or(nzi);
+    const int any_j = __syncthreads_or(nzj);
+    if (!any_i || !any_j) return;
     for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
         const int r = idx / NB, c = idx - r * NB;
         Pi[r * LD + c] = r < mi ? L[(size_t)(ri + r) * n + k0 + c] : 0.0;
@@ -417,8 +427,9 @@ __global__ void __launch_bounds__(256) k_wb_chol_update(double *Lall, const long
 __global__ void __launch_bounds__(256) k_wb_chol_solve(const double *Lall, const long long *s_off, const int *n_w,
                                                         const double *Linv_all, const long long *linv_off,
                                                         const int *slot_base, const double *rhs, double *work,
-                                                        double *x, const WinState *ws) {
+                                                        double *x, const WinState *ws, const int *row_first) {
     __shared__ double yk[NB];
+    __shared__ int blk_first;
     const int w = blockIdx.x;
     if (!ws[w].active || ws[w].factor_failed) return;
     const int n = n_w[w];
@@ -427,6 +438,7 @@ __global__ void __launch_bounds__(256) k_wb_chol_solve(const double *Lall, const
     const double *Linv = Linv_all + linv_off[w];
     double *b = work + slot_base[w];
     double *xo = x + slot_base[w];
+    const int *rf = row_first + slot_base[w];
     for (int a = threadIdx.x; a < n; a += blockDim.x) b[a] = rhs[slot_base[w] + a];
     __syncthreads();
     // forward: y_k = Lkk^-1 b_k; b_r -= L[r, k] y_k for r below
@@ -441,6 +453,7 @@ __global__ void __launch_bounds__(256) k_wb_chol_solve(const double *Lall, const
         __syncthreads();
         if (threadIdx.x < nb) b[k0 + threadIdx.x] = yk[threadIdx.x];
         for (int r = k0 + nb + threadIdx.x; r < n; r += blockDim.x) {
+            if (rf[r] > k0 + nb - 1) continue;  // L[r, block] is outside the envelope
             double s = 0.0;
             for (int t = 0; t < nb; ++t) s += L[(size_t)r * n + k0 + t] * yk[t];
             b[r] -= s;
@@ -458,7 +471,12 @@ __global__ void __launch_bounds__(256) k_wb_chol_solve(const double *Lall, const
         }
         __syncthreads();
         if (threadIdx.x < nb) xo[k0 + threadIdx.x] = yk[threadIdx.x];
-        for (int r = threadIdx.x; r < k0; r += blockDim.x) {
+        if (threadIdx.x == 0) blk_first = k0;
+        __syncthreads();
+        if (threadIdx.x < nb) atomicMin(&blk_first, rf[k0 + threadIdx.x]);
+        __syncthreads();
+        // L[k0.., r] is zero for columns r left of every row's envelope
+        for (int r = blk_first + threadIdx.x; r < k0; r += blockDim.x) {
             double s = 0.0;
             for (int t = 0; t < nb; ++t) s += L[(size_t)(k0 + t) * n + r] * yk[t];
             b[r] -= s;
@@ -494,19 +512,23 @@ __global__ void k_wb_axpy(const int *slot_win, int n, const double *c, double *x
     if (s.active && !s.factor_failed) x[a] += c[a];
 }
 
-// Per-window FP64 cost: one CTA per window over its observations (windows
-// are contiguous in point-major order). mode 0 -> cost, 1 -> trial_cost.
-__global__ void __launch_bounds__(256) k_wb_cost(const double *poses, const double *cams, const double *points,
-                                                  const int *cam_of_img, const int *cam_model, const int *ob_img,
-                                                  const int *ob_pt, const double2 *ob_xy, const long long *obs_off,
-                                                  int loss, double scale, int into_trial, WinState *ws) {
+// Per-window FP64 cost in two deterministic passes: blocks of up to
+// kWinCostChunk observations (a window's observations are contiguous in
+// point-major order) write partial sums, then each window adds its blocks in
+// order. trial = 0 -> cost, valid_obs; 1 -> trial_cost, trial_valid_obs of
+// the windows whose step was solved.
+__global__ void __launch_bounds__(256) k_wb_cost_partials(
+    const double *poses, const double *cams, const double *points, const int *cam_of_img, const int *cam_model,
+    const int *ob_img, const int *ob_pt, const double2 *ob_xy, const int *cblk_win, const long long *cblk_lo,
+    int loss, double scale, int trial, const WinState *ws, double *cpart, long long *cpart_n) {
     __shared__ double ssum[256];
     __shared__ long long scnt[256];
-    const int w = blockIdx.x;
-    if (into_trial && !(ws[w].active && !ws[w].factor_failed)) return;
+    const int blk = blockIdx.x;
+    const int w = cblk_win[blk];
+    if (trial && !(ws[w].active && !ws[w].factor_failed)) return;
     double sum = 0.0;
     long long cnt = 0;
-    for (long long o = obs_off[w] + threadIdx.x; o < obs_off[w + 1]; o += blockDim.x) {
+    for (long long o = cblk_lo[blk] + threadIdx.x; o < cblk_lo[blk + 1]; o += blockDim.x) {
         const int i = ob_img[o], p = ob_pt[o];
         const int c = cam_of_img[i];
         const double *X = points + 3 * (size_t)p;
@@ -526,21 +548,37 @@ __global__ void __launch_bounds__(256) k_wb_cost(const double *poses, const doub
     ssum[threadIdx.x] = sum;
     scnt[threadIdx.x] = cnt;
     __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            ssum[threadIdx.x] += ssum[threadIdx.x + s];
-            scnt[threadIdx.x] += scnt[threadIdx.x + s];
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            ssum[threadIdx.x] += ssum[threadIdx.x + h];
+            scnt[threadIdx.x] += scnt[threadIdx.x + h];
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        if (into_trial) {
-            ws[w].trial_cost = ssum[0];
-            ws[w].trial_valid_obs = scnt[0];
-        } else {
-            ws[w].cost = ssum[0];
-            ws[w].valid_obs = scnt[0];
-        }
+        cpart[blk] = ssum[0];
+        cpart_n[blk] = scnt[0];
+    }
+}
+
+__global__ void k_wb_cost_finalize(const int *wblk_start, const double *cpart, const long long *cpart_n, int W,
+                                   int trial, WinState *ws) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    WinState &s = ws[w];
+    if (trial && !(s.active && !s.factor_failed)) return;
+    double sum = 0.0;
+    long long cnt = 0;
+    for (int k = wblk_start[w]; k < wblk_start[w + 1]; ++k) {
+        sum += cpart[k];
+        cnt += cpart_n[k];
+    }
+    if (trial) {
+        s.trial_cost = sum;
+        s.trial_valid_obs = cnt;
+    } else {
+        s.cost = sum;
+        s.valid_obs = cnt;
     }
 }
 
@@ -802,6 +840,14 @@ void launch_wb_window_of_points(const int *win_of_input_point, const int *perm, 
     SFMBA_LAUNCH_CHECK();
 }
 
+void launch_wb_live(const Bufs &b, const WinBufs &w, bool retry, cudaStream_t s) {
+    const long long m = b.nP > b.nI ? b.nP : b.nI;
+    if (m == 0) return;
+    k_wb_live<<<div_up(m, 256), 256, 0, s>>>(w.ws, w.img_win, w.pt_win, b.nI, b.nP, retry ? 1 : 0, b.img_live,
+                                             b.pt_live);
+    SFMBA_LAUNCH_CHECK();
+}
+
 void launch_wb_init(const WinBufs &w, double initial_lambda, cudaStream_t s) {
     k_wb_init<<<grid1(w.W), 128, 0, s>>>(w.ws, w.n_w, w.W, initial_lambda);
     SFMBA_LAUNCH_CHECK();
@@ -822,11 +868,13 @@ void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s) {
     if (b.mixed)
         k_wb_point_inverse<float><<<div_up(b.nP, 256), 256, 0, s>>>((const float *)b.pt_C, (const float *)b.pt_g,
                                                                     b.pt_nfree, w.pt_win, w.ws, b.nP,
-                                                                    (float *)b.pt_Cinv, (float *)b.pt_h, b.pt_ok);
+                                                                    (float *)b.pt_Cinv, (float *)b.pt_h, b.pt_ok,
+                                                                    b.pt_live);
     else
         k_wb_point_inverse<double><<<div_up(b.nP, 256), 256, 0, s>>>((const double *)b.pt_C, (const double *)b.pt_g,
                                                                      b.pt_nfree, w.pt_win, w.ws, b.nP,
-                                                                     (double *)b.pt_Cinv, (double *)b.pt_h, b.pt_ok);
+                                                                     (double *)b.pt_Cinv, (double *)b.pt_h, b.pt_ok,
+                                                                     b.pt_live);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -834,13 +882,12 @@ void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s) {
     if (b.ngroups == 0) return;
     dispatch_D(b.D, [&](auto dc) {
         constexpr int D = decltype(dc)::value;
-        const int grid = div_up(b.ngroups, kWarps);
         if (b.mixed)
-            k_wb_schur_pairs<float, D><<<grid, 32 * kWarps, 0, s>>>(
+            k_wb_schur_pairs<float, D><<<div_up(b.ngroups, schur_warps<float>()), 32 * schur_warps<float>(), 0, s>>>(
                 (const float *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt, (const float *)b.pt_Cinv,
                 b.pt_ok, b.img_H, w.img_win, w.img_base, w.nid_w, w.simg_off, w.ws, b.S_img);
         else
-            k_wb_schur_pairs<double, D><<<grid, 32 * kWarps, 0, s>>>(
+            k_wb_schur_pairs<double, D><<<div_up(b.ngroups, schur_warps<double>()), 32 * schur_warps<double>(), 0, s>>>(
                 (const double *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
                 (const double *)b.pt_Cinv, b.pt_ok, b.img_H, w.img_win, w.img_base, w.nid_w, w.simg_off, w.ws,
                 b.S_img);
@@ -849,10 +896,15 @@ void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s) {
 }
 
 void launch_wb_fold(const Bufs &b, const WinBufs &w, cudaStream_t s) {
-    if (w.max_n == 0) return;
+    if (w.max_n == 0 || b.n == 0) return;
+    k_wb_envelope_init<<<div_up(b.n, 256), 256, 0, s>>>(w.slot_win, w.slot_base, b.n, w.ws, w.row_first);
+    SFMBA_LAUNCH_CHECK();
+    k_wb_gather_rhs<<<div_up(b.n, 256), 256, 0, s>>>(w.slot_perm, w.slot_win, b.n, b.rhs, w.rhs_p, w.ws);
+    SFMBA_LAUNCH_CHECK();
     dim3 grid(div_up(w.max_n, 128), w.max_n, w.W);
     k_wb_fold<<<grid, 128, 0, s>>>(b.S_img, w.simg_off, w.nid_w, w.n_w, w.slot_base, w.s_off, w.img_base, b.D,
-                                   b.slot_pre_start, b.slot_pre, b.slot_masked, b.diagB, w.ws, b.S, b.L);
+                                   w.slot_perm, b.slot_pre_start, b.slot_pre, b.slot_masked, b.diagB, w.ws, b.S,
+                                   b.L, w.row_first);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -864,34 +916,49 @@ void launch_wb_cholesky(const Bufs &b, const WinBufs &w, cudaStream_t s) {
         const int rem = w.max_n - k0 - NB;
         if (rem <= 0) break;
         dim3 gp(div_up(rem, PANEL_ROWS), w.W);
-        k_wb_chol_panel<<<gp, 256, kSmemPanel, s>>>(b.L, w.s_off, w.n_w, b.Linv, w.linv_off, k0, w.ws);
+        k_wb_chol_panel<<<gp, 256, kSmemPanel, s>>>(b.L, w.s_off, w.n_w, b.Linv, w.linv_off, k0, w.ws, w.row_first,
+                                                    w.slot_base);
         SFMBA_LAUNCH_CHECK();
         const long long tiles = div_up(rem, NB);
         dim3 gu((unsigned)(tiles * (tiles + 1) / 2), w.W);
-        k_wb_chol_update<<<gu, 256, kSmemTwoTiles, s>>>(b.L, w.s_off, w.n_w, k0, w.ws);
+        k_wb_chol_update<<<gu, 256, kSmemTwoTiles, s>>>(b.L, w.s_off, w.n_w, k0, w.ws, w.row_first, w.slot_base);
         SFMBA_LAUNCH_CHECK();
     }
 }
 
+// Solves of the permuted window systems: rhs_p -> x_p = b.work2 (b.work is
+// the solve's scratch).
 void launch_wb_solve(const Bufs &b, const WinBufs &w, const double *rhs, double *x, cudaStream_t s) {
-    k_wb_chol_solve<<<w.W, 256, 0, s>>>(b.L, w.s_off, w.n_w, b.Linv, w.linv_off, w.slot_base, rhs, b.work, x, w.ws);
+    k_wb_chol_solve<<<w.W, 256, 0, s>>>(b.L, w.s_off, w.n_w, b.Linv, w.linv_off, w.slot_base, rhs, b.work, x, w.ws,
+                                        w.row_first);
     SFMBA_LAUNCH_CHECK();
 }
 
 void launch_wb_refine(const Bufs &b, const WinBufs &w, cudaStream_t s) {
-    k_wb_residual<<<w.W, 256, 0, s>>>(b.S, w.s_off, w.n_w, w.slot_base, b.delta, b.rhs, b.ref_res, w.ws);
+    k_wb_residual<<<w.W, 256, 0, s>>>(b.S, w.s_off, w.n_w, w.slot_base, b.work2, w.rhs_p, b.ref_res, w.ws);
     SFMBA_LAUNCH_CHECK();
     launch_wb_solve(b, w, b.ref_res, b.ref_corr, s);
     if (b.n > 0) {
-        k_wb_axpy<<<div_up(b.n, 256), 256, 0, s>>>(w.slot_win, b.n, b.ref_corr, b.delta, w.ws);
+        k_wb_axpy<<<div_up(b.n, 256), 256, 0, s>>>(w.slot_win, b.n, b.ref_corr, b.work2, w.ws);
         SFMBA_LAUNCH_CHECK();
     }
 }
 
+void launch_wb_scatter(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    if (b.n == 0) return;
+    k_wb_scatter_delta<<<div_up(b.n, 256), 256, 0, s>>>(w.slot_perm, w.slot_win, b.n, b.work2, b.delta, w.ws);
+    SFMBA_LAUNCH_CHECK();
+}
+
 void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s) {
-    k_wb_cost<<<w.W, 256, 0, s>>>(trial ? b.poses_trial : b.poses, trial ? b.cams_trial : b.cams,
-                                  trial ? b.points_trial : b.points, b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt,
-                                  b.ob_xy, w.obs_off, b.loss, b.loss_scale, trial ? 1 : 0, w.ws);
+    if (w.ncblk > 0) {
+        k_wb_cost_partials<<<w.ncblk, 256, 0, s>>>(
+            trial ? b.poses_trial : b.poses, trial ? b.cams_trial : b.cams, trial ? b.points_trial : b.points,
+            b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt, b.ob_xy, w.cblk_win, w.cblk_lo, b.loss, b.loss_scale,
+            trial ? 1 : 0, w.ws, w.cpart, w.cpart_n);
+        SFMBA_LAUNCH_CHECK();
+    }
+    k_wb_cost_finalize<<<grid1(w.W), 128, 0, s>>>(w.wblk_start, w.cpart, w.cpart_n, w.W, trial ? 1 : 0, w.ws);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -930,7 +997,7 @@ void launch_wb_summary(const WinBufs &w, cudaStream_t s) {
 }
 
 void launch_wb_lu(const Bufs &b, const WinBufs &w, cudaStream_t s) {
-    k_wb_lu<<<w.W, 1024, 0, s>>>(b.S, b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm, b.rhs, b.delta, w.ws);
+    k_wb_lu<<<w.W, 1024, 0, s>>>(b.S, b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm, w.rhs_p, b.work2, w.ws);
     SFMBA_LAUNCH_CHECK();
 }
 

@@ -12,105 +12,43 @@
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "schur.cuh"
 
 namespace sfmba {
 
 namespace {
 
 template <typename T>
-__device__ __forceinline__ void kahan_add(T &s, T &c, T x) {
-    if constexpr (std::is_same<T, float>::value) {
-        const T y = x - c;
-        const T t = s + y;
-        c = (t - s) - y;
-        s = t;
-    } else {
-        s += x;
-    }
-}
-
-constexpr int kSchurWarps = 2;
+constexpr int schur_warps() { return sizeof(T) == 4 ? 4 : 2; }
 
 template <typename T, int D>
-__global__ void __launch_bounds__(32 * kSchurWarps)
+__global__ void __launch_bounds__(32 * schur_warps<T>())
     k_schur_pairs(const T *__restrict__ rec, const int2 *__restrict__ pairs,
                   const int *__restrict__ group_start, const int2 *__restrict__ group_ij, int ngroups,
                   const int *__restrict__ ob_pt, const T *__restrict__ pt_Cinv,
                   const unsigned char *__restrict__ pt_ok, const double *__restrict__ img_H, int nID,
                   double *__restrict__ S_img) {
-    constexpr int RS = RecLayout<D>::kStride;
-    constexpr int NE = (D * D + 31) / 32;
-    __shared__ T sM[kSchurWarps][32][4];
-    __shared__ T sA[kSchurWarps][32][2 * D];
-    __shared__ T sB[kSchurWarps][32][2 * D];
+    constexpr int W = schur_warps<T>();
+    using Tile = SchurTile<T, D>;
+    __shared__ T sA[W][32][Tile::LDS];
+    __shared__ T sP[W][32][Tile::LDS];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = blockIdx.x * kSchurWarps + wl;
+    const int g = blockIdx.x * W + wl;
     if (g >= ngroups) return;
     const int2 ij = group_ij[g];
-    const int gs = group_start[g], ge = group_start[g + 1];
-    T acc[NE], comp[NE];
-#pragma unroll
-    for (int k = 0; k < NE; ++k) acc[k] = comp[k] = T(0);
-    for (int base = gs; base < ge; base += 32) {
-        const int e = base + lane;
-        if (e < ge) {
-            const int2 ab = pairs[e];
-            const int p = ob_pt[ab.x];
-            const T *ra = rec + (size_t)ab.x * RS;
-            const T *rb = rec + (size_t)ab.y * RS;
-            if (pt_ok[p]) {
-                const T *Ci = pt_Cinv + 6 * (size_t)p;
-                const T c00 = Ci[0], c01 = Ci[1], c02 = Ci[2], c11 = Ci[3], c12 = Ci[4], c22 = Ci[5];
-                // U = Jx~_a C^-1 (2x3), M = U Jx~_b^T (2x2)
-                T U[2][3];
-#pragma unroll
-                for (int r = 0; r < 2; ++r) {
-                    const T x0 = ra[2 + 3 * r], x1 = ra[3 + 3 * r], x2 = ra[4 + 3 * r];
-                    U[r][0] = x0 * c00 + x1 * c01 + x2 * c02;
-                    U[r][1] = x0 * c01 + x1 * c11 + x2 * c12;
-                    U[r][2] = x0 * c02 + x1 * c12 + x2 * c22;
-                }
-#pragma unroll
-                for (int r = 0; r < 2; ++r)
-#pragma unroll
-                    for (int q = 0; q < 2; ++q)
-                        sM[wl][lane][2 * r + q] = U[r][0] * rb[2 + 3 * q] + U[r][1] * rb[3 + 3 * q] + U[r][2] * rb[4 + 3 * q];
-#pragma unroll
-                for (int f = 0; f < 2 * D; ++f) {
-                    sA[wl][lane][f] = ra[8 + f];
-                    sB[wl][lane][f] = rb[8 + f];
-                }
-            } else {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) sM[wl][lane][q] = T(0);
-#pragma unroll
-                for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = sB[wl][lane][f] = T(0);
-            }
-        }
-        __syncwarp();
-        const int cnt = min(32, ge - base);
-        for (int t = 0; t < cnt; ++t) {
-            const T m0 = sM[wl][t][0], m1 = sM[wl][t][1], m2 = sM[wl][t][2], m3 = sM[wl][t][3];
-#pragma unroll
-            for (int k = 0; k < NE; ++k) {
-                const int idx = lane + 32 * k;
-                if (idx < D * D) {
-                    const int r = idx / D, c = idx - r * D;
-                    const T b0 = sB[wl][t][c], b1 = sB[wl][t][D + c];
-                    kahan_add(acc[k], comp[k],
-                              sA[wl][t][r] * (m0 * b0 + m1 * b1) + sA[wl][t][D + r] * (m2 * b0 + m3 * b1));
-                }
-            }
-        }
-        __syncwarp();
-    }
+    double out[Tile::RH][Tile::CQ];
+    schur_group<T, D>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl], lane,
+                      out);
+    if (lane >= 8) return;
     const int i = ij.x, j = ij.y;
+    const int r0 = (lane >> 2) * Tile::RH, c0 = (lane & 3) * Tile::CQ;
 #pragma unroll
-    for (int k = 0; k < NE; ++k) {
-        const int idx = lane + 32 * k;
-        if (idx < D * D) {
-            const int r = idx / D, c = idx - r * D;
-            const double v = -((double)acc[k] - (double)comp[k]);
+    for (int a = 0; a < Tile::RH; ++a)
+#pragma unroll
+        for (int b = 0; b < Tile::CQ; ++b) {
+            const int r = r0 + a, c = c0 + b;
+            if (r >= D || c >= D) continue;
+            const double v = out[a][b];
             if (i == j) {
                 S_img[(size_t)(i * D + r) * nID + i * D + c] = img_H[(size_t)i * D * D + r * D + c] + v;
             } else {
@@ -118,7 +56,6 @@ __global__ void __launch_bounds__(32 * kSchurWarps)
                 S_img[(size_t)(j * D + c) * nID + i * D + r] = v;
             }
         }
-    }
 }
 
 // S[a][b] = sym( sum_{u in pre(a), w in pre(b)} S_img[u][w] ) + [a==b] lambda diag(B)[a];
@@ -519,13 +456,12 @@ void launch_schur_pairs(const Bufs &b, cudaStream_t s) {
     if (b.ngroups == 0) return;
     dispatch_D(b.D, [&](auto dc) {
         constexpr int D = decltype(dc)::value;
-        const int grid = div_up(b.ngroups, kSchurWarps);
         if (b.mixed)
-            k_schur_pairs<float, D><<<grid, 32 * kSchurWarps, 0, s>>>(
+            k_schur_pairs<float, D><<<div_up(b.ngroups, schur_warps<float>()), 32 * schur_warps<float>(), 0, s>>>(
                 (const float *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
                 (const float *)b.pt_Cinv, b.pt_ok, b.img_H, b.nID, b.S_img);
         else
-            k_schur_pairs<double, D><<<grid, 32 * kSchurWarps, 0, s>>>(
+            k_schur_pairs<double, D><<<div_up(b.ngroups, schur_warps<double>()), 32 * schur_warps<double>(), 0, s>>>(
                 (const double *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
                 (const double *)b.pt_Cinv, b.pt_ok, b.img_H, b.nID, b.S_img);
     });

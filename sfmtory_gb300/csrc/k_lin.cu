@@ -36,7 +36,7 @@ __device__ __forceinline__ void quat_to_R(const double *q, double R[9]) {
 template <typename T>
 __global__ void k_prepare_images(const double *poses, const double *cams, const int *cam_of_img,
                                  const int *cam_model, const int *img_active, int nI,
-                                 ImageLin<T> *out) {
+                                 ImageLin<T> *out, ImageLin<double> *out64) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nI) return;
     const double *q = poses + 7 * (size_t)i;
@@ -53,6 +53,18 @@ __global__ void k_prepare_images(const double *poses, const double *cams, const 
     im.active = img_active[i];
     im.pad[0] = im.pad[1] = 0;
     out[i] = im;
+    if (out64) {
+        ImageLin<double> d;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) d.R[k] = R[k];
+        d.t[0] = q[4]; d.t[1] = q[5]; d.t[2] = q[6];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) d.c[k] = cams[8 * (size_t)c + k];
+        d.model = im.model;
+        d.active = im.active;
+        d.pad[0] = d.pad[1] = 0;
+        out64[i] = d;
+    }
 }
 
 template <typename T>
@@ -71,18 +83,26 @@ __global__ void __launch_bounds__(256) k_linearize(const ImageLin<T> *img_lin, c
                                                    const float4 *points32, const int *ob_img,
                                                    const int *ob_pt, const double2 *ob_xy,
                                                    long long nO, int loss, T scale, T *rec,
-                                                   unsigned char *ob_valid) {
+                                                   unsigned char *ob_valid, const ImageLin<double> *lin64,
+                                                   const unsigned char *img_live) {
     constexpr int RS = RecLayout<D>::kStride;
     long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (o >= nO) return;
     const int i = ob_img[o], p = ob_pt[o];
+    if (img_live && !img_live[i]) return;
     const ImageLin<T> im = img_lin[i];
     T X0, X1, X2;
     load_point<T>(points, points32, p, X0, X1, X2);
     const double2 xy = ob_xy[o];
+    Res64 rin;
+    if (lin64) {  // FP32 records: residual and weight from the FP64 parameters
+        rin.use = true;
+        rin.ok = residual64_lin(lin64[i], points[3 * (size_t)p], points[3 * (size_t)p + 1], points[3 * (size_t)p + 2],
+                                xy.x, xy.y, rin.r0, rin.r1);
+    }
     T buf[RS];
     T rr[2], jx[6], jc[2 * D];
-    const bool ok = linearize<T, D>(im, X0, X1, X2, (T)xy.x, (T)xy.y, loss, scale, rr, jx, jc);
+    const bool ok = linearize<T, D>(im, X0, X1, X2, (T)xy.x, (T)xy.y, loss, scale, rr, jx, jc, nullptr, rin);
     buf[0] = rr[0]; buf[1] = rr[1];
 #pragma unroll
     for (int k = 0; k < 6; ++k) buf[2 + k] = jx[k];
@@ -107,10 +127,11 @@ __global__ void __launch_bounds__(256) k_linearize(const ImageLin<T> *img_lin, c
 template <typename T, int D>
 __global__ void k_point_reduce(const T *rec, const int *pt_start, const int *ob_img,
                                const unsigned char *ob_valid, const int *img_free, int nP, T *pt_C,
-                               T *pt_g, int *pt_nfree) {
+                               T *pt_g, int *pt_nfree, const unsigned char *pt_live) {
     constexpr int RS = RecLayout<D>::kStride;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nP) return;
+    if (pt_live && !pt_live[p]) return;
     const int s = pt_start[p], e = pt_start[p + 1];
     T c00 = 0, c01 = 0, c02 = 0, c11 = 0, c12 = 0, c22 = 0, g0 = 0, g1 = 0, g2 = 0;
     int nfree = 0;
@@ -137,7 +158,7 @@ __global__ void k_point_reduce(const T *rec, const int *pt_start, const int *ob_
 template <typename T, int D>
 __global__ void __launch_bounds__(128) k_image_reduce(const T *rec, const int *img_start,
                                                       const int *img_obs, int nI, double *img_H,
-                                                      double *img_b) {
+                                                      double *img_b, const unsigned char *img_live) {
     constexpr int RS = RecLayout<D>::kStride;
     constexpr int F = 2 * D + 2;  // Jc~ (2D) then r~ (2)
     constexpr int CH = 32;
@@ -145,6 +166,7 @@ __global__ void __launch_bounds__(128) k_image_reduce(const T *rec, const int *i
     __shared__ T sh[CH][F + 1];
     const int i = blockIdx.x;
     if (i >= nI) return;
+    if (img_live && !img_live[i]) return;
     const int tid = threadIdx.x;
     int ea = 0, eb = 0;
     const bool isH = tid < NH;
@@ -244,12 +266,13 @@ __global__ void k_point_inverse(const T *pt_C, const T *pt_g, const int *pt_nfre
 template <typename T, int D>
 __global__ void k_image_rhs(const T *rec, const int *img_start, const int *img_obs,
                             const int *ob_pt, const T *pt_h, const unsigned char *pt_ok,
-                            const double *img_b, int nI, double *img_rhs) {
+                            const double *img_b, int nI, double *img_rhs, const unsigned char *img_live) {
     constexpr int RS = RecLayout<D>::kStride;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nI) return;
     const int i = warp;
+    if (img_live && !img_live[i]) return;
     T acc[D], comp[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) acc[c] = comp[c] = T(0);
@@ -287,11 +310,13 @@ __global__ void k_gather_delta(const double *delta_slot, const int *img_slot, in
 template <typename T, int D>
 __global__ void k_backsub(const T *rec, const int *pt_start, const int *ob_img, const T *img_delta,
                           const T *pt_Cinv, const T *pt_g, const unsigned char *pt_ok,
-                          const double *points, const LMState *state, int nP, double *points_trial) {
+                          const double *points, const LMState *state, int nP, double *points_trial,
+                          const unsigned char *pt_live) {
     constexpr int RS = RecLayout<D>::kStride;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nP) return;
     if (state->factor_failed) return;
+    if (pt_live && !pt_live[p]) return;
     const double *X = points + 3 * (size_t)p;
     double *Y = points_trial + 3 * (size_t)p;
     if (!pt_ok[p]) {
@@ -546,10 +571,12 @@ void launch_prepare_images(const Bufs &b, cudaStream_t s) {
     if (b.nI == 0) return;
     if (b.mixed)
         k_prepare_images<float><<<div_up(b.nI, 128), 128, 0, s>>>(
-            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin);
+            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin,
+            (ImageLin<double> *)b.img_lin64);
     else
         k_prepare_images<double><<<div_up(b.nI, 128), 128, 0, s>>>(
-            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<double> *)b.img_lin);
+            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<double> *)b.img_lin,
+            nullptr);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -560,11 +587,12 @@ void launch_linearize(const Bufs &b, cudaStream_t s) {
         if (b.mixed)
             k_linearize<float, D><<<div_up(b.nO, 256), 256, 0, s>>>(
                 (const ImageLin<float> *)b.img_lin, b.points, b.points32, b.ob_img, b.ob_pt, b.ob_xy,
-                b.nO, b.loss, (float)b.loss_scale, (float *)b.rec, b.ob_valid);
+                b.nO, b.loss, (float)b.loss_scale, (float *)b.rec, b.ob_valid,
+                (const ImageLin<double> *)b.img_lin64, b.img_live);
         else
             k_linearize<double, D><<<div_up(b.nO, 256), 256, 0, s>>>(
                 (const ImageLin<double> *)b.img_lin, b.points, b.points32, b.ob_img, b.ob_pt, b.ob_xy,
-                b.nO, b.loss, b.loss_scale, (double *)b.rec, b.ob_valid);
+                b.nO, b.loss, b.loss_scale, (double *)b.rec, b.ob_valid, nullptr, b.img_live);
     });
     SFMBA_LAUNCH_CHECK();
 }
@@ -576,11 +604,11 @@ void launch_point_reduce(const Bufs &b, cudaStream_t s) {
         if (b.mixed)
             k_point_reduce<float, D><<<div_up(b.nP, 128), 128, 0, s>>>(
                 (const float *)b.rec, b.pt_start, b.ob_img, b.ob_valid, b.img_free, b.nP,
-                (float *)b.pt_C, (float *)b.pt_g, b.pt_nfree);
+                (float *)b.pt_C, (float *)b.pt_g, b.pt_nfree, b.pt_live);
         else
             k_point_reduce<double, D><<<div_up(b.nP, 128), 128, 0, s>>>(
                 (const double *)b.rec, b.pt_start, b.ob_img, b.ob_valid, b.img_free, b.nP,
-                (double *)b.pt_C, (double *)b.pt_g, b.pt_nfree);
+                (double *)b.pt_C, (double *)b.pt_g, b.pt_nfree, b.pt_live);
     });
     SFMBA_LAUNCH_CHECK();
 }
@@ -591,10 +619,10 @@ void launch_image_reduce(const Bufs &b, cudaStream_t s) {
         constexpr int D = decltype(dc)::value;
         if (b.mixed)
             k_image_reduce<float, D><<<b.nI, 128, 0, s>>>((const float *)b.rec, b.img_start,
-                                                          b.img_obs, b.nI, b.img_H, b.img_b);
+                                                          b.img_obs, b.nI, b.img_H, b.img_b, b.img_live);
         else
             k_image_reduce<double, D><<<b.nI, 128, 0, s>>>((const double *)b.rec, b.img_start,
-                                                           b.img_obs, b.nI, b.img_H, b.img_b);
+                                                           b.img_obs, b.nI, b.img_H, b.img_b, b.img_live);
     });
     SFMBA_LAUNCH_CHECK();
 }
@@ -627,11 +655,11 @@ void launch_image_rhs(const Bufs &b, cudaStream_t s) {
         if (b.mixed)
             k_image_rhs<float, D><<<div_up(b.nI, warps_per_block), 32 * warps_per_block, 0, s>>>(
                 (const float *)b.rec, b.img_start, b.img_obs, b.ob_pt, (const float *)b.pt_h, b.pt_ok,
-                b.img_b, b.nI, b.img_rhs);
+                b.img_b, b.nI, b.img_rhs, b.img_live);
         else
             k_image_rhs<double, D><<<div_up(b.nI, warps_per_block), 32 * warps_per_block, 0, s>>>(
                 (const double *)b.rec, b.img_start, b.img_obs, b.ob_pt, (const double *)b.pt_h,
-                b.pt_ok, b.img_b, b.nI, b.img_rhs);
+                b.pt_ok, b.img_b, b.nI, b.img_rhs, b.img_live);
     });
     SFMBA_LAUNCH_CHECK();
 }
@@ -656,12 +684,12 @@ void launch_backsub_update(const Bufs &b, const double *delta_slot, cudaStream_t
                 k_backsub<float, D><<<div_up(b.nP, 128), 128, 0, s>>>(
                     (const float *)b.rec, b.pt_start, b.ob_img, (const float *)b.img_delta,
                     (const float *)b.pt_Cinv, (const float *)b.pt_g, b.pt_ok, b.points, b.state, b.nP,
-                    b.points_trial);
+                    b.points_trial, b.pt_live);
             else
                 k_backsub<double, D><<<div_up(b.nP, 128), 128, 0, s>>>(
                     (const double *)b.rec, b.pt_start, b.ob_img, (const double *)b.img_delta,
                     (const double *)b.pt_Cinv, (const double *)b.pt_g, b.pt_ok, b.points, b.state,
-                    b.nP, b.points_trial);
+                    b.nP, b.points_trial, b.pt_live);
         });
         SFMBA_LAUNCH_CHECK();
     }

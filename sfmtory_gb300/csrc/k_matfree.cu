@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) k_mf_point_reduce(JacSrc<T> J, const unsi
         J.obrec, pchunk[warp], pchunk[warp + 1], lane,
         [&](int o, int4 rc, T (&v)[10]) {
             ObsOp<T, D, RC> op;
-            make_op_point_major<T, D, RC>(J, o, rc, op);
+            make_op_point_major<T, D, RC>(J, o, rc, op, true);
             bool ok = op.valid;
             if constexpr (!RC) ok = ob_valid[o] != 0;
             T jx[6];
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(128) k_mf_image_accum(JacSrc<T> J, long long n
             img = rc.x;
             const int pt = rc.y;
             ObsOp<T, D, RC> op;
-            make_op_image_major<T, D, RC>(J, k, rc, op);
+            make_op_image_major<T, D, RC>(J, k, rc, op, MODE == 0);
             op.jc_rows(jc);
             op.jx_rows(jx);
             if constexpr (MODE == 0) {
@@ -578,6 +578,12 @@ JacSrc<T> jac_src(const Bufs &b) {
     J.img_obs = b.img_obs;
     J.loss = b.loss;
     J.scale = (T)b.loss_scale;
+    if constexpr (std::is_same<T, float>::value) {
+        J.lin64 = (const ImageLin<double> *)b.img_lin64;
+        J.pts64 = b.points;
+        J.ob_xy = b.ob_xy;
+        J.rs = b.ob_rs;
+    }
     return J;
 }
 

@@ -42,6 +42,8 @@ struct Bufs {
     unsigned char *slot_masked = nullptr;  // [n]
     // linearisation (element type float or double by `mixed`)
     void *img_lin = nullptr;      // [nI] ImageLin<T>
+    void *img_lin64 = nullptr;    // [nI] ImageLin<double> for FP64 residuals (FP32 path)
+    float4 *ob_rs = nullptr;      // [nO] point-major FP64-derived residual, sqrt(weight), valid (FP32 PCG path)
     void *rec = nullptr;          // [nO * stride] records
     unsigned char *ob_valid = nullptr;  // [nO]
     void *pt_C = nullptr;         // [nP*6] symmetric 3x3 (00 01 02 11 12 22)
@@ -86,6 +88,10 @@ struct Bufs {
     int nparts = 0;
     int4 *obrec = nullptr;        // [nO] point-major {image, point, x, y (float bits)}
     int4 *isrec = nullptr;        // [nO] image-major {image, point, x, y (float bits)}
+    // Batched windows: per-image / per-point "take part" flags of the current
+    // phase (NULL: everything takes part). Kernels skip the rest.
+    unsigned char *img_live = nullptr;  // [nI]
+    unsigned char *pt_live = nullptr;   // [nP]
 };
 
 // Levenberg-Marquardt state of one window of a batched solve.
@@ -124,7 +130,19 @@ struct WinBufs {
     long long *linv_off = nullptr; // [W] offset of its diagonal-block inverses in Linv
     long long *obs_off = nullptr;  // [W+1] observation range (point-major order)
     int *counts = nullptr;         // [4] summary read by the host each retry
+    int *slot_perm = nullptr;      // [n] position in the window systems -> slot
+    int *row_first = nullptr;      // [n] first nonzero column of each permuted row
+    double *rhs_p = nullptr;       // [n] right-hand side in permuted order
+    // cost blocks: up to kWinCostChunk observations of one window each
+    int ncblk = 0;
+    int *cblk_win = nullptr;       // [ncblk] window of the block
+    long long *cblk_lo = nullptr;  // [ncblk+1] observation range of the block
+    int *wblk_start = nullptr;     // [W+1] first block of each window
+    double *cpart = nullptr;       // [ncblk] partial cost
+    long long *cpart_n = nullptr;  // [ncblk] partial valid count
 };
+
+constexpr int kWinCostChunk = 8192;
 
 constexpr int kCostBlocks = 1024;
 constexpr int kDotSlots = 16;
@@ -223,6 +241,8 @@ enum { WB_NOT_DONE = 0, WB_RETRY_PENDING = 1, WB_FACTOR_FAILED = 2, WB_WANTS_POL
 void launch_wb_window_of_points(const int *win_of_input_point, const int *perm, int nP, int *pt_win,
                                 cudaStream_t s);
 void launch_wb_init(const WinBufs &w, double initial_lambda, cudaStream_t s);
+// img_live / pt_live for the next phase: windows not done (retry = false) or retrying.
+void launch_wb_live(const Bufs &b, const WinBufs &w, bool retry, cudaStream_t s);
 void launch_wb_begin_outer(const WinBufs &w, int max_iterations, cudaStream_t s);
 void launch_wb_begin_retry(const WinBufs &w, cudaStream_t s);
 void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s);
@@ -231,6 +251,8 @@ void launch_wb_fold(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_cholesky(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_solve(const Bufs &b, const WinBufs &w, const double *rhs, double *x, cudaStream_t s);
 void launch_wb_refine(const Bufs &b, const WinBufs &w, cudaStream_t s);
+// delta (slot order) from the permuted solution of the retrying windows
+void launch_wb_scatter(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_lu(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s);
 void launch_wb_accept_commit(const Bufs &b, const WinBufs &w, cudaStream_t s);

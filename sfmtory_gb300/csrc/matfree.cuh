@@ -34,6 +34,13 @@ struct JacSrc {
     const int *img_obs = nullptr;            // image-major -> point-major index
     int loss = 0;
     T scale = T(1);
+    // FP64 residuals of gradient terms (FP32 operators only): per-image FP64
+    // constants, FP64 points and pixels, and the point-major store of the
+    // residual and weight the point pass computes for the image pass.
+    const ImageLin<double> *lin64 = nullptr;
+    const double *pts64 = nullptr;
+    const double2 *ob_xy = nullptr;
+    float4 *rs = nullptr;
 };
 
 // Jr~, Jx~ (2x3), Jc~ (2xD) of a stored record, 16-byte vector loads.
@@ -79,7 +86,11 @@ struct ObsOp<T, D, true> {
     T R[9];
     bool valid;
 
-    __device__ __forceinline__ void build(const JacSrc<T> &J, int img, int pt, int4 rc) {
+    // Gradient terms of the FP32 path replace the FP32 residual and weight of
+    // point-major observation o64 (>= 0): mode 1 computes them in FP64 and
+    // stores them, mode 2 loads the stored ones.
+    __device__ __forceinline__ void build(const JacSrc<T> &J, int img, int pt, int4 rc, long long o64 = -1,
+                                          int mode = 0) {
         const ImageLin<T> im = J.img_lin[img];
         T X0, X1, X2;
         if constexpr (std::is_same<T, float>::value) {
@@ -88,8 +99,26 @@ struct ObsOp<T, D, true> {
         } else {
             X0 = J.points64[3 * (size_t)pt]; X1 = J.points64[3 * (size_t)pt + 1]; X2 = J.points64[3 * (size_t)pt + 2];
         }
+        Res64 rin;
+        if (o64 >= 0 && J.lin64) {
+            rin.use = true;
+            if (mode == 2) {
+                const float4 v = J.rs[o64];
+                rin.r0 = v.x; rin.r1 = v.y; rin.s = v.z; rin.ok = v.w != 0.f;
+            } else {
+                const double2 xy = J.ob_xy[o64];
+                const double *P = J.pts64 + 3 * (size_t)pt;
+                rin.ok = residual64_lin(J.lin64[img], P[0], P[1], P[2], xy.x, xy.y, rin.r0, rin.r1);
+                if (rin.ok)
+                    rin.s = J.loss == SFMBA_LOSS_NONE
+                                ? 1.0
+                                : sqrt(robust_weight<double>(sqrt(rin.r0 * rin.r0 + rin.r1 * rin.r1), J.loss,
+                                                             (double)J.scale));
+                if (J.rs) J.rs[o64] = make_float4((float)rin.r0, (float)rin.r1, (float)rin.s, rin.ok ? 1.f : 0.f);
+            }
+        }
         valid = linearize_compact<T, D>(im, X0, X1, X2, (T)__int_as_float(rc.z), (T)__int_as_float(rc.w), J.loss,
-                                        J.scale, L);
+                                        J.scale, L, rin);
 #pragma unroll
         for (int k = 0; k < 9; ++k) R[k] = im.R[k];
     }
@@ -195,17 +224,21 @@ struct ObsOp<T, D, false> {
     }
 };
 
-// Operator of point-major observation o with packed record rc.
+// Operator of point-major observation o with packed record rc. With
+// `gradient` the recomputed form takes its residual and weight from the
+// FP64 parameters (see Res64).
 template <typename T, int D, bool RC>
-__device__ __forceinline__ void make_op_point_major(const JacSrc<T> &J, int o, int4 rc, ObsOp<T, D, RC> &op) {
-    if constexpr (RC) op.build(J, rc.x, rc.y, rc);
+__device__ __forceinline__ void make_op_point_major(const JacSrc<T> &J, int o, int4 rc, ObsOp<T, D, RC> &op,
+                                                    bool gradient = false) {
+    if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)o : -1LL, 1);
     else op.build_record(J.rec, o);
 }
 
 // Operator of image-major observation k with packed record rc.
 template <typename T, int D, bool RC>
-__device__ __forceinline__ void make_op_image_major(const JacSrc<T> &J, long long k, int4 rc, ObsOp<T, D, RC> &op) {
-    if constexpr (RC) op.build(J, rc.x, rc.y, rc);
+__device__ __forceinline__ void make_op_image_major(const JacSrc<T> &J, long long k, int4 rc, ObsOp<T, D, RC> &op,
+                                                    bool gradient = false) {
+    if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)J.img_obs[k] : -1LL, 2);
     else op.build_record(J.rec, J.img_obs[k]);
 }
 

@@ -273,6 +273,9 @@ struct Batch {
     std::vector<long long> obs_off, s_off, simg_off, linv_off;
     long long s_total = 0, simg_total = 0, linv_total = 0;
     std::vector<int> img_win, cam_win, slot_win, win_of_point;
+    std::vector<int> slot_perm;  // position in the window systems -> slot (global)
+    std::vector<int> cblk_win, wblk_start;  // cost blocks (kWinCostChunk observations)
+    std::vector<long long> cblk_lo;
     // concatenated problem arrays
     std::vector<int> cam_of_img, model, obs_image, obs_point;
     std::vector<double> cams, poses, points, obs_xy;
@@ -354,6 +357,25 @@ void build_batch(int W, const sfmba_problem *win, Batch &B) {
             B.slot_win.push_back(w);
         }
         for (int v : lw.slot_pre) L.slot_pre.push_back(v + ib * D);
+        // Factorisation order: each image's pose slots, then its camera's
+        // slots at the camera's first image, then any unreferenced camera.
+        {
+            std::vector<char> placed(lw.n, 0), cam_done(wc, 0);
+            auto place = [&](int first, int count) {
+                for (int k = 0; k < count; ++k)
+                    if (!placed[first + k]) { placed[first + k] = 1; B.slot_perm.push_back(sb + first + k); }
+            };
+            for (int i = 0; i < wi; ++i) {
+                if (lw.pose_slot[i] >= 0) place(lw.pose_slot[i], 6);
+                const int c = coi[i];
+                if (lw.cam_slot[c] >= 0 && !cam_done[c]) {
+                    cam_done[c] = 1;
+                    place(lw.cam_slot[c], model_dof(mod[c]));
+                }
+            }
+            for (int a = 0; a < lw.n; ++a)
+                if (!placed[a]) { placed[a] = 1; B.slot_perm.push_back(sb + a); }
+        }
         B.cams.insert(B.cams.end(), p.camera_params, p.camera_params + (size_t)wc * 8);
         B.poses.insert(B.poses.end(), p.poses, p.poses + (size_t)wi * 7);
         B.points.insert(B.points.end(), p.points, p.points + (size_t)wp * 3);
@@ -366,10 +388,17 @@ void build_batch(int W, const sfmba_problem *win, Batch &B) {
         B.fixed_pose.insert(B.fixed_pose.end(), fp.begin(), fp.end());
         B.fixed_cam.insert(B.fixed_cam.end(), fc.begin(), fc.end());
         B.fixed_cp.insert(B.fixed_cp.end(), fcp.begin(), fcp.end());
+        B.wblk_start.push_back((int)B.cblk_win.size());
+        for (long long lo = ob; lo < ob + wo; lo += kWinCostChunk) {
+            B.cblk_win.push_back(w);
+            B.cblk_lo.push_back(lo);
+        }
         ib += wi; cb += wc; pb += wp; sb += lw.n; ob += wo;
         B.obs_off[w + 1] = ob;
     }
     if (L.slot_pre_start.empty()) L.slot_pre_start.push_back(0);
+    B.wblk_start.push_back((int)B.cblk_win.size());
+    B.cblk_lo.push_back(ob);
     L.n = sb;
     B.s_total = so; B.simg_total = sio; B.linv_total = lo;
     sfmba_problem &q = B.problem;
@@ -553,7 +582,19 @@ class Solver {
                 w_.linv_off = A.take<long long>(W);
                 w_.obs_off = A.take<long long>((size_t)W + 1);
                 w_.counts = A.take<int>(4);
+                w_.slot_perm = A.take<int>(n);
+                const int ncb = (int)batch->cblk_win.size();
+                w_.ncblk = ncb;
+                w_.cblk_win = A.take<int>(ncb);
+                w_.cblk_lo = A.take<long long>((size_t)ncb + 1);
+                w_.wblk_start = A.take<int>((size_t)W + 1);
+                w_.cpart = A.take<double>(ncb);
+                w_.cpart_n = A.take<long long>(ncb);
+                w_.row_first = A.take<int>(n);
+                w_.rhs_p = A.take<double>(n);
                 win_in = A.take<int>(nP);
+                b.img_live = A.take<unsigned char>(nI);
+                b.pt_live = A.take<unsigned char>(nP);
             }
             b.nI = nI; b.nC = nC; b.nP = nP; b.nO = nO; b.n = n; b.D = D; b.nID = nID;
             b.mixed = mixed; b.loss = o->robust_loss; b.loss_scale = o->loss_scale_px;
@@ -594,6 +635,7 @@ class Solver {
                 const bool records = solver_ == SFMBA_SOLVER_DENSE || !mixed || polish;
                 const long long nchunks = (nO + kChunkObs - 1) / kChunkObs;
                 b.img_lin = A.take<char>((size_t)nI * sizeof(ImageLin<double>));
+                b.img_lin64 = mixed ? A.take<char>((size_t)nI * sizeof(ImageLin<double>)) : nullptr;
                 b.rec = records ? A.take<char>((size_t)nO * RS * tsz) : nullptr;
                 b.ob_valid = A.take<unsigned char>(nO);
                 b.pt_C = A.take<char>((size_t)nP * 6 * tsz);
@@ -642,6 +684,7 @@ class Solver {
                     b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * (D * (D + 1) / 2 + D) * tsz);
                     b.obrec = A.take<int4>(nO);
                     b.isrec = A.take<int4>(nO);
+                    b.ob_rs = mixed ? A.take<float4>(nO) : nullptr;
                 }
             }
             if (need_system) {
@@ -752,6 +795,10 @@ class Solver {
             put_vec(w.simg_off, batch->simg_off, s_);
             put_vec(w.linv_off, batch->linv_off, s_);
             put_vec(w.obs_off, batch->obs_off, s_);
+            put_vec(w.slot_perm, batch->slot_perm, s_);
+            put_vec(w.cblk_win, batch->cblk_win, s_);
+            put_vec(w.cblk_lo, batch->cblk_lo, s_);
+            put_vec(w.wblk_start, batch->wblk_start, s_);
             put_vec(win_in, batch->win_of_point, s_);
             launch_wb_window_of_points(win_in, b.pt_perm, nP, w.pt_win, s_);
         }
@@ -909,6 +956,7 @@ class Solver {
             { SFMBA_PHASE(PH_LM); launch_wb_begin_outer(w, o->max_iterations, s_); }
             counts();
             if (hc[WB_NOT_DONE] == 0) continue;
+            { SFMBA_PHASE(PH_LM); launch_wb_live(b, w, false, s_); }
             {
                 SFMBA_PHASE(PH_LINEARIZE);
                 launch_prepare_images(b, s_);
@@ -917,24 +965,25 @@ class Solver {
             { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
             { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
             for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
-                { SFMBA_PHASE(PH_LM); launch_wb_begin_retry(w, s_); }
+                { SFMBA_PHASE(PH_LM); launch_wb_begin_retry(w, s_); launch_wb_live(b, w, true, s_); }
                 { SFMBA_PHASE(PH_POINT_INVERSE); launch_wb_point_inverse(b, w, s_); }
                 { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); launch_fold_rhs(b, s_); }
                 { SFMBA_PHASE(PH_SCHUR); launch_wb_schur(b, w, s_); }
                 { SFMBA_PHASE(PH_FOLD); launch_wb_fold(b, w, s_); }
                 { SFMBA_PHASE(PH_CHOLESKY); launch_wb_cholesky(b, w, s_); }
-                { SFMBA_PHASE(PH_TRSV); launch_wb_solve(b, w, b.rhs, b.delta, s_); }
+                { SFMBA_PHASE(PH_TRSV); launch_wb_solve(b, w, w.rhs_p, b.work2, s_); }
                 if (b.mixed) {
                     SFMBA_PHASE(PH_REFINE);
                     for (int k = 0; k < o->refinement_steps; ++k) launch_wb_refine(b, w, s_);
                 }
+                { SFMBA_PHASE(PH_TRSV); launch_wb_scatter(b, w, s_); }
                 { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
                 { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, true, s_); }
                 { SFMBA_PHASE(PH_LM); launch_wb_accept_commit(b, w, s_); }
                 counts();
                 if (hc[WB_FACTOR_FAILED] > 0) {
                     // LU fallback for the windows whose Cholesky failed (lib.rs:1084-1092)
-                    { SFMBA_PHASE(PH_LU); launch_wb_lu(b, w, s_); }
+                    { SFMBA_PHASE(PH_LU); launch_wb_lu(b, w, s_); launch_wb_scatter(b, w, s_); }
                     { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
                     { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, true, s_); }
                     { SFMBA_PHASE(PH_LM); launch_wb_accept_commit(b, w, s_); launch_wb_reject_failed(w, s_); }
@@ -1084,7 +1133,7 @@ void sfmba_default_options(sfmba_options *o) {
     o->refinement_steps = 1;
     o->target_cost = 0.0;
     o->dense_max_dim = 6000;
-    o->fp64_polish = 1;
+    o->fp64_polish = 0;
 }
 
 int sfmba_bundle_adjust(const sfmba_problem *p, const sfmba_options *o, sfmba_result *r) {

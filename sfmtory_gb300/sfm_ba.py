@@ -159,7 +159,7 @@ class BaParams:
     pcg_tolerance: float = 0.1
     refinement_steps: int = 1
     target_cost: float = 0.0
-    fp64_polish: bool = True
+    fp64_polish: bool = False
 
     def to_options(self) -> abi.SfmbaOptions:
         return abi.default_options(
