@@ -55,6 +55,12 @@ def parse_args():
     ap.add_argument("--skip-fp64", action="store_true", help="skip the FP64 comparison solves")
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--skip-side", action="store_true",
+                    help="skip the dense 500-camera and the 512-window measurements reported beside the headline")
+    ap.add_argument("--only", choices=["dense_radial500", "windows512"],
+                    help="run only that side measurement and print its JSON object")
+    ap.add_argument("--windows-scale", type=float, default=1.0,
+                    help="point-count scale of the 512-window batch (1.0 = points U[500,20000])")
     return ap.parse_args()
 
 
@@ -333,6 +339,98 @@ def cpu_baseline_sample(p, point_stride, chol_dim):
     return v, s, sample
 
 
+# ------------------------------------------------- side workloads (rank 0)
+
+def dense_radial500(args, L, device, stream):
+    """Dense reduced-camera path: 500 SIMPLE_RADIAL cameras, 200k points,
+    ~1.2M observations (reduced dimension 4994): FP32 linearisation and
+    Schur with FP64 blocked Cholesky and one refinement step, against the
+    plain FP64 dense path, both timed to the FP64 final cost x (1 + 1e-6)."""
+    from sfmtory_gb300 import abi, native, scenes
+
+    p = scenes.radial500(seed=args.seed, scale=1.0)
+    dp = DeviceProblem(p, device)
+
+    def opts(prec, target=0.0):
+        return abi.default_options(max_iterations=args.max_iterations, robust_loss=abi.LOSS_NONE, precision=prec,
+                                   solver=abi.SOLVER_DENSE, target_cost=target)
+
+    r64, ms64_full = solve_device(L, dp, opts(abi.PRECISION_FP64), stream)
+    target = r64.final_cost * (1.0 + 1e-6)
+    r64t, ms64 = solve_device(L, dp, opts(abi.PRECISION_FP64, target), stream)
+    solve_device(L, dp, opts(abi.PRECISION_MIXED, target), stream)
+    native.profile_enable(True)
+    r32, ms32 = solve_device(L, dp, opts(abi.PRECISION_MIXED, target), stream)
+    prof = native.profile_report()
+    native.profile_enable(False)
+    n = p.reduced_dim()
+    chol = prof.get("cholesky", {"ms": 0.0, "launches": 0})
+    chol_tflops = (n ** 3 / 3.0) * chol["launches"] / (chol["ms"] * 1e-3) / 1e12 if chol["ms"] else None
+    return {
+        "workload": f"radial500: {p.num_images} SIMPLE_RADIAL cameras, {p.num_points} points, "
+                    f"{p.num_observations} observations, reduced dim {n}, squared loss",
+        "fp32_time_to_tolerance_s": ms32 / 1e3, "fp32_iterations": r32.iterations_run,
+        "fp32_final_cost": r32.final_cost, "reached_tolerance": r32.final_cost <= target,
+        "fp64_time_to_tolerance_s": ms64 / 1e3, "fp64_full_solve_s": ms64_full / 1e3,
+        "fp64_final_cost": r64.final_cost, "fp64_iterations": r64.iterations_run,
+        "speedup_vs_fp64_gpu": ms64 / ms32,
+        "obs_per_s": p.num_observations * r32.iterations_run / (ms32 / 1e3),
+        "cholesky_fp64_tflops": chol_tflops,
+        "phase_ms": {k: round(v["ms"], 3) for k, v in prof.items() if isinstance(v, dict) and v.get("launches")},
+    }
+
+
+def windows512(args, with_cpu):
+    """Batched local BA: 512 independent windows (cameras U[8,64], points
+    U[500,20000], ~5 views per point, mixed PINHOLE / SIMPLE_RADIAL / OPENCV,
+    Huber at 2 px) in one sfmba_bundle_adjust_batched call from host
+    buffers, FP32 path and FP64 path; the CPU sample runs the FP64
+    restatement of sfm-ba window by window on the host cores and checks the
+    FP32 batch's final cost of those windows against it."""
+    from sfmtory_gb300 import abi, native, scenes
+
+    wins = scenes.windows512(seed=args.seed, scale=args.windows_scale)
+    kw = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=2.0, max_iterations=args.max_iterations)
+    native.bundle_adjust_batched_arrays(wins[:16], precision=abi.PRECISION_MIXED, **kw)
+    out = {"workload": f"windows512: {len(wins)} windows, {sum(w.num_images for w in wins)} cameras, "
+                       f"{sum(w.num_points for w in wins)} points, {sum(w.num_observations for w in wins)} "
+                       f"observations, max reduced dim {max(w.reduced_dim() for w in wins)}, Huber 2 px"}
+    res = {}
+    for name, prec in (("fp32", abi.PRECISION_MIXED), ("fp64", abi.PRECISION_FP64)):
+        t0 = time.perf_counter()
+        r = native.bundle_adjust_batched_arrays(wins, precision=prec, **kw)
+        dt = time.perf_counter() - t0
+        res[name] = r
+        out[name] = {"seconds": dt, "windows_per_s": len(wins) / dt,
+                     "lm_iterations_mean": float(np.mean([x.iterations_run for x in r])),
+                     "lm_iterations_max": int(max(x.iterations_run for x in r))}
+    c32 = np.array([x.final_cost for x in res["fp32"]])
+    c64 = np.array([x.final_cost for x in res["fp64"]])
+    rel = np.abs(c32 - c64) / np.maximum(c64, 1e-300)
+    out["fp32_vs_fp64_cost_rel"] = {"max": float(rel.max()), "median": float(np.median(rel)),
+                                    "within_1e-6": int((rel <= 1e-6).sum())}
+    out["speedup_vs_fp64_gpu"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
+    if with_cpu:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        oracle.set_threads(threads)
+        t0 = time.perf_counter()
+        done, errs = 0, []
+        for k, w in enumerate(wins):
+            ref = oracle.bundle_adjust(w, **kw)
+            errs.append(abs(res["fp32"][k].final_cost - ref.final_cost) / max(ref.final_cost, 1e-300))
+            done += 1
+            if time.perf_counter() - t0 > 15.0:
+                break
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": done / dt, "unit": "windows/s", "cores": threads, "kind": "port",
+                               "sample": f"the first {done} windows solved one after another by the C++ FP64 "
+                                         f"restatement of sfm-ba ({dt:.1f} s)"}
+        out["fp32_vs_cpu_oracle_cost_rel_on_sample"] = {"max": float(max(errs)), "median": float(np.median(errs))}
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -471,12 +569,33 @@ def run_ours(args):
         "phase_ms_per_step": {k: round(v["ms"] / args.steps, 3) for k, v in prof.items()
                               if isinstance(v, dict) and v.get("launches")},
     }
+    if not args.skip_side and world == 1:
+        line["dense_radial500"] = dense_radial500(args, L, device, stream)
+        line["windows512"] = windows512(args, not args.skip_cpu)
     print(json.dumps(line), flush=True)
+
+
+def run_side_only(args):
+    import torch
+
+    from sfmtory_gb300 import native
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    device = torch.device("cuda", 0)
+    L = native.load()
+    if args.only == "dense_radial500":
+        out = dense_radial500(args, L, device, torch.cuda.Stream(device=device))
+    else:
+        out = windows512(args, not args.skip_cpu)
+    print(json.dumps(out), flush=True)
 
 
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.only:
+        run_side_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

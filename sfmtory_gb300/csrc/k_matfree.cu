@@ -101,126 +101,130 @@ __global__ void __launch_bounds__(256) k_mf_point_reduce(JacSrc<T> J, const unsi
         });
 }
 
-// Image-major accumulation of sum_o Jc~^T W_o Jc~ (upper triangle) and
-// sum_o Jc~^T v_o into one partial per (chunk, image). Each lane owns a few
-// entries; the round's observations are staged in shared memory.
+// Image-major accumulation of H_i = sum_o Jc~^T W_o Jc~ (upper triangle) and
+// sum_o Jc~^T v_o over image-aligned chunks (at most kChunkObs observations
+// of one image, one warp each), one partial per chunk:
 //   MODE 0: W = I, v = r~                 -> H_i, b_i
 //   MODE 1: W = Jx~ C^-1 Jx~^T, v = Jx~ h -> Schur diagonal block, rhs term
+// Per round of 32 observations lane t stages A_t = Jc~ (2 x D) and
+// P_t = [W A_t | v_t] (2 x (D+1)); the chunk's sum of A_t^T P_t is then a
+// product with inner dimension 2 x 32 per round, register-tiled like the
+// Schur reduction: four 8-lane subgroups take observations t = g (mod 4) and
+// each lane owns a ceil(D/2) x ceil((D+1)/4) tile of [H | b].
+template <typename T>
+constexpr int accum_warps() { return sizeof(T) == 4 ? 4 : 2; }
+
 template <typename T, int D, bool RC, int MODE>
-__global__ void __launch_bounds__(128) k_mf_image_accum(JacSrc<T> J, long long nO,
-                                                        const int *__restrict__ img_start,
-                                                        const int *__restrict__ ipart_off,
-                                                        const T *__restrict__ pt_Cinv, const T *__restrict__ pt_h,
-                                                        const unsigned char *__restrict__ pt_ok,
-                                                        T *__restrict__ part) {
+__global__ void __launch_bounds__(32 * accum_warps<T>())
+    k_mf_image_accum(JacSrc<T> J, const int4 *__restrict__ chunks, int nchunks, const T *__restrict__ pt_Cinv,
+                     const T *__restrict__ pt_h, const unsigned char *__restrict__ pt_ok, T *__restrict__ part) {
     constexpr int NH = D * (D + 1) / 2;
     constexpr int NV = NH + D;
-    constexpr int NE = (NV + 31) / 32;
-    constexpr int WPB = 4;
-    __shared__ T sJ[WPB][32][2 * D + 1];
-    __shared__ T sW[WPB][32][5];
-    __shared__ int sImg[WPB][32];
+    constexpr int E = D + 1;  // columns of P: W A, then v
+    constexpr int RH = (D + 1) / 2, CQ = (E + 3) / 4;
+    constexpr int LA = 2 * D + 1, LP = 2 * E + 1;
+    constexpr int WPB = accum_warps<T>();
+    __shared__ T sA[WPB][32][LA];
+    __shared__ T sP[WPB][32][LP];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long chunk = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const long long cs = chunk * kChunkObs;
-    if (cs >= nO) return;
-    const long long ce = cs + kChunkObs < nO ? cs + kChunkObs : nO;
-    int ea[NE], eb[NE];
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= nchunks) return;
+    const int4 ch = chunks[c];  // {image, first, end}
+    const int sg = lane >> 3, l8 = lane & 7;
+    const int r0 = (l8 >> 2) * RH, c0 = (l8 & 3) * CQ;
+    T acc[RH][CQ];
 #pragma unroll
-    for (int j = 0; j < NE; ++j) {
-        const int e = lane + 32 * j;
-        ea[j] = -1;
-        eb[j] = -1;
-        if (e < NH) {
-            int t = e, a = 0;
-            while (t >= D - a) { t -= D - a; ++a; }
-            ea[j] = a;
-            eb[j] = a + t;
-        } else if (e < NV) {
-            ea[j] = e - NH;
-        }
-    }
-    T acc[NE];
+    for (int a = 0; a < RH; ++a)
 #pragma unroll
-    for (int j = 0; j < NE; ++j) acc[j] = T(0);
-    int cur = __ldg(J.isrec + cs).x;
-    auto flush = [&](int img) {
-        T *dst = part + (size_t)partial_slot(ipart_off, img_start, img, chunk) * NV;
-#pragma unroll
-        for (int j = 0; j < NE; ++j) {
-            const int e = lane + 32 * j;
-            if (e < NV) dst[e] = acc[j];
-            acc[j] = T(0);
-        }
-    };
-    for (long long base = cs; base < ce; base += 32) {
-        const long long k = base + lane;
-        const bool valid = k < ce;
-        T jx[6] = {0, 0, 0, 0, 0, 0}, jc[2 * D];
-#pragma unroll
-        for (int c = 0; c < 2 * D; ++c) jc[c] = T(0);
-        T w00 = 0, w01 = 0, w11 = 0, v0 = 0, v1 = 0;
-        int img = 0x7fffffff;
-        if (valid) {
+        for (int b = 0; b < CQ; ++b) acc[a][b] = T(0);
+    for (int base = ch.y; base < ch.z; base += 32) {
+        const int k = base + lane;
+        bool staged = false;
+        if (k < ch.z) {
             const int4 rc = __ldg(J.isrec + k);
-            img = rc.x;
-            const int pt = rc.y;
             ObsOp<T, D, RC> op;
             make_op_image_major<T, D, RC>(J, k, rc, op, MODE == 0);
+            T jc[2 * D];
             op.jc_rows(jc);
-            op.jx_rows(jx);
-            if constexpr (MODE == 0) {
-                w00 = T(1); w11 = T(1);
-                v0 = op.r(0); v1 = op.r(1);
-            } else if (pt_ok[pt]) {
-                const T *Ci = pt_Cinv + 6 * (size_t)pt;
-                T U[2][3];
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const T a0 = jx[3 * q], a1 = jx[3 * q + 1], a2 = jx[3 * q + 2];
-                    U[q][0] = a0 * Ci[0] + a1 * Ci[1] + a2 * Ci[2];
-                    U[q][1] = a0 * Ci[1] + a1 * Ci[3] + a2 * Ci[4];
-                    U[q][2] = a0 * Ci[2] + a1 * Ci[4] + a2 * Ci[5];
+            for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = jc[f];
+            if constexpr (MODE == 0) {
+#pragma unroll
+                for (int q = 0; q < D; ++q) {
+                    sP[wl][lane][q] = jc[q];
+                    sP[wl][lane][E + q] = jc[D + q];
                 }
-                w00 = U[0][0] * jx[0] + U[0][1] * jx[1] + U[0][2] * jx[2];
-                w01 = U[0][0] * jx[3] + U[0][1] * jx[4] + U[0][2] * jx[5];
-                w11 = U[1][0] * jx[3] + U[1][1] * jx[4] + U[1][2] * jx[5];
-                const T *h = pt_h + 3 * (size_t)pt;
-                v0 = jx[0] * h[0] + jx[1] * h[1] + jx[2] * h[2];
-                v1 = jx[3] * h[0] + jx[4] * h[1] + jx[5] * h[2];
+                sP[wl][lane][D] = op.r(0);
+                sP[wl][lane][E + D] = op.r(1);
+                staged = true;
+            } else {
+                const int pt = rc.y;
+                if (pt_ok[pt]) {
+                    T jx[6];
+                    op.jx_rows(jx);
+                    const T *Ci = pt_Cinv + 6 * (size_t)pt;
+                    T U[2][3];
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const T a0 = jx[3 * q], a1 = jx[3 * q + 1], a2 = jx[3 * q + 2];
+                        U[q][0] = a0 * Ci[0] + a1 * Ci[1] + a2 * Ci[2];
+                        U[q][1] = a0 * Ci[1] + a1 * Ci[3] + a2 * Ci[4];
+                        U[q][2] = a0 * Ci[2] + a1 * Ci[4] + a2 * Ci[5];
+                    }
+                    const T w00 = U[0][0] * jx[0] + U[0][1] * jx[1] + U[0][2] * jx[2];
+                    const T w01 = U[0][0] * jx[3] + U[0][1] * jx[4] + U[0][2] * jx[5];
+                    const T w11 = U[1][0] * jx[3] + U[1][1] * jx[4] + U[1][2] * jx[5];
+                    const T *h = pt_h + 3 * (size_t)pt;
+#pragma unroll
+                    for (int q = 0; q < D; ++q) {
+                        sP[wl][lane][q] = w00 * jc[q] + w01 * jc[D + q];
+                        sP[wl][lane][E + q] = w01 * jc[q] + w11 * jc[D + q];
+                    }
+                    sP[wl][lane][D] = jx[0] * h[0] + jx[1] * h[1] + jx[2] * h[2];
+                    sP[wl][lane][E + D] = jx[3] * h[0] + jx[4] * h[1] + jx[5] * h[2];
+                    staged = true;
+                }
             }
         }
+        if (!staged) {
 #pragma unroll
-        for (int c = 0; c < 2 * D; ++c) sJ[wl][lane][c] = jc[c];
-        sW[wl][lane][0] = w00; sW[wl][lane][1] = w01; sW[wl][lane][2] = w11;
-        sW[wl][lane][3] = v0; sW[wl][lane][4] = v1;
-        sImg[wl][lane] = img;
+            for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = T(0);
+#pragma unroll
+            for (int f = 0; f < 2 * E; ++f) sP[wl][lane][f] = T(0);
+        }
         __syncwarp();
-        const int cnt = (int)(ce - base < 32 ? ce - base : 32);
-        for (int t = 0; t < cnt; ++t) {
-            const int it = sImg[wl][t];
-            if (it != cur) {
-                flush(cur);
-                cur = it;
-            }
-            const T m00 = sW[wl][t][0], m01 = sW[wl][t][1], m11 = sW[wl][t][2];
-            const T q0 = sW[wl][t][3], q1 = sW[wl][t][4];
+        const int rounds = (min(32, ch.z - base) + 3 - sg) / 4;  // observations of this subgroup
+        for (int kk = 0; kk < rounds; ++kk) {
+            const int t = sg + 4 * kk;
 #pragma unroll
-            for (int j = 0; j < NE; ++j) {
-                const int a = ea[j], b = eb[j];
-                if (a < 0) continue;
-                const T xa = sJ[wl][t][a], ya = sJ[wl][t][D + a];
-                if (b >= 0) {
-                    const T xb = sJ[wl][t][b], yb = sJ[wl][t][D + b];
-                    acc[j] += xa * (m00 * xb + m01 * yb) + ya * (m01 * xb + m11 * yb);
-                } else {
-                    acc[j] += xa * q0 + ya * q1;
-                }
+            for (int rho = 0; rho < 2; ++rho) {
+                T av[RH], pv[CQ];
+#pragma unroll
+                for (int a = 0; a < RH; ++a) av[a] = (r0 + a < D) ? sA[wl][t][rho * D + r0 + a] : T(0);
+#pragma unroll
+                for (int b = 0; b < CQ; ++b) pv[b] = (c0 + b < E) ? sP[wl][t][rho * E + c0 + b] : T(0);
+#pragma unroll
+                for (int a = 0; a < RH; ++a)
+#pragma unroll
+                    for (int b = 0; b < CQ; ++b) acc[a][b] += av[a] * pv[b];
             }
         }
         __syncwarp();
     }
-    flush(cur);
+    T *dst = part + (size_t)c * NV;
+#pragma unroll
+    for (int a = 0; a < RH; ++a)
+#pragma unroll
+        for (int b = 0; b < CQ; ++b) {
+            T v = acc[a][b];
+            v += __shfl_xor_sync(0xffffffffu, v, 8);
+            v += __shfl_xor_sync(0xffffffffu, v, 16);
+            const int row = r0 + a, col = c0 + b;
+            if (lane < 8 && row < D) {
+                if (col < D && row <= col) dst[row * D - row * (row - 1) / 2 + (col - row)] = v;
+                else if (col == D) dst[NH + row] = v;
+            }
+        }
 }
 
 // H_i (full symmetric, FP64) and b_i from the image's MODE-0 partials.
@@ -613,15 +617,15 @@ void launch_mf_image_blocks(const Bufs &b, cudaStream_t s) {
     dispatch_TDR(b, [&](auto t, auto dc, auto rc) {
         using T = decltype(t);
         constexpr int D = decltype(dc)::value;
-        if (b.nO > 0) {
-            const long long chunks = (b.nO + kChunkObs - 1) / kChunkObs;
-            k_mf_image_accum<T, D, decltype(rc)::value, 0><<<warps_grid(chunks, 128), 128, 0, s>>>(
-                jac_src<T>(b), b.nO, b.img_start, b.ipart_off, (const T *)b.pt_Cinv,
-                (const T *)b.pt_h, b.pt_ok, (T *)b.ipart2);
+        if (b.n_iachunks > 0) {
+            const int th = 32 * accum_warps<T>();
+            k_mf_image_accum<T, D, decltype(rc)::value, 0><<<warps_grid(b.n_iachunks, th), th, 0, s>>>(
+                jac_src<T>(b), b.iachunk, b.n_iachunks, (const T *)b.pt_Cinv, (const T *)b.pt_h, b.pt_ok,
+                (T *)b.ipart2);
             SFMBA_LAUNCH_CHECK();
         }
-        k_mf_image_finish0<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.ipart_off, b.nI, b.img_H,
-                                                                b.img_b);
+        k_mf_image_finish0<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.nI,
+                                                                b.img_H, b.img_b);
         SFMBA_LAUNCH_CHECK();
     });
 }
@@ -630,14 +634,14 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s) {
     dispatch_TDR(b, [&](auto t, auto dc, auto rc) {
         using T = decltype(t);
         constexpr int D = decltype(dc)::value;
-        if (b.nO > 0) {
-            const long long chunks = (b.nO + kChunkObs - 1) / kChunkObs;
-            k_mf_image_accum<T, D, decltype(rc)::value, 1><<<warps_grid(chunks, 128), 128, 0, s>>>(
-                jac_src<T>(b), b.nO, b.img_start, b.ipart_off, (const T *)b.pt_Cinv,
-                (const T *)b.pt_h, b.pt_ok, (T *)b.ipart2);
+        if (b.n_iachunks > 0) {
+            const int th = 32 * accum_warps<T>();
+            k_mf_image_accum<T, D, decltype(rc)::value, 1><<<warps_grid(b.n_iachunks, th), th, 0, s>>>(
+                jac_src<T>(b), b.iachunk, b.n_iachunks, (const T *)b.pt_Cinv, (const T *)b.pt_h, b.pt_ok,
+                (T *)b.ipart2);
             SFMBA_LAUNCH_CHECK();
         }
-        k_mf_precond_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.ipart_off, b.img_H, b.img_b,
+        k_mf_precond_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.img_H, b.img_b,
                                                        b.img_active, b.state, b.nI, b.img_rhs, (T *)b.pcg_Minv,
                                                        (T *)b.pcg_x, (T *)b.pcg_r, (T *)b.pcg_z, (T *)b.pcg_p,
                                                        b.pcg_part);

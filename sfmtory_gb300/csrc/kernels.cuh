@@ -86,6 +86,9 @@ struct Bufs {
     void *ipart = nullptr;        // [nparts*D] per-(chunk, image) partial sums
     void *ipart2 = nullptr;       // [nparts*(D(D+1)/2+D)] block partials of the image passes
     int nparts = 0;
+    int4 *iachunk = nullptr;      // image-aligned chunks {image, first, end} of the image-block passes
+    int *iachunk_off = nullptr;   // [nI+1] first chunk (= partial slot) of each image
+    int n_iachunks = 0;
     int4 *obrec = nullptr;        // [nO] point-major {image, point, x, y (float bits)}
     int4 *isrec = nullptr;        // [nO] image-major {image, point, x, y (float bits)}
     // Batched windows: per-image / per-point "take part" flags of the current

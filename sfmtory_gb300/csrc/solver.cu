@@ -682,6 +682,8 @@ class Solver {
                     b.ipart_off = A.take<int>((size_t)nI + 1);
                     b.ipart = A.take<char>((size_t)(nI + nchunks + 1) * D * tsz);
                     b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * (D * (D + 1) / 2 + D) * tsz);
+                    b.iachunk = A.take<int4>((size_t)(nI + nchunks + 1));
+                    b.iachunk_off = A.take<int>((size_t)nI + 1);
                     b.obrec = A.take<int4>(nO);
                     b.isrec = A.take<int4>(nO);
                     b.ob_rs = mixed ? A.take<float4>(nO) : nullptr;
@@ -752,6 +754,18 @@ class Solver {
             }
             b.nparts = off[nI];
             put_vec(b.ipart_off, off, s_);
+            // Image-aligned chunks of the image-block passes.
+            std::vector<int4> ia;
+            std::vector<int> ia_off(nI + 1, 0);
+            for (int i = 0; i < nI; ++i) {
+                ia_off[i] = (int)ia.size();
+                for (int lo = img_start[i]; lo < img_start[i + 1]; lo += kChunkObs)
+                    ia.push_back(make_int4(i, lo, std::min(lo + kChunkObs, img_start[i + 1]), 0));
+            }
+            ia_off[nI] = (int)ia.size();
+            b.n_iachunks = (int)ia.size();
+            put_vec(b.iachunk, ia, s_);
+            put_vec(b.iachunk_off, ia_off, s_);
             launch_mf_prepare(b, s_);
         }
         if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
