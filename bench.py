@@ -71,6 +71,27 @@ def dist_env():
     return rank, world, local
 
 
+def job_throughput(units, times, world):
+    """Whole-job rate of a replicas-only run: every rank solved its own
+    problem (``units`` = its observations x LM iterations per step, ``times``
+    = its per-step seconds). The job's step time is the slowest rank's mean
+    and its rate the units of all ranks over that time. Collective-free
+    inside the timed region; this reduction runs after it (any backend).
+    Returns (units_per_s, job_step_s)."""
+    local_t = statistics.mean(times)
+    if world == 1:
+        return units / local_t, local_t
+    import torch
+    import torch.distributed as dist
+
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([local_t], dtype=torch.float64, device=dev)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()) / float(t.item()), float(t.item())
+
+
 def make_problem(args, rank):
     from sfmtory_gb300 import scenes
 
@@ -292,7 +313,13 @@ def algorithmic_bytes(phase, nO, nP, nI, D, t, recompute):
     return None
 
 
-def roofline(profile, p, D, t, peaks, recompute=True):
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# the ncu capture of the same kernel on the same workload, recorded in
+# profiles/k_mf_points_radial2000_fp32.md (full-size radial2000, FP32 path).
+NCU_TRAFFIC = {("pcg_points", "radial2000", 1.0): 142906368 + 9755392}
+
+
+def roofline(profile, p, D, t, peaks, recompute=True, workload=None):
     phases = {k: v for k, v in profile.items() if isinstance(v, dict) and v.get("launches")}
     top = max(phases, key=lambda k: phases[k]["ms"])
     order = sorted(phases, key=lambda k: -phases[k]["ms"])
@@ -306,7 +333,8 @@ def roofline(profile, p, D, t, peaks, recompute=True):
     achieved = by / (ms_per * 1e-3) / 1e9
     return {
         "kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-        "frac": round(achieved / peak, 4) if peak else None, "traffic": None,
+        "frac": round(achieved / peak, 4) if peak else None,
+        "traffic": NCU_TRAFFIC.get((top, workload[0], workload[1])) if workload else None,
         "algorithmic_bytes_per_launch": int(by), "avg_launch_ms": round(ms_per, 4),
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peak else "fallback",
         "byte_model": "recomputed Jacobians: 16 B/observation + per-point/per-image terms" if recompute
@@ -502,7 +530,6 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    native.profile_enable(True)
     clocks = ClockSampler(local)
     clocks.start()
     times, iters, results = [], [], []
@@ -513,18 +540,17 @@ def run_ours(args):
         results.append(r)
     torch.cuda.synchronize()
     clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    obs_per_step = nO * statistics.mean(iters)
+    value, step_s = job_throughput(obs_per_step, times, world)
+    last = results[-1]
+    # Phase breakdown, roofline and launch count from one more solve with
+    # the per-phase CUDA-event profiler on (outside the timed steps).
+    native.profile_enable(True)
+    solve_device(L, dp, opts32, stream)
     prof = native.profile_report()
     native.profile_enable(False)
-    step_s = statistics.mean(times)
-    if world > 1:
-        t = torch.tensor([max(times)], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_max = float(t.item())
-    else:
-        step_max = max(times)
-    obs_per_step = nO * statistics.mean(iters)
-    value = obs_per_step * world / (step_s if world == 1 else step_max)
-    last = results[-1]
 
     # End to end through the host API (pinned buffers).
     pp = pinned_problem(p)
@@ -544,7 +570,7 @@ def run_ours(args):
     if rank != 0:
         return
     D = p.block_width()
-    roof = roofline(prof, p, D, 4, measured_peaks())
+    roof = roofline(prof, p, D, 4, measured_peaks(), workload=(args.workload, args.scale))
     cpu = None
     if not args.skip_cpu and world == 1:
         stride = max(1, p.num_points // 20000)
@@ -564,10 +590,10 @@ def run_ours(args):
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "seconds_per_step": statistics.mean(e2e_times)},
-        "gpu_launches": int(prof.get("kernel_launches", 0) // max(1, args.steps)),
+        "gpu_launches": int(prof.get("kernel_launches", 0)),
         "clocks": clk,
-        "phase_ms_per_step": {k: round(v["ms"] / args.steps, 3) for k, v in prof.items()
-                              if isinstance(v, dict) and v.get("launches")},
+        "phase_ms_profiled_step": {k: round(v["ms"], 3) for k, v in prof.items()
+                                   if isinstance(v, dict) and v.get("launches")},
     }
     if not args.skip_side and world == 1:
         line["dense_radial500"] = dense_radial500(args, L, device, stream)
