@@ -698,72 +698,98 @@ __global__ void __launch_bounds__(256) k_wb_summary(WinState *ws, int W, int *co
 }
 
 // Partial-pivoting LU of the windows whose Cholesky failed (lib.rs:1084-1092),
-// one block per window, then the solve. Column k pivots on the first
-// maximum |a|; a zero column is skipped and leaves a zero on U's diagonal,
-// which fails the solve (lambda then grows). Success clears factor_failed.
-__global__ void __launch_bounds__(1024) k_wb_lu(const double *Sall, double *Lall, const long long *s_off,
-                                                 const int *n_w, const int *slot_base, int *perm_all,
-                                                 const double *rhs, double *x, WinState *ws) {
-    __shared__ double bv[1024];
-    __shared__ int bi[1024];
-    __shared__ double red[32];
-    __shared__ int bad;
-    const int w = blockIdx.x;
-    WinState &st = ws[w];
-    if (!st.active || !st.factor_failed || st.solve_failed) return;
+// on the permuted system, for all of them at once: a compact list of the
+// failing windows, then per column k one pivot launch (one block per
+// window) and one rank-1 update launch spread over the GPU, then a
+// per-window solve. Column k pivots on the first maximum |a|; a zero column
+// is skipped and leaves a zero on U's diagonal, which fails the solve
+// (lambda then grows). Success clears factor_failed.
+__global__ void k_wb_failed_list(const WinState *ws, int W, int *list, int *count) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    if (ws[w].active && ws[w].factor_failed && !ws[w].solve_failed) list[atomicAdd(count, 1)] = w;
+}
+
+__global__ void k_wb_lu_copy(const double *Sall, double *Lall, const long long *s_off, const int *n_w,
+                             const int *list) {
+    const int w = list[blockIdx.y];
+    const long long nn = (long long)n_w[w] * n_w[w];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nn; i += (long long)gridDim.x * blockDim.x)
+        Lall[s_off[w] + i] = Sall[s_off[w] + i];
+}
+
+__global__ void __launch_bounds__(256) k_wb_lu_pivot(double *Lall, const long long *s_off, const int *n_w,
+                                                     const int *slot_base, int *perm_all, const int *list, int k) {
+    __shared__ double bv[256];
+    __shared__ int bi[256];
+    const int w = list[blockIdx.x];
     const int n = n_w[w];
-    const double *S = Sall + s_off[w];
+    if (k >= n) return;
     double *A = Lall + s_off[w];
     int *perm = perm_all + slot_base[w];
-    const double *b = rhs + slot_base[w];
-    double *xo = x + slot_base[w];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (long long i = tid; i < (long long)n * n; i += blockDim.x) A[i] = S[i];
-    if (tid == 0) bad = 0;
+    const int tid = threadIdx.x;
+    double best = -1.0;
+    int besti = k;
+    for (int r = k + tid; r < n; r += blockDim.x) {
+        const double v = fabs(A[(size_t)r * n + k]);
+        if (v > best) { best = v; besti = r; }
+    }
+    bv[tid] = best;
+    bi[tid] = besti;
     __syncthreads();
-    for (int k = 0; k < n; ++k) {
-        double best = -1.0;
-        int besti = k;
-        for (int r = k + tid; r < n; r += blockDim.x) {
-            const double v = fabs(A[(size_t)r * n + k]);
-            if (v > best) { best = v; besti = r; }
-        }
-        bv[tid] = best;
-        bi[tid] = besti;
-        __syncthreads();
-        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-            if (tid < h) {
-                const double o = bv[tid + h];
-                const int oi = bi[tid + h];
-                if (o > bv[tid] || (o == bv[tid] && oi < bi[tid])) { bv[tid] = o; bi[tid] = oi; }
-            }
-            __syncthreads();
-        }
-        const int piv = bi[0];
-        const double diag = A[(size_t)piv * n + k];
-        __syncthreads();
-        if (diag == 0.0) {
-            if (tid == 0) perm[k] = -1;
-            continue;
-        }
-        if (piv != k)
-            for (int c = tid; c < n; c += blockDim.x) {
-                const double t = A[(size_t)k * n + c];
-                A[(size_t)k * n + c] = A[(size_t)piv * n + c];
-                A[(size_t)piv * n + c] = t;
-            }
-        if (tid == 0) perm[k] = piv;
-        __syncthreads();
-        for (int r = k + 1 + tid; r < n; r += blockDim.x) A[(size_t)r * n + k] /= diag;
-        __syncthreads();
-        const int m = n - k - 1;
-        for (long long idx = tid; idx < (long long)m * m; idx += blockDim.x) {
-            const int r = k + 1 + (int)(idx / m), c = k + 1 + (int)(idx % m);
-            A[(size_t)r * n + c] -= A[(size_t)r * n + k] * A[(size_t)k * n + c];
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (tid < h) {
+            const double o = bv[tid + h];
+            const int oi = bi[tid + h];
+            if (o > bv[tid] || (o == bv[tid] && oi < bi[tid])) { bv[tid] = o; bi[tid] = oi; }
         }
         __syncthreads();
     }
+    const int piv = bi[0];
+    const double diag = A[(size_t)piv * n + k];
+    if (diag == 0.0) {
+        if (tid == 0) perm[k] = -1;
+        return;
+    }
+    if (piv != k)
+        for (int c = tid; c < n; c += blockDim.x) {
+            const double t = A[(size_t)k * n + c];
+            A[(size_t)k * n + c] = A[(size_t)piv * n + c];
+            A[(size_t)piv * n + c] = t;
+        }
+    if (tid == 0) perm[k] = piv;
+    __syncthreads();
+    for (int r = k + 1 + tid; r < n; r += blockDim.x) A[(size_t)r * n + k] /= diag;
+}
+
+// Rows k+1.. of the trailing matrix: grid (column blocks, rows, windows).
+__global__ void k_wb_lu_update(double *Lall, const long long *s_off, const int *n_w, const int *slot_base,
+                               const int *perm_all, const int *list, int k) {
+    const int w = list[blockIdx.z];
+    const int n = n_w[w];
+    const int r = k + 1 + blockIdx.y;
+    const int c = k + 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n || c >= n) return;
+    if (perm_all[slot_base[w] + k] < 0) return;
+    double *A = Lall + s_off[w];
+    A[(size_t)r * n + c] -= A[(size_t)r * n + k] * A[(size_t)k * n + c];
+}
+
+__global__ void __launch_bounds__(1024) k_wb_lu_solve(const double *Lall, const long long *s_off, const int *n_w,
+                                                       const int *slot_base, const int *perm_all, const int *list,
+                                                       const double *rhs, double *x, WinState *ws) {
+    __shared__ double red[32];
+    __shared__ int bad;
+    const int w = list[blockIdx.x];
+    WinState &st = ws[w];
+    const int n = n_w[w];
+    const double *A = Lall + s_off[w];
+    const int *perm = perm_all + slot_base[w];
+    const double *b = rhs + slot_base[w];
+    double *xo = x + slot_base[w];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int a = tid; a < n; a += blockDim.x) xo[a] = b[a];
+    if (tid == 0) bad = 0;
     __syncthreads();
     if (tid == 0)
         for (int k = 0; k < n; ++k)
@@ -996,8 +1022,25 @@ void launch_wb_summary(const WinBufs &w, cudaStream_t s) {
     SFMBA_LAUNCH_CHECK();
 }
 
-void launch_wb_lu(const Bufs &b, const WinBufs &w, cudaStream_t s) {
-    k_wb_lu<<<w.W, 1024, 0, s>>>(b.S, b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm, w.rhs_p, b.work2, w.ws);
+void launch_wb_lu(const Bufs &b, const WinBufs &w, int n_failed, cudaStream_t s) {
+    if (n_failed <= 0 || w.max_n == 0) return;
+    SFMBA_CUDA(cudaMemsetAsync(w.lu_count, 0, sizeof(int), s));
+    k_wb_failed_list<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W, w.lu_list, w.lu_count);
+    SFMBA_LAUNCH_CHECK();
+    const int nf = n_failed;
+    k_wb_lu_copy<<<dim3(64, nf), 256, 0, s>>>(b.S, b.L, w.s_off, w.n_w, w.lu_list);
+    SFMBA_LAUNCH_CHECK();
+    for (int k = 0; k < w.max_n; ++k) {
+        k_wb_lu_pivot<<<nf, 256, 0, s>>>(b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm, w.lu_list, k);
+        SFMBA_LAUNCH_CHECK();
+        const int m = w.max_n - k - 1;
+        if (m <= 0) break;
+        k_wb_lu_update<<<dim3(div_up(m, 128), m, nf), 128, 0, s>>>(b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm,
+                                                                   w.lu_list, k);
+        SFMBA_LAUNCH_CHECK();
+    }
+    k_wb_lu_solve<<<nf, 1024, 0, s>>>(b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm, w.lu_list, w.rhs_p, b.work2,
+                                      w.ws);
     SFMBA_LAUNCH_CHECK();
 }
 

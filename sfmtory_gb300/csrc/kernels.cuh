@@ -136,6 +136,8 @@ struct WinBufs {
     int *slot_perm = nullptr;      // [n] position in the window systems -> slot
     int *row_first = nullptr;      // [n] first nonzero column of each permuted row
     double *rhs_p = nullptr;       // [n] right-hand side in permuted order
+    int *lu_list = nullptr;        // [W] windows in the LU fallback
+    int *lu_count = nullptr;       // [1]
     // cost blocks: up to kWinCostChunk observations of one window each
     int ncblk = 0;
     int *cblk_win = nullptr;       // [ncblk] window of the block
@@ -256,7 +258,8 @@ void launch_wb_solve(const Bufs &b, const WinBufs &w, const double *rhs, double 
 void launch_wb_refine(const Bufs &b, const WinBufs &w, cudaStream_t s);
 // delta (slot order) from the permuted solution of the retrying windows
 void launch_wb_scatter(const Bufs &b, const WinBufs &w, cudaStream_t s);
-void launch_wb_lu(const Bufs &b, const WinBufs &w, cudaStream_t s);
+// LU fallback for the n_failed windows whose Cholesky failed in this retry.
+void launch_wb_lu(const Bufs &b, const WinBufs &w, int n_failed, cudaStream_t s);
 void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s);
 void launch_wb_accept_commit(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_reject_failed(const WinBufs &w, cudaStream_t s);

@@ -592,6 +592,8 @@ class Solver {
                 w_.cpart_n = A.take<long long>(ncb);
                 w_.row_first = A.take<int>(n);
                 w_.rhs_p = A.take<double>(n);
+                w_.lu_list = A.take<int>(W);
+                w_.lu_count = A.take<int>(1);
                 win_in = A.take<int>(nP);
                 b.img_live = A.take<unsigned char>(nI);
                 b.pt_live = A.take<unsigned char>(nP);
@@ -997,7 +999,11 @@ class Solver {
                 counts();
                 if (hc[WB_FACTOR_FAILED] > 0) {
                     // LU fallback for the windows whose Cholesky failed (lib.rs:1084-1092)
-                    { SFMBA_PHASE(PH_LU); launch_wb_lu(b, w, s_); launch_wb_scatter(b, w, s_); }
+                    {
+                        SFMBA_PHASE(PH_LU);
+                        launch_wb_lu(b, w, hc[WB_FACTOR_FAILED], s_);
+                        launch_wb_scatter(b, w, s_);
+                    }
                     { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
                     { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, true, s_); }
                     { SFMBA_PHASE(PH_LM); launch_wb_accept_commit(b, w, s_); launch_wb_reject_failed(w, s_); }
