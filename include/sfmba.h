@@ -176,6 +176,19 @@ int sfmba_refine_intrinsics(const sfmba_problem *problem, const sfmba_options *o
 int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *windows,
                                 const sfmba_options *options, sfmba_result *results);
 
+/* crates/sfm-reconstruction/src/lib.rs:1722-1768 (`filter_and_reoptimize`,
+ * the final intrinsics-guarded pass of the reconstruction): bundle
+ * adjustment, then up to two rounds of dropping the observations whose point
+ * is behind the camera (z <= 1e-9) or whose reprojection error under the
+ * previous output exceeds threshold_px, each followed by an adjustment from
+ * that output; a round that drops nothing or leaves fewer than 12
+ * observations ends the loop. Everything stays on the GPU between rounds.
+ * `result` holds the last adjustment's output and statistics; keep_out
+ * ([num_observations] or NULL) is 1 for the observations that adjustment
+ * used. Host pointers. */
+int sfmba_filter_and_reoptimize(const sfmba_problem *problem, const sfmba_options *options,
+                                double threshold_px, sfmba_result *result, uint8_t *keep_out);
+
 /* Residual and Jacobian blocks of individual observations, computed on the
  * GPU by the same device code the solver uses (crates/sfm-ba/src/lib.rs:327-590,
  * `analytic_jacobians`). For observation o: r[o][2], j_pose[o][2][6],

@@ -48,6 +48,7 @@ def lib():
             L.oracle_mean_reprojection_error.argtypes = [vp, dp]
             L.oracle_default_fixed_params_mask.argtypes = [i64, vp, vp]
             L.oracle_refine_intrinsics.argtypes = [vp, vp, vp]
+            L.oracle_filter_and_reoptimize.argtypes = [vp, vp, C.c_double, vp, vp]
             for f in (L.oracle_analytic_jacobians, L.oracle_numerical_jacobians):
                 f.argtypes = [vp, C.c_int, vp, vp, C.c_double, C.c_double, vp, vp, vp, vp]
                 f.restype = C.c_int
@@ -136,6 +137,19 @@ def default_fixed_params_mask(models) -> np.ndarray:
     if st != 0:
         raise ValueError("invalid camera model")
     return out.astype(bool)
+
+
+def filter_and_reoptimize(problem, threshold_px: float, options: SfmbaOptions | None = None, **kw):
+    """crates/sfm-reconstruction/src/lib.rs:1722-1768. Returns (result of the
+    last adjustment, keep mask of the input observations it used)."""
+    packed = PackedProblem(problem)
+    buf = ResultBuffers(packed)
+    keep = np.zeros(max(packed.struct.num_observations, 1), dtype=np.uint8)
+    st = lib().oracle_filter_and_reoptimize(C.byref(packed.struct), C.byref(_opts(options, **kw)),
+                                            C.c_double(threshold_px), C.byref(buf.struct), keep.ctypes.data)
+    if st != 0:
+        raise ValueError(f"oracle_filter_and_reoptimize failed with status {st}")
+    return OracleResult(buf), keep[: packed.struct.num_observations].astype(bool)
 
 
 def refine_intrinsics(problem, options: SfmbaOptions | None = None, **kw) -> np.ndarray:

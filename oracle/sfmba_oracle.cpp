@@ -1021,6 +1021,82 @@ int oracle_lm_iteration_sample(const sfmba_problem *p, const sfmba_options *opt,
     return SFMBA_OK;
 }
 
+// crates/sfm-reconstruction/src/lib.rs:1722-1768 (filter_and_reoptimize):
+// bundle adjustment, then up to two rounds (FILTER_ROUNDS) of dropping the
+// observations behind their camera (z <= 1e-9) or farther than threshold_px
+// from their projection under the previous output, and adjusting again from
+// that output; a round that drops nothing, or leaves fewer than 12
+// observations (MIN_OBSERVATIONS), ends the loop without another adjustment.
+// res holds the last adjustment's output; keep[o] = 1 for the input
+// observations that adjustment used (may be NULL).
+int oracle_filter_and_reoptimize(const sfmba_problem *p, const sfmba_options *opt, double threshold_px,
+                                 sfmba_result *res, uint8_t *keep) {
+    Problem P;
+    if (!load(p, P) || !opt || !res) return SFMBA_ERR_INVALID_ARGUMENT;
+    const long nO = P.nO;
+    std::vector<int32_t> img(p->obs_image, p->obs_image + nO), pt(p->obs_point, p->obs_point + nO);
+    std::vector<double> xy(p->obs_xy, p->obs_xy + 2 * nO);
+    std::vector<long> orig(nO);
+    for (long o = 0; o < nO; ++o) orig[o] = o;
+    std::vector<double> out_poses(P.nI * 7), out_points(P.nP * 3), out_cams(P.nC * 8);
+    std::vector<double> in_poses, in_points, in_cams;
+    sfmba_result r = *res;
+    r.poses = out_poses.data();
+    r.points = out_points.data();
+    r.camera_params = out_cams.data();
+    sfmba_problem cur = *p;
+    int st = oracle_bundle_adjust(&cur, opt, &r);
+    if (st != SFMBA_OK) return st;
+    std::vector<long> used = orig;
+    for (int round = 0; round < 2; ++round) {
+        std::vector<int32_t> ni, np;
+        std::vector<double> nxy;
+        std::vector<long> norig;
+        for (size_t k = 0; k < img.size(); ++k) {
+            const int c = P.cam_of_img[img[k]];
+            double rr[2];
+            if (!residual(load_pose(&out_poses[(size_t)img[k] * 7]), P.model[c], &out_cams[(size_t)c * 8],
+                          &out_points[(size_t)pt[k] * 3], xy[2 * k], xy[2 * k + 1], rr))
+                continue;
+            if (std::sqrt(rr[0] * rr[0] + rr[1] * rr[1]) <= threshold_px) {
+                ni.push_back(img[k]);
+                np.push_back(pt[k]);
+                nxy.push_back(xy[2 * k]);
+                nxy.push_back(xy[2 * k + 1]);
+                norig.push_back(orig[k]);
+            }
+        }
+        const bool same = ni.size() == img.size();
+        img.swap(ni); pt.swap(np); xy.swap(nxy); orig.swap(norig);
+        if (same || img.size() < 12) break;
+        in_poses = out_poses;
+        in_points = out_points;
+        in_cams = out_cams;
+        cur.poses = in_poses.data();
+        cur.points = in_points.data();
+        cur.camera_params = in_cams.data();
+        cur.num_observations = (int64_t)img.size();
+        cur.obs_image = img.data();
+        cur.obs_point = pt.data();
+        cur.obs_xy = xy.data();
+        st = oracle_bundle_adjust(&cur, opt, &r);
+        if (st != SFMBA_OK) return st;
+        used = orig;
+    }
+    if (res->poses) std::memcpy(res->poses, out_poses.data(), out_poses.size() * sizeof(double));
+    if (res->points) std::memcpy(res->points, out_points.data(), out_points.size() * sizeof(double));
+    if (res->camera_params) std::memcpy(res->camera_params, out_cams.data(), out_cams.size() * sizeof(double));
+    res->initial_cost = r.initial_cost;
+    res->final_cost = r.final_cost;
+    res->iterations_run = r.iterations_run;
+    res->status = r.status;
+    if (keep) {
+        std::memset(keep, 0, (size_t)nO);
+        for (long o : used) keep[o] = 1;
+    }
+    return SFMBA_OK;
+}
+
 // intrinsics.rs:116-238 (refine_intrinsics, refine_one_camera): per-camera
 // dense LM over that camera's own parameters with central-difference
 // Jacobians; cameras with fewer than 8 observations are left untouched.

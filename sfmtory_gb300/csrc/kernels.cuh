@@ -240,6 +240,27 @@ void launch_pcg_partition(Bufs &b, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
 
+// ---- filter_and_reoptimize (k_filter.cu)
+// Device arrays of the observation filter: the current observations in set
+// 0, the kept ones compacted into set 1 (the caller swaps).
+struct FilterBufs {
+    const int *cam_of_img = nullptr, *cam_model = nullptr;
+    int *img[2] = {nullptr, nullptr}, *pt[2] = {nullptr, nullptr}, *orig[2] = {nullptr, nullptr};
+    double *xy[2] = {nullptr, nullptr};
+    unsigned char *flag = nullptr;
+    int *iota = nullptr;          // 0, 1, 2, ... (the selected positions)
+    int *sel = nullptr;
+    int *count = nullptr;
+    void *temp = nullptr;
+    size_t temp_bytes = 0;
+};
+size_t filter_temp_bytes(long long nO);
+void launch_filter_iota(int *v, long long n, cudaStream_t s);
+// flags of the m current observations under (poses, cams, points); kept ones into set 1, count into *f.count
+void launch_filter_select(const FilterBufs &f, long long m, const double *poses, const double *cams,
+                          const double *points, double threshold, cudaStream_t s);
+void launch_filter_keep(const int *orig, long long m, unsigned char *keep, long long nO, cudaStream_t s);
+
 // ---- batched windows (k_batched.cu)
 // Summary counts written by launch_wb_summary.
 enum { WB_NOT_DONE = 0, WB_RETRY_PENDING = 1, WB_FACTOR_FAILED = 2, WB_WANTS_POLISH = 3 };

@@ -152,7 +152,7 @@ class Arena {
 struct Context {
     int device = -1;
     cudaStream_t stream = nullptr;
-    Arena main, pairs;
+    Arena main, pairs, aux;
     LMState *h_state = nullptr;  // pinned mirror
     int *h_counts = nullptr;     // pinned batch summary
     ~Context() {
@@ -1263,6 +1263,123 @@ int sfmba_residuals_jacobians(const sfmba_problem *p, int32_t precision, double 
         get(valid, q.valid, nO);
         SFMBA_CUDA(cudaStreamSynchronize(s));
     });
+}
+
+int sfmba_filter_and_reoptimize(const sfmba_problem *p, const sfmba_options *o, double threshold_px,
+                                sfmba_result *r, uint8_t *keep_out) {
+    const int st = guarded([&] {
+        const double t0 = now_s();
+        if (!r) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "result is NULL");
+        check_options(o);
+        check_problem_shape(p);
+        check_problem_host(p);
+        if (std::isnan(threshold_px)) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "threshold_px is NaN");
+        Context &ctx = context();
+        cudaStream_t s = ctx.stream;
+        const int nI = (int)p->num_images, nC = (int)p->num_cameras, nP = (int)p->num_points;
+        const long long nO = p->num_observations;
+        Arena &A = ctx.aux;
+        double *poses[2], *cams[2], *points[2];
+        int *cam_of_img = nullptr, *cam_model = nullptr;
+        uint8_t *fpose = nullptr, *fcam = nullptr, *fcp = nullptr;
+        unsigned char *keep = nullptr;
+        FilterBufs f;
+        const size_t tb = filter_temp_bytes(nO);
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            for (int k = 0; k < 2; ++k) {
+                poses[k] = A.take<double>((size_t)nI * 7);
+                cams[k] = A.take<double>((size_t)nC * 8);
+                points[k] = A.take<double>((size_t)nP * 3);
+                f.img[k] = A.take<int>(nO);
+                f.pt[k] = A.take<int>(nO);
+                f.xy[k] = A.take<double>((size_t)nO * 2);
+                f.orig[k] = A.take<int>(nO);
+            }
+            cam_of_img = A.take<int>(nI);
+            cam_model = A.take<int>(nC);
+            fpose = p->fixed_poses ? A.take<uint8_t>(nI) : nullptr;
+            fcam = p->fixed_cameras ? A.take<uint8_t>(nC) : nullptr;
+            fcp = p->fixed_camera_params ? A.take<uint8_t>((size_t)nC * 8) : nullptr;
+            keep = A.take<unsigned char>(nO);
+            f.flag = A.take<unsigned char>(nO);
+            f.sel = A.take<int>(nO);
+            f.iota = A.take<int>(nO);
+            f.count = A.take<int>(1);
+            f.temp = A.take<char>(tb);
+        }
+        f.temp_bytes = tb;
+        f.cam_of_img = cam_of_img;
+        f.cam_model = cam_model;
+        put(cam_of_img, p->camera_of_image, nI, false, s);
+        put(cam_model, p->camera_model, nC, false, s);
+        put(poses[0], p->poses, (size_t)nI * 7, false, s);
+        put(cams[0], p->camera_params, (size_t)nC * 8, false, s);
+        put(points[0], p->points, (size_t)nP * 3, false, s);
+        put(f.img[0], p->obs_image, nO, false, s);
+        put(f.pt[0], p->obs_point, nO, false, s);
+        put(f.xy[0], p->obs_xy, (size_t)nO * 2, false, s);
+        if (fpose) put(fpose, p->fixed_poses, nI, false, s);
+        if (fcam) put(fcam, p->fixed_cameras, nC, false, s);
+        if (fcp) put(fcp, p->fixed_camera_params, (size_t)nC * 8, false, s);
+        launch_filter_iota(f.orig[0], nO, s);
+        launch_filter_iota(f.iota, nO, s);
+        // The adjustments run on these device arrays: input parameters in one
+        // set, output in the other; observations in filter set 0.
+        sfmba_problem dp{};
+        dp.num_images = nI; dp.num_cameras = nC; dp.num_points = nP;
+        dp.camera_of_image = cam_of_img; dp.camera_model = cam_model;
+        dp.fixed_poses = fpose; dp.fixed_cameras = fcam; dp.fixed_camera_params = fcp;
+        sfmba_result dr{};
+        int cur = 0;  // parameter set of the next adjustment's input
+        long long m = nO;
+        auto adjust = [&] {
+            dp.poses = poses[cur]; dp.camera_params = cams[cur]; dp.points = points[cur];
+            dp.num_observations = m; dp.obs_image = f.img[0]; dp.obs_point = f.pt[0]; dp.obs_xy = f.xy[0];
+            dr.poses = poses[cur ^ 1]; dr.camera_params = cams[cur ^ 1]; dr.points = points[cur ^ 1];
+            const int s2 = bundle_adjust_impl(&dp, o, &dr, true, s);
+            if (s2 != SFMBA_OK) throw Error(s2, g_last_error);
+            cur ^= 1;  // the output is the next input
+        };
+        adjust();
+        for (int round = 0; round < 2; ++round) {  // FILTER_ROUNDS (lib.rs:1735)
+            launch_filter_select(f, m, poses[cur], cams[cur], points[cur], threshold_px, s);
+            int kept = 0;
+            SFMBA_CUDA(cudaMemcpyAsync(&kept, f.count, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SFMBA_CUDA(cudaStreamSynchronize(s));
+            if (kept == m || kept < 12) break;  // MIN_OBSERVATIONS (lib.rs:1736)
+            std::swap(f.img[0], f.img[1]);
+            std::swap(f.pt[0], f.pt[1]);
+            std::swap(f.xy[0], f.xy[1]);
+            std::swap(f.orig[0], f.orig[1]);
+            m = kept;
+            adjust();
+        }
+        if (r->poses && nI)
+            SFMBA_CUDA(cudaMemcpyAsync(r->poses, poses[cur], sizeof(double) * 7 * nI, cudaMemcpyDeviceToHost, s));
+        if (r->points && nP)
+            SFMBA_CUDA(cudaMemcpyAsync(r->points, points[cur], sizeof(double) * 3 * nP, cudaMemcpyDeviceToHost, s));
+        if (r->camera_params && nC)
+            SFMBA_CUDA(cudaMemcpyAsync(r->camera_params, cams[cur], sizeof(double) * 8 * nC, cudaMemcpyDeviceToHost,
+                                       s));
+        if (keep_out && nO) {
+            launch_filter_keep(f.orig[0], m, keep, nO, s);
+            SFMBA_CUDA(cudaMemcpyAsync(keep_out, keep, (size_t)nO, cudaMemcpyDeviceToHost, s));
+        }
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+        r->initial_cost = dr.initial_cost;
+        r->final_cost = dr.final_cost;
+        r->iterations_run = dr.iterations_run;
+        r->damping_retries = dr.damping_retries;
+        r->solver_used = dr.solver_used;
+        r->polish_iteration = dr.polish_iteration;
+        r->linear_iterations = dr.linear_iterations;
+        r->reduced_dim = dr.reduced_dim;
+        r->valid_observations = dr.valid_observations;
+        r->seconds = now_s() - t0;
+    });
+    if (r) r->status = st;
+    return st;
 }
 
 int sfmba_refine_intrinsics(const sfmba_problem *p, const sfmba_options *o, double *cams) {

@@ -37,6 +37,7 @@ EXPORTED_SYMBOLS = (
     "sfmba_default_fixed_params_mask",
     "sfmba_refine_intrinsics",
     "sfmba_bundle_adjust_batched",
+    "sfmba_filter_and_reoptimize",
     "sfmba_residuals_jacobians",
     "sfmba_total_cost_noalloc",
     "sfmba_profile_enable",
@@ -75,6 +76,7 @@ def load(path: str | None = None):
         L.sfmba_default_fixed_params_mask.argtypes = [C.c_int64, vp, vp]
         L.sfmba_refine_intrinsics.argtypes = [vp, vp, vp]
         L.sfmba_bundle_adjust_batched.argtypes = [C.c_int32, vp, vp, vp]
+        L.sfmba_filter_and_reoptimize.argtypes = [vp, vp, C.c_double, vp, vp]
         L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
         L.sfmba_total_cost_noalloc.argtypes = [vp, vp, vp, vp]
         L.sfmba_profile_enable.argtypes = [C.c_int32]
@@ -192,6 +194,20 @@ def bundle_adjust_batched_arrays(problems, opts: SfmbaOptions | None = None, **k
         b.struct = res[k]
         out.append(Result(b))
     return out
+
+
+def filter_and_reoptimize_arrays(problem, threshold_px: float, opts: SfmbaOptions | None = None, **kw):
+    """crates/sfm-reconstruction/src/lib.rs:1722-1768 on the GPU: returns the
+    last adjustment's Result and the keep mask of the input observations it
+    used."""
+    L = load()
+    packed = PackedProblem(problem)
+    buf = ResultBuffers(packed)
+    o = opts if opts is not None else default_options(**kw)
+    keep = np.zeros(max(packed.struct.num_observations, 1), dtype=np.uint8)
+    _check(L.sfmba_filter_and_reoptimize(C.byref(packed.struct), C.byref(o), C.c_double(threshold_px),
+                                         C.byref(buf.struct), keep.ctypes.data))
+    return Result(buf), keep[: packed.struct.num_observations].astype(bool)
 
 
 def profile_enable(on: bool = True) -> None:

@@ -242,6 +242,20 @@ def bundle_adjust_batched(inputs: Sequence[BaInput], params: BaParams = BaParams
     return out
 
 
+def filter_and_reoptimize(input: BaInput, params: BaParams, threshold_px: float) -> BaOutput:
+    """crates/sfm-reconstruction/src/lib.rs:1722-1768 - adjust, drop
+    observations behind their camera or beyond ``threshold_px``, adjust
+    again (at most two filter rounds, never below 12 observations); all on
+    the GPU."""
+    r, _ = native.filter_and_reoptimize_arrays(input.to_problem(), threshold_px, params.to_options())
+    cams = [CameraModel(c.model_id, tuple(float(x) for x in r.camera_params[k, : len(c.param_values)]))
+            for k, c in enumerate(input.cameras)]
+    poses = [Pose(tuple(map(float, r.poses[i, :4])), tuple(map(float, r.poses[i, 4:])))
+             for i in range(len(input.poses))]
+    return BaOutput(poses, [r.points[k].copy() for k in range(len(r.points))], cams,
+                    r.initial_cost, r.final_cost, r.iterations_run)
+
+
 def mean_reprojection_error(input: BaInput) -> float:
     """crates/sfm-ba/src/lib.rs:708-725."""
     return native.mean_reprojection_error_arrays(input.to_problem())

@@ -1,0 +1,59 @@
+"""filter_and_reoptimize (crates/sfm-reconstruction/src/lib.rs:1722-1768) on
+the GPU against the oracle's restatement.
+
+Bars: FP64 - the same observations kept, same iteration count of the last
+adjustment, final cost 1e-6 relative, parameters 1e-6 relative (1e-4 when
+the filter drops only the two points behind their cameras: the second
+adjustment then starts at the first one's minimum, where the cost is flat
+along the weak focal/depth directions and summation-order differences move
+the parameters by ~1e-5 while the cost agrees to 1e-6); FP32 path - final
+cost 1e-6 relative when the kept sets agree (observations within rounding
+of the threshold may flip; at most 0.1 % of them)."""
+import numpy as np
+import pytest
+
+from sfmtory_gb300 import abi, native, scenes
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=1.0, max_iterations=30)
+
+
+def _params_close(g, r, tol=1e-6):
+    for a, b in ((g.points, r.points), (g.poses, r.poses), (g.camera_params, r.camera_params)):
+        assert (np.abs(a - b) / np.maximum(np.abs(b), 1.0)).max() <= tol
+
+
+@pytest.mark.parametrize("threshold", [3.0, 1e9])
+def test_filter_fp64_matches_oracle(oracle_lib, threshold):
+    p = scenes.opencv47(seed=3, scale=0.05)  # 5 % outliers
+    g, gk = native.filter_and_reoptimize_arrays(p, threshold, solver=abi.SOLVER_DENSE, **KW)
+    r, rk = oracle_lib.filter_and_reoptimize(p, threshold, **KW)
+    assert np.array_equal(gk, rk)
+    if threshold == 3.0:
+        assert gk.sum() < p.num_observations  # outliers dropped
+    assert g.iterations_run == r.iterations_run
+    assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost
+    _params_close(g, r, 1e-6 if threshold == 3.0 else 1e-4)
+
+
+def test_filter_mixed_reaches_oracle_cost(oracle_lib):
+    p = scenes.opencv47(seed=4, scale=0.05)
+    g, gk = native.filter_and_reoptimize_arrays(p, 3.0, precision=abi.PRECISION_MIXED, solver=abi.SOLVER_DENSE,
+                                                **KW)
+    r, rk = oracle_lib.filter_and_reoptimize(p, 3.0, **KW)
+    assert (gk != rk).sum() <= max(1, p.num_observations // 1000)
+    if np.array_equal(gk, rk):
+        assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost
+
+
+def test_filter_stops_below_twelve_observations(oracle_lib):
+    """A threshold nothing passes leaves < 12 observations: the loop ends
+    after the first adjustment, which used every observation."""
+    p = scenes.recovers_ground_truth_fixture()
+    g, gk = native.filter_and_reoptimize_arrays(p, -1.0, max_iterations=30)
+    r, rk = oracle_lib.filter_and_reoptimize(p, -1.0, max_iterations=30)
+    plain = native.bundle_adjust_arrays(p, max_iterations=30)
+    assert gk.all() and rk.all()
+    assert g.iterations_run == plain.iterations_run
+    assert abs(g.final_cost - plain.final_cost) <= 1e-12 + 1e-9 * plain.final_cost

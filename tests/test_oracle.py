@@ -158,3 +158,21 @@ def test_ring16_converges(oracle_lib):
     n_obs = p.num_observations
     # Noise sigma 0.5 px -> E|r|^2 ~ 2 * 0.25 per observation.
     assert out.final_cost / n_obs < 0.6
+
+
+def test_oracle_filter_and_reoptimize_semantics(oracle_lib):
+    """lib.rs:1722-1768: with a threshold no observation exceeds and every
+    point in front, the filter keeps everything and the result is the plain
+    adjustment; with 5 % outliers and a 3 px threshold it drops some and the
+    last adjustment's observations all fit the previous output."""
+    from sfmtory_gb300 import abi, scenes
+
+    p = scenes.recovers_ground_truth_fixture()
+    plain = oracle_lib.bundle_adjust(p, max_iterations=30)
+    r, keep = oracle_lib.filter_and_reoptimize(p, 1e9, max_iterations=30)
+    assert keep.all() and r.final_cost == plain.final_cost
+    q = scenes.opencv47(seed=3, scale=0.05)
+    kw = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=1.0, max_iterations=30)
+    r, keep = oracle_lib.filter_and_reoptimize(q, 3.0, **kw)
+    assert 0.8 * q.num_observations < keep.sum() < q.num_observations
+    assert r.final_cost < oracle_lib.bundle_adjust(q, **kw).final_cost
