@@ -240,6 +240,17 @@ void launch_pcg_partition(Bufs &b, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
 
+// ---- refine_intrinsics (k_intrinsics.cu)
+struct IntrinsicsBufs {
+    int nC = 0;
+    const double *poses = nullptr, *points = nullptr, *ob_xy = nullptr;
+    const int *ob_img = nullptr, *ob_pt = nullptr, *cam_model = nullptr;
+    const int *cobs_start = nullptr, *cobs = nullptr;  // observations grouped by camera
+    double *cams = nullptr;                             // [nC][8] in / out
+};
+void launch_refine_intrinsics(const IntrinsicsBufs &q, int max_iterations, double lambda0, int loss, double scale,
+                              cudaStream_t s);
+
 // ---- filter_and_reoptimize (k_filter.cu)
 // Device arrays of the observation filter: the current observations in set
 // 0, the kept ones compacted into set 1 (the caller swaps).

@@ -112,6 +112,57 @@ struct PhaseScope {
 #define SFMBA_PHASE_CAT(a, b) SFMBA_PHASE_CAT2(a, b)
 #define SFMBA_PHASE(ph) PhaseScope SFMBA_PHASE_CAT(phase_scope_, __LINE__)(ph, s_)
 
+// A launch sequence that repeats with the same arguments (a PCG chunk, a
+// batched retry round): run directly the first time, captured from the
+// stream the second time, then launched as one CUDA graph. Bypassed while
+// the phase profiler is on (its events bracket individual launches) and on
+// the legacy default stream (which cannot be captured). The kernel-launch
+// counter counts the graph's kernels at every replay.
+class Replay {
+  public:
+    ~Replay() { reset(); }
+    void reset() {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+        uses_ = 0;
+    }
+    template <typename F>
+    void run(cudaStream_t s, bool allowed, F &&f) {
+        if (!allowed || s == cudaStreamLegacy || uses_++ == 0) {
+            f();
+            return;
+        }
+        if (!exec_) {
+            const long long before = g_kernel_launches;
+            SFMBA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            try {
+                f();
+            } catch (...) {
+                cudaGraph_t tmp = nullptr;
+                cudaStreamEndCapture(s, &tmp);
+                if (tmp) cudaGraphDestroy(tmp);
+                (void)cudaGetLastError();
+                throw;
+            }
+            cudaGraph_t g = nullptr;
+            SFMBA_CUDA(cudaStreamEndCapture(s, &g));
+            kernels_ = g_kernel_launches - before;
+            g_kernel_launches = before;
+            const cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) exec_ = nullptr;
+            SFMBA_CUDA(e);
+        }
+        SFMBA_CUDA(cudaGraphLaunch(exec_, s));
+        g_kernel_launches += kernels_;
+    }
+
+  private:
+    cudaGraphExec_t exec_ = nullptr;
+    long long kernels_ = 0;
+    int uses_ = 0;
+};
+
 // Bump allocator over one device allocation that grows on demand and is
 // kept across calls on the same thread.
 class Arena {
@@ -885,11 +936,15 @@ class Solver {
                     const int maxit = std::max(1, o->pcg_max_iterations);
                     for (int it = 0; it < maxit; it += kPcgPollEvery) {
                         const int m = std::min(kPcgPollEvery, maxit - it);
-                        for (int k = 0; k < m; ++k) {
-                            { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_); }
-                            { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_); launch_pcg_images_finish(b, s_); }
-                            { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, (it + k) & 1); }
-                        }
+                        // it is a multiple of kPcgPollEvery (even): iteration it + k has parity k & 1
+                        auto chunk = [&] {
+                            for (int k = 0; k < m; ++k) {
+                                { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_); }
+                                { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_); launch_pcg_images_finish(b, s_); }
+                                { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, k & 1); }
+                            }
+                        };
+                        pcg_chunk_.run(s_, m == kPcgPollEvery && !profiler().on, chunk);
                         read_state();
                         if (hs.pcg_done) break;
                     }
@@ -926,6 +981,7 @@ class Solver {
                 // same loop in FP64. A failed iteration's damping growth is undone.
                 polish_pending = false;
                 b.mixed = 0;
+                pcg_chunk_.reset();
                 out.polish_iteration = outer + 1;
                 if (!accepted) {
                     SFMBA_CUDA(cudaMemcpyAsync(&b.state->lambda, &lambda_start, sizeof(double),
@@ -967,6 +1023,7 @@ class Solver {
                 if (!(polish && b.mixed && hc[WB_WANTS_POLISH] > 0)) break;
                 // Every window has stopped in FP32: the parked ones continue in FP64.
                 b.mixed = 0;
+                retry_round_.reset();
                 launch_wb_start_polish(w, s_);
             }
             { SFMBA_PHASE(PH_LM); launch_wb_begin_outer(w, o->max_iterations, s_); }
@@ -981,22 +1038,29 @@ class Solver {
             { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
             { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
             for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
-                { SFMBA_PHASE(PH_LM); launch_wb_begin_retry(w, s_); launch_wb_live(b, w, true, s_); }
-                { SFMBA_PHASE(PH_POINT_INVERSE); launch_wb_point_inverse(b, w, s_); }
-                { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); launch_fold_rhs(b, s_); }
-                { SFMBA_PHASE(PH_SCHUR); launch_wb_schur(b, w, s_); }
-                { SFMBA_PHASE(PH_FOLD); launch_wb_fold(b, w, s_); }
-                { SFMBA_PHASE(PH_CHOLESKY); launch_wb_cholesky(b, w, s_); }
-                { SFMBA_PHASE(PH_TRSV); launch_wb_solve(b, w, w.rhs_p, b.work2, s_); }
-                if (b.mixed) {
-                    SFMBA_PHASE(PH_REFINE);
-                    for (int k = 0; k < o->refinement_steps; ++k) launch_wb_refine(b, w, s_);
-                }
-                { SFMBA_PHASE(PH_TRSV); launch_wb_scatter(b, w, s_); }
-                { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
-                { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, true, s_); }
-                { SFMBA_PHASE(PH_LM); launch_wb_accept_commit(b, w, s_); }
-                counts();
+                // One retry round of every window, the same launches each round
+                // (the windows taking part are flagged on the device).
+                auto round = [&] {
+                    { SFMBA_PHASE(PH_LM); launch_wb_begin_retry(w, s_); launch_wb_live(b, w, true, s_); }
+                    { SFMBA_PHASE(PH_POINT_INVERSE); launch_wb_point_inverse(b, w, s_); }
+                    { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); launch_fold_rhs(b, s_); }
+                    { SFMBA_PHASE(PH_SCHUR); launch_wb_schur(b, w, s_); }
+                    { SFMBA_PHASE(PH_FOLD); launch_wb_fold(b, w, s_); }
+                    { SFMBA_PHASE(PH_CHOLESKY); launch_wb_cholesky(b, w, s_); }
+                    { SFMBA_PHASE(PH_TRSV); launch_wb_solve(b, w, w.rhs_p, b.work2, s_); }
+                    if (b.mixed) {
+                        SFMBA_PHASE(PH_REFINE);
+                        for (int k = 0; k < o->refinement_steps; ++k) launch_wb_refine(b, w, s_);
+                    }
+                    { SFMBA_PHASE(PH_TRSV); launch_wb_scatter(b, w, s_); }
+                    { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
+                    { SFMBA_PHASE(PH_COST); launch_wb_cost(b, w, true, s_); }
+                    { SFMBA_PHASE(PH_LM); launch_wb_accept_commit(b, w, s_); }
+                    launch_wb_summary(w, s_);
+                    SFMBA_CUDA(cudaMemcpyAsync(hc, w.counts, 4 * sizeof(int), cudaMemcpyDeviceToHost, s_));
+                };
+                retry_round_.run(s_, !profiler().on, round);
+                SFMBA_CUDA(cudaStreamSynchronize(s_));
                 if (hc[WB_FACTOR_FAILED] > 0) {
                     // LU fallback for the windows whose Cholesky failed (lib.rs:1084-1092)
                     {
@@ -1074,6 +1138,7 @@ class Solver {
     Bufs b_;
     WinBufs w_;
     Layout lay_;
+    Replay pcg_chunk_, retry_round_;
     int solver_ = SFMBA_SOLVER_DENSE;
 };
 
@@ -1383,7 +1448,54 @@ int sfmba_filter_and_reoptimize(const sfmba_problem *p, const sfmba_options *o, 
 }
 
 int sfmba_refine_intrinsics(const sfmba_problem *p, const sfmba_options *o, double *cams) {
-    return guarded([&] { throw Error(SFMBA_ERR_UNSUPPORTED, "refine_intrinsics: not built yet"); });
+    return guarded([&] {
+        if (!cams) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "camera_params_inout is NULL");
+        check_options(o);
+        check_problem_shape(p);
+        check_problem_host(p);
+        Context &ctx = context();
+        cudaStream_t s = ctx.stream;
+        const int nI = (int)p->num_images, nC = (int)p->num_cameras, nP = (int)p->num_points;
+        const long long nO = p->num_observations;
+        // Observations grouped by camera (intrinsics.rs:125-128), in input order.
+        std::vector<int> start(nC + 1, 0), list((size_t)nO);
+        for (long long k = 0; k < nO; ++k) start[p->camera_of_image[p->obs_image[k]] + 1] += 1;
+        for (int c = 0; c < nC; ++c) start[c + 1] += start[c];
+        {
+            std::vector<int> fill(start.begin(), start.end() - 1);
+            for (long long k = 0; k < nO; ++k) list[fill[p->camera_of_image[p->obs_image[k]]]++] = (int)k;
+        }
+        Arena &A = ctx.aux;
+        IntrinsicsBufs q;
+        double *poses = nullptr, *points = nullptr, *xy = nullptr, *cam = nullptr;
+        int *img = nullptr, *pt = nullptr, *model = nullptr, *cs = nullptr, *cl = nullptr;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            poses = A.take<double>((size_t)nI * 7);
+            points = A.take<double>((size_t)nP * 3);
+            xy = A.take<double>((size_t)nO * 2);
+            cam = A.take<double>((size_t)nC * 8);
+            img = A.take<int>(nO);
+            pt = A.take<int>(nO);
+            model = A.take<int>(nC);
+            cs = A.take<int>((size_t)nC + 1);
+            cl = A.take<int>(nO);
+        }
+        put(poses, p->poses, (size_t)nI * 7, false, s);
+        put(points, p->points, (size_t)nP * 3, false, s);
+        put(xy, p->obs_xy, (size_t)nO * 2, false, s);
+        put(cam, p->camera_params, (size_t)nC * 8, false, s);
+        put(img, p->obs_image, nO, false, s);
+        put(pt, p->obs_point, nO, false, s);
+        put(model, p->camera_model, nC, false, s);
+        put_vec(cs, start, s);
+        put_vec(cl, list, s);
+        q.nC = nC; q.poses = poses; q.points = points; q.ob_xy = xy; q.ob_img = img; q.ob_pt = pt;
+        q.cam_model = model; q.cobs_start = cs; q.cobs = cl; q.cams = cam;
+        launch_refine_intrinsics(q, o->max_iterations, o->initial_lambda, o->robust_loss, o->loss_scale_px, s);
+        if (nC) SFMBA_CUDA(cudaMemcpyAsync(cams, cam, sizeof(double) * 8 * (size_t)nC, cudaMemcpyDeviceToHost, s));
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+    });
 }
 
 int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *windows,
