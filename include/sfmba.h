@@ -110,7 +110,10 @@ typedef struct sfmba_options {
                                      continue the same LM loop in FP64 (default 0:
                                      the FP32 path already forms its gradient from
                                      FP64 residuals and stops where FP64 does) */
-    int32_t reserved[6];
+    int32_t kernel_variant;       /* 0: launch variants of the PCG observation passes
+                                     picked by the autotuner; 1..4: force one (all
+                                     variants give the same results) */
+    int32_t reserved[5];
 } sfmba_options;
 
 /* crates/sfm-ba/src/lib.rs:240-247 (`BaOutput`). Output buffers are caller

@@ -70,7 +70,8 @@ class SfmbaOptions(C.Structure):
         ("target_cost", C.c_double),
         ("dense_max_dim", C.c_int32),
         ("fp64_polish", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("kernel_variant", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 

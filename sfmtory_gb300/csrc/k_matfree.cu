@@ -29,29 +29,22 @@ __device__ __forceinline__ void seg_scan(T (&v)[N], bool head, int lane) {
 
 // Walks one point-aligned chunk: contrib(o, rc, v) fills the lane's N
 // values from observation o with packed record rc = {image, point, x, y};
-// consume(pt, v) runs on the lane holding a point's complete sum.
-template <typename T, int N, typename Contrib, typename Consume>
+// consume(pt, v) runs on the lane holding a point's complete sum. With
+// ILP = 2 two rounds of 32 observations are taken per step and both rounds'
+// contributions are computed before either round's segmented scan, so their
+// independent loads and arithmetic overlap; the scans (and so the sums) are
+// the same as with ILP = 1.
+template <typename T, int N, int ILP = 2, typename Contrib, typename Consume>
 __device__ __forceinline__ void point_chunk(const int4 *__restrict__ obrec, int cs, int ce, int lane,
                                             Contrib contrib, Consume consume) {
     T carry[N];
 #pragma unroll
     for (int n = 0; n < N; ++n) carry[n] = T(0);
     int carry_pt = -1;
-    for (int base = cs; base < ce; base += 32) {
-        const int o = base + lane;
-        const bool valid = o < ce;
-        int4 rc = make_int4(0, -1, 0, 0);
-        if (valid) rc = __ldg(obrec + o);
-        const int pt = rc.y;
-        T v[N];
+    auto scan_round = [&](T (&v)[N], int o, bool valid, int pt) {
+        if (valid && lane == 0 && pt == carry_pt) {
 #pragma unroll
-        for (int n = 0; n < N; ++n) v[n] = T(0);
-        if (valid) {
-            contrib(o, rc, v);
-            if (lane == 0 && pt == carry_pt) {
-#pragma unroll
-                for (int n = 0; n < N; ++n) v[n] += carry[n];
-            }
+            for (int n = 0; n < N; ++n) v[n] += carry[n];
         }
         const int prev = __shfl_up_sync(0xffffffffu, pt, 1);
         seg_scan<T, N>(v, lane == 0 || pt != prev, lane);
@@ -62,6 +55,28 @@ __device__ __forceinline__ void point_chunk(const int4 *__restrict__ obrec, int 
 #pragma unroll
         for (int n = 0; n < N; ++n) carry[n] = __shfl_sync(0xffffffffu, v[n], 31);
         carry_pt = __shfl_sync(0xffffffffu, (valid && !tail) ? pt : -1, 31);
+    };
+    for (int base = cs; base < ce; base += 32 * ILP) {
+        int o[ILP];
+        bool va[ILP];
+        int4 rc[ILP];
+        T v[ILP][N];
+#pragma unroll
+        for (int r = 0; r < ILP; ++r) {
+            o[r] = base + 32 * r + lane;
+            va[r] = o[r] < ce;
+            rc[r] = make_int4(0, -1, 0, 0);
+            if (va[r]) rc[r] = __ldg(obrec + o[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < ILP; ++r) {
+#pragma unroll
+            for (int n = 0; n < N; ++n) v[r][n] = T(0);
+            if (va[r]) contrib(o[r], rc[r], v[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < ILP; ++r)
+            if (base + 32 * r < ce) scan_round(v[r], o[r], va[r], rc[r].y);
     }
 }
 
@@ -390,17 +405,28 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
     }
 }
 
+// Launch variants of the two PCG passes, picked per device and problem
+// shape by the autotuner in solver.cu: rounds of 32 observations computed
+// per step (ILP) and the minimum resident blocks per SM the register
+// allocation must allow. Every variant computes the same sums in the same
+// order.
+template <int V>
+struct PassVariant {
+    static constexpr int kILP = (V & 1) ? 2 : 1;
+    static constexpr int kMinBlocks = (V & 2) ? 4 : 3;
+};
+
 // PCG point pass: u_p = C_p^-1 sum_o Jx~^T (Jc~_o p_img(o)).
-template <typename T, int D, bool RC>
-__global__ void __launch_bounds__(256) k_mf_points(JacSrc<T> J, const int *__restrict__ pchunk, int nchunks,
-                                                   const T *__restrict__ pt_Cinv,
-                                                   const unsigned char *__restrict__ pt_ok, const T *__restrict__ p,
-                                                   const LMState *__restrict__ st, T *__restrict__ u) {
+template <typename T, int D, bool RC, int V>
+__global__ void __launch_bounds__(256, PassVariant<V>::kMinBlocks)
+    k_mf_points(JacSrc<T> J, const int *__restrict__ pchunk, int nchunks, const T *__restrict__ pt_Cinv,
+                const unsigned char *__restrict__ pt_ok, const T *__restrict__ p, const LMState *__restrict__ st,
+                T *__restrict__ u) {
     if (st->pcg_done) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nchunks) return;
-    point_chunk<T, 3>(
+    point_chunk<T, 3, PassVariant<V>::kILP>(
         J.obrec, pchunk[warp], pchunk[warp + 1], lane,
         [&](int o, int4 rc, T (&v)[3]) {
             ObsOp<T, D, RC> op;
@@ -426,11 +452,11 @@ __global__ void __launch_bounds__(256) k_mf_points(JacSrc<T> J, const int *__res
 }
 
 // PCG image pass: partial sums of Jc~^T (Jx~ u_p) per (chunk, image).
-template <typename T, int D, bool RC>
-__global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, long long nO,
-                                                   const int *__restrict__ img_start,
-                                                   const int *__restrict__ ipart_off, const T *__restrict__ u,
-                                                   const LMState *__restrict__ st, T *__restrict__ ipart) {
+template <typename T, int D, bool RC, int V>
+__global__ void __launch_bounds__(256, PassVariant<V>::kMinBlocks)
+    k_mf_images(JacSrc<T> J, long long nO, const int *__restrict__ img_start, const int *__restrict__ ipart_off,
+                const T *__restrict__ u, const LMState *__restrict__ st, T *__restrict__ ipart) {
+    constexpr int ILP = PassVariant<V>::kILP;
     if (st->pcg_done) return;
     const long long chunk = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -457,31 +483,27 @@ __global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, long long nO,
 #pragma unroll
         for (int c = 0; c < D; ++c) acc[c] = T(0);
     };
-    for (long long base = cs; base < ce; base += 32) {
-        const long long k = base + lane;
-        const bool valid = k < ce;
-        int4 rc = make_int4(0x7fffffff, 0, 0, 0);
-        if (valid) rc = __ldg(J.isrec + k);
-        const int img = rc.x;
-        T cv[D];
+    // Jc~^T (Jx~ u_p) of image-major observation k (zero when invalid).
+    auto contrib = [&](long long k, bool valid, int4 rc, T (&cv)[D]) {
 #pragma unroll
         for (int c = 0; c < D; ++c) cv[c] = T(0);
-        if (valid) {
-            const int pt = rc.y;
-            T u0, u1, u2;
-            if constexpr (std::is_same<T, float>::value) {
-                const float4 t = __ldg(reinterpret_cast<const float4 *>(u) + pt);
-                u0 = t.x; u1 = t.y; u2 = t.z;
-            } else {
-                const T *up = u + 4 * (size_t)pt;
-                u0 = up[0]; u1 = up[1]; u2 = up[2];
-            }
-            ObsOp<T, D, RC> op;
-            make_op_image_major<T, D, RC>(J, k, rc, op);
-            T z0, z1;
-            op.jx(u0, u1, u2, z0, z1);
-            op.jc_t(z0, z1, cv);
+        if (!valid) return;
+        const int pt = rc.y;
+        T u0, u1, u2;
+        if constexpr (std::is_same<T, float>::value) {
+            const float4 t = __ldg(reinterpret_cast<const float4 *>(u) + pt);
+            u0 = t.x; u1 = t.y; u2 = t.z;
+        } else {
+            const T *up = u + 4 * (size_t)pt;
+            u0 = up[0]; u1 = up[1]; u2 = up[2];
         }
+        ObsOp<T, D, RC> op;
+        make_op_image_major<T, D, RC>(J, k, rc, op);
+        T z0, z1;
+        op.jx(u0, u1, u2, z0, z1);
+        op.jc_t(z0, z1, cv);
+    };
+    auto accumulate = [&](bool valid, int img, const T (&cv)[D]) {
         while (true) {
             if (valid && img == cur) {
 #pragma unroll
@@ -492,6 +514,25 @@ __global__ void __launch_bounds__(256) k_mf_images(JacSrc<T> J, long long nO,
             flush(cur);
             cur = __shfl_sync(0xffffffffu, img, __ffs(rest) - 1);
         }
+    };
+    // ILP rounds of 32 observations per step, all computed before any is
+    // accumulated (independent work overlaps; the sums are the same).
+    for (long long base = cs; base < ce; base += 32 * ILP) {
+        long long k[ILP];
+        bool va[ILP];
+        int4 rc[ILP];
+        T cv[ILP][D];
+#pragma unroll
+        for (int r = 0; r < ILP; ++r) {
+            k[r] = base + 32 * r + lane;
+            va[r] = k[r] < ce;
+            rc[r] = make_int4(0x7fffffff, 0, 0, 0);
+            if (va[r]) rc[r] = __ldg(J.isrec + k[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < ILP; ++r) contrib(k[r], va[r], rc[r], cv[r]);
+#pragma unroll
+        for (int r = 0; r < ILP; ++r) accumulate(va[r], rc[r].x, cv[r]);
     }
     flush(cur);
 }
@@ -649,29 +690,50 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s) {
     });
 }
 
-void launch_mf_points(const Bufs &b, cudaStream_t s) {
-    if (b.npchunks == 0) return;
+template <int V>
+void mf_points_v(const Bufs &b, cudaStream_t s) {
     dispatch_TDR(b, [&](auto t, auto dc, auto rc) {
         using T = decltype(t);
         constexpr int D = decltype(dc)::value;
-        k_mf_points<T, D, decltype(rc)::value><<<warps_grid(b.npchunks, 256), 256, 0, s>>>(
+        constexpr int VV = std::is_same<T, float>::value ? V : 0;  // FP64: one variant
+        k_mf_points<T, D, decltype(rc)::value, VV><<<warps_grid(b.npchunks, 256), 256, 0, s>>>(
             jac_src<T>(b), b.pchunk, b.npchunks, (const T *)b.pt_Cinv, b.pt_ok, (const T *)b.pcg_p, b.state,
             (T *)b.pcg_u);
     });
     SFMBA_LAUNCH_CHECK();
 }
 
-void launch_mf_images(const Bufs &b, cudaStream_t s) {
-    if (b.nO == 0) return;
+template <int V>
+void mf_images_v(const Bufs &b, cudaStream_t s) {
     dispatch_TDR(b, [&](auto t, auto dc, auto rc) {
         using T = decltype(t);
         constexpr int D = decltype(dc)::value;
+        constexpr int VV = std::is_same<T, float>::value ? V : 0;
         const long long chunks = (b.nO + kChunkObs - 1) / kChunkObs;
-        k_mf_images<T, D, decltype(rc)::value><<<warps_grid(chunks, 256), 256, 0, s>>>(
-            jac_src<T>(b), b.nO, b.img_start, b.ipart_off, (const T *)b.pcg_u, b.state,
-            (T *)b.ipart);
+        k_mf_images<T, D, decltype(rc)::value, VV><<<warps_grid(chunks, 256), 256, 0, s>>>(
+            jac_src<T>(b), b.nO, b.img_start, b.ipart_off, (const T *)b.pcg_u, b.state, (T *)b.ipart);
     });
     SFMBA_LAUNCH_CHECK();
+}
+
+void launch_mf_points(const Bufs &b, cudaStream_t s, int variant) {
+    if (b.npchunks == 0) return;
+    switch (variant) {
+    case 0: mf_points_v<0>(b, s); break;
+    case 1: mf_points_v<1>(b, s); break;
+    case 2: mf_points_v<2>(b, s); break;
+    default: mf_points_v<3>(b, s); break;
+    }
+}
+
+void launch_mf_images(const Bufs &b, cudaStream_t s, int variant) {
+    if (b.nO == 0) return;
+    switch (variant) {
+    case 0: mf_images_v<0>(b, s); break;
+    case 1: mf_images_v<1>(b, s); break;
+    case 2: mf_images_v<2>(b, s); break;
+    default: mf_images_v<3>(b, s); break;
+    }
 }
 
 void launch_mf_backsub(const Bufs &b, const double *delta_slot, cudaStream_t s) {

@@ -224,8 +224,11 @@ void launch_mf_prepare(const Bufs &b, cudaStream_t s);          // packed observ
 void launch_mf_point_reduce(const Bufs &b, cudaStream_t s);     // C_p, g_p, free count
 void launch_mf_image_blocks(const Bufs &b, cudaStream_t s);     // H_i, b_i
 void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PCG start vectors
-void launch_mf_points(const Bufs &b, cudaStream_t s);           // u = C^-1 E^T p
-void launch_mf_images(const Bufs &b, cudaStream_t s);           // partials of E u
+// The two PCG passes in launch variant 0..kPassVariants-1 (same results;
+// chosen by the autotuner).
+constexpr int kPassVariants = 4;
+void launch_mf_points(const Bufs &b, cudaStream_t s, int variant);  // u = C^-1 E^T p
+void launch_mf_images(const Bufs &b, cudaStream_t s, int variant);  // partials of E u
 void launch_mf_backsub(const Bufs &b, const double *delta_slot, cudaStream_t s);
 
 // ---- matrix-free Schur PCG, vector side (k_pcg.cu)

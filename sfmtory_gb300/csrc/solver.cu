@@ -12,8 +12,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include <cub/cub.cuh>
@@ -199,6 +202,70 @@ class Arena {
     size_t cap_ = 0, off_ = 0;
     bool sizing_ = false;
 };
+
+// Autotuner of the PCG passes' launch variants (ILP depth x minimum blocks
+// per SM, k_matfree.cu): per device, pass, block width and problem size
+// (log2 of the observation count) the variant with the shortest mean of
+// three timed launches on a solve's own buffers, measured once at the first
+// FP32 PCG solve and kept for the process. Every variant computes the same
+// sums in the same order, so the choice never changes results.
+struct TuneEntry {
+    int variant = 0;
+    float us[kPassVariants] = {0};
+};
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, TuneEntry> g_tune;  // (device, pass, D, size bucket)
+
+template <typename Launch>
+int tuned_variant(int device, int pass, const Bufs &b, cudaStream_t s, Launch launch) {
+    int bucket = 0;
+    for (long long n = std::max<long long>(b.nO, 1); n > 1; n >>= 1) ++bucket;
+    const auto key = std::make_tuple(device, pass, b.D, bucket);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second.variant;
+    TuneEntry e;
+    cudaEvent_t a, z;
+    SFMBA_CUDA(cudaEventCreate(&a));
+    SFMBA_CUDA(cudaEventCreate(&z));
+    float best = 0.f;
+    for (int v = 0; v < kPassVariants; ++v) {
+        launch(v);  // warm-up
+        SFMBA_CUDA(cudaEventRecord(a, s));
+        for (int r = 0; r < 3; ++r) launch(v);
+        SFMBA_CUDA(cudaEventRecord(z, s));
+        SFMBA_CUDA(cudaEventSynchronize(z));
+        float ms = 0.f;
+        SFMBA_CUDA(cudaEventElapsedTime(&ms, a, z));
+        e.us[v] = ms * 1e3f / 3.f;
+        if (v == 0 || e.us[v] < best) {
+            best = e.us[v];
+            e.variant = v;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(z);
+    g_tune[key] = e;
+    return e.variant;
+}
+
+std::string tune_report() {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    std::string js = "[";
+    bool first = true;
+    for (const auto &kv : g_tune) {
+        char tmp[256];
+        const TuneEntry &e = kv.second;
+        std::snprintf(tmp, sizeof(tmp),
+                      "%s{\"device\":%d,\"pass\":\"%s\",\"D\":%d,\"log2_obs\":%d,\"variant\":%d,"
+                      "\"us\":[%.2f,%.2f,%.2f,%.2f]}",
+                      first ? "" : ",", std::get<0>(kv.first), std::get<1>(kv.first) == 0 ? "points" : "images",
+                      std::get<2>(kv.first), std::get<3>(kv.first), e.variant, e.us[0], e.us[1], e.us[2], e.us[3]);
+        js += tmp;
+        first = false;
+    }
+    return js + "]";
+}
 
 struct Context {
     int device = -1;
@@ -934,13 +1001,20 @@ class Solver {
                 } else {
                     { SFMBA_PHASE(PH_PCG_PRECOND); launch_mf_precond(b, s_); launch_pcg_start(b, s_); }
                     const int maxit = std::max(1, o->pcg_max_iterations);
+                    int vp = 0, vi = 0;  // launch variants of the two passes
+                    if (o->kernel_variant > 0) {
+                        vp = vi = std::min(o->kernel_variant, kPassVariants) - 1;
+                    } else if (b.mixed) {
+                        vp = tuned_variant(ctx_.device, 0, b, s_, [&](int v) { launch_mf_points(b, s_, v); });
+                        vi = tuned_variant(ctx_.device, 1, b, s_, [&](int v) { launch_mf_images(b, s_, v); });
+                    }
                     for (int it = 0; it < maxit; it += kPcgPollEvery) {
                         const int m = std::min(kPcgPollEvery, maxit - it);
                         // it is a multiple of kPcgPollEvery (even): iteration it + k has parity k & 1
                         auto chunk = [&] {
                             for (int k = 0; k < m; ++k) {
-                                { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_); }
-                                { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_); launch_pcg_images_finish(b, s_); }
+                                { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_, vp); }
+                                { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_, vi); launch_pcg_images_finish(b, s_); }
                                 { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, k & 1); }
                             }
                         };
@@ -1566,7 +1640,8 @@ int sfmba_profile_report(char *buf, int64_t len) {
                           p.launches[k]);
             js += tmp;
         }
-        js += ",\"kernel_launches\":" + std::to_string(g_kernel_launches) + "}";
+        js += ",\"kernel_launches\":" + std::to_string(g_kernel_launches);
+        js += ",\"autotune\":" + tune_report() + "}";
         if (!buf || len <= (int64_t)js.size())
             throw Error(SFMBA_ERR_INVALID_ARGUMENT, "profile buffer too small (need " + std::to_string(js.size() + 1) + ")");
         std::memcpy(buf, js.c_str(), js.size() + 1);

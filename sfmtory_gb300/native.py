@@ -219,7 +219,7 @@ def profile_report() -> dict:
     """{phase: {"ms": device milliseconds, "launches": count}} since profile_enable."""
     import json
 
-    buf = C.create_string_buffer(8192)
+    buf = C.create_string_buffer(1 << 16)
     _check(load().sfmba_profile_report(buf, len(buf)))
     return json.loads(buf.value.decode())
 
