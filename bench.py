@@ -59,6 +59,8 @@ def parse_args():
                     help="skip the dense 500-camera and the 512-window measurements reported beside the headline")
     ap.add_argument("--only", choices=["dense_radial500", "windows512"],
                     help="run only that side measurement and print its JSON object")
+    ap.add_argument("--kernel-variant", type=int, default=0,
+                    help="0: autotuned launch variants of the PCG passes; 1..4: force one (for profiling)")
     ap.add_argument("--windows-scale", type=float, default=1.0,
                     help="point-count scale of the 512-window batch (1.0 = points U[500,20000])")
     return ap.parse_args()
@@ -126,7 +128,7 @@ def solver_options(args, precision, target_cost=0.0):
     return abi.default_options(
         max_iterations=args.max_iterations, robust_loss=abi.LOSS_NONE, precision=precision,
         solver=abi.SOLVER_PCG, pcg_tolerance=args.pcg_tol, pcg_max_iterations=args.pcg_max,
-        target_cost=target_cost)
+        target_cost=target_cost, kernel_variant=args.kernel_variant)
 
 
 # ------------------------------------------------------------------ clocks
@@ -316,7 +318,7 @@ def algorithmic_bytes(phase, nO, nP, nI, D, t, recompute):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # the ncu capture of the same kernel on the same workload, recorded in
 # profiles/k_mf_points_radial2000_fp32.md (full-size radial2000, FP32 path).
-NCU_TRAFFIC = {("pcg_points", "radial2000", 1.0): 142906368 + 9755392}
+NCU_TRAFFIC = {("pcg_points", "radial2000", 1.0): 142908672 + 9396992}
 
 
 def roofline(profile, p, D, t, peaks, recompute=True, workload=None):
