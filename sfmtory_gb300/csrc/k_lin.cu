@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(256) k_cost(const double *poses, const double 
                                               const int *cam_model, const int *ob_img,
                                               const int *ob_pt, const double2 *ob_xy, long long nO,
                                               int loss, double scale, int mode, double *partials,
-                                              long long *count_partials) {
+                                              long long *count_partials, float4 *rs_out) {
     double sum = 0.0;
     long long cnt = 0;
     for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < nO;
@@ -403,8 +403,14 @@ __global__ void __launch_bounds__(256) k_cost(const double *poses, const double 
         const double *X = points + 3 * (size_t)p;
         const double2 xy = ob_xy[o];
         double rx, ry;
-        if (residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2],
-                       xy.x, xy.y, rx, ry)) {
+        const bool ok = residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2],
+                                   xy.x, xy.y, rx, ry);
+        if (rs_out) {  // FP64 residual and sqrt(weight) for the next linearisation's gradient terms
+            double sw = 1.0;
+            if (ok && loss != SFMBA_LOSS_NONE) sw = sqrt(robust_weight<double>(sqrt(rx * rx + ry * ry), loss, scale));
+            rs_out[o] = ok ? make_float4((float)rx, (float)ry, (float)sw, 1.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        if (ok) {
             const double n2 = rx * rx + ry * ry;
             if (mode == 0) {
                 if (loss == SFMBA_LOSS_NONE) sum += n2;
@@ -505,9 +511,11 @@ __global__ void k_begin_retry(LMState *st) {
 
 __global__ void k_commit(const LMState *st, int nI, int nC, int nP, const double *poses_trial,
                          const double *cams_trial, const double *points_trial, double *poses,
-                         double *cams, double *points, float4 *points32) {
+                         double *cams, double *points, float4 *points32, long long nO,
+                         const float4 *rs_trial, float4 *rs) {
     if (!st->accepted) return;
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (rs && t < nO) rs[t] = rs_trial[t];
     if (t < nP) {
         const double x = points_trial[3 * t], y = points_trial[3 * t + 1], z = points_trial[3 * t + 2];
         points[3 * t] = x; points[3 * t + 1] = y; points[3 * t + 2] = z;
@@ -707,21 +715,26 @@ void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t 
 }
 
 static void cost_impl(const Bufs &b, bool trial, int mode, double *out, long long *out_count,
-                      cudaStream_t s) {
+                      cudaStream_t s, float4 *rs_out = nullptr) {
     k_cost<<<kCostBlocks, 256, 0, s>>>(trial ? b.poses_trial : b.poses, trial ? b.cams_trial : b.cams,
                                        trial ? b.points_trial : b.points, b.cam_of_img, b.cam_model,
                                        b.ob_img, b.ob_pt, b.ob_xy, b.nO, b.loss, b.loss_scale, mode,
-                                       b.partials, b.count_partials);
+                                       b.partials, b.count_partials, rs_out);
     SFMBA_LAUNCH_CHECK();
     k_cost_finalize<<<1, 256, 0, s>>>(b.partials, b.count_partials, kCostBlocks, out, out_count);
     SFMBA_LAUNCH_CHECK();
 }
 
 void launch_cost(const Bufs &b, bool trial, bool into_trial, cudaStream_t s) {
+    // FP32 PCG path: the cost's FP64 residuals are kept for the point and
+    // image passes' gradient terms (ob_rs: current parameters; ob_rs_trial:
+    // the trial, made current by the commit when accepted).
+    float4 *rs = nullptr;
+    if (b.mixed && b.ob_rs) rs = into_trial ? b.ob_rs_trial : b.ob_rs;
     if (into_trial)
-        cost_impl(b, trial, 0, &b.state->trial_cost, &b.state->trial_valid_obs, s);
+        cost_impl(b, trial, 0, &b.state->trial_cost, &b.state->trial_valid_obs, s, rs);
     else
-        cost_impl(b, trial, 0, &b.state->cost, &b.state->valid_obs, s);
+        cost_impl(b, trial, 0, &b.state->cost, &b.state->valid_obs, s, rs);
 }
 
 void launch_mean_error(const Bufs &b, cudaStream_t s) {
@@ -750,13 +763,16 @@ void launch_begin_retry(const Bufs &b, cudaStream_t s) {
 }
 
 void launch_commit(const Bufs &b, cudaStream_t s) {
+    const bool rs = b.mixed && b.ob_rs;
     long long m = b.nP;
     if (7LL * b.nI > m) m = 7LL * b.nI;
     if (8LL * b.nC > m) m = 8LL * b.nC;
+    if (rs && b.nO > m) m = b.nO;
     if (m == 0) return;
     k_commit<<<div_up(m, 256), 256, 0, s>>>(b.state, b.nI, b.nC, b.nP, b.poses_trial, b.cams_trial,
                                             b.points_trial, b.poses, b.cams, b.points,
-                                            b.mixed ? b.points32 : nullptr);
+                                            b.mixed ? b.points32 : nullptr, b.nO, rs ? b.ob_rs_trial : nullptr,
+                                            rs ? b.ob_rs : nullptr);
     SFMBA_LAUNCH_CHECK();
 }
 

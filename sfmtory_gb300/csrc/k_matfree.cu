@@ -623,12 +623,7 @@ JacSrc<T> jac_src(const Bufs &b) {
     J.img_obs = b.img_obs;
     J.loss = b.loss;
     J.scale = (T)b.loss_scale;
-    if constexpr (std::is_same<T, float>::value) {
-        J.lin64 = (const ImageLin<double> *)b.img_lin64;
-        J.pts64 = b.points;
-        J.ob_xy = b.ob_xy;
-        J.rs = b.ob_rs;
-    }
+    if constexpr (std::is_same<T, float>::value) J.rs = b.ob_rs;
     return J;
 }
 

@@ -43,7 +43,8 @@ struct Bufs {
     // linearisation (element type float or double by `mixed`)
     void *img_lin = nullptr;      // [nI] ImageLin<T>
     void *img_lin64 = nullptr;    // [nI] ImageLin<double> for FP64 residuals (FP32 path)
-    float4 *ob_rs = nullptr;      // [nO] point-major FP64-derived residual, sqrt(weight), valid (FP32 PCG path)
+    float4 *ob_rs = nullptr;      // [nO] point-major FP64 residual, sqrt(weight), valid at the current parameters (FP32 PCG path)
+    float4 *ob_rs_trial = nullptr;  // [nO] the same at the trial parameters (written by the trial cost)
     void *rec = nullptr;          // [nO * stride] records
     unsigned char *ob_valid = nullptr;  // [nO]
     void *pt_C = nullptr;         // [nP*6] symmetric 3x3 (00 01 02 11 12 22)

@@ -34,13 +34,10 @@ struct JacSrc {
     const int *img_obs = nullptr;            // image-major -> point-major index
     int loss = 0;
     T scale = T(1);
-    // FP64 residuals of gradient terms (FP32 operators only): per-image FP64
-    // constants, FP64 points and pixels, and the point-major store of the
-    // residual and weight the point pass computes for the image pass.
-    const ImageLin<double> *lin64 = nullptr;
-    const double *pts64 = nullptr;
-    const double2 *ob_xy = nullptr;
-    float4 *rs = nullptr;
+    // FP64 residuals of gradient terms (FP32 operators only): the point-major
+    // store of residual, sqrt(weight) and validity that the cost kernel wrote
+    // for the current parameters.
+    const float4 *rs = nullptr;
 };
 
 // Jr~, Jx~ (2x3), Jc~ (2xD) of a stored record, 16-byte vector loads.
@@ -87,10 +84,9 @@ struct ObsOp<T, D, true> {
     bool valid;
 
     // Gradient terms of the FP32 path replace the FP32 residual and weight of
-    // point-major observation o64 (>= 0): mode 1 computes them in FP64 and
-    // stores them, mode 2 loads the stored ones.
-    __device__ __forceinline__ void build(const JacSrc<T> &J, int img, int pt, int4 rc, long long o64 = -1,
-                                          int mode = 0) {
+    // point-major observation o64 (>= 0) by the FP64 ones the cost kernel
+    // stored for the current parameters (J.rs).
+    __device__ __forceinline__ void build(const JacSrc<T> &J, int img, int pt, int4 rc, long long o64 = -1) {
         const ImageLin<T> im = J.img_lin[img];
         T X0, X1, X2;
         if constexpr (std::is_same<T, float>::value) {
@@ -100,22 +96,10 @@ struct ObsOp<T, D, true> {
             X0 = J.points64[3 * (size_t)pt]; X1 = J.points64[3 * (size_t)pt + 1]; X2 = J.points64[3 * (size_t)pt + 2];
         }
         Res64 rin;
-        if (o64 >= 0 && J.lin64) {
+        if (o64 >= 0 && J.rs) {
+            const float4 v = J.rs[o64];
             rin.use = true;
-            if (mode == 2) {
-                const float4 v = J.rs[o64];
-                rin.r0 = v.x; rin.r1 = v.y; rin.s = v.z; rin.ok = v.w != 0.f;
-            } else {
-                const double2 xy = J.ob_xy[o64];
-                const double *P = J.pts64 + 3 * (size_t)pt;
-                rin.ok = residual64_lin(J.lin64[img], P[0], P[1], P[2], xy.x, xy.y, rin.r0, rin.r1);
-                if (rin.ok)
-                    rin.s = J.loss == SFMBA_LOSS_NONE
-                                ? 1.0
-                                : sqrt(robust_weight<double>(sqrt(rin.r0 * rin.r0 + rin.r1 * rin.r1), J.loss,
-                                                             (double)J.scale));
-                if (J.rs) J.rs[o64] = make_float4((float)rin.r0, (float)rin.r1, (float)rin.s, rin.ok ? 1.f : 0.f);
-            }
+            rin.r0 = v.x; rin.r1 = v.y; rin.s = v.z; rin.ok = v.w != 0.f;
         }
         valid = linearize_compact<T, D>(im, X0, X1, X2, (T)__int_as_float(rc.z), (T)__int_as_float(rc.w), J.loss,
                                         J.scale, L, rin);
@@ -230,7 +214,7 @@ struct ObsOp<T, D, false> {
 template <typename T, int D, bool RC>
 __device__ __forceinline__ void make_op_point_major(const JacSrc<T> &J, int o, int4 rc, ObsOp<T, D, RC> &op,
                                                     bool gradient = false) {
-    if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)o : -1LL, 1);
+    if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)o : -1LL);
     else op.build_record(J.rec, o);
 }
 
@@ -238,7 +222,7 @@ __device__ __forceinline__ void make_op_point_major(const JacSrc<T> &J, int o, i
 template <typename T, int D, bool RC>
 __device__ __forceinline__ void make_op_image_major(const JacSrc<T> &J, long long k, int4 rc, ObsOp<T, D, RC> &op,
                                                     bool gradient = false) {
-    if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)J.img_obs[k] : -1LL, 2);
+    if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)J.img_obs[k] : -1LL);
     else op.build_record(J.rec, J.img_obs[k]);
 }
 

@@ -807,6 +807,7 @@ class Solver {
                     b.obrec = A.take<int4>(nO);
                     b.isrec = A.take<int4>(nO);
                     b.ob_rs = mixed ? A.take<float4>(nO) : nullptr;
+                    b.ob_rs_trial = mixed ? A.take<float4>(nO) : nullptr;
                 }
             }
             if (need_system) {
