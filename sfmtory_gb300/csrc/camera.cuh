@@ -152,8 +152,8 @@ __device__ __forceinline__ T robust_weight(T n, int loss, T scale) {
 // Optional FP64 residual of an observation. The FP32 path computes the
 // pixel residual u - obs from ~1e3 px quantities, which leaves ~1e-4 px of
 // rounding: far above what the gradient near the minimum can tolerate. The
-// kernels that form gradient terms pass the FP64 residual here; the robust
-// weight then comes from it too.
+// kernels that form gradient terms pass the FP64 residual (and sqrt of the
+// robust weight) that the FP64 cost kernel stored for these parameters.
 struct Res64 {
     bool use = false;
     bool ok = false;
@@ -352,26 +352,6 @@ __device__ __forceinline__ bool residual64(const double *pose7, int model, const
     const double iz = 1.0 / pc2;
     double u, v;
     project64(model, c, pc0 * iz, pc1 * iz, u, v);
-    rx = u - ox;
-    ry = v - oy;
-    return true;
-}
-
-// FP64 residual for the gradient terms of the FP32 path, from an image's
-// FP64 rotation matrix: 12 FMAs for R X + t, and 1/z from the FP32
-// reciprocal refined by one Newton-Raphson step x' = x (2 - z x), which
-// squares the relative error (2^-23 -> ~2^-46), instead of an FP64 divide.
-__device__ __forceinline__ bool residual64_lin(const ImageLin<double> &im, double X0, double X1, double X2,
-                                               double ox, double oy, double &rx, double &ry) {
-    const double pc0 = im.R[0] * X0 + im.R[1] * X1 + im.R[2] * X2 + im.t[0];
-    const double pc1 = im.R[3] * X0 + im.R[4] * X1 + im.R[5] * X2 + im.t[1];
-    const double pc2 = im.R[6] * X0 + im.R[7] * X1 + im.R[8] * X2 + im.t[2];
-    if (!(pc2 > kMinDepth)) return false;
-    const float izf = __frcp_rn((float)pc2);
-    double iz = (double)izf;
-    iz = isfinite(izf) ? iz * (2.0 - pc2 * iz) : 1.0 / pc2;
-    double u, v;
-    project64(im.model, im.c, pc0 * iz, pc1 * iz, u, v);
     rx = u - ox;
     ry = v - oy;
     return true;

@@ -210,8 +210,10 @@ __global__ void k_wb_scatter_delta(const int *slot_perm, const int *slot_win, in
 
 // Window w's system in permuted slot order: S[a][b] from its image-level
 // blocks, damping with the window's lambda, masks, symmetrisation, and the
-// envelope. Grid: (column blocks, row, window).
-__global__ void __launch_bounds__(128) k_wb_fold(const double *__restrict__ S_img,
+// envelope. One block per fold block {window, first row, end row} (about
+// 8192 entries each, listed on the host), so windows that are not retrying
+// cost one early exit per block.
+__global__ void __launch_bounds__(128) k_wb_fold(const int4 *__restrict__ fold_blk, const double *__restrict__ S_img,
                                                  const long long *__restrict__ simg_off,
                                                  const int *__restrict__ nid_w, const int *__restrict__ n_w,
                                                  const int *__restrict__ slot_base, const long long *__restrict__ s_off,
@@ -222,39 +224,47 @@ __global__ void __launch_bounds__(128) k_wb_fold(const double *__restrict__ S_im
                                                  const double *__restrict__ diagB, const WinState *__restrict__ ws,
                                                  double *__restrict__ S, double *__restrict__ L,
                                                  int *__restrict__ row_first) {
-    const int w = blockIdx.z;
+    const int4 fb = fold_blk[blockIdx.x];
+    const int w = fb.x;
     if (!ws[w].active) return;
     const int n = n_w[w];
-    const int a = blockIdx.y;
-    if (a >= n || (int)(blockIdx.x * blockDim.x) >= n) return;
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int sb = slot_base[w];
-    int first = 0x7fffffff;
-    if (b < n) {
-        const int ga = slot_perm[sb + a], gb = slot_perm[sb + b];
-        const int nid = nid_w[w];
-        const int ub = img_base[w] * D;  // first image-level index of the window
-        const double *Sw = S_img + simg_off[w];
-        double v;
-        if (masked[ga] || masked[gb]) {
-            v = a == b ? 1.0 : 0.0;
-        } else {
-            double vab = 0.0, vba = 0.0;
-            for (int x = pre_start[ga]; x < pre_start[ga + 1]; ++x)
-                for (int y = pre_start[gb]; y < pre_start[gb + 1]; ++y) {
-                    const int ux = pre[x] - ub, uy = pre[y] - ub;
-                    vab += Sw[(size_t)ux * nid + uy];
-                    vba += Sw[(size_t)uy * nid + ux];
+    const int nid = nid_w[w];
+    const int ub = img_base[w] * D;  // first image-level index of the window
+    const double *Sw = S_img + simg_off[w];
+    const double lam = ws[w].lambda;
+    double *Sd = S + s_off[w], *Ld = L + s_off[w];
+    for (int a = fb.y; a < fb.z; ++a) {
+        const int ga = slot_perm[sb + a];
+        const bool ma = masked[ga];
+        const int as = pre_start[ga], ae = pre_start[ga + 1];
+        int first = 0x7fffffff;
+        for (int b0 = 0; b0 < n; b0 += blockDim.x) {
+            const int b = b0 + threadIdx.x;
+            if (b < n) {
+                const int gb = slot_perm[sb + b];
+                double v;
+                if (ma || masked[gb]) {
+                    v = a == b ? 1.0 : 0.0;
+                } else {
+                    double vab = 0.0, vba = 0.0;
+                    for (int x = as; x < ae; ++x)
+                        for (int y = pre_start[gb]; y < pre_start[gb + 1]; ++y) {
+                            const int ux = pre[x] - ub, uy = pre[y] - ub;
+                            vab += Sw[(size_t)ux * nid + uy];
+                            vba += Sw[(size_t)uy * nid + ux];
+                        }
+                    v = 0.5 * (vab + vba);
+                    if (a == b) v += diagB[ga] * lam;
                 }
-            v = 0.5 * (vab + vba);
-            if (a == b) v += diagB[ga] * ws[w].lambda;
+                Sd[(size_t)a * n + b] = v;
+                Ld[(size_t)a * n + b] = v;
+                if (b < a && v != 0.0 && b < first) first = b;
+            }
         }
-        S[s_off[w] + (size_t)a * n + b] = v;
-        L[s_off[w] + (size_t)a * n + b] = v;
-        if (b < a && v != 0.0) first = b;
+        first = __reduce_min_sync(0xffffffffu, first);
+        if ((threadIdx.x & 31) == 0 && first < a) atomicMin(row_first + sb + a, first);
     }
-    first = __reduce_min_sync(0xffffffffu, first);
-    if ((threadIdx.x & 31) == 0 && first < a) atomicMin(row_first + sb + a, first);
 }
 
 // ---- batched blocked Cholesky (one matrix per window, leading dim n_w)
@@ -520,7 +530,7 @@ __global__ void k_wb_axpy(const int *slot_win, int n, const double *c, double *x
 __global__ void __launch_bounds__(256) k_wb_cost_partials(
     const double *poses, const double *cams, const double *points, const int *cam_of_img, const int *cam_model,
     const int *ob_img, const int *ob_pt, const double2 *ob_xy, const int *cblk_win, const long long *cblk_lo,
-    int loss, double scale, int trial, const WinState *ws, double *cpart, long long *cpart_n) {
+    int loss, double scale, int trial, const WinState *ws, double *cpart, long long *cpart_n, float4 *rs_out) {
     __shared__ double ssum[256];
     __shared__ long long scnt[256];
     const int blk = blockIdx.x;
@@ -534,16 +544,21 @@ __global__ void __launch_bounds__(256) k_wb_cost_partials(
         const double *X = points + 3 * (size_t)p;
         const double2 xy = ob_xy[o];
         double rx, ry;
-        if (residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2], xy.x, xy.y,
-                       rx, ry)) {
+        const bool ok = residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2],
+                                   xy.x, xy.y, rx, ry);
+        double w = 1.0;
+        if (ok) {
             const double n2 = rx * rx + ry * ry;
             if (loss == SFMBA_LOSS_NONE) sum += n2;
             else {
                 const double nn = sqrt(n2);
-                sum += robust_weight<double>(nn, loss, scale) * nn * nn;
+                w = robust_weight<double>(nn, loss, scale);
+                sum += w * nn * nn;
             }
             ++cnt;
         }
+        // FP64 residual and sqrt(weight) for the next linearisation (FP32 records)
+        if (rs_out) rs_out[o] = ok ? make_float4((float)rx, (float)ry, (float)sqrt(w), 1.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     ssum[threadIdx.x] = sum;
     scnt[threadIdx.x] = cnt;
@@ -619,8 +634,9 @@ __global__ void k_wb_reject_failed(WinState *ws, int W) {
 __global__ void k_wb_commit(const WinState *ws, const int *pt_win, const int *img_win, const int *cam_win, int nI,
                             int nC, int nP, const double *poses_trial, const double *cams_trial,
                             const double *points_trial, double *poses, double *cams, double *points,
-                            float4 *points32) {
+                            float4 *points32, long long nO, const int *ob_pt, const float4 *rs_trial, float4 *rs) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (rs && t < nO && ws[pt_win[ob_pt[t]]].accepted) rs[t] = rs_trial[t];
     if (t < nP && ws[pt_win[t]].accepted) {
         const double x = points_trial[3 * t], y = points_trial[3 * t + 1], z = points_trial[3 * t + 2];
         points[3 * t] = x; points[3 * t + 1] = y; points[3 * t + 2] = z;
@@ -927,10 +943,10 @@ void launch_wb_fold(const Bufs &b, const WinBufs &w, cudaStream_t s) {
     SFMBA_LAUNCH_CHECK();
     k_wb_gather_rhs<<<div_up(b.n, 256), 256, 0, s>>>(w.slot_perm, w.slot_win, b.n, b.rhs, w.rhs_p, w.ws);
     SFMBA_LAUNCH_CHECK();
-    dim3 grid(div_up(w.max_n, 128), w.max_n, w.W);
-    k_wb_fold<<<grid, 128, 0, s>>>(b.S_img, w.simg_off, w.nid_w, w.n_w, w.slot_base, w.s_off, w.img_base, b.D,
-                                   w.slot_perm, b.slot_pre_start, b.slot_pre, b.slot_masked, b.diagB, w.ws, b.S,
-                                   b.L, w.row_first);
+    if (w.n_fold_blk == 0) return;
+    k_wb_fold<<<w.n_fold_blk, 128, 0, s>>>(w.fold_blk, b.S_img, w.simg_off, w.nid_w, w.n_w, w.slot_base, w.s_off,
+                                           w.img_base, b.D, w.slot_perm, b.slot_pre_start, b.slot_pre,
+                                           b.slot_masked, b.diagB, w.ws, b.S, b.L, w.row_first);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -981,7 +997,8 @@ void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s)
         k_wb_cost_partials<<<w.ncblk, 256, 0, s>>>(
             trial ? b.poses_trial : b.poses, trial ? b.cams_trial : b.cams, trial ? b.points_trial : b.points,
             b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt, b.ob_xy, w.cblk_win, w.cblk_lo, b.loss, b.loss_scale,
-            trial ? 1 : 0, w.ws, w.cpart, w.cpart_n);
+            trial ? 1 : 0, w.ws, w.cpart, w.cpart_n,
+            (b.mixed && b.ob_rs) ? (trial ? b.ob_rs_trial : b.ob_rs) : nullptr);
         SFMBA_LAUNCH_CHECK();
     }
     k_wb_cost_finalize<<<grid1(w.W), 128, 0, s>>>(w.wblk_start, w.cpart, w.cpart_n, w.W, trial ? 1 : 0, w.ws);
@@ -991,13 +1008,16 @@ void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s)
 void launch_wb_accept_commit(const Bufs &b, const WinBufs &w, cudaStream_t s) {
     k_wb_accept<<<grid1(w.W), 128, 0, s>>>(w.ws, w.W);
     SFMBA_LAUNCH_CHECK();
+    const bool rs = b.mixed && b.ob_rs;
     long long m = b.nP;
     if (7LL * b.nI > m) m = 7LL * b.nI;
     if (8LL * b.nC > m) m = 8LL * b.nC;
+    if (rs && b.nO > m) m = b.nO;
     if (m == 0) return;
     k_wb_commit<<<div_up(m, 256), 256, 0, s>>>(w.ws, w.pt_win, w.img_win, w.cam_win, b.nI, b.nC, b.nP, b.poses_trial,
                                                b.cams_trial, b.points_trial, b.poses, b.cams, b.points,
-                                               b.mixed ? b.points32 : nullptr);
+                                               b.mixed ? b.points32 : nullptr, b.nO, b.ob_pt,
+                                               rs ? b.ob_rs_trial : nullptr, rs ? b.ob_rs : nullptr);
     SFMBA_LAUNCH_CHECK();
 }
 

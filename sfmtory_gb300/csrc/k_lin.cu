@@ -36,7 +36,7 @@ __device__ __forceinline__ void quat_to_R(const double *q, double R[9]) {
 template <typename T>
 __global__ void k_prepare_images(const double *poses, const double *cams, const int *cam_of_img,
                                  const int *cam_model, const int *img_active, int nI,
-                                 ImageLin<T> *out, ImageLin<double> *out64) {
+                                 ImageLin<T> *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nI) return;
     const double *q = poses + 7 * (size_t)i;
@@ -53,18 +53,6 @@ __global__ void k_prepare_images(const double *poses, const double *cams, const 
     im.active = img_active[i];
     im.pad[0] = im.pad[1] = 0;
     out[i] = im;
-    if (out64) {
-        ImageLin<double> d;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) d.R[k] = R[k];
-        d.t[0] = q[4]; d.t[1] = q[5]; d.t[2] = q[6];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) d.c[k] = cams[8 * (size_t)c + k];
-        d.model = im.model;
-        d.active = im.active;
-        d.pad[0] = d.pad[1] = 0;
-        out64[i] = d;
-    }
 }
 
 template <typename T>
@@ -83,7 +71,7 @@ __global__ void __launch_bounds__(256) k_linearize(const ImageLin<T> *img_lin, c
                                                    const float4 *points32, const int *ob_img,
                                                    const int *ob_pt, const double2 *ob_xy,
                                                    long long nO, int loss, T scale, T *rec,
-                                                   unsigned char *ob_valid, const ImageLin<double> *lin64,
+                                                   unsigned char *ob_valid, const float4 *rs,
                                                    const unsigned char *img_live) {
     constexpr int RS = RecLayout<D>::kStride;
     long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -95,10 +83,10 @@ __global__ void __launch_bounds__(256) k_linearize(const ImageLin<T> *img_lin, c
     load_point<T>(points, points32, p, X0, X1, X2);
     const double2 xy = ob_xy[o];
     Res64 rin;
-    if (lin64) {  // FP32 records: residual and weight from the FP64 parameters
+    if (rs) {  // FP32 records: FP64 residual and weight stored by the cost kernel
+        const float4 v = rs[o];
         rin.use = true;
-        rin.ok = residual64_lin(lin64[i], points[3 * (size_t)p], points[3 * (size_t)p + 1], points[3 * (size_t)p + 2],
-                                xy.x, xy.y, rin.r0, rin.r1);
+        rin.r0 = v.x; rin.r1 = v.y; rin.s = v.z; rin.ok = v.w != 0.f;
     }
     T buf[RS];
     T rr[2], jx[6], jc[2 * D];
@@ -149,62 +137,6 @@ __global__ void k_point_reduce(const T *rec, const int *pt_start, const int *ob_
     T *g = pt_g + 3 * (size_t)p;
     g[0] = g0; g[1] = g1; g[2] = g2;
     pt_nfree[p] = nfree;
-}
-
-// H_i = sum Jc~^T Jc~ and b_i = sum Jc~^T r~ over the image's observations
-// (lib.rs:872-908: pose, camera and pose-camera cross blocks at image level).
-// One CTA per image; each thread owns one entry; records staged in shared
-// memory in chunks; FP32 sums are compensated (Kahan).
-template <typename T, int D>
-__global__ void __launch_bounds__(128) k_image_reduce(const T *rec, const int *img_start,
-                                                      const int *img_obs, int nI, double *img_H,
-                                                      double *img_b, const unsigned char *img_live) {
-    constexpr int RS = RecLayout<D>::kStride;
-    constexpr int F = 2 * D + 2;  // Jc~ (2D) then r~ (2)
-    constexpr int CH = 32;
-    constexpr int NH = D * (D + 1) / 2;
-    __shared__ T sh[CH][F + 1];
-    const int i = blockIdx.x;
-    if (i >= nI) return;
-    if (img_live && !img_live[i]) return;
-    const int tid = threadIdx.x;
-    int ea = 0, eb = 0;
-    const bool isH = tid < NH;
-    const bool isB = !isH && tid < NH + D;
-    if (isH) {  // tid -> (a, b), a <= b
-        int t = tid, a = 0;
-        while (t >= D - a) { t -= D - a; ++a; }
-        ea = a; eb = a + t;
-    } else if (isB) {
-        ea = tid - NH;
-    }
-    T acc = 0, comp = 0;
-    const int s = img_start[i], e = img_start[i + 1];
-    for (int base = s; base < e; base += CH) {
-        const int cnt = min(CH, e - base);
-        for (int idx = tid; idx < cnt * F; idx += blockDim.x) {
-            const int k = idx / F, f = idx - k * F;
-            const int o = img_obs[base + k];
-            const T *r = rec + (size_t)o * RS;
-            sh[k][f] = f < 2 * D ? r[8 + f] : r[f - 2 * D];
-        }
-        __syncthreads();
-        if (isH) {
-            for (int k = 0; k < cnt; ++k)
-                kahan_add(acc, comp, sh[k][ea] * sh[k][eb] + sh[k][D + ea] * sh[k][D + eb]);
-        } else if (isB) {
-            for (int k = 0; k < cnt; ++k)
-                kahan_add(acc, comp, sh[k][ea] * sh[k][2 * D] + sh[k][D + ea] * sh[k][2 * D + 1]);
-        }
-        __syncthreads();
-    }
-    if (isH) {
-        double *H = img_H + (size_t)i * D * D;
-        H[ea * D + eb] = (double)acc;
-        H[eb * D + ea] = (double)acc;
-    } else if (isB) {
-        img_b[(size_t)i * D + ea] = (double)acc;
-    }
 }
 
 // diag(B) at slot level: sum of the image-level diagonal entries mapped
@@ -579,12 +511,10 @@ void launch_prepare_images(const Bufs &b, cudaStream_t s) {
     if (b.nI == 0) return;
     if (b.mixed)
         k_prepare_images<float><<<div_up(b.nI, 128), 128, 0, s>>>(
-            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin,
-            (ImageLin<double> *)b.img_lin64);
+            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin);
     else
         k_prepare_images<double><<<div_up(b.nI, 128), 128, 0, s>>>(
-            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<double> *)b.img_lin,
-            nullptr);
+            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<double> *)b.img_lin);
     SFMBA_LAUNCH_CHECK();
 }
 
@@ -595,8 +525,7 @@ void launch_linearize(const Bufs &b, cudaStream_t s) {
         if (b.mixed)
             k_linearize<float, D><<<div_up(b.nO, 256), 256, 0, s>>>(
                 (const ImageLin<float> *)b.img_lin, b.points, b.points32, b.ob_img, b.ob_pt, b.ob_xy,
-                b.nO, b.loss, (float)b.loss_scale, (float *)b.rec, b.ob_valid,
-                (const ImageLin<double> *)b.img_lin64, b.img_live);
+                b.nO, b.loss, (float)b.loss_scale, (float *)b.rec, b.ob_valid, b.ob_rs, b.img_live);
         else
             k_linearize<double, D><<<div_up(b.nO, 256), 256, 0, s>>>(
                 (const ImageLin<double> *)b.img_lin, b.points, b.points32, b.ob_img, b.ob_pt, b.ob_xy,
@@ -617,20 +546,6 @@ void launch_point_reduce(const Bufs &b, cudaStream_t s) {
             k_point_reduce<double, D><<<div_up(b.nP, 128), 128, 0, s>>>(
                 (const double *)b.rec, b.pt_start, b.ob_img, b.ob_valid, b.img_free, b.nP,
                 (double *)b.pt_C, (double *)b.pt_g, b.pt_nfree, b.pt_live);
-    });
-    SFMBA_LAUNCH_CHECK();
-}
-
-void launch_image_reduce(const Bufs &b, cudaStream_t s) {
-    if (b.nI == 0) return;
-    dispatch_D(b.D, [&](auto dc) {
-        constexpr int D = decltype(dc)::value;
-        if (b.mixed)
-            k_image_reduce<float, D><<<b.nI, 128, 0, s>>>((const float *)b.rec, b.img_start,
-                                                          b.img_obs, b.nI, b.img_H, b.img_b, b.img_live);
-        else
-            k_image_reduce<double, D><<<b.nI, 128, 0, s>>>((const double *)b.rec, b.img_start,
-                                                           b.img_obs, b.nI, b.img_H, b.img_b, b.img_live);
     });
     SFMBA_LAUNCH_CHECK();
 }

@@ -145,6 +145,7 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (c >= nchunks) return;
     const int4 ch = chunks[c];  // {image, first, end}
+    if (J.img_live && !J.img_live[ch.x]) return;  // batched windows not taking part
     const int sg = lane >> 3, l8 = lane & 7;
     const int r0 = (l8 >> 2) * RH, c0 = (l8 & 3) * CQ;
     T acc[RH][CQ];
@@ -246,12 +247,14 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
 template <typename T, int D>
 __global__ void __launch_bounds__(128) k_mf_image_finish0(const T *__restrict__ part,
                                                           const int *__restrict__ ipart_off, int nI,
+                                                          const unsigned char *__restrict__ img_live,
                                                           double *__restrict__ img_H, double *__restrict__ img_b) {
     constexpr int NH = D * (D + 1) / 2;
     constexpr int NV = NH + D;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= nI) return;
+    if (img_live && !img_live[i]) return;
     for (int e = lane; e < NV; e += 32) {
         double s = 0.0;
         for (int k = ipart_off[i]; k < ipart_off[i + 1]; ++k) s += (double)part[(size_t)k * NV + e];
@@ -582,8 +585,10 @@ __global__ void k_pack_records(const int *img_obs, const int *ob_img, const int 
                                long long nO, int4 *obrec, int4 *isrec) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= nO) return;
-    const double2 a = ob_xy[k];
-    obrec[k] = make_int4(ob_img[k], ob_pt[k], __float_as_int((float)a.x), __float_as_int((float)a.y));
+    if (obrec) {  // point-major records: PCG solver only
+        const double2 a = ob_xy[k];
+        obrec[k] = make_int4(ob_img[k], ob_pt[k], __float_as_int((float)a.x), __float_as_int((float)a.y));
+    }
     const int o = img_obs[k];
     const double2 b = ob_xy[o];
     isrec[k] = make_int4(ob_img[o], ob_pt[o], __float_as_int((float)b.x), __float_as_int((float)b.y));
@@ -624,6 +629,7 @@ JacSrc<T> jac_src(const Bufs &b) {
     J.loss = b.loss;
     J.scale = (T)b.loss_scale;
     if constexpr (std::is_same<T, float>::value) J.rs = b.ob_rs;
+    J.img_live = b.img_live;
     return J;
 }
 
@@ -661,8 +667,32 @@ void launch_mf_image_blocks(const Bufs &b, cudaStream_t s) {
             SFMBA_LAUNCH_CHECK();
         }
         k_mf_image_finish0<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.nI,
-                                                                b.img_H, b.img_b);
+                                                                b.img_live, b.img_H, b.img_b);
         SFMBA_LAUNCH_CHECK();
+    });
+}
+
+// H_i, b_i from the stored records (dense and batched paths): the same
+// register-tiled accumulation over image-aligned chunks, Jacobians read
+// from the records (RC = false) in the records' precision.
+void launch_image_blocks_records(const Bufs &b, cudaStream_t s) {
+    dispatch_D(b.D, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        auto run = [&](auto t) {
+            using T = decltype(t);
+            if (b.n_iachunks > 0) {
+                const int th = 32 * accum_warps<T>();
+                k_mf_image_accum<T, D, false, 0><<<warps_grid(b.n_iachunks, th), th, 0, s>>>(
+                    jac_src<T>(b), b.iachunk, b.n_iachunks, (const T *)b.pt_Cinv, (const T *)b.pt_h, b.pt_ok,
+                    (T *)b.ipart2);
+                SFMBA_LAUNCH_CHECK();
+            }
+            k_mf_image_finish0<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.nI,
+                                                                    b.img_live, b.img_H, b.img_b);
+            SFMBA_LAUNCH_CHECK();
+        };
+        if (b.mixed) run(0.0f);
+        else run(0.0);
     });
 }
 

@@ -42,8 +42,7 @@ struct Bufs {
     unsigned char *slot_masked = nullptr;  // [n]
     // linearisation (element type float or double by `mixed`)
     void *img_lin = nullptr;      // [nI] ImageLin<T>
-    void *img_lin64 = nullptr;    // [nI] ImageLin<double> for FP64 residuals (FP32 path)
-    float4 *ob_rs = nullptr;      // [nO] point-major FP64 residual, sqrt(weight), valid at the current parameters (FP32 PCG path)
+    float4 *ob_rs = nullptr;      // [nO] point-major FP64 residual, sqrt(weight), valid at the current parameters (FP32 path)
     float4 *ob_rs_trial = nullptr;  // [nO] the same at the trial parameters (written by the trial cost)
     void *rec = nullptr;          // [nO * stride] records
     unsigned char *ob_valid = nullptr;  // [nO]
@@ -137,6 +136,8 @@ struct WinBufs {
     int *slot_perm = nullptr;      // [n] position in the window systems -> slot
     int *row_first = nullptr;      // [n] first nonzero column of each permuted row
     double *rhs_p = nullptr;       // [n] right-hand side in permuted order
+    int4 *fold_blk = nullptr;      // [n_fold_blk] {window, first row, end row} of the fold kernel
+    int n_fold_blk = 0;
     int *lu_list = nullptr;        // [W] windows in the LU fallback
     int *lu_count = nullptr;       // [1]
     // cost blocks: up to kWinCostChunk observations of one window each
@@ -191,7 +192,6 @@ void validate_problem_device(const int *cam_of_img, const int *cam_model, const 
 void launch_prepare_images(const Bufs &b, cudaStream_t s);
 void launch_linearize(const Bufs &b, cudaStream_t s);
 void launch_point_reduce(const Bufs &b, cudaStream_t s);
-void launch_image_reduce(const Bufs &b, cudaStream_t s);
 void launch_diag_fold(const Bufs &b, cudaStream_t s);
 void launch_point_inverse(const Bufs &b, cudaStream_t s);
 void launch_image_rhs(const Bufs &b, cudaStream_t s);
@@ -224,6 +224,7 @@ void launch_lu_solve(const Bufs &b, cudaStream_t s);
 void launch_mf_prepare(const Bufs &b, cudaStream_t s);          // packed observation records
 void launch_mf_point_reduce(const Bufs &b, cudaStream_t s);     // C_p, g_p, free count
 void launch_mf_image_blocks(const Bufs &b, cudaStream_t s);     // H_i, b_i
+void launch_image_blocks_records(const Bufs &b, cudaStream_t s);  // H_i, b_i from stored records
 void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PCG start vectors
 // The two PCG passes in launch variant 0..kPassVariants-1 (same results;
 // chosen by the autotuner).

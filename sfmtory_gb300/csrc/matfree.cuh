@@ -38,6 +38,7 @@ struct JacSrc {
     // store of residual, sqrt(weight) and validity that the cost kernel wrote
     // for the current parameters.
     const float4 *rs = nullptr;
+    const unsigned char *img_live = nullptr;  // batched windows: images taking part (NULL: all)
 };
 
 // Jr~, Jx~ (2x3), Jc~ (2xD) of a stored record, 16-byte vector loads.

@@ -393,6 +393,7 @@ struct Batch {
     std::vector<int> img_win, cam_win, slot_win, win_of_point;
     std::vector<int> slot_perm;  // position in the window systems -> slot (global)
     std::vector<int> cblk_win, wblk_start;  // cost blocks (kWinCostChunk observations)
+    std::vector<int4> fold_blk;             // fold blocks: {window, first row, end row}
     std::vector<long long> cblk_lo;
     // concatenated problem arrays
     std::vector<int> cam_of_img, model, obs_image, obs_point;
@@ -506,6 +507,10 @@ void build_batch(int W, const sfmba_problem *win, Batch &B) {
         B.fixed_pose.insert(B.fixed_pose.end(), fp.begin(), fp.end());
         B.fixed_cam.insert(B.fixed_cam.end(), fc.begin(), fc.end());
         B.fixed_cp.insert(B.fixed_cp.end(), fcp.begin(), fcp.end());
+        {
+            const int rows = std::max(1, 8192 / std::max(lw.n, 1));
+            for (int r0 = 0; r0 < lw.n; r0 += rows) B.fold_blk.push_back(make_int4(w, r0, std::min(lw.n, r0 + rows), 0));
+        }
         B.wblk_start.push_back((int)B.cblk_win.size());
         for (long long lo = ob; lo < ob + wo; lo += kWinCostChunk) {
             B.cblk_win.push_back(w);
@@ -711,6 +716,8 @@ class Solver {
                 w_.row_first = A.take<int>(n);
                 w_.rhs_p = A.take<double>(n);
                 w_.lu_list = A.take<int>(W);
+                w_.n_fold_blk = (int)batch->fold_blk.size();
+                w_.fold_blk = A.take<int4>(batch->fold_blk.size());
                 w_.lu_count = A.take<int>(1);
                 win_in = A.take<int>(nP);
                 b.img_live = A.take<unsigned char>(nI);
@@ -755,7 +762,8 @@ class Solver {
                 const bool records = solver_ == SFMBA_SOLVER_DENSE || !mixed || polish;
                 const long long nchunks = (nO + kChunkObs - 1) / kChunkObs;
                 b.img_lin = A.take<char>((size_t)nI * sizeof(ImageLin<double>));
-                b.img_lin64 = mixed ? A.take<char>((size_t)nI * sizeof(ImageLin<double>)) : nullptr;
+                b.ob_rs = mixed ? A.take<float4>(nO) : nullptr;
+                b.ob_rs_trial = mixed ? A.take<float4>(nO) : nullptr;
                 b.rec = records ? A.take<char>((size_t)nO * RS * tsz) : nullptr;
                 b.ob_valid = A.take<unsigned char>(nO);
                 b.pt_C = A.take<char>((size_t)nP * 6 * tsz);
@@ -768,6 +776,12 @@ class Solver {
                 b.img_b = A.take<double>((size_t)nID);
                 b.img_rhs = A.take<double>((size_t)nID);
                 b.img_delta = A.take<char>((size_t)nID * tsz);
+                // Image-aligned chunks, their partials and the image-major packed
+                // records of the image-block passes (H_i, b_i; PCG preconditioner).
+                b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * (D * (D + 1) / 2 + D) * tsz);
+                b.iachunk = A.take<int4>((size_t)(nI + nchunks + 1));
+                b.iachunk_off = A.take<int>((size_t)nI + 1);
+                b.isrec = A.take<int4>(nO);
                 b.rhs = A.take<double>(n);
                 b.delta = A.take<double>(n);
                 b.diagB = A.take<double>(n);
@@ -801,13 +815,7 @@ class Solver {
                     b.pchunk = A.take<int>((size_t)nchunks + 1);
                     b.ipart_off = A.take<int>((size_t)nI + 1);
                     b.ipart = A.take<char>((size_t)(nI + nchunks + 1) * D * tsz);
-                    b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * (D * (D + 1) / 2 + D) * tsz);
-                    b.iachunk = A.take<int4>((size_t)(nI + nchunks + 1));
-                    b.iachunk_off = A.take<int>((size_t)nI + 1);
                     b.obrec = A.take<int4>(nO);
-                    b.isrec = A.take<int4>(nO);
-                    b.ob_rs = mixed ? A.take<float4>(nO) : nullptr;
-                    b.ob_rs_trial = mixed ? A.take<float4>(nO) : nullptr;
                 }
             }
             if (need_system) {
@@ -864,17 +872,19 @@ class Solver {
         }
         sort_observations(src_pt, src_img, src_xy, nO, nP, nI, b, sort_temp, sort_tmp, k1, v1, k2, v2, s_);
         SFMBA_CUDA(cudaMemsetAsync(b.state, 0, sizeof(LMState), s_));
-        if (need_system && solver_ == SFMBA_SOLVER_PCG) {
-            launch_pcg_partition(b, s_);
-            // Partial-sum slots of the image pass: one per (chunk, image) overlap.
+        if (need_system) {
             std::vector<int> img_start = fetch(b.img_start, (size_t)nI + 1, true, s_);
-            std::vector<int> off(nI + 1, 0);
-            for (int i = 0; i < nI; ++i) {
-                const int a = img_start[i], e = img_start[i + 1];
-                off[i + 1] = off[i] + (e > a ? (e - 1) / kChunkObs - a / kChunkObs + 1 : 0);
+            if (solver_ == SFMBA_SOLVER_PCG) {
+                launch_pcg_partition(b, s_);
+                // Partial-sum slots of the image pass: one per (chunk, image) overlap.
+                std::vector<int> off(nI + 1, 0);
+                for (int i = 0; i < nI; ++i) {
+                    const int a = img_start[i], e = img_start[i + 1];
+                    off[i + 1] = off[i] + (e > a ? (e - 1) / kChunkObs - a / kChunkObs + 1 : 0);
+                }
+                b.nparts = off[nI];
+                put_vec(b.ipart_off, off, s_);
             }
-            b.nparts = off[nI];
-            put_vec(b.ipart_off, off, s_);
             // Image-aligned chunks of the image-block passes.
             std::vector<int4> ia;
             std::vector<int> ia_off(nI + 1, 0);
@@ -932,6 +942,7 @@ class Solver {
             put_vec(w.obs_off, batch->obs_off, s_);
             put_vec(w.slot_perm, batch->slot_perm, s_);
             put_vec(w.cblk_win, batch->cblk_win, s_);
+            put_vec(w.fold_blk, batch->fold_blk, s_);
             put_vec(w.cblk_lo, batch->cblk_lo, s_);
             put_vec(w.wblk_start, batch->wblk_start, s_);
             put_vec(win_in, batch->win_of_point, s_);
@@ -974,7 +985,7 @@ class Solver {
             }
             if (solver_ == SFMBA_SOLVER_DENSE) {
                 { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
-                { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
+                { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_blocks_records(b, s_); launch_diag_fold(b, s_); }
             } else {
                 { SFMBA_PHASE(PH_POINT_REDUCE); launch_mf_point_reduce(b, s_); }
                 { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_mf_image_blocks(b, s_); }
@@ -1111,7 +1122,7 @@ class Solver {
                 launch_linearize(b, s_);
             }
             { SFMBA_PHASE(PH_POINT_REDUCE); launch_point_reduce(b, s_); }
-            { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_reduce(b, s_); launch_diag_fold(b, s_); }
+            { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_blocks_records(b, s_); launch_diag_fold(b, s_); }
             for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
                 // One retry round of every window, the same launches each round
                 // (the windows taking part are flagged on the device).
