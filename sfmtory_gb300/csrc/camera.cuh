@@ -42,9 +42,10 @@ struct __align__(16) ImageLin {
 // Forward projection of normalised coordinates plus the local derivatives
 // the adjoint pass needs: A = d(u,v)/d(xp,yp) (2x2) and the parameter
 // columns G = d(u,v)/d(params) (2x8, zero past the model's count).
-template <typename T>
+template <typename T, int M = -1>
 __device__ __forceinline__ void distort(int model, const T *c, T xp, T yp, T &u, T &v, T A[2][2],
                                         T G[2][8]) {
+    if constexpr (M >= 0) model = M;
 #pragma unroll
     for (int i = 0; i < 8; ++i) { G[0][i] = T(0); G[1][i] = T(0); }
     A[0][1] = T(0);
@@ -249,7 +250,7 @@ struct LinCompact {
     bool pose_on;
 };
 
-template <typename T, int D>
+template <typename T, int D, int M = -1>
 __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T X1, T X2, T ox, T oy, int loss,
                                                   T scale, LinCompact<T, D> &L, const Res64 &rin = Res64()) {
     L.q[0] = im.R[0] * X0 + im.R[1] * X1 + im.R[2] * X2;
@@ -271,7 +272,7 @@ __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T
     const T iz = T(1) / pc2;
     const T xp = pc0 * iz, yp = pc1 * iz;
     T u, v, A[2][2], G[2][8];
-    distort<T>(im.model, im.c, xp, yp, u, v, A, G);
+    distort<T, M>(im.model, im.c, xp, yp, u, v, A, G);
     T s;
     if (rin.use) {
         const double sd = rin.s >= 0.0 ? rin.s

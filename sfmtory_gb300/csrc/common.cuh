@@ -44,10 +44,19 @@ constexpr double kMinDepth = 1e-9;            // crates/sfm-ba/src/lib.rs:256, 3
 constexpr double kFunctionTolerance = 1e-6;   // lib.rs:814
 constexpr int kMaxDampingRetries = 8;         // lib.rs:914
 
-__host__ __device__ inline int model_dof(int model) {
+__host__ __device__ constexpr int model_dof(int model) {
     // crates/sfm-core/src/camera.rs:136-163 (params().len())
     return model == 0 ? 3 : model == 1 ? 4 : model == 2 ? 4 : model == 3 ? 5 : (model == 4 || model == 5) ? 8 : 0;
 }
+
+// Camera model M (a compile-time model id, or -1 for the runtime switch)
+// is specialised for a block width D when every camera of a problem has
+// model M and D is that model's width: the projection and its derivatives
+// then compile without the switch over models.
+__host__ __device__ constexpr bool model_fits_width(int M, int D) { return M >= 0 && 6 + model_dof(M) == D; }
+
+// D rounded up to a multiple of 4 (16-byte rows of FP32 image vectors).
+__host__ __device__ constexpr int pad4(int D) { return (D + 3) & ~3; }
 
 // Width of the per-image variable block: 6 pose columns + the widest camera.
 __host__ __device__ constexpr int block_width_for(int kmax) {

@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(const T *Minv, const T *p, c
 // other parity slot (read by the next iteration only) and the counters.
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const double *part, int nI, int nID,
-                                                 int parity, T *p) {
+                                                 int parity, T *p, int D, T *p4) {
     __shared__ double sh[256];
     if (st->pcg_done) return;
     double a = 0.0, b = 0.0;
@@ -193,7 +193,12 @@ __global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const 
     if (stop) return;
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= nID) return;
-    p[u] = (T)((double)z[u] + beta * (double)p[u]);
+    const T pn = (T)((double)z[u] + beta * (double)p[u]);
+    p[u] = pn;
+    if (p4) {
+        const int i = u / D;
+        p4[(size_t)i * pad4(D) + (u - i * D)] = pn;
+    }
 }
 
 template <typename T>
@@ -233,7 +238,8 @@ void vector_t(const Bufs &b, cudaStream_t s, int parity) {
                                                        (T *)b.pcg_r, (T *)b.pcg_z, b.pcg_part);
     SFMBA_LAUNCH_CHECK();
     k_pcg_dir<T><<<div_up(b.nID, 256), 256, 0, s>>>((const T *)b.pcg_z, b.state, b.pcg_part, b.nI, b.nID, parity,
-                                                    (T *)b.pcg_p);
+                                                    (T *)b.pcg_p, b.D,
+                                                    std::is_same<T, float>::value ? (T *)(void *)b.pcg_p4 : nullptr);
     SFMBA_LAUNCH_CHECK();
 }
 

@@ -16,6 +16,7 @@ struct Bufs {
     int D = 6;        // image block width: 6 pose columns + widest camera
     int nID = 0;      // nI * D
     int mixed = 0;    // 1: FP32 linearisation/Schur/PCG, 0: FP64
+    int uniform_model = -1;  // the model of every camera, -1 when they differ
     int loss = 0;
     double loss_scale = 1.0;
     // problem, solver layout
@@ -75,6 +76,7 @@ struct Bufs {
     long long *count_partials = nullptr;
     // PCG (matrix-free) vectors, [nI*D] each, element type T
     void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
+    float *pcg_p4 = nullptr;      // FP32: [nI*pad4(D)] copy of p with 16-byte rows (point pass)
     void *pcg_u = nullptr;        // [nP*4] per-point Cinv E^T p
     void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
     double *pcg_part = nullptr;   // [3*nI] per-image partial dot products

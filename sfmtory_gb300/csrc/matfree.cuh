@@ -74,11 +74,11 @@ __device__ __forceinline__ void load_record(const T *__restrict__ rec, long long
 // interface: recomputed from the pixel, point and image constants (RC), or
 // read from a stored record. Image blocks are D wide: 3 rotation, 3
 // translation, then the camera's parameters.
-template <typename T, int D, bool RC>
+template <typename T, int D, bool RC, int M = -1>
 struct ObsOp;
 
-template <typename T, int D>
-struct ObsOp<T, D, true> {
+template <typename T, int D, int M>
+struct ObsOp<T, D, true, M> {
     static constexpr int K = LinCompact<T, D>::K;
     LinCompact<T, D> L;
     T R[9];
@@ -102,7 +102,7 @@ struct ObsOp<T, D, true> {
             rin.use = true;
             rin.r0 = v.x; rin.r1 = v.y; rin.s = v.z; rin.ok = v.w != 0.f;
         }
-        valid = linearize_compact<T, D>(im, X0, X1, X2, (T)__int_as_float(rc.z), (T)__int_as_float(rc.w), J.loss,
+        valid = linearize_compact<T, D, M>(im, X0, X1, X2, (T)__int_as_float(rc.z), (T)__int_as_float(rc.w), J.loss,
                                         J.scale, L, rin);
 #pragma unroll
         for (int k = 0; k < 9; ++k) R[k] = im.R[k];
@@ -168,8 +168,8 @@ struct ObsOp<T, D, true> {
     }
 };
 
-template <typename T, int D>
-struct ObsOp<T, D, false> {
+template <typename T, int D, int M>
+struct ObsOp<T, D, false, M> {
     T rr[2], jxm[6], jcm[2 * D];
     bool valid;
 
@@ -212,16 +212,16 @@ struct ObsOp<T, D, false> {
 // Operator of point-major observation o with packed record rc. With
 // `gradient` the recomputed form takes its residual and weight from the
 // FP64 parameters (see Res64).
-template <typename T, int D, bool RC>
-__device__ __forceinline__ void make_op_point_major(const JacSrc<T> &J, int o, int4 rc, ObsOp<T, D, RC> &op,
+template <typename T, int D, bool RC, int M>
+__device__ __forceinline__ void make_op_point_major(const JacSrc<T> &J, int o, int4 rc, ObsOp<T, D, RC, M> &op,
                                                     bool gradient = false) {
     if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)o : -1LL);
     else op.build_record(J.rec, o);
 }
 
 // Operator of image-major observation k with packed record rc.
-template <typename T, int D, bool RC>
-__device__ __forceinline__ void make_op_image_major(const JacSrc<T> &J, long long k, int4 rc, ObsOp<T, D, RC> &op,
+template <typename T, int D, bool RC, int M>
+__device__ __forceinline__ void make_op_image_major(const JacSrc<T> &J, long long k, int4 rc, ObsOp<T, D, RC, M> &op,
                                                     bool gradient = false) {
     if constexpr (RC) op.build(J, rc.x, rc.y, rc, gradient ? (long long)J.img_obs[k] : -1LL);
     else op.build_record(J.rec, J.img_obs[k]);

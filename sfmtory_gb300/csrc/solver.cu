@@ -725,6 +725,9 @@ class Solver {
             }
             b.nI = nI; b.nC = nC; b.nP = nP; b.nO = nO; b.n = n; b.D = D; b.nID = nID;
             b.mixed = mixed; b.loss = o->robust_loss; b.loss_scale = o->loss_scale_px;
+            b.uniform_model = nC > 0 ? model[0] : -1;
+            for (int c = 1; c < nC; ++c)
+                if (model[c] != b.uniform_model) { b.uniform_model = -1; break; }
             b.pcg_tol = o->pcg_tolerance > 0.0 ? o->pcg_tolerance : 0.1;
             b.cam_model = A.take<int>(nC);
             b.cam_of_img = A.take<int>(nI);
@@ -808,6 +811,7 @@ class Solver {
                     b.pcg_r = A.take<char>((size_t)nID * tsz);
                     b.pcg_z = A.take<char>((size_t)nID * tsz);
                     b.pcg_p = A.take<char>((size_t)nID * tsz);
+                    b.pcg_p4 = mixed ? A.take<float>((size_t)nI * pad4(D)) : nullptr;
                     b.pcg_q = A.take<char>((size_t)nID * tsz);
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
                     b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
@@ -897,6 +901,7 @@ class Solver {
             b.n_iachunks = (int)ia.size();
             put_vec(b.iachunk, ia, s_);
             put_vec(b.iachunk_off, ia_off, s_);
+            if (b.pcg_p4) SFMBA_CUDA(cudaMemsetAsync(b.pcg_p4, 0, sizeof(float) * (size_t)nI * pad4(D), s_));
             launch_mf_prepare(b, s_);
         }
         if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
