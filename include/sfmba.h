@@ -192,6 +192,66 @@ int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *window
 int sfmba_filter_and_reoptimize(const sfmba_problem *problem, const sfmba_options *options,
                                 double threshold_px, sfmba_result *result, uint8_t *keep_out);
 
+/* How the global adjustment treats camera intrinsics
+ * (crates/sfm-reconstruction/src/lib.rs:1300-1316, `IntrinsicsMode`). */
+typedef enum sfmba_intrinsics_mode {
+    SFMBA_INTRINSICS_FIXED = 0,        /* intrinsics held                                   */
+    SFMBA_INTRINSICS_FREE = 1,         /* one plain solve with intrinsics free              */
+    SFMBA_INTRINSICS_FREE_GUARDED = 2  /* filtered solves, fixed-vs-free comparison         */
+} sfmba_intrinsics_mode;
+
+/* The intrinsics handling of the reference's global bundle adjustment
+ * (crates/sfm-reconstruction/src/lib.rs:1567-1708, inside
+ * `run_bundle_adjustment`), over an already-built problem. The problem's
+ * fixed_cameras mask holds the cameras the user fixed; a camera seen by
+ * fewer than 5 images is also held when intrinsics are free (:1601-1611,
+ * :1638-1657).
+ *   FIXED: one adjustment with every camera fixed.
+ *   FREE: one adjustment with the free cameras free (:1598-1621).
+ *   FREE_GUARDED: `filter_and_reoptimize` (threshold max_reprojection_error_px)
+ *     with every camera fixed, then, if some camera has >= 5 images, again
+ *     with the free cameras free; the free result is taken iff every camera's
+ *     distortion coefficients are below 0.5 in magnitude (:1672-1677) and its
+ *     plain mean reprojection error over ALL the problem's observations is
+ *     lower than the fixed result's (:1567-1578, :1691-1695).
+ * The options (max_iterations, loss, ...) are used as given: the reference's
+ * caller picks max_iterations per mode (200 / 50 / 50, :1494-1520).
+ * result: the chosen adjustment. keep_out ([num_observations] or NULL): the
+ * observations the chosen adjustment used (all 1 without filtering).
+ * chose_free_out (or NULL): 1 if the intrinsics-free result was taken.
+ * mean_errors_out ([2] or NULL): plain mean reprojection error of the fixed
+ * and of the free candidate (NaN for one not run). Host pointers. */
+int sfmba_adjust_global(const sfmba_problem *problem, const sfmba_options *options,
+                        int32_t intrinsics_mode, double max_reprojection_error_px,
+                        sfmba_result *result, uint8_t *keep_out, int32_t *chose_free_out,
+                        double *mean_errors_out);
+
+/* crates/sfm-geometry/src/pnp.rs:151-206 (`refine_pose_gauss_newton`) for
+ * num independent poses in one call: pose k (poses[k][7], qw qx qy qz tx ty
+ * tz, in and out) takes `iterations` Gauss-Newton steps (left rotation
+ * increment, additive translation, J^T J + 1e-9 I solved by partial-pivot
+ * LU; a singular or non-finite step ends the pose's loop) over its
+ * correspondences [offsets[k], offsets[k+1]) of points3d ([N][3], world) and
+ * points2d_norm ([N][2], normalised image coordinates); offsets[0] = 0,
+ * N = offsets[num]. Host pointers. */
+int sfmba_refine_pose_gauss_newton_batched(int32_t num, const int64_t *offsets, const double *points3d,
+                                           const double *points2d_norm, int32_t iterations, double *poses);
+
+/* crates/sfm-geometry/src/pnp.rs:211-309 (`pnp_ransac`, with ransac.rs:72-131
+ * and pnp.rs:22-130) for num images at once, correspondences laid out as in
+ * sfmba_refine_pose_gauss_newton_batched: 6-point DLT hypotheses from the
+ * xorshift64 stream seeded 0xFACADE, the adaptive iteration count at
+ * confidence 0.999 (at most max_iterations), the local refit over the
+ * inliers and two Gauss-Newton polish rounds, each kept only if it loses no
+ * inliers; `threshold` in normalised units. found_out[k] = 0 where the
+ * reference returns None (then poses_out[k] is unspecified and the mask 0);
+ * else poses_out[k][7] and inliers_out[offsets[k] + i] (may be NULL).
+ * iterations_out[k] (may be NULL): RANSAC iterations run. Host pointers. */
+int sfmba_pnp_ransac_batched(int32_t num, const int64_t *offsets, const double *points3d,
+                             const double *points2d_norm, double threshold, int32_t max_iterations,
+                             double *poses_out, uint8_t *inliers_out, int32_t *found_out,
+                             int64_t *iterations_out);
+
 /* Residual and Jacobian blocks of individual observations, computed on the
  * GPU by the same device code the solver uses (crates/sfm-ba/src/lib.rs:327-590,
  * `analytic_jacobians`). For observation o: r[o][2], j_pose[o][2][6],

@@ -29,8 +29,9 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++ -fopenmp)."""
-    src = os.path.join(_HERE, "sfmba_oracle.cpp")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("sfmba_oracle.cpp", "pnp_oracle.cpp", "Makefile")]
+    if force or not os.path.exists(_LIB_PATH) or any(os.path.getmtime(_LIB_PATH) < os.path.getmtime(s)
+                                                     for s in srcs):
         subprocess.run(["make", "-C", _HERE, "-B" if force else "liboracle_sfmba.so"], check=True,
                        stdout=subprocess.DEVNULL)
     return _LIB_PATH
@@ -49,6 +50,9 @@ def lib():
             L.oracle_default_fixed_params_mask.argtypes = [i64, vp, vp]
             L.oracle_refine_intrinsics.argtypes = [vp, vp, vp]
             L.oracle_filter_and_reoptimize.argtypes = [vp, vp, C.c_double, vp, vp]
+            L.oracle_adjust_global.argtypes = [vp, vp, C.c_int, C.c_double, vp, vp, vp, vp]
+            L.oracle_refine_pose_gauss_newton.argtypes = [C.c_int, vp, vp, vp, C.c_int, vp]
+            L.oracle_pnp_ransac.argtypes = [C.c_long, vp, vp, C.c_double, C.c_long, vp, vp, vp, vp]
             for f in (L.oracle_analytic_jacobians, L.oracle_numerical_jacobians):
                 f.argtypes = [vp, C.c_int, vp, vp, C.c_double, C.c_double, vp, vp, vp, vp]
                 f.restype = C.c_int
@@ -152,6 +156,24 @@ def filter_and_reoptimize(problem, threshold_px: float, options: SfmbaOptions | 
     return OracleResult(buf), keep[: packed.struct.num_observations].astype(bool)
 
 
+def adjust_global(problem, mode: int, threshold_px: float, options: SfmbaOptions | None = None, **kw):
+    """crates/sfm-reconstruction/src/lib.rs:1567-1708 (fixed-vs-free
+    intrinsics handling). Returns (result, keep mask, chose_free, (fixed
+    mean error, free mean error))."""
+    packed = PackedProblem(problem)
+    buf = ResultBuffers(packed)
+    keep = np.zeros(max(packed.struct.num_observations, 1), dtype=np.uint8)
+    chose = C.c_int32(-1)
+    errs = np.full(2, np.nan)
+    st = lib().oracle_adjust_global(C.byref(packed.struct), C.byref(_opts(options, **kw)), int(mode),
+                                    C.c_double(threshold_px), C.byref(buf.struct), keep.ctypes.data,
+                                    C.byref(chose), errs.ctypes.data)
+    if st != 0:
+        raise ValueError(f"oracle_adjust_global failed with status {st}")
+    return (OracleResult(buf), keep[: packed.struct.num_observations].astype(bool), bool(chose.value),
+            (float(errs[0]), float(errs[1])))
+
+
 def refine_intrinsics(problem, options: SfmbaOptions | None = None, **kw) -> np.ndarray:
     """intrinsics.rs refine_intrinsics defaults: 30 iterations, lambda 1e-3, Huber 2 px."""
     base = dict(max_iterations=30)
@@ -237,3 +259,38 @@ def lm_iteration_sample(problem, point_stride: int, chol_dim: int, options: Sfmb
         "schur_scale": schur_scale, "cholesky_scale": chol_scale, "seconds_per_iteration": est,
         "measured_s": float(out[:6].sum()),
     }
+
+
+def refine_pose_gauss_newton(poses, points3d_list, points2d_list, iterations: int) -> np.ndarray:
+    """crates/sfm-geometry/src/pnp.rs:151-206 for each pose (rows of
+    ``poses``, qw qx qy qz tx ty tz) over its own correspondences."""
+    poses = np.ascontiguousarray(poses, dtype=np.float64).copy()
+    off = np.concatenate([[0], np.cumsum([len(p) for p in points3d_list])]).astype(np.int64)
+    X = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1, 3) for p in points3d_list])
+                             if len(points3d_list) else np.zeros((0, 3)))
+    uv = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1, 2) for p in points2d_list])
+                              if len(points2d_list) else np.zeros((0, 2)))
+    st = lib().oracle_refine_pose_gauss_newton(len(poses), off.ctypes.data, X.ctypes.data, uv.ctypes.data,
+                                               int(iterations), poses.ctypes.data)
+    if st != 0:
+        raise ValueError(f"oracle_refine_pose_gauss_newton failed with status {st}")
+    return poses
+
+
+def pnp_ransac(points3d, points2d_norm, threshold: float, max_iterations: int):
+    """crates/sfm-geometry/src/pnp.rs:211-309. Returns None or (pose [7],
+    inlier mask, RANSAC iterations run)."""
+    X = np.ascontiguousarray(points3d, dtype=np.float64).reshape(-1, 3)
+    uv = np.ascontiguousarray(points2d_norm, dtype=np.float64).reshape(-1, 2)
+    n = len(X)
+    pose = np.zeros(7)
+    mask = np.zeros(max(n, 1), np.uint8)
+    found = C.c_int32(0)
+    iters = C.c_int64(0)
+    st = lib().oracle_pnp_ransac(n, X.ctypes.data, uv.ctypes.data, C.c_double(threshold), int(max_iterations),
+                                 pose.ctypes.data, mask.ctypes.data, C.byref(found), C.byref(iters))
+    if st != 0:
+        raise ValueError(f"oracle_pnp_ransac failed with status {st}")
+    if not found.value:
+        return None
+    return pose, mask[:n].astype(bool), int(iters.value)

@@ -1097,6 +1097,106 @@ int oracle_filter_and_reoptimize(const sfmba_problem *p, const sfmba_options *op
     return SFMBA_OK;
 }
 
+// crates/sfm-reconstruction/src/lib.rs:1567-1708 (the intrinsics handling of
+// run_bundle_adjustment over a built problem): mode 0 (Fixed) adjusts with
+// every camera fixed; mode 1 (Free) adjusts once with the cameras that have
+// >= 5 images and are not fixed by the caller left free (:1598-1621); mode 2
+// (FreeGuarded) runs filter_and_reoptimize with every camera fixed and, if
+// some camera has >= 5 images, with those cameras free, and keeps the free
+// result iff every camera's opencv_distortion() coefficient is below 0.5 in
+// magnitude (:1672-1677) and its plain mean reprojection error over all the
+// input observations (:1567-1578) is below the fixed result's (:1691-1695).
+// chose_free = 1 when the free result was taken; errors[2] = the two mean
+// errors (NaN for a candidate not run); keep as in filter_and_reoptimize.
+int oracle_adjust_global(const sfmba_problem *p, const sfmba_options *opt, int mode, double threshold_px,
+                         sfmba_result *res, uint8_t *keep, int32_t *chose_free, double *errors) {
+    Problem P;
+    if (!load(p, P) || !opt || !res || mode < 0 || mode > 2) return SFMBA_ERR_INVALID_ARGUMENT;
+    std::vector<int> per_cam(P.nC, 0);
+    for (long i = 0; i < P.nI; ++i) per_cam[P.cam_of_img[i]] += 1;
+    std::vector<uint8_t> all_fixed(P.nC, 1), free_fixed(P.nC, 0);
+    bool any_eligible = false;
+    for (long c = 0; c < P.nC; ++c) {
+        const bool user = p->fixed_cameras && p->fixed_cameras[c];
+        free_fixed[c] = (per_cam[c] < 5 || user) ? 1 : 0;
+        if (per_cam[c] >= 5) any_eligible = true;
+    }
+    struct Cand {
+        std::vector<double> poses, points, cams;
+        std::vector<uint8_t> keep;
+        sfmba_result r{};
+        double err = std::numeric_limits<double>::quiet_NaN();
+    };
+    auto run = [&](const std::vector<uint8_t> &fc, Cand &c) {
+        sfmba_problem q = *p;
+        q.fixed_cameras = fc.data();
+        c.poses.assign(P.nI * 7, 0.0);
+        c.points.assign(P.nP * 3, 0.0);
+        c.cams.assign(P.nC * 8, 0.0);
+        c.keep.assign((size_t)P.nO + 1, 1);
+        c.r = sfmba_result{};
+        c.r.poses = c.poses.data();
+        c.r.points = c.points.data();
+        c.r.camera_params = c.cams.data();
+        return mode == 2 ? oracle_filter_and_reoptimize(&q, opt, threshold_px, &c.r, c.keep.data())
+                         : oracle_bundle_adjust(&q, opt, &c.r);
+    };
+    auto eval_error = [&](Cand &c) {
+        sfmba_problem q = *p;
+        q.poses = c.poses.data();
+        q.points = c.points.data();
+        q.camera_params = c.cams.data();
+        q.fixed_poses = nullptr;
+        q.fixed_cameras = nullptr;
+        q.fixed_camera_params = nullptr;
+        return oracle_mean_reprojection_error(&q, &c.err);
+    };
+    Cand fixed, free;
+    Cand *chosen = nullptr;
+    int st = SFMBA_OK;
+    if (mode == 1) {
+        if ((st = run(free_fixed, free)) != SFMBA_OK) return st;
+        chosen = &free;
+    } else {
+        if ((st = run(all_fixed, fixed)) != SFMBA_OK) return st;
+        chosen = &fixed;
+        if (mode == 2 && any_eligible) {
+            if ((st = run(free_fixed, free)) != SFMBA_OK) return st;
+            bool plausible = true;
+            for (long c = 0; c < P.nC; ++c) {
+                const double *k = &free.cams[(size_t)c * 8];
+                double d[6] = {0, 0, 0, 0, 0, 0};
+                switch (P.model[c]) {
+                case 2: d[0] = k[3]; break;
+                case 3: d[0] = k[3]; d[1] = k[4]; break;
+                case 4: d[0] = k[4]; d[1] = k[5]; d[2] = k[6]; d[3] = k[7]; break;
+                case 5: d[0] = k[4]; d[1] = k[5]; d[4] = k[6]; d[5] = k[7]; break;
+                default: break;
+                }
+                for (double v : d) plausible = plausible && std::fabs(v) < 0.5;
+            }
+            if ((st = eval_error(fixed)) != SFMBA_OK) return st;
+            if ((st = eval_error(free)) != SFMBA_OK) return st;
+            if (plausible && free.err < fixed.err) chosen = &free;
+        }
+    }
+    if (res->poses) std::memcpy(res->poses, chosen->poses.data(), chosen->poses.size() * sizeof(double));
+    if (res->points) std::memcpy(res->points, chosen->points.data(), chosen->points.size() * sizeof(double));
+    if (res->camera_params)
+        std::memcpy(res->camera_params, chosen->cams.data(), chosen->cams.size() * sizeof(double));
+    res->initial_cost = chosen->r.initial_cost;
+    res->final_cost = chosen->r.final_cost;
+    res->iterations_run = chosen->r.iterations_run;
+    res->status = SFMBA_OK;
+    if (keep && P.nO) std::memcpy(keep, chosen->keep.data(), (size_t)P.nO);
+    if (chose_free) *chose_free = chosen == &free ? 1 : 0;
+    if (errors) {
+        errors[0] = fixed.err;
+        errors[1] = free.err;
+    }
+    return SFMBA_OK;
+}
+
 // intrinsics.rs:116-238 (refine_intrinsics, refine_one_camera): per-camera
 // dense LM over that camera's own parameters with central-difference
 // Jacobians; cameras with fewer than 8 observations are left untouched.

@@ -20,6 +20,8 @@ MODEL_DOF = (3, 4, 4, 5, 8, 8)  # camera.rs:136-163, params().len()
 LOSS_NONE, LOSS_HUBER, LOSS_CAUCHY = range(3)
 PRECISION_FP64, PRECISION_MIXED = range(2)
 SOLVER_AUTO, SOLVER_DENSE, SOLVER_PCG = range(3)
+# sfmba_intrinsics_mode (crates/sfm-reconstruction/src/lib.rs:1300-1316).
+INTRINSICS_FIXED, INTRINSICS_FREE, INTRINSICS_FREE_GUARDED = range(3)
 
 STATUS_NAMES = {
     0: "OK",

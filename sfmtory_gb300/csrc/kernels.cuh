@@ -258,6 +258,36 @@ struct IntrinsicsBufs {
 void launch_refine_intrinsics(const IntrinsicsBufs &q, int max_iterations, double lambda0, int loss, double scale,
                               cudaStream_t s);
 
+// ---- PnP registration and pose refinement (k_pnp.cu)
+// Device arrays of the batched RANSAC PnP: P images, image k's
+// correspondences [off[k], off[k+1]) of X ([N][3]) and uv ([N][2],
+// normalised); B hypotheses per round.
+struct PnpBufs {
+    int P = 0, B = 0;
+    long long max_it = 0;
+    double thr = 0.0;
+    const long long *off = nullptr;
+    const double *X = nullptr, *uv = nullptr;
+    const unsigned long long *raw = nullptr;  // [6 * max_it] xorshift64 stream
+    void *state = nullptr;                    // [P] per-image RANSAC state
+    double *models = nullptr;                 // [P * B][8]
+    unsigned char *valid = nullptr;           // [P * B]
+    long long *counts = nullptr;              // [P * B]
+    int *active = nullptr;                    // images whose loop goes on
+    double *dlt_scratch = nullptr;            // [N][24] DLT rows of the local refit
+    long long *slot_scratch = nullptr;        // [N]
+    unsigned char *mask = nullptr, *mask_trial = nullptr;  // [N]
+    double *poses = nullptr;                  // [P][7] out
+    int *found = nullptr;                     // [P] out
+};
+size_t pnp_state_bytes();
+void launch_pnp_init(const PnpBufs &q, cudaStream_t s);
+void launch_pnp_round(const PnpBufs &q, long long round_base, cudaStream_t s);
+void launch_pnp_finish(const PnpBufs &q, cudaStream_t s);
+void launch_pnp_iterations(const PnpBufs &q, long long *iters, cudaStream_t s);
+void launch_refine_pose_gn(const long long *off, const double *X, const double *uv, int P, int iterations,
+                           double *poses, cudaStream_t s);
+
 // ---- filter_and_reoptimize (k_filter.cu)
 // Device arrays of the observation filter: the current observations in set
 // 0, the kept ones compacted into set 1 (the caller swaps).

@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -1536,6 +1537,257 @@ int sfmba_filter_and_reoptimize(const sfmba_problem *p, const sfmba_options *o, 
     });
     if (r) r->status = st;
     return st;
+}
+
+namespace {
+
+// CameraModel::opencv_distortion (crates/sfm-core/src/camera.rs:192-200):
+// the distortion coefficients of `params` in OpenCV order, zero where the
+// model has none.
+void opencv_distortion(int model, const double *c, double out[6]) {
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    switch (model) {
+    case SFMBA_SIMPLE_RADIAL: out[0] = c[3]; break;
+    case SFMBA_RADIAL: out[0] = c[3]; out[1] = c[4]; break;
+    case SFMBA_OPENCV: out[0] = c[4]; out[1] = c[5]; out[2] = c[6]; out[3] = c[7]; break;
+    case SFMBA_OPENCV_FISHEYE: out[0] = c[4]; out[1] = c[5]; out[4] = c[6]; out[5] = c[7]; break;
+    default: break;
+    }
+}
+
+// One candidate of the global adjustment, in host buffers.
+struct Candidate {
+    std::vector<double> poses, points, cams;
+    std::vector<uint8_t> keep;
+    sfmba_result r{};
+    double mean_error = std::numeric_limits<double>::quiet_NaN();
+};
+
+}  // namespace
+
+int sfmba_adjust_global(const sfmba_problem *p, const sfmba_options *o, int32_t mode, double threshold_px,
+                        sfmba_result *r, uint8_t *keep_out, int32_t *chose_free_out, double *mean_errors_out) {
+    const int st = guarded([&] {
+        const double t0 = now_s();
+        if (!r) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "result is NULL");
+        if (mode != SFMBA_INTRINSICS_FIXED && mode != SFMBA_INTRINSICS_FREE && mode != SFMBA_INTRINSICS_FREE_GUARDED)
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "unknown intrinsics mode");
+        check_options(o);
+        check_problem_shape(p);
+        check_problem_host(p);
+        const int nI = (int)p->num_images, nC = (int)p->num_cameras, nP = (int)p->num_points;
+        const long long nO = p->num_observations;
+        // Images per camera (lib.rs:1639-1642) and the cameras left free when
+        // intrinsics are free: seen by >= 5 images and not fixed by the user
+        // (:1601-1611, :1648-1657).
+        std::vector<int> per_cam(nC, 0);
+        for (int i = 0; i < nI; ++i) per_cam[p->camera_of_image[i]] += 1;
+        constexpr int kMinImagesPerCamera = 5;
+        std::vector<uint8_t> all_fixed(nC, 1), free_fixed(nC, 0);
+        bool any_eligible = false;
+        for (int c = 0; c < nC; ++c) {
+            const bool user = p->fixed_cameras && p->fixed_cameras[c];
+            free_fixed[c] = (per_cam[c] < kMinImagesPerCamera || user) ? 1 : 0;
+            any_eligible = any_eligible || per_cam[c] >= kMinImagesPerCamera;
+        }
+        // run_ba (:1585-1593): the filtered adjustment in the guarded mode,
+        // the plain one otherwise.
+        auto run = [&](const std::vector<uint8_t> &fixed_cams, Candidate &out) {
+            sfmba_problem q = *p;
+            q.fixed_cameras = fixed_cams.data();
+            out.poses.assign((size_t)nI * 7, 0.0);
+            out.points.assign((size_t)nP * 3, 0.0);
+            out.cams.assign((size_t)nC * 8, 0.0);
+            out.keep.assign((size_t)nO, 1);
+            out.r = sfmba_result{};
+            out.r.poses = out.poses.data();
+            out.r.points = out.points.data();
+            out.r.camera_params = out.cams.data();
+            const int s2 = mode == SFMBA_INTRINSICS_FREE_GUARDED
+                               ? sfmba_filter_and_reoptimize(&q, o, threshold_px, &out.r, out.keep.data())
+                               : sfmba_bundle_adjust(&q, o, &out.r);
+            if (s2 != SFMBA_OK) throw Error(s2, g_last_error);
+        };
+        // eval_error (:1567-1578): plain mean reprojection error of the
+        // output over all the problem's observations.
+        auto eval_error = [&](Candidate &c) {
+            sfmba_problem q = *p;
+            q.poses = c.poses.data();
+            q.points = c.points.data();
+            q.camera_params = c.cams.data();
+            q.fixed_poses = nullptr;
+            q.fixed_cameras = nullptr;
+            q.fixed_camera_params = nullptr;
+            const int s2 = sfmba_mean_reprojection_error(&q, &c.mean_error);
+            if (s2 != SFMBA_OK) throw Error(s2, g_last_error);
+        };
+        Candidate fixed, free;
+        Candidate *chosen = nullptr;
+        if (mode == SFMBA_INTRINSICS_FREE) {  // :1598-1621, no comparison
+            run(free_fixed, free);
+            chosen = &free;
+        } else {
+            run(all_fixed, fixed);
+            chosen = &fixed;
+            if (mode == SFMBA_INTRINSICS_FREE_GUARDED && any_eligible) {
+                run(free_fixed, free);
+                bool plausible = true;  // :1672-1677
+                for (int c = 0; c < nC; ++c) {
+                    double d[6];
+                    opencv_distortion(p->camera_model[c], free.cams.data() + 8 * (size_t)c, d);
+                    for (int k = 0; k < 6; ++k) plausible = plausible && std::fabs(d[k]) < 0.5;
+                }
+                eval_error(fixed);
+                eval_error(free);
+                if (plausible && free.mean_error < fixed.mean_error) chosen = &free;  // :1691-1695
+            }
+        }
+        if (r->poses) std::memcpy(r->poses, chosen->poses.data(), sizeof(double) * 7 * (size_t)nI);
+        if (r->points) std::memcpy(r->points, chosen->points.data(), sizeof(double) * 3 * (size_t)nP);
+        if (r->camera_params) std::memcpy(r->camera_params, chosen->cams.data(), sizeof(double) * 8 * (size_t)nC);
+        if (keep_out && nO) std::memcpy(keep_out, chosen->keep.data(), (size_t)nO);
+        if (chose_free_out) *chose_free_out = chosen == &free ? 1 : 0;
+        if (mean_errors_out) {
+            mean_errors_out[0] = fixed.mean_error;
+            mean_errors_out[1] = free.mean_error;
+        }
+        double *pp = r->poses, *pt = r->points, *pc = r->camera_params;
+        *r = chosen->r;
+        r->poses = pp; r->points = pt; r->camera_params = pc;
+        r->seconds = now_s() - t0;
+    });
+    if (r) r->status = st;
+    return st;
+}
+
+namespace {
+
+// Offsets of a batch of correspondence sets: 0 first, non-decreasing.
+long long check_offsets(int32_t num, const int64_t *offsets) {
+    if (num < 0) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "negative batch size");
+    if (num > 0 && !offsets) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "offsets is NULL");
+    if (num == 0) return 0;
+    if (offsets[0] != 0) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "offsets[0] must be 0");
+    for (int32_t k = 0; k < num; ++k)
+        if (offsets[k + 1] < offsets[k]) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "offsets decrease");
+    return offsets[num];
+}
+
+}  // namespace
+
+int sfmba_refine_pose_gauss_newton_batched(int32_t num, const int64_t *offsets, const double *points3d,
+                                           const double *points2d_norm, int32_t iterations, double *poses) {
+    return guarded([&] {
+        const long long N = check_offsets(num, offsets);
+        if (iterations < 0) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "negative iteration count");
+        if (num > 0 && !poses) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "poses is NULL");
+        if (N > 0 && (!points3d || !points2d_norm)) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "points are NULL");
+        if (num == 0) return;
+        Context &ctx = context();
+        cudaStream_t s = ctx.stream;
+        Arena &A = ctx.aux;
+        long long *off = nullptr;
+        double *X = nullptr, *uv = nullptr, *P = nullptr;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            off = A.take<long long>((size_t)num + 1);
+            X = A.take<double>((size_t)N * 3 + 1);
+            uv = A.take<double>((size_t)N * 2 + 1);
+            P = A.take<double>((size_t)num * 7);
+        }
+        put(off, reinterpret_cast<const long long *>(offsets), (size_t)num + 1, false, s);
+        if (N) {
+            put(X, points3d, (size_t)N * 3, false, s);
+            put(uv, points2d_norm, (size_t)N * 2, false, s);
+        }
+        put(P, poses, (size_t)num * 7, false, s);
+        launch_refine_pose_gn(off, X, uv, num, iterations, P, s);
+        SFMBA_CUDA(cudaMemcpyAsync(poses, P, sizeof(double) * 7 * (size_t)num, cudaMemcpyDeviceToHost, s));
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int sfmba_pnp_ransac_batched(int32_t num, const int64_t *offsets, const double *points3d,
+                             const double *points2d_norm, double threshold, int32_t max_iterations,
+                             double *poses_out, uint8_t *inliers_out, int32_t *found_out, int64_t *iterations_out) {
+    return guarded([&] {
+        const long long N = check_offsets(num, offsets);
+        if (max_iterations < 0) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "negative max_iterations");
+        if (std::isnan(threshold)) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "threshold is NaN");
+        if (num > 0 && (!poses_out || !found_out)) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "outputs are NULL");
+        if (N > 0 && (!points3d || !points2d_norm)) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "points are NULL");
+        if (num == 0) return;
+        if ((long long)num * 32 > (1LL << 31) - 1) throw Error(SFMBA_ERR_UNSUPPORTED, "too many images");
+        Context &ctx = context();
+        cudaStream_t s = ctx.stream;
+        Arena &A = ctx.aux;
+        PnpBufs q;
+        q.P = num;
+        q.max_it = max_iterations;
+        q.B = (int)std::max<long long>(1, std::min<long long>(128, max_iterations));
+        q.thr = threshold;
+        long long *off = nullptr, *iters = nullptr;
+        double *X = nullptr, *uv = nullptr;
+        unsigned long long *raw = nullptr;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            off = A.take<long long>((size_t)num + 1);
+            X = A.take<double>((size_t)N * 3 + 1);
+            uv = A.take<double>((size_t)N * 2 + 1);
+            raw = A.take<unsigned long long>((size_t)6 * max_iterations + 1);
+            q.state = A.take<char>(pnp_state_bytes() * (size_t)num);
+            q.models = A.take<double>((size_t)num * q.B * 8);
+            q.valid = A.take<unsigned char>((size_t)num * q.B);
+            q.counts = A.take<long long>((size_t)num * q.B);
+            q.active = A.take<int>(1);
+            q.dlt_scratch = A.take<double>((size_t)N * 24 + 1);
+            q.slot_scratch = A.take<long long>((size_t)N + 1);
+            q.mask = A.take<unsigned char>((size_t)N + 1);
+            q.mask_trial = A.take<unsigned char>((size_t)N + 1);
+            q.poses = A.take<double>((size_t)num * 7);
+            q.found = A.take<int>(num);
+            iters = A.take<long long>(num);
+        }
+        q.off = off;
+        q.X = X;
+        q.uv = uv;
+        q.raw = raw;
+        // ransac.rs:43-60: xorshift64 seeded 0xFACADE | 1, six values per iteration.
+        std::vector<unsigned long long> stream((size_t)6 * max_iterations);
+        unsigned long long x = 0xFACADEull | 1ull;
+        for (auto &v : stream) {
+            x ^= x << 13;
+            x ^= x >> 7;
+            x ^= x << 17;
+            v = x;
+        }
+        put(off, reinterpret_cast<const long long *>(offsets), (size_t)num + 1, false, s);
+        if (N) {
+            put(X, points3d, (size_t)N * 3, false, s);
+            put(uv, points2d_norm, (size_t)N * 2, false, s);
+        }
+        if (!stream.empty()) put_vec(raw, stream, s);
+        launch_pnp_init(q, s);
+        for (long long base = 0; base < max_iterations; base += q.B) {
+            launch_pnp_round(q, base, s);
+            int active = 0;
+            SFMBA_CUDA(cudaMemcpyAsync(&active, q.active, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SFMBA_CUDA(cudaStreamSynchronize(s));
+            if (active == 0) break;
+        }
+        launch_pnp_finish(q, s);
+        launch_pnp_iterations(q, iters, s);
+        std::vector<int> found(num);
+        SFMBA_CUDA(cudaMemcpyAsync(poses_out, q.poses, sizeof(double) * 7 * (size_t)num, cudaMemcpyDeviceToHost, s));
+        SFMBA_CUDA(cudaMemcpyAsync(found.data(), q.found, sizeof(int) * (size_t)num, cudaMemcpyDeviceToHost, s));
+        if (inliers_out && N)
+            SFMBA_CUDA(cudaMemcpyAsync(inliers_out, q.mask, (size_t)N, cudaMemcpyDeviceToHost, s));
+        if (iterations_out)
+            SFMBA_CUDA(cudaMemcpyAsync(iterations_out, iters, sizeof(long long) * (size_t)num,
+                                       cudaMemcpyDeviceToHost, s));
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+        for (int32_t k = 0; k < num; ++k) found_out[k] = found[k];
+    });
 }
 
 int sfmba_refine_intrinsics(const sfmba_problem *p, const sfmba_options *o, double *cams) {

@@ -38,6 +38,9 @@ EXPORTED_SYMBOLS = (
     "sfmba_refine_intrinsics",
     "sfmba_bundle_adjust_batched",
     "sfmba_filter_and_reoptimize",
+    "sfmba_adjust_global",
+    "sfmba_refine_pose_gauss_newton_batched",
+    "sfmba_pnp_ransac_batched",
     "sfmba_residuals_jacobians",
     "sfmba_total_cost_noalloc",
     "sfmba_profile_enable",
@@ -77,6 +80,9 @@ def load(path: str | None = None):
         L.sfmba_refine_intrinsics.argtypes = [vp, vp, vp]
         L.sfmba_bundle_adjust_batched.argtypes = [C.c_int32, vp, vp, vp]
         L.sfmba_filter_and_reoptimize.argtypes = [vp, vp, C.c_double, vp, vp]
+        L.sfmba_adjust_global.argtypes = [vp, vp, C.c_int32, C.c_double, vp, vp, vp, vp]
+        L.sfmba_refine_pose_gauss_newton_batched.argtypes = [C.c_int32, vp, vp, vp, C.c_int32, vp]
+        L.sfmba_pnp_ransac_batched.argtypes = [C.c_int32, vp, vp, vp, C.c_double, C.c_int32, vp, vp, vp, vp]
         L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
         L.sfmba_total_cost_noalloc.argtypes = [vp, vp, vp, vp]
         L.sfmba_profile_enable.argtypes = [C.c_int32]
@@ -208,6 +214,73 @@ def filter_and_reoptimize_arrays(problem, threshold_px: float, opts: SfmbaOption
     _check(L.sfmba_filter_and_reoptimize(C.byref(packed.struct), C.byref(o), C.c_double(threshold_px),
                                          C.byref(buf.struct), keep.ctypes.data))
     return Result(buf), keep[: packed.struct.num_observations].astype(bool)
+
+
+def adjust_global_arrays(problem, mode: int, threshold_px: float, opts: SfmbaOptions | None = None, **kw):
+    """The fixed-vs-free intrinsics handling of the reference's global
+    adjustment (crates/sfm-reconstruction/src/lib.rs:1567-1708) on the GPU.
+    Returns (Result of the chosen adjustment, keep mask, chose_free,
+    (fixed mean error, free mean error))."""
+    L = load()
+    packed = PackedProblem(problem)
+    buf = ResultBuffers(packed)
+    o = opts if opts is not None else default_options(**kw)
+    keep = np.zeros(max(packed.struct.num_observations, 1), dtype=np.uint8)
+    chose = C.c_int32(-1)
+    errs = np.full(2, np.nan)
+    _check(L.sfmba_adjust_global(C.byref(packed.struct), C.byref(o), C.c_int32(mode), C.c_double(threshold_px),
+                                 C.byref(buf.struct), keep.ctypes.data, C.byref(chose), errs.ctypes.data))
+    return (Result(buf), keep[: packed.struct.num_observations].astype(bool), bool(chose.value),
+            (float(errs[0]), float(errs[1])))
+
+
+def _pack_correspondences(points3d_list, points2d_list):
+    if len(points3d_list) != len(points2d_list):
+        raise ValueError("points3d and points2d lists differ in length")
+    n = [len(p) for p in points3d_list]
+    if any(len(b) != a for a, b in zip(n, points2d_list)):
+        raise ValueError("a 3D/2D correspondence set differs in length")
+    off = np.concatenate([[0], np.cumsum(n)]).astype(np.int64)
+    X = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1, 3) for p in points3d_list])
+                             if n and off[-1] else np.zeros((1, 3)))
+    uv = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1, 2) for p in points2d_list])
+                              if n and off[-1] else np.zeros((1, 2)))
+    return off, X, uv
+
+
+def refine_pose_gauss_newton_batched(poses, points3d_list, points2d_list, iterations: int) -> np.ndarray:
+    """crates/sfm-geometry/src/pnp.rs:151-206 on the GPU for every pose
+    (rows qw qx qy qz tx ty tz) over its own correspondences."""
+    L = load()
+    off, X, uv = _pack_correspondences(points3d_list, points2d_list)
+    out = np.ascontiguousarray(poses, dtype=np.float64).reshape(-1, 7).copy()
+    if len(out) != len(off) - 1:
+        raise ValueError("one pose per correspondence set")
+    _check(L.sfmba_refine_pose_gauss_newton_batched(len(out), off.ctypes.data, X.ctypes.data, uv.ctypes.data,
+                                                    int(iterations), out.ctypes.data))
+    return out
+
+
+def pnp_ransac_batched(points3d_list, points2d_list, threshold: float, max_iterations: int):
+    """crates/sfm-geometry/src/pnp.rs:211-309 on the GPU for many images.
+    Returns, per image, None or (pose [7], inlier mask, RANSAC iterations)."""
+    L = load()
+    off, X, uv = _pack_correspondences(points3d_list, points2d_list)
+    P = len(off) - 1
+    poses = np.zeros((max(P, 1), 7))
+    mask = np.zeros(max(int(off[-1]), 1), np.uint8)
+    found = np.zeros(max(P, 1), np.int32)
+    iters = np.zeros(max(P, 1), np.int64)
+    _check(L.sfmba_pnp_ransac_batched(P, off.ctypes.data, X.ctypes.data, uv.ctypes.data, C.c_double(threshold),
+                                      int(max_iterations), poses.ctypes.data, mask.ctypes.data,
+                                      found.ctypes.data, iters.ctypes.data))
+    out = []
+    for k in range(P):
+        if not found[k]:
+            out.append(None)
+        else:
+            out.append((poses[k].copy(), mask[off[k]:off[k + 1]].astype(bool), int(iters[k])))
+    return out
 
 
 def profile_enable(on: bool = True) -> None:

@@ -27,6 +27,8 @@ from .problem import (
     perturb_pose,
     project,
     quat_from_euler,
+    quat_from_scaled_axis,
+    quat_to_matrix,
 )
 
 
@@ -459,3 +461,83 @@ WORKLOADS = {
     "radial500": radial500,
     "radial2000": radial2000,
 }
+
+
+def shared_ring(seed: int = 0, scale: float = 0.1, images_per_camera=(8, 8), model: int = PINHOLE,
+                k: float = 0.0) -> Problem:
+    """ring16's geometry with its 16 images sharing a few physical cameras
+    (``images_per_camera[c]`` consecutive images each), for the fixed-vs-free
+    intrinsics handling of the global adjustment. PINHOLE keeps ring16's
+    observations; SIMPLE_RADIAL re-projects them with distortion ``k``
+    (true f = 1200, cx = 800, cy = 600) plus 0.5 px noise, and starts from
+    the true k. Each camera starts with its first image's 3 % focal error."""
+    base = ring16(seed=seed, scale=scale)
+    assert sum(images_per_camera) == 16
+    cam_of_img = np.repeat(np.arange(len(images_per_camera), dtype=np.int32), images_per_camera)
+    first = np.concatenate([[0], np.cumsum(images_per_camera)[:-1]])
+    n_cam = len(images_per_camera)
+    obs = base.obs_xy
+    if model == SIMPLE_RADIAL:
+        true = _pad([1200.0, 800.0, 600.0, k])
+        pc = camera_frame(base.meta["true_poses"][base.obs_image], base.meta["true_points"][base.obs_point])
+        rng = np.random.default_rng(seed + 1000)
+        obs = project(np.full(len(pc), SIMPLE_RADIAL), np.tile(true, (len(pc), 1)), pc)
+        obs = (obs + rng.normal(0.0, 0.5, obs.shape)).astype(np.float32).astype(np.float64)
+        cams = np.tile(true, (n_cam, 1))
+        cams[:, 0] = base.camera_params[first, 0]
+        mask = np.zeros((n_cam, MAX_CAMERA_PARAMS), bool)
+        mask[:, 1:3] = True
+    else:
+        cams = base.camera_params[first].copy()
+        mask = base.fixed_camera_params[first].copy()
+    return base.copy(camera_of_image=cam_of_img, camera_model=np.full(n_cam, model, np.int32),
+                     camera_params=cams, obs_xy=obs, fixed_cameras=np.zeros(n_cam, bool),
+                     fixed_camera_params=mask,
+                     meta=dict(base.meta, name="shared_ring", images_per_camera=tuple(images_per_camera)))
+
+
+def pnp_known_pose_fixture():
+    """recovers_known_pose_from_synthetic_correspondences
+    (crates/sfm-geometry/src/pnp.rs:311-339): true pose from Euler angles
+    (0.05, -0.1, 0.02) and t = (0.2, -0.1, 0.5); 30 points
+    (0.5 sin 0.5t, 0.5 cos 0.3t, 5 + 0.2t) and their exact normalised
+    projections. Returns (pose [7], points [30, 3], uv [30, 2])."""
+    pose = np.concatenate([quat_from_euler(0.05, -0.1, 0.02), [0.2, -0.1, 0.5]])
+    t = np.arange(30, dtype=np.float64)
+    X = np.stack([0.5 * np.sin(t * 0.5), 0.5 * np.cos(t * 0.3), 5.0 + 0.2 * t], 1)
+    pc = camera_frame(np.tile(pose, (30, 1)), X)
+    return pose, X, pc[:, :2] / pc[:, 2:3]
+
+
+def pnp_batch(seed: int = 0, num_images: int = 64, n_min: int = 200, n_max: int = 2000, outlier_frac: float = 0.3,
+              noise_px: float = 0.5, focal: float = 1200.0):
+    """Registration of many images at once, as the incremental pipeline
+    registers them (crates/sfm-reconstruction/src/lib.rs:654-676): per image
+    n ~ U[n_min, n_max] 2D-3D correspondences of points 4-12 units in front
+    of the camera inside a 60 degree cone, normalised observations with
+    ``noise_px`` / focal noise, a fraction replaced by uniform outliers.
+    Returns (true poses [num_images, 7], list of points [n, 3], list of
+    uv [n, 2], threshold = 8 px / focal)."""
+    rng = np.random.default_rng(seed)
+    poses, Xs, uvs = [], [], []
+    for _ in range(num_images):
+        ax = rng.normal(size=3)
+        ax *= rng.uniform(0.0, 0.5) / np.linalg.norm(ax)
+        q = quat_from_scaled_axis(ax)
+        t = rng.uniform(-2.0, 2.0, 3)
+        pose = np.concatenate([q, t])
+        n = int(rng.integers(n_min, n_max + 1))
+        d = rng.uniform(4.0, 12.0, n)
+        xy = rng.uniform(-0.55, 0.55, (n, 2))
+        pc = np.concatenate([xy * d[:, None], d[:, None]], 1)
+        # world point X with R X + t = pc
+        R = quat_to_matrix(q)
+        X = (pc - t) @ R
+        uv = xy + rng.normal(0.0, noise_px / focal, (n, 2))
+        k = int(round(outlier_frac * n))
+        idx = rng.choice(n, k, replace=False)
+        uv[idx] = rng.uniform(-0.6, 0.6, (k, 2))
+        poses.append(pose)
+        Xs.append(X)
+        uvs.append(uv)
+    return np.array(poses), Xs, uvs, 8.0 / focal

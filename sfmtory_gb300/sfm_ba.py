@@ -18,7 +18,7 @@ from __future__ import annotations
 
 import enum
 from dataclasses import dataclass, field
-from typing import List, Optional, Sequence
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -254,6 +254,40 @@ def filter_and_reoptimize(input: BaInput, params: BaParams, threshold_px: float)
              for i in range(len(input.poses))]
     return BaOutput(poses, [r.points[k].copy() for k in range(len(r.points))], cams,
                     r.initial_cost, r.final_cost, r.iterations_run)
+
+
+class IntrinsicsMode(enum.IntEnum):
+    """crates/sfm-reconstruction/src/lib.rs:1300-1316."""
+
+    FIXED = 0
+    FREE = 1
+    FREE_GUARDED = 2
+
+
+#: max_iterations the reference's run_bundle_adjustment gives each mode
+#: (crates/sfm-reconstruction/src/lib.rs:1494-1520).
+GLOBAL_MAX_ITERATIONS = {IntrinsicsMode.FREE_GUARDED: 200, IntrinsicsMode.FREE: 50, IntrinsicsMode.FIXED: 50}
+
+
+def adjust_global(input: BaInput, params: BaParams, intrinsics: IntrinsicsMode,
+                  max_reprojection_error_px: float) -> Tuple[BaOutput, bool]:
+    """The intrinsics handling of the reference's global bundle adjustment
+    (crates/sfm-reconstruction/src/lib.rs:1567-1708) over a built BaInput:
+    FIXED holds every camera; FREE frees the cameras seen by >= 5 images
+    that ``input.fixed_cameras`` does not fix; FREE_GUARDED runs
+    ``filter_and_reoptimize`` both ways and keeps the free result only if
+    its distortion is plausible (|d| < 0.5) and its plain mean reprojection
+    error is lower. ``params`` is used as given (the reference's caller
+    picks ``max_iterations`` per mode, see GLOBAL_MAX_ITERATIONS). Returns
+    the chosen output and whether it is the intrinsics-free one."""
+    r, _, chose_free, _ = native.adjust_global_arrays(input.to_problem(), int(intrinsics),
+                                                      max_reprojection_error_px, params.to_options())
+    cams = [CameraModel(c.model_id, tuple(float(x) for x in r.camera_params[k, : len(c.param_values)]))
+            for k, c in enumerate(input.cameras)]
+    poses = [Pose(tuple(map(float, r.poses[i, :4])), tuple(map(float, r.poses[i, 4:])))
+             for i in range(len(input.poses))]
+    return BaOutput(poses, [r.points[k].copy() for k in range(len(r.points))], cams,
+                    r.initial_cost, r.final_cost, r.iterations_run), chose_free
 
 
 def mean_reprojection_error(input: BaInput) -> float:

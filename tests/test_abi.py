@@ -97,3 +97,37 @@ def test_batched_rejects_invalid_input_before_device():
     assert L.sfmba_bundle_adjust_batched(1, C.byref(packed.struct), C.byref(bad_opts), res) == 1
     assert res[0].status == 1
     assert L.sfmba_bundle_adjust_batched(0, None, C.byref(o), None) == 0
+
+
+def test_pnp_entries_reject_invalid_input_before_device():
+    """Batch offsets must start at 0 and not decrease; counts and iteration
+    limits must be non-negative; an empty batch is a no-op."""
+    L = native.load()
+    off_bad = np.array([0, 10, 5], np.int64)
+    off_start = np.array([3, 10], np.int64)
+    X = np.zeros((10, 3))
+    uv = np.zeros((10, 2))
+    poses = np.zeros((2, 7))
+    found = np.zeros(2, np.int32)
+    for off, n in ((off_bad, 2), (off_start, 1)):
+        assert L.sfmba_pnp_ransac_batched(n, off.ctypes.data, X.ctypes.data, uv.ctypes.data, C.c_double(0.01),
+                                          100, poses.ctypes.data, None, found.ctypes.data, None) == 1
+        assert L.sfmba_refine_pose_gauss_newton_batched(n, off.ctypes.data, X.ctypes.data, uv.ctypes.data, 5,
+                                                        poses.ctypes.data) == 1
+    ok = np.array([0, 10], np.int64)
+    assert L.sfmba_pnp_ransac_batched(1, ok.ctypes.data, X.ctypes.data, uv.ctypes.data, C.c_double(0.01), -1,
+                                      poses.ctypes.data, None, found.ctypes.data, None) == 1
+    assert L.sfmba_pnp_ransac_batched(1, ok.ctypes.data, X.ctypes.data, uv.ctypes.data, C.c_double(float("nan")),
+                                      10, poses.ctypes.data, None, found.ctypes.data, None) == 1
+    assert L.sfmba_refine_pose_gauss_newton_batched(1, ok.ctypes.data, X.ctypes.data, uv.ctypes.data, -2,
+                                                    poses.ctypes.data) == 1
+    assert L.sfmba_pnp_ransac_batched(-1, None, None, None, C.c_double(0.01), 10, None, None, None, None) == 1
+    assert L.sfmba_pnp_ransac_batched(0, None, None, None, C.c_double(0.01), 10, None, None, None, None) == 0
+    assert L.sfmba_refine_pose_gauss_newton_batched(0, None, None, None, 10, None) == 0
+
+
+def test_adjust_global_rejects_unknown_mode_before_device():
+    p = scenes.shared_ring(0, 0.05)
+    with pytest.raises(native.SfmbaError) as e:
+        native.adjust_global_arrays(p, 7, 4.0)
+    assert e.value.status == 1

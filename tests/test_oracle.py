@@ -176,3 +176,78 @@ def test_oracle_filter_and_reoptimize_semantics(oracle_lib):
     r, keep = oracle_lib.filter_and_reoptimize(q, 3.0, **kw)
     assert 0.8 * q.num_observations < keep.sum() < q.num_observations
     assert r.final_cost < oracle_lib.bundle_adjust(q, **kw).final_cost
+
+
+def _with_outliers(p, frac=0.03, seed=7):
+    rng = np.random.default_rng(seed)
+    q = p.copy()
+    idx = rng.choice(q.num_observations, int(frac * q.num_observations), replace=False)
+    q.obs_xy[idx] = rng.uniform([0.0, 0.0], [1600.0, 1200.0], size=(len(idx), 2))
+    return q
+
+
+def test_oracle_adjust_global_semantics(oracle_lib):
+    """crates/sfm-reconstruction/src/lib.rs:1567-1708 restated: FIXED holds
+    every camera; FREE leaves a camera with < 5 images held; FREE_GUARDED
+    filters, takes the free result when its plain mean error is lower, and
+    rejects it when a distortion coefficient reaches 0.5 even though its
+    error is lower."""
+    kw = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=1.0, max_iterations=50)
+    p = _with_outliers(scenes.shared_ring(0, 0.1))
+    r, keep, chose, errs = oracle_lib.adjust_global(p, 0, 4.0, **kw)
+    assert not chose and keep.all() and np.isnan(errs).all()
+    assert np.array_equal(r.camera_params, p.camera_params)
+    r, keep, chose, errs = oracle_lib.adjust_global(p, 2, 4.0, **kw)
+    assert chose and errs[1] < errs[0]
+    assert 0.95 * p.num_observations < keep.sum() < p.num_observations  # outliers filtered
+    few = scenes.shared_ring(0, 0.1, images_per_camera=(12, 4))
+    r, _, chose, _ = oracle_lib.adjust_global(few, 1, 4.0, **kw)
+    assert chose and np.array_equal(r.camera_params[1], few.camera_params[1])
+    assert not np.array_equal(r.camera_params[0], few.camera_params[0])
+    # A user-fixed camera stays held too.
+    held = few.copy(fixed_cameras=np.array([True, False]))
+    r, _, _, _ = oracle_lib.adjust_global(held, 1, 4.0, **kw)
+    assert np.array_equal(r.camera_params, few.camera_params)
+    rad = scenes.shared_ring(0, 0.1, model=abi.SIMPLE_RADIAL, k=0.6)
+    r, _, chose, errs = oracle_lib.adjust_global(rad, 2, 4.0, **kw)
+    assert not chose and errs[1] < errs[0]
+    assert np.array_equal(r.camera_params, rad.camera_params)
+
+
+def test_oracle_pnp_recovers_known_pose(oracle_lib):
+    """recovers_known_pose_from_synthetic_correspondences (crates/sfm-geometry/
+    src/pnp.rs:311-339): threshold 0.01, 500 iterations; every point an
+    inlier, rotation and translation errors below 1e-4."""
+    from sfmtory_gb300.problem import quat_to_matrix
+
+    pose, X, uv = scenes.pnp_known_pose_fixture()
+    r = oracle_lib.pnp_ransac(X, uv, 0.01, 500)
+    assert r is not None
+    p, inl, _ = r
+    assert inl.all()
+    Rt, Re = quat_to_matrix(pose[:4]), quat_to_matrix(p[:4])
+    assert np.arccos(np.clip((np.trace(Rt.T @ Re) - 1) / 2, -1, 1)) < 1e-4
+    assert np.linalg.norm(p[4:] - pose[4:]) < 1e-4
+
+
+def test_oracle_pnp_none_cases(oracle_lib):
+    """pnp.rs:217-219 / ransac.rs:88: fewer than 6 correspondences or no
+    iterations give None; coplanar points fail the conditioning test of
+    every sample (pnp.rs:115-130), so no model is ever found."""
+    pose, X, uv = scenes.pnp_known_pose_fixture()
+    assert oracle_lib.pnp_ransac(X[:5], uv[:5], 0.01, 500) is None
+    assert oracle_lib.pnp_ransac(X, uv, 0.01, 0) is None
+    flat = X.copy()
+    flat[:, 2] = 5.0
+    assert oracle_lib.pnp_ransac(flat, uv, 0.01, 50) is None
+
+
+def test_oracle_refine_pose_converges_on_exact_data(oracle_lib):
+    """refine_pose_gauss_newton (pnp.rs:151-206) from a perturbed pose on
+    noise-free correspondences returns to the true pose."""
+    pose, X, uv = scenes.pnp_known_pose_fixture()
+    init = pose.copy()
+    init[4:] += [0.02, -0.01, 0.03]
+    out = oracle_lib.refine_pose_gauss_newton(init[None], [X], [uv], 10)[0]
+    assert np.abs(out[4:] - pose[4:]).max() < 1e-9
+    assert min(np.abs(out[:4] - pose[:4]).max(), np.abs(out[:4] + pose[:4]).max()) < 1e-9
