@@ -57,7 +57,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-side", action="store_true",
                     help="skip the dense 500-camera and the 512-window measurements reported beside the headline")
-    ap.add_argument("--only", choices=["dense_radial500", "windows512"],
+    ap.add_argument("--only", choices=["dense_radial500", "windows512", "pnp"],
                     help="run only that side measurement and print its JSON object")
     ap.add_argument("--kernel-variant", type=int, default=0,
                     help="0: autotuned launch variants of the PCG passes; 1..4: force one (for profiling)")
@@ -461,6 +461,51 @@ def windows512(args, with_cpu):
     return out
 
 
+def pnp_batch_measure(args, with_cpu, num_images=4096):
+    """Camera registration (crates/sfm-geometry/src/pnp.rs:211-309) of many
+    images in one sfmba_pnp_ransac_batched call from host buffers: per
+    image 200-2000 correspondences, 30 % outliers, 0.5 px noise, threshold
+    8 px / 1200 px focal, at most 2000 RANSAC iterations (the reference
+    pipeline's settings, crates/sfm-reconstruction/src/lib.rs:117-118). The
+    CPU sample runs the oracle's restatement image by image on one core and
+    checks the GPU's models on those images against it."""
+    from sfmtory_gb300 import native, scenes
+
+    P, Xs, uvs, thr = scenes.pnp_batch(args.seed, num_images=num_images)
+    n_corr = int(sum(len(x) for x in Xs))
+    native.pnp_ransac_batched(Xs[:64], uvs[:64], thr, 2000)
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        got = native.pnp_ransac_batched(Xs, uvs, thr, 2000)
+        times.append(time.perf_counter() - t0)
+    dt = statistics.median(times)
+    iters = [g[2] for g in got if g is not None]
+    out = {"workload": f"pnp{num_images}: {num_images} images, {n_corr} correspondences (200-2000 per image, "
+                       f"30 % outliers), threshold 8 px at f = 1200, max 2000 iterations",
+           "seconds": dt, "images_per_s": num_images / dt,
+           "registered": int(sum(g is not None for g in got)),
+           "ransac_iterations_mean": float(np.mean(iters)) if iters else 0.0}
+    if with_cpu:
+        import oracle
+
+        t0 = time.perf_counter()
+        done = same = 0
+        while done < num_images and time.perf_counter() - t0 < 10.0:
+            ref = oracle.pnp_ransac(Xs[done], uvs[done], thr, 2000)
+            g = got[done]
+            same += int((ref is None and g is None) or (ref is not None and g is not None and
+                                                        np.array_equal(ref[1], g[1]) and ref[2] == g[2]))
+            done += 1
+        cdt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": done / cdt, "unit": "images/s", "cores": 1, "kind": "port",
+                               "sample": f"the first {done} images registered one after another by the C++ "
+                                         f"restatement of pnp_ransac ({cdt:.1f} s)"}
+        out["same_inliers_and_iterations_as_cpu_on_sample"] = f"{same}/{done}"
+        out["speedup_vs_cpu_core"] = out["images_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -600,6 +645,7 @@ def run_ours(args):
     if not args.skip_side and world == 1:
         line["dense_radial500"] = dense_radial500(args, L, device, stream)
         line["windows512"] = windows512(args, not args.skip_cpu)
+        line["pnp4096"] = pnp_batch_measure(args, not args.skip_cpu)
     print(json.dumps(line), flush=True)
 
 
@@ -614,6 +660,8 @@ def run_side_only(args):
     L = native.load()
     if args.only == "dense_radial500":
         out = dense_radial500(args, L, device, torch.cuda.Stream(device=device))
+    elif args.only == "pnp":
+        out = pnp_batch_measure(args, not args.skip_cpu)
     else:
         out = windows512(args, not args.skip_cpu)
     print(json.dumps(out), flush=True)

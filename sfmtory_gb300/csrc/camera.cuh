@@ -153,13 +153,16 @@ __device__ __forceinline__ T robust_weight(T n, int loss, T scale) {
 // Optional FP64 residual of an observation. The FP32 path computes the
 // pixel residual u - obs from ~1e3 px quantities, which leaves ~1e-4 px of
 // rounding: far above what the gradient near the minimum can tolerate. The
-// kernels that form gradient terms pass the FP64 residual (and sqrt of the
-// robust weight) that the FP64 cost kernel stored for these parameters.
+// kernels that form gradient terms pass the residual and sqrt of the robust
+// weight that the FP64 cost kernel computed for these parameters, stored
+// rounded to FP32 (relative error 6e-8 of a value that is already small,
+// against the ~1e-4 px absolute error of an FP32 projection); they are
+// combined in FP32, which keeps GB300's narrow FP64 pipe out of the passes.
 struct Res64 {
     bool use = false;
     bool ok = false;
-    double r0 = 0.0, r1 = 0.0;  // unweighted residual
-    double s = -1.0;            // sqrt of the robust weight; < 0: from (r0, r1)
+    float r0 = 0.f, r1 = 0.f;  // unweighted residual
+    float s = 1.f;             // sqrt of the robust weight
 };
 
 // Residual and Jacobian of one observation, weighted by sqrt(w).
@@ -194,14 +197,10 @@ __device__ __forceinline__ bool linearize(const ImageLin<T> &im, T X0, T X1, T X
     distort<T>(im.model, im.c, xp, yp, u, v, A, G);
     T s;
     if (rin.use) {
-        const double w = rin.s >= 0.0 ? rin.s * rin.s
-                                      : robust_weight<double>(sqrt(rin.r0 * rin.r0 + rin.r1 * rin.r1), loss,
-                                                              (double)scale);
-        const double sd = rin.s >= 0.0 ? rin.s : sqrt(w);
-        rr[0] = (T)(rin.r0 * sd);
-        rr[1] = (T)(rin.r1 * sd);
-        s = (T)sd;
-        if (weight) *weight = (T)w;
+        s = (T)rin.s;
+        rr[0] = (T)rin.r0 * s;
+        rr[1] = (T)rin.r1 * s;
+        if (weight) *weight = s * s;
     } else {
         rr[0] = u - ox;
         rr[1] = v - oy;
@@ -275,14 +274,9 @@ __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T
     distort<T, M>(im.model, im.c, xp, yp, u, v, A, G);
     T s;
     if (rin.use) {
-        const double sd = rin.s >= 0.0 ? rin.s
-                          : loss == SFMBA_LOSS_NONE
-                              ? 1.0
-                              : sqrt(robust_weight<double>(sqrt(rin.r0 * rin.r0 + rin.r1 * rin.r1), loss,
-                                                           (double)scale));
-        L.r[0] = (T)(rin.r0 * sd);
-        L.r[1] = (T)(rin.r1 * sd);
-        s = (T)sd;
+        s = (T)rin.s;
+        L.r[0] = (T)rin.r0 * s;
+        L.r[1] = (T)rin.r1 * s;
     } else {
         const T r0 = u - ox, r1 = v - oy;
         s = loss == SFMBA_LOSS_NONE ? T(1) : dev_sqrt<T>(robust_weight<T>(dev_sqrt<T>(r0 * r0 + r1 * r1), loss, scale));
