@@ -252,6 +252,45 @@ int sfmba_pnp_ransac_batched(int32_t num, const int64_t *offsets, const double *
                              double *poses_out, uint8_t *inliers_out, int32_t *found_out,
                              int64_t *iterations_out);
 
+/* Statistics of cmd_refine (crates/sfm-cli/src/main.rs:1110-1123). */
+typedef struct sfmba_refine_report {
+    int64_t num_images;
+    int64_t num_cameras;
+    int64_t num_points3d;
+    int64_t num_observations;
+    double initial_cost;
+    double final_cost;
+    int32_t iterations_run;
+    int32_t reserved_i;
+    double mean_error_before_px;  /* Reconstruction::mean_reprojection_error before */
+    double mean_error_after_px;   /* ... and after, with the recomputed point errors */
+    double seconds;
+    double reserved[4];
+} sfmba_refine_report;
+
+/* `sfmtory refine` (crates/sfm-cli/src/main.rs:946-1130) over a COLMAP text
+ * model (cameras.txt, images.txt, points3D.txt; crates/sfm-io/src/colmap.rs)
+ * in dir_in: one global bundle adjustment on the GPU with image 0 (in id
+ * order) anchored, cameras fixed or (refine_intrinsics) free with the
+ * principal point masked, every point's stored error recomputed as its mean
+ * pixel reprojection error, the refined model written to dir_out (may be
+ * dir_in; created if missing). options NULL: the reference's Huber loss and
+ * 200 iterations. Fewer than 2 images, no points, no observation linking a
+ * track to a registered image's keypoint, a malformed file or an image whose
+ * camera is missing are errors (SFMBA_ERR_INVALID_ARGUMENT). */
+int sfmba_colmap_refine(const char *dir_in, const char *dir_out, const sfmba_options *options,
+                        int32_t refine_intrinsics, sfmba_refine_report *report);
+
+/* crates/sfm-io/src/colmap.rs: read the text model in dir_in and write it to
+ * dir_out in the reference's number formats (read_model + write_model). */
+int sfmba_colmap_rewrite(const char *dir_in, const char *dir_out);
+
+/* Reads the text model in dir: counts[5] = cameras, images, points3D, track
+ * elements, keypoints (may be NULL); mean_error =
+ * Reconstruction::mean_reprojection_error (crates/sfm-core/src/model.rs:84-97,
+ * may be NULL). */
+int sfmba_colmap_model_stats(const char *dir, int64_t *counts, double *mean_error);
+
 /* Residual and Jacobian blocks of individual observations, computed on the
  * GPU by the same device code the solver uses (crates/sfm-ba/src/lib.rs:327-590,
  * `analytic_jacobians`). For observation o: r[o][2], j_pose[o][2][6],

@@ -98,6 +98,25 @@ class SfmbaResult(C.Structure):
     ]
 
 
+class SfmbaRefineReport(C.Structure):
+    """sfmba_refine_report (statistics of crates/sfm-cli/src/main.rs cmd_refine)."""
+
+    _fields_ = [
+        ("num_images", C.c_int64),
+        ("num_cameras", C.c_int64),
+        ("num_points3d", C.c_int64),
+        ("num_observations", C.c_int64),
+        ("initial_cost", C.c_double),
+        ("final_cost", C.c_double),
+        ("iterations_run", C.c_int32),
+        ("reserved_i", C.c_int32),
+        ("mean_error_before_px", C.c_double),
+        ("mean_error_after_px", C.c_double),
+        ("seconds", C.c_double),
+        ("reserved", C.c_double * 4),
+    ]
+
+
 def default_options(**overrides) -> SfmbaOptions:
     """Reference BaParams::default() (crates/sfm-ba/src/lib.rs:229-238) plus
     the GB300 solver controls; keyword arguments override fields."""

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsfmba_gb300.so")
 SOURCES = ["k_setup.cu", "k_lin.cu", "k_dense.cu", "k_pcg.cu", "k_matfree.cu", "k_mf_pcg.cu", "k_noalloc.cu", "k_batched.cu",
-           "k_filter.cu", "k_intrinsics.cu", "k_pnp.cu", "solver.cu"]
+           "k_filter.cu", "k_intrinsics.cu", "k_pnp.cu", "colmap_io.cpp", "solver.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-ffp-contract=off"]
@@ -30,7 +30,7 @@ def nvcc() -> str:
 
 
 def _deps():
-    inc = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    inc = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     inc.append(os.path.join(os.path.dirname(HERE), "include", "sfmba.h"))
     return inc
 

@@ -45,6 +45,31 @@ __global__ void k_filter_keep(const int *orig, long long m, unsigned char *keep)
     if (k < m) keep[orig[k]] = 1;
 }
 
+// Per-point mean pixel reprojection error (crates/sfm-cli/src/main.rs:1076-1098):
+// the point's observations are [pt_obs[p], pt_obs[p+1]) of a point-ordered
+// list; those in front of their camera (z > 1e-9) are averaged, in order.
+// n_out[p] = how many were.
+__global__ void k_point_errors(const double *poses, const double *cams, const double *points, const int *cam_of_img,
+                               const int *cam_model, const int *ob_img, const double *ob_xy, const long long *pt_obs,
+                               int nP, double *err_out, int *n_out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nP) return;
+    const double *X = points + 3 * (size_t)p;
+    double total = 0.0;
+    int n = 0;
+    for (long long o = pt_obs[p]; o < pt_obs[p + 1]; ++o) {
+        const int i = ob_img[o], c = cam_of_img[i];
+        double rx, ry;
+        if (residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2], ob_xy[2 * o],
+                       ob_xy[2 * o + 1], rx, ry)) {
+            total += sqrt(rx * rx + ry * ry);
+            ++n;
+        }
+    }
+    err_out[p] = n > 0 ? total / n : 0.0;
+    n_out[p] = n;
+}
+
 __global__ void k_filter_iota(int *v, long long n) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k < n) v[k] = (int)k;
@@ -78,6 +103,15 @@ void launch_filter_select(const FilterBufs &f, long long m, const double *poses,
     SFMBA_CUDA(cub::DeviceSelect::Flagged(f.temp, bytes, f.iota, f.flag, f.sel, f.count, (int)m, s));
     k_filter_gather<<<div_up(m, 256), 256, 0, s>>>(f.sel, f.count, f.img[0], f.pt[0], f.xy[0], f.orig[0], f.img[1],
                                                     f.pt[1], f.xy[1], f.orig[1]);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_point_errors(const double *poses, const double *cams, const double *points, const int *cam_of_img,
+                         const int *cam_model, const int *ob_img, const double *ob_xy, const long long *pt_obs,
+                         int nP, double *err_out, int *n_out, cudaStream_t s) {
+    if (nP == 0) return;
+    k_point_errors<<<div_up(nP, 128), 128, 0, s>>>(poses, cams, points, cam_of_img, cam_model, ob_img, ob_xy, pt_obs,
+                                                   nP, err_out, n_out);
     SFMBA_LAUNCH_CHECK();
 }
 

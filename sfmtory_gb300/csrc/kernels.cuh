@@ -303,6 +303,10 @@ struct FilterBufs {
     size_t temp_bytes = 0;
 };
 size_t filter_temp_bytes(long long nO);
+// Per-point mean reprojection error over a point-ordered observation list.
+void launch_point_errors(const double *poses, const double *cams, const double *points, const int *cam_of_img,
+                         const int *cam_model, const int *ob_img, const double *ob_xy, const long long *pt_obs,
+                         int nP, double *err_out, int *n_out, cudaStream_t s);
 void launch_filter_iota(int *v, long long n, cudaStream_t s);
 // flags of the m current observations under (poses, cams, points); kept ones into set 1, count into *f.count
 void launch_filter_select(const FilterBufs &f, long long m, const double *poses, const double *cams,

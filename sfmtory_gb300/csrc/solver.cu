@@ -23,6 +23,7 @@
 #include <cub/cub.cuh>
 
 #include "camera.cuh"
+#include "colmap_io.h"
 #include "kernels.cuh"
 
 namespace sfmba {
@@ -1787,6 +1788,198 @@ int sfmba_pnp_ransac_batched(int32_t num, const int64_t *offsets, const double *
                                        cudaMemcpyDeviceToHost, s));
         SFMBA_CUDA(cudaStreamSynchronize(s));
         for (int32_t k = 0; k < num; ++k) found_out[k] = found[k];
+    });
+}
+
+int sfmba_colmap_model_stats(const char *dir, int64_t *counts, double *mean_error) {
+    return guarded([&] {
+        if (!dir) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "dir is NULL");
+        const ColmapModel m = colmap_read(dir);
+        if (counts) {
+            long long track = 0, kp = 0;
+            for (const auto &kv : m.points) track += (long long)kv.second.track.size();
+            for (const auto &kv : m.images) kp += (long long)kv.second.keypoints.size();
+            counts[0] = (int64_t)m.cameras.size();
+            counts[1] = (int64_t)m.images.size();
+            counts[2] = (int64_t)m.points.size();
+            counts[3] = track;
+            counts[4] = kp;
+        }
+        if (mean_error) *mean_error = m.mean_reprojection_error();
+    });
+}
+
+int sfmba_colmap_rewrite(const char *dir_in, const char *dir_out) {
+    return guarded([&] {
+        if (!dir_in || !dir_out) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "dir is NULL");
+        colmap_write(colmap_read(dir_in), dir_out);
+    });
+}
+
+int sfmba_colmap_refine(const char *dir_in, const char *dir_out, const sfmba_options *o, int32_t refine_intrinsics,
+                        sfmba_refine_report *rep) {
+    return guarded([&] {
+        const double t0 = now_s();
+        if (!dir_in || !dir_out) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "dir is NULL");
+        sfmba_options opt;
+        if (o) {
+            opt = *o;
+        } else {  // cmd_refine's BaParams (main.rs:1049-1057): Huber, 200 iterations
+            sfmba_default_options(&opt);
+            opt.robust_loss = SFMBA_LOSS_HUBER;
+            opt.max_iterations = 200;
+        }
+        check_options(&opt);
+        ColmapModel m = colmap_read(dir_in);
+        if (m.images.size() < 2)
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT, "need at least 2 registered images in " + std::string(dir_in));
+        if (m.points.empty()) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "no 3D points in " + std::string(dir_in));
+        // Compact indices as cmd_refine (main.rs:969-1035): images in id
+        // order, one camera block per physical camera in first-use order,
+        // points in id order; observations are the track elements whose
+        // image and keypoint exist, point by point (the reference walks a
+        // hash map here, an order without meaning for the result).
+        std::vector<uint32_t> image_ids;
+        std::map<uint32_t, int> image_pos;
+        for (const auto &kv : m.images) {
+            image_pos[kv.first] = (int)image_ids.size();
+            image_ids.push_back(kv.first);
+        }
+        std::vector<uint32_t> camera_id_list;
+        std::map<uint32_t, int> camera_index_of;
+        std::vector<int32_t> cam_of_img, cam_model;
+        std::vector<double> cam_params, poses;
+        for (uint32_t id : image_ids) {
+            const ColmapImage &im = m.images.at(id);
+            auto it = camera_index_of.find(im.camera_id);
+            if (it == camera_index_of.end()) {
+                auto c = m.cameras.find(im.camera_id);
+                if (c == m.cameras.end())
+                    throw Error(SFMBA_ERR_INVALID_ARGUMENT, "image " + std::to_string(id) + " uses unknown camera " +
+                                                                std::to_string(im.camera_id));
+                it = camera_index_of.emplace(im.camera_id, (int)camera_id_list.size()).first;
+                camera_id_list.push_back(im.camera_id);
+                cam_model.push_back(c->second.model);
+                for (double v : c->second.params) cam_params.push_back(v);
+            }
+            cam_of_img.push_back(it->second);
+            for (double v : im.q) poses.push_back(v);
+            for (double v : im.t) poses.push_back(v);
+        }
+        std::vector<uint64_t> point_ids;
+        std::vector<double> points;
+        std::vector<int32_t> ob_img, ob_pt;
+        std::vector<double> ob_xy;
+        std::vector<long long> pt_obs{0};
+        for (const auto &kv : m.points) {
+            const int cp = (int)point_ids.size();
+            point_ids.push_back(kv.first);
+            for (double v : kv.second.xyz) points.push_back(v);
+            for (const auto &te : kv.second.track) {
+                auto ip = image_pos.find(te.first);
+                if (ip == image_pos.end()) continue;
+                const ColmapImage &im = m.images.at(te.first);
+                if (te.second >= im.keypoints.size()) continue;
+                ob_img.push_back(ip->second);
+                ob_pt.push_back(cp);
+                ob_xy.push_back((double)im.keypoints[te.second].first);
+                ob_xy.push_back((double)im.keypoints[te.second].second);
+            }
+            pt_obs.push_back((long long)ob_img.size());
+        }
+        if (ob_img.empty())
+            throw Error(SFMBA_ERR_INVALID_ARGUMENT,
+                        "no observations linking tracked points to registered images; nothing to refine");
+        const int nI = (int)image_ids.size(), nC = (int)camera_id_list.size(), nP = (int)point_ids.size();
+        const long long nO = (long long)ob_img.size();
+        // Image 0 anchored; cameras fixed, or free with the principal point
+        // masked (main.rs:1037-1047).
+        std::vector<uint8_t> fixed_poses(nI, 0), fixed_cams(nC, refine_intrinsics ? 0 : 1), fcp((size_t)nC * 8, 0);
+        fixed_poses[0] = 1;
+        if (refine_intrinsics) {
+            const int st = sfmba_default_fixed_params_mask(nC, cam_model.data(), fcp.data());
+            if (st != SFMBA_OK) throw Error(st, g_last_error);
+        }
+        sfmba_problem q{};
+        q.num_images = nI; q.num_cameras = nC; q.num_points = nP; q.num_observations = nO;
+        q.camera_of_image = cam_of_img.data(); q.camera_model = cam_model.data(); q.camera_params = cam_params.data();
+        q.poses = poses.data(); q.points = points.data();
+        q.obs_image = ob_img.data(); q.obs_point = ob_pt.data(); q.obs_xy = ob_xy.data();
+        q.fixed_poses = fixed_poses.data(); q.fixed_cameras = fixed_cams.data();
+        q.fixed_camera_params = refine_intrinsics ? fcp.data() : nullptr;
+        const double before = m.mean_reprojection_error();
+        std::vector<double> out_poses((size_t)nI * 7), out_points((size_t)nP * 3), out_cams((size_t)nC * 8);
+        sfmba_result r{};
+        r.poses = out_poses.data(); r.points = out_points.data(); r.camera_params = out_cams.data();
+        const int st = sfmba_bundle_adjust(&q, &opt, &r);
+        if (st != SFMBA_OK) throw Error(st, g_last_error);
+        // Write back (main.rs:1062-1074).
+        for (int k = 0; k < nI; ++k) {
+            ColmapImage &im = m.images.at(image_ids[k]);
+            for (int j = 0; j < 4; ++j) im.q[j] = out_poses[(size_t)k * 7 + j];
+            for (int j = 0; j < 3; ++j) im.t[j] = out_poses[(size_t)k * 7 + 4 + j];
+        }
+        for (int k = 0; k < nP; ++k)
+            for (int j = 0; j < 3; ++j) m.points.at(point_ids[k]).xyz[j] = out_points[(size_t)k * 3 + j];
+        if (refine_intrinsics)
+            for (int c = 0; c < nC; ++c)
+                for (int j = 0; j < 8; ++j) m.cameras.at(camera_id_list[c]).params[j] = out_cams[(size_t)c * 8 + j];
+        // Each point's error against the refined model, on the device
+        // (main.rs:1076-1098): the mean over its observations in front of
+        // the camera; a point with none keeps its error.
+        {
+            Context &ctx = context();
+            cudaStream_t s = ctx.stream;
+            Arena &A = ctx.aux;
+            double *d_poses = nullptr, *d_cams = nullptr, *d_points = nullptr, *d_xy = nullptr, *d_err = nullptr;
+            int *d_coi = nullptr, *d_model = nullptr, *d_img = nullptr, *d_n = nullptr;
+            long long *d_pt_obs = nullptr;
+            for (int pass = 0; pass < 2; ++pass) {
+                if (pass == 0) A.begin_sizing(); else A.commit();
+                d_poses = A.take<double>((size_t)nI * 7);
+                d_cams = A.take<double>((size_t)nC * 8);
+                d_points = A.take<double>((size_t)nP * 3);
+                d_xy = A.take<double>((size_t)nO * 2);
+                d_err = A.take<double>(nP);
+                d_coi = A.take<int>(nI);
+                d_model = A.take<int>(nC);
+                d_img = A.take<int>(nO);
+                d_n = A.take<int>(nP);
+                d_pt_obs = A.take<long long>((size_t)nP + 1);
+            }
+            const std::vector<double> &cams_now = refine_intrinsics ? out_cams : cam_params;
+            put(d_poses, out_poses.data(), out_poses.size(), false, s);
+            put(d_cams, cams_now.data(), cams_now.size(), false, s);
+            put(d_points, out_points.data(), out_points.size(), false, s);
+            put(d_xy, ob_xy.data(), ob_xy.size(), false, s);
+            put_vec(d_coi, cam_of_img, s);
+            put_vec(d_model, cam_model, s);
+            put_vec(d_img, ob_img, s);
+            put_vec(d_pt_obs, pt_obs, s);
+            launch_point_errors(d_poses, d_cams, d_points, d_coi, d_model, d_img, d_xy, d_pt_obs, nP, d_err, d_n, s);
+            std::vector<double> err(nP);
+            std::vector<int> cnt(nP);
+            SFMBA_CUDA(cudaMemcpyAsync(err.data(), d_err, sizeof(double) * nP, cudaMemcpyDeviceToHost, s));
+            SFMBA_CUDA(cudaMemcpyAsync(cnt.data(), d_n, sizeof(int) * nP, cudaMemcpyDeviceToHost, s));
+            SFMBA_CUDA(cudaStreamSynchronize(s));
+            for (int k = 0; k < nP; ++k)
+                if (cnt[k] > 0) m.points.at(point_ids[k]).error = err[k];
+        }
+        const double after = m.mean_reprojection_error();
+        colmap_write(m, dir_out);
+        if (rep) {
+            *rep = sfmba_refine_report{};
+            rep->num_images = nI;
+            rep->num_cameras = nC;
+            rep->num_points3d = nP;
+            rep->num_observations = nO;
+            rep->initial_cost = r.initial_cost;
+            rep->final_cost = r.final_cost;
+            rep->iterations_run = r.iterations_run;
+            rep->mean_error_before_px = before;
+            rep->mean_error_after_px = after;
+            rep->seconds = now_s() - t0;
+        }
     });
 }
 

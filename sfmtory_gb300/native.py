@@ -41,6 +41,9 @@ EXPORTED_SYMBOLS = (
     "sfmba_adjust_global",
     "sfmba_refine_pose_gauss_newton_batched",
     "sfmba_pnp_ransac_batched",
+    "sfmba_colmap_refine",
+    "sfmba_colmap_rewrite",
+    "sfmba_colmap_model_stats",
     "sfmba_residuals_jacobians",
     "sfmba_total_cost_noalloc",
     "sfmba_profile_enable",
@@ -83,6 +86,9 @@ def load(path: str | None = None):
         L.sfmba_adjust_global.argtypes = [vp, vp, C.c_int32, C.c_double, vp, vp, vp, vp]
         L.sfmba_refine_pose_gauss_newton_batched.argtypes = [C.c_int32, vp, vp, vp, C.c_int32, vp]
         L.sfmba_pnp_ransac_batched.argtypes = [C.c_int32, vp, vp, vp, C.c_double, C.c_int32, vp, vp, vp, vp]
+        L.sfmba_colmap_refine.argtypes = [C.c_char_p, C.c_char_p, vp, C.c_int32, vp]
+        L.sfmba_colmap_rewrite.argtypes = [C.c_char_p, C.c_char_p]
+        L.sfmba_colmap_model_stats.argtypes = [C.c_char_p, vp, vp]
         L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
         L.sfmba_total_cost_noalloc.argtypes = [vp, vp, vp, vp]
         L.sfmba_profile_enable.argtypes = [C.c_int32]
@@ -280,6 +286,44 @@ def pnp_ransac_batched(points3d_list, points2d_list, threshold: float, max_itera
             out.append(None)
         else:
             out.append((poses[k].copy(), mask[off[k]:off[k + 1]].astype(bool), int(iters[k])))
+    return out
+
+
+def colmap_refine(dir_in: str, dir_out: str | None = None, refine_intrinsics: bool = False,
+                  opts: SfmbaOptions | None = None, **kw) -> dict:
+    """`sfmtory refine` (crates/sfm-cli/src/main.rs:946-1130) on the COLMAP
+    text model in ``dir_in``, written to ``dir_out`` (default: in place).
+    Without options the reference's Huber loss and 200 iterations; keyword
+    arguments override option fields. Returns the report as a dict."""
+    from .abi import SfmbaRefineReport
+
+    L = load()
+    o = opts
+    if o is None and kw:
+        base = dict(robust_loss=1, max_iterations=200)
+        base.update(kw)
+        o = default_options(**base)
+    rep = SfmbaRefineReport()
+    _check(L.sfmba_colmap_refine(os.fsencode(dir_in), os.fsencode(dir_out or dir_in),
+                                 C.byref(o) if o is not None else None, 1 if refine_intrinsics else 0,
+                                 C.byref(rep)))
+    return {f: getattr(rep, f) for f, _ in SfmbaRefineReport._fields_ if not f.startswith("reserved")}
+
+
+def colmap_rewrite(dir_in: str, dir_out: str) -> None:
+    """crates/sfm-io/src/colmap.rs read_model then write_model."""
+    _check(load().sfmba_colmap_rewrite(os.fsencode(dir_in), os.fsencode(dir_out)))
+
+
+def colmap_model_stats(dir: str) -> dict:
+    """Counts of the text model in ``dir`` and its
+    Reconstruction::mean_reprojection_error."""
+    counts = np.zeros(5, np.int64)
+    err = C.c_double(0.0)
+    _check(load().sfmba_colmap_model_stats(os.fsencode(dir), counts.ctypes.data, C.byref(err)))
+    keys = ("cameras", "images", "points3d", "track_elements", "keypoints")
+    out = {k: int(v) for k, v in zip(keys, counts)}
+    out["mean_reprojection_error"] = err.value
     return out
 
 
