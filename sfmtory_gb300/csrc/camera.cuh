@@ -298,7 +298,9 @@ __device__ __forceinline__ bool linearize_compact(const ImageLin<T> &im, T X0, T
 
 // Pixel of normalised coordinates (xn, yn) under `model` in FP64
 // (crates/sfm-core/src/camera.rs:204-244).
+template <int M = -1>
 __device__ __forceinline__ void project64(int model, const double *c, double xn, double yn, double &u, double &v) {
+    if constexpr (M >= 0) model = M;
     switch (model) {
     case SFMBA_SIMPLE_PINHOLE: u = c[0] * xn + c[1]; v = c[0] * yn + c[2]; break;
     case SFMBA_PINHOLE: u = c[0] * xn + c[2]; v = c[1] * yn + c[3]; break;
@@ -347,6 +349,26 @@ __device__ __forceinline__ bool residual64(const double *pose7, int model, const
     const double iz = 1.0 / pc2;
     double u, v;
     project64(model, c, pc0 * iz, pc1 * iz, u, v);
+    rx = u - ox;
+    ry = v - oy;
+    return true;
+}
+
+// The same residual from the pose's FP64 rotation matrix and translation
+// (rt = R row-major, then t): R X + t in 9 multiply-adds instead of the
+// quaternion form's ~30 operations on GB300's narrow FP64 pipe. R is the
+// quaternion's exact rotation up to rounding, so the two forms agree to
+// ~1e-16 relative per coordinate.
+template <int M = -1>
+__device__ __forceinline__ bool residual64_rt(const double *rt, int model, const double *c, double X0, double X1,
+                                              double X2, double ox, double oy, double &rx, double &ry) {
+    const double pc0 = rt[0] * X0 + rt[1] * X1 + rt[2] * X2 + rt[9];
+    const double pc1 = rt[3] * X0 + rt[4] * X1 + rt[5] * X2 + rt[10];
+    const double pc2 = rt[6] * X0 + rt[7] * X1 + rt[8] * X2 + rt[11];
+    if (!(pc2 > kMinDepth)) return false;
+    const double iz = 1.0 / pc2;
+    double u, v;
+    project64<M>(model, c, pc0 * iz, pc1 * iz, u, v);
     rx = u - ox;
     ry = v - oy;
     return true;

@@ -528,7 +528,7 @@ __global__ void k_wb_axpy(const int *slot_win, int n, const double *c, double *x
 // order. trial = 0 -> cost, valid_obs; 1 -> trial_cost, trial_valid_obs of
 // the windows whose step was solved.
 __global__ void __launch_bounds__(256) k_wb_cost_partials(
-    const double *poses, const double *cams, const double *points, const int *cam_of_img, const int *cam_model,
+    const double *rt, const double *cams, const double *points, const int *cam_of_img, const int *cam_model,
     const int *ob_img, const int *ob_pt, const double2 *ob_xy, const int *cblk_win, const long long *cblk_lo,
     int loss, double scale, int trial, const WinState *ws, double *cpart, long long *cpart_n, float4 *rs_out) {
     __shared__ double ssum[256];
@@ -544,8 +544,8 @@ __global__ void __launch_bounds__(256) k_wb_cost_partials(
         const double *X = points + 3 * (size_t)p;
         const double2 xy = ob_xy[o];
         double rx, ry;
-        const bool ok = residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2],
-                                   xy.x, xy.y, rx, ry);
+        const bool ok = residual64_rt(rt + 12 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2],
+                                      xy.x, xy.y, rx, ry);
         double w = 1.0;
         if (ok) {
             const double n2 = rx * rx + ry * ry;
@@ -994,8 +994,9 @@ void launch_wb_scatter(const Bufs &b, const WinBufs &w, cudaStream_t s) {
 
 void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s) {
     if (w.ncblk > 0) {
+        launch_pose_rt64(trial ? b.poses_trial : b.poses, b.nI, b.img_rt64, s);
         k_wb_cost_partials<<<w.ncblk, 256, 0, s>>>(
-            trial ? b.poses_trial : b.poses, trial ? b.cams_trial : b.cams, trial ? b.points_trial : b.points,
+            b.img_rt64, trial ? b.cams_trial : b.cams, trial ? b.points_trial : b.points,
             b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt, b.ob_xy, w.cblk_win, w.cblk_lo, b.loss, b.loss_scale,
             trial ? 1 : 0, w.ws, w.cpart, w.cpart_n,
             (b.mixed && b.ob_rs) ? (trial ? b.ob_rs_trial : b.ob_rs) : nullptr);

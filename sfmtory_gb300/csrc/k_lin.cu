@@ -320,7 +320,27 @@ __global__ void k_update_images(const double *poses, const double *cams, const i
 // FP64 cost over all observations with a fixed grid so the summation order
 // is the same on every call. mode 0: sum w |r|^2 (lib.rs:727-745);
 // mode 1: sum |r| (lib.rs:708-725); mode 2: sum |r|^2.
-__global__ void __launch_bounds__(256) k_cost(const double *poses, const double *cams,
+// Per-image FP64 rotation matrix and translation of the poses the cost
+// evaluates ([nI][12]).
+__global__ void k_pose_rt64(const double *poses, int nI, double *rt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI) return;
+    const double *q = poses + 7 * (size_t)i;
+    double R[9];
+    quat_to_R(q, R);
+    double *o = rt + 12 * (size_t)i;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) o[k] = R[k];
+    o[9] = q[4];
+    o[10] = q[5];
+    o[11] = q[6];
+}
+
+// Robust cost / mean error of all observations in FP64 (lib.rs:708-745),
+// block partial sums in a fixed order. M: the camera model when every camera
+// has it (-1: the runtime switch).
+template <int M>
+__global__ void __launch_bounds__(256) k_cost(const double *rt, const double *cams,
                                               const double *points, const int *cam_of_img,
                                               const int *cam_model, const int *ob_img,
                                               const int *ob_pt, const double2 *ob_xy, long long nO,
@@ -335,8 +355,8 @@ __global__ void __launch_bounds__(256) k_cost(const double *poses, const double 
         const double *X = points + 3 * (size_t)p;
         const double2 xy = ob_xy[o];
         double rx, ry;
-        const bool ok = residual64(poses + 7 * (size_t)i, cam_model[c], cams + 8 * (size_t)c, X[0], X[1], X[2],
-                                   xy.x, xy.y, rx, ry);
+        const bool ok = residual64_rt<M>(rt + 12 * (size_t)i, M >= 0 ? M : cam_model[c], cams + 8 * (size_t)c, X[0],
+                                         X[1], X[2], xy.x, xy.y, rx, ry);
         if (rs_out) {  // FP64 residual and sqrt(weight) for the next linearisation's gradient terms
             double sw = 1.0;
             if (ok && loss != SFMBA_LOSS_NONE) sw = sqrt(robust_weight<double>(sqrt(rx * rx + ry * ry), loss, scale));
@@ -629,12 +649,29 @@ void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t 
     }
 }
 
+void launch_pose_rt64(const double *poses, int nI, double *rt, cudaStream_t s) {
+    if (nI == 0) return;
+    k_pose_rt64<<<div_up(nI, 128), 128, 0, s>>>(poses, nI, rt);
+    SFMBA_LAUNCH_CHECK();
+}
+
 static void cost_impl(const Bufs &b, bool trial, int mode, double *out, long long *out_count,
                       cudaStream_t s, float4 *rs_out = nullptr) {
-    k_cost<<<kCostBlocks, 256, 0, s>>>(trial ? b.poses_trial : b.poses, trial ? b.cams_trial : b.cams,
-                                       trial ? b.points_trial : b.points, b.cam_of_img, b.cam_model,
-                                       b.ob_img, b.ob_pt, b.ob_xy, b.nO, b.loss, b.loss_scale, mode,
-                                       b.partials, b.count_partials, rs_out);
+    launch_pose_rt64(trial ? b.poses_trial : b.poses, b.nI, b.img_rt64, s);
+    auto run = [&](auto mc) {
+        k_cost<decltype(mc)::value><<<kCostBlocks, 256, 0, s>>>(
+            b.img_rt64, trial ? b.cams_trial : b.cams, trial ? b.points_trial : b.points, b.cam_of_img, b.cam_model,
+            b.ob_img, b.ob_pt, b.ob_xy, b.nO, b.loss, b.loss_scale, mode, b.partials, b.count_partials, rs_out);
+    };
+    switch (b.uniform_model) {
+    case SFMBA_SIMPLE_PINHOLE: run(std::integral_constant<int, SFMBA_SIMPLE_PINHOLE>()); break;
+    case SFMBA_PINHOLE: run(std::integral_constant<int, SFMBA_PINHOLE>()); break;
+    case SFMBA_SIMPLE_RADIAL: run(std::integral_constant<int, SFMBA_SIMPLE_RADIAL>()); break;
+    case SFMBA_RADIAL: run(std::integral_constant<int, SFMBA_RADIAL>()); break;
+    case SFMBA_OPENCV: run(std::integral_constant<int, SFMBA_OPENCV>()); break;
+    case SFMBA_OPENCV_FISHEYE: run(std::integral_constant<int, SFMBA_OPENCV_FISHEYE>()); break;
+    default: run(std::integral_constant<int, -1>()); break;
+    }
     SFMBA_LAUNCH_CHECK();
     k_cost_finalize<<<1, 256, 0, s>>>(b.partials, b.count_partials, kCostBlocks, out, out_count);
     SFMBA_LAUNCH_CHECK();

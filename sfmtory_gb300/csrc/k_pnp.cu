@@ -17,6 +17,7 @@
 // local refit (DLT over all inliers, a 2m x 12 Jacobi SVD with CTA-wide
 // column dot products), the never-regress checks and the two Gauss-Newton
 // polish rounds (pnp.rs:236-306) run with one CTA per image. All FP64.
+#include <climits>
 #include <cstdint>
 
 #include "kernels.cuh"
@@ -373,8 +374,12 @@ __global__ void k_pnp_select(const long long *off, int P, int B, long long round
             }
         }
     }
-    if (!S.done && S.iter >= min(max_it, max(S.needed, 1LL))) S.done = 1;
-    if (!S.done) atomicAdd(active, 1);
+    const long long limit = min(max_it, max(S.needed, 1LL));
+    if (!S.done && S.iter >= limit) S.done = 1;
+    if (!S.done) {
+        atomicAdd(active, 1);
+        atomicMax(active + 1, (int)min(limit - S.iter, (long long)INT_MAX));  // iterations still to run
+    }
 }
 
 // FP64 block sum (kPnpThreads threads) of NV values per thread into out (all threads).
@@ -718,7 +723,7 @@ void launch_pnp_round(const PnpBufs &q, long long round_base, cudaStream_t s) {
     k_pnp_score<<<div_up(total * 32, 256), 256, 0, s>>>(q.off, q.X, q.uv, q.P, q.B, q.thr, q.models, q.valid,
                                                         q.counts);
     SFMBA_LAUNCH_CHECK();
-    SFMBA_CUDA(cudaMemsetAsync(q.active, 0, sizeof(int), s));
+    SFMBA_CUDA(cudaMemsetAsync(q.active, 0, 2 * sizeof(int), s));
     k_pnp_select<<<div_up(q.P, 128), 128, 0, s>>>(q.off, q.P, q.B, round_base, q.max_it, q.models, q.valid,
                                                   q.counts, (PnpState *)q.state, q.active);
     SFMBA_LAUNCH_CHECK();

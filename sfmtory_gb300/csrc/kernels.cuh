@@ -73,6 +73,7 @@ struct Bufs {
     // LM bookkeeping
     LMState *state = nullptr;
     double *partials = nullptr;   // [kCostBlocks*2]
+    double *img_rt64 = nullptr;   // [nI][12] FP64 R (row-major) and t of the poses the cost evaluates
     long long *count_partials = nullptr;
     // PCG (matrix-free) vectors, [nI*D] each, element type T
     void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
@@ -202,6 +203,8 @@ void launch_backsub_update(const Bufs &b, const double *delta_slot, cudaStream_t
 void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t s);
 // cost of (poses, cams, points) or of the trial buffers, into state->cost/trial_cost
 void launch_cost(const Bufs &b, bool trial, bool into_trial, cudaStream_t s);
+// FP64 rotation matrix and translation of every pose ([nI][12]) for the cost.
+void launch_pose_rt64(const double *poses, int nI, double *rt, cudaStream_t s);
 void launch_mean_error(const Bufs &b, cudaStream_t s);  // -> partials; host finalises
 void launch_accept(const Bufs &b, cudaStream_t s);
 void launch_commit(const Bufs &b, cudaStream_t s);
@@ -273,7 +276,7 @@ struct PnpBufs {
     double *models = nullptr;                 // [P * B][8]
     unsigned char *valid = nullptr;           // [P * B]
     long long *counts = nullptr;              // [P * B]
-    int *active = nullptr;                    // images whose loop goes on
+    int *active = nullptr;                    // [2]: images whose loop goes on, most iterations left
     double *dlt_scratch = nullptr;            // [N][24] DLT rows of the local refit
     long long *slot_scratch = nullptr;        // [N]
     unsigned char *mask = nullptr, *mask_trial = nullptr;  // [N]

@@ -756,6 +756,7 @@ class Solver {
             b.slot_masked = A.take<unsigned char>(n);
             b.state = A.take<LMState>(1);
             b.partials = A.take<double>(kCostBlocks);
+            b.img_rt64 = A.take<double>((size_t)nI * 12 + 1);
             b.count_partials = A.take<long long>(kCostBlocks);
             d_bad = A.take<int>(1);
             if (!device) {
@@ -1725,7 +1726,12 @@ int sfmba_pnp_ransac_batched(int32_t num, const int64_t *offsets, const double *
         PnpBufs q;
         q.P = num;
         q.max_it = max_iterations;
-        q.B = (int)std::max<long long>(1, std::min<long long>(128, max_iterations));
+        // Hypotheses per image per round: at most kMaxRound; the first round
+        // takes 64 (the pipeline's usual inlier ratios end the loop within
+        // ~60 iterations), later rounds what the longest remaining loop needs.
+        constexpr int kMaxRound = 128;
+        const int b_cap = (int)std::max<long long>(1, std::min<long long>(kMaxRound, max_iterations));
+        q.B = b_cap;
         q.thr = threshold;
         long long *off = nullptr, *iters = nullptr;
         double *X = nullptr, *uv = nullptr;
@@ -1740,7 +1746,7 @@ int sfmba_pnp_ransac_batched(int32_t num, const int64_t *offsets, const double *
             q.models = A.take<double>((size_t)num * q.B * 8);
             q.valid = A.take<unsigned char>((size_t)num * q.B);
             q.counts = A.take<long long>((size_t)num * q.B);
-            q.active = A.take<int>(1);
+            q.active = A.take<int>(2);
             q.dlt_scratch = A.take<double>((size_t)N * 24 + 1);
             q.slot_scratch = A.take<long long>((size_t)N + 1);
             q.mask = A.take<unsigned char>((size_t)N + 1);
@@ -1769,12 +1775,16 @@ int sfmba_pnp_ransac_batched(int32_t num, const int64_t *offsets, const double *
         }
         if (!stream.empty()) put_vec(raw, stream, s);
         launch_pnp_init(q, s);
-        for (long long base = 0; base < max_iterations; base += q.B) {
+        int round = std::min(b_cap, 64);
+        for (long long base = 0; base < max_iterations;) {
+            q.B = round;
             launch_pnp_round(q, base, s);
-            int active = 0;
-            SFMBA_CUDA(cudaMemcpyAsync(&active, q.active, sizeof(int), cudaMemcpyDeviceToHost, s));
+            base += round;
+            int act[2] = {0, 0};
+            SFMBA_CUDA(cudaMemcpyAsync(act, q.active, sizeof(act), cudaMemcpyDeviceToHost, s));
             SFMBA_CUDA(cudaStreamSynchronize(s));
-            if (active == 0) break;
+            if (act[0] == 0) break;
+            round = std::min(b_cap, std::max(8, (act[1] + 7) / 8 * 8));
         }
         launch_pnp_finish(q, s);
         launch_pnp_iterations(q, iters, s);
