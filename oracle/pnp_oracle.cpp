@@ -126,9 +126,37 @@ void jacobi_svd(std::vector<double> &a, int m, int n, std::vector<double> &v, st
     }
 }
 
+// Householder QR of the column-major m x n matrix a (m > n), returning the
+// n x n upper-triangular R column-major: column k is reflected by
+// v = x - alpha e1 with alpha = -sign(x0) |x| (x0 = 0 counts as positive).
+// A and R have the same right singular vectors.
+void householder_r(std::vector<double> &a, int m, int n, std::vector<double> &r) {
+    r.assign((size_t)n * n, 0.0);
+    for (int k = 0; k < n; ++k) {
+        double *x = &a[(size_t)k * m];
+        double s = 0.0;
+        for (int i = k; i < m; ++i) s += x[i] * x[i];
+        const double nrm = std::sqrt(s), x0 = x[k];
+        const double alpha = x0 >= 0.0 ? -nrm : nrm;
+        const double v0 = x0 - alpha;
+        const double beta = s - x0 * x0 + v0 * v0;  // v.v
+        x[k] = v0;
+        if (beta > 0.0)
+            for (int j = k + 1; j < n; ++j) {
+                double *y = &a[(size_t)j * m];
+                double d = 0.0;
+                for (int i = k; i < m; ++i) d += x[i] * y[i];
+                const double f = 2.0 * d / beta;
+                for (int i = k; i < m; ++i) y[i] -= f * x[i];
+            }
+        r[(size_t)k * n + k] = beta > 0.0 ? alpha : x0;
+        for (int j = k + 1; j < n; ++j) r[(size_t)j * n + k] = a[(size_t)j * m + k];
+    }
+}
+
 // linalg.rs:11-20 (null_space_vector): the right singular vector of the
 // smallest singular value (first one on ties). Rows of the 2n x 12 system
-// of pnp.rs:28-47.
+// of pnp.rs:28-47; a taller system is first reduced to its 12 x 12 R factor.
 bool dlt_null_vector(const double *X, const double *uv, const long *idx, long n, double out[12]) {
     const int m = (int)(2 * n);
     std::vector<double> a((size_t)m * 12, 0.0), v, sv;
@@ -142,7 +170,13 @@ bool dlt_null_vector(const double *X, const double *uv, const long *idx, long n,
         A(r1, 4) = x; A(r1, 5) = y; A(r1, 6) = z; A(r1, 7) = 1.0;
         A(r1, 8) = -w * x; A(r1, 9) = -w * y; A(r1, 10) = -w * z; A(r1, 11) = -w;
     }
-    jacobi_svd(a, m, 12, v, sv);
+    if (m > 12) {
+        std::vector<double> r;
+        householder_r(a, m, 12, r);
+        jacobi_svd(r, 12, 12, v, sv);
+    } else {
+        jacobi_svd(a, m, 12, v, sv);
+    }
     int best = 0;
     for (int j = 1; j < 12; ++j)
         if (sv[j] < sv[best]) best = j;

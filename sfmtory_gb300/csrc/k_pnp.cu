@@ -541,10 +541,12 @@ __device__ long long cta_inliers(const double *X, const double *uv, long long n,
 }
 
 // DLT over the correspondences with inl[i] != 0 (m of them, m >= 6) by one
-// CTA: the 2m x 12 system in scratch a (column-major), one-sided Jacobi
-// with CTA-wide column dot products, the same cyclic order and threshold
-// as the serial solver. Pose in sh.pose; returns false where pnp_dlt
-// returns None.
+// CTA: the 2m x 12 system in scratch a (column-major), reduced to its 12 x 12
+// R factor by Householder reflections (column norms and the 11 column dot
+// products of each step reduced over the CTA), then thread 0 takes the
+// one-sided Jacobi SVD of R (A and R share their right singular vectors) —
+// the same steps as the oracle's restatement. Pose in sh.pose; false where
+// pnp_dlt returns None.
 __device__ bool cta_dlt(const double *X, const double *uv, const unsigned char *inl, long long n, long long m,
                         double *a, CtaShared &sh, long long *slot) {
     const long long M = 2 * m;
@@ -556,56 +558,59 @@ __device__ bool cta_dlt(const double *X, const double *uv, const unsigned char *
     __syncthreads();
     for (long long i = threadIdx.x; i < n; i += blockDim.x)
         if (slot[i] >= 0) dlt_rows(X + 3 * i, uv + 2 * i, a, (int)M, (int)(2 * slot[i]));
-    for (int q = threadIdx.x; q < 144; q += blockDim.x) sh.V[q] = (q % 13 == 0) ? 1.0 : 0.0;
     __syncthreads();
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        if (threadIdx.x == 0) sh.flag = 0;
+    // sh.V holds R (column-major 12 x 12) as it is produced; a 12 x 12
+    // system (6 inliers) is its own R, as in the oracle.
+    for (int q = threadIdx.x; q < 144; q += blockDim.x) sh.V[q] = M > 12 ? 0.0 : a[q];
+    __syncthreads();
+    for (int k = 0; k < 12 && M > 12; ++k) {
+        double *x = a + k * M;
+        double g[1] = {0.0};
+        for (long long r = k + threadIdx.x; r < M; r += blockDim.x) g[0] += x[r] * x[r];
+        cta_sum<1>(g, sh.red, sh.gram);
+        const double s = sh.gram[0], x0 = x[k];
+        const double nrm = sqrt(s);
+        const double alpha = x0 >= 0.0 ? -nrm : nrm;
+        const double v0 = x0 - alpha;
+        const double beta = s - x0 * x0 + v0 * v0;
+        __syncthreads();  // every thread has read x[k]
+        if (threadIdx.x == 0) {
+            x[k] = v0;
+            sh.V[k * 12 + k] = beta > 0.0 ? alpha : x0;
+        }
         __syncthreads();
-        for (int p = 0; p < 11; ++p)
-            for (int q = p + 1; q < 12; ++q) {
-                double g[3] = {0.0, 0.0, 0.0};
-                const double *ap = a + p * M, *aq = a + q * M;
-                for (long long r = threadIdx.x; r < M; r += blockDim.x) {
-                    g[0] += ap[r] * ap[r];
-                    g[1] += aq[r] * aq[r];
-                    g[2] += ap[r] * aq[r];
-                }
-                cta_sum<3>(g, sh.red, sh.gram);
-                double c, s;
-                if (!jacobi_cs(sh.gram[0], sh.gram[1], sh.gram[2], c, s)) continue;
-                if (threadIdx.x == 0) sh.flag = 1;
-                double *wp = a + p * M, *wq = a + q * M;
-                for (long long r = threadIdx.x; r < M; r += blockDim.x) {
-                    const double x = wp[r], y = wq[r];
-                    wp[r] = c * x - s * y;
-                    wq[r] = s * x + c * y;
-                }
-                if (threadIdx.x < 12) {
-                    const double x = sh.V[p * 12 + threadIdx.x], y = sh.V[q * 12 + threadIdx.x];
-                    sh.V[p * 12 + threadIdx.x] = c * x - s * y;
-                    sh.V[q * 12 + threadIdx.x] = s * x + c * y;
-                }
-                __syncthreads();
+        if (beta > 0.0 && k < 11) {
+            double d[11];
+#pragma unroll
+            for (int j = 0; j < 11; ++j) d[j] = 0.0;
+            for (long long r = k + threadIdx.x; r < M; r += blockDim.x) {
+                const double vr = x[r];
+#pragma unroll
+                for (int j = 0; j < 11; ++j)
+                    if (k + 1 + j < 12) d[j] += vr * a[(k + 1 + j) * M + r];
             }
+            cta_sum<11>(d, sh.red, sh.sums);
+            for (long long r = k + threadIdx.x; r < M; r += blockDim.x) {
+                const double vr = x[r];
+#pragma unroll
+                for (int j = 0; j < 11; ++j)
+                    if (k + 1 + j < 12) a[(k + 1 + j) * M + r] -= (2.0 * sh.sums[j] / beta) * vr;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0)
+            for (int j = k + 1; j < 12; ++j) sh.V[j * 12 + k] = a[j * M + k];
         __syncthreads();
-        const int rotated = sh.flag;
-        __syncthreads();
-        if (!rotated) break;
     }
-    // Column norms, smallest first found.
-    double nv[12];
-    for (int j = 0; j < 12; ++j) {
-        double g[3] = {0.0, 0.0, 0.0};
-        for (long long r = threadIdx.x; r < M; r += blockDim.x) g[0] += a[j * M + r] * a[j * M + r];
-        cta_sum<3>(g, sh.red, sh.gram);
-        nv[j] = sqrt(sh.gram[0]);
-    }
-    int best = 0;
-    for (int j = 1; j < 12; ++j)
-        if (nv[j] < nv[best]) best = j;
     if (threadIdx.x == 0) {
+        double R[144], V[144], sv[12];
+        for (int q = 0; q < 144; ++q) R[q] = sh.V[q];
+        jacobi_svd_serial<12, 12>(R, V, sv);
+        int best = 0;
+        for (int j = 1; j < 12; ++j)
+            if (sv[j] < sv[best]) best = j;
         double p[12];
-        for (int c = 0; c < 12; ++c) p[c] = sh.V[best * 12 + c];
+        for (int c = 0; c < 12; ++c) p[c] = V[best * 12 + c];
         PPose out;
         sh.flag = pose_from_projection(p, out);
         if (sh.flag) sh.pose = out;

@@ -231,9 +231,11 @@ void launch_mf_point_reduce(const Bufs &b, cudaStream_t s);     // C_p, g_p, fre
 void launch_mf_image_blocks(const Bufs &b, cudaStream_t s);     // H_i, b_i
 void launch_image_blocks_records(const Bufs &b, cudaStream_t s);  // H_i, b_i from stored records
 void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PCG start vectors
-// The two PCG passes in launch variant 0..kPassVariants-1 (same results;
-// chosen by the autotuner).
-constexpr int kPassVariants = 4;
+// The two PCG passes in launch variant 0..k{Point,Image}PassVariants-1
+// (same results; chosen by the autotuner).
+constexpr int kPointPassVariants = 4;
+constexpr int kImagePassVariants = 4;
+constexpr int kPassVariants = kPointPassVariants;  // the larger of the two
 void launch_mf_points(const Bufs &b, cudaStream_t s, int variant);  // u = C^-1 E^T p
 void launch_mf_images(const Bufs &b, cudaStream_t s, int variant);  // partials of E u
 void launch_mf_backsub(const Bufs &b, const double *delta_slot, cudaStream_t s);

@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -61,6 +62,10 @@ struct Profiler {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     double ms[PH_COUNT] = {0};
     long long launches[PH_COUNT] = {0};
+    std::map<std::string, double> host_ms;  // wall time of host stages (ms)
+    void host(const char *name, double seconds) {
+        if (on) host_ms[name] += seconds * 1e3;
+    }
     cudaEvent_t take() {
         if (used == pool.size()) {
             cudaEvent_t e;
@@ -85,6 +90,7 @@ struct Profiler {
     void reset() {
         resolve();
         for (int k = 0; k < PH_COUNT; ++k) { ms[k] = 0; launches[k] = 0; }
+        host_ms.clear();
     }
 };
 
@@ -213,13 +219,14 @@ class Arena {
 // sums in the same order, so the choice never changes results.
 struct TuneEntry {
     int variant = 0;
+    int count = 0;  // variants timed
     float us[kPassVariants] = {0};
 };
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int>, TuneEntry> g_tune;  // (device, pass, D, size bucket)
 
 template <typename Launch>
-int tuned_variant(int device, int pass, const Bufs &b, cudaStream_t s, Launch launch) {
+int tuned_variant(int device, int pass, int count, const Bufs &b, cudaStream_t s, Launch launch) {
     int bucket = 0;
     for (long long n = std::max<long long>(b.nO, 1); n > 1; n >>= 1) ++bucket;
     const auto key = std::make_tuple(device, pass, b.D, bucket);
@@ -227,11 +234,12 @@ int tuned_variant(int device, int pass, const Bufs &b, cudaStream_t s, Launch la
     auto it = g_tune.find(key);
     if (it != g_tune.end()) return it->second.variant;
     TuneEntry e;
+    e.count = count;
     cudaEvent_t a, z;
     SFMBA_CUDA(cudaEventCreate(&a));
     SFMBA_CUDA(cudaEventCreate(&z));
     float best = 0.f;
-    for (int v = 0; v < kPassVariants; ++v) {
+    for (int v = 0; v < count; ++v) {
         launch(v);  // warm-up
         SFMBA_CUDA(cudaEventRecord(a, s));
         for (int r = 0; r < 3; ++r) launch(v);
@@ -258,12 +266,15 @@ std::string tune_report() {
     for (const auto &kv : g_tune) {
         char tmp[256];
         const TuneEntry &e = kv.second;
-        std::snprintf(tmp, sizeof(tmp),
-                      "%s{\"device\":%d,\"pass\":\"%s\",\"D\":%d,\"log2_obs\":%d,\"variant\":%d,"
-                      "\"us\":[%.2f,%.2f,%.2f,%.2f]}",
+        std::snprintf(tmp, sizeof(tmp), "%s{\"device\":%d,\"pass\":\"%s\",\"D\":%d,\"log2_obs\":%d,\"variant\":%d,\"us\":[",
                       first ? "" : ",", std::get<0>(kv.first), std::get<1>(kv.first) == 0 ? "points" : "images",
-                      std::get<2>(kv.first), std::get<3>(kv.first), e.variant, e.us[0], e.us[1], e.us[2], e.us[3]);
+                      std::get<2>(kv.first), std::get<3>(kv.first), e.variant);
         js += tmp;
+        for (int v = 0; v < e.count; ++v) {
+            std::snprintf(tmp, sizeof(tmp), "%s%.2f", v ? "," : "", e.us[v]);
+            js += tmp;
+        }
+        js += "]}";
         first = false;
     }
     return js + "]";
@@ -406,6 +417,30 @@ struct Batch {
     const sfmba_problem &window(int w) const { return windows[w]; }
 };
 
+// Runs f(k) for k in [0, n) on up to 16 host threads, in contiguous ranges.
+template <typename F>
+void parallel_for(int n, F &&f) {
+    const int threads = std::max(1, std::min<int>({16, (int)std::thread::hardware_concurrency(), n}));
+    if (threads <= 1) {
+        for (int k = 0; k < n; ++k) f(k);
+        return;
+    }
+    std::vector<std::thread> pool;
+    std::exception_ptr err;
+    std::mutex mu;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&, t] {
+            try {
+                for (int k = (int)((long long)n * t / threads); k < (int)((long long)n * (t + 1) / threads); ++k) f(k);
+            } catch (...) {
+                std::lock_guard<std::mutex> lock(mu);
+                if (!err) err = std::current_exception();
+            }
+        });
+    for (auto &th : pool) th.join();
+    if (err) std::rethrow_exception(err);
+}
+
 void build_batch(int W, const sfmba_problem *win, Batch &B) {
     // the window index is a grid dimension (y or z) of the per-window kernels
     if (W > 65535) throw Error(SFMBA_ERR_UNSUPPORTED, "at most 65535 windows per batch");
@@ -428,10 +463,10 @@ void build_batch(int W, const sfmba_problem *win, Batch &B) {
     B.img_base.resize(W); B.cam_base.resize(W); B.pt_base.resize(W); B.slot_base.resize(W);
     B.n_w.resize(W); B.nid_w.resize(W);
     B.obs_off.assign(W + 1, 0); B.s_off.resize(W); B.simg_off.resize(W); B.linv_off.resize(W);
-    B.cam_of_img.reserve(nI); B.model.reserve(nC); B.obs_image.reserve(nO); B.obs_point.reserve(nO);
-    B.cams.reserve(nC * 8); B.poses.reserve(nI * 7); B.points.reserve(nP * 3); B.obs_xy.reserve(nO * 2);
+    B.cam_of_img.reserve(nI); B.model.reserve(nC);
+    B.cams.reserve(nC * 8); B.poses.reserve(nI * 7);
     B.fixed_pose.reserve(nI); B.fixed_cam.reserve(nC); B.fixed_cp.reserve(nC * 8);
-    B.img_win.reserve(nI); B.cam_win.reserve(nC); B.win_of_point.reserve(nP);
+    B.img_win.reserve(nI); B.cam_win.reserve(nC);
     int ib = 0, cb = 0, pb = 0, sb = 0;
     long long ob = 0, so = 0, sio = 0, lo = 0;
     for (int w = 0; w < W; ++w) {
@@ -499,13 +534,6 @@ void build_batch(int W, const sfmba_problem *win, Batch &B) {
         }
         B.cams.insert(B.cams.end(), p.camera_params, p.camera_params + (size_t)wc * 8);
         B.poses.insert(B.poses.end(), p.poses, p.poses + (size_t)wi * 7);
-        B.points.insert(B.points.end(), p.points, p.points + (size_t)wp * 3);
-        B.win_of_point.insert(B.win_of_point.end(), wp, w);
-        for (long long o = 0; o < wo; ++o) {
-            B.obs_image.push_back(p.obs_image[o] + ib);
-            B.obs_point.push_back(p.obs_point[o] + pb);
-        }
-        B.obs_xy.insert(B.obs_xy.end(), p.obs_xy, p.obs_xy + (size_t)wo * 2);
         B.fixed_pose.insert(B.fixed_pose.end(), fp.begin(), fp.end());
         B.fixed_cam.insert(B.fixed_cam.end(), fc.begin(), fc.end());
         B.fixed_cp.insert(B.fixed_cp.end(), fcp.begin(), fcp.end());
@@ -524,6 +552,25 @@ void build_batch(int W, const sfmba_problem *win, Batch &B) {
     if (L.slot_pre_start.empty()) L.slot_pre_start.push_back(0);
     B.wblk_start.push_back((int)B.cblk_win.size());
     B.cblk_lo.push_back(ob);
+    // Points and observations (the bulk of the batch), window by window on
+    // the host threads into their final places.
+    B.points.resize((size_t)nP * 3);
+    B.win_of_point.resize(nP);
+    B.obs_image.resize(nO);
+    B.obs_point.resize(nO);
+    B.obs_xy.resize((size_t)nO * 2);
+    parallel_for(W, [&](int w) {
+        const sfmba_problem &p = win[w];
+        const long long o0 = B.obs_off[w];
+        const int ib0 = B.img_base[w], pb0 = B.pt_base[w];
+        std::copy(p.points, p.points + (size_t)p.num_points * 3, B.points.begin() + (size_t)pb0 * 3);
+        std::fill(B.win_of_point.begin() + pb0, B.win_of_point.begin() + pb0 + p.num_points, w);
+        for (long long o = 0; o < p.num_observations; ++o) {
+            B.obs_image[o0 + o] = p.obs_image[o] + ib0;
+            B.obs_point[o0 + o] = p.obs_point[o] + pb0;
+        }
+        std::copy(p.obs_xy, p.obs_xy + (size_t)p.num_observations * 2, B.obs_xy.begin() + (size_t)o0 * 2);
+    });
     L.n = sb;
     B.s_total = so; B.simg_total = sio; B.linv_total = lo;
     sfmba_problem &q = B.problem;
@@ -1023,10 +1070,13 @@ class Solver {
                     const int maxit = std::max(1, o->pcg_max_iterations);
                     int vp = 0, vi = 0;  // launch variants of the two passes
                     if (o->kernel_variant > 0) {
-                        vp = vi = std::min(o->kernel_variant, kPassVariants) - 1;
+                        vp = std::min(o->kernel_variant, kPointPassVariants) - 1;
+                        vi = (o->kernel_variant - 1) % kImagePassVariants;
                     } else if (b.mixed) {
-                        vp = tuned_variant(ctx_.device, 0, b, s_, [&](int v) { launch_mf_points(b, s_, v); });
-                        vi = tuned_variant(ctx_.device, 1, b, s_, [&](int v) { launch_mf_images(b, s_, v); });
+                        vp = tuned_variant(ctx_.device, 0, kPointPassVariants, b, s_,
+                                           [&](int v) { launch_mf_points(b, s_, v); });
+                        vi = tuned_variant(ctx_.device, 1, kImagePassVariants, b, s_,
+                                           [&](int v) { launch_mf_images(b, s_, v); });
                     }
                     for (int it = 0; it < maxit; it += kPcgPollEvery) {
                         const int m = std::min(kPcgPollEvery, maxit - it);
@@ -2053,12 +2103,16 @@ int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *window
             throw Error(SFMBA_ERR_INVALID_ARGUMENT, "windows or results is NULL");
         check_options(o);
         if (num_windows == 0) return;
-        for (int w = 0; w < num_windows; ++w) {
-            check_problem_shape(&windows[w]);
-            check_problem_host(&windows[w]);
-        }
+        Profiler &prof = profiler();
+        double t = now_s();
+        for (int w = 0; w < num_windows; ++w) check_problem_shape(&windows[w]);
+        parallel_for(num_windows, [&](int w) { check_problem_host(&windows[w]); });
+        prof.host("batch_validate", now_s() - t);
+        t = now_s();
         Batch B;
         build_batch(num_windows, windows, B);
+        prof.host("batch_build", now_s() - t);
+        t = now_s();
         Context &ctx = context();
         cudaStream_t s = ctx.stream;
         Solver solver(ctx, s);
@@ -2066,8 +2120,15 @@ int sfmba_bundle_adjust_batched(int32_t num_windows, const sfmba_problem *window
             PhaseScope ps(PH_SETUP, s);
             solver.setup(&B.problem, o, false, true, &B);
         }
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+        prof.host("batch_setup", now_s() - t);
+        t = now_s();
         std::vector<WinState> ws = solver.run_batched(o);
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+        prof.host("batch_solve", now_s() - t);
+        t = now_s();
         solver.copy_out_batched(B, results);
+        prof.host("batch_copy_out", now_s() - t);
         profiler().resolve();
         const double secs = now_s() - t0;
         for (int w = 0; w < num_windows; ++w) {
@@ -2113,6 +2174,15 @@ int sfmba_profile_report(char *buf, int64_t len) {
             js += tmp;
         }
         js += ",\"kernel_launches\":" + std::to_string(g_kernel_launches);
+        js += ",\"host_ms\":{";
+        bool first = true;
+        for (const auto &kv : p.host_ms) {
+            char tmp[160];
+            std::snprintf(tmp, sizeof(tmp), "%s\"%s\":%.3f", first ? "" : ",", kv.first.c_str(), kv.second);
+            js += tmp;
+            first = false;
+        }
+        js += "}";
         js += ",\"autotune\":" + tune_report() + "}";
         if (!buf || len <= (int64_t)js.size())
             throw Error(SFMBA_ERR_INVALID_ARGUMENT, "profile buffer too small (need " + std::to_string(js.size() + 1) + ")");
