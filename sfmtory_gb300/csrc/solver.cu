@@ -469,17 +469,29 @@ void build_batch(int W, const sfmba_problem *win, Batch &B) {
     B.img_win.reserve(nI); B.cam_win.reserve(nC);
     int ib = 0, cb = 0, pb = 0, sb = 0;
     long long ob = 0, so = 0, sio = 0, lo = 0;
-    for (int w = 0; w < W; ++w) {
+    // Each window slotted on its own (independent), on the host threads.
+    std::vector<Layout> lays(W);
+    parallel_for(W, [&](int w) {
         const sfmba_problem &p = win[w];
-        const int wi = (int)p.num_images, wc = (int)p.num_cameras, wp = (int)p.num_points;
-        const long long wo = p.num_observations;
+        const int wi = (int)p.num_images, wc = (int)p.num_cameras;
         std::vector<int> coi(p.camera_of_image, p.camera_of_image + wi);
         std::vector<int> mod(p.camera_model, p.camera_model + wc);
         std::vector<unsigned char> fp(wi, 0), fc(wc, 0), fcp((size_t)wc * 8, 0);
         if (p.fixed_poses) fp.assign(p.fixed_poses, p.fixed_poses + wi);
         if (p.fixed_cameras) fc.assign(p.fixed_cameras, p.fixed_cameras + wc);
         if (p.fixed_camera_params) fcp.assign(p.fixed_camera_params, p.fixed_camera_params + (size_t)wc * 8);
-        Layout lw = make_layout(wi, wc, wp, wo, coi, mod, fp, fc, fcp, D);
+        lays[w] = make_layout(wi, wc, (int)p.num_points, p.num_observations, coi, mod, fp, fc, fcp, D);
+    });
+    for (int w = 0; w < W; ++w) {
+        const sfmba_problem &p = win[w];
+        const int wi = (int)p.num_images, wc = (int)p.num_cameras, wp = (int)p.num_points;
+        const long long wo = p.num_observations;
+        const int *coi = p.camera_of_image, *mod = p.camera_model;
+        std::vector<unsigned char> fp(wi, 0), fc(wc, 0), fcp((size_t)wc * 8, 0);
+        if (p.fixed_poses) fp.assign(p.fixed_poses, p.fixed_poses + wi);
+        if (p.fixed_cameras) fc.assign(p.fixed_cameras, p.fixed_cameras + wc);
+        if (p.fixed_camera_params) fcp.assign(p.fixed_camera_params, p.fixed_camera_params + (size_t)wc * 8);
+        const Layout &lw = lays[w];
         if (lw.n > 16384)
             throw Error(SFMBA_ERR_UNSUPPORTED, "window " + std::to_string(w) + " has more than 16384 unknowns");
         B.img_base[w] = ib; B.cam_base[w] = cb; B.pt_base[w] = pb; B.slot_base[w] = sb;
