@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--max-iterations", type=int, default=50)
     ap.add_argument("--pcg-tol", type=float, default=0.1)
     ap.add_argument("--pcg-max", type=int, default=100)
+    ap.add_argument("--pcg-coarse", type=int, default=0,
+                    help="clusters of the PCG preconditioner's coarse correction (0: 64, -1: block-Jacobi alone)")
     ap.add_argument("--skip-fp64", action="store_true", help="skip the FP64 comparison solves")
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -106,7 +108,9 @@ def workload_config(args, p):
         "workload": f"{args.workload}: {p.num_images} {_model_name(p)} cameras, {p.num_points} points, "
                     f"{p.num_observations} observations, track length mean {counts.mean():.2f} max {counts.max()}",
         "reduced_dim": p.reduced_dim(),
-        "solver": "matrix-free Schur PCG, block-Jacobi, tol %g, max %d it/retry" % (args.pcg_tol, args.pcg_max),
+        "solver": "matrix-free Schur PCG, block-Jacobi%s, tol %g, max %d it/retry" % (
+            "" if args.pcg_coarse < 0 else " + coarse correction (%d clusters of consecutive images)" % (
+                args.pcg_coarse or 64), args.pcg_tol, args.pcg_max),
         "loss": "squared",
         "max_lm_iterations": args.max_iterations,
         "seed": args.seed,
@@ -128,7 +132,7 @@ def solver_options(args, precision, target_cost=0.0):
     return abi.default_options(
         max_iterations=args.max_iterations, robust_loss=abi.LOSS_NONE, precision=precision,
         solver=abi.SOLVER_PCG, pcg_tolerance=args.pcg_tol, pcg_max_iterations=args.pcg_max,
-        target_cost=target_cost, kernel_variant=args.kernel_variant)
+        target_cost=target_cost, kernel_variant=args.kernel_variant, pcg_coarse_clusters=args.pcg_coarse)
 
 
 # ------------------------------------------------------------------ clocks

@@ -113,7 +113,10 @@ typedef struct sfmba_options {
     int32_t kernel_variant;       /* 0: launch variants of the PCG observation passes
                                      picked by the autotuner; 1..4: force one (all
                                      variants give the same results) */
-    int32_t reserved[5];
+    int32_t pcg_coarse_clusters;  /* PCG solver: clusters of consecutive images in the
+                                     coarse correction of the preconditioner (0: 64,
+                                     at most 128; < 0: block-Jacobi alone) */
+    int32_t reserved[4];
 } sfmba_options;
 
 /* crates/sfm-ba/src/lib.rs:240-247 (`BaOutput`). Output buffers are caller

@@ -73,7 +73,8 @@ class SfmbaOptions(C.Structure):
         ("dense_max_dim", C.c_int32),
         ("fp64_polish", C.c_int32),
         ("kernel_variant", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("pcg_coarse_clusters", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 

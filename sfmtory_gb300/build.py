@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsfmba_gb300.so")
 SOURCES = ["k_setup.cu", "k_lin.cu", "k_dense.cu", "k_pcg.cu", "k_matfree.cu", "k_mf_pcg.cu", "k_noalloc.cu", "k_batched.cu",
-           "k_filter.cu", "k_intrinsics.cu", "k_pnp.cu", "colmap_io.cpp", "solver.cu"]
+           "k_filter.cu", "k_intrinsics.cu", "k_pnp.cu", "k_coarse.cu", "colmap_io.cpp", "solver.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-ffp-contract=off"]
@@ -68,7 +68,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES))
     if force or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcusolver"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -1,0 +1,446 @@
+// Two-level preconditioner of the matrix-free Schur PCG: block-Jacobi on
+// the image blocks plus an additive coarse correction Z A_c^-1 Z^T, where Z
+// is piecewise constant over clusters of consecutive images (one coarse
+// unknown per cluster and image-block column) and A_c = Z^T S Z is the exact
+// Galerkin projection of the damped Schur complement
+//   S = (B + lambda diag B) - E C^-1 E^T.
+// Block-Jacobi leaves the smooth, long-range modes of a long camera sequence
+// (drift along the trajectory) to the Krylov iteration; the coarse space
+// removes them. Z^T B Z is the sum of a cluster's image blocks; Z^T E C^-1
+// E^T Z sums, for every point, Y_c^T C_p^-1 Y_c' over the clusters c, c' its
+// observations fall in, with Y_c = sum over its observations in cluster c of
+// Jx~^T Jc~ (the Jacobians recomputed or read as in the PCG passes).
+//
+// The point-cluster pairs are grouped by cluster pair once per solve
+// (sorted, so each group's points are in point order) and cut into chunks
+// of at most kCoarseChunk points; one warp per chunk forms the chunk's
+// D x D contribution with the register-tiled product of the Schur
+// reduction (inner dimension 3 per point), and one block per group sums its
+// chunks in order — no atomics, so A_c is bit-reproducible. A_c is factored
+// and inverted in FP32 by cuSOLVER (it is small: clusters x D <= 1408) and
+// applied as a dense product each iteration.
+#include <cub/cub.cuh>
+
+#include "mf_passes.cuh"
+
+namespace sfmba {
+
+namespace {
+
+// Distinct clusters among a point's observations, in increasing order.
+__device__ int point_clusters(const int *ob_img, const int *img_cluster, int s, int e, int *out) {
+    int k = 0;
+    for (int o = s; o < e; ++o) {
+        const int c = img_cluster[ob_img[o]];
+        bool seen = false;
+        for (int j = 0; j < k && !seen; ++j) seen = out[j] == c;
+        if (seen) continue;
+        int j = k++;
+        while (j > 0 && out[j - 1] > c) {  // insertion keeps them sorted
+            out[j] = out[j - 1];
+            --j;
+        }
+        out[j] = c;
+    }
+    return k;
+}
+
+__global__ void k_coarse_count(const int *pt_start, const int *ob_img, const int *img_cluster, int nP,
+                               long long *count) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nP) return;
+    int cl[kMaxCoarseClusters];
+    const int k = point_clusters(ob_img, img_cluster, pt_start[p], pt_start[p + 1], cl);
+    count[p] = (long long)k * (k + 1) / 2;
+}
+
+__global__ void k_coarse_emit(const int *pt_start, const int *ob_img, const int *img_cluster, int nP, int nc,
+                              const long long *off, int *key, int *val) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nP) return;
+    int cl[kMaxCoarseClusters];
+    const int k = point_clusters(ob_img, img_cluster, pt_start[p], pt_start[p + 1], cl);
+    long long w = off[p];
+    for (int a = 0; a < k; ++a)
+        for (int b = a; b < k; ++b) {
+            key[w] = cl[a] * nc + cl[b];
+            val[w] = p;
+            ++w;
+        }
+}
+
+__global__ void k_key_counts(const int *key, long long n, int *counts) {
+    // counts of each key in the sorted key array: boundaries of equal runs
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    if (t == 0 || key[t] != key[t - 1]) {
+        long long e = t + 1;
+        while (e < n && key[e] == key[t]) ++e;
+        counts[key[t]] = (int)(e - t);
+    }
+}
+
+// A_c = 0, then block (c, c) = sum over the cluster's images of
+// (H_i + lambda diag H_i) on the image's unknown columns.
+__global__ void k_coarse_diag(const double *img_H, const int *img_active, const int *clu_start, int nc, int D,
+                              const LMState *st, double *A) {
+    const int c = blockIdx.x;
+    if (c >= nc) return;
+    const int Nc = nc * D;
+    const double lam = st->lambda;
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+        const int a = e / D, b = e - a * D;
+        double s = 0.0;
+        for (int i = clu_start[c]; i < clu_start[c + 1]; ++i) {
+            const int act = img_active[i];
+            if (!((act >> a) & 1) || !((act >> b) & 1)) continue;
+            const double h = img_H[(size_t)i * D * D + a * D + b];
+            s += h + (a == b ? lam * h : 0.0);
+        }
+        A[(size_t)(c * D + a) * Nc + c * D + b] = s;
+    }
+}
+
+// Chunk q of the pair groups: minus sum over its points of Y_c^T C^-1 Y_c'.
+// One warp per chunk; per round of 32 points lane t stages A_t = Y_c (3 x D)
+// and P_t = C^-1 Y_c' (3 x D); the D x D product over 3 x 32 inner terms is
+// register-tiled as in the Schur reduction, rounds added with Kahan
+// compensation (FP32), output in FP64.
+template <typename T>
+constexpr int coarse_warps() { return sizeof(T) == 4 ? 4 : 2; }  // static shared memory under 48 KB
+
+template <typename T, int D, bool RC, int M>
+__global__ void __launch_bounds__(32 * coarse_warps<T>()) k_coarse_pairs(JacSrc<T> J, const int *__restrict__ pt_start,
+                                                      const int *__restrict__ img_cluster,
+                                                      const int4 *__restrict__ chunks, int nchunks,
+                                                      const int *__restrict__ pair_pt,
+                                                      const int2 *__restrict__ group_cc, const T *__restrict__ pt_Cinv,
+                                                      const unsigned char *__restrict__ pt_ok,
+                                                      double *__restrict__ part) {
+    constexpr int RH = (D + 1) / 2, CQ = (D + 3) / 4;
+    constexpr int LD = 3 * D + 1;
+    constexpr int WPB = coarse_warps<T>();
+    __shared__ T sA[WPB][32][LD];
+    __shared__ T sP[WPB][32][LD];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (q >= nchunks) return;
+    const int4 ch = chunks[q];  // {group, first, end}
+    const int2 cc = group_cc[ch.x];
+    const int sg = lane >> 3, l8 = lane & 7;
+    const int r0 = (l8 >> 2) * RH, c0 = (l8 & 3) * CQ;
+    T acc[RH][CQ], comp[RH][CQ];
+#pragma unroll
+    for (int a = 0; a < RH; ++a)
+#pragma unroll
+        for (int b = 0; b < CQ; ++b) acc[a][b] = comp[a][b] = T(0);
+    for (int base = ch.y; base < ch.z; base += 32) {
+        const int k = base + lane;
+        T ya[3][D], yb[3][D];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < D; ++c) ya[r][c] = yb[r][c] = T(0);
+        bool staged = false;
+        if (k < ch.z) {
+            const int p = pair_pt[k];
+            if (pt_ok[p]) {
+                for (int o = pt_start[p]; o < pt_start[p + 1]; ++o) {
+                    const int4 rc = __ldg(J.obrec + o);
+                    const int cl = img_cluster[rc.x];
+                    if (cl != cc.x && cl != cc.y) continue;
+                    ObsOp<T, D, RC, M> op;
+                    make_op_point_major<T, D, RC>(J, o, rc, op);
+                    T jx[6], jc[2 * D];
+                    op.jx_rows(jx);
+                    op.jc_rows(jc);
+                    if (cl == cc.x) {
+#pragma unroll
+                        for (int r = 0; r < 3; ++r)
+#pragma unroll
+                            for (int c = 0; c < D; ++c) ya[r][c] += jx[r] * jc[c] + jx[3 + r] * jc[D + c];
+                    }
+                    if (cl == cc.y) {
+#pragma unroll
+                        for (int r = 0; r < 3; ++r)
+#pragma unroll
+                            for (int c = 0; c < D; ++c) yb[r][c] += jx[r] * jc[c] + jx[3 + r] * jc[D + c];
+                    }
+                }
+                const T *Ci = pt_Cinv + 6 * (size_t)p;
+                const T m00 = Ci[0], m01 = Ci[1], m02 = Ci[2], m11 = Ci[3], m12 = Ci[4], m22 = Ci[5];
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    sA[wl][lane][c] = ya[0][c];
+                    sA[wl][lane][D + c] = ya[1][c];
+                    sA[wl][lane][2 * D + c] = ya[2][c];
+                    sP[wl][lane][c] = m00 * yb[0][c] + m01 * yb[1][c] + m02 * yb[2][c];
+                    sP[wl][lane][D + c] = m01 * yb[0][c] + m11 * yb[1][c] + m12 * yb[2][c];
+                    sP[wl][lane][2 * D + c] = m02 * yb[0][c] + m12 * yb[1][c] + m22 * yb[2][c];
+                }
+                staged = true;
+            }
+        }
+        if (!staged) {
+#pragma unroll
+            for (int f = 0; f < 3 * D; ++f) sA[wl][lane][f] = sP[wl][lane][f] = T(0);
+        }
+        __syncwarp();
+        T pt[RH][CQ];
+#pragma unroll
+        for (int a = 0; a < RH; ++a)
+#pragma unroll
+            for (int b = 0; b < CQ; ++b) pt[a][b] = T(0);
+#pragma unroll 2
+        for (int kk = 0; kk < 8; ++kk) {
+            const int t = sg + 4 * kk;
+#pragma unroll
+            for (int rho = 0; rho < 3; ++rho) {
+                T av[RH], pv[CQ];
+#pragma unroll
+                for (int a = 0; a < RH; ++a) av[a] = (r0 + a < D) ? sA[wl][t][rho * D + r0 + a] : T(0);
+#pragma unroll
+                for (int b = 0; b < CQ; ++b) pv[b] = (c0 + b < D) ? sP[wl][t][rho * D + c0 + b] : T(0);
+#pragma unroll
+                for (int a = 0; a < RH; ++a)
+#pragma unroll
+                    for (int b = 0; b < CQ; ++b) pt[a][b] += av[a] * pv[b];
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < RH; ++a)
+#pragma unroll
+            for (int b = 0; b < CQ; ++b) {
+                if constexpr (std::is_same<T, float>::value) {
+                    const T y = pt[a][b] - comp[a][b];
+                    const T t = acc[a][b] + y;
+                    comp[a][b] = (t - acc[a][b]) - y;
+                    acc[a][b] = t;
+                } else {
+                    acc[a][b] += pt[a][b];
+                }
+            }
+        __syncwarp();
+    }
+    double *dst = part + (size_t)q * D * D;
+#pragma unroll
+    for (int a = 0; a < RH; ++a)
+#pragma unroll
+        for (int b = 0; b < CQ; ++b) {
+            double v = (double)acc[a][b] - (double)comp[a][b];
+            v += __shfl_xor_sync(0xffffffffu, v, 8);
+            v += __shfl_xor_sync(0xffffffffu, v, 16);
+            const int row = r0 + a, col = c0 + b;
+            if (lane < 8 && row < D && col < D) dst[row * D + col] = -v;
+        }
+}
+
+// Group g's chunks summed in order into block (c, c') of A_c, and its
+// transpose into (c', c) for c != c'. Columns that are not unknowns of any
+// image are left at zero (k_coarse_to32 puts 1 on their diagonal).
+__global__ void k_coarse_finish(const double *part, const int *group_chunk_off, const int2 *group_cc, int ngroups,
+                                int nc, int D, double *A) {
+    const int g = blockIdx.x;
+    if (g >= ngroups) return;
+    const int Nc = nc * D;
+    const int2 cc = group_cc[g];
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+        const int a = e / D, b = e - a * D;
+        double s = 0.0;
+        for (int q = group_chunk_off[g]; q < group_chunk_off[g + 1]; ++q) s += part[(size_t)q * D * D + e];
+        A[(size_t)(cc.x * D + a) * Nc + cc.y * D + b] += s;
+        if (cc.x != cc.y) A[(size_t)(cc.y * D + b) * Nc + cc.x * D + a] += s;
+    }
+}
+
+// FP32 copy for the factorisation: diagonal scaled by (1 + 1e-6) (keeps the
+// FP32 Cholesky of a nearly singular coarse matrix away from breakdown; it
+// is a preconditioner), an empty row/column gets a unit diagonal; Ainv = I.
+__global__ void k_coarse_to32(const double *A, int Nc, float *A32, float *Ainv) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)Nc * Nc) return;
+    const int r = (int)(e / Nc), c = (int)(e - (long long)r * Nc);
+    double v = A[e];
+    if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + 1e-6);
+    A32[e] = (float)v;
+    Ainv[e] = r == c ? 1.f : 0.f;
+}
+
+// Ainv = (X + X^T) / 2 for the solve's result X (the preconditioner must be
+// symmetric; the FP32 solve leaves rounding-level asymmetry).
+__global__ void k_coarse_sym(float *Ainv, int Nc) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)Nc * Nc) return;
+    const int r = (int)(e / Nc), c = (int)(e - (long long)r * Nc);
+    if (c <= r) return;
+    const float v = 0.5f * (Ainv[e] + Ainv[(size_t)c * Nc + r]);
+    Ainv[e] = v;
+    Ainv[(size_t)c * Nc + r] = v;
+}
+
+// zc = Z^T r: per cluster and column, the sum over the cluster's images in
+// image order. One warp per cluster.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_coarse_restrict(const T *__restrict__ r, const int *__restrict__ clu_start,
+                                                         int nc, const LMState *__restrict__ st, int check_done,
+                                                         double *__restrict__ zc) {
+    if (check_done && st->pcg_done) return;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (c >= nc || lane >= D) return;
+    double s = 0.0;
+    for (int i = clu_start[c]; i < clu_start[c + 1]; ++i) s += (double)r[(size_t)i * D + lane];
+    zc[c * D + lane] = s;
+}
+
+// cc = A_c^-1 zc, one warp per row (the 16-byte loads of the FP32 inverse
+// are the traffic: Nc^2 x 4 bytes, L2-resident between iterations).
+template <typename T>
+__global__ void __launch_bounds__(256) k_coarse_gemv(const float *__restrict__ Ainv, const double *__restrict__ zc,
+                                                     int Nc, const LMState *__restrict__ st, int check_done,
+                                                     T *__restrict__ cc) {
+    if (check_done && st->pcg_done) return;
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= Nc) return;
+    const float *a = Ainv + (size_t)row * Nc;
+    double s = 0.0;
+    for (int j = lane; j < Nc; j += 32) s += (double)__ldg(a + j) * zc[j];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) cc[row] = (T)s;
+}
+
+// z_i += cc[cluster(i)] on the image's unknown columns; partials of r.z and
+// r.r. init: the start of a solve — p = z (and its padded FP32 copy), and the
+// solve's done flag (set by the previous solve) is not consulted.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_coarse_z(const T *__restrict__ r, const T *__restrict__ cc,
+                                                  const int *__restrict__ img_cluster,
+                                                  const int *__restrict__ img_active, const LMState *__restrict__ st,
+                                                  int nI, int init, T *__restrict__ z, T *__restrict__ p,
+                                                  float *__restrict__ p4, double *__restrict__ part) {
+    if (!init && st->pcg_done) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= nI) return;
+    const size_t base = (size_t)i * D;
+    double rz = 0.0, rr = 0.0;
+    if (lane < D) {
+        const double rc = (double)r[base + lane];
+        double zc = (double)z[base + lane];
+        if ((img_active[i] >> lane) & 1) zc += (double)cc[(size_t)img_cluster[i] * D + lane];
+        const T zt = (T)zc;
+        z[base + lane] = zt;
+        if (init) {
+            p[base + lane] = zt;
+            if (p4) p4[(size_t)i * pad4(D) + lane] = (float)zt;
+        }
+        rz = rc * (double)zt;
+        rr = rc * rc;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        rz += __shfl_xor_sync(0xffffffffu, rz, off);
+        rr += __shfl_xor_sync(0xffffffffu, rr, off);
+    }
+    if (lane == 0) {
+        part[i] = rz;
+        part[nI + i] = rr;
+    }
+}
+
+}  // namespace
+
+size_t coarse_setup_temp_bytes(int nP, long long npairs_max) {
+    size_t a = 0, bsz = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, a, (long long *)nullptr, (long long *)nullptr, nP > 0 ? nP : 1);
+    const int n = (int)std::max<long long>(1, std::min<long long>(npairs_max, (1LL << 31) - 1));
+    cub::DeviceRadixSort::SortPairs(nullptr, bsz, (int *)nullptr, (int *)nullptr, (int *)nullptr, (int *)nullptr, n);
+    return std::max(a, bsz);
+}
+
+long long launch_coarse_count(const Bufs &b, long long *count, long long *off, void *temp, size_t temp_bytes,
+                              cudaStream_t s) {
+    if (b.nP == 0) return 0;
+    k_coarse_count<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, b.ob_img, b.co.img_cluster, b.nP, count);
+    SFMBA_LAUNCH_CHECK();
+    size_t tb = temp_bytes;
+    SFMBA_CUDA(cub::DeviceScan::ExclusiveSum(temp, tb, count, off, b.nP, s));
+    long long last_off = 0, last_cnt = 0;
+    SFMBA_CUDA(cudaMemcpyAsync(&last_off, off + b.nP - 1, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    SFMBA_CUDA(cudaMemcpyAsync(&last_cnt, count + b.nP - 1, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    SFMBA_CUDA(cudaStreamSynchronize(s));
+    return last_off + last_cnt;
+}
+
+void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, int *key, int *val, int *key2,
+                         int *val_sorted, int *key_counts, void *temp, size_t temp_bytes, cudaStream_t s) {
+    const int nc = b.co.nc;
+    k_coarse_emit<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, b.ob_img, b.co.img_cluster, b.nP, nc, off, key, val);
+    SFMBA_LAUNCH_CHECK();
+    size_t tb = temp_bytes;
+    int bits = 1;
+    while ((1LL << bits) < (long long)nc * nc) ++bits;
+    SFMBA_CUDA(cub::DeviceRadixSort::SortPairs(temp, tb, key, key2, val, val_sorted, (int)npairs, 0, bits, s));
+    SFMBA_CUDA(cudaMemsetAsync(key_counts, 0, sizeof(int) * (size_t)nc * nc, s));
+    k_key_counts<<<div_up(npairs, 256), 256, 0, s>>>(key2, npairs, key_counts);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
+    const CoarseBufs &co = b.co;
+    const int D = b.D, Nc = co.nc * D;
+    SFMBA_CUDA(cudaMemsetAsync(co.A, 0, sizeof(double) * (size_t)Nc * Nc, s));
+    k_coarse_diag<<<co.nc, 128, 0, s>>>(b.img_H, b.img_active, co.clu_start, co.nc, D, b.state, co.A);
+    SFMBA_LAUNCH_CHECK();
+    if (co.nchunks > 0) {
+        dispatch_D(D, [&](auto dc) {
+            constexpr int DD = decltype(dc)::value;
+            if (b.mixed)
+                k_coarse_pairs<float, DD, true, -1><<<div_up(co.nchunks, 4), 128, 0, s>>>(
+                    jac_src<float>(b), b.pt_start, co.img_cluster, co.chunk, co.nchunks, co.pair_pt,
+                    co.group_cc, (const float *)b.pt_Cinv, b.pt_ok, co.chunk_part);
+            else
+                k_coarse_pairs<double, DD, false, -1><<<div_up(co.nchunks, 2), 64, 0, s>>>(
+                    jac_src<double>(b), b.pt_start, co.img_cluster, co.chunk, co.nchunks, co.pair_pt,
+                    co.group_cc, (const double *)b.pt_Cinv, b.pt_ok, co.chunk_part);
+        });
+        SFMBA_LAUNCH_CHECK();
+        k_coarse_finish<<<co.ngroups, 128, 0, s>>>(co.chunk_part, co.group_chunk_off, co.group_cc, co.ngroups, co.nc,
+                                                   D, co.A);
+        SFMBA_LAUNCH_CHECK();
+    }
+    k_coarse_to32<<<div_up((long long)Nc * Nc, 256), 256, 0, s>>>(co.A, Nc, co.A32, co.Ainv);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_coarse_symmetrize(const Bufs &b, cudaStream_t s) {
+    const int Nc = b.co.nc * b.D;
+    k_coarse_sym<<<div_up((long long)Nc * Nc, 256), 256, 0, s>>>(b.co.Ainv, Nc);
+    SFMBA_LAUNCH_CHECK();
+}
+
+void launch_coarse_correct(const Bufs &b, bool init, cudaStream_t s) {
+    const CoarseBufs &co = b.co;
+    const int Nc = co.nc * b.D;
+    dispatch_D(b.D, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        auto run = [&](auto t) {
+            using T = decltype(t);
+            k_coarse_restrict<T, D><<<div_up(co.nc, 8), 256, 0, s>>>((const T *)b.pcg_r, co.clu_start, co.nc, b.state,
+                                                                     init ? 0 : 1, co.zc);
+            SFMBA_LAUNCH_CHECK();
+            k_coarse_gemv<T><<<div_up(Nc, 8), 256, 0, s>>>(co.Ainv, co.zc, Nc, b.state, init ? 0 : 1, (T *)co.cc);
+            SFMBA_LAUNCH_CHECK();
+            k_coarse_z<T, D><<<div_up(b.nI, 8), 256, 0, s>>>(
+                (const T *)b.pcg_r, (const T *)co.cc, co.img_cluster, b.img_active, b.state, b.nI, init ? 1 : 0,
+                (T *)b.pcg_z, (T *)b.pcg_p, std::is_same<T, float>::value ? b.pcg_p4 : nullptr, b.pcg_part);
+            SFMBA_LAUNCH_CHECK();
+        };
+        if (b.mixed) run(0.0f);
+        else run(0.0);
+    });
+}
+
+}  // namespace sfmba

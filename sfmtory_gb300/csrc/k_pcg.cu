@@ -232,11 +232,12 @@ void images_finish_t(const Bufs &b, cudaStream_t s) {
 }
 
 template <typename T, int D>
-void vector_t(const Bufs &b, cudaStream_t s, int parity) {
+void vector_t(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
     k_pcg_update<T, D><<<div_up(b.nI, 8), 256, 0, s>>>((const T *)b.pcg_Minv, (const T *)b.pcg_p,
                                                        (const T *)b.pcg_q, b.state, b.nI, parity, (T *)b.pcg_x,
                                                        (T *)b.pcg_r, (T *)b.pcg_z, b.pcg_part);
     SFMBA_LAUNCH_CHECK();
+    if (coarse) launch_coarse_correct(b, false, s);  // z += Z A_c^-1 Z^T r, new r.z partials
     k_pcg_dir<T><<<div_up(b.nID, 256), 256, 0, s>>>((const T *)b.pcg_z, b.state, b.pcg_part, b.nI, b.nID, parity,
                                                     (T *)b.pcg_p, b.D,
                                                     std::is_same<T, float>::value ? (T *)(void *)b.pcg_p4 : nullptr);
@@ -261,11 +262,11 @@ void launch_pcg_start(const Bufs &b, cudaStream_t s) {
 SFMBA_PCG_LAUNCHER(launch_pcg_images_finish, images_finish_t)
 #undef SFMBA_PCG_LAUNCHER
 
-void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity) {
+void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
     dispatch_D(b.D, [&](auto dc) {
         constexpr int D = decltype(dc)::value;
-        if (b.mixed) vector_t<float, D>(b, s, parity);
-        else vector_t<double, D>(b, s, parity);
+        if (b.mixed) vector_t<float, D>(b, s, parity, coarse);
+        else vector_t<double, D>(b, s, parity, coarse);
     });
 }
 

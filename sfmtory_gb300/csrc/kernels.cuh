@@ -8,6 +8,31 @@
 namespace sfmba {
 
 // Device buffers of one solve (all owned by the workspace arena).
+// Coarse correction of the PCG preconditioner (k_coarse.cu).
+constexpr int kMaxCoarseClusters = 128;
+constexpr int kDefaultCoarseClusters = 64;
+constexpr int kCoarseChunk = 64;  // points per warp in the coarse assembly
+struct CoarseBufs {
+    int nc = 0;                       // clusters (0: off)
+    int *img_cluster = nullptr;       // [nI]
+    int *clu_start = nullptr;         // [nc+1] first image of each cluster (consecutive images)
+    int *pair_pt = nullptr;           // points of the point-cluster pairs, grouped by cluster pair
+    int ngroups = 0;
+    int2 *group_cc = nullptr;         // [ngroups] (c, c'), c <= c'
+    int *group_chunk_off = nullptr;   // [ngroups+1]
+    int nchunks = 0;
+    int4 *chunk = nullptr;            // [nchunks] {group, first, end, 0} into pair_pt
+    double *chunk_part = nullptr;     // [nchunks][D*D]
+    double *A = nullptr;              // [Nc*Nc] coarse matrix, FP64
+    float *A32 = nullptr;             // [Nc*Nc] FP32 copy, factored in place
+    float *Ainv = nullptr;            // [Nc*Nc]
+    void *cc = nullptr;               // [Nc] coarse correction, element type of the PCG vectors
+    double *zc = nullptr;             // [Nc] Z^T r
+    int *info = nullptr;              // factorisation status
+    float *work = nullptr;
+    int lwork = 0;
+};
+
 struct Bufs {
     // sizes
     int nI = 0, nC = 0, nP = 0;
@@ -78,6 +103,7 @@ struct Bufs {
     // PCG (matrix-free) vectors, [nI*D] each, element type T
     void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
     float *pcg_p4 = nullptr;      // FP32: [nI*pad4(D)] copy of p with 16-byte rows (point pass)
+    CoarseBufs co;                // coarse correction of the preconditioner
     void *pcg_u = nullptr;        // [nP*4] per-point Cinv E^T p
     void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
     double *pcg_part = nullptr;   // [3*nI] per-image partial dot products
@@ -246,11 +272,26 @@ void launch_pcg_start(const Bufs &b, cudaStream_t s);
 // One PCG iteration is launch_mf_points, launch_mf_images, then
 // launch_pcg_images_finish (q = S p) and launch_pcg_vector (x, r, z, p).
 void launch_pcg_images_finish(const Bufs &b, cudaStream_t s);
-void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity);  // parity = iteration & 1
+void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity, bool coarse = false);  // parity = iteration & 1
 // Work partition of the matrix-free passes (after sort_observations).
 void launch_pcg_partition(Bufs &b, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
+
+// ---- coarse correction of the PCG preconditioner (k_coarse.cu)
+size_t coarse_setup_temp_bytes(int nP, long long npairs_max);
+// Pairs count per point (exclusive-scanned into off); returns the total.
+long long launch_coarse_count(const Bufs &b, long long *count, long long *off, void *temp, size_t temp_bytes,
+                              cudaStream_t s);
+// Emits and sorts the point-cluster pairs; key_counts[c * nc + c'] = group sizes.
+void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, int *key, int *val, int *key2,
+                         int *val_sorted, int *key_counts, void *temp, size_t temp_bytes, cudaStream_t s);
+// A_c for the current damping and point inverses; FP32 copy and Ainv = I for the factorisation.
+void launch_coarse_assemble(const Bufs &b, cudaStream_t s);
+// z += Z Ainv Z^T r with the r.z / r.r partials (init: the start of a solve, p = z).
+void launch_coarse_correct(const Bufs &b, bool init, cudaStream_t s);
+// Symmetrise Ainv after the solve with the identity.
+void launch_coarse_symmetrize(const Bufs &b, cudaStream_t s);
 
 // ---- refine_intrinsics (k_intrinsics.cu)
 struct IntrinsicsBufs {

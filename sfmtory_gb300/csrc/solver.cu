@@ -22,6 +22,7 @@
 #include <vector>
 
 #include <cub/cub.cuh>
+#include <cusolverDn.h>
 
 #include "camera.cuh"
 #include "colmap_io.h"
@@ -48,11 +49,13 @@ const char *const kPhaseNames[] = {"setup",        "linearize",   "point_reduce"
                                    "point_inverse", "image_rhs",  "schur_pairs",  "fold",
                                    "cholesky",     "trsv",        "refine",       "pcg_precond",
                                    "pcg_points",   "pcg_images",  "pcg_vector",   "backsub_update",
-                                   "cost",         "lu",          "lm_bookkeeping"};
+                                   "cost",         "lu",          "lm_bookkeeping", "coarse_assemble",
+                                   "coarse_factor"};
 enum Phase {
     PH_SETUP, PH_LINEARIZE, PH_POINT_REDUCE, PH_IMAGE_REDUCE, PH_POINT_INVERSE, PH_IMAGE_RHS,
     PH_SCHUR, PH_FOLD, PH_CHOLESKY, PH_TRSV, PH_REFINE, PH_PCG_PRECOND, PH_PCG_POINTS,
-    PH_PCG_IMAGES, PH_PCG_VECTOR, PH_BACKSUB, PH_COST, PH_LU, PH_LM, PH_COUNT
+    PH_PCG_IMAGES, PH_PCG_VECTOR, PH_BACKSUB, PH_COST, PH_LU, PH_LM, PH_COARSE_ASSEMBLE, PH_COARSE_FACTOR,
+    PH_COUNT
 };
 
 struct Profiler {
@@ -203,7 +206,6 @@ class Arena {
         off_ += bytes;
         return reinterpret_cast<T *>(p);
     }
-    size_t capacity() const { return cap_; }
 
   private:
     char *base_ = nullptr;
@@ -283,10 +285,12 @@ std::string tune_report() {
 struct Context {
     int device = -1;
     cudaStream_t stream = nullptr;
-    Arena main, pairs, aux;
+    Arena main, pairs, aux, coarse;
     LMState *h_state = nullptr;  // pinned mirror
     int *h_counts = nullptr;     // pinned batch summary
+    cusolverDnHandle_t dn = nullptr;  // coarse factorisation (created on first use)
     ~Context() {
+        if (dn) cusolverDnDestroy(dn);
         if (h_state) cudaFreeHost(h_state);
         if (h_counts) cudaFreeHost(h_counts);
         if (stream) cudaStreamDestroy(stream);
@@ -682,6 +686,125 @@ class Solver {
   public:
     Solver(Context &ctx, cudaStream_t s) : ctx_(ctx), s_(s) {}
 
+    // Clusters of consecutive images and the point-cluster pair groups of
+    // the coarse correction (k_coarse.cu), once per solve. requested: 0 ->
+    // kDefaultCoarseClusters, < 0 -> off.
+    void setup_coarse(int requested) {
+        Bufs &b = b_;
+        CoarseBufs &co = b.co;
+        co = CoarseBufs{};
+        if (requested < 0 || b.nI < 2 || b.n == 0 || b.nP == 0) return;
+        int nc = requested == 0 ? kDefaultCoarseClusters : std::min(requested, kMaxCoarseClusters);
+        nc = std::min(nc, b.nI);
+        const int D = b.D, Nc = nc * D, nI = b.nI, nP = b.nP;
+        std::vector<int> clu_start(nc + 1), img_cluster(nI);
+        for (int c = 0; c <= nc; ++c) clu_start[c] = (int)((long long)c * nI / nc);
+        for (int c = 0; c < nc; ++c)
+            for (int i = clu_start[c]; i < clu_start[c + 1]; ++i) img_cluster[i] = c;
+        if (!ctx_.dn && cusolverDnCreate(&ctx_.dn) != CUSOLVER_STATUS_SUCCESS)
+            throw Error(SFMBA_ERR_CUDA, "cusolverDnCreate failed");
+        if (cusolverDnSetStream(ctx_.dn, s_) != CUSOLVER_STATUS_SUCCESS)
+            throw Error(SFMBA_ERR_CUDA, "cusolverDnSetStream failed");
+        Arena &A = ctx_.coarse;
+        long long *count = nullptr, *off = nullptr;
+        int *key_counts = nullptr;
+        void *temp1 = nullptr;
+        const size_t t1 = coarse_setup_temp_bytes(nP, 1);
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            co.img_cluster = A.take<int>(nI);
+            co.clu_start = A.take<int>((size_t)nc + 1);
+            co.A = A.take<double>((size_t)Nc * Nc);
+            co.A32 = A.take<float>((size_t)Nc * Nc);
+            co.Ainv = A.take<float>((size_t)Nc * Nc);
+            co.cc = A.take<double>(Nc);
+            co.zc = A.take<double>(Nc);
+            co.info = A.take<int>(1);
+            count = A.take<long long>((size_t)nP + 1);
+            off = A.take<long long>((size_t)nP + 1);
+            key_counts = A.take<int>((size_t)nc * nc);
+            temp1 = A.take<char>(t1);
+        }
+        put_vec(co.img_cluster, img_cluster, s_);
+        put_vec(co.clu_start, clu_start, s_);
+        const long long npairs = launch_coarse_count(b, count, off, temp1, t1, s_);
+        if (npairs <= 0 || npairs > (1LL << 31) - 1) {
+            co = CoarseBufs{};
+            return;
+        }
+        int lwork = 0;
+        if (cusolverDnSpotrf_bufferSize(ctx_.dn, CUBLAS_FILL_MODE_LOWER, Nc, co.A32, Nc, &lwork) !=
+            CUSOLVER_STATUS_SUCCESS)
+            throw Error(SFMBA_ERR_CUDA, "cusolverDnSpotrf_bufferSize failed");
+        const int max_groups = nc * (nc + 1) / 2;
+        const long long max_chunks = npairs / kCoarseChunk + max_groups + 1;
+        Arena &P = ctx_.pairs;
+        const size_t t2 = coarse_setup_temp_bytes(nP, npairs);
+        int *key = nullptr, *val = nullptr, *key2 = nullptr, *val_sorted = nullptr;
+        void *temp2 = nullptr;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) P.begin_sizing(); else P.commit();
+            key = P.take<int>(npairs);
+            val = P.take<int>(npairs);
+            key2 = P.take<int>(npairs);
+            val_sorted = P.take<int>(npairs);
+            temp2 = P.take<char>(t2);
+            co.group_cc = P.take<int2>(max_groups);
+            co.group_chunk_off = P.take<int>((size_t)max_groups + 1);
+            co.chunk = P.take<int4>(max_chunks);
+            co.chunk_part = P.take<double>((size_t)max_chunks * D * D);
+            co.work = P.take<float>((size_t)std::max(lwork, 1));
+        }
+        co.lwork = lwork;
+        co.nc = nc;
+        launch_coarse_group(b, off, npairs, key, val, key2, val_sorted, key_counts, temp2, t2, s_);
+        const std::vector<int> kc = fetch(key_counts, (size_t)nc * nc, true, s_);
+        std::vector<int2> gcc;
+        std::vector<int> goff{0};
+        std::vector<int4> chunks;
+        long long pos = 0;
+        for (int k = 0; k < nc * nc; ++k) {
+            const int cnt = kc[k];
+            if (cnt == 0) continue;
+            const int g = (int)gcc.size();
+            gcc.push_back(make_int2(k / nc, k % nc));
+            for (int a = 0; a < cnt; a += kCoarseChunk)
+                chunks.push_back(make_int4(g, (int)(pos + a), (int)(pos + std::min(cnt, a + kCoarseChunk)), 0));
+            goff.push_back((int)chunks.size());
+            pos += cnt;
+        }
+        co.pair_pt = val_sorted;
+        co.ngroups = (int)gcc.size();
+        co.nchunks = (int)chunks.size();
+        put_vec(co.group_cc, gcc, s_);
+        put_vec(co.group_chunk_off, goff, s_);
+        put_vec(co.chunk, chunks, s_);
+    }
+
+    // A_c for this retry, FP32 Cholesky and inverse; false (block-Jacobi
+    // alone for this retry) when the factorisation breaks down.
+    bool factor_coarse() {
+        Bufs &b = b_;
+        CoarseBufs &co = b.co;
+        if (co.nc == 0) return false;
+        const int Nc = co.nc * b.D;
+        { SFMBA_PHASE(PH_COARSE_ASSEMBLE); launch_coarse_assemble(b, s_); }
+        SFMBA_PHASE(PH_COARSE_FACTOR);
+        if (cusolverDnSetStream(ctx_.dn, s_) != CUSOLVER_STATUS_SUCCESS ||
+            cusolverDnSpotrf(ctx_.dn, CUBLAS_FILL_MODE_LOWER, Nc, co.A32, Nc, co.work, co.lwork, co.info) !=
+                CUSOLVER_STATUS_SUCCESS)
+            throw Error(SFMBA_ERR_CUDA, "cusolverDnSpotrf failed");
+        int info = -1;
+        SFMBA_CUDA(cudaMemcpyAsync(&info, co.info, sizeof(int), cudaMemcpyDeviceToHost, s_));
+        SFMBA_CUDA(cudaStreamSynchronize(s_));
+        if (info != 0) return false;
+        if (cusolverDnSpotrs(ctx_.dn, CUBLAS_FILL_MODE_LOWER, Nc, Nc, co.A32, Nc, co.Ainv, Nc, co.info) !=
+            CUSOLVER_STATUS_SUCCESS)
+            throw Error(SFMBA_ERR_CUDA, "cusolverDnSpotrs failed");
+        launch_coarse_symmetrize(b, s_);
+        return true;
+    }
+
     void read_state() {
         SFMBA_CUDA(cudaMemcpyAsync(ctx_.h_state, b_.state, sizeof(LMState), cudaMemcpyDeviceToHost, s_));
         SFMBA_CUDA(cudaStreamSynchronize(s_));
@@ -950,6 +1073,7 @@ class Solver {
                 }
                 b.nparts = off[nI];
                 put_vec(b.ipart_off, off, s_);
+                setup_coarse(o->pcg_coarse_clusters);
             }
             // Image-aligned chunks of the image-block passes.
             std::vector<int4> ia;
@@ -967,12 +1091,10 @@ class Solver {
             launch_mf_prepare(b, s_);
         }
         if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
-            size_t scan_need = 0;
             // pair count scan uses the sort temp (cub scan needs little)
             b.npairs = count_pairs(b, pair_scan, sort_temp, sort_tmp, s_);
             if (b.npairs > (1LL << 31) - 1)
                 throw Error(SFMBA_ERR_UNSUPPORTED, "too many observation pairs for the dense Schur path");
-            (void)scan_need;
             const size_t ptemp = pairs_temp_bytes(b.npairs, nI);
             Arena &P = ctx_.pairs;
             unsigned *ka = nullptr, *kb = nullptr;
@@ -1078,7 +1200,26 @@ class Solver {
                     }
                     { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
                 } else {
-                    { SFMBA_PHASE(PH_PCG_PRECOND); launch_mf_precond(b, s_); launch_pcg_start(b, s_); }
+                    bool coarse = false;
+                    if (b.co.nc > 0) {
+                        // The coarse inverse is refreshed when the damping has moved by 10x
+                        // or 4 outer iterations have passed since it was formed; in between
+                        // the previous one (still symmetric positive definite) is used.
+                        const double lam = hs.lambda;
+                        if (!coarse_valid_ || outer - coarse_outer_ >= 4 || lam < coarse_lambda_ * 0.1 ||
+                            lam > coarse_lambda_ * 10.0) {
+                            coarse_valid_ = factor_coarse();
+                            coarse_lambda_ = lam;
+                            coarse_outer_ = outer;
+                        }
+                        coarse = coarse_valid_;
+                    }
+                    {
+                        SFMBA_PHASE(PH_PCG_PRECOND);
+                        launch_mf_precond(b, s_);
+                        if (coarse) launch_coarse_correct(b, true, s_);
+                        launch_pcg_start(b, s_);
+                    }
                     const int maxit = std::max(1, o->pcg_max_iterations);
                     int vp = 0, vi = 0;  // launch variants of the two passes
                     if (o->kernel_variant > 0) {
@@ -1097,10 +1238,10 @@ class Solver {
                             for (int k = 0; k < m; ++k) {
                                 { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_, vp); }
                                 { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_, vi); launch_pcg_images_finish(b, s_); }
-                                { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, k & 1); }
+                                { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, k & 1, coarse); }
                             }
                         };
-                        pcg_chunk_.run(s_, m == kPcgPollEvery && !profiler().on, chunk);
+                        (coarse ? pcg_chunk_coarse_ : pcg_chunk_).run(s_, m == kPcgPollEvery && !profiler().on, chunk);
                         read_state();
                         if (hs.pcg_done) break;
                     }
@@ -1285,8 +1426,6 @@ class Solver {
     }
 
     const Bufs &bufs() const { return b_; }
-    cudaStream_t stream() const { return s_; }
-    Context &ctx() { return ctx_; }
 
   private:
     Context &ctx_;
@@ -1294,7 +1433,10 @@ class Solver {
     Bufs b_;
     WinBufs w_;
     Layout lay_;
-    Replay pcg_chunk_, retry_round_;
+    Replay pcg_chunk_, pcg_chunk_coarse_, retry_round_;
+    bool coarse_valid_ = false;  // the coarse inverse in b_.co.Ainv is usable
+    double coarse_lambda_ = 0.0;
+    int coarse_outer_ = 0;
     int solver_ = SFMBA_SOLVER_DENSE;
 };
 

@@ -239,3 +239,39 @@ def test_profile_report_counts_phases():
     native.profile_enable(False)
     assert rep["linearize"]["launches"] >= 1 and rep["cholesky"]["ms"] > 0
     assert rep["kernel_launches"] > 10
+
+
+@pytest.mark.parametrize("models", [(m,) for m in range(6)] + [(abi.PINHOLE, abi.SIMPLE_RADIAL, abi.OPENCV)],
+                         ids=[abi.MODEL_NAMES[m] for m in range(6)] + ["mixed"])
+def test_pcg_mixed_each_camera_model_reaches_oracle_cost(oracle_lib, models):
+    """The FP32 PCG passes are compiled with the camera model as a constant
+    when every camera shares it (one case per model) and keep the runtime
+    switch otherwise (mixed); each reaches the FP64 oracle's final cost to
+    1e-6 relative."""
+    p = scenes.local_window(np.random.default_rng(11), 24, 1500, models=models)
+    kw = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=2.0, max_iterations=40)
+    r = oracle_lib.bundle_adjust(p, **kw)
+    g = native.bundle_adjust_arrays(p, solver=abi.SOLVER_PCG, precision=abi.PRECISION_MIXED,
+                                    pcg_tolerance=1e-6, pcg_max_iterations=300, **kw)
+    assert g.solver_used == abi.SOLVER_PCG
+    assert g.final_cost <= r.final_cost * (1 + 1e-6), (g.final_cost, r.final_cost)
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_pcg_coarse_correction_cuts_iterations(precision):
+    """The coarse correction of the PCG preconditioner (clusters of
+    consecutive images, A_c = Z^T S Z) changes only the Krylov iteration:
+    solved tightly, both preconditioners follow the dense FP64 solve's LM
+    trajectory (itself held to the oracle by the tests above; same cost to
+    1e-6), and the two-level one needs fewer iterations on a long camera
+    sequence (283 cameras)."""
+    p = scenes.radial2000(seed=2, scale=0.02)
+    kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=6)
+    ref = native.bundle_adjust_arrays(p, solver=abi.SOLVER_DENSE, dense_max_dim=10000, **kw)
+    pk = dict(kw, solver=abi.SOLVER_PCG, precision=precision, pcg_tolerance=1e-6, pcg_max_iterations=3000)
+    bj = native.bundle_adjust_arrays(p, pcg_coarse_clusters=-1, **pk)
+    co = native.bundle_adjust_arrays(p, pcg_coarse_clusters=32, **pk)
+    assert ref.solver_used == abi.SOLVER_DENSE
+    for g in (bj, co):
+        assert abs(g.final_cost - ref.final_cost) <= 1e-6 * ref.final_cost, (g.final_cost, ref.final_cost)
+    assert co.linear_iterations < bj.linear_iterations, (co.linear_iterations, bj.linear_iterations)
