@@ -69,15 +69,11 @@ __global__ void k_coarse_emit(const int *pt_start, const int *ob_img, const int 
         }
 }
 
+// Size of every group: integer atomics, so the counts do not depend on the
+// order in which they land.
 __global__ void k_key_counts(const int *key, long long n, int *counts) {
-    // counts of each key in the sorted key array: boundaries of equal runs
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    if (t == 0 || key[t] != key[t - 1]) {
-        long long e = t + 1;
-        while (e < n && key[e] == key[t]) ++e;
-        counts[key[t]] = (int)(e - t);
-    }
+    if (t < n) atomicAdd(&counts[key[t]], 1);
 }
 
 // A_c = 0, then block (c, c) = sum over the cluster's images of

@@ -1202,12 +1202,12 @@ class Solver {
                 } else {
                     bool coarse = false;
                     if (b.co.nc > 0) {
-                        // The coarse inverse is refreshed when the damping has moved by 10x
-                        // or 4 outer iterations have passed since it was formed; in between
+                        // The coarse inverse is refreshed when the damping has moved by 100x
+                        // or 6 outer iterations have passed since it was formed; in between
                         // the previous one (still symmetric positive definite) is used.
                         const double lam = hs.lambda;
-                        if (!coarse_valid_ || outer - coarse_outer_ >= 4 || lam < coarse_lambda_ * 0.1 ||
-                            lam > coarse_lambda_ * 10.0) {
+                        if (!coarse_valid_ || outer - coarse_outer_ >= 6 || lam < coarse_lambda_ * 0.01 ||
+                            lam > coarse_lambda_ * 100.0) {
                             coarse_valid_ = factor_coarse();
                             coarse_lambda_ = lam;
                             coarse_outer_ = outer;
