@@ -69,11 +69,18 @@ __global__ void k_coarse_emit(const int *pt_start, const int *ob_img, const int 
         }
 }
 
-// Size of every group: integer atomics, so the counts do not depend on the
-// order in which they land.
+// Size of every group from the sorted keys: the first element of a run adds
+// -start and the last adds end + 1, so only two integer atomics per group
+// land on a counter (no contention on long runs) and the sum is exact.
 __global__ void k_key_counts(const int *key, long long n, int *counts) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t < n) atomicAdd(&counts[key[t]], 1);
+    if (t >= n) return;
+    const int k = key[t];
+    const bool first = t == 0 || key[t - 1] != k;
+    const bool last = t == n - 1 || key[t + 1] != k;
+    if (first && last) atomicAdd(&counts[k], 1);
+    else if (first) atomicAdd(&counts[k], -(int)t);
+    else if (last) atomicAdd(&counts[k], (int)(t + 1));
 }
 
 // A_c = 0, then block (c, c) = sum over the cluster's images of
