@@ -46,27 +46,30 @@ __device__ int point_clusters(const int *ob_img, const int *img_cluster, int s, 
 }
 
 __global__ void k_coarse_count(const int *pt_start, const int *ob_img, const int *img_cluster, int nP,
-                               long long *count) {
+                               long long *count, long long *kcount) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nP) return;
     int cl[kMaxCoarseClusters];
     const int k = point_clusters(ob_img, img_cluster, pt_start[p], pt_start[p + 1], cl);
     count[p] = (long long)k * (k + 1) / 2;
+    kcount[p] = k;
 }
 
 __global__ void k_coarse_emit(const int *pt_start, const int *ob_img, const int *img_cluster, int nP, int nc,
-                              const long long *off, int *key, int *val) {
+                              const long long *off, const long long *inc_off, int *key, int *val, int *inc_cl) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nP) return;
     int cl[kMaxCoarseClusters];
     const int k = point_clusters(ob_img, img_cluster, pt_start[p], pt_start[p + 1], cl);
     long long w = off[p];
-    for (int a = 0; a < k; ++a)
+    for (int a = 0; a < k; ++a) {
+        inc_cl[inc_off[p] + a] = cl[a];
         for (int b = a; b < k; ++b) {
             key[w] = cl[a] * nc + cl[b];
             val[w] = p;
             ++w;
         }
+    }
 }
 
 // Size of every group from the sorted keys: the first element of a run adds
@@ -104,6 +107,52 @@ __global__ void k_coarse_diag(const double *img_H, const int *img_active, const 
     }
 }
 
+// Y_c = sum over the point's observations in cluster c of Jx~^T Jc~ (3 x D,
+// row-major), one thread per point-cluster incidence, the observations
+// taken in the point's order; every point-cluster pair of the assembly then
+// reads its two Y instead of recomputing the Jacobians per pair.
+template <typename T, int D, bool RC, int M>
+__global__ void __launch_bounds__(128) k_coarse_y(JacSrc<T> J, const int *__restrict__ pt_start,
+                                                  const int *__restrict__ img_cluster,
+                                                  const long long *__restrict__ inc_off,
+                                                  const int *__restrict__ inc_cl, int nP, long long ninc,
+                                                  const unsigned char *__restrict__ pt_ok, T *__restrict__ Y) {
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= ninc) return;
+    int lo = 0, hi = nP - 1;  // the point of incidence j: last p with inc_off[p] <= j
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inc_off[mid] <= j) lo = mid;
+        else hi = mid - 1;
+    }
+    const int p = lo, c = inc_cl[j];
+    T y[3][D];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int d = 0; d < D; ++d) y[r][d] = T(0);
+    if (pt_ok[p]) {
+        for (int o = pt_start[p]; o < pt_start[p + 1]; ++o) {
+            const int4 rc = __ldg(J.obrec + o);
+            if (img_cluster[rc.x] != c) continue;
+            ObsOp<T, D, RC, M> op;
+            make_op_point_major<T, D, RC>(J, o, rc, op);
+            T jx[6], jc[2 * D];
+            op.jx_rows(jx);
+            op.jc_rows(jc);
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int d = 0; d < D; ++d) y[r][d] += jx[r] * jc[d] + jx[3 + r] * jc[D + d];
+        }
+    }
+    T *dst = Y + (size_t)j * 3 * D;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int d = 0; d < D; ++d) dst[r * D + d] = y[r][d];
+}
+
 // Chunk q of the pair groups: minus sum over its points of Y_c^T C^-1 Y_c'.
 // One warp per chunk; per round of 32 points lane t stages A_t = Y_c (3 x D)
 // and P_t = C^-1 Y_c' (3 x D); the D x D product over 3 x 32 inner terms is
@@ -112,9 +161,10 @@ __global__ void k_coarse_diag(const double *img_H, const int *img_active, const 
 template <typename T>
 constexpr int coarse_warps() { return sizeof(T) == 4 ? 4 : 2; }  // static shared memory under 48 KB
 
-template <typename T, int D, bool RC, int M>
-__global__ void __launch_bounds__(32 * coarse_warps<T>()) k_coarse_pairs(JacSrc<T> J, const int *__restrict__ pt_start,
-                                                      const int *__restrict__ img_cluster,
+template <typename T, int D>
+__global__ void __launch_bounds__(32 * coarse_warps<T>()) k_coarse_pairs(const T *__restrict__ Y,
+                                                      const long long *__restrict__ inc_off,
+                                                      const int *__restrict__ inc_cl,
                                                       const int4 *__restrict__ chunks, int nchunks,
                                                       const int *__restrict__ pair_pt,
                                                       const int2 *__restrict__ group_cc, const T *__restrict__ pt_Cinv,
@@ -139,47 +189,27 @@ __global__ void __launch_bounds__(32 * coarse_warps<T>()) k_coarse_pairs(JacSrc<
         for (int b = 0; b < CQ; ++b) acc[a][b] = comp[a][b] = T(0);
     for (int base = ch.y; base < ch.z; base += 32) {
         const int k = base + lane;
-        T ya[3][D], yb[3][D];
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < D; ++c) ya[r][c] = yb[r][c] = T(0);
         bool staged = false;
         if (k < ch.z) {
             const int p = pair_pt[k];
-            if (pt_ok[p]) {
-                for (int o = pt_start[p]; o < pt_start[p + 1]; ++o) {
-                    const int4 rc = __ldg(J.obrec + o);
-                    const int cl = img_cluster[rc.x];
-                    if (cl != cc.x && cl != cc.y) continue;
-                    ObsOp<T, D, RC, M> op;
-                    make_op_point_major<T, D, RC>(J, o, rc, op);
-                    T jx[6], jc[2 * D];
-                    op.jx_rows(jx);
-                    op.jc_rows(jc);
-                    if (cl == cc.x) {
-#pragma unroll
-                        for (int r = 0; r < 3; ++r)
-#pragma unroll
-                            for (int c = 0; c < D; ++c) ya[r][c] += jx[r] * jc[c] + jx[3 + r] * jc[D + c];
-                    }
-                    if (cl == cc.y) {
-#pragma unroll
-                        for (int r = 0; r < 3; ++r)
-#pragma unroll
-                            for (int c = 0; c < D; ++c) yb[r][c] += jx[r] * jc[c] + jx[3 + r] * jc[D + c];
-                    }
-                }
+            long long ia = inc_off[p], ib = ia;  // the point's incidences of clusters c and c'
+            const long long iend = inc_off[p + 1];
+            while (ia < iend && inc_cl[ia] != cc.x) ++ia;
+            ib = ia;
+            while (ib < iend && inc_cl[ib] != cc.y) ++ib;
+            if (pt_ok[p] && ib < iend) {
+                const T *ya = Y + (size_t)ia * 3 * D, *yb = Y + (size_t)ib * 3 * D;
                 const T *Ci = pt_Cinv + 6 * (size_t)p;
                 const T m00 = Ci[0], m01 = Ci[1], m02 = Ci[2], m11 = Ci[3], m12 = Ci[4], m22 = Ci[5];
 #pragma unroll
                 for (int c = 0; c < D; ++c) {
-                    sA[wl][lane][c] = ya[0][c];
-                    sA[wl][lane][D + c] = ya[1][c];
-                    sA[wl][lane][2 * D + c] = ya[2][c];
-                    sP[wl][lane][c] = m00 * yb[0][c] + m01 * yb[1][c] + m02 * yb[2][c];
-                    sP[wl][lane][D + c] = m01 * yb[0][c] + m11 * yb[1][c] + m12 * yb[2][c];
-                    sP[wl][lane][2 * D + c] = m02 * yb[0][c] + m12 * yb[1][c] + m22 * yb[2][c];
+                    const T b0 = yb[c], b1 = yb[D + c], b2 = yb[2 * D + c];
+                    sA[wl][lane][c] = ya[c];
+                    sA[wl][lane][D + c] = ya[D + c];
+                    sA[wl][lane][2 * D + c] = ya[2 * D + c];
+                    sP[wl][lane][c] = m00 * b0 + m01 * b1 + m02 * b2;
+                    sP[wl][lane][D + c] = m01 * b0 + m11 * b1 + m12 * b2;
+                    sP[wl][lane][2 * D + c] = m02 * b0 + m12 * b1 + m22 * b2;
                 }
                 staged = true;
             }
@@ -188,7 +218,7 @@ __global__ void __launch_bounds__(32 * coarse_warps<T>()) k_coarse_pairs(JacSrc<
 #pragma unroll
             for (int f = 0; f < 3 * D; ++f) sA[wl][lane][f] = sP[wl][lane][f] = T(0);
         }
-        __syncwarp();
+    __syncwarp();
         T pt[RH][CQ];
 #pragma unroll
         for (int a = 0; a < RH; ++a)
@@ -292,7 +322,16 @@ __global__ void __launch_bounds__(256) k_coarse_restrict(const T *__restrict__ r
     const int lane = threadIdx.x & 31;
     if (c >= nc || lane >= D) return;
     double s = 0.0;
-    for (int i = clu_start[c]; i < clu_start[c + 1]; ++i) s += (double)r[(size_t)i * D + lane];
+    const int i1 = clu_start[c + 1];
+    int i = clu_start[c];
+    for (; i + 8 <= i1; i += 8) {  // loads eight at a time, added in image order
+        T w[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w[u] = r[(size_t)(i + u) * D + lane];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += (double)w[u];
+    }
+    for (; i < i1; ++i) s += (double)r[(size_t)i * D + lane];
     zc[c * D + lane] = s;
 }
 
@@ -308,7 +347,19 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(const float *__restrict__ A
     if (row >= Nc) return;
     const float *a = Ainv + (size_t)row * Nc;
     double s = 0.0;
-    for (int j = lane; j < Nc; j += 32) s += (double)__ldg(a + j) * zc[j];
+    int j = lane;
+    for (; j + 7 * 32 < Nc; j += 8 * 32) {  // loads eight at a time, accumulated in column order
+        float w[8];
+        double y[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            w[u] = __ldg(a + j + 32 * u);
+            y[u] = zc[j + 32 * u];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += (double)w[u] * y[u];
+    }
+    for (; j < Nc; j += 32) s += (double)__ldg(a + j) * zc[j];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
     if (lane == 0) cc[row] = (T)s;
@@ -363,16 +414,20 @@ size_t coarse_setup_temp_bytes(int nP, long long npairs_max) {
     return std::max(a, bsz);
 }
 
-long long launch_coarse_count(const Bufs &b, long long *count, long long *off, void *temp, size_t temp_bytes,
-                              cudaStream_t s) {
+long long launch_coarse_count(const Bufs &b, long long *count, long long *off, long long *kcount,
+                              long long *inc_off, long long *ninc, void *temp, size_t temp_bytes, cudaStream_t s) {
+    *ninc = 0;
     if (b.nP == 0) return 0;
-    k_coarse_count<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, b.ob_img, b.co.img_cluster, b.nP, count);
+    k_coarse_count<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, b.ob_img, b.co.img_cluster, b.nP, count, kcount);
     SFMBA_LAUNCH_CHECK();
     size_t tb = temp_bytes;
     SFMBA_CUDA(cub::DeviceScan::ExclusiveSum(temp, tb, count, off, b.nP, s));
+    tb = temp_bytes;
+    SFMBA_CUDA(cub::DeviceScan::ExclusiveSum(temp, tb, kcount, inc_off, b.nP + 1, s));  // kcount[nP] = 0
     long long last_off = 0, last_cnt = 0;
     SFMBA_CUDA(cudaMemcpyAsync(&last_off, off + b.nP - 1, sizeof(long long), cudaMemcpyDeviceToHost, s));
     SFMBA_CUDA(cudaMemcpyAsync(&last_cnt, count + b.nP - 1, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    SFMBA_CUDA(cudaMemcpyAsync(ninc, inc_off + b.nP, sizeof(long long), cudaMemcpyDeviceToHost, s));
     SFMBA_CUDA(cudaStreamSynchronize(s));
     return last_off + last_cnt;
 }
@@ -380,7 +435,8 @@ long long launch_coarse_count(const Bufs &b, long long *count, long long *off, v
 void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, int *key, int *val, int *key2,
                          int *val_sorted, int *key_counts, void *temp, size_t temp_bytes, cudaStream_t s) {
     const int nc = b.co.nc;
-    k_coarse_emit<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, b.ob_img, b.co.img_cluster, b.nP, nc, off, key, val);
+    k_coarse_emit<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, b.ob_img, b.co.img_cluster, b.nP, nc, off,
+                                                    b.co.inc_off, key, val, b.co.inc_cl);
     SFMBA_LAUNCH_CHECK();
     size_t tb = temp_bytes;
     int bits = 1;
@@ -400,14 +456,24 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
     if (co.nchunks > 0) {
         dispatch_D(D, [&](auto dc) {
             constexpr int DD = decltype(dc)::value;
-            if (b.mixed)
-                k_coarse_pairs<float, DD, true, -1><<<div_up(co.nchunks, 4), 128, 0, s>>>(
-                    jac_src<float>(b), b.pt_start, co.img_cluster, co.chunk, co.nchunks, co.pair_pt,
-                    co.group_cc, (const float *)b.pt_Cinv, b.pt_ok, co.chunk_part);
-            else
-                k_coarse_pairs<double, DD, false, -1><<<div_up(co.nchunks, 2), 64, 0, s>>>(
-                    jac_src<double>(b), b.pt_start, co.img_cluster, co.chunk, co.nchunks, co.pair_pt,
-                    co.group_cc, (const double *)b.pt_Cinv, b.pt_ok, co.chunk_part);
+            const unsigned yb = (unsigned)div_up(co.ninc, 128);
+            if (b.mixed) {
+                k_coarse_y<float, DD, true, -1><<<yb, 128, 0, s>>>(jac_src<float>(b), b.pt_start, co.img_cluster,
+                                                                   co.inc_off, co.inc_cl, b.nP, co.ninc, b.pt_ok,
+                                                                   (float *)co.ybuf);
+                SFMBA_LAUNCH_CHECK();
+                k_coarse_pairs<float, DD><<<div_up(co.nchunks, 4), 128, 0, s>>>(
+                    (const float *)co.ybuf, co.inc_off, co.inc_cl, co.chunk, co.nchunks, co.pair_pt, co.group_cc,
+                    (const float *)b.pt_Cinv, b.pt_ok, co.chunk_part);
+            } else {
+                k_coarse_y<double, DD, false, -1><<<yb, 128, 0, s>>>(jac_src<double>(b), b.pt_start, co.img_cluster,
+                                                                     co.inc_off, co.inc_cl, b.nP, co.ninc, b.pt_ok,
+                                                                     (double *)co.ybuf);
+                SFMBA_LAUNCH_CHECK();
+                k_coarse_pairs<double, DD><<<div_up(co.nchunks, 2), 64, 0, s>>>(
+                    (const double *)co.ybuf, co.inc_off, co.inc_cl, co.chunk, co.nchunks, co.pair_pt, co.group_cc,
+                    (const double *)b.pt_Cinv, b.pt_ok, co.chunk_part);
+            }
         });
         SFMBA_LAUNCH_CHECK();
         k_coarse_finish<<<co.ngroups, 128, 0, s>>>(co.chunk_part, co.group_chunk_off, co.group_cc, co.ngroups, co.nc,

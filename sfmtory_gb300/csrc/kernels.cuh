@@ -17,6 +17,10 @@ struct CoarseBufs {
     int *img_cluster = nullptr;       // [nI]
     int *clu_start = nullptr;         // [nc+1] first image of each cluster (consecutive images)
     int *pair_pt = nullptr;           // points of the point-cluster pairs, grouped by cluster pair
+    long long ninc = 0;               // point-cluster incidences (a point's distinct clusters)
+    long long *inc_off = nullptr;     // [nP+1] first incidence of each point
+    int *inc_cl = nullptr;            // [ninc] cluster of each incidence, increasing within a point
+    void *ybuf = nullptr;             // [ninc][3*D] Y_c of each incidence, element type of the linearisation
     int ngroups = 0;
     int2 *group_cc = nullptr;         // [ngroups] (c, c'), c <= c'
     int *group_chunk_off = nullptr;   // [ngroups+1]
@@ -280,10 +284,12 @@ void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
 
 // ---- coarse correction of the PCG preconditioner (k_coarse.cu)
 size_t coarse_setup_temp_bytes(int nP, long long npairs_max);
-// Pairs count per point (exclusive-scanned into off); returns the total.
-long long launch_coarse_count(const Bufs &b, long long *count, long long *off, void *temp, size_t temp_bytes,
-                              cudaStream_t s);
-// Emits and sorts the point-cluster pairs; key_counts[c * nc + c'] = group sizes.
+// Pairs count per point (exclusive-scanned into off) and distinct clusters
+// per point (scanned into inc_off, total in *ninc); returns the pair total.
+long long launch_coarse_count(const Bufs &b, long long *count, long long *off, long long *kcount,
+                              long long *inc_off, long long *ninc, void *temp, size_t temp_bytes, cudaStream_t s);
+// Emits and sorts the point-cluster pairs; key_counts[c * nc + c'] = group
+// sizes; the clusters of every incidence into b.co.inc_cl.
 void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, int *key, int *val, int *key2,
                          int *val_sorted, int *key_counts, void *temp, size_t temp_bytes, cudaStream_t s);
 // A_c for the current damping and point inverses; FP32 copy and Ainv = I for the factorisation.

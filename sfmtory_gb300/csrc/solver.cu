@@ -706,10 +706,10 @@ class Solver {
         if (cusolverDnSetStream(ctx_.dn, s_) != CUSOLVER_STATUS_SUCCESS)
             throw Error(SFMBA_ERR_CUDA, "cusolverDnSetStream failed");
         Arena &A = ctx_.coarse;
-        long long *count = nullptr, *off = nullptr;
+        long long *count = nullptr, *off = nullptr, *kcount = nullptr;
         int *key_counts = nullptr;
         void *temp1 = nullptr;
-        const size_t t1 = coarse_setup_temp_bytes(nP, 1);
+        const size_t t1 = coarse_setup_temp_bytes(nP + 1, 1);
         for (int pass = 0; pass < 2; ++pass) {
             if (pass == 0) A.begin_sizing(); else A.commit();
             co.img_cluster = A.take<int>(nI);
@@ -722,13 +722,17 @@ class Solver {
             co.info = A.take<int>(1);
             count = A.take<long long>((size_t)nP + 1);
             off = A.take<long long>((size_t)nP + 1);
+            kcount = A.take<long long>((size_t)nP + 1);
+            co.inc_off = A.take<long long>((size_t)nP + 1);
             key_counts = A.take<int>((size_t)nc * nc);
             temp1 = A.take<char>(t1);
         }
         put_vec(co.img_cluster, img_cluster, s_);
         put_vec(co.clu_start, clu_start, s_);
-        const long long npairs = launch_coarse_count(b, count, off, temp1, t1, s_);
-        if (npairs <= 0 || npairs > (1LL << 31) - 1) {
+        SFMBA_CUDA(cudaMemsetAsync(kcount + nP, 0, sizeof(long long), s_));
+        long long ninc = 0;
+        const long long npairs = launch_coarse_count(b, count, off, kcount, co.inc_off, &ninc, temp1, t1, s_);
+        if (npairs <= 0 || npairs > (1LL << 31) - 1 || ninc <= 0) {
             co = CoarseBufs{};
             return;
         }
@@ -754,7 +758,10 @@ class Solver {
             co.chunk = P.take<int4>(max_chunks);
             co.chunk_part = P.take<double>((size_t)max_chunks * D * D);
             co.work = P.take<float>((size_t)std::max(lwork, 1));
+            co.inc_cl = P.take<int>(ninc);
+            co.ybuf = P.take<double>((size_t)ninc * 3 * D);  // FP64-sized: an FP64 polish reuses it
         }
+        co.ninc = ninc;
         co.lwork = lwork;
         co.nc = nc;
         launch_coarse_group(b, off, npairs, key, val, key2, val_sorted, key_counts, temp2, t2, s_);
