@@ -9,6 +9,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace sfmba {
 
@@ -369,6 +370,56 @@ __device__ __forceinline__ bool residual64_rt(const double *rt, int model, const
     const double iz = 1.0 / pc2;
     double u, v;
     project64<M>(model, c, pc0 * iz, pc1 * iz, u, v);
+    rx = u - ox;
+    ry = v - oy;
+    return true;
+}
+
+// project64 in double-float arithmetic, operation for operation, for the
+// five models without a transcendental (OPENCV_FISHEYE stays in FP64).
+// c: the camera's parameters as pairs.
+template <int M = -1>
+__device__ __forceinline__ void project_df(int model, const dfl *c, dfl xn, dfl yn, dfl &u, dfl &v) {
+    if constexpr (M >= 0) model = M;
+    const dfl one = df_make(1.f);
+    switch (model) {
+    case SFMBA_SIMPLE_PINHOLE: u = c[0] * xn + c[1]; v = c[0] * yn + c[2]; break;
+    case SFMBA_PINHOLE: u = c[0] * xn + c[2]; v = c[1] * yn + c[3]; break;
+    case SFMBA_SIMPLE_RADIAL: {
+        const dfl r2 = xn * xn + yn * yn, d = one + c[3] * r2;
+        u = c[0] * (xn * d) + c[1]; v = c[0] * (yn * d) + c[2];
+        break;
+    }
+    case SFMBA_RADIAL: {
+        const dfl r2 = xn * xn + yn * yn, d = one + c[3] * r2 + c[4] * r2 * r2;
+        u = c[0] * (xn * d) + c[1]; v = c[0] * (yn * d) + c[2];
+        break;
+    }
+    default: {  // SFMBA_OPENCV
+        const dfl r2 = xn * xn + yn * yn, rad = one + c[4] * r2 + c[5] * r2 * r2;
+        const dfl xy = xn * yn;
+        const dfl xd = xn * rad + df_scale2(c[6], 2.f) * xy + c[7] * (r2 + df_scale2(xn * xn, 2.f));
+        const dfl yd = yn * rad + c[6] * (r2 + df_scale2(yn * yn, 2.f)) + df_scale2(c[7], 2.f) * xy;
+        u = c[0] * xd + c[2]; v = c[1] * yd + c[3];
+        break;
+    }
+    }
+}
+
+// residual64_rt in double-float arithmetic: rt as 12 pairs (R row-major,
+// then t), the point and the observation as pairs.
+template <int M = -1>
+__device__ __forceinline__ bool residual_df(const dfl *rt, int model, const dfl *c, dfl X0, dfl X1, dfl X2, dfl ox,
+                                            dfl oy, dfl &rx, dfl &ry) {
+    const dfl pc0 = rt[0] * X0 + rt[1] * X1 + rt[2] * X2 + rt[9];
+    const dfl pc1 = rt[3] * X0 + rt[4] * X1 + rt[5] * X2 + rt[10];
+    const dfl pc2 = rt[6] * X0 + rt[7] * X1 + rt[8] * X2 + rt[11];
+    // pc2 > kMinDepth, decided in FP64 only near the threshold
+    const bool front = pc2.hi > 2e-9f ? true : pc2.hi < 5e-10f ? false : df_to_double(pc2) > kMinDepth;
+    if (!front) return false;
+    const dfl iz = df_recip(pc2);
+    dfl u, v;
+    project_df<M>(model, c, pc0 * iz, pc1 * iz, u, v);
     rx = u - ox;
     ry = v - oy;
     return true;

@@ -396,6 +396,111 @@ __global__ void __launch_bounds__(256) k_cost(const double *rt, const double *ca
     }
 }
 
+// The FP32 path's cost (mode 0): k_cost with the projection chain in
+// double-float arithmetic on the FP32 pipe; robust weights, the depth test
+// near its threshold and the block sums stay FP64. The per-thread sum of
+// squared norms is carried as a pair and added to FP64 once per thread.
+template <int M>
+__global__ void __launch_bounds__(256) k_cost_df(const float *rt_df, const float *cams_df, const float4 *pts_df,
+                                                 const int *cam_of_img, const int *cam_model, const int *ob_img,
+                                                 const int *ob_pt, const float4 *xy_df, long long nO, int loss,
+                                                 double scale, double *partials, long long *count_partials,
+                                                 float4 *rs_out) {
+    dfl sum2 = df_make(0.f);
+    double wsum = 0.0;
+    long long cnt = 0;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < nO;
+         o += (long long)gridDim.x * blockDim.x) {
+        const int i = ob_img[o], p = ob_pt[o];
+        const int c = cam_of_img[i];
+        dfl rt[12], cp[8];
+        const float4 *r4 = reinterpret_cast<const float4 *>(rt_df + 24 * (size_t)i);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float4 v = __ldg(r4 + k);
+            rt[2 * k] = {v.x, v.y};
+            rt[2 * k + 1] = {v.z, v.w};
+        }
+        const float4 *c4 = reinterpret_cast<const float4 *>(cams_df + 16 * (size_t)c);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 v = __ldg(c4 + k);
+            cp[2 * k] = {v.x, v.y};
+            cp[2 * k + 1] = {v.z, v.w};
+        }
+        const float4 pa = pts_df[2 * (size_t)p], pb = pts_df[2 * (size_t)p + 1];
+        const float4 xy = xy_df[o];
+        dfl rx, ry;
+        const bool ok = residual_df<M>(rt, M >= 0 ? M : cam_model[c], cp, {pa.x, pa.y}, {pa.z, pa.w}, {pb.x, pb.y},
+                                       {xy.x, xy.y}, {xy.z, xy.w}, rx, ry);
+        const dfl n2 = ok ? rx * rx + ry * ry : df_make(0.f);
+        float sw = 1.f;
+        if (ok && loss != SFMBA_LOSS_NONE) {
+            const double n2d = df_to_double(n2), n = sqrt(n2d), w = robust_weight<double>(n, loss, scale);
+            sw = (float)sqrt(w);
+            wsum += w * n * n;
+        }
+        if (rs_out)  // residual and sqrt(weight) for the next linearisation's gradient terms
+            rs_out[o] = ok ? make_float4(rx.hi, ry.hi, sw, 1.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ok) {
+            if (loss == SFMBA_LOSS_NONE) sum2 = sum2 + n2;
+            ++cnt;
+        }
+    }
+    __shared__ double ssum[256];
+    __shared__ long long scnt[256];
+    ssum[threadIdx.x] = df_to_double(sum2) + wsum;
+    scnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            ssum[threadIdx.x] += ssum[threadIdx.x + w];
+            scnt[threadIdx.x] += scnt[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = ssum[0];
+        count_partials[blockIdx.x] = scnt[0];
+    }
+}
+
+// Pairs of the points, pose matrices and camera parameters the cost
+// evaluates: threads [0, nP) points, then nI * 12 pose entries, then nC * 8
+// camera parameters.
+__global__ void k_split_df(const double *points, int nP, const double *rt64, int nI, const double *cams, int nC,
+                           float4 *pts_df, float *rt_df, float *cams_df) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < nP) {
+        const double *X = points + 3 * (size_t)t;
+        const dfl x = df_from(X[0]), y = df_from(X[1]), z = df_from(X[2]);
+        pts_df[2 * t] = make_float4(x.hi, x.lo, y.hi, y.lo);
+        pts_df[2 * t + 1] = make_float4(z.hi, z.lo, 0.f, 0.f);
+        return;
+    }
+    t -= nP;
+    if (t < 12LL * nI) {
+        const dfl v = df_from(rt64[t]);
+        rt_df[2 * t] = v.hi;
+        rt_df[2 * t + 1] = v.lo;
+        return;
+    }
+    t -= 12LL * nI;
+    if (t < 8LL * nC) {
+        const dfl v = df_from(cams[t]);
+        cams_df[2 * t] = v.hi;
+        cams_df[2 * t + 1] = v.lo;
+    }
+}
+
+__global__ void k_split_xy_df(const double2 *xy, long long nO, float4 *xy_df) {
+    const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (o >= nO) return;
+    const double2 v = xy[o];
+    const dfl x = df_from(v.x), y = df_from(v.y);
+    xy_df[o] = make_float4(x.hi, x.lo, y.hi, y.lo);
+}
+
 __global__ void k_cost_finalize(const double *partials, const long long *count_partials, int nb,
                                 double *out, long long *out_count) {
     __shared__ double ssum[256];
@@ -649,6 +754,12 @@ void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t 
     }
 }
 
+void launch_split_xy_df(const Bufs &b, cudaStream_t s) {
+    if (!b.df_cost || b.nO == 0) return;
+    k_split_xy_df<<<div_up(b.nO, 256), 256, 0, s>>>(b.ob_xy, b.nO, b.ob_xy_df);
+    SFMBA_LAUNCH_CHECK();
+}
+
 void launch_pose_rt64(const double *poses, int nI, double *rt, cudaStream_t s) {
     if (nI == 0) return;
     k_pose_rt64<<<div_up(nI, 128), 128, 0, s>>>(poses, nI, rt);
@@ -658,9 +769,33 @@ void launch_pose_rt64(const double *poses, int nI, double *rt, cudaStream_t s) {
 static void cost_impl(const Bufs &b, bool trial, int mode, double *out, long long *out_count,
                       cudaStream_t s, float4 *rs_out = nullptr) {
     launch_pose_rt64(trial ? b.poses_trial : b.poses, b.nI, b.img_rt64, s);
+    const double *cams = trial ? b.cams_trial : b.cams, *points = trial ? b.points_trial : b.points;
+    if (mode == 0 && b.mixed && b.df_cost) {
+        const long long nsplit = (long long)b.nP + 12LL * b.nI + 8LL * b.nC;
+        k_split_df<<<div_up(nsplit, 256), 256, 0, s>>>(points, b.nP, b.img_rt64, b.nI, cams, b.nC, b.pts_df, b.rt_df,
+                                                       b.cams_df);
+        SFMBA_LAUNCH_CHECK();
+        auto run_df = [&](auto mc) {
+            k_cost_df<decltype(mc)::value><<<kCostBlocks, 256, 0, s>>>(
+                b.rt_df, b.cams_df, b.pts_df, b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt, b.ob_xy_df, b.nO, b.loss,
+                b.loss_scale, b.partials, b.count_partials, rs_out);
+        };
+        switch (b.uniform_model) {
+        case SFMBA_SIMPLE_PINHOLE: run_df(std::integral_constant<int, SFMBA_SIMPLE_PINHOLE>()); break;
+        case SFMBA_PINHOLE: run_df(std::integral_constant<int, SFMBA_PINHOLE>()); break;
+        case SFMBA_SIMPLE_RADIAL: run_df(std::integral_constant<int, SFMBA_SIMPLE_RADIAL>()); break;
+        case SFMBA_RADIAL: run_df(std::integral_constant<int, SFMBA_RADIAL>()); break;
+        case SFMBA_OPENCV: run_df(std::integral_constant<int, SFMBA_OPENCV>()); break;
+        default: run_df(std::integral_constant<int, -1>()); break;
+        }
+        SFMBA_LAUNCH_CHECK();
+        k_cost_finalize<<<1, 256, 0, s>>>(b.partials, b.count_partials, kCostBlocks, out, out_count);
+        SFMBA_LAUNCH_CHECK();
+        return;
+    }
     auto run = [&](auto mc) {
         k_cost<decltype(mc)::value><<<kCostBlocks, 256, 0, s>>>(
-            b.img_rt64, trial ? b.cams_trial : b.cams, trial ? b.points_trial : b.points, b.cam_of_img, b.cam_model,
+            b.img_rt64, cams, points, b.cam_of_img, b.cam_model,
             b.ob_img, b.ob_pt, b.ob_xy, b.nO, b.loss, b.loss_scale, mode, b.partials, b.count_partials, rs_out);
     };
     switch (b.uniform_model) {

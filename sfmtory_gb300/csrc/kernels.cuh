@@ -103,6 +103,12 @@ struct Bufs {
     LMState *state = nullptr;
     double *partials = nullptr;   // [kCostBlocks*2]
     double *img_rt64 = nullptr;   // [nI][12] FP64 R (row-major) and t of the poses the cost evaluates
+    // Double-float copies for the FP32 path's cost (no OPENCV_FISHEYE camera):
+    int df_cost = 0;
+    float4 *ob_xy_df = nullptr;   // [nO] {x hi, x lo, y hi, y lo}
+    float4 *pts_df = nullptr;     // [nP][2] {x hi, x lo, y hi, y lo}, {z hi, z lo, 0, 0}
+    float *rt_df = nullptr;       // [nI][24] img_rt64 as pairs
+    float *cams_df = nullptr;     // [nC][16] camera parameters as pairs
     long long *count_partials = nullptr;
     // PCG (matrix-free) vectors, [nI*D] each, element type T
     void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
@@ -234,6 +240,8 @@ void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t 
 // cost of (poses, cams, points) or of the trial buffers, into state->cost/trial_cost
 void launch_cost(const Bufs &b, bool trial, bool into_trial, cudaStream_t s);
 // FP64 rotation matrix and translation of every pose ([nI][12]) for the cost.
+// Double-float copy of the observations for the FP32 path's cost (b.df_cost).
+void launch_split_xy_df(const Bufs &b, cudaStream_t s);
 void launch_pose_rt64(const double *poses, int nI, double *rt, cudaStream_t s);
 void launch_mean_error(const Bufs &b, cudaStream_t s);  // -> partials; host finalises
 void launch_accept(const Bufs &b, cudaStream_t s);

@@ -946,6 +946,14 @@ class Solver {
             b.state = A.take<LMState>(1);
             b.partials = A.take<double>(kCostBlocks);
             b.img_rt64 = A.take<double>((size_t)nI * 12 + 1);
+            // Double-float cost buffers: FP32 single-problem path, no fisheye camera.
+            bool df = mixed && !batch;
+            for (int c = 0; c < nC && df; ++c) df = model[c] != SFMBA_OPENCV_FISHEYE;
+            b.df_cost = df ? 1 : 0;
+            b.ob_xy_df = df ? A.take<float4>(nO) : nullptr;
+            b.pts_df = df ? A.take<float4>((size_t)nP * 2) : nullptr;
+            b.rt_df = df ? A.take<float>((size_t)nI * 24 + 4) : nullptr;
+            b.cams_df = df ? A.take<float>((size_t)nC * 16 + 4) : nullptr;
             b.count_partials = A.take<long long>(kCostBlocks);
             d_bad = A.take<int>(1);
             if (!device) {
@@ -1067,6 +1075,7 @@ class Solver {
             src_pt = obs_pt_new;
         }
         sort_observations(src_pt, src_img, src_xy, nO, nP, nI, b, sort_temp, sort_tmp, k1, v1, k2, v2, s_);
+        launch_split_xy_df(b, s_);
         SFMBA_CUDA(cudaMemsetAsync(b.state, 0, sizeof(LMState), s_));
         if (need_system) {
             std::vector<int> img_start = fetch(b.img_start, (size_t)nI + 1, true, s_);

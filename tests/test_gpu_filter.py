@@ -7,8 +7,9 @@ the filter drops only the two points behind their cameras: the second
 adjustment then starts at the first one's minimum, where the cost is flat
 along the weak focal/depth directions and summation-order differences move
 the parameters by ~1e-5 while the cost agrees to 1e-6); FP32 path - final
-cost 1e-6 relative when the kept sets agree (observations within rounding
-of the threshold may flip; at most 0.1 % of them)."""
+cost 1e-6 relative with the FP64 polish, 1e-5 without, when the kept sets
+agree (observations within rounding of the threshold may flip; at most
+0.1 % of them)."""
 import numpy as np
 import pytest
 
@@ -37,14 +38,22 @@ def test_filter_fp64_matches_oracle(oracle_lib, threshold):
     _params_close(g, r, 1e-6 if threshold == 3.0 else 1e-4)
 
 
-def test_filter_mixed_reaches_oracle_cost(oracle_lib):
+@pytest.mark.parametrize("polish", [0, 1])
+def test_filter_mixed_reaches_oracle_cost(oracle_lib, polish):
+    """With the FP64 polish the FP32 path's final cost is the oracle's to
+    1e-6. Without it the FP32 loop stops where its own Huber-weighted
+    relative decrease falls below 1e-6, which on this flat 47-camera
+    problem lands within 1e-5 of the FP64 minimum (rounding-level changes
+    move that stopping point)."""
     p = scenes.opencv47(seed=4, scale=0.05)
     g, gk = native.filter_and_reoptimize_arrays(p, 3.0, precision=abi.PRECISION_MIXED, solver=abi.SOLVER_DENSE,
-                                                **KW)
+                                                fp64_polish=polish, **KW)
     r, rk = oracle_lib.filter_and_reoptimize(p, 3.0, **KW)
     assert (gk != rk).sum() <= max(1, p.num_observations // 1000)
     if np.array_equal(gk, rk):
-        assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost
+        bar = 1e-6 if polish else 1e-5
+        assert g.final_cost <= r.final_cost * (1 + bar), (g.final_cost, r.final_cost)
+        assert g.final_cost >= r.final_cost * (1 - 1e-6), (g.final_cost, r.final_cost)
 
 
 def test_filter_stops_below_twelve_observations(oracle_lib):

@@ -275,3 +275,21 @@ def test_pcg_coarse_correction_cuts_iterations(precision):
     for g in (bj, co):
         assert abs(g.final_cost - ref.final_cost) <= 1e-6 * ref.final_cost, (g.final_cost, ref.final_cost)
     assert co.linear_iterations < bj.linear_iterations, (co.linear_iterations, bj.linear_iterations)
+
+
+@pytest.mark.parametrize("models", [(m,) for m in range(6)] + [(abi.PINHOLE, abi.SIMPLE_RADIAL, abi.OPENCV)],
+                         ids=[abi.MODEL_NAMES[m] for m in range(6)] + ["mixed"])
+@pytest.mark.parametrize("loss", [abi.LOSS_NONE, abi.LOSS_HUBER])
+def test_mixed_cost_double_float_matches_fp64(oracle_lib, models, loss):
+    """The FP32 path evaluates the cost with the projection in double-float
+    arithmetic (FP32 pairs; OPENCV_FISHEYE cameras keep FP64): its initial
+    cost is the FP64 oracle's to 1e-10 relative, and the final cost it
+    reports is the FP64 cost of the parameters it returns to 1e-10."""
+    p = scenes.local_window(np.random.default_rng(12), 24, 1500, models=models)
+    kw = dict(robust_loss=loss, loss_scale_px=2.0)
+    ref0 = oracle_lib.total_cost(p, **kw)
+    g = native.bundle_adjust_arrays(p, solver=abi.SOLVER_PCG, precision=abi.PRECISION_MIXED, max_iterations=4, **kw)
+    assert abs(g.initial_cost - ref0) <= 1e-10 * ref0, (g.initial_cost, ref0)
+    out = p.copy(poses=g.poses, points=g.points, camera_params=g.camera_params)
+    ref1 = oracle_lib.total_cost(out, **kw)
+    assert abs(g.final_cost - ref1) <= 1e-10 * ref1, (g.final_cost, ref1)
