@@ -576,6 +576,73 @@ __global__ void __launch_bounds__(256) k_wb_cost_partials(
     }
 }
 
+// k_wb_cost_partials for the FP32 batch with the projection in double-float
+// arithmetic (the pair copies of b.df_cost; robust weights and block sums
+// FP64), as the single-problem FP32 cost.
+__global__ void __launch_bounds__(256) k_wb_cost_partials_df(
+    const float *rt_df, const float *cams_df, const float4 *pts_df, const int *cam_of_img, const int *cam_model,
+    const int *ob_img, const int *ob_pt, const float4 *xy_df, const int *cblk_win, const long long *cblk_lo,
+    int loss, double scale, int trial, const WinState *ws, double *cpart, long long *cpart_n, float4 *rs_out) {
+    __shared__ double ssum[256];
+    __shared__ long long scnt[256];
+    const int blk = blockIdx.x;
+    const int w = cblk_win[blk];
+    if (trial && !(ws[w].active && !ws[w].factor_failed)) return;
+    dfl sum2 = df_make(0.f);
+    double wsum = 0.0;
+    long long cnt = 0;
+    for (long long o = cblk_lo[blk] + threadIdx.x; o < cblk_lo[blk + 1]; o += blockDim.x) {
+        const int i = ob_img[o], p = ob_pt[o];
+        const int c = cam_of_img[i];
+        dfl rt[12], cp[8];
+        const float4 *r4 = reinterpret_cast<const float4 *>(rt_df + 24 * (size_t)i);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float4 v = __ldg(r4 + k);
+            rt[2 * k] = {v.x, v.y};
+            rt[2 * k + 1] = {v.z, v.w};
+        }
+        const float4 *c4 = reinterpret_cast<const float4 *>(cams_df + 16 * (size_t)c);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 v = __ldg(c4 + k);
+            cp[2 * k] = {v.x, v.y};
+            cp[2 * k + 1] = {v.z, v.w};
+        }
+        const float4 pa = pts_df[2 * (size_t)p], pb = pts_df[2 * (size_t)p + 1];
+        const float4 xy = xy_df[o];
+        dfl rx, ry;
+        const bool ok = residual_df(rt, cam_model[c], cp, {pa.x, pa.y}, {pa.z, pa.w}, {pb.x, pb.y}, {xy.x, xy.y},
+                                    {xy.z, xy.w}, rx, ry);
+        float sw = 1.f;
+        if (ok) {
+            const dfl n2 = rx * rx + ry * ry;
+            if (loss == SFMBA_LOSS_NONE) sum2 = sum2 + n2;
+            else {
+                const double nn = sqrt(df_to_double(n2)), wt = robust_weight<double>(nn, loss, scale);
+                wsum += wt * nn * nn;
+                sw = (float)sqrt(wt);
+            }
+            ++cnt;
+        }
+        if (rs_out) rs_out[o] = ok ? make_float4(rx.hi, ry.hi, sw, 1.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    ssum[threadIdx.x] = df_to_double(sum2) + wsum;
+    scnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            ssum[threadIdx.x] += ssum[threadIdx.x + h];
+            scnt[threadIdx.x] += scnt[threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        cpart[blk] = ssum[0];
+        cpart_n[blk] = scnt[0];
+    }
+}
+
 __global__ void k_wb_cost_finalize(const int *wblk_start, const double *cpart, const long long *cpart_n, int W,
                                    int trial, WinState *ws) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
@@ -993,7 +1060,15 @@ void launch_wb_scatter(const Bufs &b, const WinBufs &w, cudaStream_t s) {
 }
 
 void launch_wb_cost(const Bufs &b, const WinBufs &w, bool trial, cudaStream_t s) {
-    if (w.ncblk > 0) {
+    if (w.ncblk > 0 && b.mixed && b.df_cost) {
+        launch_pose_rt64(trial ? b.poses_trial : b.poses, b.nI, b.img_rt64, s);
+        launch_split_df(b, trial, s);
+        k_wb_cost_partials_df<<<w.ncblk, 256, 0, s>>>(
+            b.rt_df, b.cams_df, b.pts_df, b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt, b.ob_xy_df, w.cblk_win,
+            w.cblk_lo, b.loss, b.loss_scale, trial ? 1 : 0, w.ws, w.cpart, w.cpart_n,
+            b.ob_rs ? (trial ? b.ob_rs_trial : b.ob_rs) : nullptr);
+        SFMBA_LAUNCH_CHECK();
+    } else if (w.ncblk > 0) {
         launch_pose_rt64(trial ? b.poses_trial : b.poses, b.nI, b.img_rt64, s);
         k_wb_cost_partials<<<w.ncblk, 256, 0, s>>>(
             b.img_rt64, trial ? b.cams_trial : b.cams, trial ? b.points_trial : b.points,

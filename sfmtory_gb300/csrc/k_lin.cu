@@ -754,6 +754,15 @@ void launch_update_images(const Bufs &b, const double *delta_slot, cudaStream_t 
     }
 }
 
+void launch_split_df(const Bufs &b, bool trial, cudaStream_t s) {
+    const long long nsplit = (long long)b.nP + 12LL * b.nI + 8LL * b.nC;
+    if (nsplit == 0) return;
+    k_split_df<<<div_up(nsplit, 256), 256, 0, s>>>(trial ? b.points_trial : b.points, b.nP, b.img_rt64, b.nI,
+                                                   trial ? b.cams_trial : b.cams, b.nC, b.pts_df, b.rt_df,
+                                                   b.cams_df);
+    SFMBA_LAUNCH_CHECK();
+}
+
 void launch_split_xy_df(const Bufs &b, cudaStream_t s) {
     if (!b.df_cost || b.nO == 0) return;
     k_split_xy_df<<<div_up(b.nO, 256), 256, 0, s>>>(b.ob_xy, b.nO, b.ob_xy_df);
@@ -771,10 +780,7 @@ static void cost_impl(const Bufs &b, bool trial, int mode, double *out, long lon
     launch_pose_rt64(trial ? b.poses_trial : b.poses, b.nI, b.img_rt64, s);
     const double *cams = trial ? b.cams_trial : b.cams, *points = trial ? b.points_trial : b.points;
     if (mode == 0 && b.mixed && b.df_cost) {
-        const long long nsplit = (long long)b.nP + 12LL * b.nI + 8LL * b.nC;
-        k_split_df<<<div_up(nsplit, 256), 256, 0, s>>>(points, b.nP, b.img_rt64, b.nI, cams, b.nC, b.pts_df, b.rt_df,
-                                                       b.cams_df);
-        SFMBA_LAUNCH_CHECK();
+        launch_split_df(b, trial, s);
         auto run_df = [&](auto mc) {
             k_cost_df<decltype(mc)::value><<<kCostBlocks, 256, 0, s>>>(
                 b.rt_df, b.cams_df, b.pts_df, b.cam_of_img, b.cam_model, b.ob_img, b.ob_pt, b.ob_xy_df, b.nO, b.loss,

@@ -242,6 +242,9 @@ void launch_cost(const Bufs &b, bool trial, bool into_trial, cudaStream_t s);
 // FP64 rotation matrix and translation of every pose ([nI][12]) for the cost.
 // Double-float copy of the observations for the FP32 path's cost (b.df_cost).
 void launch_split_xy_df(const Bufs &b, cudaStream_t s);
+// Double-float copies of the points, pose matrices (img_rt64, formed first)
+// and camera parameters the cost evaluates (current or trial).
+void launch_split_df(const Bufs &b, bool trial, cudaStream_t s);
 void launch_pose_rt64(const double *poses, int nI, double *rt, cudaStream_t s);
 void launch_mean_error(const Bufs &b, cudaStream_t s);  // -> partials; host finalises
 void launch_accept(const Bufs &b, cudaStream_t s);
