@@ -72,6 +72,17 @@ __global__ void k_coarse_emit(const int *pt_start, const int *ob_img, const int 
     }
 }
 
+// Sort keys of the incidences: their point's track length (capped at 2^16 - 1).
+__global__ void k_inc_keys(const int *pt_start, const long long *inc_off, int nP, int *key, int *val) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nP) return;
+    const int len = min(pt_start[p + 1] - pt_start[p], 65535);
+    for (long long a = inc_off[p]; a < inc_off[p + 1]; ++a) {
+        key[a] = len;
+        val[a] = (int)a;
+    }
+}
+
 // Size of every group from the sorted keys: the first element of a run adds
 // -start and the last adds end + 1, so only two integer atomics per group
 // land on a counter (no contention on long runs) and the sum is exact.
@@ -115,10 +126,14 @@ template <typename T, int D, bool RC, int M>
 __global__ void __launch_bounds__(128) k_coarse_y(JacSrc<T> J, const int *__restrict__ pt_start,
                                                   const int *__restrict__ img_cluster,
                                                   const long long *__restrict__ inc_off,
-                                                  const int *__restrict__ inc_cl, int nP, long long ninc,
+                                                  const int *__restrict__ inc_cl,
+                                                  const int *__restrict__ inc_order, int nP, long long ninc,
                                                   const unsigned char *__restrict__ pt_ok, T *__restrict__ Y) {
-    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (j >= ninc) return;
+    // Threads take the incidences in track-length order, so a warp's
+    // threads walk tracks of similar length.
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= ninc) return;
+    const long long j = inc_order[t];
     int lo = 0, hi = nP - 1;  // the point of incidence j: last p with inc_off[p] <= j
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -447,6 +462,16 @@ void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, 
     SFMBA_LAUNCH_CHECK();
 }
 
+void launch_coarse_inc_order(const Bufs &b, int *key, int *val, int *key2, void *temp, size_t temp_bytes,
+                             cudaStream_t s) {
+    const CoarseBufs &co = b.co;
+    if (co.ninc <= 0) return;
+    k_inc_keys<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, co.inc_off, b.nP, key, val);
+    SFMBA_LAUNCH_CHECK();
+    size_t tb = temp_bytes;
+    SFMBA_CUDA(cub::DeviceRadixSort::SortPairs(temp, tb, key, key2, val, co.inc_order, (int)co.ninc, 0, 16, s));
+}
+
 void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
     const CoarseBufs &co = b.co;
     const int D = b.D, Nc = co.nc * D;
@@ -459,16 +484,16 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
             const unsigned yb = (unsigned)div_up(co.ninc, 128);
             if (b.mixed) {
                 k_coarse_y<float, DD, true, -1><<<yb, 128, 0, s>>>(jac_src<float>(b), b.pt_start, co.img_cluster,
-                                                                   co.inc_off, co.inc_cl, b.nP, co.ninc, b.pt_ok,
-                                                                   (float *)co.ybuf);
+                                                                   co.inc_off, co.inc_cl, co.inc_order, b.nP,
+                                                                   co.ninc, b.pt_ok, (float *)co.ybuf);
                 SFMBA_LAUNCH_CHECK();
                 k_coarse_pairs<float, DD><<<div_up(co.nchunks, 4), 128, 0, s>>>(
                     (const float *)co.ybuf, co.inc_off, co.inc_cl, co.chunk, co.nchunks, co.pair_pt, co.group_cc,
                     (const float *)b.pt_Cinv, b.pt_ok, co.chunk_part);
             } else {
                 k_coarse_y<double, DD, false, -1><<<yb, 128, 0, s>>>(jac_src<double>(b), b.pt_start, co.img_cluster,
-                                                                     co.inc_off, co.inc_cl, b.nP, co.ninc, b.pt_ok,
-                                                                     (double *)co.ybuf);
+                                                                     co.inc_off, co.inc_cl, co.inc_order, b.nP,
+                                                                     co.ninc, b.pt_ok, (double *)co.ybuf);
                 SFMBA_LAUNCH_CHECK();
                 k_coarse_pairs<double, DD><<<div_up(co.nchunks, 2), 64, 0, s>>>(
                     (const double *)co.ybuf, co.inc_off, co.inc_cl, co.chunk, co.nchunks, co.pair_pt, co.group_cc,

@@ -20,6 +20,7 @@ struct CoarseBufs {
     long long ninc = 0;               // point-cluster incidences (a point's distinct clusters)
     long long *inc_off = nullptr;     // [nP+1] first incidence of each point
     int *inc_cl = nullptr;            // [ninc] cluster of each incidence, increasing within a point
+    int *inc_order = nullptr;         // [ninc] incidences by their point's track length (k_coarse_y's thread order)
     void *ybuf = nullptr;             // [ninc][3*D] Y_c of each incidence, element type of the linearisation
     int ngroups = 0;
     int2 *group_cc = nullptr;         // [ngroups] (c, c'), c <= c'
@@ -303,6 +304,10 @@ long long launch_coarse_count(const Bufs &b, long long *count, long long *off, l
 // sizes; the clusters of every incidence into b.co.inc_cl.
 void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, int *key, int *val, int *key2,
                          int *val_sorted, int *key_counts, void *temp, size_t temp_bytes, cudaStream_t s);
+// inc_order: the incidences sorted by their point's track length (key, val,
+// key2 are scratch of at least ninc entries).
+void launch_coarse_inc_order(const Bufs &b, int *key, int *val, int *key2, void *temp, size_t temp_bytes,
+                             cudaStream_t s);
 // A_c for the current damping and point inverses; FP32 copy and Ainv = I for the factorisation.
 void launch_coarse_assemble(const Bufs &b, cudaStream_t s);
 // z += Z Ainv Z^T r with the r.z / r.r partials (init: the start of a solve, p = z).

@@ -780,12 +780,14 @@ class Solver {
             co.chunk_part = P.take<double>((size_t)max_chunks * D * D);
             co.work = P.take<float>((size_t)std::max(lwork, 1));
             co.inc_cl = P.take<int>(ninc);
+            co.inc_order = P.take<int>(ninc);
             co.ybuf = P.take<double>((size_t)ninc * 3 * D);  // FP64-sized: an FP64 polish reuses it
         }
         co.ninc = ninc;
         co.lwork = lwork;
         co.nc = nc;
         launch_coarse_group(b, off, npairs, key, val, key2, val_sorted, key_counts, temp2, t2, s_);
+        launch_coarse_inc_order(b, key, val, key2, temp2, t2, s_);  // the pair keys are consumed
         const std::vector<int> kc = fetch(key_counts, (size_t)nc * nc, true, s_);
         std::vector<int2> gcc;
         std::vector<int> goff{0};
