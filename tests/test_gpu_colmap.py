@@ -1,5 +1,5 @@
 """`sfmtory refine` (crates/sfm-cli/src/main.rs:946-1130) on a COLMAP text
-model, on the GPU, against the Python restatement of the driver on the CPU
+model, on the GPU, against the Python restatement of that command on the CPU
 oracle (oracle/colmap_text.py).
 
 Bars (FP64): final cost 1e-6 relative and the same iteration count; the
