@@ -80,3 +80,14 @@ def test_gpu_jacobians_match_golden():
         assert valid[0]
         for got, key in ((r[0], "r"), (jp[0], "jp"), (jx[0], "jx"), (jc[0], "jc")):
             assert G.rel_err(got, z[f"m{m}_{key}"]) < 1e-9
+
+
+def test_pcg_coarse_polish_reaches_golden_cost():
+    """PCG with the coarse correction and the FP64 polish: the chunk graphs
+    captured for the FP32 loop are dropped when the loop continues in FP64,
+    and the polished result reaches the FP64 oracle's final cost to 1e-6."""
+    p, kw, exp = G.load("radial2000_s0005")
+    r = native.bundle_adjust_arrays(p, precision=abi.PRECISION_MIXED, solver=abi.SOLVER_PCG, fp64_polish=1,
+                                    pcg_tolerance=1e-10, pcg_max_iterations=2000, **kw)
+    assert r.polish_iteration >= 0
+    assert r.final_cost <= exp["final_cost"] * (1 + 1e-6), (r.final_cost, exp["final_cost"])
