@@ -59,7 +59,8 @@ void launch_mf_image_blocks(const Bufs &b, cudaStream_t s) {
             SFMBA_LAUNCH_CHECK();
         }
         k_mf_image_finish0<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.nI,
-                                                                b.img_live, b.img_H, b.img_b);
+                                                                b.img_live, b.img_H, b.img_b,
+                                                                D * (D + 1) / 2 + D);
         SFMBA_LAUNCH_CHECK();
     });
 }
@@ -80,7 +81,8 @@ void launch_image_blocks_records(const Bufs &b, cudaStream_t s) {
                 SFMBA_LAUNCH_CHECK();
             }
             k_mf_image_finish0<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.nI,
-                                                                    b.img_live, b.img_H, b.img_b);
+                                                                    b.img_live, b.img_H, b.img_b,
+                                                                    D * (D + 1) / 2 + D);
             SFMBA_LAUNCH_CHECK();
         };
         if (b.mixed) run(0.0f);
@@ -102,8 +104,36 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s) {
         k_mf_precond_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.img_H, b.img_b,
                                                        b.img_active, b.state, b.nI, b.img_rhs, (T *)b.pcg_Minv,
                                                        (T *)b.pcg_x, (T *)b.pcg_r, (T *)b.pcg_z, (T *)b.pcg_p,
-                                                       (T *)pcg_p4_of<T>(b), b.pcg_part);
+                                                       (T *)pcg_p4_of<T>(b), b.pcg_part, D * (D + 1) / 2 + D);
         SFMBA_LAUNCH_CHECK();
+    });
+}
+
+void launch_mf_precond_fused(const Bufs &b, cudaStream_t s) {
+    dispatch_TDR(b, [&](auto t, auto dc, auto rc, auto mc) {
+        using T = decltype(t);
+        constexpr int D = decltype(dc)::value;
+        constexpr int NV = D * (D + 1) / 2 + D;
+        if constexpr (std::is_same<T, float>::value) {
+            if (b.n_iachunks > 0) {
+                const int th = 32 * accum_warps<T>();
+                k_mf_image_accum<T, D, decltype(rc)::value, 2, decltype(mc)::value>
+                    <<<warps_grid(b.n_iachunks, th), th, 0, s>>>(jac_src<T>(b), b.iachunk, b.n_iachunks,
+                                                                 (const T *)b.pt_Cinv, (const T *)b.pt_h, b.pt_ok,
+                                                                 (T *)b.ipart2);
+                SFMBA_LAUNCH_CHECK();
+            }
+            k_mf_image_finish0<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.nI,
+                                                                    b.img_live, b.img_H, b.img_b, 2 * NV);
+            SFMBA_LAUNCH_CHECK();
+            k_mf_precond_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>(
+                (const T *)b.ipart2 + NV, b.iachunk_off, b.img_H, b.img_b, b.img_active, b.state, b.nI, b.img_rhs,
+                (T *)b.pcg_Minv, (T *)b.pcg_x, (T *)b.pcg_r, (T *)b.pcg_z, (T *)b.pcg_p, (T *)pcg_p4_of<T>(b),
+                b.pcg_part, 2 * NV);
+            SFMBA_LAUNCH_CHECK();
+        } else {
+            throw Error(SFMBA_ERR_INTERNAL, "the fused image pass is FP32 only");
+        }
     });
 }
 

@@ -273,6 +273,9 @@ void launch_mf_point_reduce(const Bufs &b, cudaStream_t s);     // C_p, g_p, fre
 void launch_mf_image_blocks(const Bufs &b, cudaStream_t s);     // H_i, b_i
 void launch_image_blocks_records(const Bufs &b, cudaStream_t s);  // H_i, b_i from stored records
 void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PCG start vectors
+// FP32: H_i, b_i and the preconditioner from one image-aligned pass (the
+// MODE-0 and MODE-1 sums together), then both finishes.
+void launch_mf_precond_fused(const Bufs &b, cudaStream_t s);
 // The two PCG passes in launch variant 0..k{Point,Image}PassVariants-1
 // (same results; chosen by the autotuner).
 constexpr int kPointPassVariants = 4;

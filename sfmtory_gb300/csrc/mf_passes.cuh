@@ -125,6 +125,8 @@ __global__ void __launch_bounds__(256) k_mf_point_reduce(JacSrc<T> J, const unsi
 // of one image, one warp each), one partial per chunk:
 //   MODE 0: W = I, v = r~                 -> H_i, b_i
 //   MODE 1: W = Jx~ C^-1 Jx~^T, v = Jx~ h -> Schur diagonal block, rhs term
+//   MODE 2: both in one pass, P_t = [A_t | r~ | W A_t | v] (2 x 2(D+1)); the
+//           chunk's partial holds the MODE-0 sums, then the MODE-1 sums
 // Per round of 32 observations lane t stages A_t = Jc~ (2 x D) and
 // P_t = [W A_t | v_t] (2 x (D+1)); the chunk's sum of A_t^T P_t is then a
 // product with inner dimension 2 x 32 per round, register-tiled like the
@@ -139,9 +141,11 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
                      const T *__restrict__ pt_h, const unsigned char *__restrict__ pt_ok, T *__restrict__ part) {
     constexpr int NH = D * (D + 1) / 2;
     constexpr int NV = NH + D;
-    constexpr int E = D + 1;  // columns of P: W A, then v
-    constexpr int RH = (D + 1) / 2, CQ = (E + 3) / 4;
-    constexpr int LA = 2 * D + 1, LP = 2 * E + 1;
+    constexpr int E = D + 1;                       // columns of one block of P: W A, then v
+    constexpr int EP = MODE == 2 ? 2 * E : E;      // columns of P
+    constexpr int NVP = MODE == 2 ? 2 * NV : NV;   // partial entries per chunk
+    constexpr int RH = (D + 1) / 2, CQ = (EP + 3) / 4;
+    constexpr int LA = 2 * D + 1, LP = 2 * EP + 1;
     constexpr int WPB = accum_warps<T>();
     __shared__ T sA[WPB][32][LA];
     __shared__ T sP[WPB][32][LP];
@@ -163,12 +167,49 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
         if (k < ch.z) {
             const int4 rc = __ldg(J.isrec + k);
             ObsOp<T, D, RC, M> op;
-            make_op_image_major<T, D, RC>(J, k, rc, op, MODE == 0);
+            make_op_image_major<T, D, RC>(J, k, rc, op, MODE != 1);
             T jc[2 * D];
             op.jc_rows(jc);
 #pragma unroll
             for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = jc[f];
-            if constexpr (MODE == 0) {
+            if constexpr (MODE == 2) {
+#pragma unroll
+                for (int q = 0; q < D; ++q) {
+                    sP[wl][lane][q] = jc[q];
+                    sP[wl][lane][EP + q] = jc[D + q];
+                }
+                sP[wl][lane][D] = op.r(0);
+                sP[wl][lane][EP + D] = op.r(1);
+                const int pt = rc.y;
+                T w00 = T(0), w01 = T(0), w11 = T(0), v0 = T(0), v1 = T(0);
+                if (pt_ok[pt]) {  // otherwise the observation adds to H_i, b_i only
+                    T jx[6];
+                    op.jx_rows(jx);
+                    const T *Ci = pt_Cinv + 6 * (size_t)pt;
+                    T U[2][3];
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const T a0 = jx[3 * q], a1 = jx[3 * q + 1], a2 = jx[3 * q + 2];
+                        U[q][0] = a0 * Ci[0] + a1 * Ci[1] + a2 * Ci[2];
+                        U[q][1] = a0 * Ci[1] + a1 * Ci[3] + a2 * Ci[4];
+                        U[q][2] = a0 * Ci[2] + a1 * Ci[4] + a2 * Ci[5];
+                    }
+                    w00 = U[0][0] * jx[0] + U[0][1] * jx[1] + U[0][2] * jx[2];
+                    w01 = U[0][0] * jx[3] + U[0][1] * jx[4] + U[0][2] * jx[5];
+                    w11 = U[1][0] * jx[3] + U[1][1] * jx[4] + U[1][2] * jx[5];
+                    const T *h = pt_h + 3 * (size_t)pt;
+                    v0 = jx[0] * h[0] + jx[1] * h[1] + jx[2] * h[2];
+                    v1 = jx[3] * h[0] + jx[4] * h[1] + jx[5] * h[2];
+                }
+#pragma unroll
+                for (int q = 0; q < D; ++q) {
+                    sP[wl][lane][E + q] = w00 * jc[q] + w01 * jc[D + q];
+                    sP[wl][lane][EP + E + q] = w01 * jc[q] + w11 * jc[D + q];
+                }
+                sP[wl][lane][E + D] = v0;
+                sP[wl][lane][EP + E + D] = v1;
+                staged = true;
+            } else if constexpr (MODE == 0) {
 #pragma unroll
                 for (int q = 0; q < D; ++q) {
                     sP[wl][lane][q] = jc[q];
@@ -210,7 +251,7 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
 #pragma unroll
             for (int f = 0; f < 2 * D; ++f) sA[wl][lane][f] = T(0);
 #pragma unroll
-            for (int f = 0; f < 2 * E; ++f) sP[wl][lane][f] = T(0);
+            for (int f = 0; f < 2 * EP; ++f) sP[wl][lane][f] = T(0);
         }
         __syncwarp();
         const int rounds = (min(32, ch.z - base) + 3 - sg) / 4;  // observations of this subgroup
@@ -222,7 +263,7 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
 #pragma unroll
                 for (int a = 0; a < RH; ++a) av[a] = (r0 + a < D) ? sA[wl][t][rho * D + r0 + a] : T(0);
 #pragma unroll
-                for (int b = 0; b < CQ; ++b) pv[b] = (c0 + b < E) ? sP[wl][t][rho * E + c0 + b] : T(0);
+                for (int b = 0; b < CQ; ++b) pv[b] = (c0 + b < EP) ? sP[wl][t][rho * EP + c0 + b] : T(0);
 #pragma unroll
                 for (int a = 0; a < RH; ++a)
 #pragma unroll
@@ -231,7 +272,7 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
         }
         __syncwarp();
     }
-    T *dst = part + (size_t)c * NV;
+    T *dst = part + (size_t)c * NVP;
 #pragma unroll
     for (int a = 0; a < RH; ++a)
 #pragma unroll
@@ -240,9 +281,11 @@ __global__ void __launch_bounds__(32 * accum_warps<T>())
             v += __shfl_xor_sync(0xffffffffu, v, 8);
             v += __shfl_xor_sync(0xffffffffu, v, 16);
             const int row = r0 + a, col = c0 + b;
-            if (lane < 8 && row < D) {
-                if (col < D && row <= col) dst[row * D - row * (row - 1) / 2 + (col - row)] = v;
-                else if (col == D) dst[NH + row] = v;
+            const int blk = col >= E ? 1 : 0, cl = col - blk * E;  // block of P, column within it
+            if (lane < 8 && row < D && col < EP) {
+                T *d = dst + blk * NV;
+                if (cl < D && row <= cl) d[row * D - row * (row - 1) / 2 + (cl - row)] = v;
+                else if (cl == D) d[NH + row] = v;
             }
         }
 }
@@ -252,7 +295,8 @@ template <typename T, int D>
 __global__ void __launch_bounds__(128) k_mf_image_finish0(const T *__restrict__ part,
                                                           const int *__restrict__ ipart_off, int nI,
                                                           const unsigned char *__restrict__ img_live,
-                                                          double *__restrict__ img_H, double *__restrict__ img_b) {
+                                                          double *__restrict__ img_H, double *__restrict__ img_b,
+                                                          int stride) {
     constexpr int NH = D * (D + 1) / 2;
     constexpr int NV = NH + D;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -261,7 +305,7 @@ __global__ void __launch_bounds__(128) k_mf_image_finish0(const T *__restrict__ 
     if (img_live && !img_live[i]) return;
     for (int e = lane; e < NV; e += 32) {
         double s = 0.0;
-        for (int k = ipart_off[i]; k < ipart_off[i + 1]; ++k) s += (double)part[(size_t)k * NV + e];
+        for (int k = ipart_off[i]; k < ipart_off[i + 1]; ++k) s += (double)part[(size_t)k * stride + e];
         if (e < NH) {
             int t = e, a = 0;
             while (t >= D - a) { t -= D - a; ++a; }
@@ -289,7 +333,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
                                                            double *__restrict__ img_rhs, T *__restrict__ Minv_out,
                                                            T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
                                                            T *__restrict__ p, T *__restrict__ p4,
-                                                           double *__restrict__ dots) {
+                                                           double *__restrict__ dots, int stride) {
     constexpr int NH = D * (D + 1) / 2;
     constexpr int NV = NH + D;
     constexpr int WPB = 4;
@@ -310,7 +354,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
     const int p0 = ipart_off[i], p1 = ipart_off[i + 1];
     for (int e = lane; e < NV; e += 32) {
         double sum = 0.0;
-        for (int k = p0; k < p1; ++k) sum += (double)part[(size_t)k * NV + e];
+        for (int k = p0; k < p1; ++k) sum += (double)part[(size_t)k * stride + e];
         if (e < NH) {
             int t = e, a = 0;
             while (t >= D - a) { t -= D - a; ++a; }

@@ -1008,7 +1008,7 @@ class Solver {
                 b.img_delta = A.take<char>((size_t)nID * tsz);
                 // Image-aligned chunks, their partials and the image-major packed
                 // records of the image-block passes (H_i, b_i; PCG preconditioner).
-                b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * (D * (D + 1) / 2 + D) * tsz);
+                b.ipart2 = A.take<char>((size_t)(nI + nchunks + 1) * 2 * (D * (D + 1) / 2 + D) * tsz);  // fused: 2 sums
                 b.iachunk = A.take<int4>((size_t)(nI + nchunks + 1));
                 b.iachunk_off = A.take<int>((size_t)nI + 1);
                 b.isrec = A.take<int4>(nO);
@@ -1220,7 +1220,8 @@ class Solver {
                 { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_blocks_records(b, s_); launch_diag_fold(b, s_); }
             } else {
                 { SFMBA_PHASE(PH_POINT_REDUCE); launch_mf_point_reduce(b, s_); }
-                { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_mf_image_blocks(b, s_); }
+                // FP32: H_i and b_i come with the preconditioner's pass in each retry.
+                if (!b.mixed) { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_mf_image_blocks(b, s_); }
             }
             read_state();
             // lib.rs:855-857: no observation in front of its camera
@@ -1243,8 +1244,10 @@ class Solver {
                     }
                     { SFMBA_PHASE(PH_BACKSUB); launch_backsub_update(b, b.delta, s_); }
                 } else {
+                    const bool fused = b.mixed;  // H_i, b_i and the preconditioner in one pass
+                    if (fused) { SFMBA_PHASE(PH_PCG_PRECOND); launch_mf_precond_fused(b, s_); }
                     bool coarse = false;
-                    if (b.co.nc > 0) {
+                    if (b.co.nc > 0) {  // the assembly reads H_i
                         // The coarse inverse is refreshed when the damping has moved by 100x
                         // or 6 outer iterations have passed since it was formed; in between
                         // the previous one (still symmetric positive definite) is used.
@@ -1259,7 +1262,7 @@ class Solver {
                     }
                     {
                         SFMBA_PHASE(PH_PCG_PRECOND);
-                        launch_mf_precond(b, s_);
+                        if (!fused) launch_mf_precond(b, s_);
                         if (coarse) launch_coarse_correct(b, true, s_);
                         launch_pcg_start(b, s_);
                     }
