@@ -34,11 +34,7 @@ thread_local long long g_kernel_launches = 0;
 
 namespace {
 
-// PCG iterations between host convergence polls: chunks of 2, 4 or 8
-// iterations (each replayed as its own CUDA graph), the next size chosen from
-// the residual's observed decay so that few iterations run past convergence.
-constexpr int kPcgChunks[3] = {2, 4, 8};
-constexpr int kPcgFirstChunk = 1;  // index into kPcgChunks
+constexpr int kPcgPollEvery = 8;  // PCG iterations between host convergence polls
 
 thread_local std::string g_last_error;
 
@@ -1277,12 +1273,9 @@ class Solver {
                         vi = tuned_variant(ctx_.device, 1, kImagePassVariants, b, s_,
                                            [&](int v) { launch_mf_images(b, s_, v); });
                     }
-                    int ci = kPcgFirstChunk;
-                    double rr_prev = -1.0;
-                    for (int it = 0; it < maxit;) {
-                        const int full = kPcgChunks[ci];
-                        const int m = std::min(full, maxit - it);
-                        // it is even (every chunk but a capped last one is): iteration it + k has parity k & 1
+                    for (int it = 0; it < maxit; it += kPcgPollEvery) {
+                        const int m = std::min(kPcgPollEvery, maxit - it);
+                        // it is a multiple of kPcgPollEvery (even): iteration it + k has parity k & 1
                         auto chunk = [&] {
                             for (int k = 0; k < m; ++k) {
                                 { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_, vp); }
@@ -1290,19 +1283,9 @@ class Solver {
                                 { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, k & 1, coarse); }
                             }
                         };
-                        pcg_chunk_[coarse ? 1 : 0][ci].run(s_, m == full && !profiler().on, chunk);
-                        it += m;
+                        pcg_chunk_[coarse ? 1 : 0].run(s_, m == kPcgPollEvery && !profiler().on, chunk);
                         read_state();
                         if (hs.pcg_done) break;
-                        // Iterations still needed at the decay rate of the last chunk
-                        // (|r|^2 per iteration), rounded up to a chunk size.
-                        const double goal = hs.pcg_tol2 * hs.pcg_bb, rr = hs.pcg_rr;
-                        if (rr_prev < 0.0) rr_prev = hs.pcg_bb;  // |r0|^2
-                        double need = kPcgChunks[2];
-                        const double rate = rr_prev > 0.0 && rr > 0.0 ? std::pow(rr / rr_prev, 1.0 / m) : 1.0;
-                        if (rate < 1.0 && goal > 0.0 && rr > goal) need = std::log(goal / rr) / std::log(rate);
-                        ci = need <= kPcgChunks[0] ? 0 : need <= kPcgChunks[1] ? 1 : 2;
-                        rr_prev = rr;
                     }
                     { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_finish(b, b.delta, s_); }
                     { SFMBA_PHASE(PH_BACKSUB); launch_mf_backsub(b, b.delta, s_); }
@@ -1337,8 +1320,7 @@ class Solver {
                 // same loop in FP64. A failed iteration's damping growth is undone.
                 polish_pending = false;
                 b.mixed = 0;
-                for (auto &row : pcg_chunk_)  // the captured FP32 chunks do not apply any more
-                    for (auto &g : row) g.reset();
+                for (auto &g : pcg_chunk_) g.reset();  // the captured FP32 chunks do not apply any more
                 out.polish_iteration = outer + 1;
                 if (!accepted) {
                     SFMBA_CUDA(cudaMemcpyAsync(&b.state->lambda, &lambda_start, sizeof(double),
@@ -1493,7 +1475,7 @@ class Solver {
     Bufs b_;
     WinBufs w_;
     Layout lay_;
-    Replay pcg_chunk_[2][3], retry_round_;  // [coarse][chunk size]
+    Replay pcg_chunk_[2], retry_round_;  // PCG chunk without / with the coarse correction
     bool coarse_valid_ = false;  // the coarse inverse in b_.co.Ainv is usable
     double coarse_lambda_ = 0.0;
     int coarse_outer_ = 0;
