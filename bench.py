@@ -147,6 +147,7 @@ class ClockSampler:
         self.dev = device_index
         self.proc = None
         self.path = None
+        self.skip = 0  # lines sampled before the timed region (set by mark)
 
     def start(self):
         fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
@@ -187,9 +188,8 @@ class ClockSampler:
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         lines = [line for line in open(self.path) if line.count(",") >= 8]
-        skip = getattr(self, "skip", 0)
-        if len(lines) > skip:  # the lines sampled during the timed region
-            lines = lines[skip:]
+        if len(lines) > self.skip:  # the lines sampled during the timed region
+            lines = lines[self.skip:]
         for line in lines:
             f = [x.strip() for x in line.split(",")]
             try:
