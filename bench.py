@@ -59,7 +59,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-side", action="store_true",
                     help="skip the dense 500-camera and the 512-window measurements reported beside the headline")
-    ap.add_argument("--only", choices=["dense_radial500", "windows512", "pnp"],
+    ap.add_argument("--only", choices=["dense_radial500", "windows512", "pnp", "full_solve_opencv47"],
                     help="run only that side measurement and print its JSON object")
     ap.add_argument("--kernel-variant", type=int, default=0,
                     help="0: autotuned launch variants of the PCG passes; 1..4: force one (for profiling)")
@@ -339,10 +339,38 @@ def algorithmic_bytes(phase, nO, nP, nI, D, t, recompute):
     return None
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# the ncu capture of the same kernel on the same workload, recorded in
-# profiles/k_mf_points_radial2000_fp32.md (full-size radial2000, FP32 path).
-NCU_TRAFFIC = {("pcg_points", "radial2000", 1.0): 142908672 + 9396992}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+# an ncu capture, kept in profiles/ncu_traffic.json beside the capture's
+# summary: one entry per (phase, workload, scale) with the SHA-256 of the
+# kernel sources it was captured from. An entry whose sources have changed
+# since is not used (traffic null) instead of reporting a stale figure.
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+
+
+def sources_sha(files):
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in files:
+        with open(os.path.join(ROOT, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def ncu_traffic(phase, workload, scale):
+    if not os.path.exists(TRAFFIC_FILE):
+        return None, "no ncu traffic file"
+    for e in json.load(open(TRAFFIC_FILE)).get("entries", []):
+        if (e.get("phase"), e.get("workload"), float(e.get("scale", -1))) != (phase, workload, float(scale)):
+            continue
+        try:
+            current = sources_sha(e["sources"])
+        except OSError:
+            return None, "kernel sources of the capture not found"
+        if current != e.get("sources_sha"):
+            return None, "kernel sources changed since the capture (%s != %s)" % (current, e.get("sources_sha"))
+        return int(e["dram_bytes_per_launch"]), e.get("summary")
+    return None, "no capture of this kernel and workload"
 
 
 def roofline(profile, p, D, t, peaks, recompute=True, workload=None):
@@ -357,10 +385,11 @@ def roofline(profile, p, D, t, peaks, recompute=True, workload=None):
     by = algorithmic_bytes(top, p.num_observations, p.num_points, p.num_images, D, t, recompute)
     peak = peaks.get("hbm_gbs")
     achieved = by / (ms_per * 1e-3) / 1e9
+    traffic, traffic_src = ncu_traffic(top, workload[0], workload[1]) if workload else (None, None)
     return {
         "kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
         "frac": round(achieved / peak, 4) if peak else None,
-        "traffic": NCU_TRAFFIC.get((top, workload[0], workload[1])) if workload else None,
+        "traffic": traffic, "traffic_source": traffic_src,
         "algorithmic_bytes_per_launch": int(by), "avg_launch_ms": round(ms_per, 4),
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peak else "fallback",
         "byte_model": "recomputed Jacobians: 16 B/observation + per-point/per-image terms" if recompute
@@ -378,19 +407,45 @@ def measured_peaks():
 # ------------------------------------------------------------ CPU baseline
 
 def cpu_baseline_sample(p, point_stride, chol_dim):
+    """One LM iteration of the reference algorithm (the C++ FP64 restatement
+    of sfm-ba) on the full problem, on the host cores. Measured: Jacobians,
+    normal-equation assembly, back-substitution and trial cost over every
+    observation; the Schur accumulation over a sample of the points (scaled
+    by the point count: its work is per point). Modelled, not measured: the
+    unblocked dense LL^T of the full reduced system, timed at chol_dim and
+    scaled by (n / chol_dim)^3. ``value`` counts the measured part only
+    (an upper bound on the reference's rate); the model is returned beside
+    it."""
     import oracle
 
     t0 = time.perf_counter()
     s = oracle.lm_iteration_sample(p, point_stride=point_stride, chol_dim=chol_dim)
     wall = time.perf_counter() - t0
-    v = p.num_observations / s["seconds_per_iteration"]
-    sample = (f"one LM iteration of the C++ FP64 restatement of sfm-ba on the full problem: Jacobians, "
-              f"assembly, back-substitution and trial cost of all {p.num_observations} observations timed; "
-              f"Schur accumulation timed on {s['schur_points']} points and scaled x{s['schur_scale']:.1f} "
-              f"(ideal {s['threads']}-thread speed-up, per-thread accumulator reduction not counted); unblocked "
-              f"dense LL^T timed at n={s['chol_dim']} and scaled by (n/{s['chol_dim']})^3 to n={s['reduced_dim']}; "
-              f"extrapolated {s['seconds_per_iteration']:.1f} s/iteration from {wall:.1f} s measured")
-    return v, s, sample
+    schur_scaled = s["schur_sample_s"] * s["schur_scale"]
+    measured = s["jacobians_s"] + s["assembly_s"] + schur_scaled + s["backsub_update_s"] + s["trial_cost_s"]
+    chol_model = s["cholesky_sample_s"] * s["cholesky_scale"]
+    v = p.num_observations / measured
+    sample = (f"one LM iteration of the C++ FP64 restatement of sfm-ba on the full problem, without its dense "
+              f"factorisation: Jacobians, assembly, back-substitution and trial cost of all {p.num_observations} "
+              f"observations timed; Schur accumulation timed on {s['schur_points']} points and scaled "
+              f"x{s['schur_scale']:.1f} to all points ({s['threads']} threads); {measured:.2f} s per iteration "
+              f"from {wall:.1f} s of wall time. The unblocked dense LL^T of the n={s['reduced_dim']} reduced "
+              f"system is not in the value (see 'extrapolated')")
+    extra = {
+        "measured_s_per_iteration_without_factorisation": measured,
+        "phases_s": {"jacobians": s["jacobians_s"], "assembly": s["assembly_s"],
+                     "schur_sample": s["schur_sample_s"], "schur_scaled_to_all_points": schur_scaled,
+                     "backsub_update": s["backsub_update_s"], "trial_cost": s["trial_cost_s"]},
+        "extrapolated": {
+            "what": f"unblocked single-thread dense LL^T (nalgebra semantics) timed at n={s['chol_dim']} and "
+                    f"scaled by (n/{s['chol_dim']})^3 to n={s['reduced_dim']}: a model, not a measurement",
+            "cholesky_sample_s": s["cholesky_sample_s"], "cholesky_model_s": chol_model,
+            "seconds_per_iteration_with_factorisation": measured + chol_model,
+            "obs_per_s_with_factorisation": p.num_observations / (measured + chol_model),
+        },
+        "wall_s": wall,
+    }
+    return v, s, sample, extra
 
 
 # ------------------------------------------------- side workloads (rank 0)
@@ -433,6 +488,48 @@ def dense_radial500(args, L, device, stream):
         "cholesky_fp64_tflops": chol_tflops,
         "phase_ms": {k: round(v["ms"], 3) for k, v in prof.items() if isinstance(v, dict) and v.get("launches")},
     }
+
+
+def full_solve_opencv47(args, L, device, stream, with_cpu):
+    """A fully measured CPU-vs-GPU comparison on a configuration the
+    reference algorithm finishes in seconds: 47 OPENCV cameras, 20k points,
+    ~120k observations, 5 % outliers, Huber at 1 px, 50 LM iterations at
+    most (reduced dimension 652). The C++ FP64 restatement of sfm-ba solves
+    it on all host cores; the GPU solves it on the FP64 and the FP32 path
+    (device-resident, CUDA events). Costs of both GPU results are compared
+    with the CPU result."""
+    from sfmtory_gb300 import abi, scenes
+
+    p = scenes.opencv47(seed=args.seed, scale=1.0)
+    dp = DeviceProblem(p, device)
+    kw = dict(max_iterations=50, robust_loss=abi.LOSS_HUBER, loss_scale_px=1.0)
+    out = {"workload": f"opencv47: {p.num_images} OPENCV cameras, {p.num_points} points, {p.num_observations} "
+                       f"observations, 5 % outliers, Huber 1 px, reduced dim {p.reduced_dim()}"}
+    res = {}
+    for name, prec in (("gpu_fp64", abi.PRECISION_FP64), ("gpu_fp32", abi.PRECISION_MIXED)):
+        o = abi.default_options(precision=prec, **kw)
+        solve_device(L, dp, o, stream)
+        ms = []
+        for _ in range(3):
+            r, t = solve_device(L, dp, o, stream)
+            ms.append(t)
+        res[name] = r
+        out[name] = {"seconds": statistics.mean(ms) / 1e3, "iterations": r.iterations_run,
+                     "final_cost": r.final_cost}
+    if with_cpu:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        oracle.set_threads(threads)
+        t0 = time.perf_counter()
+        ref = oracle.bundle_adjust(p, **kw)
+        dt = time.perf_counter() - t0
+        out["cpu_reference_port"] = {"seconds": dt, "iterations": ref.iterations_run, "final_cost": ref.final_cost,
+                                     "cores": threads, "kind": "port"}
+        for name in ("gpu_fp64", "gpu_fp32"):
+            out[name]["cost_rel_vs_cpu"] = abs(res[name].final_cost - ref.final_cost) / ref.final_cost
+            out[name]["speedup_vs_cpu"] = dt / out[name]["seconds"]
+    return out
 
 
 def windows512(args, with_cpu):
@@ -532,32 +629,37 @@ def pnp_batch_measure(args, with_cpu, num_images=4096):
 
 
 def run_reference(args):
+    """The reference arm: per step one sampled LM iteration of the reference
+    algorithm on the host cores (cpu_baseline_sample); ``ms_per_step`` is
+    the wall time each step took, ``value`` its measured observation rate
+    without the dense factorisation, and ``extrapolated`` the modelled full
+    iteration."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import oracle
-
     p = make_problem(args, 0)
     stride = max(1, p.num_points // 20000)
     chol_dim = min(2000, p.reduced_dim())
-    vals = []
+    vals, walls = [], []
     info = None
     for k in range(args.warmup + args.steps):
-        v, s, sample = cpu_baseline_sample(p, stride, chol_dim)
+        v, s, sample, extra = cpu_baseline_sample(p, stride, chol_dim)
         if k >= args.warmup:
             vals.append(v)
-            info = (s, sample)
+            walls.append(extra["wall_s"])
+            info = (s, sample, extra)
     v = statistics.mean(vals)
-    s, sample = info
+    s, sample, extra = info
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": s["seconds_per_iteration"] * 1e3, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(walls) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args, p),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": s["threads"], "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "phases_s": {k: s[k] for k in ("jacobians_s", "assembly_s", "schur_sample_s", "cholesky_sample_s",
-                                        "backsub_update_s", "trial_cost_s")},
+        "value_is": "observations per second of one reference LM iteration without its dense factorisation, "
+                    "measured (an upper bound on the reference's rate)",
+        **{k: extra[k] for k in ("measured_s_per_iteration_without_factorisation", "phases_s", "extrapolated")},
     }
     print(json.dumps(line), flush=True)
 
@@ -568,7 +670,7 @@ def run_ours(args):
     import torch
 
     from sfmtory_gb300 import abi, native
-    from sfmtory_gb300.problem import rms_reprojection_error
+    from sfmtory_gb300.problem import parameter_errors, rms_reprojection_error
 
     rank, world, local = dist_env()
     if not torch.cuda.is_available():
@@ -595,6 +697,8 @@ def run_ours(args):
         opts64 = solver_options(args, abi.PRECISION_FP64)
         solve_device(L, dp, opts64, stream)
         r64, ms64_full = solve_device(L, dp, opts64, stream)
+        out64 = (dp.out_poses.cpu().numpy().copy(), dp.out_points.cpu().numpy().copy(),
+                 dp.out_cams.cpu().numpy().copy())
         target = r64.final_cost * (1.0 + 1e-6)
         opts64t = solver_options(args, abi.PRECISION_FP64, target)
         solve_device(L, dp, opts64t, stream)
@@ -650,6 +754,46 @@ def run_ours(args):
     out_poses = dp.out_poses.cpu().numpy()
     out_cams = dp.out_cams.cpu().numpy()
     rms32 = rms_reprojection_error(p.copy(points=out_points, poses=out_poses, camera_params=out_cams))
+    vs64 = None
+    if fp64:
+        # FP32 result (stopped at the FP64 cost x (1 + 1e-6)) against the FP64
+        # path's own converged result: RMS and parameters, raw and with the
+        # free scale removed (pose 0 is the fixed gauge).
+        # Context: how far the FP64 path's own parameters move in its last
+        # iteration (the same solve stopped one iteration earlier), and the
+        # FP32 path run to its own convergence (no target) against it.
+        def pe_of(a):
+            e = parameter_errors(*a, *out64)
+            return {"raw": e["raw"], "normalized": e["normalized"], "raw_max": e["raw_max"],
+                    "normalized_max": e["normalized_max"], "scale_ratio": e["scale_ratio"]}
+
+        def outputs():
+            return (dp.out_poses.cpu().numpy().copy(), dp.out_points.cpu().numpy().copy(),
+                    dp.out_cams.cpu().numpy().copy())
+
+        r32c, _ = solve_device(L, dp, solver_options(args, abi.PRECISION_MIXED), stream)
+        out32c = outputs()
+        prev64 = None
+        if fp64["iterations"] > 1:
+            o = solver_options(args, abi.PRECISION_FP64)
+            o.max_iterations = fp64["iterations"] - 1
+            solve_device(L, dp, o, stream)
+            prev64 = pe_of(outputs())
+        rms64 = rms_reprojection_error(p.copy(poses=out64[0], points=out64[1], camera_params=out64[2]))
+        fp64["rms_px"] = rms64
+        vs64 = {"rms_px_fp64": rms64, "rms_diff_px": abs(rms32 - rms64),
+                "cost_rel": abs(last.final_cost - fp64["final_cost"]) / fp64["final_cost"],
+                "param_rel_err": pe_of((out_poses, out_points, out_cams)),
+                "fp32_converged": {"iterations": r32c.iterations_run, "final_cost": r32c.final_cost,
+                                   "cost_rel": abs(r32c.final_cost - fp64["final_cost"]) / fp64["final_cost"],
+                                   "rms_diff_px": abs(rms_reprojection_error(p.copy(
+                                       poses=out32c[0], points=out32c[1], camera_params=out32c[2])) - rms64),
+                                   "param_rel_err": pe_of(out32c)},
+                "fp64_last_iteration_moved": prev64,
+                "note": "param_rel_err: the FP32 result at the tolerance target (FP64 cost x (1 + 1e-6)) against "
+                        "the FP64 path's converged result; fp32_converged: the FP32 path run to its own stopping "
+                        "rule; fp64_last_iteration_moved: the FP64 path's parameters one iteration before its "
+                        "end against its end (the resolution of the stopping rule along flat directions)"}
 
     if rank != 0:
         return
@@ -658,10 +802,9 @@ def run_ours(args):
     cpu = None
     if not args.skip_cpu and world == 1:
         stride = max(1, p.num_points // 20000)
-        v, s, sample = cpu_baseline_sample(p, stride, min(2000, p.reduced_dim()))
-        import oracle
-
-        cpu = {"value": v, "unit": UNIT, "cores": s["threads"], "kind": "port", "sample": sample}
+        v, s, sample, extra = cpu_baseline_sample(p, stride, min(2000, p.reduced_dim()))
+        cpu = {"value": v, "unit": UNIT, "cores": s["threads"], "kind": "port", "sample": sample,
+               "extrapolated": extra["extrapolated"]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -671,6 +814,7 @@ def run_ours(args):
         "final_cost": last.final_cost, "initial_cost": last.initial_cost,
         "reached_tolerance": (last.final_cost <= target) if target else None, "rms_px": rms32,
         "fp64_gpu": fp64, "speedup_vs_fp64_gpu": (fp64["time_to_tolerance_s"] / step_s) if fp64 else None,
+        "fp32_vs_fp64": vs64,
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "seconds_per_step": statistics.mean(e2e_times)},
@@ -681,6 +825,7 @@ def run_ours(args):
     }
     if not args.skip_side and world == 1:
         line["dense_radial500"] = dense_radial500(args, L, device, stream)
+        line["full_solve_opencv47"] = full_solve_opencv47(args, L, device, stream, not args.skip_cpu)
         line["windows512"] = windows512(args, not args.skip_cpu)
         line["pnp4096"] = pnp_batch_measure(args, not args.skip_cpu)
     print(json.dumps(line), flush=True)
@@ -699,6 +844,8 @@ def run_side_only(args):
         out = dense_radial500(args, L, device, torch.cuda.Stream(device=device))
     elif args.only == "pnp":
         out = pnp_batch_measure(args, not args.skip_cpu)
+    elif args.only == "full_solve_opencv47":
+        out = full_solve_opencv47(args, L, device, torch.cuda.Stream(device=device), not args.skip_cpu)
     else:
         out = windows512(args, not args.skip_cpu)
     print(json.dumps(out), flush=True)

@@ -304,17 +304,81 @@ int sfmba_residuals_jacobians(const sfmba_problem *problem, int32_t precision, d
                               double *j_pose, double *j_point, double *j_camera,
                               uint8_t *valid);
 
+/* A reconstruction in progress as sfm-reconstruction holds it during
+ * incremental growth (crates/sfm-reconstruction/src/lib.rs:126-129
+ * `PointWork` {xyz, track of (image, keypoint)}, the registered flags, the
+ * poses and cameras): input of the local-window builder. Each track element
+ * carries its keypoint's pixel (the reference reads it from the image's
+ * features, lib.rs:131-134). */
+typedef struct sfmba_reconstruction {
+    int64_t num_images;
+    int64_t num_cameras;
+    int64_t num_points;
+    const int32_t *camera_of_image;   /* [num_images]                                  */
+    const int32_t *camera_model;      /* [num_cameras] sfmba_camera_model              */
+    const double *camera_params;      /* [num_cameras][8]                              */
+    const double *poses;              /* [num_images][7]; registered images only read  */
+    const uint8_t *registered;        /* [num_images]                                  */
+    const uint8_t *pose_fixed;        /* [num_images] or NULL: poses the caller pinned
+                                         (ImageInput::pose_fixed with an initial pose) */
+    const double *points;             /* [num_points][3]                               */
+    const int64_t *track_offsets;     /* [num_points+1], track_offsets[0] = 0          */
+    const int32_t *track_image;       /* [track_offsets[num_points]]                   */
+    const double *track_xy;           /* [track_offsets[num_points]][2] pixels         */
+} sfmba_reconstruction;
+
+/* Caller-owned output arrays of one local window, sized by the counts of a
+ * sizing call (images I, cameras C, points P, observations O). Any pointer
+ * may be NULL to skip that array. */
+typedef struct sfmba_window_buffers {
+    int32_t *image_ids;            /* [I] reconstruction image of each window image  */
+    int32_t *camera_ids;           /* [C] reconstruction camera of each window camera */
+    int32_t *point_ids;            /* [P] reconstruction point of each window point  */
+    int32_t *camera_of_image;      /* [I]                                             */
+    int32_t *camera_model;         /* [C]                                             */
+    double *camera_params;         /* [C][8]                                          */
+    double *poses;                 /* [I][7]                                          */
+    double *points;                /* [P][3]                                          */
+    int32_t *obs_image;            /* [O]                                             */
+    int32_t *obs_point;            /* [O]                                             */
+    double *obs_xy;                /* [O][2]                                          */
+    uint8_t *fixed_poses;          /* [I]                                             */
+    uint8_t *fixed_cameras;        /* [C] all 1: local bundles hold the intrinsics    */
+    uint8_t *fixed_camera_params;  /* [C][8] default_fixed_params_mask                */
+} sfmba_window_buffers;
+
+/* BaScope::Local window construction (crates/sfm-reconstruction/src/lib.rs:
+ * 1287-1299, :1320, :1336-1473) for num_centers centre images at once: the
+ * centre's points (tracks of >= 2 elements) free; the centre and its
+ * num_free_neighbours most co-visible registered images (ties by index;
+ * LOCAL_BA_NUM_IMAGES = 6 in the reference) free; every other registered
+ * image observing those points present and fixed, as are seed_image (-1:
+ * none) and the pinned poses; if no pose is fixed, the first window image;
+ * compact indices in the reference's order; cameras fixed with the
+ * principal point masked. counts_out[k][4] = images, cameras, points,
+ * observations of window k, all 0 where the reference makes no solve (fewer
+ * than two images or no observation). windows NULL: sizes only; else
+ * num_centers buffer sets sized by an earlier sizing call with the same
+ * arguments (checked). Host computation; each window can be passed to
+ * sfmba_bundle_adjust or, all together, to sfmba_bundle_adjust_batched. */
+int sfmba_local_windows(const sfmba_reconstruction *rec, int32_t seed_image, int32_t num_free_neighbours,
+                        int32_t num_centers, const int32_t *centers, int64_t *counts_out,
+                        sfmba_window_buffers *windows);
+
 /* No counterpart in the reference. The robust cost of sfmba_total_cost for
  * a problem whose arrays are all in device memory, computed without
  * allocating any memory, for callers that cannot let a library allocate
  * (a fixed per-component slice of the GPU, or a thread that must not pay
  * for cudaFree's device-wide synchronisation). The result is written to
  * `out_cost_device` (device memory) on `stream` (NULL: the default stream);
- * the call returns once it is there. Scratch is a fixed 64 KB array inside
- * the library, held on every device the library is used on until exit;
- * at most SFMBA_NOALLOC_MAX_OBSERVATIONS observations (larger problems are
- * rejected with SFMBA_ERR_INVALID_ARGUMENT). The first call on a device
- * looks up the array's device address - make it before any stream capture.
+ * the call waits for its stream and returns once the result is there, so it
+ * must not be called on a stream that is being captured into a CUDA graph.
+ * Scratch is a fixed 32 KB array inside the library, held on every device
+ * the library is used on until exit; at most SFMBA_NOALLOC_MAX_OBSERVATIONS
+ * observations (larger problems are rejected with
+ * SFMBA_ERR_INVALID_ARGUMENT). The first call on a device looks up the
+ * array's device address. Indices and model ids are validated as
+ * sfmba_total_cost validates them (SFMBA_ERR_INVALID_ARGUMENT, NaN written).
  * Calls share the array: calls that overlap on one GPU race. */
 #define SFMBA_NOALLOC_MAX_OBSERVATIONS 16777216
 int sfmba_total_cost_noalloc(const sfmba_problem *problem, const sfmba_options *options,

@@ -65,6 +65,7 @@ def lib():
             L.oracle_threads.restype = C.c_int
             L.oracle_phase_seconds.argtypes = [vp]
             L.oracle_lm_iteration_sample.argtypes = [vp, vp, C.c_int, C.c_int, vp]
+            L.oracle_jacobians_batch.argtypes = [vp, C.c_int, C.c_double, vp, vp, vp, vp, vp]
             _lib = L
     return _lib
 
@@ -208,6 +209,23 @@ def analytic_jacobians(pose7, model, params, X, obs):
 def numerical_jacobians(pose7, model, params, X, obs):
     """Central differences, step 1e-6 (lib.rs:600-670)."""
     return _jac(lib().oracle_numerical_jacobians, pose7, model, params, X, obs)
+
+
+def jacobians_batch(problem, numerical: bool = False, h_rel: float = 1e-6):
+    """Residuals and Jacobians of every observation in input order: analytic
+    (lib.rs:327-590) or central differences with step h_rel * max(1, |value|)
+    per parameter (pose increments at 0: step h_rel). Returns (r [nO,2],
+    J_pose [nO,2,6], J_point [nO,2,3], J_cam [nO,2,8], valid [nO])."""
+    packed = PackedProblem(problem)
+    n = int(packed.struct.num_observations)
+    r, jp, jx = np.zeros((n, 2)), np.zeros((n, 2, 6)), np.zeros((n, 2, 3))
+    jc, valid = np.zeros((n, 2, 8)), np.zeros(max(n, 1), np.uint8)
+    st = lib().oracle_jacobians_batch(C.byref(packed.struct), 1 if numerical else 0, C.c_double(h_rel),
+                                      r.ctypes.data, jp.ctypes.data, jx.ctypes.data, jc.ctypes.data,
+                                      valid.ctypes.data)
+    if st != 0:
+        raise ValueError(f"oracle_jacobians_batch failed with status {st}")
+    return r, jp, jx, jc, valid[:n].astype(bool)
 
 
 def perturb_pose(pose7, delta6) -> np.ndarray:

@@ -574,6 +574,77 @@ int oracle_numerical_jacobians(const double *pose7, int model, const double *par
     return 1;
 }
 
+// Jacobians of every observation of a problem, in input order, for checks
+// over a whole scene. mode 0: analytic (lib.rs:327-590). mode 1: central
+// differences as lib.rs:600-670 but with a step relative to the parameter,
+// h = h_rel * max(1, |value|) (pose increments are taken at 0, so their step
+// is h_rel). Outputs r[nO][2], jp[nO][2][6], jx[nO][2][3], jc[nO][2][8]
+// (columns past the model's parameter count 0), valid[nO].
+int oracle_jacobians_batch(const sfmba_problem *p, int mode, double h_rel, double *r, double *jp, double *jx,
+                           double *jc, uint8_t *valid) {
+    Problem P;
+    if (!load(p, P) || (mode != 0 && mode != 1) || !(h_rel > 0.0)) return SFMBA_ERR_INVALID_ARGUMENT;
+#pragma omp parallel for schedule(static)
+    for (long o = 0; o < P.nO; ++o) {
+        const int i = P.ob_img[o], c = P.cam_of_img[i], model = P.model[c];
+        const Pose pose = load_pose(&P.poses[(size_t)i * 7]);
+        const double *cp = &P.cam[(size_t)c * 8];
+        const double *X = &P.points[(size_t)P.ob_pt[o] * 3];
+        const double ox = P.ob_xy[2 * o], oy = P.ob_xy[2 * o + 1];
+        double *ro = r + 2 * o, *jpo = jp + 12 * o, *jxo = jx + 6 * o, *jco = jc + 16 * o;
+        for (int k = 0; k < 16; ++k) jco[k] = 0.0;
+        if (mode == 0) {
+            Jac J;
+            valid[o] = analytic(pose, model, cp, X, ox, oy, J) ? 1 : 0;
+            if (!valid[o]) continue;
+            std::memcpy(ro, J.r, sizeof(J.r));
+            std::memcpy(jpo, J.jp, sizeof(J.jp));
+            std::memcpy(jxo, J.jx, sizeof(J.jx));
+            std::memcpy(jco, J.jc, sizeof(J.jc));
+            continue;
+        }
+        double r0[2];
+        valid[o] = residual(pose, model, cp, X, ox, oy, r0) ? 1 : 0;
+        if (!valid[o]) continue;
+        ro[0] = r0[0]; ro[1] = r0[1];
+        auto col = [&](const double rp[2], const double rm[2], double h, double *dst, int stride, int k) {
+            dst[0 * stride + k] = (rp[0] - rm[0]) / (2.0 * h);
+            dst[1 * stride + k] = (rp[1] - rm[1]) / (2.0 * h);
+        };
+        auto res_or_r0 = [&](const Pose &Q, const double *cc, const double *XX, double out[2]) {
+            if (!residual(Q, model, cc, XX, ox, oy, out)) { out[0] = r0[0]; out[1] = r0[1]; }
+        };
+        for (int k = 0; k < 6; ++k) {
+            double dp[6] = {0}, dm[6] = {0};
+            dp[k] = h_rel; dm[k] = -h_rel;
+            double rp[2], rm[2];
+            res_or_r0(perturb_pose(pose, dp), cp, X, rp);
+            res_or_r0(perturb_pose(pose, dm), cp, X, rm);
+            col(rp, rm, h_rel, jpo, 6, k);
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double h = h_rel * std::max(1.0, std::fabs(X[k]));
+            double Xp[3] = {X[0], X[1], X[2]}, Xm[3] = {X[0], X[1], X[2]};
+            Xp[k] += h; Xm[k] -= h;
+            double rp[2], rm[2];
+            res_or_r0(pose, cp, Xp, rp);
+            res_or_r0(pose, cp, Xm, rm);
+            col(rp, rm, (Xp[k] - Xm[k]) * 0.5, jxo, 3, k);
+        }
+        for (int k = 0; k < model_dof(model); ++k) {
+            const double h = h_rel * std::max(1.0, std::fabs(cp[k]));
+            double cpp[8], cpm[8];
+            std::memcpy(cpp, cp, sizeof(cpp)); std::memcpy(cpm, cp, sizeof(cpm));
+            cpp[k] += h; cpm[k] -= h;
+            double rp[2], rm[2];
+            res_or_r0(pose, cpp, X, rp);
+            res_or_r0(pose, cpm, X, rm);
+            col(rp, rm, (cpp[k] - cpm[k]) * 0.5, jco, 8, k);
+        }
+    }
+    return SFMBA_OK;
+}
+
 double oracle_robust_weight(double n, int loss, double scale) { return robust_weight(n, loss, scale); }
 
 int oracle_total_cost(const sfmba_problem *p, const sfmba_options *o, double *out) {

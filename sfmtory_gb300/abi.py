@@ -58,6 +58,30 @@ class SfmbaProblem(C.Structure):
     ]
 
 
+class SfmbaReconstruction(C.Structure):
+    _fields_ = [
+        ("num_images", C.c_int64),
+        ("num_cameras", C.c_int64),
+        ("num_points", C.c_int64),
+        ("camera_of_image", C.c_void_p),
+        ("camera_model", C.c_void_p),
+        ("camera_params", C.c_void_p),
+        ("poses", C.c_void_p),
+        ("registered", C.c_void_p),
+        ("pose_fixed", C.c_void_p),
+        ("points", C.c_void_p),
+        ("track_offsets", C.c_void_p),
+        ("track_image", C.c_void_p),
+        ("track_xy", C.c_void_p),
+    ]
+
+
+class SfmbaWindowBuffers(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "image_ids", "camera_ids", "point_ids", "camera_of_image", "camera_model", "camera_params", "poses",
+        "points", "obs_image", "obs_point", "obs_xy", "fixed_poses", "fixed_cameras", "fixed_camera_params")]
+
+
 class SfmbaOptions(C.Structure):
     _fields_ = [
         ("max_iterations", C.c_int32),

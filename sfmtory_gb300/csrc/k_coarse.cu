@@ -98,7 +98,8 @@ __global__ void k_key_counts(const int *key, long long n, int *counts) {
 }
 
 // A_c = 0, then block (c, c) = sum over the cluster's images of
-// (H_i + lambda diag H_i) on the image's unknown columns.
+// (H_i + lambda diag H_i) on the image's own unknown columns (pmask: a
+// shared camera's columns are not in the coarse space).
 __global__ void k_coarse_diag(const double *img_H, const int *img_active, const int *clu_start, int nc, int D,
                               const LMState *st, double *A) {
     const int c = blockIdx.x;
@@ -125,6 +126,7 @@ __global__ void k_coarse_diag(const double *img_H, const int *img_active, const 
 template <typename T, int D, bool RC, int M>
 __global__ void __launch_bounds__(128) k_coarse_y(JacSrc<T> J, const int *__restrict__ pt_start,
                                                   const int *__restrict__ img_cluster,
+                                                  const int *__restrict__ img_pmask,
                                                   const long long *__restrict__ inc_off,
                                                   const int *__restrict__ inc_cl,
                                                   const int *__restrict__ inc_order, int nP, long long ninc,
@@ -155,10 +157,12 @@ __global__ void __launch_bounds__(128) k_coarse_y(JacSrc<T> J, const int *__rest
             T jx[6], jc[2 * D];
             op.jx_rows(jx);
             op.jc_rows(jc);
+            const int pm = img_pmask[rc.x];  // a shared camera's columns are not in the coarse space
 #pragma unroll
             for (int r = 0; r < 3; ++r)
 #pragma unroll
-                for (int d = 0; d < D; ++d) y[r][d] += jx[r] * jc[d] + jx[3 + r] * jc[D + d];
+                for (int d = 0; d < D; ++d)
+                    if ((pm >> d) & 1) y[r][d] += jx[r] * jc[d] + jx[3 + r] * jc[D + d];
         }
     }
     T *dst = Y + (size_t)j * 3 * D;
@@ -330,7 +334,8 @@ __global__ void k_coarse_sym(float *Ainv, int Nc) {
 // image order. One warp per cluster.
 template <typename T, int D>
 __global__ void __launch_bounds__(256) k_coarse_restrict(const T *__restrict__ r, const int *__restrict__ clu_start,
-                                                         int nc, const LMState *__restrict__ st, int check_done,
+                                                         const int *__restrict__ img_pmask, int nc,
+                                                         const LMState *__restrict__ st, int check_done,
                                                          double *__restrict__ zc) {
     if (check_done && st->pcg_done) return;
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -342,11 +347,13 @@ __global__ void __launch_bounds__(256) k_coarse_restrict(const T *__restrict__ r
     for (; i + 8 <= i1; i += 8) {  // loads eight at a time, added in image order
         T w[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) w[u] = r[(size_t)(i + u) * D + lane];
+        for (int u = 0; u < 8; ++u)
+            w[u] = ((img_pmask[i + u] >> lane) & 1) ? r[(size_t)(i + u) * D + lane] : T(0);
 #pragma unroll
         for (int u = 0; u < 8; ++u) s += (double)w[u];
     }
-    for (; i < i1; ++i) s += (double)r[(size_t)i * D + lane];
+    for (; i < i1; ++i)
+        if ((img_pmask[i] >> lane) & 1) s += (double)r[(size_t)i * D + lane];
     zc[c * D + lane] = s;
 }
 
@@ -386,7 +393,8 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(const float *__restrict__ A
 template <typename T, int D>
 __global__ void __launch_bounds__(256) k_coarse_z(const T *__restrict__ r, const T *__restrict__ cc,
                                                   const int *__restrict__ img_cluster,
-                                                  const int *__restrict__ img_active, const LMState *__restrict__ st,
+                                                  const int *__restrict__ img_pmask,
+                                                  const int *__restrict__ img_dmask, const LMState *__restrict__ st,
                                                   int nI, int init, T *__restrict__ z, T *__restrict__ p,
                                                   float *__restrict__ p4, double *__restrict__ part) {
     if (!init && st->pcg_done) return;
@@ -398,15 +406,18 @@ __global__ void __launch_bounds__(256) k_coarse_z(const T *__restrict__ r, const
     if (lane < D) {
         const double rc = (double)r[base + lane];
         double zc = (double)z[base + lane];
-        if ((img_active[i] >> lane) & 1) zc += (double)cc[(size_t)img_cluster[i] * D + lane];
+        const bool own = (img_pmask[i] >> lane) & 1;  // a shared camera's columns keep their entries
+        if (own) zc += (double)cc[(size_t)img_cluster[i] * D + lane];
         const T zt = (T)zc;
         z[base + lane] = zt;
-        if (init) {
+        if (init && own) {
             p[base + lane] = zt;
             if (p4) p4[(size_t)i * pad4(D) + lane] = (float)zt;
         }
-        rz = rc * (double)zt;
-        rr = rc * rc;
+        if ((img_dmask[i] >> lane) & 1) {
+            rz = rc * (double)zt;
+            rr = rc * rc;
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -476,7 +487,7 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
     const CoarseBufs &co = b.co;
     const int D = b.D, Nc = co.nc * D;
     SFMBA_CUDA(cudaMemsetAsync(co.A, 0, sizeof(double) * (size_t)Nc * Nc, s));
-    k_coarse_diag<<<co.nc, 128, 0, s>>>(b.img_H, b.img_active, co.clu_start, co.nc, D, b.state, co.A);
+    k_coarse_diag<<<co.nc, 128, 0, s>>>(b.img_H, b.img_pmask, co.clu_start, co.nc, D, b.state, co.A);
     SFMBA_LAUNCH_CHECK();
     if (co.nchunks > 0) {
         dispatch_D(D, [&](auto dc) {
@@ -484,7 +495,7 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
             const unsigned yb = (unsigned)div_up(co.ninc, 128);
             if (b.mixed) {
                 k_coarse_y<float, DD, true, -1><<<yb, 128, 0, s>>>(jac_src<float>(b), b.pt_start, co.img_cluster,
-                                                                   co.inc_off, co.inc_cl, co.inc_order, b.nP,
+                                                                   b.img_pmask, co.inc_off, co.inc_cl, co.inc_order, b.nP,
                                                                    co.ninc, b.pt_ok, (float *)co.ybuf);
                 SFMBA_LAUNCH_CHECK();
                 k_coarse_pairs<float, DD><<<div_up(co.nchunks, 4), 128, 0, s>>>(
@@ -492,7 +503,7 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
                     (const float *)b.pt_Cinv, b.pt_ok, co.chunk_part);
             } else {
                 k_coarse_y<double, DD, false, -1><<<yb, 128, 0, s>>>(jac_src<double>(b), b.pt_start, co.img_cluster,
-                                                                     co.inc_off, co.inc_cl, co.inc_order, b.nP,
+                                                                     b.img_pmask, co.inc_off, co.inc_cl, co.inc_order, b.nP,
                                                                      co.ninc, b.pt_ok, (double *)co.ybuf);
                 SFMBA_LAUNCH_CHECK();
                 k_coarse_pairs<double, DD><<<div_up(co.nchunks, 2), 64, 0, s>>>(
@@ -522,13 +533,14 @@ void launch_coarse_correct(const Bufs &b, bool init, cudaStream_t s) {
         constexpr int D = decltype(dc)::value;
         auto run = [&](auto t) {
             using T = decltype(t);
-            k_coarse_restrict<T, D><<<div_up(co.nc, 8), 256, 0, s>>>((const T *)b.pcg_r, co.clu_start, co.nc, b.state,
-                                                                     init ? 0 : 1, co.zc);
+            k_coarse_restrict<T, D><<<div_up(co.nc, 8), 256, 0, s>>>((const T *)b.pcg_r, co.clu_start, b.img_pmask,
+                                                                     co.nc, b.state, init ? 0 : 1, co.zc);
             SFMBA_LAUNCH_CHECK();
             k_coarse_gemv<T><<<div_up(Nc, 8), 256, 0, s>>>(co.Ainv, co.zc, Nc, b.state, init ? 0 : 1, (T *)co.cc);
             SFMBA_LAUNCH_CHECK();
             k_coarse_z<T, D><<<div_up(b.nI, 8), 256, 0, s>>>(
-                (const T *)b.pcg_r, (const T *)co.cc, co.img_cluster, b.img_active, b.state, b.nI, init ? 1 : 0,
+                (const T *)b.pcg_r, (const T *)co.cc, co.img_cluster, b.img_pmask, b.img_dmask, b.state, b.nI,
+                init ? 1 : 0,
                 (T *)b.pcg_z, (T *)b.pcg_p, std::is_same<T, float>::value ? b.pcg_p4 : nullptr, b.pcg_part);
             SFMBA_LAUNCH_CHECK();
         };

@@ -11,7 +11,7 @@
 //
 // The per-block partial sums that sfmba_total_cost keeps in its workspace
 // live here in one fixed array compiled into the library
-// (`g_noalloc_scratch`, 64 KB + a flag). Every GPU this library is used on
+// (`g_noalloc_scratch`, 32 KB + a flag). Every GPU this library is used on
 // holds that array until the process exits. Its size bounds the problem:
 // at most kNoAllocMaxObservations observations (4096 blocks x 4096
 // observations). All calls on a device share the array and it keeps the
@@ -21,10 +21,17 @@
 // GPU (different streams, or different host threads on one device) race on
 // the array and may both return wrong sums: serialise them.
 //
+// Validation matches sfmba_total_cost: every observation's image and point
+// index, every image's camera index and every camera's model id are
+// checked on the device before use; any bad entry makes the call return
+// SFMBA_ERR_INVALID_ARGUMENT (and NaN in the output).
+//
 // The host needs the array's device address, which is not the address of
 // the host-side symbol; the first call on each device looks it up with
-// cudaGetSymbolAddress (with that device current) and caches it, so make
-// that first call before any stream capture on the device.
+// cudaGetSymbolAddress (with that device current) and caches it. Every call
+// then reads the bad-index flag back into host memory and waits for its
+// stream, so the call returns only once the result is in place and cannot be
+// made on a stream that is being captured into a CUDA graph.
 #include <mutex>
 
 #include "camera.cuh"
@@ -43,7 +50,6 @@ constexpr int kMaxDevices = 64;
 
 struct NoAllocScratch {
     double sum[kNoAllocMaxBlocks];
-    long long count[kNoAllocMaxBlocks];
     int bad_index;
 };
 
@@ -53,14 +59,23 @@ std::mutex g_noalloc_mutex;
 NoAllocScratch *g_noalloc_ptr[kMaxDevices] = {};
 
 // Per-block partial of the robust cost; indices are range-checked so a bad
-// array is reported instead of read out of bounds.
+// array is reported instead of read out of bounds. The blocks also check
+// every image's camera index and every camera's model, as sfmba_total_cost
+// does on the host, including entries no observation reaches.
 __global__ void __launch_bounds__(kNoAllocThreads)
     k_cost_noalloc_partials(sfmba_problem p, int loss, double scale, NoAllocScratch *scr) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < p.num_images + p.num_cameras;
+         k += stride) {
+        const bool bad = k < p.num_images
+                             ? (p.camera_of_image[k] < 0 || p.camera_of_image[k] >= p.num_cameras)
+                             : model_dof(p.camera_model[k - p.num_images]) == 0;
+        if (bad) atomicOr(&scr->bad_index, 1);
+    }
     const long long begin = blockIdx.x * kNoAllocObsPerBlock;
     long long end = begin + kNoAllocObsPerBlock;
     if (end > p.num_observations) end = p.num_observations;
     double sum = 0.0;
-    long long cnt = 0;
     for (long long o = begin + threadIdx.x; o < end; o += blockDim.x) {
         const int i = p.obs_image[o], pt = p.obs_point[o];
         if (i < 0 || i >= p.num_images || pt < 0 || pt >= p.num_points) {
@@ -78,25 +93,16 @@ __global__ void __launch_bounds__(kNoAllocThreads)
                        X[2], p.obs_xy[2 * o], p.obs_xy[2 * o + 1], rx, ry)) {
             const double n = sqrt(rx * rx + ry * ry);
             sum += robust_weight<double>(n, loss, scale) * n * n;
-            ++cnt;
         }
     }
     __shared__ double ssum[kNoAllocThreads];
-    __shared__ long long scnt[kNoAllocThreads];
     ssum[threadIdx.x] = sum;
-    scnt[threadIdx.x] = cnt;
     __syncthreads();
     for (int w = kNoAllocThreads / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            ssum[threadIdx.x] += ssum[threadIdx.x + w];
-            scnt[threadIdx.x] += scnt[threadIdx.x + w];
-        }
+        if (threadIdx.x < w) ssum[threadIdx.x] += ssum[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        scr->sum[blockIdx.x] = ssum[0];
-        scr->count[blockIdx.x] = scnt[0];
-    }
+    if (threadIdx.x == 0) scr->sum[blockIdx.x] = ssum[0];
 }
 
 // Sums the partials this call wrote, in a fixed order.
@@ -160,9 +166,13 @@ extern "C" int sfmba_total_cost_noalloc(const sfmba_problem *p, const sfmba_opti
                      "holds 4096 partial sums of 4096 observations); use sfmba_total_cost");
         return SFMBA_ERR_INVALID_ARGUMENT;
     }
-    if (p->num_observations > 0 &&
-        (!p->obs_image || !p->obs_point || !p->obs_xy || !p->poses || !p->points || !p->camera_of_image ||
-         !p->camera_model || !p->camera_params)) {
+    if (p->num_images > (1 << 20) || p->num_cameras > (1 << 20)) {
+        record_error("sfmba_total_cost_noalloc: problem too large for 32-bit indices");
+        return SFMBA_ERR_INVALID_ARGUMENT;
+    }
+    if ((p->num_observations > 0 && (!p->obs_image || !p->obs_point || !p->obs_xy || !p->points)) ||
+        (p->num_images > 0 && (!p->poses || !p->camera_of_image)) ||
+        (p->num_cameras > 0 && (!p->camera_model || !p->camera_params))) {
         record_error("sfmba_total_cost_noalloc: a problem array is NULL");
         return SFMBA_ERR_INVALID_ARGUMENT;
     }
@@ -182,8 +192,9 @@ extern "C" int sfmba_total_cost_noalloc(const sfmba_problem *p, const sfmba_opti
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int nblocks = (int)((p->num_observations + kNoAllocObsPerBlock - 1) / kNoAllocObsPerBlock);
     cudaError_t e = cudaMemsetAsync(&scr->bad_index, 0, sizeof(int), s);
-    if (e == cudaSuccess && nblocks > 0) {
-        k_cost_noalloc_partials<<<nblocks, kNoAllocThreads, 0, s>>>(*p, loss, scale, scr);
+    if (e == cudaSuccess && (nblocks > 0 || p->num_images + p->num_cameras > 0)) {
+        // at least one block, so the image and camera checks run without observations
+        k_cost_noalloc_partials<<<nblocks > 0 ? nblocks : 1, kNoAllocThreads, 0, s>>>(*p, loss, scale, scr);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -199,7 +210,8 @@ extern "C" int sfmba_total_cost_noalloc(const sfmba_problem *p, const sfmba_opti
         return SFMBA_ERR_CUDA;
     }
     if (bad) {
-        record_error("sfmba_total_cost_noalloc: observation, image or camera index out of range");
+        record_error("sfmba_total_cost_noalloc: observation, image or camera index out of range, or an "
+                     "unknown camera model id");
         return SFMBA_ERR_INVALID_ARGUMENT;
     }
     return SFMBA_OK;

@@ -1,6 +1,7 @@
-// Vector side of the matrix-free Schur-complement PCG (image level: each
-// free camera belongs to one image, so image blocks and the reference's slot
-// blocks coincide up to order):
+// Vector side of the matrix-free Schur-complement PCG (image level: a free
+// camera of one image is part of that image's block; a camera shared by
+// several images is one slot block kept as copies in its images' blocks, see
+// k_shared.cu):
 //
 //   S p = (H + lambda diag H) p - sum_p E_p^T C_p^-1 E_p p
 //
@@ -78,12 +79,15 @@ __global__ void k_pcg_scalar_init(const double *part, int nI, double tol2, LMSta
     }
 }
 
-// q_i = (H_i + lambda diag H_i) p_i - sum of the image's partials; part[i] = p_i . q_i.
+// q_i = (H_i + lambda diag H_i) p_i - sum of the image's partials; part[i] =
+// p_i . q_i over the image's own columns (pmask; a shared camera's columns
+// are added by launch_shared_qreduce once summed over its images).
 template <typename T, int D>
 __global__ void __launch_bounds__(128) k_pcg_images_finish(const T *__restrict__ ipart,
                                                            const int *__restrict__ ipart_off,
                                                            const double *__restrict__ img_H,
                                                            const int *__restrict__ img_active,
+                                                           const int *__restrict__ img_pmask,
                                                            const T *__restrict__ p, const LMState *__restrict__ st,
                                                            int nI, T *__restrict__ q, double *__restrict__ part) {
     if (st->pcg_done) return;
@@ -92,6 +96,7 @@ __global__ void __launch_bounds__(128) k_pcg_images_finish(const T *__restrict__
     if (i >= nI) return;
     const double lam = st->lambda;
     const int act = img_active[i];
+    const int pm = img_pmask[i];
     const double *H = img_H + (size_t)i * D * D;
     const T *pv = p + (size_t)i * D;
     double pq = 0.0;
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(128) k_pcg_images_finish(const T *__restrict__
         hp += lam * H[c * D + c] * (double)pv[c];
         const double qc = ((act >> c) & 1) ? hp - sch : 0.0;
         q[(size_t)i * D + c] = (T)qc;
-        pq = (double)pv[c] * (double)(T)qc;
+        if ((pm >> c) & 1) pq = (double)pv[c] * (double)(T)qc;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
@@ -137,12 +142,13 @@ __global__ void k_point_chunks(const int *pt_start, int nP, long long nO, int nc
 
 
 // x += alpha p; r -= alpha q; z = M^-1 r; per-image partials of r.z and
-// r.r. alpha = (r.z) / (p.q) with p.q reduced from the image pass's
-// partials by every block in the same order (no separate scalar kernel).
-// One warp per image, 8 images per block.
+// r.r over the columns dmask counts. alpha = (r.z) / (p.q) with p.q reduced
+// from the image pass's partials by every block in the same order (no
+// separate scalar kernel). One warp per image, 8 images per block.
 template <typename T, int D>
-__global__ void __launch_bounds__(256) k_pcg_update(const T *Minv, const T *p, const T *q, LMState *st, int nI,
-                                                    int parity, T *x, T *r, T *z, double *part) {
+__global__ void __launch_bounds__(256) k_pcg_update(const T *Minv, const T *p, const T *q, const int *img_dmask,
+                                                    LMState *st, int nI, int parity, T *x, T *r, T *z,
+                                                    double *part) {
     __shared__ double sh[256];
     if (st->pcg_done) return;
     double a = strided_sum(part + 2 * nI, nI);
@@ -176,8 +182,10 @@ __global__ void __launch_bounds__(256) k_pcg_update(const T *Minv, const T *p, c
     double rz = 0.0, rr = 0.0;
     if (lane < D) {
         z[base + lane] = (T)zc;
-        rz = (double)rc * (double)(T)zc;
-        rr = (double)rc * (double)rc;
+        if ((img_dmask[i] >> lane) & 1) {
+            rz = (double)rc * (double)(T)zc;
+            rr = (double)rc * (double)rc;
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -193,9 +201,11 @@ __global__ void __launch_bounds__(256) k_pcg_update(const T *Minv, const T *p, c
 // Convergence test and p = z + beta p, beta = (r.z)_new / (r.z)_old. Every
 // block reduces the partials itself; block 0 records the new r.z in the
 // other parity slot (read by the next iteration only) and the counters.
+// img_owner (shared cameras, else NULL): a linked image's camera entries of
+// z are its owner's, so p stays a copy of the owner's there.
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const double *part, int nI, int nID,
-                                                 int parity, T *p, int D, T *p4) {
+                                                 int parity, T *p, int D, T *p4, const int *img_owner) {
     __shared__ double sh[256];
     if (st->pcg_done) return;
     double a = strided_sum(part, nI), b = strided_sum(part + nI, nI);
@@ -217,7 +227,12 @@ __global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const 
     if (stop) return;
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= nID) return;
-    const T pn = (T)((double)z[u] + beta * (double)p[u]);
+    int zu = u;
+    if (img_owner) {
+        const int i = u / D, c = u - i * D;
+        if (c >= 6) zu = img_owner[i] * D + c;
+    }
+    const T pn = (T)((double)z[zu] + beta * (double)p[u]);
     p[u] = pn;
     if (p4) {
         const int i = u / D;
@@ -250,21 +265,23 @@ void dispatch_D(int D, F &&f) {
 template <typename T, int D>
 void images_finish_t(const Bufs &b, cudaStream_t s) {
     k_pcg_images_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart, b.ipart_off, b.img_H,
-                                                              b.img_active, (const T *)b.pcg_p, b.state, b.nI,
-                                                              (T *)b.pcg_q, b.pcg_part);
+                                                              b.img_active, b.img_pmask, (const T *)b.pcg_p, b.state,
+                                                              b.nI, (T *)b.pcg_q, b.pcg_part);
     SFMBA_LAUNCH_CHECK();
+    if (b.sh.nsh > 0) launch_shared_qreduce(b, s);
 }
 
 template <typename T, int D>
 void vector_t(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
     k_pcg_update<T, D><<<div_up(b.nI, 8), 256, 0, s>>>((const T *)b.pcg_Minv, (const T *)b.pcg_p,
-                                                       (const T *)b.pcg_q, b.state, b.nI, parity, (T *)b.pcg_x,
-                                                       (T *)b.pcg_r, (T *)b.pcg_z, b.pcg_part);
+                                                       (const T *)b.pcg_q, b.img_dmask, b.state, b.nI, parity,
+                                                       (T *)b.pcg_x, (T *)b.pcg_r, (T *)b.pcg_z, b.pcg_part);
     SFMBA_LAUNCH_CHECK();
     if (coarse) launch_coarse_correct(b, false, s);  // z += Z A_c^-1 Z^T r, new r.z partials
     k_pcg_dir<T><<<div_up(b.nID, 256), 256, 0, s>>>((const T *)b.pcg_z, b.state, b.pcg_part, b.nI, b.nID, parity,
                                                     (T *)b.pcg_p, b.D,
-                                                    std::is_same<T, float>::value ? (T *)(void *)b.pcg_p4 : nullptr);
+                                                    std::is_same<T, float>::value ? (T *)(void *)b.pcg_p4 : nullptr,
+                                                    b.sh.nsh > 0 ? b.sh.img_owner : nullptr);
     SFMBA_LAUNCH_CHECK();
 }
 

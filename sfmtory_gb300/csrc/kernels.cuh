@@ -38,6 +38,32 @@ struct CoarseBufs {
     int lwork = 0;
 };
 
+// Free cameras shared by several images, on the PCG solver. The reduced
+// system has one slot block per camera (lib.rs:753-787); the PCG's vectors
+// are image level, so every image using a shared camera ("linked" image)
+// carries a copy of the camera's entries and the first such image (the
+// owner) holds the ones the preconditioner and the dot products count. The
+// camera's block of the block-Jacobi preconditioner is exact:
+//   sum_i (H_i + lambda diag H_i)_cc - sum_p Y_pc^T C_p^-1 Y_pc,
+// Y_pc = sum over p's observations in images of camera c of Jx~^T Jc~_cam,
+// one (point, camera) incidence each, summed per camera in a fixed order.
+struct SharedBufs {
+    int nsh = 0;                      // shared free cameras (0: none)
+    int *img_owner = nullptr;         // [nI] image holding the camera entries (itself if not linked)
+    int *img_shcam = nullptr;         // [nI] shared-camera index of the image, -1 if not linked
+    int *sh_img_start = nullptr;      // [nsh+1]
+    int *sh_imgs = nullptr;           // images of each shared camera, in image order
+    long long ninc = 0;               // (point, shared camera) incidences
+    long long *inc_off = nullptr;     // [nP+1] first incidence of each point
+    int *inc_sorted = nullptr;        // [ninc] incidences ordered by camera (then point)
+    void *inc_W = nullptr;            // [ninc][NS] upper triangle of Y^T C^-1 Y (kernel precision)
+    int nchunks = 0;
+    int4 *chunk = nullptr;            // [nchunks] {camera, first, end, 0} into inc_sorted
+    int *cam_chunk_off = nullptr;     // [nsh+1]
+    double *chunk_part = nullptr;     // [nchunks][NS]
+};
+constexpr int kSharedChunk = 256;     // incidences per warp in the per-camera sums
+
 struct Bufs {
     // sizes
     int nI = 0, nC = 0, nP = 0;
@@ -65,6 +91,13 @@ struct Bufs {
     int *pt_old2new = nullptr;    // [nP] caller's point index -> solver point index
     int *img_slot = nullptr;      // [nI*D] slot of column r of image i, -1 if not an unknown
     int *img_active = nullptr;    // [nI] bit r: column r is an unknown
+    // Column masks of the PCG vector kernels (both = img_active without
+    // shared cameras): pmask - columns an image's own block-Jacobi block and
+    // coarse space cover (a linked image's camera columns excluded); dmask -
+    // columns counted in dot products (the owner's camera columns included).
+    int *img_pmask = nullptr;     // [nI]
+    int *img_dmask = nullptr;     // [nI]
+    SharedBufs sh;
     int *img_free = nullptr;      // [nI] pose free or camera free
     int *cam_slot = nullptr;      // [nC] first slot of the camera, -1 if fixed
     int *pose_slot = nullptr;     // [nI] first slot of the pose, -1 if fixed
@@ -296,6 +329,21 @@ void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity, bool coarse = 
 void launch_pcg_partition(Bufs &b, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.
 void launch_pcg_finish(const Bufs &b, double *delta_slot, cudaStream_t s);
+
+// ---- shared free cameras on the PCG solver (k_shared.cu)
+size_t shared_setup_temp_bytes(int nP, long long ninc);
+// Distinct shared cameras per point, scanned into b.sh.inc_off; returns the total.
+long long launch_shared_count(const Bufs &b, long long *count, void *temp, size_t temp_bytes, cudaStream_t s);
+// Incidences sorted by camera into b.sh.inc_sorted; cam_counts[c] = incidences of camera c.
+void launch_shared_sort(const Bufs &b, int *key, int *val, int *key2, int *cam_counts, void *temp,
+                        size_t temp_bytes, cudaStream_t s);
+// Per damping retry, after the point inverses and the image-block pass:
+// the shared cameras' exact preconditioner blocks, their rhs, and the PCG
+// start vectors on their columns (after the image blocks' own start).
+void launch_shared_precond(const Bufs &b, cudaStream_t s);
+// q on the shared cameras' columns: summed over each camera's images and
+// copied back to all of them; the owner's p.q partial.
+void launch_shared_qreduce(const Bufs &b, cudaStream_t s);
 
 // ---- coarse correction of the PCG preconditioner (k_coarse.cu)
 size_t coarse_setup_temp_bytes(int nP, long long npairs_max);

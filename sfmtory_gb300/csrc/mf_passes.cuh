@@ -329,6 +329,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
                                                            const double *__restrict__ img_H,
                                                            const double *__restrict__ img_b,
                                                            const int *__restrict__ img_active,
+                                                           const int *__restrict__ img_pmask,
                                                            const LMState *__restrict__ st, int nI,
                                                            double *__restrict__ img_rhs, T *__restrict__ Minv_out,
                                                            T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
@@ -350,6 +351,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
     double *invd = invd_s[wl];
     const double lam = st->lambda;
     const int act = img_active[i];
+    const int pm = img_pmask[i];  // the image's own block (a linked image's camera columns are not in it)
     const double *H = img_H + (size_t)i * D * D;
     const int p0 = ipart_off[i], p1 = ipart_off[i + 1];
     for (int e = lane; e < NV; e += 32) {
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
             const int b = a + t;
             double v = H[a * D + b] - sum;
             if (a == b) v += H[a * D + a] * lam;
-            const bool on = ((act >> a) & 1) && ((act >> b) & 1);
+            const bool on = ((pm >> a) & 1) && ((pm >> b) & 1);
             if (!on) v = a == b ? 1.0 : 0.0;
             L[a][b] = v;
             L[b][a] = v;
@@ -427,7 +429,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
     __syncwarp();
     for (int idx = lane; idx < D * D; idx += 32) {
         const int a = idx / D, c = idx - a * D;
-        const bool on = ((act >> a) & 1) && ((act >> c) & 1);
+        const bool on = ((pm >> a) & 1) && ((pm >> c) & 1);
         if (!on) Mi[a][c] = 0.0;
         Minv_out[(size_t)i * D * D + idx] = (T)Mi[a][c];
     }
@@ -444,8 +446,10 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
         z[u] = zt;
         p[u] = zt;
         if (p4) p4[(size_t)i * pad4(D) + lane] = zt;
-        rz = (double)rt * (double)zt;
-        rr = (double)rt * (double)rt;
+        if ((pm >> lane) & 1) {  // a shared camera's entries are counted by launch_shared_precond
+            rz = (double)rt * (double)zt;
+            rr = (double)rt * (double)rt;
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {

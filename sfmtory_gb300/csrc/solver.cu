@@ -35,6 +35,7 @@ thread_local long long g_kernel_launches = 0;
 namespace {
 
 constexpr int kPcgPollEvery = 8;  // PCG iterations between host convergence polls
+constexpr int kDenseMaxDim = 16384;  // largest reduced system the dense path forms
 
 thread_local std::string g_last_error;
 
@@ -285,7 +286,7 @@ std::string tune_report() {
 struct Context {
     int device = -1;
     cudaStream_t stream = nullptr;
-    Arena main, pairs, aux, coarse;
+    Arena main, pairs, aux, coarse, shared, shared_inc;
     LMState *h_state = nullptr;  // pinned mirror
     int *h_counts = nullptr;     // pinned batch summary
     cusolverDnHandle_t dn = nullptr;  // coarse factorisation (created on first use)
@@ -330,6 +331,12 @@ struct Layout {
     std::vector<int> slot_pre_start, slot_pre;
     std::vector<unsigned char> slot_masked;
     bool injective = true;
+    // Free cameras used by several images (PCG solver, k_shared.cu): the
+    // owner image (first user) of each image's camera columns, its shared-
+    // camera index, the column masks of the PCG vector kernels, and the
+    // images of each shared camera in image order.
+    std::vector<int> img_owner, img_shcam, img_pmask, img_dmask;
+    std::vector<int> sh_img_start, sh_imgs;
 };
 
 Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> &cam_of_img,
@@ -388,6 +395,35 @@ Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> 
     }
     for (int c = 0; c < nC; ++c)
         if (cam_users[c] > 1) L.injective = false;
+    L.img_owner.resize(nI);
+    L.img_shcam.assign(nI, -1);
+    L.img_pmask = L.img_active;
+    L.img_dmask = L.img_active;
+    std::vector<int> owner(nC, -1), shidx(nC, -1), sh_count;
+    for (int i = 0; i < nI; ++i) {
+        const int c = cam_of_img[i];
+        L.img_owner[i] = i;
+        if (L.cam_slot[c] < 0 || cam_users[c] < 2) continue;
+        if (owner[c] < 0) {
+            owner[c] = i;
+            shidx[c] = (int)sh_count.size();
+            sh_count.push_back(0);
+        }
+        L.img_owner[i] = owner[c];
+        L.img_shcam[i] = shidx[c];
+        sh_count[shidx[c]] += 1;
+        L.img_pmask[i] = L.img_active[i] & 0x3f;
+        if (owner[c] != i) L.img_dmask[i] = L.img_active[i] & 0x3f;
+    }
+    const int nsh = (int)sh_count.size();
+    L.sh_img_start.assign(nsh + 1, 0);
+    for (int k = 0; k < nsh; ++k) L.sh_img_start[k + 1] = L.sh_img_start[k] + sh_count[k];
+    L.sh_imgs.resize(L.sh_img_start[nsh]);
+    {
+        std::vector<int> fill(L.sh_img_start.begin(), L.sh_img_start.end() - 1);
+        for (int i = 0; i < nI; ++i)
+            if (L.img_shcam[i] >= 0) L.sh_imgs[fill[L.img_shcam[i]]++] = i;
+    }
     L.slot_pre_start.assign(n + 1, 0);
     for (int a = 0; a < n; ++a) L.slot_pre_start[a + 1] = L.slot_pre_start[a] + (int)pre[a].size();
     L.slot_pre.reserve(L.slot_pre_start[n]);
@@ -811,6 +847,75 @@ class Solver {
         put_vec(co.chunk, chunks, s_);
     }
 
+    // Shared free cameras on the PCG solver (k_shared.cu), once per solve:
+    // the images of each shared camera, the (point, camera) incidences
+    // sorted by camera and cut into chunks of kSharedChunk, and the buffers
+    // of the per-retry camera blocks. tsz: element size of the kernel
+    // precision (double when an FP64 polish may follow).
+    void setup_shared(size_t tsz) {
+        Bufs &b = b_;
+        SharedBufs &sh = b.sh;
+        const int nsh = (int)lay_.sh_img_start.size() - 1;
+        const int nI = b.nI, nP = b.nP, D = b.D;
+        const int KC = D - 6, NS = KC * (KC + 1) / 2;
+        Arena &A = ctx_.shared;
+        long long *count = nullptr;
+        void *temp = nullptr;
+        int *cam_counts = nullptr;
+        size_t t1 = shared_setup_temp_bytes(nP, 1);
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) A.begin_sizing(); else A.commit();
+            sh.img_owner = A.take<int>(nI);
+            sh.img_shcam = A.take<int>(nI);
+            sh.sh_img_start = A.take<int>((size_t)nsh + 1);
+            sh.sh_imgs = A.take<int>(lay_.sh_imgs.size());
+            sh.inc_off = A.take<long long>((size_t)nP + 1);
+            sh.cam_chunk_off = A.take<int>((size_t)nsh + 1);
+            cam_counts = A.take<int>(nsh);
+            count = A.take<long long>((size_t)nP + 1);
+            temp = A.take<char>(t1);
+        }
+        sh.nsh = nsh;
+        put_vec(sh.img_owner, lay_.img_owner, s_);
+        put_vec(sh.img_shcam, lay_.img_shcam, s_);
+        put_vec(sh.sh_img_start, lay_.sh_img_start, s_);
+        put_vec(sh.sh_imgs, lay_.sh_imgs, s_);
+        sh.ninc = launch_shared_count(b, count, temp, t1, s_);
+        if (sh.ninc > (1LL << 31) - 1)
+            throw Error(SFMBA_ERR_UNSUPPORTED, "too many point-camera incidences for the shared-camera blocks");
+        const size_t t2 = shared_setup_temp_bytes(nP, sh.ninc);
+        Arena &P = ctx_.shared_inc;
+        int *key = nullptr, *val = nullptr, *key2 = nullptr;
+        void *temp2 = nullptr;
+        const long long max_chunks = sh.ninc / kSharedChunk + nsh + 1;
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 0) P.begin_sizing(); else P.commit();
+            key = P.take<int>(sh.ninc);
+            val = P.take<int>(sh.ninc);
+            key2 = P.take<int>(sh.ninc);
+            temp2 = P.take<char>(t2);
+            sh.inc_sorted = P.take<int>(sh.ninc);
+            sh.inc_W = P.take<char>((size_t)sh.ninc * NS * tsz);
+            sh.chunk = P.take<int4>(max_chunks);
+            sh.chunk_part = P.take<double>((size_t)max_chunks * NS);
+        }
+        launch_shared_sort(b, key, val, key2, cam_counts, temp2, t2, s_);
+        const std::vector<int> cnt = fetch(cam_counts, (size_t)nsh, true, s_);
+        std::vector<int4> chunks;
+        std::vector<int> off{0};
+        int pos = 0;
+        for (int c = 0; c < nsh; ++c) {
+            for (int a = 0; a < cnt[c]; a += kSharedChunk)
+                chunks.push_back(make_int4(c, pos + a, pos + std::min(cnt[c], a + kSharedChunk), 0));
+            off.push_back((int)chunks.size());
+            pos += cnt[c];
+        }
+        sh.nchunks = (int)chunks.size();
+        put_vec(sh.chunk, chunks, s_);
+        put_vec(sh.cam_chunk_off, off, s_);
+        SFMBA_CUDA(cudaStreamSynchronize(s_));  // host vectors above go out of scope
+    }
+
     // A_c for this retry, FP32 Cholesky and inverse; false (block-Jacobi
     // alone for this retry) when the factorisation breaks down.
     bool factor_coarse() {
@@ -866,13 +971,10 @@ class Solver {
         } else if (o->solver == SFMBA_SOLVER_PCG) solver_ = SFMBA_SOLVER_PCG;
         else if (o->solver == SFMBA_SOLVER_AUTO)
             solver_ = (n <= std::max(1, o->dense_max_dim)) ? SFMBA_SOLVER_DENSE : SFMBA_SOLVER_PCG;
-        if (solver_ == SFMBA_SOLVER_PCG && !lay_.injective)
-            throw Error(SFMBA_ERR_UNSUPPORTED,
-                        "the PCG solver needs every free camera to belong to one image; use the dense solver");
-        if (!batch && solver_ == SFMBA_SOLVER_DENSE && n > 16384)
-            throw Error(SFMBA_ERR_UNSUPPORTED, "dense reduced system above 16384 unknowns; use the PCG solver");
-        if (solver_ == SFMBA_SOLVER_DENSE && nI > 65535)
-            throw Error(SFMBA_ERR_UNSUPPORTED, "dense solver supports at most 65535 images; use the PCG solver");
+        // The dense path holds S, its factor and the image-level Schur blocks
+        // (3 n^2 + (nI D)^2 doubles); larger systems go to the PCG solver,
+        // which takes every camera-sharing pattern (k_shared.cu).
+        if (!batch && solver_ == SFMBA_SOLVER_DENSE && (n > kDenseMaxDim || nI > 65535)) solver_ = SFMBA_SOLVER_PCG;
         const int nID = nI * D;
         // The mixed path may finish in FP64 (fp64_polish): its typed buffers
         // are sized for doubles so the same allocation serves both precisions.
@@ -960,6 +1062,8 @@ class Solver {
             b.img_obs = A.take<int>(nO);
             b.img_slot = A.take<int>((size_t)nID);
             b.img_active = A.take<int>(nI);
+            b.img_pmask = A.take<int>(nI);
+            b.img_dmask = A.take<int>(nI);
             b.img_free = A.take<int>(nI);
             b.cam_slot = A.take<int>(nC);
             b.pose_slot = A.take<int>(nI);
@@ -1083,6 +1187,8 @@ class Solver {
         }
         put_vec(b.img_slot, lay_.img_slot, s_);
         put_vec(b.img_active, lay_.img_active, s_);
+        put_vec(b.img_pmask, lay_.img_pmask, s_);
+        put_vec(b.img_dmask, lay_.img_dmask, s_);
         put_vec(b.img_free, lay_.img_free, s_);
         put_vec(b.cam_slot, lay_.cam_slot, s_);
         put_vec(b.pose_slot, lay_.pose_slot, s_);
@@ -1113,6 +1219,8 @@ class Solver {
                 b.nparts = off[nI];
                 put_vec(b.ipart_off, off, s_);
                 setup_coarse(o->pcg_coarse_clusters);
+                b.sh = SharedBufs();
+                if (lay_.sh_img_start.size() > 1) setup_shared(tsz);
             }
             // Image-aligned chunks of the image-block passes.
             std::vector<int4> ia;
@@ -1259,6 +1367,7 @@ class Solver {
                     {
                         SFMBA_PHASE(PH_PCG_PRECOND);
                         if (!fused) launch_mf_precond(b, s_);
+                        if (b.sh.nsh > 0) launch_shared_precond(b, s_);
                         if (coarse) launch_coarse_correct(b, true, s_);
                         launch_pcg_start(b, s_);
                     }

@@ -91,6 +91,7 @@ def load(path: str | None = None):
         L.sfmba_colmap_model_stats.argtypes = [C.c_char_p, vp, vp]
         L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
         L.sfmba_total_cost_noalloc.argtypes = [vp, vp, vp, vp]
+        L.sfmba_local_windows.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp]
         L.sfmba_profile_enable.argtypes = [C.c_int32]
         L.sfmba_profile_report.argtypes = [C.c_char_p, C.c_int64]
         L.sfmba_last_error.restype = C.c_char_p
@@ -191,6 +192,70 @@ def residuals_jacobians(problem, fp32: bool = False):
     _check(L.sfmba_residuals_jacobians(C.byref(packed.struct), 1 if fp32 else 0, r.ctypes.data,
                                        jp.ctypes.data, jx.ctypes.data, jc.ctypes.data, valid.ctypes.data))
     return r, jp, jx, jc, valid.astype(bool)
+
+
+def local_windows(rec, centers, seed_image: int = -1, num_free_neighbours: int = 6):
+    """BaScope::Local windows (crates/sfm-reconstruction/src/lib.rs:1336-1473)
+    of a :class:`~sfmtory_gb300.problem.Reconstruction` for each centre image,
+    through sfmba_local_windows. Returns, per centre, None where the
+    reference makes no solve, else (Problem, image_ids, camera_ids,
+    point_ids) with the reconstruction indices of the window's entries."""
+    from .abi import SfmbaReconstruction, SfmbaWindowBuffers
+    from .problem import Problem
+
+    L = load()
+    keep = []
+
+    def ptr(a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a.ctypes.data
+
+    R = SfmbaReconstruction()
+    R.num_images, R.num_cameras, R.num_points = len(rec.poses), len(rec.camera_model), len(rec.points)
+    R.camera_of_image = ptr(rec.camera_of_image, np.int32)
+    R.camera_model = ptr(rec.camera_model, np.int32)
+    cp = np.zeros((len(rec.camera_model), 8))
+    cp[:, : np.asarray(rec.camera_params).shape[1]] = rec.camera_params
+    R.camera_params = ptr(cp, np.float64)
+    R.poses = ptr(rec.poses, np.float64)
+    R.registered = ptr(rec.registered, np.uint8)
+    R.pose_fixed = ptr(rec.pose_fixed, np.uint8) if rec.pose_fixed is not None else None
+    R.points = ptr(rec.points, np.float64)
+    R.track_offsets = ptr(rec.track_offsets, np.int64)
+    R.track_image = ptr(rec.track_image, np.int32)
+    R.track_xy = ptr(np.asarray(rec.track_xy, np.float64).reshape(-1, 2), np.float64)
+    cen = np.ascontiguousarray(centers, dtype=np.int32)
+    counts = np.zeros((len(cen), 4), np.int64)
+    _check(L.sfmba_local_windows(C.byref(R), int(seed_image), int(num_free_neighbours), len(cen), cen.ctypes.data,
+                                 counts.ctypes.data, None))
+    bufs = (SfmbaWindowBuffers * max(1, len(cen)))()
+    arrays = []
+    for k, (nI, nC, nP, nO) in enumerate(counts):
+        a = dict(image_ids=np.zeros(nI, np.int32), camera_ids=np.zeros(nC, np.int32), point_ids=np.zeros(nP, np.int32),
+                 camera_of_image=np.zeros(nI, np.int32), camera_model=np.zeros(nC, np.int32),
+                 camera_params=np.zeros((nC, 8)), poses=np.zeros((nI, 7)), points=np.zeros((nP, 3)),
+                 obs_image=np.zeros(nO, np.int32), obs_point=np.zeros(nO, np.int32), obs_xy=np.zeros((nO, 2)),
+                 fixed_poses=np.zeros(nI, np.uint8), fixed_cameras=np.zeros(nC, np.uint8),
+                 fixed_camera_params=np.zeros((nC, 8), np.uint8))
+        for name, arr in a.items():
+            setattr(bufs[k], name, arr.ctypes.data if arr.size else None)
+        arrays.append(a)
+    _check(L.sfmba_local_windows(C.byref(R), int(seed_image), int(num_free_neighbours), len(cen), cen.ctypes.data,
+                                 counts.ctypes.data, bufs))
+    out = []
+    for k, a in enumerate(arrays):
+        if counts[k, 3] == 0:
+            out.append(None)
+            continue
+        prob = Problem(camera_of_image=a["camera_of_image"], camera_model=a["camera_model"],
+                       camera_params=a["camera_params"], poses=a["poses"], points=a["points"],
+                       obs_image=a["obs_image"], obs_point=a["obs_point"], obs_xy=a["obs_xy"],
+                       fixed_poses=a["fixed_poses"].astype(bool), fixed_cameras=a["fixed_cameras"].astype(bool),
+                       fixed_camera_params=a["fixed_camera_params"].astype(bool),
+                       meta={"name": "local_window", "center": int(cen[k])})
+        out.append((prob, a["image_ids"], a["camera_ids"], a["point_ids"]))
+    return out
 
 
 def bundle_adjust_batched_arrays(problems, opts: SfmbaOptions | None = None, **kw) -> list[Result]:

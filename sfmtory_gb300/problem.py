@@ -100,6 +100,28 @@ class Problem:
 
 # ---------------------------------------------------------------- quaternions
 
+@dataclass
+class Reconstruction:
+    """A reconstruction in progress, as sfm-reconstruction holds it while it
+    grows (crates/sfm-reconstruction/src/lib.rs:126-129 `PointWork`: a
+    point's position and its track of (image, keypoint)), in array form:
+    tracks are CSR (``track_offsets`` [nP+1]) with each element's image and
+    keypoint pixel; ``registered`` images have valid poses; ``pose_fixed``
+    marks poses the caller pinned."""
+
+    camera_of_image: np.ndarray
+    camera_model: np.ndarray
+    camera_params: np.ndarray
+    poses: np.ndarray
+    registered: np.ndarray
+    points: np.ndarray
+    track_offsets: np.ndarray
+    track_image: np.ndarray
+    track_xy: np.ndarray
+    pose_fixed: Optional[np.ndarray] = None
+    meta: dict = field(default_factory=dict)
+
+
 def quat_from_euler(roll: float, pitch: float, yaw: float) -> np.ndarray:
     """Unit quaternion (w, x, y, z) of R = Rz(yaw) Ry(pitch) Rx(roll): the
     roll-pitch-yaw convention of nalgebra's UnitQuaternion::from_euler_angles,
@@ -260,3 +282,57 @@ def rms_reprojection_error(p: Problem) -> float:
     if not valid.any():
         return 0.0
     return float(np.sqrt(np.mean(np.sum(r[valid] ** 2, axis=1))))
+
+
+def camera_centers(poses: np.ndarray) -> np.ndarray:
+    """World position of each camera, C = -R^T t, for poses [n, 7]."""
+    q = np.asarray(poses[:, :4], np.float64)
+    qc = q * np.array([1.0, -1.0, -1.0, -1.0])
+    return -quat_rotate(qc, np.asarray(poses[:, 4:], np.float64))
+
+
+def _rel(a: np.ndarray, b: np.ndarray) -> float:
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    if a.size == 0:
+        return 0.0
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0)))
+
+
+def parameter_errors(poses, points, camera_params, ref_poses, ref_points, ref_camera_params,
+                     anchor: int = 0, second: int = 1) -> dict:
+    """Errors of one solution's parameters against a reference solution.
+
+    raw: max over entries of |a - b| / max(|b|, 1), per group (poses, points,
+    cameras). normalized: the same after removing the free scale of a problem
+    whose gauge is fixed by one pose (crates/sfm-ba/src/lib.rs:1454-1460):
+    each solution's camera centres and points are taken relative to the
+    anchor camera's centre C0 and divided by that solution's |C1 - C0|
+    (C1: the centre of image ``second``); rotations and intrinsics are
+    scale-free and compared as they are (quaternions sign-aligned).
+    """
+    out = {"raw": {"poses": _rel(poses, ref_poses), "points": _rel(points, ref_points),
+                   "cameras": _rel(camera_params, ref_camera_params)}}
+    ca, cb = camera_centers(np.asarray(poses)), camera_centers(np.asarray(ref_poses))
+    sa = np.linalg.norm(ca[second] - ca[anchor]) if len(ca) > max(anchor, second) else 1.0
+    sb = np.linalg.norm(cb[second] - cb[anchor]) if len(cb) > max(anchor, second) else 1.0
+    sa, sb = (sa if sa > 0 else 1.0), (sb if sb > 0 else 1.0)
+    qa, qb = np.asarray(poses, np.float64)[:, :4], np.asarray(ref_poses, np.float64)[:, :4]
+    qa = qa * np.where(np.sum(qa * qb, axis=1, keepdims=True) < 0, -1.0, 1.0)
+    pa = (np.asarray(points, np.float64) - ca[anchor]) / sa
+    pb = (np.asarray(ref_points, np.float64) - cb[anchor]) / sb
+    out["normalized"] = {
+        "rotations": _rel(qa, qb),
+        "centers": _rel((ca - ca[anchor]) / sa, (cb - cb[anchor]) / sb),
+        "points": _rel(pa, pb),
+        "cameras": _rel(camera_params, ref_camera_params),
+    }
+    out["raw_max"] = max(out["raw"].values())
+    out["normalized_max"] = max(out["normalized"].values())
+    out["scale_ratio"] = float(sa / sb)
+    return out
+
+
+def rms_of(p: Problem, poses, points, camera_params) -> float:
+    """RMS reprojection error (px) of p's observations under the given parameters."""
+    return rms_reprojection_error(p.copy(poses=np.asarray(poses), points=np.asarray(points),
+                                         camera_params=np.asarray(camera_params)))

@@ -404,6 +404,115 @@ def radial2000(seed: int = 0, scale: float = 1.0) -> Problem:
         mask_principal_point=True, name="radial2000", extra_meta={"seed": seed, "scale": scale})
 
 
+def reconstruction_in_progress(seed: int = 0, n_images: int = 60, n_points: int = 6000, n_cameras: int = 3,
+                               unregistered: float = 0.15, pinned: int = 2):
+    """A reconstruction part way through incremental growth, for the local
+    bundle-adjustment windows (crates/sfm-reconstruction/src/lib.rs:
+    1287-1299, :1336-1473): ``n_images`` on a 120 degree arc of radius 8
+    around a radius-2 ball of points, taken with ``n_cameras`` physical
+    cameras (PINHOLE / SIMPLE_RADIAL / RADIAL, consecutive runs of images);
+    each point's track covers a run of 1 + Poisson(4) consecutive images (so
+    some tracks have a single element); a fraction ``unregistered`` of the
+    images is not registered yet (their track elements stay in the tracks);
+    ``pinned`` registered images carry caller-pinned poses. Keypoints are the
+    true projections plus 0.5 px noise, rounded to float32; poses and points
+    are perturbed as in the benchmark scenes."""
+    from .problem import Reconstruction
+
+    rng = np.random.default_rng(seed)
+    ang = np.deg2rad(np.linspace(-60.0, 60.0, n_images))
+    centers = np.stack([8.0 * np.cos(ang), 8.0 * np.sin(ang), rng.uniform(-0.5, 0.5, n_images)], 1)
+    poses_true = look_at_pose(centers, np.zeros(3))
+    group = (np.arange(n_images) * n_cameras // n_images).astype(np.int32)
+    models = np.array([(PINHOLE, SIMPLE_RADIAL, RADIAL)[c % 3] for c in range(n_cameras)], np.int32)
+    cams = np.zeros((n_cameras, MAX_CAMERA_PARAMS))
+    for c, m in enumerate(models):
+        f = rng.uniform(1000, 1400)
+        cams[c, :(4 if m != RADIAL else 5)] = {PINHOLE: [f, f * 1.01, 800, 600], SIMPLE_RADIAL: [f, 800, 600, 0.01],
+                                   RADIAL: [f, 800, 600, 0.01, -0.002]}[int(m)]
+    d = rng.normal(size=(n_points, 3))
+    pts_true = d / np.linalg.norm(d, axis=1, keepdims=True) * (2.0 * rng.random(n_points) ** (1 / 3))[:, None]
+    lens = 1 + rng.poisson(4.0, n_points)
+    start = rng.integers(0, n_images, n_points)
+    off = [0]
+    t_img, t_xy = [], []
+    for p in range(n_points):
+        imgs = [int(start[p]) + k for k in range(lens[p])]
+        imgs = [i for i in imgs if i < n_images]
+        pc = camera_frame(poses_true[imgs], np.repeat(pts_true[p:p + 1], len(imgs), 0))
+        ok = pc[:, 2] > 0.1
+        imgs = [i for i, o in zip(imgs, ok) if o]
+        if not imgs:
+            off.append(off[-1])
+            continue
+        pc = camera_frame(poses_true[imgs], np.repeat(pts_true[p:p + 1], len(imgs), 0))
+        uv = project(models[group[imgs]], cams[group[imgs]], pc)
+        uv = (uv + rng.normal(0.0, 0.5, uv.shape)).astype(np.float32).astype(np.float64)
+        t_img.extend(imgs)
+        t_xy.extend(uv.tolist())
+        off.append(off[-1] + len(imgs))
+    registered = rng.random(n_images) >= unregistered
+    registered[0] = True
+    axis = rng.normal(size=(n_images, 3))
+    axis /= np.linalg.norm(axis, axis=1, keepdims=True)
+    tdir = rng.normal(size=(n_images, 3))
+    tdir /= np.linalg.norm(tdir, axis=1, keepdims=True)
+    delta = np.concatenate([axis * np.deg2rad(0.5), tdir * 0.05], 1)
+    delta[0] = 0.0
+    poses = perturb_pose(poses_true, delta)
+    pdir = rng.normal(size=pts_true.shape)
+    pdir /= np.linalg.norm(pdir, axis=1, keepdims=True)
+    points = pts_true + pdir * 0.02
+    pose_fixed = np.zeros(n_images, bool)
+    reg_idx = np.flatnonzero(registered)
+    if pinned:
+        pose_fixed[rng.choice(reg_idx[1:], min(pinned, len(reg_idx) - 1), replace=False)] = True
+    return Reconstruction(camera_of_image=group, camera_model=models, camera_params=cams, poses=poses,
+                          registered=registered, points=points, track_offsets=np.asarray(off, np.int64),
+                          track_image=np.asarray(t_img, np.int32),
+                          track_xy=np.asarray(t_xy, np.float64).reshape(-1, 2), pose_fixed=pose_fixed,
+                          meta={"name": "reconstruction_in_progress", "seed": seed})
+
+
+def shared_radial(seed: int = 0, scale: float = 1.0, n_cameras: int = 1) -> Problem:
+    """radial2000's geometry (2000 images on a smooth loop, 1M points,
+    power-law tracks; ``scale`` shrinks points and images together) taken
+    with ``n_cameras`` physical RADIAL cameras, each used by a consecutive
+    run of images: the global adjustment of a sequence shot with one or a
+    few cameras, where every camera is one free block shared by many images
+    (crates/sfm-reconstruction/src/lib.rs:1489-1520). Observations are
+    projected with the shared true cameras (f U[900,1500], k1 U[-0.05,0.05],
+    k2 U[-0.01,0.01]); each camera starts with a 3 % focal error; principal
+    points masked; pose 0 fixed."""
+    rng = np.random.default_rng(seed)
+    n_img = 2000 if scale >= 1 else max(16, int(round(2000 * scale ** 0.5)))
+    n_cameras = max(1, min(n_cameras, n_img))
+    poses_true = _smooth_loop(rng, n_img, 20.0, 2.0, 0.05)
+    group = (np.arange(n_img) * n_cameras // n_img).astype(np.int32)
+    phys = np.zeros((n_cameras, MAX_CAMERA_PARAMS))
+    phys[:, 0] = rng.uniform(900, 1500, n_cameras)
+    phys[:, 1], phys[:, 2] = 800.0, 600.0
+    phys[:, 3] = rng.uniform(-0.05, 0.05, n_cameras)
+    phys[:, 4] = rng.uniform(-0.01, 0.01, n_cameras)
+    cam_true = phys[group]
+    n_pts = max(16, int(round(1_000_000 * scale)))
+    d = rng.normal(size=(n_pts, 3))
+    pts = d / np.linalg.norm(d, axis=1, keepdims=True) * (3.0 * rng.random(n_pts) ** (1 / 3))[:, None]
+    counts = power_law_counts(rng, n_pts, hi=min(200, n_img))
+    views_img, views_pt = _contiguous_views(rng, n_img, counts, loop=True)
+    p = _finish_scene(
+        rng, cam_model=np.full(n_img, RADIAL), cam_true=cam_true,
+        image_wh=np.tile([1600.0, 1200.0], (n_img, 1)), poses_true=poses_true, pts_true=pts,
+        views_img=views_img, views_pt=views_pt, noise_px=0.5, outlier_frac=0.0,
+        fixed_first_pose=True, rot_deg=1.0, trans_abs=0.4, point_rel=0.01, focal_rel=0.03,
+        mask_principal_point=True, name="shared_radial",
+        extra_meta={"seed": seed, "scale": scale, "n_cameras": n_cameras})
+    first = np.searchsorted(group, np.arange(n_cameras))
+    return p.copy(camera_of_image=group, camera_model=p.camera_model[first], camera_params=p.camera_params[first],
+                  fixed_cameras=np.zeros(n_cameras, bool), fixed_camera_params=p.fixed_camera_params[first],
+                  meta=dict(p.meta, true_camera_params=phys))
+
+
 def local_window(rng, n_cam, n_pts, views=5.0, models=(PINHOLE, SIMPLE_RADIAL, OPENCV)) -> Problem:
     """One local-BA window: ``n_cam`` cameras on a 60 degree arc of radius 8
     looking at a radius-2 ball of ``n_pts`` points, each seen by

@@ -1,0 +1,45 @@
+"""Local bundle-adjustment windows built from a reconstruction in progress
+(sfmba_local_windows, the reference's BaScope::Local construction) and solved
+together in one sfmba_bundle_adjust_batched call, each against the FP64
+oracle run on that window alone (as the reference runs one local bundle per
+registration, crates/sfm-reconstruction/src/lib.rs:708-719).
+
+Bars: FP64 batch - same iterations, final cost and parameters 1e-6
+relative; mixed batch - final cost 1e-6 relative."""
+import numpy as np
+import pytest
+
+from sfmtory_gb300 import abi, native, scenes
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=2.0, max_iterations=50)  # BaParams::default()
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.maximum(np.abs(np.asarray(b)), 1.0)))
+
+
+@pytest.fixture(scope="module")
+def windows():
+    rec = scenes.reconstruction_in_progress(seed=11, n_images=60, n_points=6000, n_cameras=3)
+    centers = [int(c) for c in np.flatnonzero(rec.registered)[::3]]
+    built = [w for w in native.local_windows(rec, centers, seed_image=0) if w is not None]
+    assert len(built) >= 10
+    return [w[0] for w in built]
+
+
+def test_local_windows_batched_fp64_follow_oracle(oracle_lib, windows):
+    got = native.bundle_adjust_batched_arrays(windows, **KW)
+    for p, g in zip(windows, got):
+        r = oracle_lib.bundle_adjust(p, **KW)
+        assert g.iterations_run == r.iterations_run
+        assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost
+        assert _rel(g.points, r.points) <= 1e-6 and _rel(g.poses, r.poses) <= 1e-6
+
+
+def test_local_windows_batched_mixed_reach_oracle_cost(oracle_lib, windows):
+    got = native.bundle_adjust_batched_arrays(windows, precision=abi.PRECISION_MIXED, **KW)
+    for p, g in zip(windows, got):
+        r = oracle_lib.bundle_adjust(p, **KW)
+        assert g.final_cost <= r.final_cost * (1 + 1e-6), (g.final_cost, r.final_cost)

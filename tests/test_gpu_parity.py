@@ -224,11 +224,20 @@ def test_pcg_mixed_radial_reaches_oracle_cost(oracle_lib):
     assert abs(g64.final_cost - r.final_cost) <= 1e-6 * r.final_cost
 
 
-def test_pcg_rejects_shared_free_camera():
-    p = scenes.shared_focal_fixture().copy(fixed_cameras=np.array([False]))
-    with pytest.raises(native.SfmbaError) as e:
-        native.bundle_adjust_arrays(p, solver=abi.SOLVER_PCG)
-    assert e.value.status == 5
+def test_pcg_shared_free_camera_matches_oracle(oracle_lib):
+    """The reference's joint-focal test scene (one camera shared by four
+    images, lib.rs:1487-1592) on the PCG solver: the shared camera is one
+    unknown block, as in the reference's slotting (lib.rs:753-787)."""
+    p = scenes.shared_focal_fixture()
+    pre = oracle_lib.bundle_adjust(p, max_iterations=50)
+    joint = p.copy(poses=pre.poses, points=pre.points, fixed_cameras=np.array([False]))
+    r = oracle_lib.bundle_adjust(joint, max_iterations=50)
+    g = native.bundle_adjust_arrays(joint, max_iterations=50, solver=abi.SOLVER_PCG, pcg_tolerance=1e-12,
+                                    pcg_max_iterations=500)
+    assert g.solver_used == abi.SOLVER_PCG
+    assert abs(g.camera_params[0, 0] - 1500.0) / 1500.0 < 0.02
+    assert abs(g.camera_params[0, 0] - r.camera_params[0, 0]) < 1e-6 * 1500
+    assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost + 1e-12
 
 
 def test_profile_report_counts_phases():
