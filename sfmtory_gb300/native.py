@@ -41,6 +41,7 @@ EXPORTED_SYMBOLS = (
     "sfmba_adjust_global",
     "sfmba_refine_pose_gauss_newton_batched",
     "sfmba_pnp_ransac_batched",
+    "sfmba_local_windows",
     "sfmba_colmap_refine",
     "sfmba_colmap_rewrite",
     "sfmba_colmap_model_stats",
