@@ -16,9 +16,14 @@
 // of at most kCoarseChunk points; one warp per chunk forms the chunk's
 // D x D contribution with the register-tiled product of the Schur
 // reduction (inner dimension 3 per point), and one block per group sums its
-// chunks in order — no atomics, so A_c is bit-reproducible. A_c is factored
-// and inverted in FP32 by cuSOLVER (it is small: clusters x D <= 1408) and
-// applied as a dense product each iteration.
+// chunks in order — no atomics, so A_c is bit-reproducible. A_c is small
+// (clusters x D <= 1792) and is inverted in FP32 by a block sweep in one
+// cooperative launch (k_coarse_sweep below); the inverse is applied as a
+// dense product each iteration.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
 #include <cub/cub.cuh>
 
 #include "mf_passes.cuh"
@@ -289,7 +294,7 @@ __global__ void __launch_bounds__(32 * coarse_warps<T>()) k_coarse_pairs(const T
 
 // Group g's chunks summed in order into block (c, c') of A_c, and its
 // transpose into (c', c) for c != c'. Columns that are not unknowns of any
-// image are left at zero (k_coarse_to32 puts 1 on their diagonal).
+// image are left at zero (k_coarse_sweep puts 1 on their diagonal).
 __global__ void k_coarse_finish(const double *part, const int *group_chunk_off, const int2 *group_cc, int ngroups,
                                 int nc, int D, double *A) {
     const int g = blockIdx.x;
@@ -305,29 +310,182 @@ __global__ void k_coarse_finish(const double *part, const int *group_chunk_off, 
     }
 }
 
-// FP32 copy for the factorisation: diagonal scaled by (1 + 1e-6) (keeps the
-// FP32 Cholesky of a nearly singular coarse matrix away from breakdown; it
-// is a preconditioner), an empty row/column gets a unit diagonal; Ainv = I.
-__global__ void k_coarse_to32(const double *A, int Nc, float *A32, float *Ainv) {
-    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (e >= (long long)Nc * Nc) return;
-    const int r = (int)(e / Nc), c = (int)(e - (long long)r * Nc);
-    double v = A[e];
-    if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + 1e-6);
-    A32[e] = (float)v;
-    Ainv[e] = r == c ? 1.f : 0.f;
+// ------------------------------------------------------------ coarse inverse
+// A_c^-1 by the block sweep (Gauss-Jordan elimination in place, symmetric
+// positive definite, pivot blocks of kSwPiv in order, no pivoting). Sweeping
+// the pivot block K of the current matrix M with P = M_KK^-1 gives
+//   M_KK <- -P,  M_RK <- M_RK P,  M_KR <- P M_KR,  M_RR <- M_RR - M_RK P M_KR
+// (R: every other index); after every block is swept M = -A^-1. The pivot
+// block of an unswept K is a Schur complement of A, so it stays positive
+// definite. Every step is a rank-32 update of the whole matrix, written to
+// the other of two buffers (ping-pong), so one grid barrier per step
+// suffices. The matrix is padded to a multiple of kSwTile with an identity
+// block (its inverse is the identity, and it does not couple to A). The
+// whole sweep is FP32: n^3 FP64 operations would take ~0.3 ms at the GPU's
+// FP64 rate, and the inverse is a preconditioner applied in FP32.
+//
+// Each block computes the step's P itself (one warp, rows in registers,
+// the scalar sweep with shuffles), from the same data in the same order, so
+// every block gets the same P and the same pivot test: a pivot that is not
+// > 0 (or a non-finite one) stops every block at the same step, before the
+// next barrier. Then the block writes its 64 x 64 output tiles.
+constexpr int kSwPiv = 32;
+constexpr int kSwTile = 64;
+
+// Lane r of the calling warp holds row r of the 32 x 32 block; on return it
+// holds row r of -A^-1 (the block swept on every index). False if a pivot
+// is not > 0 or not finite (the same answer in every lane).
+__device__ __forceinline__ bool sweep32(float (&a)[kSwPiv], int lane) {
+#pragma unroll
+    for (int j = 0; j < kSwPiv; ++j) {
+        const float piv = __shfl_sync(0xffffffffu, a[j], j);
+        const float ip = 1.0f / piv;
+        if (!(piv > 0.0f) || !isfinite(ip)) return false;
+        const float f = a[j];
+#pragma unroll
+        for (int c = 0; c < kSwPiv; ++c) {
+            if (c == j) continue;
+            const float ajc = __shfl_sync(0xffffffffu, a[c], j) * ip;
+            a[c] = lane == j ? ajc : fmaf(-f, ajc, a[c]);
+        }
+        a[j] = lane == j ? -ip : f * ip;
+    }
+    return true;
 }
 
-// Ainv = (X + X^T) / 2 for the solve's result X (the preconditioner must be
-// symmetric; the FP32 solve leaves rounding-level asymmetry).
-__global__ void k_coarse_sym(float *Ainv, int Nc) {
-    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (e >= (long long)Nc * Nc) return;
-    const int r = (int)(e / Nc), c = (int)(e - (long long)r * Nc);
-    if (c <= r) return;
-    const float v = 0.5f * (Ainv[e] + Ainv[(size_t)c * Nc + r]);
-    Ainv[e] = v;
-    Ainv[(size_t)c * Nc + r] = v;
+struct SweepArgs {
+    const double *A;  // [Nc x Nc] coarse matrix (FP64)
+    int Nc, Np;       // size, padded size (multiple of kSwTile)
+    float *X0, *X1;   // [Np x Np] ping-pong buffers
+    float *Ainv;      // [Nc x Nc] result
+    int *fail;        // set when a pivot block is not positive definite
+};
+
+__global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ float sP[kSwPiv][kSwPiv + 1];
+    __shared__ float sC[kSwTile][kSwPiv + 1];   // M[I rows, K]
+    __shared__ float sB[kSwPiv][kSwTile + 1];   // M[K, J cols]
+    __shared__ float sW[kSwPiv][kSwTile + 1];   // P M[K, J cols]
+    __shared__ float sV[kSwTile][kSwPiv + 1];   // M[I rows, K] P
+    __shared__ int sfail;
+    const int Nc = g.Nc, Np = g.Np;
+    const int nt = Np / kSwTile, tiles = nt * nt;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = tid & 15, ty = tid >> 4;
+    // Start: the padded FP32 copy with the diagonal lifted by 1e-6 relative
+    // (keeps a nearly singular coarse matrix away from breakdown; it is a
+    // preconditioner); an empty row/column gets a unit diagonal.
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const int R0 = (t / nt) * kSwTile, C0 = (t % nt) * kSwTile;
+        for (int e = tid; e < kSwTile * kSwTile; e += blockDim.x) {
+            const int r = R0 + e / kSwTile, c = C0 + e % kSwTile;
+            double v = r == c ? 1.0 : 0.0;
+            if (r < Nc && c < Nc) {
+                v = g.A[(size_t)r * Nc + c];
+                if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + 1e-6);
+            }
+            g.X0[(size_t)r * Np + c] = (float)v;
+        }
+    }
+    grid.sync();
+    const int steps = Np / kSwPiv;
+    for (int k = 0; k < steps; ++k) {
+        const float *src = (k & 1) ? g.X1 : g.X0;
+        float *dst = (k & 1) ? g.X0 : g.X1;
+        const int k0 = k * kSwPiv;
+        if (warp == 0) {
+            float a[kSwPiv];
+            const float4 *row = reinterpret_cast<const float4 *>(src + (size_t)(k0 + lane) * Np + k0);
+#pragma unroll
+            for (int q = 0; q < kSwPiv / 4; ++q) {
+                const float4 v = row[q];
+                a[4 * q] = v.x;
+                a[4 * q + 1] = v.y;
+                a[4 * q + 2] = v.z;
+                a[4 * q + 3] = v.w;
+            }
+            const bool ok = sweep32(a, lane);
+            if (lane == 0) sfail = ok ? 0 : 1;
+#pragma unroll
+            for (int c = 0; c < kSwPiv; ++c) sP[lane][c] = -a[c];
+        }
+        __syncthreads();
+        if (sfail) {  // every block stops at this step; the result is all zeros
+            if (blockIdx.x == 0 && tid == 0) *g.fail = 1;
+            for (long long e = blockIdx.x * (long long)blockDim.x + tid; e < (long long)Nc * Nc;
+                 e += (long long)gridDim.x * blockDim.x)
+                g.Ainv[e] = 0.0f;
+            return;
+        }
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+            const int R0 = (t / nt) * kSwTile, C0 = (t % nt) * kSwTile;
+            const int rK = (k0 >= R0 && k0 < R0 + kSwTile) ? k0 - R0 : -1;  // tile rows in K
+            const int cK = (k0 >= C0 && k0 < C0 + kSwTile) ? k0 - C0 : -1;  // tile columns in K
+            for (int e = tid; e < kSwTile * kSwPiv; e += blockDim.x) {
+                const int r = e / kSwPiv, q = e % kSwPiv;
+                sC[r][q] = src[(size_t)(R0 + r) * Np + k0 + q];
+                const int u = e / kSwTile, c = e % kSwTile;
+                sB[u][c] = src[(size_t)(k0 + u) * Np + C0 + c];
+            }
+            __syncthreads();
+            for (int e = tid; e < kSwPiv * kSwTile; e += blockDim.x) {  // W = P B
+                const int u = e / kSwTile, c = e % kSwTile;
+                float w = 0.0f;
+#pragma unroll 8
+                for (int q = 0; q < kSwPiv; ++q) w = fmaf(sP[u][q], sB[q][c], w);
+                sW[u][c] = w;
+            }
+            if (cK >= 0)
+                for (int e = tid; e < kSwTile * kSwPiv; e += blockDim.x) {  // V = C P
+                    const int r = e / kSwPiv, c = e % kSwPiv;
+                    float v = 0.0f;
+#pragma unroll 8
+                    for (int q = 0; q < kSwPiv; ++q) v = fmaf(sC[r][q], sP[q][c], v);
+                    sV[r][c] = v;
+                }
+            __syncthreads();
+            float acc[4][4] = {};
+#pragma unroll 4
+            for (int q = 0; q < kSwPiv; ++q) {
+                float x[4], y[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) x[i] = sC[ty * 4 + i][q];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) y[j] = sW[q][tx + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(x[i], y[j], acc[i][j]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = ty * 4 + i;
+                const bool inK_r = rK >= 0 && r >= rK && r < rK + kSwPiv;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = tx + 16 * j;
+                    const bool inK_c = cK >= 0 && c >= cK && c < cK + kSwPiv;
+                    float v;
+                    if (inK_r && inK_c) v = -sP[r - rK][c - cK];
+                    else if (inK_r) v = sW[r - rK][c];
+                    else if (inK_c) v = sV[r][c - cK];
+                    else v = src[(size_t)(R0 + r) * Np + C0 + c] - acc[i][j];
+                    dst[(size_t)(R0 + r) * Np + C0 + c] = v;
+                }
+            }
+            __syncthreads();  // the shared tiles are reused by the next tile
+        }
+        grid.sync();
+    }
+    // The swept matrix is -A^-1: Ainv = -(X + X^T) / 2 (symmetric to the last bit).
+    const float *X = (steps & 1) ? g.X1 : g.X0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + tid; e < (long long)Nc * Nc;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / Nc), c = (int)(e - (long long)r * Nc);
+        g.Ainv[e] = -0.5f * (X[(size_t)r * Np + c] + X[(size_t)c * Np + r]);
+    }
 }
 
 // zc = Z^T r: per cluster and column, the sum over the cluster's images in
@@ -516,13 +674,37 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
                                                    D, co.A);
         SFMBA_LAUNCH_CHECK();
     }
-    k_coarse_to32<<<div_up((long long)Nc * Nc, 256), 256, 0, s>>>(co.A, Nc, co.A32, co.Ainv);
-    SFMBA_LAUNCH_CHECK();
 }
 
-void launch_coarse_symmetrize(const Bufs &b, cudaStream_t s) {
-    const int Nc = b.co.nc * b.D;
-    k_coarse_sym<<<div_up((long long)Nc * Nc, 256), 256, 0, s>>>(b.co.Ainv, Nc);
+int coarse_padded_size(int Nc) { return div_up(Nc, kSwTile) * kSwTile; }
+
+void launch_coarse_invert(const Bufs &b, cudaStream_t s) {
+    const CoarseBufs &co = b.co;
+    const int Nc = co.nc * b.D, Np = coarse_padded_size(Nc);
+    SFMBA_CUDA(cudaMemsetAsync(co.fail, 0, sizeof(int), s));
+    static int cap_dev = -1, cap = 0;  // co-resident blocks, queried once per device
+    int dev = 0;
+    SFMBA_CUDA(cudaGetDevice(&dev));
+    if (cap_dev != dev) {
+        int per_sm = 0, sms = 0;
+        SFMBA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coarse_sweep, 256, 0));
+        SFMBA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cap = per_sm * sms;
+        cap_dev = dev;
+    }
+    if (cap < 1) throw Error(SFMBA_ERR_INTERNAL, "the coarse inverse kernel cannot be resident");
+    const int nt = Np / kSwTile;
+    SweepArgs g{co.A, Nc, Np, co.X32, co.X32 + (size_t)Np * Np, co.Ainv, co.fail};
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)std::min(nt * nt, cap));
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SFMBA_CUDA(cudaLaunchKernelEx(&cfg, k_coarse_sweep, g));
     SFMBA_LAUNCH_CHECK();
 }
 

@@ -29,13 +29,11 @@ struct CoarseBufs {
     int4 *chunk = nullptr;            // [nchunks] {group, first, end, 0} into pair_pt
     double *chunk_part = nullptr;     // [nchunks][D*D]
     double *A = nullptr;              // [Nc*Nc] coarse matrix, FP64
-    float *A32 = nullptr;             // [Nc*Nc] FP32 copy, factored in place
-    float *Ainv = nullptr;            // [Nc*Nc]
+    float *X32 = nullptr;             // [2][Np*Np] ping-pong buffers of the block sweep (coarse_padded_size)
+    int *fail = nullptr;              // set when the sweep meets a pivot block that is not positive definite
+    float *Ainv = nullptr;            // [Nc*Nc] symmetric FP32 A^-1, applied per iteration
     void *cc = nullptr;               // [Nc] coarse correction, element type of the PCG vectors
     double *zc = nullptr;             // [Nc] Z^T r
-    int *info = nullptr;              // factorisation status
-    float *work = nullptr;
-    int lwork = 0;
 };
 
 // Free cameras shared by several images, on the PCG solver. The reduced
@@ -359,12 +357,15 @@ void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, 
 // key2 are scratch of at least ninc entries).
 void launch_coarse_inc_order(const Bufs &b, int *key, int *val, int *key2, void *temp, size_t temp_bytes,
                              cudaStream_t s);
-// A_c for the current damping and point inverses; FP32 copy and Ainv = I for the factorisation.
+// A_c (FP64) for the current damping and point inverses.
 void launch_coarse_assemble(const Bufs &b, cudaStream_t s);
 // z += Z Ainv Z^T r with the r.z / r.r partials (init: the start of a solve, p = z).
 void launch_coarse_correct(const Bufs &b, bool init, cudaStream_t s);
-// Symmetrise Ainv after the solve with the identity.
-void launch_coarse_symmetrize(const Bufs &b, cudaStream_t s);
+// Ainv = A_c^-1 in FP32 by the block sweep (one cooperative launch); on a
+// breakdown *co.fail = 1 and Ainv = 0.
+void launch_coarse_invert(const Bufs &b, cudaStream_t s);
+// Side of the sweep's square buffers for an Nc x Nc coarse matrix.
+int coarse_padded_size(int Nc);
 
 // ---- refine_intrinsics (k_intrinsics.cu)
 struct IntrinsicsBufs {

@@ -22,7 +22,6 @@
 #include <vector>
 
 #include <cub/cub.cuh>
-#include <cusolverDn.h>
 
 #include "camera.cuh"
 #include "colmap_io.h"
@@ -289,9 +288,7 @@ struct Context {
     Arena main, pairs, aux, coarse, shared, shared_inc;
     LMState *h_state = nullptr;  // pinned mirror
     int *h_counts = nullptr;     // pinned batch summary
-    cusolverDnHandle_t dn = nullptr;  // coarse factorisation (created on first use)
     ~Context() {
-        if (dn) cusolverDnDestroy(dn);
         if (h_state) cudaFreeHost(h_state);
         if (h_counts) cudaFreeHost(h_counts);
         if (stream) cudaStreamDestroy(stream);
@@ -758,10 +755,6 @@ class Solver {
         for (int c = 0; c <= nc; ++c) clu_start[c] = (int)((long long)c * nI / nc);
         for (int c = 0; c < nc; ++c)
             for (int i = clu_start[c]; i < clu_start[c + 1]; ++i) img_cluster[i] = c;
-        if (!ctx_.dn && cusolverDnCreate(&ctx_.dn) != CUSOLVER_STATUS_SUCCESS)
-            throw Error(SFMBA_ERR_CUDA, "cusolverDnCreate failed");
-        if (cusolverDnSetStream(ctx_.dn, s_) != CUSOLVER_STATUS_SUCCESS)
-            throw Error(SFMBA_ERR_CUDA, "cusolverDnSetStream failed");
         Arena &A = ctx_.coarse;
         long long *count = nullptr, *off = nullptr, *kcount = nullptr;
         int *key_counts = nullptr;
@@ -772,11 +765,11 @@ class Solver {
             co.img_cluster = A.take<int>(nI);
             co.clu_start = A.take<int>((size_t)nc + 1);
             co.A = A.take<double>((size_t)Nc * Nc);
-            co.A32 = A.take<float>((size_t)Nc * Nc);
+            co.X32 = A.take<float>((size_t)2 * coarse_padded_size(Nc) * coarse_padded_size(Nc));
+            co.fail = A.take<int>(1);
             co.Ainv = A.take<float>((size_t)Nc * Nc);
             co.cc = A.take<double>(Nc);
             co.zc = A.take<double>(Nc);
-            co.info = A.take<int>(1);
             count = A.take<long long>((size_t)nP + 1);
             off = A.take<long long>((size_t)nP + 1);
             kcount = A.take<long long>((size_t)nP + 1);
@@ -793,10 +786,6 @@ class Solver {
             co = CoarseBufs{};
             return;
         }
-        int lwork = 0;
-        if (cusolverDnSpotrf_bufferSize(ctx_.dn, CUBLAS_FILL_MODE_LOWER, Nc, co.A32, Nc, &lwork) !=
-            CUSOLVER_STATUS_SUCCESS)
-            throw Error(SFMBA_ERR_CUDA, "cusolverDnSpotrf_bufferSize failed");
         const int max_groups = nc * (nc + 1) / 2;
         const long long max_chunks = npairs / kCoarseChunk + max_groups + 1;
         Arena &P = ctx_.pairs;
@@ -814,13 +803,11 @@ class Solver {
             co.group_chunk_off = P.take<int>((size_t)max_groups + 1);
             co.chunk = P.take<int4>(max_chunks);
             co.chunk_part = P.take<double>((size_t)max_chunks * D * D);
-            co.work = P.take<float>((size_t)std::max(lwork, 1));
             co.inc_cl = P.take<int>(ninc);
             co.inc_order = P.take<int>(ninc);
             co.ybuf = P.take<double>((size_t)ninc * 3 * D);  // FP64-sized: an FP64 polish reuses it
         }
         co.ninc = ninc;
-        co.lwork = lwork;
         co.nc = nc;
         launch_coarse_group(b, off, npairs, key, val, key2, val_sorted, key_counts, temp2, t2, s_);
         launch_coarse_inc_order(b, key, val, key2, temp2, t2, s_);  // the pair keys are consumed
@@ -916,28 +903,19 @@ class Solver {
         SFMBA_CUDA(cudaStreamSynchronize(s_));  // host vectors above go out of scope
     }
 
-    // A_c for this retry, FP32 Cholesky and inverse; false (block-Jacobi
-    // alone for this retry) when the factorisation breaks down.
+    // A_c for this retry and its FP32 inverse; false (block-Jacobi alone
+    // for this retry) when the sweep breaks down.
     bool factor_coarse() {
         Bufs &b = b_;
         CoarseBufs &co = b.co;
         if (co.nc == 0) return false;
-        const int Nc = co.nc * b.D;
         { SFMBA_PHASE(PH_COARSE_ASSEMBLE); launch_coarse_assemble(b, s_); }
         SFMBA_PHASE(PH_COARSE_FACTOR);
-        if (cusolverDnSetStream(ctx_.dn, s_) != CUSOLVER_STATUS_SUCCESS ||
-            cusolverDnSpotrf(ctx_.dn, CUBLAS_FILL_MODE_LOWER, Nc, co.A32, Nc, co.work, co.lwork, co.info) !=
-                CUSOLVER_STATUS_SUCCESS)
-            throw Error(SFMBA_ERR_CUDA, "cusolverDnSpotrf failed");
-        int info = -1;
-        SFMBA_CUDA(cudaMemcpyAsync(&info, co.info, sizeof(int), cudaMemcpyDeviceToHost, s_));
+        launch_coarse_invert(b, s_);
+        int failed = 1;
+        SFMBA_CUDA(cudaMemcpyAsync(&failed, co.fail, sizeof(int), cudaMemcpyDeviceToHost, s_));
         SFMBA_CUDA(cudaStreamSynchronize(s_));
-        if (info != 0) return false;
-        if (cusolverDnSpotrs(ctx_.dn, CUBLAS_FILL_MODE_LOWER, Nc, Nc, co.A32, Nc, co.Ainv, Nc, co.info) !=
-            CUSOLVER_STATUS_SUCCESS)
-            throw Error(SFMBA_ERR_CUDA, "cusolverDnSpotrs failed");
-        launch_coarse_symmetrize(b, s_);
-        return true;
+        return failed == 0;
     }
 
     void read_state() {

@@ -58,11 +58,20 @@ def test_mixed_reaches_golden_cost(name, polish):
 
 @pytest.mark.parametrize("name", ["ring16_s005", "radial2000_s0005", "window_mixed_models"])
 def test_pcg_reaches_golden_cost(name):
+    """PCG solved tightly: FP64 to a relative residual of 1e-10 reaches the
+    oracle's final cost to 1e-6; so does the mixed path (FP32 PCG to 1e-6,
+    the most its FP32 vectors resolve) with the FP64 polish. The mixed path
+    alone ends within 1e-4: the LM loop stops at the first accepted step
+    that lowers the cost by < 1e-6 relative (lib.rs:1215-1221), and on
+    ring16 the oracle's own iteration 8 lowers it by just over that, so a
+    step computed in FP32 can end the loop there."""
     p, kw, exp = G.load(name)
-    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
-        r = native.bundle_adjust_arrays(p, precision=prec, solver=abi.SOLVER_PCG, pcg_tolerance=1e-10,
-                                        pcg_max_iterations=2000, **kw)
-        assert r.final_cost <= exp["final_cost"] * (1 + 1e-6), (prec, r.final_cost, exp["final_cost"])
+    runs = ((abi.PRECISION_FP64, 1e-10, 0, 1e-6), (abi.PRECISION_MIXED, 1e-6, 1, 1e-6),
+            (abi.PRECISION_MIXED, 1e-6, 0, 1e-4))
+    for prec, tol, polish, bar in runs:
+        r = native.bundle_adjust_arrays(p, precision=prec, solver=abi.SOLVER_PCG, pcg_tolerance=tol,
+                                        pcg_max_iterations=2000, fp64_polish=polish, **kw)
+        assert r.final_cost <= exp["final_cost"] * (1 + bar), (prec, polish, r.final_cost, exp["final_cost"])
 
 
 def test_gpu_jacobians_match_golden():

