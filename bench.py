@@ -453,40 +453,81 @@ def cpu_baseline_sample(p, point_stride, chol_dim):
 def dense_radial500(args, L, device, stream):
     """Dense reduced-camera path: 500 SIMPLE_RADIAL cameras, 200k points,
     ~1.2M observations (reduced dimension 4994): FP32 linearisation and
-    Schur with FP64 blocked Cholesky and one refinement step, against the
-    plain FP64 dense path, both timed to the FP64 final cost x (1 + 1e-6)."""
+    Schur with an FP64-accurate blocked Cholesky whose trailing updates run
+    on the BF16 tensor cores by error-free splitting, and one FP64
+    refinement step, against the plain FP64 dense path (FP64 fused
+    multiply-adds throughout), both timed to the FP64 final cost x
+    (1 + 1e-6). The mixed path with FP64 fused multiply-add updates is
+    timed beside them."""
     from sfmtory_gb300 import abi, native, scenes
 
     p = scenes.radial500(seed=args.seed, scale=1.0)
     dp = DeviceProblem(p, device)
 
-    def opts(prec, target=0.0):
+    def opts(prec, target=0.0, fma=0):
         return abi.default_options(max_iterations=args.max_iterations, robust_loss=abi.LOSS_NONE, precision=prec,
-                                   solver=abi.SOLVER_DENSE, target_cost=target)
+                                   solver=abi.SOLVER_DENSE, target_cost=target, dense_fp64_fma=fma)
+
+    def profiled(o):
+        native.profile_enable(True)  # phase breakdown from one more solve, outside the timing
+        solve_device(L, dp, o, stream)
+        prof = native.profile_report()
+        native.profile_enable(False)
+        return prof
 
     r64, ms64_full = solve_device(L, dp, opts(abi.PRECISION_FP64), stream)
     target = r64.final_cost * (1.0 + 1e-6)
     r64t, ms64 = solve_device(L, dp, opts(abi.PRECISION_FP64, target), stream)
     solve_device(L, dp, opts(abi.PRECISION_MIXED, target), stream)
     r32, ms32 = solve_device(L, dp, opts(abi.PRECISION_MIXED, target), stream)
-    native.profile_enable(True)  # phase breakdown from one more solve, outside the timing
-    solve_device(L, dp, opts(abi.PRECISION_MIXED, target), stream)
-    prof = native.profile_report()
-    native.profile_enable(False)
+    r32f, ms32f = solve_device(L, dp, opts(abi.PRECISION_MIXED, target, fma=1), stream)
+    prof = profiled(opts(abi.PRECISION_MIXED, target))
+    prof64 = profiled(opts(abi.PRECISION_FP64, target))
     n = p.reduced_dim()
-    chol = prof.get("cholesky", {"ms": 0.0, "launches": 0})
-    chol_tflops = (n ** 3 / 3.0) * chol["launches"] / (chol["ms"] * 1e-3) / 1e12 if chol["ms"] else None
+    flops = n ** 3 / 3.0  # FP64 operations of one factorisation
+
+    def per_factor(pr):
+        c = pr.get("cholesky", {"ms": 0.0, "launches": 0})
+        return c["ms"] / c["launches"] if c.get("launches") else None
+
+    t_oz, t_fma = per_factor(prof), per_factor(prof64)
+    peaks = native.measure_peaks()
+    mp = measured_peaks()
+    bf16_peak = mp.get("bf16_tflops")
+    chol = {"n": n, "fp64_flops_per_factorisation": flops,
+            "tensor_update_ms": t_oz, "fp64_fma_ms": t_fma,
+            "tensor_update_fp64_equiv_tflops": flops / (t_oz * 1e-3) / 1e12 if t_oz else None,
+            "fp64_fma_tflops": flops / (t_fma * 1e-3) / 1e12 if t_fma else None,
+            "peaks_measured_here": peaks}
+    if t_fma:
+        chol["fp64_fma_roofline"] = {"bound": "fp64", "achieved": chol["fp64_fma_tflops"],
+                                     "peak": peaks["dfma_tflops"], "unit": "TFLOP/s",
+                                     "frac": chol["fp64_fma_tflops"] / peaks["dfma_tflops"],
+                                     "peak_source": "sfmba_measure_peaks DFMA probe on this GPU"}
+    if t_oz:
+        # 28 BF16 products per FP64 product of the trailing update
+        bf16 = 28.0 * flops / (t_oz * 1e-3) / 1e12
+        chol["tensor_update_roofline"] = {
+            "bound": "tensor", "achieved_bf16_tflops": bf16, "unit": "TFLOP/s",
+            "peak": bf16_peak, "frac": bf16 / bf16_peak if bf16_peak else None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)",
+            "mma_sync_ceiling_tflops": peaks["bf16_mma_tflops"],
+            "frac_of_mma_sync_ceiling": bf16 / peaks["bf16_mma_tflops"]}
     return {
         "workload": f"radial500: {p.num_images} SIMPLE_RADIAL cameras, {p.num_points} points, "
                     f"{p.num_observations} observations, reduced dim {n}, squared loss",
         "fp32_time_to_tolerance_s": ms32 / 1e3, "fp32_iterations": r32.iterations_run,
         "fp32_final_cost": r32.final_cost, "reached_tolerance": r32.final_cost <= target,
+        "fp32_fp64_fma_updates_time_to_tolerance_s": ms32f / 1e3,
+        "fp32_fp64_fma_updates_reached_tolerance": r32f.final_cost <= target,
         "fp64_time_to_tolerance_s": ms64 / 1e3, "fp64_full_solve_s": ms64_full / 1e3,
         "fp64_final_cost": r64.final_cost, "fp64_iterations": r64.iterations_run,
         "speedup_vs_fp64_gpu": ms64 / ms32,
         "obs_per_s": p.num_observations * r32.iterations_run / (ms32 / 1e3),
-        "cholesky_fp64_tflops": chol_tflops,
+        "cholesky": chol,
         "phase_ms": {k: round(v["ms"], 3) for k, v in prof.items() if isinstance(v, dict) and v.get("launches")},
+        "phase_ms_fp64": {k: round(v["ms"], 3) for k, v in prof64.items()
+                          if isinstance(v, dict) and v.get("launches")},
     }
 
 

@@ -116,7 +116,12 @@ typedef struct sfmba_options {
     int32_t pcg_coarse_clusters;  /* PCG solver: clusters of consecutive images in the
                                      coarse correction of the preconditioner (0: 64,
                                      at most 128; < 0: block-Jacobi alone) */
-    int32_t reserved[4];
+    int32_t dense_fp64_fma;       /* dense solver, mixed path: 0 (default) runs the
+                                     Cholesky's trailing updates on the BF16 tensor
+                                     cores by error-free splitting (FP64 accuracy);
+                                     1 keeps FP64 fused multiply-adds, as the FP64
+                                     path does */
+    int32_t reserved[3];
 } sfmba_options;
 
 /* crates/sfm-ba/src/lib.rs:240-247 (`BaOutput`). Output buffers are caller
@@ -383,6 +388,24 @@ int sfmba_local_windows(const sfmba_reconstruction *rec, int32_t seed_image, int
 #define SFMBA_NOALLOC_MAX_OBSERVATIONS 16777216
 int sfmba_total_cost_noalloc(const sfmba_problem *problem, const sfmba_options *options,
                              double *out_cost_device, void *stream);
+
+/* Benchmarking aid (no counterpart in the reference): throughput of the
+ * current GPU's arithmetic units that the dense Cholesky can use, in
+ * TFLOP/s: out[0] FP64 fused multiply-add, out[1] the FP64 tensor
+ * instruction (mma.sync m8n8k4), out[2] the BF16 tensor instruction
+ * (mma.sync m16n8k16, FP32 accumulation). */
+int sfmba_measure_peaks(double *out);
+
+/* Test and benchmarking aid (the factorisation of lib.rs:1081-1094 on its
+ * own): the blocked Cholesky of the dense solver applied to the symmetric
+ * positive-definite n x n matrix A (host, row-major; its lower triangle is
+ * read) on the GPU. L (host, n x n) receives the lower factor, zeros above
+ * the diagonal. tensor_update != 0 runs the trailing updates on the BF16
+ * tensor cores by error-free splitting (the mixed path's choice), 0 with
+ * FP64 fused multiply-adds. *seconds (if not NULL): device time of the
+ * factorisation. A matrix that is not positive definite gives
+ * SFMBA_ERR_INVALID_ARGUMENT. */
+int sfmba_dense_cholesky(int64_t n, const double *A, double *L, int32_t tensor_update, double *seconds);
 
 /* Benchmarking aid (no counterpart in the reference): when enabled, every
  * kernel phase of the solves made on this thread is bracketed by CUDA events

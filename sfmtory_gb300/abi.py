@@ -98,7 +98,8 @@ class SfmbaOptions(C.Structure):
         ("fp64_polish", C.c_int32),
         ("kernel_variant", C.c_int32),
         ("pcg_coarse_clusters", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("dense_fp64_fma", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 

@@ -128,6 +128,10 @@ struct Bufs {
     double *S = nullptr;          // [n*n] symmetric reduced system
     double *L = nullptr;          // [n*n] Cholesky / LU factors
     double *Linv = nullptr;       // [nblocks*64*64] inverses of diagonal blocks
+    // Tensor-core trailing updates of the Cholesky (NULL: FP64 fused
+    // multiply-adds): BF16 slices [7][n][64] and exponents [n] of a panel.
+    uint16_t *oz_slices = nullptr;
+    int *oz_exp = nullptr;
     int *lu_perm = nullptr;       // [n]
     double *rhs = nullptr, *delta = nullptr, *diagB = nullptr, *work = nullptr, *work2 = nullptr;  // [n]
     double *ref_res = nullptr, *ref_corr = nullptr;  // [n] refinement residual and correction
@@ -366,6 +370,13 @@ void launch_coarse_correct(const Bufs &b, bool init, cudaStream_t s);
 void launch_coarse_invert(const Bufs &b, cudaStream_t s);
 // Side of the sweep's square buffers for an Nc x Nc coarse matrix.
 int coarse_padded_size(int Nc);
+
+// ---- throughput probes (k_peaks.cu): TFLOP/s of FP64 FMA, FP64 mma.sync
+// m8n8k4 and BF16 mma.sync m16n8k16 on the current device.
+struct PeakRates {
+    double dfma_tflops = 0.0, dmma_tflops = 0.0, bf16_mma_tflops = 0.0;
+};
+PeakRates measure_peaks(cudaStream_t s, double *sink);
 
 // ---- refine_intrinsics (k_intrinsics.cu)
 struct IntrinsicsBufs {

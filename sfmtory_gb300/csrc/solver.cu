@@ -26,6 +26,7 @@
 #include "camera.cuh"
 #include "colmap_io.h"
 #include "kernels.cuh"
+#include "ozaki.cuh"
 
 namespace sfmba {
 
@@ -1111,6 +1112,12 @@ class Solver {
                     b.Linv = A.take<double>((size_t)div_up(n, kCholNB) * kCholNB * kCholNB);
                     b.lu_perm = A.take<int>(n);
                     pair_scan = A.take<long long>(nP);
+                    b.oz_slices = nullptr;
+                    b.oz_exp = nullptr;
+                    if (mixed && !o->dense_fp64_fma) {  // tensor-core trailing updates (ozaki.cuh)
+                        b.oz_slices = A.take<uint16_t>((size_t)kOzSlices * n * kOzK);
+                        b.oz_exp = A.take<int>(n);
+                    }
                 } else {
                     b.pcg_x = A.take<char>((size_t)nID * tsz);
                     b.pcg_r = A.take<char>((size_t)nID * tsz);
@@ -2470,6 +2477,82 @@ int sfmba_profile_report(char *buf, int64_t len) {
         if (!buf || len <= (int64_t)js.size())
             throw Error(SFMBA_ERR_INVALID_ARGUMENT, "profile buffer too small (need " + std::to_string(js.size() + 1) + ")");
         std::memcpy(buf, js.c_str(), js.size() + 1);
+    });
+}
+
+int sfmba_measure_peaks(double *out) {
+    return guarded([&] {
+        if (!out) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "out is NULL");
+        Context &ctx = context();
+        double *sink = nullptr;
+        SFMBA_CUDA(cudaMalloc(&sink, sizeof(double)));
+        PeakRates r{};
+        try {
+            r = measure_peaks(ctx.stream, sink);
+        } catch (...) {
+            cudaFree(sink);
+            throw;
+        }
+        SFMBA_CUDA(cudaFree(sink));
+        out[0] = r.dfma_tflops;
+        out[1] = r.dmma_tflops;
+        out[2] = r.bf16_mma_tflops;
+    });
+}
+
+int sfmba_dense_cholesky(int64_t n, const double *A, double *L, int32_t tensor_update, double *seconds) {
+    return guarded([&] {
+        if (n <= 0 || n > 32768) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "n must be in [1, 32768]");
+        if (!A || !L) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "A or L is NULL");
+        Context &ctx = context();
+        cudaStream_t s = ctx.stream;
+        Bufs b;
+        b.n = (int)n;
+        std::vector<void *> owned;
+        auto dev_alloc = [&](size_t bytes) {
+            void *p = nullptr;
+            if (cudaMalloc(&p, bytes) != cudaSuccess) {
+                (void)cudaGetLastError();
+                for (void *q : owned) cudaFree(q);
+                throw Error(SFMBA_ERR_OUT_OF_MEMORY, "device allocation failed");
+            }
+            owned.push_back(p);
+            return p;
+        };
+        const size_t nn = (size_t)n * n;
+        b.L = (double *)dev_alloc(nn * sizeof(double));
+        b.Linv = (double *)dev_alloc((size_t)div_up((int)n, kCholNB) * kCholNB * kCholNB * sizeof(double));
+        b.state = (LMState *)dev_alloc(sizeof(LMState));
+        if (tensor_update) {
+            b.oz_slices = (uint16_t *)dev_alloc((size_t)kOzSlices * n * kOzK * sizeof(uint16_t));
+            b.oz_exp = (int *)dev_alloc((size_t)n * sizeof(int));
+        }
+        int failed = 0;
+        float ms = 0.0f;
+        try {
+            SFMBA_CUDA(cudaMemcpyAsync(b.L, A, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+            SFMBA_CUDA(cudaMemsetAsync(b.state, 0, sizeof(LMState), s));
+            cudaEvent_t e0, e1;
+            SFMBA_CUDA(cudaEventCreate(&e0));
+            SFMBA_CUDA(cudaEventCreate(&e1));
+            SFMBA_CUDA(cudaEventRecord(e0, s));
+            launch_cholesky(b, s);
+            SFMBA_CUDA(cudaEventRecord(e1, s));
+            SFMBA_CUDA(cudaMemcpyAsync(&failed, &b.state->factor_failed, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SFMBA_CUDA(cudaMemcpyAsync(L, b.L, nn * sizeof(double), cudaMemcpyDeviceToHost, s));
+            SFMBA_CUDA(cudaStreamSynchronize(s));
+            SFMBA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        } catch (...) {
+            for (void *q : owned) cudaFree(q);
+            throw;
+        }
+        for (void *q : owned) cudaFree(q);
+        if (failed) throw Error(SFMBA_ERR_INVALID_ARGUMENT, "the matrix is not positive definite");
+        for (int64_t r = 0; r < n; ++r)
+            for (int64_t c = r + 1; c < n; ++c) L[r * n + c] = 0.0;
+        if (seconds) *seconds = ms * 1e-3;
     });
 }
 

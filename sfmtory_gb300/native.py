@@ -47,6 +47,8 @@ EXPORTED_SYMBOLS = (
     "sfmba_colmap_model_stats",
     "sfmba_residuals_jacobians",
     "sfmba_total_cost_noalloc",
+    "sfmba_measure_peaks",
+    "sfmba_dense_cholesky",
     "sfmba_profile_enable",
     "sfmba_profile_report",
     "sfmba_last_error",
@@ -93,6 +95,8 @@ def load(path: str | None = None):
         L.sfmba_residuals_jacobians.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
         L.sfmba_total_cost_noalloc.argtypes = [vp, vp, vp, vp]
         L.sfmba_local_windows.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp]
+        L.sfmba_measure_peaks.argtypes = [vp]
+        L.sfmba_dense_cholesky.argtypes = [C.c_int64, vp, vp, C.c_int32, vp]
         L.sfmba_profile_enable.argtypes = [C.c_int32]
         L.sfmba_profile_report.argtypes = [C.c_char_p, C.c_int64]
         L.sfmba_last_error.restype = C.c_char_p
@@ -391,6 +395,24 @@ def colmap_model_stats(dir: str) -> dict:
     out = {k: int(v) for k, v in zip(keys, counts)}
     out["mean_reprojection_error"] = err.value
     return out
+
+
+def measure_peaks() -> dict:
+    """TFLOP/s of the GPU's FP64 FMA, FP64 mma.sync and BF16 mma.sync units."""
+    out = np.zeros(3)
+    _check(load().sfmba_measure_peaks(out.ctypes.data))
+    return {"dfma_tflops": float(out[0]), "dmma_tflops": float(out[1]), "bf16_mma_tflops": float(out[2])}
+
+
+def dense_cholesky(A: np.ndarray, tensor_update: bool = True):
+    """(L, seconds): the dense solver's blocked Cholesky of the SPD matrix A on the GPU."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    n = A.shape[0]
+    L = np.zeros_like(A)
+    sec = C.c_double(0.0)
+    _check(load().sfmba_dense_cholesky(n, A.ctypes.data, L.ctypes.data, 1 if tensor_update else 0,
+                                       C.byref(sec)))
+    return L, sec.value
 
 
 def profile_enable(on: bool = True) -> None:
