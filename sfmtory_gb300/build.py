@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsfmba_gb300.so")
 SOURCES = ["k_setup.cu", "k_lin.cu", "k_dense.cu", "k_pcg.cu", "k_matfree.cu", "k_mf_pcg.cu", "k_noalloc.cu", "k_batched.cu",
-           "k_filter.cu", "k_intrinsics.cu", "k_pnp.cu", "k_coarse.cu", "k_shared.cu", "local_windows.cpp", "k_peaks.cu", "colmap_io.cpp", "solver.cu"]
+           "k_filter.cu", "k_intrinsics.cu", "k_pnp.cu", "k_coarse.cu", "k_shared.cu", "local_windows.cpp", "k_peaks.cu", "k_pcg_coop.cu", "colmap_io.cpp", "solver.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-ffp-contract=off"]

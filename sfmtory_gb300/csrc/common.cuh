@@ -57,6 +57,13 @@ __host__ __device__ constexpr bool model_fits_width(int M, int D) { return M >= 
 
 // D rounded up to a multiple of 4 (16-byte rows of FP32 image vectors).
 __host__ __device__ constexpr int pad4(int D) { return (D + 3) & ~3; }
+// Index of entry c of image i in a plane layout of nI image vectors: entries
+// 4k..4k+3 of every image form plane k ([nI] float4), so a warp reading one
+// plane for neighbouring images touches a few 128-byte lines, not one line
+// per image.
+__host__ __device__ __forceinline__ size_t plane_index(int nI, int i, int c) {
+    return ((size_t)(c >> 2) * nI + i) * 4 + (c & 3);
+}
 
 // Width of the per-image variable block: 6 pose columns + the widest camera.
 __host__ __device__ constexpr int block_width_for(int kmax) {

@@ -36,7 +36,7 @@ __device__ __forceinline__ void quat_to_R(const double *q, double R[9]) {
 template <typename T>
 __global__ void k_prepare_images(const double *poses, const double *cams, const int *cam_of_img,
                                  const int *cam_model, const int *img_active, int nI,
-                                 ImageLin<T> *out) {
+                                 ImageLin<T> *out, float4 *mv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nI) return;
     const double *q = poses + 7 * (size_t)i;
@@ -53,6 +53,13 @@ __global__ void k_prepare_images(const double *poses, const double *cams, const 
     im.active = img_active[i];
     im.pad[0] = im.pad[1] = 0;
     out[i] = im;
+    if (mv) {  // the same FP32 values in planes (MvOp)
+        mv[i] = make_float4((float)im.R[0], (float)im.R[1], (float)im.R[2], (float)im.R[3]);
+        mv[nI + i] = make_float4((float)im.R[4], (float)im.R[5], (float)im.R[6], (float)im.R[7]);
+        mv[2 * (size_t)nI + i] = make_float4((float)im.R[8], (float)im.t[0], (float)im.t[1], (float)im.t[2]);
+        mv[3 * (size_t)nI + i] = make_float4((float)im.c[0], (float)im.c[1], (float)im.c[2], (float)im.c[3]);
+        mv[4 * (size_t)nI + i] = make_float4((float)im.c[4], (float)im.c[5], (float)im.c[6], (float)im.c[7]);
+    }
 }
 
 template <typename T>
@@ -636,10 +643,11 @@ void launch_prepare_images(const Bufs &b, cudaStream_t s) {
     if (b.nI == 0) return;
     if (b.mixed)
         k_prepare_images<float><<<div_up(b.nI, 128), 128, 0, s>>>(
-            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin);
+            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin, b.img_mv);
     else
         k_prepare_images<double><<<div_up(b.nI, 128), 128, 0, s>>>(
-            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<double> *)b.img_lin);
+            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<double> *)b.img_lin,
+            nullptr);
     SFMBA_LAUNCH_CHECK();
 }
 

@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const 
     p[u] = pn;
     if (p4) {
         const int i = u / D;
-        p4[(size_t)i * pad4(D) + (u - i * D)] = pn;
+        p4[plane_index(nI, i, u - i * D)] = pn;
     }
 }
 

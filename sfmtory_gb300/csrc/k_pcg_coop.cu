@@ -1,0 +1,378 @@
+// The vector side of one PCG iteration as a single cooperative launch.
+//
+// After the two observation passes, an iteration needs a chain of small
+// steps with a grid-wide dependency between each: q = S p from the image
+// pass's partials (and the sum over a shared camera's images), the p.q
+// reduction and alpha, x/r updates with z = M^-1 r, the coarse correction
+// (restriction over image clusters, the dense product with A_c^-1,
+// prolongation), the r.z reduction, beta and the new direction. As separate
+// launches each step costs a launch and a drain of the GPU; here one grid of
+// co-resident blocks runs them all with grid-wide barriers between them
+// (cooperative launch: every block is resident, so the barriers cannot
+// wait on a block that never runs). The arithmetic, its order and the
+// results are those of k_pcg_images_finish, k_sh_qreduce, k_pcg_update,
+// k_coarse_restrict / gemv / z and k_pcg_dir; every reduction that decides
+// whether to stop is computed by every block in the same order, so all
+// blocks take the same branch and reach the same barriers.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <type_traits>
+
+#include "kernels.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace sfmba {
+
+namespace {
+
+__device__ __forceinline__ double block_sum_c(double v, double *sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// v[t] + v[t + B] + ... for thread t of a B-thread block, added in that
+// order, loads issued eight at a time (as in k_pcg.cu).
+__device__ __forceinline__ double strided_sum_c(const double *__restrict__ v, int n) {
+    const int B = blockDim.x;
+    double a = 0.0;
+    int k = threadIdx.x;
+    for (; k + 7 * B < n; k += 8 * B) {
+        double w[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w[u] = v[k + u * B];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a += w[u];
+    }
+    for (; k < n; k += B) a += v[k];
+    return a;
+}
+
+template <typename T>
+struct VecArgs {
+    const T *ipart;
+    const int *ipart_off;
+    const double *img_H;
+    const int *img_active, *img_pmask, *img_dmask;
+    const T *Minv;
+    T *p, *q, *x, *r, *z;
+    float *p4;
+    double *part;
+    LMState *st;
+    int nI, nID, parity;
+    // shared cameras (nsh = 0: none)
+    int nsh;
+    const int *sh_img_start, *sh_imgs, *img_owner;
+    // coarse correction (nc = 0: none)
+    int nc, Nc;
+    const int *clu_start, *img_cluster;
+    const float *Ainv;
+    double *zc;
+    T *cc;
+};
+
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[256];
+    LMState *st = a.st;
+    // Read before any block of this launch writes the state (block 0 writes
+    // it only after the first grid barrier), so every block sees one value.
+    if (st->pcg_done) return;
+    const int nI = a.nI;
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    const double lam = st->lambda;
+    // q_i = (H_i + lambda diag H_i) p_i - sum of the image's partials; p.q over pmask.
+    for (int i = gw; i < nI; i += nw) {
+        const int act = a.img_active[i], pm = a.img_pmask[i];
+        const double *H = a.img_H + (size_t)i * D * D;
+        const T *pv = a.p + (size_t)i * D;
+        double pq = 0.0;
+        if (lane < D) {
+            const int c = lane;
+            double sch = 0.0;
+            const int k1 = a.ipart_off[i + 1];
+            int k = a.ipart_off[i];
+            for (; k + 8 <= k1; k += 8) {
+                T w[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) w[u] = a.ipart[(size_t)(k + u) * D + c];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) sch += (double)w[u];
+            }
+            for (; k < k1; ++k) sch += (double)a.ipart[(size_t)k * D + c];
+            double hp = 0.0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) hp += H[c * D + d] * (double)pv[d];
+            hp += lam * H[c * D + c] * (double)pv[c];
+            const double qc = ((act >> c) & 1) ? hp - sch : 0.0;
+            a.q[(size_t)i * D + c] = (T)qc;
+            if ((pm >> c) & 1) pq = (double)pv[c] * (double)(T)qc;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
+        if (lane == 0) a.part[2 * nI + i] = pq;
+    }
+    grid.sync();
+    if constexpr (D > 6) {
+        if (a.nsh > 0) {  // shared cameras: q summed over each camera's images, the owner's p.q
+            constexpr int KC = D - 6;
+            for (int c = gw; c < a.nsh; c += nw) {
+                const int i0 = a.sh_img_start[c], i1 = a.sh_img_start[c + 1];
+                const int owner = a.sh_imgs[i0];
+                double pq = 0.0;
+                if (lane < KC) {
+                    double s = 0.0;
+                    for (int k = i0; k < i1; ++k) s += (double)a.q[(size_t)a.sh_imgs[k] * D + 6 + lane];
+                    const T qt = (T)s;
+                    for (int k = i0; k < i1; ++k) a.q[(size_t)a.sh_imgs[k] * D + 6 + lane] = qt;
+                    pq = (double)a.p[(size_t)owner * D + 6 + lane] * (double)qt;
+                }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
+                if (lane == 0) a.part[2 * nI + owner] += pq;
+            }
+            grid.sync();
+        }
+    }
+    // alpha = (r.z) / (p.q); x += alpha p; r -= alpha q; z = M^-1 r; r.z, r.r partials.
+    {
+        const double pq = block_sum_c(strided_sum_c(a.part + 2 * nI, nI), sh);
+        if (!(pq > 0.0) || !isfinite(pq)) {  // breakdown (every block sees it): keep the iterate
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                st->pcg_done = 1;
+                st->pcg_alpha = 0.0;
+            }
+            return;
+        }
+        const double alpha = st->pcg_rzbuf[a.parity] / pq;
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->pcg_alpha = alpha;
+        for (int i = gw; i < nI; i += nw) {
+            const size_t base = (size_t)i * D;
+            T rc = T(0);
+            if (lane < D) {
+                a.x[base + lane] = (T)((double)a.x[base + lane] + alpha * (double)a.p[base + lane]);
+                rc = (T)((double)a.r[base + lane] - alpha * (double)a.q[base + lane]);
+                a.r[base + lane] = rc;
+            }
+            double zc = 0.0;
+            const T *M = a.Minv + (size_t)i * D * D;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const T rd = __shfl_sync(0xffffffffu, rc, d);
+                if (lane < D) zc += (double)M[lane * D + d] * (double)rd;
+            }
+            double rz = 0.0, rr = 0.0;
+            if (lane < D) {
+                a.z[base + lane] = (T)zc;
+                if ((a.img_dmask[i] >> lane) & 1) {
+                    rz = (double)rc * (double)(T)zc;
+                    rr = (double)rc * (double)rc;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                rz += __shfl_xor_sync(0xffffffffu, rz, off);
+                rr += __shfl_xor_sync(0xffffffffu, rr, off);
+            }
+            if (lane == 0) {
+                a.part[i] = rz;
+                a.part[nI + i] = rr;
+            }
+        }
+    }
+    grid.sync();
+    if (a.nc > 0) {
+        // zc = Z^T r (per cluster and column, image order, own columns only)
+        for (int c = gw; c < a.nc; c += nw) {
+            if (lane < D) {
+                double s = 0.0;
+                const int i1 = a.clu_start[c + 1];
+                int i = a.clu_start[c];
+                for (; i + 8 <= i1; i += 8) {
+                    T w[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        w[u] = ((a.img_pmask[i + u] >> lane) & 1) ? a.r[(size_t)(i + u) * D + lane] : T(0);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) s += (double)w[u];
+                }
+                for (; i < i1; ++i)
+                    if ((a.img_pmask[i] >> lane) & 1) s += (double)a.r[(size_t)i * D + lane];
+                a.zc[c * D + lane] = s;
+            }
+        }
+        grid.sync();
+        // cc = A_c^-1 zc, one warp per row
+        for (int row = gw; row < a.Nc; row += nw) {
+            const float *ar = a.Ainv + (size_t)row * a.Nc;
+            double s = 0.0;
+            int j = lane;
+            for (; j + 7 * 32 < a.Nc; j += 8 * 32) {
+                float w[8];
+                double y[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    w[u] = __ldg(ar + j + 32 * u);
+                    y[u] = a.zc[j + 32 * u];
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) s += (double)w[u] * y[u];
+            }
+            for (; j < a.Nc; j += 32) s += (double)__ldg(ar + j) * a.zc[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+            if (lane == 0) a.cc[row] = (T)s;
+        }
+        grid.sync();
+        // z_i += cc[cluster(i)] on the image's own columns; r.z, r.r partials
+        for (int i = gw; i < nI; i += nw) {
+            const size_t base = (size_t)i * D;
+            double rz = 0.0, rr = 0.0;
+            if (lane < D) {
+                const double rc = (double)a.r[base + lane];
+                double zc = (double)a.z[base + lane];
+                if ((a.img_pmask[i] >> lane) & 1) zc += (double)a.cc[(size_t)a.img_cluster[i] * D + lane];
+                const T zt = (T)zc;
+                a.z[base + lane] = zt;
+                if ((a.img_dmask[i] >> lane) & 1) {
+                    rz = rc * (double)zt;
+                    rr = rc * rc;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                rz += __shfl_xor_sync(0xffffffffu, rz, off);
+                rr += __shfl_xor_sync(0xffffffffu, rr, off);
+            }
+            if (lane == 0) {
+                a.part[i] = rz;
+                a.part[nI + i] = rr;
+            }
+        }
+        grid.sync();
+    }
+    // convergence test, beta, p = z + beta p
+    double rz = strided_sum_c(a.part, nI), rr = strided_sum_c(a.part + nI, nI);
+    rz = block_sum_c(rz, sh);
+    rr = block_sum_c(rr, sh);
+    const bool stop = rr <= st->pcg_tol2 * st->pcg_bb || !(rz > 0.0) || !isfinite(rz);
+    const double beta = stop ? 0.0 : rz / st->pcg_rzbuf[a.parity];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->pcg_iterations += 1;
+        st->pcg_total += 1;
+        st->pcg_rr = rr;
+        if (stop) {
+            st->pcg_done = 1;
+        } else {
+            st->pcg_beta = beta;
+            st->pcg_rzbuf[a.parity ^ 1] = rz;
+        }
+    }
+    if (stop) return;
+    const int nthreads = gridDim.x * blockDim.x;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.nID; u += nthreads) {
+        const int i = u / D, c = u - i * D;
+        const int zu = (a.img_owner && c >= 6) ? a.img_owner[i] * D + c : u;
+        const T pn = (T)((double)a.z[zu] + beta * (double)a.p[u]);
+        a.p[u] = pn;
+        if (a.p4) a.p4[plane_index(nI, i, c)] = (float)pn;
+    }
+}
+
+template <typename F>
+void dispatch_D_coop(int D, F &&f) {
+    switch (D) {
+    case 6: f(std::integral_constant<int, 6>()); break;
+    case 9: f(std::integral_constant<int, 9>()); break;
+    case 10: f(std::integral_constant<int, 10>()); break;
+    case 11: f(std::integral_constant<int, 11>()); break;
+    case 14: f(std::integral_constant<int, 14>()); break;
+    default: throw Error(SFMBA_ERR_INTERNAL, "unsupported image block width");
+    }
+}
+
+template <typename T, int D>
+void run_coop(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
+    VecArgs<T> a{};
+    a.ipart = (const T *)b.ipart;
+    a.ipart_off = b.ipart_off;
+    a.img_H = b.img_H;
+    a.img_active = b.img_active;
+    a.img_pmask = b.img_pmask;
+    a.img_dmask = b.img_dmask;
+    a.Minv = (const T *)b.pcg_Minv;
+    a.p = (T *)b.pcg_p;
+    a.q = (T *)b.pcg_q;
+    a.x = (T *)b.pcg_x;
+    a.r = (T *)b.pcg_r;
+    a.z = (T *)b.pcg_z;
+    a.p4 = std::is_same<T, float>::value ? b.pcg_p4 : nullptr;
+    a.part = b.pcg_part;
+    a.st = b.state;
+    a.nI = b.nI;
+    a.nID = b.nID;
+    a.parity = parity;
+    a.nsh = b.sh.nsh;
+    a.sh_img_start = b.sh.sh_img_start;
+    a.sh_imgs = b.sh.sh_imgs;
+    a.img_owner = b.sh.nsh > 0 ? b.sh.img_owner : nullptr;
+    if (coarse) {
+        a.nc = b.co.nc;
+        a.Nc = b.co.nc * D;
+        a.clu_start = b.co.clu_start;
+        a.img_cluster = b.co.img_cluster;
+        a.Ainv = b.co.Ainv;
+        a.zc = b.co.zc;
+        a.cc = (T *)b.co.cc;
+    }
+    // Co-resident grid: as many blocks as the widest phase needs, at most
+    // what the GPU holds at once (queried once per instance and device).
+    static int cap_dev = -1, cap = 0;
+    int dev = 0;
+    SFMBA_CUDA(cudaGetDevice(&dev));
+    if (cap_dev != dev) {
+        int per_sm = 0, sms = 0;
+        SFMBA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_vec_coop<T, D>, 256, 0));
+        SFMBA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cap = per_sm * sms;
+        cap_dev = dev;
+    }
+    if (cap < 1) throw Error(SFMBA_ERR_INTERNAL, "the PCG vector kernel cannot be resident");
+    const int want = std::max(std::max(std::max(div_up(b.nI, 8), div_up(a.Nc, 8)), div_up(a.nsh, 8)), 1);
+    const int grid = std::min(want, cap);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SFMBA_CUDA(cudaLaunchKernelEx(&cfg, k_pcg_vec_coop<T, D>, a));
+    SFMBA_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+void launch_pcg_iteration_vector(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
+    dispatch_D_coop(b.D, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        if (b.mixed) run_coop<float, D>(b, s, parity, coarse);
+        else run_coop<double, D>(b, s, parity, coarse);
+    });
+}
+
+}  // namespace sfmba

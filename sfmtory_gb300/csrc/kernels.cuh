@@ -148,7 +148,9 @@ struct Bufs {
     long long *count_partials = nullptr;
     // PCG (matrix-free) vectors, [nI*D] each, element type T
     void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
-    float *pcg_p4 = nullptr;      // FP32: [nI*pad4(D)] copy of p with 16-byte rows (point pass)
+    float *pcg_p4 = nullptr;      // FP32: copy of p in planes (plane_index; pad4(D)/4 planes of [nI] float4), point pass
+    float4 *img_mv = nullptr;     // FP32 PCG: per-image constants of MvOp in 5 planes of [nI] float4:
+                                  //   (R0 R1 R2 R3) (R4 R5 R6 R7) (R8 t0 t1 t2) (c0 c1 c2 c3) (c4 c5 c6 c7)
     CoarseBufs co;                // coarse correction of the preconditioner
     void *pcg_u = nullptr;        // [nP*4] per-point Cinv E^T p
     void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
@@ -327,6 +329,10 @@ void launch_pcg_start(const Bufs &b, cudaStream_t s);
 // launch_pcg_images_finish (q = S p) and launch_pcg_vector (x, r, z, p).
 void launch_pcg_images_finish(const Bufs &b, cudaStream_t s);
 void launch_pcg_vector(const Bufs &b, cudaStream_t s, int parity, bool coarse = false);  // parity = iteration & 1
+// Everything of one PCG iteration after the image pass (q = S p, the
+// shared cameras' sums, alpha, x/r/z, the coarse correction, beta, p) as one
+// cooperative launch with grid-wide barriers (k_pcg_coop.cu).
+void launch_pcg_iteration_vector(const Bufs &b, cudaStream_t s, int parity, bool coarse);
 // Work partition of the matrix-free passes (after sort_observations).
 void launch_pcg_partition(Bufs &b, cudaStream_t s);
 // Scatter the image-level solution to the slot-level delta.

@@ -39,6 +39,8 @@ struct JacSrc {
     // for the current parameters.
     const float4 *rs = nullptr;
     const unsigned char *img_live = nullptr;  // batched windows: images taking part (NULL: all)
+    const float4 *mv = nullptr;  // FP32 PCG: MvOp's per-image constants in planes (Bufs::img_mv)
+    int nI = 0;
 };
 
 // Jr~, Jx~ (2x3), Jc~ (2xD) of a stored record, 16-byte vector loads.
@@ -206,6 +208,167 @@ struct ObsOp<T, D, false, M> {
     __device__ __forceinline__ void jc_rows(T jc[2 * D]) const {
 #pragma unroll
         for (int c = 0; c < 2 * D; ++c) jc[c] = jcm[c];
+    }
+};
+
+// The Jacobian of one observation as the PCG passes apply it, recomputed in
+// FP32 for a camera model known at compile time (SIMPLE_PINHOLE, PINHOLE,
+// SIMPLE_RADIAL, RADIAL): instead of forming the 2 x 2 pixel derivative A,
+// the 2 x k parameter columns G and the compact rows d = s A Pn, it keeps
+// the normalised point (xp, yp), 1/z, q = R X and the model's scalars and
+// applies each factor in closed form. With Pn = [[1, 0, -xp], [0, 1, -yp]]/z:
+//   pose and point:  J v = s A Pn (omega x q + dt + R dX),
+//   transposes:      e = Pn^T A^T (s a); pose = [q x e, e], point = R^T e,
+//   camera:          J p_cam = s G p_cam, J^T a = s G^T a.
+// For the radial models A = f (d I + 2 d' x x^T) with x = (xp, yp) is
+// symmetric, so A and A^T are one formula. The same values as ObsOp in
+// exact arithmetic (about half the FP32 instructions); columns that are not
+// unknowns need no mask here because the PCG vectors are zero on them and
+// the image pass's sums for them are discarded by k_pcg_images_finish. The
+// per-image constants come from five planes of float4 (Bufs::img_mv), so
+// neighbouring images share cache lines.
+template <int M>
+__host__ __device__ constexpr bool mv_model() {
+    return M == SFMBA_SIMPLE_PINHOLE || M == SFMBA_PINHOLE || M == SFMBA_SIMPLE_RADIAL || M == SFMBA_RADIAL;
+}
+
+template <int D, int M>
+struct MvOp {
+    static_assert(model_fits_width(M, D), "MvOp covers exactly the model's columns");
+    float R[9];
+    float q0, q1, q2;
+    float xp, yp, iz, s;
+    float f, fy, d, dd2, r2;  // model scalars: fx (f), fy, radial factor d, 2 d(d)/d(r2), r^2
+
+    __device__ __forceinline__ void build(const JacSrc<float> &J, int img, int pt, int4 rc) {
+        const float4 *mv = J.mv + img;
+        const size_t nI = (size_t)J.nI;
+        const float4 m0 = __ldg(mv), m1 = __ldg(mv + nI), m2 = __ldg(mv + 2 * nI), c03 = __ldg(mv + 3 * nI);
+        float c4 = 0.0f;
+        if constexpr (M == SFMBA_RADIAL) c4 = __ldg(mv + 4 * nI).x;
+        const float4 X = __ldg(J.points32 + pt);
+        R[0] = m0.x; R[1] = m0.y; R[2] = m0.z; R[3] = m0.w;
+        R[4] = m1.x; R[5] = m1.y; R[6] = m1.z; R[7] = m1.w;
+        R[8] = m2.x;
+        q0 = R[0] * X.x + R[1] * X.y + R[2] * X.z;
+        q1 = R[3] * X.x + R[4] * X.y + R[5] * X.z;
+        q2 = R[6] * X.x + R[7] * X.y + R[8] * X.z;
+        const float pc0 = q0 + m2.y, pc1 = q1 + m2.z, pc2 = q2 + m2.w;
+        const bool ok = pc2 > float(kMinDepth);
+        iz = ok ? 1.0f / pc2 : 0.0f;
+        xp = pc0 * iz;
+        yp = pc1 * iz;
+        f = c03.x;
+        fy = f;
+        d = 1.0f;
+        dd2 = 0.0f;
+        r2 = xp * xp + yp * yp;
+        float cx = c03.y, cy = c03.z;
+        if constexpr (M == SFMBA_PINHOLE) {
+            fy = c03.y;
+            cx = c03.z;
+            cy = c03.w;
+        } else if constexpr (M == SFMBA_SIMPLE_RADIAL) {
+            d = 1.0f + c03.w * r2;
+            dd2 = 2.0f * c03.w;
+        } else if constexpr (M == SFMBA_RADIAL) {
+            d = 1.0f + r2 * (c03.w + c4 * r2);
+            dd2 = 2.0f * (c03.w + 2.0f * c4 * r2);
+        }
+        s = ok ? 1.0f : 0.0f;
+        if (ok && J.loss != SFMBA_LOSS_NONE) {  // sqrt of the robust weight of the FP32 residual
+            const float r0 = f * xp * d + cx - __int_as_float(rc.z);
+            const float r1 = fy * yp * d + cy - __int_as_float(rc.w);
+            s = sqrtf(robust_weight<float>(sqrtf(r0 * r0 + r1 * r1), J.loss, J.scale));
+        }
+    }
+    // (a0, a1) = A (x, y)
+    __device__ __forceinline__ void apply_A(float x, float y, float &a0, float &a1) const {
+        if constexpr (M == SFMBA_SIMPLE_RADIAL || M == SFMBA_RADIAL) {
+            const float t = dd2 * (xp * x + yp * y);
+            a0 = f * (d * x + xp * t);
+            a1 = f * (d * y + yp * t);
+        } else {
+            a0 = f * x;
+            a1 = fy * y;
+        }
+    }
+    // (s0, s1) = J~ v for an image-block vector v (pose, then camera columns).
+    __device__ __forceinline__ void jc_dot(const float *v, float &s0, float &s1) const {
+        const float w0 = v[1] * q2 - v[2] * q1 + v[3];
+        const float w1 = v[2] * q0 - v[0] * q2 + v[4];
+        const float w2 = v[0] * q1 - v[1] * q0 + v[5];
+        float a0, a1;
+        apply_A((w0 - xp * w2) * iz, (w1 - yp * w2) * iz, a0, a1);
+        if constexpr (M == SFMBA_SIMPLE_PINHOLE) {
+            a0 += xp * v[6] + v[7];
+            a1 += yp * v[6] + v[8];
+        } else if constexpr (M == SFMBA_PINHOLE) {
+            a0 += xp * v[6] + v[8];
+            a1 += yp * v[7] + v[9];
+        } else {
+            float k = d * v[6] + f * r2 * v[9];
+            if constexpr (M == SFMBA_RADIAL) k += f * r2 * r2 * v[10];
+            a0 += xp * k + v[7];
+            a1 += yp * k + v[8];
+        }
+        s0 = s * a0;
+        s1 = s * a1;
+    }
+    // e = Pn^T A^T (s a)
+    __device__ __forceinline__ void pull(float a0, float a1, float &e0, float &e1, float &e2) const {
+        float b0, b1;
+        apply_A(s * a0, s * a1, b0, b1);  // A symmetric (radial) or diagonal (pinhole)
+        e0 = b0 * iz;
+        e1 = b1 * iz;
+        e2 = -(xp * b0 + yp * b1) * iz;
+    }
+    // out = Jx~^T (a0, a1) = R^T e
+    __device__ __forceinline__ void jx_t(float a0, float a1, float out[3]) const {
+        float e0, e1, e2;
+        pull(a0, a1, e0, e1, e2);
+        out[0] = R[0] * e0 + R[3] * e1 + R[6] * e2;
+        out[1] = R[1] * e0 + R[4] * e1 + R[7] * e2;
+        out[2] = R[2] * e0 + R[5] * e1 + R[8] * e2;
+    }
+    // (z0, z1) = Jx~ u = s A Pn R u
+    __device__ __forceinline__ void jx(float u0, float u1, float u2, float &z0, float &z1) const {
+        const float a = R[0] * u0 + R[1] * u1 + R[2] * u2;
+        const float b = R[3] * u0 + R[4] * u1 + R[5] * u2;
+        const float c = R[6] * u0 + R[7] * u1 + R[8] * u2;
+        float a0, a1;
+        apply_A((a - xp * c) * iz, (b - yp * c) * iz, a0, a1);
+        z0 = s * a0;
+        z1 = s * a1;
+    }
+    // out = Jc~^T (z0, z1) = [q x e, e, s G^T z]
+    __device__ __forceinline__ void jc_t(float z0, float z1, float out[D]) const {
+        float e0, e1, e2;
+        pull(z0, z1, e0, e1, e2);
+        out[0] = q1 * e2 - q2 * e1;
+        out[1] = q2 * e0 - q0 * e2;
+        out[2] = q0 * e1 - q1 * e0;
+        out[3] = e0;
+        out[4] = e1;
+        out[5] = e2;
+        const float g0 = s * z0, g1 = s * z1;
+        if constexpr (M == SFMBA_SIMPLE_PINHOLE) {
+            out[6] = xp * g0 + yp * g1;
+            out[7] = g0;
+            out[8] = g1;
+        } else if constexpr (M == SFMBA_PINHOLE) {
+            out[6] = xp * g0;
+            out[7] = yp * g1;
+            out[8] = g0;
+            out[9] = g1;
+        } else {
+            const float t = xp * g0 + yp * g1;
+            out[6] = d * t;
+            out[7] = g0;
+            out[8] = g1;
+            out[9] = f * r2 * t;
+            if constexpr (M == SFMBA_RADIAL) out[10] = f * r2 * r2 * t;
+        }
     }
 };
 

@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
         r[u] = rt;
         z[u] = zt;
         p[u] = zt;
-        if (p4) p4[(size_t)i * pad4(D) + lane] = zt;
+        if (p4) p4[plane_index(nI, i, lane)] = zt;
         if ((pm >> lane) & 1) {  // a shared camera's entries are counted by launch_shared_precond
             rz = (double)rt * (double)zt;
             rr = (double)rt * (double)rt;
@@ -467,17 +467,18 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
 // per step (ILP) and the minimum resident blocks per SM the register
 // allocation must allow. Every variant computes the same sums in the same
 // order.
-// Image-block vector entries of image i: from the 16-byte padded FP32
-// mirror (pad4(D) floats per image, D/4 rounded up vector loads) when it
-// exists, else from the D-strided vector.
+// Image-block vector entries of image i: from the FP32 mirror in planes
+// (plane_index; D/4 rounded up vector loads, one per plane) when it exists,
+// else from the D-strided vector.
 template <typename T, int D>
-__device__ __forceinline__ void load_image_vec(const T *__restrict__ v, const T *__restrict__ v4, int i, T (&out)[D]) {
+__device__ __forceinline__ void load_image_vec(const T *__restrict__ v, const T *__restrict__ v4, int i, int nI,
+                                               T (&out)[D]) {
     if constexpr (std::is_same<T, float>::value) {
         if (v4) {
-            const float4 *q = reinterpret_cast<const float4 *>(v4 + (size_t)i * pad4(D));
+            const float4 *q = reinterpret_cast<const float4 *>(v4);
 #pragma unroll
             for (int k = 0; k < pad4(D) / 4; ++k) {
-                const float4 t = __ldg(q + k);
+                const float4 t = __ldg(q + (size_t)k * nI + i);
                 if (4 * k + 0 < D) out[4 * k + 0] = t.x;
                 if (4 * k + 1 < D) out[4 * k + 1] = t.y;
                 if (4 * k + 2 < D) out[4 * k + 2] = t.z;
@@ -509,13 +510,20 @@ __global__ void __launch_bounds__(256, PassVariant<V>::kMinBlocks)
     point_chunk<T, 3, PassVariant<V>::kILP>(
         J.obrec, pchunk[warp], pchunk[warp + 1], lane,
         [&](int o, int4 rc, T (&v)[3]) {
-            ObsOp<T, D, RC, M> op;
-            make_op_point_major<T, D, RC>(J, o, rc, op);
             T pv[D];
-            load_image_vec<T, D>(p, p4, rc.x, pv);
+            load_image_vec<T, D>(p, p4, rc.x, J.nI, pv);
             T s0, s1;
-            op.jc_dot(pv, s0, s1);
-            op.jx_t(s0, s1, v);
+            if constexpr (RC && mv_model<M>()) {
+                MvOp<D, M> op;
+                op.build(J, rc.x, rc.y, rc);
+                op.jc_dot(pv, s0, s1);
+                op.jx_t(s0, s1, v);
+            } else {
+                ObsOp<T, D, RC, M> op;
+                make_op_point_major<T, D, RC>(J, o, rc, op);
+                op.jc_dot(pv, s0, s1);
+                op.jx_t(s0, s1, v);
+            }
         },
         [&](int pt, const T (&v)[3]) {
             T u0 = 0, u1 = 0, u2 = 0;
@@ -576,11 +584,18 @@ __global__ void __launch_bounds__(256, PassVariant<V>::kMinBlocks)
             const T *up = u + 4 * (size_t)pt;
             u0 = up[0]; u1 = up[1]; u2 = up[2];
         }
-        ObsOp<T, D, RC, M> op;
-        make_op_image_major<T, D, RC>(J, k, rc, op);
         T z0, z1;
-        op.jx(u0, u1, u2, z0, z1);
-        op.jc_t(z0, z1, cv);
+        if constexpr (RC && mv_model<M>()) {
+            MvOp<D, M> op;
+            op.build(J, rc.x, rc.y, rc);
+            op.jx(u0, u1, u2, z0, z1);
+            op.jc_t(z0, z1, cv);
+        } else {
+            ObsOp<T, D, RC, M> op;
+            make_op_image_major<T, D, RC>(J, k, rc, op);
+            op.jx(u0, u1, u2, z0, z1);
+            op.jc_t(z0, z1, cv);
+        }
     };
     auto accumulate = [&](bool valid, int img, const T (&cv)[D]) {
         while (true) {
@@ -714,6 +729,8 @@ JacSrc<T> jac_src(const Bufs &b) {
     J.scale = (T)b.loss_scale;
     if constexpr (std::is_same<T, float>::value) J.rs = b.ob_rs;
     J.img_live = b.img_live;
+    J.mv = b.img_mv;
+    J.nI = b.nI;
     return J;
 }
 

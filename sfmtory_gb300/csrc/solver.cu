@@ -1124,6 +1124,7 @@ class Solver {
                     b.pcg_z = A.take<char>((size_t)nID * tsz);
                     b.pcg_p = A.take<char>((size_t)nID * tsz);
                     b.pcg_p4 = mixed ? A.take<float>((size_t)nI * pad4(D)) : nullptr;
+                    b.img_mv = mixed ? A.take<float4>((size_t)5 * nI) : nullptr;
                     b.pcg_q = A.take<char>((size_t)nID * tsz);
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
                     b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
@@ -1373,8 +1374,8 @@ class Solver {
                         auto chunk = [&] {
                             for (int k = 0; k < m; ++k) {
                                 { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_, vp); }
-                                { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_, vi); launch_pcg_images_finish(b, s_); }
-                                { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_vector(b, s_, k & 1, coarse); }
+                                { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_, vi); }
+                                { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_iteration_vector(b, s_, k & 1, coarse); }
                             }
                         };
                         pcg_chunk_[coarse ? 1 : 0].run(s_, m == kPcgPollEvery && !profiler().on, chunk);
