@@ -10,6 +10,7 @@
 #include <type_traits>
 
 #include "camera.cuh"
+#include "chol_block.cuh"
 #include "kernels.cuh"
 #include "schur.cuh"
 
@@ -275,7 +276,8 @@ __global__ void __launch_bounds__(256) k_wb_chol_diag(double *Lall, const long l
     extern __shared__ double sm[];
     double *A = sm;
     double *X = sm + NB * LD;
-    __shared__ int fail;
+    __shared__ double buf[NB + 1];
+    static_assert(LD == kBlkLD, "tile stride of chol_block_factor_invert");
     const int w = blockIdx.x;
     const int n = n_w[w];
     if (!ws[w].active || ws[w].factor_failed || k0 >= n) return;
@@ -286,27 +288,8 @@ __global__ void __launch_bounds__(256) k_wb_chol_diag(double *Lall, const long l
         const int r = idx / nb, c = idx - r * nb;
         A[r * LD + c] = c <= r ? L[(size_t)(k0 + r) * n + k0 + c] : 0.0;
     }
-    if (tid == 0) fail = 0;
     __syncthreads();
-    for (int j = 0; j < nb; ++j) {
-        if (tid == 0) {
-            const double d = A[j * LD + j];
-            if (!(d > 0.0)) fail = 1;
-            else A[j * LD + j] = sqrt(d);
-        }
-        __syncthreads();
-        if (fail) break;
-        const double piv = A[j * LD + j];
-        for (int i = j + 1 + tid; i < nb; i += blockDim.x) A[i * LD + j] /= piv;
-        __syncthreads();
-        const int m = nb - j - 1;
-        for (int idx = tid; idx < m * m; idx += blockDim.x) {
-            const int i = j + 1 + idx / m, l = j + 1 + idx % m;
-            if (l <= i) A[i * LD + l] -= A[i * LD + j] * A[l * LD + j];
-        }
-        __syncthreads();
-    }
-    if (fail) {
+    if (!chol_block_factor_invert(A, X, nb, buf)) {
         if (tid == 0) ws[w].factor_failed = 1;
         return;
     }
@@ -314,16 +297,6 @@ __global__ void __launch_bounds__(256) k_wb_chol_diag(double *Lall, const long l
         const int r = idx / nb, c = idx - r * nb;
         if (c <= r) L[(size_t)(k0 + r) * n + k0 + c] = A[r * LD + c];
     }
-    if (tid < nb) {
-        const int c = tid;
-        for (int r = 0; r < c; ++r) X[r * LD + c] = 0.0;
-        for (int r = c; r < nb; ++r) {
-            double s = r == c ? 1.0 : 0.0;
-            for (int k = c; k < r; ++k) s -= A[r * LD + k] * X[k * LD + c];
-            X[r * LD + c] = s / A[r * LD + r];
-        }
-    }
-    __syncthreads();
     double *out = Linv_all + linv_off[w] + (size_t)(k0 / NB) * NB * NB;
     for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
         const int r = idx / NB, c = idx - r * NB;

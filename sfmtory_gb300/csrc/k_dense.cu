@@ -13,6 +13,7 @@
 //     FP64 accuracy; the plain FP64 path keeps FP64 fused multiply-adds.
 #include <type_traits>
 
+#include "chol_block.cuh"
 #include "kernels.cuh"
 #include "ozaki.cuh"
 #include "schur.cuh"
@@ -110,7 +111,8 @@ __global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, dou
     extern __shared__ double sm[];
     double *A = sm;            // NB x LD
     double *X = sm + NB * LD;  // NB x LD
-    __shared__ int fail;
+    __shared__ double buf[NB + 1];
+    static_assert(LD == kBlkLD, "tile stride of chol_block_factor_invert");
     if (st->factor_failed) return;
     const int nb = min(NB, n - k0);
     const int tid = threadIdx.x;
@@ -118,27 +120,8 @@ __global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, dou
         const int r = idx / nb, c = idx - r * nb;
         A[r * LD + c] = c <= r ? L[(size_t)(k0 + r) * n + k0 + c] : 0.0;
     }
-    if (tid == 0) fail = 0;
     __syncthreads();
-    for (int j = 0; j < nb; ++j) {
-        if (tid == 0) {
-            const double d = A[j * LD + j];
-            if (!(d > 0.0)) fail = 1;
-            else A[j * LD + j] = sqrt(d);
-        }
-        __syncthreads();
-        if (fail) break;
-        const double piv = A[j * LD + j];
-        for (int i = j + 1 + tid; i < nb; i += blockDim.x) A[i * LD + j] /= piv;
-        __syncthreads();
-        const int m = nb - j - 1;
-        for (int idx = tid; idx < m * m; idx += blockDim.x) {
-            const int i = j + 1 + idx / m, l = j + 1 + idx % m;
-            if (l <= i) A[i * LD + l] -= A[i * LD + j] * A[l * LD + j];
-        }
-        __syncthreads();
-    }
-    if (fail) {
+    if (!chol_block_factor_invert(A, X, nb, buf)) {
         if (tid == 0) st->factor_failed = 1;
         return;
     }
@@ -146,17 +129,6 @@ __global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, dou
         const int r = idx / nb, c = idx - r * nb;
         if (c <= r) L[(size_t)(k0 + r) * n + k0 + c] = A[r * LD + c];
     }
-    // Inverse of the lower-triangular factor, one column per thread.
-    if (tid < nb) {
-        const int c = tid;
-        for (int r = 0; r < c; ++r) X[r * LD + c] = 0.0;
-        for (int r = c; r < nb; ++r) {
-            double s = r == c ? 1.0 : 0.0;
-            for (int k = c; k < r; ++k) s -= A[r * LD + k] * X[k * LD + c];
-            X[r * LD + c] = s / A[r * LD + r];
-        }
-    }
-    __syncthreads();
     double *out = Linv + (size_t)(k0 / NB) * NB * NB;
     for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
         const int r = idx / NB, c = idx - r * NB;
