@@ -116,11 +116,11 @@ typedef struct sfmba_options {
     int32_t pcg_coarse_clusters;  /* PCG solver: clusters of consecutive images in the
                                      coarse correction of the preconditioner (0: 64,
                                      at most 128; < 0: block-Jacobi alone) */
-    int32_t dense_fp64_fma;       /* dense solver, mixed path: 0 (default) runs the
-                                     Cholesky's trailing updates on the BF16 tensor
-                                     cores by error-free splitting (FP64 accuracy);
-                                     1 keeps FP64 fused multiply-adds, as the FP64
-                                     path does */
+    int32_t dense_fp64_fma;       /* dense solver and batched windows, mixed path:
+                                     0 (default) runs the Cholesky's trailing updates
+                                     on the BF16 tensor cores by error-free splitting
+                                     (FP64 accuracy); 1 keeps FP64 fused
+                                     multiply-adds, as the FP64 path does */
     int32_t reserved[3];
 } sfmba_options;
 

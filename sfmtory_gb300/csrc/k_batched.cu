@@ -12,6 +12,7 @@
 #include "camera.cuh"
 #include "chol_block.cuh"
 #include "kernels.cuh"
+#include "ozaki.cuh"
 #include "schur.cuh"
 
 namespace sfmba {
@@ -402,6 +403,55 @@ __global__ void __launch_bounds__(256) k_wb_chol_update(double *Lall, const long
             L[(size_t)(ri + r) * n + rj + c] -= acc[a][b];
         }
     }
+}
+
+// Tensor-core form of the two kernels above for the mixed batch (ozaki.cuh):
+// slices and exponents of window w's panel rows (global slot index
+// slot_base[w] + row; slices [kOzSlices][ntot][64]), then the trailing tiles.
+__global__ void __launch_bounds__(256) k_wb_oz_split(const double *Lall, const long long *s_off, const int *n_w,
+                                                      int k0, const WinState *ws, const int *slot_base, int ntot,
+                                                      __nv_bfloat16 *slices, int *exps) {
+    const int w = blockIdx.y;
+    const int n = n_w[w];
+    if (!ws[w].active || ws[w].factor_failed || k0 >= n) return;
+    const int nb = min(NB, n - k0);
+    const int r = k0 + nb + blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= n) return;
+    const int g = slot_base[w] + r;
+    oz_split_row(Lall + s_off[w] + (size_t)r * n + k0, nb, threadIdx.x & 31, slices + (size_t)g * kOzK,
+                 (size_t)ntot * kOzK, exps + g);
+}
+
+__global__ void __launch_bounds__(128, 1) k_wb_oz_update(double *Lall, const long long *s_off, const int *n_w, int k0,
+                                                         const WinState *ws, const int *row_first,
+                                                         const int *slot_base, int ntot,
+                                                         const __nv_bfloat16 *slices, const int *exps) {
+    extern __shared__ __align__(16) unsigned char oz_sm[];
+    __shared__ double fR[kOzTile], fC[kOzTile];
+    const int w = blockIdx.y;
+    const int n = n_w[w];
+    if (!ws[w].active || ws[w].factor_failed || k0 + NB >= n) return;
+    const int t0 = k0 + NB;
+    const long long q = blockIdx.x;
+    int ti = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while ((long long)(ti + 1) * (ti + 2) / 2 <= q) ++ti;
+    while ((long long)ti * (ti + 1) / 2 > q) --ti;
+    const int tj = (int)(q - (long long)ti * (ti + 1) / 2);
+    const int ri = t0 + ti * kOzTile, rj = t0 + tj * kOzTile;
+    if (ri >= n || rj >= n) return;
+    const int mi = min(kOzTile, n - ri), mj = min(kOzTile, n - rj);
+    // a panel tile whose rows all start right of this column block is zero
+    const int sb = slot_base[w];
+    const int *rf = row_first + sb;
+    const int tr = threadIdx.x;
+    const bool nzi = tr < mi && rf[ri + tr] <= k0 + NB - 1;
+    const bool nzj = tr >= kOzTile && tr - kOzTile < mj && rf[rj + tr - kOzTile] <= k0 + NB - 1;
+    const int any_i = __syncthreads_or(nzi);
+    const int any_j = __syncthreads_or(nzj);
+    if (!any_i || !any_j) return;
+    oz_tile_update(Lall + s_off[w] + (size_t)ri * n + rj, (size_t)n, mi, mj, ti == tj,
+                   slices + (size_t)(sb + ri) * kOzK, slices + (size_t)(sb + rj) * kOzK, (size_t)ntot * kOzK,
+                   exps + sb + ri, exps + sb + rj, oz_sm, fR, fC);
 }
 
 // Whole triangular solve L L^T x = b of window w in one CTA (windows are at
@@ -908,6 +958,7 @@ void set_smem_limits() {
     SFMBA_CUDA(cudaFuncSetAttribute(k_wb_chol_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTwoTiles));
     SFMBA_CUDA(cudaFuncSetAttribute(k_wb_chol_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTwoTiles));
     SFMBA_CUDA(cudaFuncSetAttribute(k_wb_chol_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPanel));
+    SFMBA_CUDA(cudaFuncSetAttribute(k_wb_oz_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOzSmem));
     done = true;
 }
 
@@ -1003,7 +1054,15 @@ void launch_wb_cholesky(const Bufs &b, const WinBufs &w, cudaStream_t s) {
         SFMBA_LAUNCH_CHECK();
         const long long tiles = div_up(rem, NB);
         dim3 gu((unsigned)(tiles * (tiles + 1) / 2), w.W);
-        k_wb_chol_update<<<gu, 256, kSmemTwoTiles, s>>>(b.L, w.s_off, w.n_w, k0, w.ws, w.row_first, w.slot_base);
+        if (b.oz_slices) {  // tensor-core update (ozaki.cuh)
+            k_wb_oz_split<<<dim3(div_up(rem, 8), w.W), 256, 0, s>>>(b.L, w.s_off, w.n_w, k0, w.ws, w.slot_base, b.n,
+                                                                    (__nv_bfloat16 *)b.oz_slices, b.oz_exp);
+            SFMBA_LAUNCH_CHECK();
+            k_wb_oz_update<<<gu, 128, kOzSmem, s>>>(b.L, w.s_off, w.n_w, k0, w.ws, w.row_first, w.slot_base, b.n,
+                                                    (const __nv_bfloat16 *)b.oz_slices, b.oz_exp);
+        } else {
+            k_wb_chol_update<<<gu, 256, kSmemTwoTiles, s>>>(b.L, w.s_off, w.n_w, k0, w.ws, w.row_first, w.slot_base);
+        }
         SFMBA_LAUNCH_CHECK();
     }
 }

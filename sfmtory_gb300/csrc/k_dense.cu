@@ -237,8 +237,6 @@ __global__ void __launch_bounds__(256) k_oz_split(const double *L, int n, int k0
 __global__ void __launch_bounds__(128, 1) k_oz_update(double *L, int n, int k0, const __nv_bfloat16 *slices,
                                                       const int *exps, const LMState *st) {
     extern __shared__ __align__(16) unsigned char oz_sm[];
-    __nv_bfloat16 *sR = reinterpret_cast<__nv_bfloat16 *>(oz_sm);
-    __nv_bfloat16 *sC = sR + (size_t)kOzSlices * kOzTile * kOzLds;
     __shared__ double fR[kOzTile], fC[kOzTile];
     if (st->factor_failed) return;
     const int t0 = k0 + NB;
@@ -249,67 +247,9 @@ __global__ void __launch_bounds__(128, 1) k_oz_update(double *L, int n, int k0, 
     const int tj = (int)(q - (long long)ti * (ti + 1) / 2);
     const int ri = t0 + ti * kOzTile, rj = t0 + tj * kOzTile;
     if (ri >= n || rj >= n) return;
-    const bool diag = ti == tj;
-    auto load = [&](__nv_bfloat16 *dst, int r0) {  // 16-byte pieces, rows past n as zeros
-        for (int e = threadIdx.x; e < kOzSlices * kOzTile * 8; e += blockDim.x) {
-            const int i = e / (kOzTile * 8), rr = (e / 8) % kOzTile, ch = e % 8;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (r0 + rr < n)
-                v = *reinterpret_cast<const uint4 *>(slices + (size_t)i * n * kOzK + (size_t)(r0 + rr) * kOzK + ch * 8);
-            *reinterpret_cast<uint4 *>(dst + ((size_t)i * kOzTile + rr) * kOzLds + ch * 8) = v;
-        }
-    };
-    load(sR, ri);
-    if (!diag) load(sC, rj);
-    const __nv_bfloat16 *cs = diag ? sR : sC;
-    if (threadIdx.x < kOzTile) {
-        const int r = ri + threadIdx.x;
-        fR[threadIdx.x] = r < n ? ldexp(1.0, exps[r] - 24) : 0.0;
-    } else {
-        const int c = rj + threadIdx.x - kOzTile;
-        fC[threadIdx.x - kOzTile] = c < n ? ldexp(1.0, exps[c]) : 0.0;
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wr = warp >> 1, wc = warp & 1;
-    float T[2][4][4], acc[2][4][4];
-    int I[2][4][4];
-    for (int d = 8; d >= 2; --d) {  // weight 2^-8d; the smallest first
-#pragma unroll
-        for (int m = 0; m < 2; ++m)
-#pragma unroll
-            for (int nn = 0; nn < 4; ++nn)
-#pragma unroll
-                for (int e = 0; e < 4; ++e) acc[m][nn][e] = 0.0f;
-        for (int i = max(1, d - kOzSlices); i <= min(kOzSlices, d - 1); ++i)
-            oz_product(sR, cs, i - 1, d - i - 1, wr, wc, lane, acc);
-#pragma unroll
-        for (int m = 0; m < 2; ++m)
-#pragma unroll
-            for (int nn = 0; nn < 4; ++nn)
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const float g = acc[m][nn][e];
-                    if (d == 8) T[m][nn][e] = g;
-                    else if (d >= 4) T[m][nn][e] = fmaf(T[m][nn][e], 0.00390625f, g);
-                    else if (d == 3) I[m][nn][e] = __float2int_rn(g);
-                    else I[m][nn][e] = __float2int_rn(g) * 256 + I[m][nn][e];
-                }
-    }
-    const int g = lane >> 2, tg = lane & 3;
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int nn = 0; nn < 4; ++nn)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int row = wr * 32 + m * 16 + g + 8 * (e >> 1), col = wc * 32 + nn * 8 + 2 * tg + (e & 1);
-                const int r = ri + row, c = rj + col;
-                if (r >= n || c >= n || (diag && c > r)) continue;
-                const double v = fma((double)T[m][nn][e], 0.00390625, (double)I[m][nn][e]);
-                double *a = L + (size_t)r * n + c;
-                *a = fma(-v * fR[row], fC[col], *a);
-            }
+    oz_tile_update(L + (size_t)ri * n + rj, (size_t)n, min(kOzTile, n - ri), min(kOzTile, n - rj), ti == tj,
+                   slices + (size_t)ri * kOzK, slices + (size_t)rj * kOzK, (size_t)n * kOzK, exps + ri, exps + rj,
+                   oz_sm, fR, fC);
 }
 
 // Forward step k of L y = b: y_k = Lkk^-1 b_k, then b_r -= L[r, k-block] y_k

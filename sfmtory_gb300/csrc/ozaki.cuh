@@ -110,4 +110,75 @@ __device__ __forceinline__ void oz_product(const __nv_bfloat16 *sR, const __nv_b
     }
 }
 
+// One 64 x 64 tile of the update, A[r, c] -= (P P^T)[r, c] for r < mi,
+// c < mj (c <= r on a diagonal tile), by a 128-thread block. A: the tile's
+// first entry, row stride lda. slR / slC: slice 0 of the tile's first row /
+// column (64 BF16 per row, slice i at + i * slice_stride). eR / eC: the
+// exponents of those rows. smem: kOzSmem bytes of dynamic shared memory;
+// fR, fC: [64] shared.
+__device__ __forceinline__ void oz_tile_update(double *A, size_t lda, int mi, int mj, bool diag,
+                                               const __nv_bfloat16 *slR, const __nv_bfloat16 *slC,
+                                               size_t slice_stride, const int *eR, const int *eC,
+                                               unsigned char *smem, double *fR, double *fC) {
+    __nv_bfloat16 *sR = reinterpret_cast<__nv_bfloat16 *>(smem);
+    __nv_bfloat16 *sC = sR + (size_t)kOzSlices * kOzTile * kOzLds;
+    auto load = [&](__nv_bfloat16 *dst, const __nv_bfloat16 *src, int rows) {  // 16-byte pieces, missing rows zero
+        for (int e = threadIdx.x; e < kOzSlices * kOzTile * 8; e += blockDim.x) {
+            const int i = e / (kOzTile * 8), rr = (e / 8) % kOzTile, ch = e % 8;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (rr < rows) v = *reinterpret_cast<const uint4 *>(src + (size_t)i * slice_stride + (size_t)rr * kOzK + ch * 8);
+            *reinterpret_cast<uint4 *>(dst + ((size_t)i * kOzTile + rr) * kOzLds + ch * 8) = v;
+        }
+    };
+    load(sR, slR, mi);
+    if (!diag) load(sC, slC, mj);
+    const __nv_bfloat16 *cs = diag ? sR : sC;
+    if (threadIdx.x < kOzTile) {
+        fR[threadIdx.x] = (int)threadIdx.x < mi ? ldexp(1.0, eR[threadIdx.x] - 24) : 0.0;
+    } else if (threadIdx.x < 2 * kOzTile) {
+        const int c = threadIdx.x - kOzTile;
+        fC[c] = c < mj ? ldexp(1.0, eC[c]) : 0.0;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wr = warp >> 1, wc = warp & 1;
+    float T[2][4][4], acc[2][4][4];
+    int I[2][4][4];
+    for (int d = 8; d >= 2; --d) {  // weight 2^-8d; the smallest first
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int nn = 0; nn < 4; ++nn)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[m][nn][e] = 0.0f;
+        for (int i = max(1, d - kOzSlices); i <= min(kOzSlices, d - 1); ++i)
+            oz_product(sR, cs, i - 1, d - i - 1, wr, wc, lane, acc);
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int nn = 0; nn < 4; ++nn)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float g = acc[m][nn][e];
+                    if (d == 8) T[m][nn][e] = g;
+                    else if (d >= 4) T[m][nn][e] = fmaf(T[m][nn][e], 0.00390625f, g);
+                    else if (d == 3) I[m][nn][e] = __float2int_rn(g);
+                    else I[m][nn][e] = __float2int_rn(g) * 256 + I[m][nn][e];
+                }
+    }
+    const int g = lane >> 2, tg = lane & 3;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int nn = 0; nn < 4; ++nn)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int r = wr * 32 + m * 16 + g + 8 * (e >> 1), c = wc * 32 + nn * 8 + 2 * tg + (e & 1);
+                if (r >= mi || c >= mj || (diag && c > r)) continue;
+                const double v = fma((double)T[m][nn][e], 0.00390625, (double)I[m][nn][e]);
+                double *a = A + (size_t)r * lda + c;
+                *a = fma(-v * fR[r], fC[c], *a);
+            }
+}
+
 }  // namespace sfmba

@@ -1105,6 +1105,12 @@ class Solver {
                     b.Linv = A.take<double>((size_t)batch->linv_total);
                     b.lu_perm = A.take<int>(n);
                     pair_scan = A.take<long long>(nP);
+                    b.oz_slices = nullptr;
+                    b.oz_exp = nullptr;
+                    if (mixed && !o->dense_fp64_fma) {  // tensor-core trailing updates (ozaki.cuh)
+                        b.oz_slices = A.take<uint16_t>((size_t)kOzSlices * n * kOzK);
+                        b.oz_exp = A.take<int>(n);
+                    }
                 } else if (solver_ == SFMBA_SOLVER_DENSE) {
                     b.S_img = A.take<double>((size_t)nID * nID);
                     b.S = A.take<double>((size_t)n * n);
