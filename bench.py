@@ -863,6 +863,7 @@ def run_ours(args):
         "clocks": clk,
         "phase_ms_profiled_step": {k: round(v["ms"], 3) for k, v in prof.items()
                                    if isinstance(v, dict) and v.get("launches")},
+        "counts_profiled_step": prof.get("counts", {}),
     }
     if not args.skip_side and world == 1:
         line["dense_radial500"] = dense_radial500(args, L, device, stream)

@@ -326,21 +326,34 @@ __global__ void k_coarse_finish(const double *part, const int *group_chunk_off, 
 //
 // Each block computes the step's P itself (one warp, rows in registers,
 // the scalar sweep with shuffles), from the same data in the same order, so
-// every block gets the same P and the same pivot test: a pivot that is not
-// > 0 (or a non-finite one) stops every block at the same step, before the
-// next barrier. Then the block writes its 64 x 64 output tiles.
+// every block gets the same P and takes the same branches. In exact
+// arithmetic every pivot of the lifted matrix is at least the lift,
+// 1e-6 of its diagonal entry (a Schur complement of A + D is at least D);
+// an FP32 pivot below that (rounding in a nearly singular direction) is
+// raised to it, which sweeps A + E with E >= 0 diagonal: still a symmetric
+// positive-definite preconditioner. A non-finite pivot stops every block at
+// the same step, before the next barrier. Then the block writes its
+// 64 x 64 output tiles.
 constexpr int kSwPiv = 32;
 constexpr int kSwTile = 64;
 
-// Lane r of the calling warp holds row r of the 32 x 32 block; on return it
-// holds row r of -A^-1 (the block swept on every index). False if a pivot
-// is not > 0 or not finite (the same answer in every lane).
-__device__ __forceinline__ bool sweep32(float (&a)[kSwPiv], int lane) {
+// Lane r of the calling warp holds row r of the 32 x 32 block and floor,
+// the smallest admissible value of pivot r; on return it holds row r of
+// -A^-1 (the block swept on every index, pivots below their floor raised to
+// it, counted in *raised). False if a pivot is not finite (the same answer
+// in every lane).
+__device__ __forceinline__ bool sweep32(float (&a)[kSwPiv], float floor, int lane, int *raised) {
 #pragma unroll
     for (int j = 0; j < kSwPiv; ++j) {
-        const float piv = __shfl_sync(0xffffffffu, a[j], j);
+        float piv = __shfl_sync(0xffffffffu, a[j], j);
+        const float fl = __shfl_sync(0xffffffffu, floor, j);
+        if (!isfinite(piv)) return false;
+        if (!(piv > fl)) {
+            piv = fl;
+            ++*raised;
+        }
         const float ip = 1.0f / piv;
-        if (!(piv > 0.0f) || !isfinite(ip)) return false;
+        if (!isfinite(ip)) return false;
         const float f = a[j];
 #pragma unroll
         for (int c = 0; c < kSwPiv; ++c) {
@@ -358,7 +371,8 @@ struct SweepArgs {
     int Nc, Np;       // size, padded size (multiple of kSwTile)
     float *X0, *X1;   // [Np x Np] ping-pong buffers
     float *Ainv;      // [Nc x Nc] result
-    int *fail;        // set when a pivot block is not positive definite
+    float *dref;      // [Np] the lifted diagonal (pivot floors: 1e-6 of it)
+    int *stats;       // [0]: set on a non-finite pivot; [1]: pivots raised to their floor
 };
 
 __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
@@ -387,6 +401,7 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
                 if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + 1e-6);
             }
             g.X0[(size_t)r * Np + c] = (float)v;
+            if (r == c) g.dref[r] = (float)v;
         }
     }
     grid.sync();
@@ -406,14 +421,18 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
                 a[4 * q + 2] = v.z;
                 a[4 * q + 3] = v.w;
             }
-            const bool ok = sweep32(a, lane);
-            if (lane == 0) sfail = ok ? 0 : 1;
+            int raised = 0;
+            const bool ok = sweep32(a, 1e-6f * fabsf(g.dref[k0 + lane]), lane, &raised);
+            if (lane == 0) {
+                sfail = ok ? 0 : 1;
+                if (blockIdx.x == 0 && raised) g.stats[1] += raised;
+            }
 #pragma unroll
             for (int c = 0; c < kSwPiv; ++c) sP[lane][c] = -a[c];
         }
         __syncthreads();
         if (sfail) {  // every block stops at this step; the result is all zeros
-            if (blockIdx.x == 0 && tid == 0) *g.fail = 1;
+            if (blockIdx.x == 0 && tid == 0) g.stats[0] = 1;
             for (long long e = blockIdx.x * (long long)blockDim.x + tid; e < (long long)Nc * Nc;
                  e += (long long)gridDim.x * blockDim.x)
                 g.Ainv[e] = 0.0f;
@@ -681,7 +700,7 @@ int coarse_padded_size(int Nc) { return div_up(Nc, kSwTile) * kSwTile; }
 void launch_coarse_invert(const Bufs &b, cudaStream_t s) {
     const CoarseBufs &co = b.co;
     const int Nc = co.nc * b.D, Np = coarse_padded_size(Nc);
-    SFMBA_CUDA(cudaMemsetAsync(co.fail, 0, sizeof(int), s));
+    SFMBA_CUDA(cudaMemsetAsync(co.fail, 0, 2 * sizeof(int), s));
     static int cap_dev = -1, cap = 0;  // co-resident blocks, queried once per device
     int dev = 0;
     SFMBA_CUDA(cudaGetDevice(&dev));
@@ -694,7 +713,7 @@ void launch_coarse_invert(const Bufs &b, cudaStream_t s) {
     }
     if (cap < 1) throw Error(SFMBA_ERR_INTERNAL, "the coarse inverse kernel cannot be resident");
     const int nt = Np / kSwTile;
-    SweepArgs g{co.A, Nc, Np, co.X32, co.X32 + (size_t)Np * Np, co.Ainv, co.fail};
+    SweepArgs g{co.A, Nc, Np, co.X32, co.X32 + (size_t)Np * Np, co.Ainv, co.X32 + (size_t)2 * Np * Np, co.fail};
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)std::min(nt * nt, cap));
     cfg.blockDim = dim3(256);

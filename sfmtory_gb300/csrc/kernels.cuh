@@ -29,8 +29,9 @@ struct CoarseBufs {
     int4 *chunk = nullptr;            // [nchunks] {group, first, end, 0} into pair_pt
     double *chunk_part = nullptr;     // [nchunks][D*D]
     double *A = nullptr;              // [Nc*Nc] coarse matrix, FP64
-    float *X32 = nullptr;             // [2][Np*Np] ping-pong buffers of the block sweep (coarse_padded_size)
-    int *fail = nullptr;              // set when the sweep meets a pivot block that is not positive definite
+    float *X32 = nullptr;             // [2][Np*Np] ping-pong buffers of the block sweep (coarse_padded_size),
+                                      // then [Np] pivot floors
+    int *fail = nullptr;              // [2]: the sweep met a non-finite pivot; pivots raised to their floor
     float *Ainv = nullptr;            // [Nc*Nc] symmetric FP32 A^-1, applied per iteration
     void *cc = nullptr;               // [Nc] coarse correction, element type of the PCG vectors
     double *zc = nullptr;             // [Nc] Z^T r
@@ -372,7 +373,8 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s);
 // z += Z Ainv Z^T r with the r.z / r.r partials (init: the start of a solve, p = z).
 void launch_coarse_correct(const Bufs &b, bool init, cudaStream_t s);
 // Ainv = A_c^-1 in FP32 by the block sweep (one cooperative launch); on a
-// breakdown *co.fail = 1 and Ainv = 0.
+// non-finite pivot co.fail[0] = 1 and Ainv = 0; co.fail[1] counts the
+// pivots raised to their floor.
 void launch_coarse_invert(const Bufs &b, cudaStream_t s);
 // Side of the sweep's square buffers for an Nc x Nc coarse matrix.
 int coarse_padded_size(int Nc);

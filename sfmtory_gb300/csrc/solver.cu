@@ -67,8 +67,12 @@ struct Profiler {
     double ms[PH_COUNT] = {0};
     long long launches[PH_COUNT] = {0};
     std::map<std::string, double> host_ms;  // wall time of host stages (ms)
+    std::map<std::string, long long> counts;  // event counts (coarse inverses, their breakdowns)
     void host(const char *name, double seconds) {
         if (on) host_ms[name] += seconds * 1e3;
+    }
+    void count(const char *name, long long k) {
+        if (on) counts[name] += k;
     }
     cudaEvent_t take() {
         if (used == pool.size()) {
@@ -95,6 +99,7 @@ struct Profiler {
         resolve();
         for (int k = 0; k < PH_COUNT; ++k) { ms[k] = 0; launches[k] = 0; }
         host_ms.clear();
+        counts.clear();
     }
 };
 
@@ -766,8 +771,8 @@ class Solver {
             co.img_cluster = A.take<int>(nI);
             co.clu_start = A.take<int>((size_t)nc + 1);
             co.A = A.take<double>((size_t)Nc * Nc);
-            co.X32 = A.take<float>((size_t)2 * coarse_padded_size(Nc) * coarse_padded_size(Nc));
-            co.fail = A.take<int>(1);
+            co.X32 = A.take<float>((size_t)(2 * coarse_padded_size(Nc) + 1) * coarse_padded_size(Nc));
+            co.fail = A.take<int>(2);
             co.Ainv = A.take<float>((size_t)Nc * Nc);
             co.cc = A.take<double>(Nc);
             co.zc = A.take<double>(Nc);
@@ -913,10 +918,13 @@ class Solver {
         { SFMBA_PHASE(PH_COARSE_ASSEMBLE); launch_coarse_assemble(b, s_); }
         SFMBA_PHASE(PH_COARSE_FACTOR);
         launch_coarse_invert(b, s_);
-        int failed = 1;
-        SFMBA_CUDA(cudaMemcpyAsync(&failed, co.fail, sizeof(int), cudaMemcpyDeviceToHost, s_));
+        int st[2] = {1, 0};
+        SFMBA_CUDA(cudaMemcpyAsync(st, co.fail, sizeof(st), cudaMemcpyDeviceToHost, s_));
         SFMBA_CUDA(cudaStreamSynchronize(s_));
-        return failed == 0;
+        profiler().count("coarse_inverses", 1);
+        profiler().count("coarse_inverse_failed", st[0]);
+        profiler().count("coarse_pivots_raised", st[1]);
+        return st[0] == 0;
     }
 
     void read_state() {
@@ -2477,6 +2485,12 @@ int sfmba_profile_report(char *buf, int64_t len) {
             char tmp[160];
             std::snprintf(tmp, sizeof(tmp), "%s\"%s\":%.3f", first ? "" : ",", kv.first.c_str(), kv.second);
             js += tmp;
+            first = false;
+        }
+        js += "},\"counts\":{";
+        first = true;
+        for (const auto &kv : p.counts) {
+            js += (first ? "\"" : ",\"") + kv.first + "\":" + std::to_string(kv.second);
             first = false;
         }
         js += "}";
