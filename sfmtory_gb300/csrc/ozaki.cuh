@@ -16,13 +16,16 @@
 //   G_ij = S_i[R] S_j[C]^T,
 // of which the 28 terms with i + j <= 8 are kept (the others lie below
 // 2^-64 of the scale). Products of one weight d = i + j share an FP32
-// accumulator G_d (exact for d <= 5: at most four products, < 2^24); the
-// groups d >= 4 are folded in FP32, T = G_4 + G_5/2^8 + ... + G_8/2^32
-// (rounding below 2^-56 of the scale), the two leading ones exactly in
-// 32-bit integers, I = 2^8 G_2 + G_3 (< 2^31), and
-//   (P P^T)[r, c] = 2^(e_r + e_c - 24) (I + T / 2^8)
-// is formed and subtracted in FP64: five FP64 operations per entry and
-// panel instead of 64 fused multiply-adds.
+// accumulator G_d (exact for d <= 5: at most four products, < 2^24; the
+// five of d = 6 may round by a unit, 2^-52 of the scale). The groups
+// d <= 6 are combined exactly in 64-bit integers,
+//   L = 2^32 G_2 + 2^24 G_3 + 2^16 G_4 + 2^8 G_5 + G_6   (< 2^55),
+// the last two in FP32, T = G_7 + G_8 / 2^8 (rounding below 2^-80 of the
+// scale), and
+//   (P P^T)[r, c] = 2^(e_r + e_c - 48) (L + T / 2^8)
+// is formed in FP64 (L rounds to 53 bits: the FP64 rounding of the product
+// itself) and subtracted: five FP64 operations per entry and panel instead
+// of 64 fused multiply-adds.
 //
 // The products run as warp-level mma.sync m16n8k16 (BF16 in, FP32
 // accumulate) from shared memory through ldmatrix; a 4-warp block owns a
@@ -134,7 +137,7 @@ __device__ __forceinline__ void oz_tile_update(double *A, size_t lda, int mi, in
     if (!diag) load(sC, slC, mj);
     const __nv_bfloat16 *cs = diag ? sR : sC;
     if (threadIdx.x < kOzTile) {
-        fR[threadIdx.x] = (int)threadIdx.x < mi ? ldexp(1.0, eR[threadIdx.x] - 24) : 0.0;
+        fR[threadIdx.x] = (int)threadIdx.x < mi ? ldexp(1.0, eR[threadIdx.x] - 48) : 0.0;
     } else if (threadIdx.x < 2 * kOzTile) {
         const int c = threadIdx.x - kOzTile;
         fC[c] = c < mj ? ldexp(1.0, eC[c]) : 0.0;
@@ -143,8 +146,8 @@ __device__ __forceinline__ void oz_tile_update(double *A, size_t lda, int mi, in
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wr = warp >> 1, wc = warp & 1;
     float T[2][4][4], acc[2][4][4];
-    int I[2][4][4];
-    for (int d = 8; d >= 2; --d) {  // weight 2^-8d; the smallest first
+    long long I[2][4][4];
+    for (int d = 2; d <= 8; ++d) {  // weight 2^-8d; the largest first
 #pragma unroll
         for (int m = 0; m < 2; ++m)
 #pragma unroll
@@ -160,10 +163,10 @@ __device__ __forceinline__ void oz_tile_update(double *A, size_t lda, int mi, in
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const float g = acc[m][nn][e];
-                    if (d == 8) T[m][nn][e] = g;
-                    else if (d >= 4) T[m][nn][e] = fmaf(T[m][nn][e], 0.00390625f, g);
-                    else if (d == 3) I[m][nn][e] = __float2int_rn(g);
-                    else I[m][nn][e] = __float2int_rn(g) * 256 + I[m][nn][e];
+                    if (d == 2) I[m][nn][e] = (long long)__float2int_rn(g);
+                    else if (d <= 6) I[m][nn][e] = I[m][nn][e] * 256 + (long long)__float2int_rn(g);
+                    else if (d == 7) T[m][nn][e] = g;
+                    else T[m][nn][e] = fmaf(g, 0.00390625f, T[m][nn][e]);
                 }
     }
     const int g = lane >> 2, tg = lane & 3;
