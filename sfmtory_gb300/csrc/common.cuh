@@ -106,6 +106,7 @@ struct LMState {
     double pcg_beta;
     double pcg_tol2;     // stop when |r|^2 <= tol2 |b|^2
     long long pcg_total;  // iterations summed over the whole solve
+    int pcg_breakdowns;   // solves ended by p.q <= 0 or r.z <= 0 (not by the tolerance), whole solve
 };
 
 inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }

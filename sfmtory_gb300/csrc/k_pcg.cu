@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(const T *Minv, const T *p, c
     if (!(a > 0.0) || !isfinite(a)) {  // breakdown: keep the current iterate
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             st->pcg_done = 1;
+            st->pcg_breakdowns += 1;
             st->pcg_alpha = 0.0;
         }
         return;
@@ -219,6 +220,7 @@ __global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const 
         st->pcg_rr = b;
         if (stop) {
             st->pcg_done = 1;
+            if (!(b <= st->pcg_tol2 * st->pcg_bb)) st->pcg_breakdowns += 1;
         } else {
             st->pcg_beta = beta;
             st->pcg_rzbuf[parity ^ 1] = a;

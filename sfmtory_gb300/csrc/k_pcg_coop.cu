@@ -151,6 +151,7 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         if (!(pq > 0.0) || !isfinite(pq)) {  // breakdown (every block sees it): keep the iterate
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 st->pcg_done = 1;
+                st->pcg_breakdowns += 1;
                 st->pcg_alpha = 0.0;
             }
             return;
@@ -274,6 +275,7 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         st->pcg_rr = rr;
         if (stop) {
             st->pcg_done = 1;
+            if (!(rr <= st->pcg_tol2 * st->pcg_bb)) st->pcg_breakdowns += 1;
         } else {
             st->pcg_beta = beta;
             st->pcg_rzbuf[a.parity ^ 1] = rz;

@@ -68,6 +68,7 @@ struct Profiler {
     long long launches[PH_COUNT] = {0};
     std::map<std::string, double> host_ms;  // wall time of host stages (ms)
     std::map<std::string, long long> counts;  // event counts (coarse inverses, their breakdowns)
+    std::vector<std::string> trace;           // one JSON object per LM outer iteration of single solves
     void host(const char *name, double seconds) {
         if (on) host_ms[name] += seconds * 1e3;
     }
@@ -100,6 +101,7 @@ struct Profiler {
         for (int k = 0; k < PH_COUNT; ++k) { ms[k] = 0; launches[k] = 0; }
         host_ms.clear();
         counts.clear();
+        trace.clear();
     }
 };
 
@@ -1416,6 +1418,15 @@ class Solver {
                 }
             }
             bool stop = !accepted;
+            if (profiler().on) {
+                char tmp[320];
+                std::snprintf(tmp, sizeof(tmp),
+                              "{\"outer\":%d,\"accepted\":%d,\"fp32\":%d,\"cost\":%.17g,\"cost_before\":%.17g,"
+                              "\"lambda\":%.6g,\"retries\":%d,\"pcg_total\":%lld,\"pcg_breakdowns\":%d}",
+                              outer, accepted ? 1 : 0, b.mixed, hs.cost, hs.cost_before, hs.lambda, out.retries,
+                              hs.pcg_total, hs.pcg_breakdowns);
+                profiler().trace.push_back(tmp);
+            }
             if (accepted) {
                 out.final_cost = hs.cost;
                 out.valid_obs = hs.valid_obs;
@@ -2493,7 +2504,9 @@ int sfmba_profile_report(char *buf, int64_t len) {
             js += (first ? "\"" : ",\"") + kv.first + "\":" + std::to_string(kv.second);
             first = false;
         }
-        js += "}";
+        js += "},\"lm_trace\":[";
+        for (size_t k = 0; k < p.trace.size(); ++k) js += (k ? "," : "") + p.trace[k];
+        js += "]";
         js += ",\"autotune\":" + tune_report() + "}";
         if (!buf || len <= (int64_t)js.size())
             throw Error(SFMBA_ERR_INVALID_ARGUMENT, "profile buffer too small (need " + std::to_string(js.size() + 1) + ")");

@@ -424,9 +424,16 @@ def profile_report() -> dict:
     """{phase: {"ms": device milliseconds, "launches": count}} since profile_enable."""
     import json
 
-    buf = C.create_string_buffer(1 << 16)
-    _check(load().sfmba_profile_report(buf, len(buf)))
-    return json.loads(buf.value.decode())
+    size = 1 << 16
+    while True:
+        buf = C.create_string_buffer(size)
+        st = load().sfmba_profile_report(buf, len(buf))
+        if st == 0:
+            return json.loads(buf.value.decode())
+        msg = load().sfmba_last_error().decode(errors="replace")
+        if "need" not in msg or size >= 1 << 26:
+            _check(st)
+        size *= 4
 
 
 def version() -> str:
