@@ -322,13 +322,15 @@ __global__ void k_coarse_finish(const double *part, const int *group_chunk_off, 
 // suffices. The matrix is padded to a multiple of kSwTile with an identity
 // block (its inverse is the identity, and it does not couple to A). The
 // whole sweep is FP32: n^3 FP64 operations would take ~0.3 ms at the GPU's
-// FP64 rate, and the inverse is a preconditioner applied in FP32.
+// FP64 rate, and the inverse is a preconditioner applied in FP32. The
+// diagonal is lifted by kCoarseLift relative first.
 //
 // Each block computes the step's P itself (one warp, rows in registers,
 // the scalar sweep with shuffles), from the same data in the same order, so
 // every block gets the same P and takes the same branches. In exact
 // arithmetic every pivot of the lifted matrix is at least the lift,
-// 1e-6 of its diagonal entry (a Schur complement of A + D is at least D);
+// kCoarseLift of its diagonal entry (a Schur complement of A + D is at
+// least D);
 // an FP32 pivot below that (rounding in a nearly singular direction) is
 // raised to it, which sweeps A + E with E >= 0 diagonal: still a symmetric
 // positive-definite preconditioner. A non-finite pivot stops every block at
@@ -336,6 +338,13 @@ __global__ void k_coarse_finish(const double *part, const int *group_chunk_off, 
 // 64 x 64 output tiles.
 constexpr int kSwPiv = 32;
 constexpr int kSwTile = 64;
+// Relative diagonal lift of A_c. It bounds how much the coarse correction
+// amplifies the nearly singular direction (the reconstruction's free
+// scale), where the FP32 PCG vectors carry rounding of ~1e-7 of their
+// norm: with a 1e-6 lift the FP32 path's last LM steps lost up to 10x of
+// their decrease to that noise on the 2000-camera problem, with 1e-5 they
+// follow the FP64 path's steps (the FP64 path is unchanged either way).
+constexpr double kCoarseLift = 1e-5;
 
 // Lane r of the calling warp holds row r of the 32 x 32 block and floor,
 // the smallest admissible value of pivot r; on return it holds row r of
@@ -371,7 +380,7 @@ struct SweepArgs {
     int Nc, Np;       // size, padded size (multiple of kSwTile)
     float *X0, *X1;   // [Np x Np] ping-pong buffers
     float *Ainv;      // [Nc x Nc] result
-    float *dref;      // [Np] the lifted diagonal (pivot floors: 1e-6 of it)
+    float *dref;      // [Np] the lifted diagonal (pivot floors: kCoarseLift of it)
     int *stats;       // [0]: set on a non-finite pivot; [1]: pivots raised to their floor
 };
 
@@ -388,9 +397,9 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
     const int nt = Np / kSwTile, tiles = nt * nt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = tid & 15, ty = tid >> 4;
-    // Start: the padded FP32 copy with the diagonal lifted by 1e-6 relative
-    // (keeps a nearly singular coarse matrix away from breakdown; it is a
-    // preconditioner); an empty row/column gets a unit diagonal.
+    // Start: the padded FP32 copy with the diagonal lifted by kCoarseLift
+    // relative (keeps a nearly singular coarse matrix away from breakdown; it
+    // is a preconditioner); an empty row/column gets a unit diagonal.
     for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
         const int R0 = (t / nt) * kSwTile, C0 = (t % nt) * kSwTile;
         for (int e = tid; e < kSwTile * kSwTile; e += blockDim.x) {
@@ -398,7 +407,7 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
             double v = r == c ? 1.0 : 0.0;
             if (r < Nc && c < Nc) {
                 v = g.A[(size_t)r * Nc + c];
-                if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + 1e-6);
+                if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + kCoarseLift);
             }
             g.X0[(size_t)r * Np + c] = (float)v;
             if (r == c) g.dref[r] = (float)v;
@@ -422,7 +431,7 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
                 a[4 * q + 3] = v.w;
             }
             int raised = 0;
-            const bool ok = sweep32(a, 1e-6f * fabsf(g.dref[k0 + lane]), lane, &raised);
+            const bool ok = sweep32(a, (float)kCoarseLift * fabsf(g.dref[k0 + lane]), lane, &raised);
             if (lane == 0) {
                 sfail = ok ? 0 : 1;
                 if (blockIdx.x == 0 && raised) g.stats[1] += raised;

@@ -163,21 +163,37 @@ __global__ void __launch_bounds__(256) k_chol_panel(double *L, int n, int k0, co
     }
 }
 
+// Tile (ti, tj), tj <= ti, of block q of a trailing update launch. part 0:
+// every lower tile; 1: the first tile column (tj = 0, the next diagonal
+// block's column, updated first for the look-ahead); 2: the others.
+__device__ __forceinline__ void trailing_tile(long long q, int part, int &ti, int &tj) {
+    if (part == 1) {
+        ti = (int)q;
+        tj = 0;
+        return;
+    }
+    int a = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while ((long long)(a + 1) * (a + 2) / 2 <= q) ++a;
+    while ((long long)a * (a + 1) / 2 > q) --a;
+    ti = a;
+    tj = (int)(q - (long long)a * (a + 1) / 2);
+    if (part == 2) {
+        ++ti;
+        ++tj;
+    }
+}
+
 // Trailing update of the lower triangle: A[I,J] -= P_I P_J^T for the 64x64
 // tiles (I >= J) right of the panel. Each thread owns a 4x4 register tile.
-__global__ void __launch_bounds__(256) k_chol_update(double *L, int n, int k0, const LMState *st) {
+__global__ void __launch_bounds__(256) k_chol_update(double *L, int n, int k0, int part, const LMState *st) {
     extern __shared__ double sm[];
     double *Pi = sm;            // NB x LD
     double *Pj = sm + NB * LD;  // NB x LD
     if (st->factor_failed) return;
     const int nb = min(NB, n - k0);
     const int t0 = k0 + nb;
-    // tile index q -> (ti, tj), tj <= ti
-    const long long q = blockIdx.x;
-    int ti = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
-    while ((long long)(ti + 1) * (ti + 2) / 2 <= q) ++ti;
-    while ((long long)ti * (ti + 1) / 2 > q) --ti;
-    const int tj = (int)(q - (long long)ti * (ti + 1) / 2);
+    int ti, tj;
+    trailing_tile(blockIdx.x, part, ti, tj);
     const int ri = t0 + ti * NB, rj = t0 + tj * NB;
     if (ri >= n || rj >= n) return;
     const int mi = min(NB, n - ri), mj = min(NB, n - rj);
@@ -234,17 +250,15 @@ __global__ void __launch_bounds__(256) k_oz_split(const double *L, int n, int k0
 // A[I, J] -= P_I P_J^T for the 64 x 64 lower tiles (I >= J) right of the
 // panel, from the slices of k_oz_split (ozaki.cuh). One 4-warp block per
 // tile; a diagonal tile writes its lower triangle.
-__global__ void __launch_bounds__(128, 1) k_oz_update(double *L, int n, int k0, const __nv_bfloat16 *slices,
-                                                      const int *exps, const LMState *st) {
+__global__ void __launch_bounds__(128, 1) k_oz_update(double *L, int n, int k0, int part,
+                                                      const __nv_bfloat16 *slices, const int *exps,
+                                                      const LMState *st) {
     extern __shared__ __align__(16) unsigned char oz_sm[];
     __shared__ double fR[kOzTile], fC[kOzTile];
     if (st->factor_failed) return;
     const int t0 = k0 + NB;
-    const long long q = blockIdx.x;
-    int ti = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
-    while ((long long)(ti + 1) * (ti + 2) / 2 <= q) ++ti;
-    while ((long long)ti * (ti + 1) / 2 > q) --ti;
-    const int tj = (int)(q - (long long)ti * (ti + 1) / 2);
+    int ti, tj;
+    trailing_tile(blockIdx.x, part, ti, tj);
     const int ri = t0 + ti * kOzTile, rj = t0 + tj * kOzTile;
     if (ri >= n || rj >= n) return;
     oz_tile_update(L + (size_t)ri * n + rj, (size_t)n, min(kOzTile, n - ri), min(kOzTile, n - rj), ti == tj,
@@ -496,26 +510,92 @@ void launch_fold_rhs(const Bufs &b, cudaStream_t s) {
     SFMBA_LAUNCH_CHECK();
 }
 
+namespace {
+
+// Second stream and two events of the look-ahead, per host thread and device.
+struct LookAhead {
+    int device = -1;
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t col_done = nullptr, next_ready = nullptr;
+    ~LookAhead() {
+        if (col_done) cudaEventDestroy(col_done);
+        if (next_ready) cudaEventDestroy(next_ready);
+        if (s2) cudaStreamDestroy(s2);
+    }
+};
+
+LookAhead &look_ahead() {
+    thread_local LookAhead la;
+    int dev = 0;
+    SFMBA_CUDA(cudaGetDevice(&dev));
+    if (la.device != dev) {
+        if (la.s2) {
+            cudaEventDestroy(la.col_done);
+            cudaEventDestroy(la.next_ready);
+            cudaStreamDestroy(la.s2);
+        }
+        la.device = dev;
+        SFMBA_CUDA(cudaStreamCreateWithFlags(&la.s2, cudaStreamNonBlocking));
+        SFMBA_CUDA(cudaEventCreateWithFlags(&la.col_done, cudaEventDisableTiming));
+        SFMBA_CUDA(cudaEventCreateWithFlags(&la.next_ready, cudaEventDisableTiming));
+    }
+    return la;
+}
+
+}  // namespace
+
+// Blocked right-looking Cholesky with a look-ahead of one panel: after the
+// panel of block k, the tile column of block k + 1 is updated first; then
+// the diagonal factor, panel (and slices) of block k + 1 run on a second
+// stream while the rest of block k's trailing update runs on s. The
+// diagonal factor is the serial part (one block, FP64-pipe bound), so it
+// hides behind the bulk update. Tensor-core updates read the panel slices of
+// their own step: two slice buffers alternate by step.
 void launch_cholesky(const Bufs &b, cudaStream_t s) {
     set_smem_limits();
     const int n = b.n;
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        k_chol_diag<<<1, 256, kSmemTwoTiles, s>>>(b.L, n, k0, b.Linv, b.state);
+    if (n == 0) return;
+    const bool oz = b.oz_slices != nullptr;
+    const size_t slice_elems = (size_t)kOzSlices * n * kOzK;
+    auto slices = [&](int k0) { return (__nv_bfloat16 *)b.oz_slices + ((k0 / NB) & 1) * slice_elems; };
+    auto exps = [&](int k0) { return b.oz_exp + ((k0 / NB) & 1) * (size_t)n; };
+    // diagonal factor, panel and (tensor path) slices of block k0, on stream st
+    auto head = [&](int k0, cudaStream_t st) {
+        k_chol_diag<<<1, 256, kSmemTwoTiles, st>>>(b.L, n, k0, b.Linv, b.state);
         SFMBA_LAUNCH_CHECK();
         const int rem = n - k0 - NB;
-        if (rem <= 0) break;
-        k_chol_panel<<<div_up(rem, PANEL_ROWS), 256, kSmemPanel, s>>>(b.L, n, k0, b.Linv, b.state);
+        if (rem <= 0) return;
+        k_chol_panel<<<div_up(rem, PANEL_ROWS), 256, kSmemPanel, st>>>(b.L, n, k0, b.Linv, b.state);
         SFMBA_LAUNCH_CHECK();
-        const long long tiles = div_up(rem, NB);
-        if (b.oz_slices) {  // tensor-core update (ozaki.cuh)
-            k_oz_split<<<div_up(rem, 8), 256, 0, s>>>(b.L, n, k0, (__nv_bfloat16 *)b.oz_slices, b.oz_exp, b.state);
+        if (oz) {
+            k_oz_split<<<div_up(rem, 8), 256, 0, st>>>(b.L, n, k0, slices(k0), exps(k0), b.state);
             SFMBA_LAUNCH_CHECK();
-            k_oz_update<<<(unsigned)(tiles * (tiles + 1) / 2), 128, kOzSmem, s>>>(
-                b.L, n, k0, (const __nv_bfloat16 *)b.oz_slices, b.oz_exp, b.state);
-        } else {
-            k_chol_update<<<(unsigned)(tiles * (tiles + 1) / 2), 256, kSmemTwoTiles, s>>>(b.L, n, k0, b.state);
         }
+    };
+    auto update = [&](int k0, int part, long long blocks, cudaStream_t st) {
+        if (blocks <= 0) return;
+        if (oz)
+            k_oz_update<<<(unsigned)blocks, 128, kOzSmem, st>>>(b.L, n, k0, part, slices(k0), exps(k0), b.state);
+        else
+            k_chol_update<<<(unsigned)blocks, 256, kSmemTwoTiles, st>>>(b.L, n, k0, part, b.state);
         SFMBA_LAUNCH_CHECK();
+    };
+    head(0, s);
+    for (int k0 = 0; k0 + NB < n; k0 += NB) {
+        const long long tiles = div_up(n - k0 - NB, NB);
+        const int k1 = k0 + NB;
+        update(k0, 1, tiles, s);  // tile column of block k1
+        if (tiles == 1) {
+            head(k1, s);
+            continue;
+        }
+        LookAhead &la = look_ahead();
+        SFMBA_CUDA(cudaEventRecord(la.col_done, s));
+        SFMBA_CUDA(cudaStreamWaitEvent(la.s2, la.col_done, 0));
+        head(k1, la.s2);
+        SFMBA_CUDA(cudaEventRecord(la.next_ready, la.s2));
+        update(k0, 2, (tiles - 1) * tiles / 2, s);
+        SFMBA_CUDA(cudaStreamWaitEvent(s, la.next_ready, 0));
     }
 }
 

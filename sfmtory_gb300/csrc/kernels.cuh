@@ -130,7 +130,9 @@ struct Bufs {
     double *L = nullptr;          // [n*n] Cholesky / LU factors
     double *Linv = nullptr;       // [nblocks*64*64] inverses of diagonal blocks
     // Tensor-core trailing updates of the Cholesky (NULL: FP64 fused
-    // multiply-adds): BF16 slices [7][n][64] and exponents [n] of a panel.
+    // multiply-adds): BF16 slices [7][n][64] and exponents [n] of a panel;
+    // two of each (alternating by panel) for the single dense system, one
+    // for the batched windows.
     uint16_t *oz_slices = nullptr;
     int *oz_exp = nullptr;
     int *lu_perm = nullptr;       // [n]

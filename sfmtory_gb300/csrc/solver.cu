@@ -1131,8 +1131,8 @@ class Solver {
                     b.oz_slices = nullptr;
                     b.oz_exp = nullptr;
                     if (mixed && !o->dense_fp64_fma) {  // tensor-core trailing updates (ozaki.cuh)
-                        b.oz_slices = A.take<uint16_t>((size_t)kOzSlices * n * kOzK);
-                        b.oz_exp = A.take<int>(n);
+                        b.oz_slices = A.take<uint16_t>((size_t)2 * kOzSlices * n * kOzK);
+                        b.oz_exp = A.take<int>((size_t)2 * n);
                     }
                 } else {
                     b.pcg_x = A.take<char>((size_t)nID * tsz);
@@ -2558,8 +2558,8 @@ int sfmba_dense_cholesky(int64_t n, const double *A, double *L, int32_t tensor_u
         b.Linv = (double *)dev_alloc((size_t)div_up((int)n, kCholNB) * kCholNB * kCholNB * sizeof(double));
         b.state = (LMState *)dev_alloc(sizeof(LMState));
         if (tensor_update) {
-            b.oz_slices = (uint16_t *)dev_alloc((size_t)kOzSlices * n * kOzK * sizeof(uint16_t));
-            b.oz_exp = (int *)dev_alloc((size_t)n * sizeof(int));
+            b.oz_slices = (uint16_t *)dev_alloc((size_t)2 * kOzSlices * n * kOzK * sizeof(uint16_t));
+            b.oz_exp = (int *)dev_alloc((size_t)2 * n * sizeof(int));
         }
         int failed = 0;
         float ms = 0.0f;
