@@ -65,6 +65,9 @@ def parse_args():
                     help="0: autotuned launch variants of the PCG passes; 1..4: force one (for profiling)")
     ap.add_argument("--windows-scale", type=float, default=1.0,
                     help="point-count scale of the 512-window batch (1.0 = points U[500,20000])")
+    ap.add_argument("--record-traffic", metavar="CSV",
+                    help="read an ncu --csv capture of the point pass (dram__bytes_read.sum, dram__bytes_write.sum) "
+                         "and store its DRAM bytes per launch for --workload/--scale in profiles/ncu_traffic.json")
     return ap.parse_args()
 
 
@@ -371,6 +374,42 @@ def ncu_traffic(phase, workload, scale):
             return None, "kernel sources changed since the capture (%s != %s)" % (current, e.get("sources_sha"))
         return int(e["dram_bytes_per_launch"]), e.get("summary")
     return None, "no capture of this kernel and workload"
+
+
+# Kernel sources of the PCG point pass: a traffic entry is valid while they are unchanged.
+POINT_PASS_SOURCES = ["sfmtory_gb300/csrc/" + f for f in
+                      ("mf_passes.cuh", "matfree.cuh", "camera.cuh", "common.cuh", "kernels.cuh", "k_mf_pcg.cu")]
+
+
+def record_traffic(args):
+    import csv
+
+    rows = list(csv.reader(open(args.record_traffic).read().splitlines()))
+    hdr = next(r for r in rows if "Metric Name" in r)
+    recs = [dict(zip(hdr, r)) for r in rows[rows.index(hdr) + 1:] if len(r) == len(hdr)]
+    launches = {}
+    for r in recs:
+        if "k_mf_points" not in r["Kernel Name"]:
+            continue
+        if r["Metric Name"] in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}.get(r["Metric Unit"], 1)
+            launches.setdefault(r["ID"], 0.0)
+            launches[r["ID"]] += float(r["Metric Value"].replace(",", "")) * scale
+    if not launches:
+        raise SystemExit("no k_mf_points launch with DRAM byte counters in " + args.record_traffic)
+    per_launch = int(sum(launches.values()) / len(launches))
+    data = json.load(open(TRAFFIC_FILE)) if os.path.exists(TRAFFIC_FILE) else {"entries": []}
+    key = ("pcg_points", args.workload, float(args.scale))
+    data["entries"] = [e for e in data["entries"]
+                       if (e.get("phase"), e.get("workload"), float(e.get("scale", -1))) != key]
+    data["entries"].append({
+        "phase": "pcg_points", "workload": args.workload, "scale": args.scale,
+        "dram_bytes_per_launch": per_launch, "launches_captured": len(launches),
+        "sources": POINT_PASS_SOURCES, "sources_sha": sources_sha(POINT_PASS_SOURCES),
+        "summary": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mf_points, per launch"})
+    with open(TRAFFIC_FILE, "w") as fh:
+        json.dump(data, fh, indent=1)
+    print(json.dumps(data["entries"][-1]))
 
 
 def roofline(profile, p, D, t, peaks, recompute=True, workload=None):
@@ -895,7 +934,9 @@ def run_side_only(args):
 
 def main():
     args = parse_args()
-    if args.only:
+    if args.record_traffic:
+        record_traffic(args)
+    elif args.only:
         run_side_only(args)
     elif args.impl == "reference":
         run_reference(args)
