@@ -642,6 +642,12 @@ def windows512(args, with_cpu):
     out["fp32_vs_fp64_cost_rel"] = {"max": float(rel.max()), "median": float(np.median(rel)),
                                     "within_1e-6": int((rel <= 1e-6).sum())}
     out["speedup_vs_fp64_gpu"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
+    native.profile_enable(True)  # phase breakdown of one more FP32 batch, outside the timing
+    native.bundle_adjust_batched_arrays(wins, precision=abi.PRECISION_MIXED, **kw)
+    prof = native.profile_report()
+    native.profile_enable(False)
+    out["fp32_phase_ms"] = {k: round(v["ms"], 3) for k, v in prof.items() if isinstance(v, dict) and v.get("launches")}
+    out["fp32_host_ms"] = prof.get("host_ms", {})
     if with_cpu:
         import oracle
 
