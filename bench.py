@@ -62,7 +62,7 @@ def parse_args():
     ap.add_argument("--only", choices=["dense_radial500", "windows512", "pnp", "full_solve_opencv47"],
                     help="run only that side measurement and print its JSON object")
     ap.add_argument("--kernel-variant", type=int, default=0,
-                    help="0: autotuned launch variants of the PCG passes; 1..4: force one (for profiling)")
+                    help="0: autotuned launch variants of the PCG passes; 1..6: force one (for profiling)")
     ap.add_argument("--windows-scale", type=float, default=1.0,
                     help="point-count scale of the 512-window batch (1.0 = points U[500,20000])")
     ap.add_argument("--record-traffic", metavar="CSV",

@@ -37,7 +37,9 @@ void launch_mf_points(const Bufs &b, cudaStream_t s, int variant) {
     case 0: mf_points_v<0>(b, s); break;
     case 1: mf_points_v<1>(b, s); break;
     case 2: mf_points_v<2>(b, s); break;
-    default: mf_points_v<3>(b, s); break;
+    case 3: mf_points_v<3>(b, s); break;
+    case 4: mf_points_v<4>(b, s); break;
+    default: mf_points_v<5>(b, s); break;
     }
 }
 
@@ -47,7 +49,9 @@ void launch_mf_images(const Bufs &b, cudaStream_t s, int variant) {
     case 0: mf_images_v<0>(b, s); break;
     case 1: mf_images_v<1>(b, s); break;
     case 2: mf_images_v<2>(b, s); break;
-    default: mf_images_v<3>(b, s); break;
+    case 3: mf_images_v<3>(b, s); break;
+    case 4: mf_images_v<4>(b, s); break;
+    default: mf_images_v<5>(b, s); break;
     }
 }
 

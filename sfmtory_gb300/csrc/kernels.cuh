@@ -318,8 +318,8 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PC
 void launch_mf_precond_fused(const Bufs &b, cudaStream_t s);
 // The two PCG passes in launch variant 0..k{Point,Image}PassVariants-1
 // (same results; chosen by the autotuner).
-constexpr int kPointPassVariants = 4;
-constexpr int kImagePassVariants = 4;
+constexpr int kPointPassVariants = 6;
+constexpr int kImagePassVariants = 6;
 constexpr int kPassVariants = kPointPassVariants;  // the larger of the two
 void launch_mf_points(const Bufs &b, cudaStream_t s, int variant);  // u = C^-1 E^T p
 void launch_mf_images(const Bufs &b, cudaStream_t s, int variant);  // partials of E u

@@ -492,9 +492,9 @@ __device__ __forceinline__ void load_image_vec(const T *__restrict__ v, const T 
 }
 
 template <int V>
-struct PassVariant {
-    static constexpr int kILP = (V & 1) ? 2 : 1;
-    static constexpr int kMinBlocks = (V & 2) ? 4 : 3;
+struct PassVariant {  // 0-3: one or two rounds x 3 or 4 blocks/SM; 4, 5: one round, 5 or 6 blocks/SM
+    static constexpr int kILP = (V < 4 && (V & 1)) ? 2 : 1;
+    static constexpr int kMinBlocks = V < 4 ? ((V & 2) ? 4 : 3) : V + 1;
 };
 
 // PCG point pass: u_p = C_p^-1 sum_o Jx~^T (Jc~_o p_img(o)).

@@ -13,7 +13,7 @@ def test_pass_variants_are_bit_identical():
     p = scenes.radial2000(seed=3, scale=0.05)
     kw = dict(precision=abi.PRECISION_MIXED, solver=abi.SOLVER_PCG, robust_loss=abi.LOSS_NONE, max_iterations=8)
     ref = native.bundle_adjust_arrays(p, kernel_variant=1, **kw)
-    for v in (2, 3, 4, 0):
+    for v in (2, 3, 4, 5, 6, 0):
         r = native.bundle_adjust_arrays(p, kernel_variant=v, **kw)
         assert r.final_cost == ref.final_cost, v
         assert r.iterations_run == ref.iterations_run and r.linear_iterations == ref.linear_iterations
