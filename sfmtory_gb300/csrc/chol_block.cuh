@@ -58,7 +58,7 @@ __device__ __forceinline__ void inv_step_update(double (&a)[4][4], const double 
 
 // A: [64][kBlkLD] shared, lower triangle of the nb x nb block on entry, the
 // factor on exit. X: [64][kBlkLD] shared, L^-1 on exit (zeros above the
-// diagonal and outside nb). buf: [65] shared scratch. Returns false (and
+// diagonal and outside nb). buf: [67] shared scratch. Returns false (and
 // leaves A, X unspecified) if a pivot is not > 0 (0, negative and NaN all
 // fail, as nalgebra's Cholesky::new). Every thread of the block must call it.
 __device__ __forceinline__ bool chol_block_factor_invert(double *A, double *X, int nb, double *buf) {
@@ -76,10 +76,18 @@ __device__ __forceinline__ bool chol_block_factor_invert(double *A, double *X, i
     bool ok = true;
     for (int j = 0; j < nb; ++j) {
         const int pj = j >> 4, rj = j & 15;
-        if (ty == rj && tx == rj) {  // owner of (j, j)
+        if (ty == rj && tx == rj) {  // owner of (j, j): the pivot, its square root and reciprocal
+            double d = 0.0;
 #pragma unroll
             for (int p = 0; p < 4; ++p)
-                if (p == pj) buf[64] = a[p][p];
+                if (p == pj) d = a[p][p];
+            buf[64] = d;
+            if (d > 0.0) {  // once per step (FP64 square roots and divisions are slow on this GPU)
+                const double sd = sqrt(d);
+                buf[65] = sd;
+                buf[66] = 1.0 / sd;
+                X[j] = buf[66];  // kept for the inverse (X is written only at its end)
+            }
         }
         __syncthreads();
         const double d = buf[64];
@@ -87,8 +95,8 @@ __device__ __forceinline__ bool chol_block_factor_invert(double *A, double *X, i
             ok = false;
             break;  // every thread read the same pivot
         }
-        const double sd = sqrt(d), inv = 1.0 / sd;
         if (tx == rj) {  // owners of column j: scale it below the pivot, publish it
+            const double sd = buf[65], inv = buf[66];
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
                 const int i = ty + 16 * p;
@@ -123,8 +131,8 @@ __device__ __forceinline__ bool chol_block_factor_invert(double *A, double *X, i
     // L X = I, right-looking over the rows of X.
     for (int k = 0; k < nb; ++k) {
         const int pk = k >> 4, rk = k & 15;
-        const double inv = 1.0 / A[k * kBlkLD + k];
-        if (ty == rk) {  // owners of row k: scale and publish it
+        if (ty == rk) {  // owners of row k: scale by 1 / L_kk (from the factorisation) and publish it
+            const double inv = X[k];
 #pragma unroll
             for (int p = 0; p < 4; ++p)
                 if (p == pk)

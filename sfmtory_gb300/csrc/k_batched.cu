@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(256) k_wb_chol_diag(double *Lall, const long l
     extern __shared__ double sm[];
     double *A = sm;
     double *X = sm + NB * LD;
-    __shared__ double buf[NB + 1];
+    __shared__ double buf[NB + 3];
     static_assert(LD == kBlkLD, "tile stride of chol_block_factor_invert");
     const int w = blockIdx.x;
     const int n = n_w[w];

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, dou
     extern __shared__ double sm[];
     double *A = sm;            // NB x LD
     double *X = sm + NB * LD;  // NB x LD
-    __shared__ double buf[NB + 1];
+    __shared__ double buf[NB + 3];
     static_assert(LD == kBlkLD, "tile stride of chol_block_factor_invert");
     if (st->factor_failed) return;
     const int nb = min(NB, n - k0);
