@@ -277,12 +277,13 @@ __global__ void __launch_bounds__(256) k_trsv_fwd(const double *L, int n, int k0
     const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
     if (threadIdx.x < nb) bk[threadIdx.x] = b[k0 + threadIdx.x];
     __syncthreads();
-    if (threadIdx.x < nb) {
+    if (threadIdx.x < nb) {  // four interleaved partial sums (FP64 latency)
         const int r = threadIdx.x;
-        double s = 0.0;
-        for (int t = 0; t <= r; ++t) s += inv[r * NB + t] * bk[t];
-        yk[r] = s;
-        if (blockIdx.x == 0) y[k0 + r] = s;
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int t = 0; t <= r; ++t) s[t & 3] += inv[r * NB + t] * bk[t];
+        const double v = (s[0] + s[1]) + (s[2] + s[3]);
+        yk[r] = v;
+        if (blockIdx.x == 0) y[k0 + r] = v;
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -307,19 +308,23 @@ __global__ void __launch_bounds__(256) k_trsv_bwd(const double *L, int n, int k0
     const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
     if (threadIdx.x < nb) yk[threadIdx.x] = y[k0 + threadIdx.x];
     __syncthreads();
-    if (threadIdx.x < nb) {
+    if (threadIdx.x < nb) {  // four interleaved partial sums: FP64 latency, not a 64-long chain
         const int c = threadIdx.x;
-        double s = 0.0;
-        for (int r = c; r < nb; ++r) s += inv[r * NB + c] * yk[r];
-        xk[c] = s;
-        if (blockIdx.x == 0) x[k0 + c] = s;
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int r = c; r < nb; ++r) s[(r - c) & 3] += inv[r * NB + c] * yk[r];
+        const double v = (s[0] + s[1]) + (s[2] + s[3]);
+        xk[c] = v;
+        if (blockIdx.x == 0) x[k0 + c] = v;
     }
     __syncthreads();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= k0) return;
-    double s = 0.0;
-    for (int t = 0; t < nb; ++t) s += L[(size_t)(k0 + t) * n + r] * xk[t];
-    y[r] -= s;
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int t = 0; t < nb; t += 4)
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (t + u < nb) s[u] += L[(size_t)(k0 + t + u) * n + r] * xk[t + u];
+    y[r] -= (s[0] + s[1]) + (s[2] + s[3]);
 }
 
 // res = rhs - S x (one warp per row).
