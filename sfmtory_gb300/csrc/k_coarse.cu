@@ -328,9 +328,9 @@ __global__ void k_coarse_finish(const double *part, const int *group_chunk_off, 
 // Each block computes the step's P itself (one warp, rows in registers,
 // the scalar sweep with shuffles), from the same data in the same order, so
 // every block gets the same P and takes the same branches. In exact
-// arithmetic every pivot of the lifted matrix is at least the lift,
-// kCoarseLift of its diagonal entry (a Schur complement of A + D is at
-// least D);
+// arithmetic every pivot of the lifted, scaled matrix (unit diagonal) is
+// at least the lift, kCoarseLift (a Schur complement of A + D is at least
+// D);
 // an FP32 pivot below that (rounding in a nearly singular direction) is
 // raised to it, which sweeps A + E with E >= 0 diagonal: still a symmetric
 // positive-definite preconditioner. A non-finite pivot stops every block at
@@ -380,7 +380,7 @@ struct SweepArgs {
     int Nc, Np;       // size, padded size (multiple of kSwTile)
     float *X0, *X1;   // [Np x Np] ping-pong buffers
     float *Ainv;      // [Nc x Nc] result
-    float *dref;      // [Np] the lifted diagonal (pivot floors: kCoarseLift of it)
+    double *scl;      // [Np] symmetric scaling 1 / sqrt(lifted diagonal)
     int *stats;       // [0]: set on a non-finite pivot; [1]: pivots raised to their floor
 };
 
@@ -397,9 +397,20 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
     const int nt = Np / kSwTile, tiles = nt * nt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = tid & 15, ty = tid >> 4;
-    // Start: the padded FP32 copy with the diagonal lifted by kCoarseLift
-    // relative (keeps a nearly singular coarse matrix away from breakdown; it
-    // is a preconditioner); an empty row/column gets a unit diagonal.
+    // Start: the diagonal lifted by kCoarseLift relative (keeps a nearly
+    // singular coarse matrix away from breakdown; it is a preconditioner; an
+    // empty row/column gets a unit diagonal), then scaled symmetrically to a
+    // unit diagonal, D^-1/2 A D^-1/2: the columns mix units (rotations,
+    // translations, focal lengths, distortion) over many orders of
+    // magnitude, which an unscaled FP32 elimination does not resolve. The
+    // padded FP32 copy of the scaled matrix is swept; its inverse is scaled
+    // back at the end.
+    for (long long r = blockIdx.x * (long long)blockDim.x + tid; r < Np; r += (long long)gridDim.x * blockDim.x) {
+        double d = r < Nc ? g.A[(size_t)r * Nc + r] : 1.0;
+        d = d == 0.0 ? 1.0 : d * (1.0 + kCoarseLift);
+        g.scl[r] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;  // a diagonal <= 0 is left for the pivot test
+    }
+    grid.sync();
     for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
         const int R0 = (t / nt) * kSwTile, C0 = (t % nt) * kSwTile;
         for (int e = tid; e < kSwTile * kSwTile; e += blockDim.x) {
@@ -408,9 +419,9 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
             if (r < Nc && c < Nc) {
                 v = g.A[(size_t)r * Nc + c];
                 if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + kCoarseLift);
+                v *= g.scl[r] * g.scl[c];
             }
             g.X0[(size_t)r * Np + c] = (float)v;
-            if (r == c) g.dref[r] = (float)v;
         }
     }
     grid.sync();
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
                 a[4 * q + 3] = v.w;
             }
             int raised = 0;
-            const bool ok = sweep32(a, (float)kCoarseLift * fabsf(g.dref[k0 + lane]), lane, &raised);
+            const bool ok = sweep32(a, (float)kCoarseLift, lane, &raised);  // the scaled, lifted diagonal is 1
             if (lane == 0) {
                 sfail = ok ? 0 : 1;
                 if (blockIdx.x == 0 && raised) g.stats[1] += raised;
@@ -507,12 +518,14 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
         }
         grid.sync();
     }
-    // The swept matrix is -A^-1: Ainv = -(X + X^T) / 2 (symmetric to the last bit).
+    // The swept matrix is -(D^-1/2 A D^-1/2)^-1: Ainv = -D^-1/2 (X + X^T) / 2
+    // D^-1/2 (symmetric to the last bit).
     const float *X = (steps & 1) ? g.X1 : g.X0;
     for (long long e = blockIdx.x * (long long)blockDim.x + tid; e < (long long)Nc * Nc;
          e += (long long)gridDim.x * blockDim.x) {
         const int r = (int)(e / Nc), c = (int)(e - (long long)r * Nc);
-        g.Ainv[e] = -0.5f * (X[(size_t)r * Np + c] + X[(size_t)c * Np + r]);
+        const float s = (float)g.scl[r] * (float)g.scl[c];
+        g.Ainv[e] = -0.5f * (X[(size_t)r * Np + c] + X[(size_t)c * Np + r]) * s;
     }
 }
 
@@ -722,7 +735,8 @@ void launch_coarse_invert(const Bufs &b, cudaStream_t s) {
     }
     if (cap < 1) throw Error(SFMBA_ERR_INTERNAL, "the coarse inverse kernel cannot be resident");
     const int nt = Np / kSwTile;
-    SweepArgs g{co.A, Nc, Np, co.X32, co.X32 + (size_t)Np * Np, co.Ainv, co.X32 + (size_t)2 * Np * Np, co.fail};
+    SweepArgs g{co.A, Nc, Np, co.X32, co.X32 + (size_t)Np * Np, co.Ainv,
+                reinterpret_cast<double *>(co.X32 + (size_t)2 * Np * Np), co.fail};
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)std::min(nt * nt, cap));
     cfg.blockDim = dim3(256);

@@ -30,7 +30,7 @@ struct CoarseBufs {
     double *chunk_part = nullptr;     // [nchunks][D*D]
     double *A = nullptr;              // [Nc*Nc] coarse matrix, FP64
     float *X32 = nullptr;             // [2][Np*Np] ping-pong buffers of the block sweep (coarse_padded_size),
-                                      // then [Np] pivot floors
+                                      // then [Np] doubles: the symmetric scaling
     int *fail = nullptr;              // [2]: the sweep met a non-finite pivot; pivots raised to their floor
     float *Ainv = nullptr;            // [Nc*Nc] symmetric FP32 A^-1, applied per iteration
     void *cc = nullptr;               // [Nc] coarse correction, element type of the PCG vectors

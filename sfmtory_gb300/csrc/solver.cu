@@ -773,7 +773,7 @@ class Solver {
             co.img_cluster = A.take<int>(nI);
             co.clu_start = A.take<int>((size_t)nc + 1);
             co.A = A.take<double>((size_t)Nc * Nc);
-            co.X32 = A.take<float>((size_t)(2 * coarse_padded_size(Nc) + 1) * coarse_padded_size(Nc));
+            co.X32 = A.take<float>((size_t)(2 * coarse_padded_size(Nc) + 2) * coarse_padded_size(Nc));
             co.fail = A.take<int>(2);
             co.Ainv = A.take<float>((size_t)Nc * Nc);
             co.cc = A.take<double>(Nc);
