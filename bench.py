@@ -115,6 +115,8 @@ def workload_config(args, p):
             "" if args.pcg_coarse < 0 else " + coarse correction (%d clusters of consecutive images)" % (
                 args.pcg_coarse or 64), args.pcg_tol, args.pcg_max),
         "loss": "squared",
+        "fp32_arm": "FP32+adjoint with the FP64 polish (the loop continues in FP64 if its own stopping rule "
+                    "fires before the target)",
         "max_lm_iterations": args.max_iterations,
         "seed": args.seed,
         "scale": args.scale,
@@ -129,13 +131,14 @@ def _model_name(p):
     return "/".join(MODEL_NAMES[m] for m in ms)
 
 
-def solver_options(args, precision, target_cost=0.0):
+def solver_options(args, precision, target_cost=0.0, polish=0):
     from sfmtory_gb300 import abi
 
     return abi.default_options(
         max_iterations=args.max_iterations, robust_loss=abi.LOSS_NONE, precision=precision,
         solver=abi.SOLVER_PCG, pcg_tolerance=args.pcg_tol, pcg_max_iterations=args.pcg_max,
-        target_cost=target_cost, kernel_variant=args.kernel_variant, pcg_coarse_clusters=args.pcg_coarse)
+        target_cost=target_cost, kernel_variant=args.kernel_variant, pcg_coarse_clusters=args.pcg_coarse,
+        fp64_polish=polish)
 
 
 # ------------------------------------------------------------------ clocks
@@ -797,7 +800,10 @@ def run_ours(args):
                 "time_to_tolerance_s": ms64 / 1e3, "time_to_tolerance_samples_s": [m / 1e3 for m in ms64s],
                 "iterations_to_tolerance": r64t.iterations_run, "pcg_iterations": r64.linear_iterations}
 
-    opts32 = solver_options(args, abi.PRECISION_MIXED, target)
+    # The FP32 arm as a user gets FP64 quality: with the FP64 polish, so that
+    # where the FP32 loop's own stopping rule fires short of the target the
+    # same loop continues in FP64 (that time is inside the timed solve).
+    opts32 = solver_options(args, abi.PRECISION_MIXED, target, polish=1)
     clocks = ClockSampler(local)
     clocks.start()  # started before the warm-up, so its start-up lag is not in the timed region
     for _ in range(max(3, args.warmup)):
@@ -899,6 +905,7 @@ def run_ours(args):
         "lm_iterations_per_s": statistics.mean(iters) / step_s, "pcg_iterations": last.linear_iterations,
         "final_cost": last.final_cost, "initial_cost": last.initial_cost,
         "reached_tolerance": (last.final_cost <= target) if target else None, "rms_px": rms32,
+        "polish_iteration": last.polish_iteration,
         "fp64_gpu": fp64, "speedup_vs_fp64_gpu": (fp64["time_to_tolerance_s"] / step_s) if fp64 else None,
         "fp32_vs_fp64": vs64,
         "roofline": roof, "cpu_baseline": cpu,

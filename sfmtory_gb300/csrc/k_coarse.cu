@@ -375,6 +375,14 @@ __device__ __forceinline__ bool sweep32(float (&a)[kSwPiv], float floor, int lan
     return true;
 }
 
+// Diagonal entry of the swept matrix: lifted by kCoarseLift relative; an
+// empty row/column gets 1, and a negative entry (FP32 assembly noise on a
+// nearly singular column) its magnitude, which keeps the preconditioner
+// positive definite.
+__device__ __forceinline__ double lifted_diagonal(double d) {
+    return d == 0.0 ? 1.0 : fabs(d) * (1.0 + kCoarseLift);
+}
+
 struct SweepArgs {
     const double *A;  // [Nc x Nc] coarse matrix (FP64)
     int Nc, Np;       // size, padded size (multiple of kSwTile)
@@ -406,9 +414,7 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
     // padded FP32 copy of the scaled matrix is swept; its inverse is scaled
     // back at the end.
     for (long long r = blockIdx.x * (long long)blockDim.x + tid; r < Np; r += (long long)gridDim.x * blockDim.x) {
-        double d = r < Nc ? g.A[(size_t)r * Nc + r] : 1.0;
-        d = d == 0.0 ? 1.0 : d * (1.0 + kCoarseLift);
-        g.scl[r] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;  // a diagonal <= 0 is left for the pivot test
+        g.scl[r] = 1.0 / sqrt(lifted_diagonal(r < Nc ? g.A[(size_t)r * Nc + r] : 1.0));
     }
     grid.sync();
     for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
@@ -418,7 +424,7 @@ __global__ void __launch_bounds__(256) k_coarse_sweep(SweepArgs g) {
             double v = r == c ? 1.0 : 0.0;
             if (r < Nc && c < Nc) {
                 v = g.A[(size_t)r * Nc + c];
-                if (r == c) v = v == 0.0 ? 1.0 : v * (1.0 + kCoarseLift);
+                if (r == c) v = lifted_diagonal(v);
                 v *= g.scl[r] * g.scl[c];
             }
             g.X0[(size_t)r * Np + c] = (float)v;

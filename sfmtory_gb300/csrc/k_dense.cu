@@ -540,7 +540,11 @@ LookAhead &look_ahead() {
             cudaStreamDestroy(la.s2);
         }
         la.device = dev;
-        SFMBA_CUDA(cudaStreamCreateWithFlags(&la.s2, cudaStreamNonBlocking));
+        // The highest priority: the next panel's blocks are dispatched as soon
+        // as the trailing update's blocks free an SM, not after all of them.
+        int least = 0, greatest = 0;
+        SFMBA_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SFMBA_CUDA(cudaStreamCreateWithPriority(&la.s2, cudaStreamNonBlocking, greatest));
         SFMBA_CUDA(cudaEventCreateWithFlags(&la.col_done, cudaEventDisableTiming));
         SFMBA_CUDA(cudaEventCreateWithFlags(&la.next_ready, cudaEventDisableTiming));
     }

@@ -11,6 +11,7 @@ namespace sfmba {
 // Coarse correction of the PCG preconditioner (k_coarse.cu).
 constexpr int kMaxCoarseClusters = 128;
 constexpr int kDefaultCoarseClusters = 64;
+constexpr int kMinImagesPerCluster = 4;
 constexpr int kCoarseChunk = 64;  // points per warp in the coarse assembly
 struct CoarseBufs {
     int nc = 0;                       // clusters (0: off)

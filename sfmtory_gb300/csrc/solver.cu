@@ -757,7 +757,12 @@ class Solver {
         co = CoarseBufs{};
         if (requested < 0 || b.nI < 2 || b.n == 0 || b.nP == 0) return;
         int nc = requested == 0 ? kDefaultCoarseClusters : std::min(requested, kMaxCoarseClusters);
-        nc = std::min(nc, b.nI);
+        // At least kMinImagesPerCluster images per cluster: with one image per
+        // cluster the coarse space repeats the block-Jacobi blocks and A_c is
+        // the whole reduced system, whose FP32 inverse an ill-conditioned
+        // problem does not survive; a few small clusters keep the smooth modes.
+        nc = std::min(nc, b.nI / kMinImagesPerCluster);
+        if (nc < 2) return;
         const int D = b.D, Nc = nc * D, nI = b.nI, nP = b.nP;
         std::vector<int> clu_start(nc + 1), img_cluster(nI);
         for (int c = 0; c <= nc; ++c) clu_start[c] = (int)((long long)c * nI / nc);

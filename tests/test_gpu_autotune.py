@@ -27,6 +27,6 @@ def test_autotune_report_lists_choices():
     rep = native.profile_report()["autotune"]
     assert {e["pass"] for e in rep} >= {"points", "images"}
     for e in rep:
-        n = 4
+        n = 6
         assert 0 <= e["variant"] < n and len(e["us"]) == n and min(e["us"]) > 0
         assert e["us"][e["variant"]] == min(e["us"])
