@@ -255,7 +255,7 @@ struct MvOp {
         q2 = R[6] * X.x + R[7] * X.y + R[8] * X.z;
         const float pc0 = q0 + m2.y, pc1 = q1 + m2.z, pc2 = q2 + m2.w;
         const bool ok = pc2 > float(kMinDepth);
-        iz = ok ? 1.0f / pc2 : 0.0f;
+        iz = ok ? __frcp_rn(pc2) : 0.0f;  // the correctly rounded 1 / pc2
         xp = pc0 * iz;
         yp = pc1 * iz;
         f = c03.x;

@@ -12,21 +12,22 @@ namespace sfmba {
 
 namespace {
 
+// Inclusive segmented warp scan (segments start at head lanes). The lane
+// `off` places back is added while it lies in the lane's segment, found once
+// from the ballot of heads (the same additions in the same order as carrying
+// a head flag through the levels).
 template <typename T, int N>
 __device__ __forceinline__ void seg_scan(T (&v)[N], bool head, int lane) {
-    bool h = head;
+    const unsigned heads = __ballot_sync(0xffffffffu, head) | 1u;
+    const int seg_start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
         T a[N];
 #pragma unroll
         for (int n = 0; n < N; ++n) a[n] = shfl_up(v[n], off);
-        const bool hf = __shfl_up_sync(0xffffffffu, h, off);
-        if (lane >= off) {
-            if (!h) {
+        if (lane - off >= seg_start) {
 #pragma unroll
-                for (int n = 0; n < N; ++n) v[n] += a[n];
-            }
-            h = h || hf;
+            for (int n = 0; n < N; ++n) v[n] += a[n];
         }
     }
 }
