@@ -77,6 +77,12 @@ struct VecArgs {
     const float *Ainv;
     double *zc;
     T *cc;
+    // fused coarse phase: every warp holds one image and block b images
+    // [8b, 8b + 8), so a block restricts its own images (zpart: [blocks][3][D]
+    // per-block sums over the <= 3 clusters they touch) and, after one
+    // barrier, applies the coarse correction to them (zc rebuilt per block).
+    int fused;
+    double *zpart;
 };
 
 template <typename T, int D>
@@ -158,6 +164,7 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         }
         const double alpha = st->pcg_rzbuf[a.parity] / pq;
         if (blockIdx.x == 0 && threadIdx.x == 0) st->pcg_alpha = alpha;
+        __shared__ double rs[8][16];  // fused coarse: this block's images' restricted residuals
         for (int i = gw; i < nI; i += nw) {
             const size_t base = (size_t)i * D;
             T rc = T(0);
@@ -180,6 +187,7 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
                     rz = (double)rc * (double)(T)zc;
                     rr = (double)rc * (double)rc;
                 }
+                if (a.fused) rs[threadIdx.x >> 5][lane] = ((a.img_pmask[i] >> lane) & 1) ? (double)rc : 0.0;
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
@@ -191,9 +199,76 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
                 a.part[nI + i] = rr;
             }
         }
+        if (a.fused) {  // per-block sums of the restriction over the clusters of images [8b, 8b + 8)
+            __syncthreads();
+            const int i0 = blockIdx.x * 8, i1 = min(i0 + 8, nI);
+            if (i0 < nI && (int)threadIdx.x < 3 * D) {
+                const int s = threadIdx.x / D, d = threadIdx.x - s * D;
+                const int c = a.img_cluster[i0] + s;
+                double v = 0.0;
+                for (int i = i0; i < i1; ++i)
+                    if (a.img_cluster[i] == c) v += rs[i - i0][d];
+                a.zpart[((size_t)blockIdx.x * 3 + s) * D + d] = v;
+            }
+        }
     }
     grid.sync();
-    if (a.nc > 0) {
+    if (a.nc > 0 && a.fused) {
+        // zc = Z^T r from the per-block sums (every block rebuilds all of it),
+        // cc rows of this block's clusters, z_i += cc[cluster(i)] for its
+        // images, r.z / r.r partials.
+        __shared__ double zcs[kMaxCoarseClusters * 14];
+        __shared__ double ccs[3 * 16];
+        for (int e = threadIdx.x; e < a.Nc; e += blockDim.x) {
+            const int c = e / D, d = e - c * D;
+            const int b0 = a.clu_start[c] / 8, b1 = (a.clu_start[c + 1] - 1) / 8;
+            double v = 0.0;
+            for (int b = b0; b <= b1; ++b)
+                v += a.zpart[((size_t)b * 3 + (c - a.img_cluster[b * 8])) * D + d];
+            zcs[e] = v;
+        }
+        __syncthreads();
+        const int i0 = blockIdx.x * 8, i1 = min(i0 + 8, nI);
+        if (i0 < nI) {
+            const int c0 = a.img_cluster[i0], nrow = (a.img_cluster[i1 - 1] - c0 + 1) * D;
+            const int wl = threadIdx.x >> 5;
+            for (int rl = wl; rl < nrow; rl += blockDim.x >> 5) {
+                const float *ar = a.Ainv + (size_t)(c0 * D + rl) * a.Nc;
+                T s = T(0);
+                for (int j = lane; j < a.Nc; j += 32) s += (T)__ldg(ar + j) * (T)zcs[j];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+                if (lane == 0) ccs[rl] = (double)s;
+            }
+            __syncthreads();
+            const int i = gw;
+            if (i < i1) {
+                const size_t base = (size_t)i * D;
+                double rz = 0.0, rr = 0.0;
+                if (lane < D) {
+                    const double rc = (double)a.r[base + lane];
+                    double zc = (double)a.z[base + lane];
+                    if ((a.img_pmask[i] >> lane) & 1) zc += ccs[(a.img_cluster[i] - c0) * D + lane];
+                    const T zt = (T)zc;
+                    a.z[base + lane] = zt;
+                    if ((a.img_dmask[i] >> lane) & 1) {
+                        rz = rc * (double)zt;
+                        rr = rc * rc;
+                    }
+                }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    rz += __shfl_xor_sync(0xffffffffu, rz, off);
+                    rr += __shfl_xor_sync(0xffffffffu, rr, off);
+                }
+                if (lane == 0) {
+                    a.part[i] = rz;
+                    a.part[nI + i] = rr;
+                }
+            }
+        }
+        grid.sync();
+    } else if (a.nc > 0) {
         // zc = Z^T r (per cluster and column, image order, own columns only)
         for (int c = gw; c < a.nc; c += nw) {
             if (lane < D) {
@@ -353,6 +428,9 @@ void run_coop(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
     if (cap < 1) throw Error(SFMBA_ERR_INTERNAL, "the PCG vector kernel cannot be resident");
     const int want = std::max(std::max(std::max(div_up(b.nI, 8), div_up(a.Nc, 8)), div_up(a.nsh, 8)), 1);
     const int grid = std::min(want, cap);
+    // The fused coarse phase needs image i on warp i (block b: images 8b..8b+7).
+    a.fused = (coarse && (long long)grid * 8 >= b.nI && D <= 16 && b.co.zpart) ? 1 : 0;
+    a.zpart = b.co.zpart;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(256);

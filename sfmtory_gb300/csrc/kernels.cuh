@@ -36,6 +36,7 @@ struct CoarseBufs {
     float *Ainv = nullptr;            // [Nc*Nc] symmetric FP32 A^-1, applied per iteration
     void *cc = nullptr;               // [Nc] coarse correction, element type of the PCG vectors
     double *zc = nullptr;             // [Nc] Z^T r
+    double *zpart = nullptr;          // [ceil(nI/8)][3][D] per-block restriction sums (cooperative CG kernel)
 };
 
 // Free cameras shared by several images, on the PCG solver. The reduced

@@ -783,6 +783,7 @@ class Solver {
             co.Ainv = A.take<float>((size_t)Nc * Nc);
             co.cc = A.take<double>(Nc);
             co.zc = A.take<double>(Nc);
+            co.zpart = A.take<double>((size_t)(div_up(nI, 8) + 1) * 3 * D);
             count = A.take<long long>((size_t)nP + 1);
             off = A.take<long long>((size_t)nP + 1);
             kcount = A.take<long long>((size_t)nP + 1);
