@@ -28,7 +28,8 @@ constexpr int schur_warps() { return sizeof(T) == 4 ? 4 : 2; }
 template <typename T, int D>
 __global__ void __launch_bounds__(32 * schur_warps<T>())
     k_schur_pairs(const T *__restrict__ rec, const int2 *__restrict__ pairs,
-                  const int *__restrict__ group_start, const int2 *__restrict__ group_ij, int ngroups,
+                  const int *__restrict__ group_start, const int2 *__restrict__ group_ij,
+                  const int *__restrict__ group_order, int ngroups,
                   const int *__restrict__ ob_pt, const T *__restrict__ pt_Cinv,
                   const unsigned char *__restrict__ pt_ok, const double *__restrict__ img_H, int nID,
                   double *__restrict__ S_img) {
@@ -37,8 +38,8 @@ __global__ void __launch_bounds__(32 * schur_warps<T>())
     __shared__ T sA[W][32][Tile::LDS];
     __shared__ T sP[W][32][Tile::LDS];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = blockIdx.x * W + wl;
-    if (g >= ngroups) return;
+    if (blockIdx.x * W + wl >= ngroups) return;
+    const int g = group_order[blockIdx.x * W + wl];
     const int2 ij = group_ij[g];
     double out[Tile::RH][Tile::CQ];
     schur_group<T, D>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl], lane,
@@ -487,11 +488,11 @@ void launch_schur_pairs(const Bufs &b, cudaStream_t s) {
         constexpr int D = decltype(dc)::value;
         if (b.mixed)
             k_schur_pairs<float, D><<<div_up(b.ngroups, schur_warps<float>()), 32 * schur_warps<float>(), 0, s>>>(
-                (const float *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
+                (const float *)b.rec, b.pairs, b.group_start, b.group_ij, b.group_order, b.ngroups, b.ob_pt,
                 (const float *)b.pt_Cinv, b.pt_ok, b.img_H, b.nID, b.S_img);
         else
             k_schur_pairs<double, D><<<div_up(b.ngroups, schur_warps<double>()), 32 * schur_warps<double>(), 0, s>>>(
-                (const double *)b.rec, b.pairs, b.group_start, b.group_ij, b.ngroups, b.ob_pt,
+                (const double *)b.rec, b.pairs, b.group_start, b.group_ij, b.group_order, b.ngroups, b.ob_pt,
                 (const double *)b.pt_Cinv, b.pt_ok, b.img_H, b.nID, b.S_img);
     });
     SFMBA_LAUNCH_CHECK();

@@ -91,6 +91,11 @@ __global__ void k_emit_pairs(const int *pt_start, const int *ob_img, int nP, int
     }
 }
 
+__global__ void k_iota(int *v, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = i;
+}
+
 __global__ void k_group_decode(const unsigned *unique_keys, const int *d_ngroups, int nI,
                                int2 *group_ij) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -292,6 +297,19 @@ void build_pairs(Bufs &b, const long long *d_count_scan, unsigned *keys_a, unsig
     SFMBA_CUDA(cub::DeviceScan::ExclusiveSum(temp, tb, counts, b.group_start, ng + 1, s));
     k_group_decode<<<div_up(ng, 256), 256, 0, s>>>(keys_a, d_ngroups, b.nI, b.group_ij);
     SFMBA_LAUNCH_CHECK();
+    // Launch order of the Schur kernels: the groups with the most pairs first
+    // (stable, so equal counts keep their order), so the long groups do not
+    // start last and leave the GPU idle behind them.
+    int *iota = counts + (np + 1);  // the upper half of vals_b
+    k_iota<<<div_up(ng, 256), 256, 0, s>>>(iota, ng);
+    SFMBA_LAUNCH_CHECK();
+    size_t need = 0;
+    SFMBA_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, need, counts, (int *)keys_b, iota, b.group_order, ng,
+                                                         0, 32, s));
+    if (need > temp_bytes) throw Error(SFMBA_ERR_INTERNAL, "group sort temp too small");
+    tb = temp_bytes;
+    SFMBA_CUDA(cub::DeviceRadixSort::SortPairsDescending(temp, tb, counts, (int *)keys_b, iota, b.group_order, ng, 0,
+                                                         32, s));
 }
 
 }  // namespace sfmba

@@ -125,6 +125,7 @@ struct Bufs {
     int2 *pairs = nullptr;        // [npairs] (obs a, obs b), grouped by image pair
     int *group_start = nullptr;   // [ngroups+1]
     int2 *group_ij = nullptr;     // [ngroups]
+    int *group_order = nullptr;   // [ngroups] groups by decreasing pair count: the Schur kernels' launch order
     long long npairs = 0;
     int ngroups = 0;
     double *S_img = nullptr;      // [nID*nID]

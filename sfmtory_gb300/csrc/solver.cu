@@ -1261,6 +1261,7 @@ class Solver {
                 b.pairs = P.take<int2>(b.npairs);
                 b.group_start = P.take<int>(b.npairs + 1);
                 b.group_ij = P.take<int2>(b.npairs);
+                b.group_order = P.take<int>(b.npairs);
                 ka = P.take<unsigned>(b.npairs);
                 kb = P.take<unsigned>(b.npairs);
                 vb = P.take<int2>(b.npairs + 1);
