@@ -906,6 +906,7 @@ def run_ours(args):
         "final_cost": last.final_cost, "initial_cost": last.initial_cost,
         "reached_tolerance": (last.final_cost <= target) if target else None, "rms_px": rms32,
         "polish_iteration": last.polish_iteration,
+        "step_ms": [round(t * 1e3, 3) for t in times],
         "fp64_gpu": fp64, "speedup_vs_fp64_gpu": (fp64["time_to_tolerance_s"] / step_s) if fp64 else None,
         "fp32_vs_fp64": vs64,
         "roofline": roof, "cpu_baseline": cpu,
