@@ -11,6 +11,9 @@
 //     fallback (lib.rs:1081-1094). On the mixed path the trailing updates
 //     run on the BF16 tensor cores by error-free splitting (ozaki.cuh), to
 //     FP64 accuracy; the plain FP64 path keeps FP64 fused multiply-adds.
+#include <cooperative_groups.h>
+
+#include <algorithm>
 #include <type_traits>
 
 #include "chol_block.cuh"
@@ -328,6 +331,70 @@ __global__ void __launch_bounds__(256) k_trsv_bwd(const double *L, int n, int k0
     y[r] -= (s[0] + s[1]) + (s[2] + s[3]);
 }
 
+// Both triangular solves of L L^T x = rhs in one cooperative launch: the
+// forward sweep (L y = rhs, rhs copied to `work` and updated in place) then
+// the backward sweep (L^T x = y, y updated in place), one grid barrier per
+// 64-wide block step instead of a launch. Every block forms the step's
+// diagonal product with Lkk^-1 itself from the same data (so no barrier is
+// spent on publishing it), then updates its share of the remaining rows: one
+// warp per row below in the forward sweep, one thread per row above (reading
+// L down its columns, coalesced) in the backward sweep.
+__global__ void __launch_bounds__(256) k_trsv_coop(const double *L, int n, const double *Linv, double *work,
+                                                    double *y, double *x, const LMState *st) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double vk[NB], bk[NB];
+    if (st->factor_failed) return;  // read-only here: every block takes the same branch
+    const int nblk = (n + NB - 1) / NB;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + tid) >> 5), nw = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int k = 0; k < nblk; ++k) {
+        const int k0 = k * NB, nb = min(NB, n - k0);
+        const double *inv = Linv + (size_t)k * NB * NB;
+        if (tid < nb) bk[tid] = work[k0 + tid];
+        __syncthreads();
+        if (tid < nb) {  // y_k = Lkk^-1 b_k, four interleaved partial sums
+            double s[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int t = 0; t <= tid; ++t) s[t & 3] += inv[tid * NB + t] * bk[t];
+            const double v = (s[0] + s[1]) + (s[2] + s[3]);
+            vk[tid] = v;
+            if (blockIdx.x == 0) y[k0 + tid] = v;
+        }
+        __syncthreads();
+        for (int r = k0 + nb + gw; r < n; r += nw) {
+            double s = 0.0;
+            for (int t = lane; t < nb; t += 32) s += L[(size_t)r * n + k0 + t] * vk[t];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+            if (lane == 0) work[r] -= s;
+        }
+        grid.sync();
+    }
+    for (int k = nblk - 1; k >= 0; --k) {
+        const int k0 = k * NB, nb = min(NB, n - k0);
+        const double *inv = Linv + (size_t)k * NB * NB;
+        if (tid < nb) bk[tid] = y[k0 + tid];
+        __syncthreads();
+        if (tid < nb) {  // x_k = Lkk^-T y_k
+            double s[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int r = tid; r < nb; ++r) s[(r - tid) & 3] += inv[r * NB + tid] * bk[r];
+            const double v = (s[0] + s[1]) + (s[2] + s[3]);
+            vk[tid] = v;
+            if (blockIdx.x == 0) x[k0 + tid] = v;
+        }
+        __syncthreads();
+        for (int r = blockIdx.x * blockDim.x + tid; r < k0; r += gridDim.x * blockDim.x) {
+            double s[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int t = 0; t < nb; t += 4)
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (t + u < nb) s[u] += L[(size_t)(k0 + t + u) * n + r] * vk[t + u];
+            y[r] -= (s[0] + s[1]) + (s[2] + s[3]);
+        }
+        grid.sync();
+    }
+}
+
 // res = rhs - S x (one warp per row).
 __global__ void k_residual(const double *S, int n, const double *x, const double *rhs, double *res,
                            const LMState *st) {
@@ -611,8 +678,34 @@ void launch_cholesky(const Bufs &b, cudaStream_t s) {
 
 void launch_cholesky_solve(const Bufs &b, const double *rhs, double *x, cudaStream_t s) {
     const int n = b.n;
+    if (n == 0) return;
     // forward: work <- rhs (updated in place), y -> work2
     SFMBA_CUDA(cudaMemcpyAsync(b.work, rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    static int cap_dev = -1, cap = 0;  // one block per SM: the diagonal products are formed per block
+    int dev = 0;
+    SFMBA_CUDA(cudaGetDevice(&dev));
+    if (cap_dev != dev) {
+        int per_sm = 0, sms = 0;
+        SFMBA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_coop, 256, 0));
+        SFMBA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cap = per_sm > 0 ? sms : 0;
+        cap_dev = dev;
+    }
+    if (cap > 0) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)std::min(cap, div_up(n, 8)));
+        cfg.blockDim = dim3(256);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        SFMBA_CUDA(cudaLaunchKernelEx(&cfg, k_trsv_coop, (const double *)b.L, n, (const double *)b.Linv, b.work,
+                                      b.work2, x, (const LMState *)b.state));
+        SFMBA_LAUNCH_CHECK();
+        return;
+    }
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int rem = n - k0 - NB;
         const int grid = rem > 0 ? div_up(rem, 8) : 1;
