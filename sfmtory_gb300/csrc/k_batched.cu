@@ -7,6 +7,8 @@
 // the accept / commit rules (crates/sfm-ba/src/lib.rs:914-1221, applied to
 // each window independently as sfm-reconstruction's BaScope::Local calls
 // would, lib.rs:1287-1299 there).
+#include <cooperative_groups.h>
+
 #include <type_traits>
 
 #include "camera.cuh"
@@ -882,6 +884,74 @@ __global__ void k_wb_lu_update(double *Lall, const long long *s_off, const int *
     A[(size_t)r * n + c] -= A[(size_t)r * n + k] * A[(size_t)k * n + c];
 }
 
+// The column loop of the two kernels above in one cooperative launch: per
+// column k, the failed windows' pivots (a block per window, grid-stride),
+// a grid barrier, the rank-1 updates of all their trailing rows (a block per
+// (window, row), grid-stride), a grid barrier: 2 barriers per column
+// instead of 2 launches. Same arithmetic in the same order.
+__global__ void __launch_bounds__(256) k_wb_lu_coop(double *Lall, const long long *s_off, const int *n_w,
+                                                     const int *slot_base, int *perm_all, const int *list, int nf,
+                                                     int max_n) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double bv[256];
+    __shared__ int bi[256];
+    const int tid = threadIdx.x;
+    for (int k = 0; k < max_n; ++k) {
+        for (int f = blockIdx.x; f < nf; f += gridDim.x) {
+            const int w = list[f];
+            const int n = n_w[w];
+            if (k >= n) continue;
+            double *A = Lall + s_off[w];
+            int *perm = perm_all + slot_base[w];
+            double best = -1.0;
+            int besti = k;
+            for (int r = k + tid; r < n; r += blockDim.x) {
+                const double v = fabs(A[(size_t)r * n + k]);
+                if (v > best) { best = v; besti = r; }
+            }
+            bv[tid] = best;
+            bi[tid] = besti;
+            __syncthreads();
+            for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+                if (tid < h) {
+                    const double o = bv[tid + h];
+                    const int oi = bi[tid + h];
+                    if (o > bv[tid] || (o == bv[tid] && oi < bi[tid])) { bv[tid] = o; bi[tid] = oi; }
+                }
+                __syncthreads();
+            }
+            const int piv = bi[0];
+            const double diag = A[(size_t)piv * n + k];
+            if (diag != 0.0) {
+                if (piv != k)
+                    for (int c = tid; c < n; c += blockDim.x) {
+                        const double t = A[(size_t)k * n + c];
+                        A[(size_t)k * n + c] = A[(size_t)piv * n + c];
+                        A[(size_t)piv * n + c] = t;
+                    }
+                __syncthreads();
+                for (int r = k + 1 + tid; r < n; r += blockDim.x) A[(size_t)r * n + k] /= diag;
+            }
+            if (tid == 0) perm[k] = diag != 0.0 ? piv : -1;
+            __syncthreads();  // bv / bi are reused by the next window
+        }
+        grid.sync();
+        const int m = max_n - k - 1;
+        if (m <= 0) break;
+        for (long long q = blockIdx.x; q < (long long)nf * m; q += gridDim.x) {
+            const int f = (int)(q / m), r = k + 1 + (int)(q - (long long)f * m);
+            const int w = list[f];
+            const int n = n_w[w];
+            if (r >= n || perm_all[slot_base[w] + k] < 0) continue;
+            double *A = Lall + s_off[w];
+            const double lrk = A[(size_t)r * n + k];
+            for (int c = k + 1 + tid; c < n; c += blockDim.x) A[(size_t)r * n + c] -= lrk * A[(size_t)k * n + c];
+        }
+        grid.sync();
+    }
+}
+
 __global__ void __launch_bounds__(1024) k_wb_lu_solve(const double *Lall, const long long *s_off, const int *n_w,
                                                        const int *slot_base, const int *perm_all, const int *list,
                                                        const double *rhs, double *x, WinState *ws) {
@@ -1159,7 +1229,31 @@ void launch_wb_lu(const Bufs &b, const WinBufs &w, int n_failed, cudaStream_t s)
     const int nf = n_failed;
     k_wb_lu_copy<<<dim3(64, nf), 256, 0, s>>>(b.S, b.L, w.s_off, w.n_w, w.lu_list);
     SFMBA_LAUNCH_CHECK();
-    for (int k = 0; k < w.max_n; ++k) {
+    static int cap_dev = -1, cap = 0;  // co-resident blocks of the cooperative column loop
+    int dev = 0;
+    SFMBA_CUDA(cudaGetDevice(&dev));
+    if (cap_dev != dev) {
+        int per_sm = 0, sms = 0;
+        SFMBA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wb_lu_coop, 256, 0));
+        SFMBA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cap = per_sm * sms;
+        cap_dev = dev;
+    }
+    if (cap > 0) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)cap);
+        cfg.blockDim = dim3(256);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        SFMBA_CUDA(cudaLaunchKernelEx(&cfg, k_wb_lu_coop, b.L, (const long long *)w.s_off, (const int *)w.n_w,
+                                      (const int *)w.slot_base, b.lu_perm, (const int *)w.lu_list, nf, w.max_n));
+        SFMBA_LAUNCH_CHECK();
+    }
+    for (int k = 0; cap == 0 && k < w.max_n; ++k) {
         k_wb_lu_pivot<<<nf, 256, 0, s>>>(b.L, w.s_off, w.n_w, w.slot_base, b.lu_perm, w.lu_list, k);
         SFMBA_LAUNCH_CHECK();
         const int m = w.max_n - k - 1;
