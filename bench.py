@@ -62,7 +62,7 @@ def parse_args():
     ap.add_argument("--only", choices=["dense_radial500", "windows512", "pnp", "full_solve_opencv47"],
                     help="run only that side measurement and print its JSON object")
     ap.add_argument("--kernel-variant", type=int, default=0,
-                    help="0: autotuned launch variants of the PCG passes; 1..6: force one (for profiling)")
+                    help="0: autotuned launch variants of the PCG passes; 1..10: force one (for profiling)")
     ap.add_argument("--windows-scale", type=float, default=1.0,
                     help="point-count scale of the 512-window batch (1.0 = points U[500,20000])")
     ap.add_argument("--record-traffic", metavar="CSV",
@@ -626,7 +626,12 @@ def windows512(args, with_cpu):
 
     wins = scenes.windows512(seed=args.seed, scale=args.windows_scale)
     kw = dict(robust_loss=abi.LOSS_HUBER, loss_scale_px=2.0, max_iterations=args.max_iterations)
-    native.bundle_adjust_batched_arrays(wins[:16], precision=abi.PRECISION_MIXED, **kw)
+    if args.kernel_variant > 0:
+        kw["kernel_variant"] = args.kernel_variant
+    # warm-up: one full batch per precision (the launch-shape autotuner times
+    # its candidates at the first batch of this size in the process)
+    native.bundle_adjust_batched_arrays(wins, precision=abi.PRECISION_MIXED, **kw)
+    native.bundle_adjust_batched_arrays(wins, precision=abi.PRECISION_FP64, **kw)
     out = {"workload": f"windows512: {len(wins)} windows, {sum(w.num_images for w in wins)} cameras, "
                        f"{sum(w.num_points for w in wins)} points, {sum(w.num_observations for w in wins)} "
                        f"observations, max reduced dim {max(w.reduced_dim() for w in wins)}, Huber 2 px"}
@@ -651,6 +656,7 @@ def windows512(args, with_cpu):
     native.profile_enable(False)
     out["fp32_phase_ms"] = {k: round(v["ms"], 3) for k, v in prof.items() if isinstance(v, dict) and v.get("launches")}
     out["fp32_host_ms"] = prof.get("host_ms", {})
+    out["autotune_us"] = [e for e in prof.get("autotune", []) if e["pass"].startswith("wb_")]
     if with_cpu:
         import oracle
 
@@ -825,12 +831,17 @@ def run_ours(args):
     obs_per_step = nO * statistics.mean(iters)
     value, step_s = job_throughput(obs_per_step, times, world)
     last = results[-1]
-    # Phase breakdown, roofline and launch count from one more solve with
-    # the per-phase CUDA-event profiler on (outside the timed steps).
+    # Phase breakdown and roofline from one more solve with the per-phase
+    # CUDA-event profiler on (outside the timed steps; it polls PCG
+    # convergence after every iteration, so each timed pass launch does one
+    # iteration's work), then the kernel launches of one solve run as the
+    # timed steps run it (CUDA graphs, polls every 8 PCG iterations).
     native.profile_enable(True)
     solve_device(L, dp, opts32, stream)
     prof = native.profile_report()
-    native.profile_enable(False)
+    native.profile_enable(False)  # also clears the launch count
+    solve_device(L, dp, opts32, stream)
+    launches_per_step = int(native.profile_report().get("kernel_launches", 0))
 
     # End to end through the host API (pinned buffers).
     pp = pinned_problem(p)
@@ -912,11 +923,13 @@ def run_ours(args):
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "seconds_per_step": statistics.mean(e2e_times)},
-        "gpu_launches": int(prof.get("kernel_launches", 0)),
+        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches_per_step": launches_per_step,
         "clocks": clk,
         "phase_ms_profiled_step": {k: round(v["ms"], 3) for k, v in prof.items()
                                    if isinstance(v, dict) and v.get("launches")},
         "counts_profiled_step": prof.get("counts", {}),
+        "autotune_us": prof.get("autotune"),
     }
     if not args.skip_side and world == 1:
         line["dense_radial500"] = dense_radial500(args, L, device, stream)

@@ -111,7 +111,7 @@ typedef struct sfmba_options {
                                      the FP32 path already forms its gradient from
                                      FP64 residuals and stops where FP64 does) */
     int32_t kernel_variant;       /* 0: launch variants of the PCG observation passes
-                                     picked by the autotuner; 1..6: force one (all
+                                     picked by the autotuner; 1..10: force one (all
                                      variants give the same results) */
     int32_t pcg_coarse_clusters;  /* PCG solver: clusters of consecutive images in the
                                      coarse correction of the preconditioner (0: 64,

@@ -136,13 +136,26 @@ __global__ void k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_n
     pt_ok[p] = 1;
 }
 
-template <typename T>
-constexpr int schur_warps() { return sizeof(T) == 4 ? 4 : 2; }
+// Launch shapes of the batched Schur reduction, picked by the autotuner in
+// solver.cu: warps per block and the minimum resident blocks per SM (the
+// register budget of the 7 x 4 FP32 / FP64 tile sums plus their Kahan
+// terms). Every shape runs one warp per image pair with the same
+// arithmetic, so the sums and results are the same.
+template <typename T, int V>
+struct WbSchurShape {
+    static constexpr bool kF = sizeof(T) == 4;
+    static constexpr int kW = kF ? ((V == 3 || V == 4) ? 2 : 4) : 2;
+    static constexpr int kMinBlocks = kF ? (V == 0 ? 1 : V == 1 ? 5 : V == 2 ? 6 : V == 3 ? 10 : V == 4 ? 12 :
+                                            V == 5 ? 8 : V == 6 ? 1 : V == 7 ? 6 : V == 8 ? 1 : 8)
+                                         : (V == 0 ? 1 : V == 1 ? 4 : V == 2 ? 6 : V == 3 ? 8 : V == 4 ? 10 :
+                                            V == 5 ? 12 : V == 6 ? 1 : V == 7 ? 6 : V == 8 ? 1 : 8);
+    static constexpr int kSG = V < 6 ? 4 : V < 8 ? 2 : 1;  // subgroups of the tile (schur.cuh)
+};
 
 // Schur reduction of the image pairs of every retrying window (one warp per
 // pair, schur.cuh), written into the window's image-level block matrix.
-template <typename T, int D>
-__global__ void __launch_bounds__(32 * schur_warps<T>())
+template <typename T, int D, int V>
+__global__ void __launch_bounds__(32 * WbSchurShape<T, V>::kW, WbSchurShape<T, V>::kMinBlocks)
     k_wb_schur_pairs(const T *__restrict__ rec, const int2 *__restrict__ pairs, const int *__restrict__ group_start,
                      const int2 *__restrict__ group_ij, const int *__restrict__ group_order, int ngroups,
                      const int *__restrict__ ob_pt,
@@ -151,8 +164,9 @@ __global__ void __launch_bounds__(32 * schur_warps<T>())
                      const int *__restrict__ img_base, const int *__restrict__ nid_w,
                      const long long *__restrict__ simg_off, const WinState *__restrict__ ws,
                      double *__restrict__ S_img) {
-    constexpr int W = schur_warps<T>();
-    using Tile = SchurTile<T, D>;
+    constexpr int W = WbSchurShape<T, V>::kW;
+    constexpr int SG = WbSchurShape<T, V>::kSG;
+    using Tile = SchurTile<T, D, SG>;
     __shared__ T sA[W][32][Tile::LDS];
     __shared__ T sP[W][32][Tile::LDS];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -162,9 +176,9 @@ __global__ void __launch_bounds__(32 * schur_warps<T>())
     const int w = img_win[ij.x];
     if (!ws[w].active) return;
     double out[Tile::RH][Tile::CQ];
-    schur_group<T, D>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl], lane,
-                      out);
-    if (lane >= 8) return;
+    schur_group<T, D, SG>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl],
+                          lane, out);
+    if (lane >= Tile::LS) return;
     const int li = ij.x - img_base[w], lj = ij.y - img_base[w];
     const int nid = nid_w[w];
     double *Sw = S_img + simg_off[w];
@@ -1082,20 +1096,37 @@ void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s) {
     SFMBA_LAUNCH_CHECK();
 }
 
-void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s) {
-    if (b.ngroups == 0) return;
+template <typename T, int V>
+void wb_schur_v(const Bufs &b, const WinBufs &w, cudaStream_t s) {
+    constexpr int W = WbSchurShape<T, V>::kW;
     dispatch_D(b.D, [&](auto dc) {
         constexpr int D = decltype(dc)::value;
-        if (b.mixed)
-            k_wb_schur_pairs<float, D><<<div_up(b.ngroups, schur_warps<float>()), 32 * schur_warps<float>(), 0, s>>>(
-                (const float *)b.rec, b.pairs, b.group_start, b.group_ij, b.group_order, b.ngroups, b.ob_pt, (const float *)b.pt_Cinv,
-                b.pt_ok, b.img_H, w.img_win, w.img_base, w.nid_w, w.simg_off, w.ws, b.S_img);
-        else
-            k_wb_schur_pairs<double, D><<<div_up(b.ngroups, schur_warps<double>()), 32 * schur_warps<double>(), 0, s>>>(
-                (const double *)b.rec, b.pairs, b.group_start, b.group_ij, b.group_order, b.ngroups, b.ob_pt,
-                (const double *)b.pt_Cinv, b.pt_ok, b.img_H, w.img_win, w.img_base, w.nid_w, w.simg_off, w.ws,
-                b.S_img);
+        k_wb_schur_pairs<T, D, V><<<div_up(b.ngroups, W), 32 * W, 0, s>>>(
+            (const T *)b.rec, b.pairs, b.group_start, b.group_ij, b.group_order, b.ngroups, b.ob_pt,
+            (const T *)b.pt_Cinv, b.pt_ok, b.img_H, w.img_win, w.img_base, w.nid_w, w.simg_off, w.ws, b.S_img);
     });
+}
+
+template <typename T>
+void wb_schur_t(const Bufs &b, const WinBufs &w, cudaStream_t s, int variant) {
+    switch (variant) {
+    case 0: wb_schur_v<T, 0>(b, w, s); break;
+    case 1: wb_schur_v<T, 1>(b, w, s); break;
+    case 2: wb_schur_v<T, 2>(b, w, s); break;
+    case 3: wb_schur_v<T, 3>(b, w, s); break;
+    case 4: wb_schur_v<T, 4>(b, w, s); break;
+    case 5: wb_schur_v<T, 5>(b, w, s); break;
+    case 6: wb_schur_v<T, 6>(b, w, s); break;
+    case 7: wb_schur_v<T, 7>(b, w, s); break;
+    case 8: wb_schur_v<T, 8>(b, w, s); break;
+    default: wb_schur_v<T, 9>(b, w, s); break;
+    }
+}
+
+void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s, int variant) {
+    if (b.ngroups == 0) return;
+    if (b.mixed) wb_schur_t<float>(b, w, s, variant);
+    else wb_schur_t<double>(b, w, s, variant);
     SFMBA_LAUNCH_CHECK();
 }
 

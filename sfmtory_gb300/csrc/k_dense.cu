@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(32 * schur_warps<T>())
     double out[Tile::RH][Tile::CQ];
     schur_group<T, D>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl], lane,
                       out);
-    if (lane >= 8) return;
+    if (lane >= Tile::LS) return;
     const int i = ij.x, j = ij.y;
     const int r0 = (lane >> 2) * Tile::RH, c0 = (lane & 3) * Tile::CQ;
 #pragma unroll

@@ -53,12 +53,19 @@ __global__ void k_prepare_images(const double *poses, const double *cams, const 
     im.active = img_active[i];
     im.pad[0] = im.pad[1] = 0;
     out[i] = im;
-    if (mv) {  // the same FP32 values in planes (MvOp)
+    if (mv) {  // the same FP32 values in planes (MvOp): R, t, then the model's scalars {f, fy, k1, k2} and {cx, cy}
         mv[i] = make_float4((float)im.R[0], (float)im.R[1], (float)im.R[2], (float)im.R[3]);
         mv[nI + i] = make_float4((float)im.R[4], (float)im.R[5], (float)im.R[6], (float)im.R[7]);
         mv[2 * (size_t)nI + i] = make_float4((float)im.R[8], (float)im.t[0], (float)im.t[1], (float)im.t[2]);
-        mv[3 * (size_t)nI + i] = make_float4((float)im.c[0], (float)im.c[1], (float)im.c[2], (float)im.c[3]);
-        mv[4 * (size_t)nI + i] = make_float4((float)im.c[4], (float)im.c[5], (float)im.c[6], (float)im.c[7]);
+        // PINHOLE: fx, fy, cx, cy; SIMPLE_PINHOLE / SIMPLE_RADIAL / RADIAL: f, cx, cy, k1, k2
+        // (the operator serves only these four models)
+        const bool pin = im.model == SFMBA_PINHOLE;
+        const float f = (float)im.c[0], fy = (float)(pin ? im.c[1] : im.c[0]);
+        const float cx = (float)(pin ? im.c[2] : im.c[1]), cy = (float)(pin ? im.c[3] : im.c[2]);
+        const float k1 = (im.model == SFMBA_SIMPLE_RADIAL || im.model == SFMBA_RADIAL) ? (float)im.c[3] : 0.f;
+        const float k2 = im.model == SFMBA_RADIAL ? (float)im.c[4] : 0.f;
+        mv[3 * (size_t)nI + i] = make_float4(f, fy, k1, k2);
+        mv[4 * (size_t)nI + i] = make_float4(cx, cy, 0.f, 0.f);
     }
 }
 

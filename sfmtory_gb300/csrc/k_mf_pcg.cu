@@ -39,7 +39,11 @@ void launch_mf_points(const Bufs &b, cudaStream_t s, int variant) {
     case 2: mf_points_v<2>(b, s); break;
     case 3: mf_points_v<3>(b, s); break;
     case 4: mf_points_v<4>(b, s); break;
-    default: mf_points_v<5>(b, s); break;
+    case 5: mf_points_v<5>(b, s); break;
+    case 6: mf_points_v<6>(b, s); break;
+    case 7: mf_points_v<7>(b, s); break;
+    case 8: mf_points_v<8>(b, s); break;
+    default: mf_points_v<9>(b, s); break;
     }
 }
 
@@ -51,7 +55,11 @@ void launch_mf_images(const Bufs &b, cudaStream_t s, int variant) {
     case 2: mf_images_v<2>(b, s); break;
     case 3: mf_images_v<3>(b, s); break;
     case 4: mf_images_v<4>(b, s); break;
-    default: mf_images_v<5>(b, s); break;
+    case 5: mf_images_v<5>(b, s); break;
+    case 6: mf_images_v<6>(b, s); break;
+    case 7: mf_images_v<7>(b, s); break;
+    case 8: mf_images_v<8>(b, s); break;
+    default: mf_images_v<9>(b, s); break;
     }
 }
 

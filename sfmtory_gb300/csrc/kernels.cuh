@@ -156,7 +156,7 @@ struct Bufs {
     void *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
     float *pcg_p4 = nullptr;      // FP32: copy of p in planes (plane_index; pad4(D)/4 planes of [nI] float4), point pass
     float4 *img_mv = nullptr;     // FP32 PCG: per-image constants of MvOp in 5 planes of [nI] float4:
-                                  //   (R0 R1 R2 R3) (R4 R5 R6 R7) (R8 t0 t1 t2) (c0 c1 c2 c3) (c4 c5 c6 c7)
+                                  //   (R0 R1 R2 R3) (R4 R5 R6 R7) (R8 t0 t1 t2) (f fy k1 k2) (cx cy 0 0)
     CoarseBufs co;                // coarse correction of the preconditioner
     void *pcg_u = nullptr;        // [nP*4] per-point Cinv E^T p
     void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
@@ -321,9 +321,9 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PC
 void launch_mf_precond_fused(const Bufs &b, cudaStream_t s);
 // The two PCG passes in launch variant 0..k{Point,Image}PassVariants-1
 // (same results; chosen by the autotuner).
-constexpr int kPointPassVariants = 6;
-constexpr int kImagePassVariants = 6;
-constexpr int kPassVariants = kPointPassVariants;  // the larger of the two
+constexpr int kPointPassVariants = 10;
+constexpr int kImagePassVariants = 10;
+constexpr int kPassVariants = kPointPassVariants;  // the most variants of any tuned kernel
 void launch_mf_points(const Bufs &b, cudaStream_t s, int variant);  // u = C^-1 E^T p
 void launch_mf_images(const Bufs &b, cudaStream_t s, int variant);  // partials of E u
 void launch_mf_backsub(const Bufs &b, const double *delta_slot, cudaStream_t s);
@@ -468,7 +468,10 @@ void launch_wb_live(const Bufs &b, const WinBufs &w, bool retry, cudaStream_t s)
 void launch_wb_begin_outer(const WinBufs &w, int max_iterations, cudaStream_t s);
 void launch_wb_begin_retry(const WinBufs &w, cudaStream_t s);
 void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s);
-void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s);
+// variant: launch shape (k_batched.cu WbSchurShape), 0 .. kWbSchurVariants - 1; all give the same sums
+constexpr int kWbSchurVariants = 6;
+constexpr int kWbSchurForced = 10;  // shapes reachable by sfmba_options.kernel_variant (6..9: other tilings)
+void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s, int variant = 0);
 void launch_wb_fold(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_cholesky(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_solve(const Bufs &b, const WinBufs &w, const double *rhs, double *x, cudaStream_t s);

@@ -225,8 +225,10 @@ struct ObsOp<T, D, false, M> {
 // exact arithmetic (about half the FP32 instructions); columns that are not
 // unknowns need no mask here because the PCG vectors are zero on them and
 // the image pass's sums for them are discarded by k_pcg_images_finish. The
-// per-image constants come from five planes of float4 (Bufs::img_mv), so
-// neighbouring images share cache lines.
+// per-image constants come from planes of float4 (Bufs::img_mv: R and t in
+// three, the model's scalars {f, fy, k1, k2} in the fourth, {cx, cy} in a
+// fifth read only for a robust loss), so neighbouring images share cache
+// lines.
 template <int M>
 __host__ __device__ constexpr bool mv_model() {
     return M == SFMBA_SIMPLE_PINHOLE || M == SFMBA_PINHOLE || M == SFMBA_SIMPLE_RADIAL || M == SFMBA_RADIAL;
@@ -243,9 +245,7 @@ struct MvOp {
     __device__ __forceinline__ void build(const JacSrc<float> &J, int img, int pt, int4 rc) {
         const float4 *mv = J.mv + img;
         const size_t nI = (size_t)J.nI;
-        const float4 m0 = __ldg(mv), m1 = __ldg(mv + nI), m2 = __ldg(mv + 2 * nI), c03 = __ldg(mv + 3 * nI);
-        float c4 = 0.0f;
-        if constexpr (M == SFMBA_RADIAL) c4 = __ldg(mv + 4 * nI).x;
+        const float4 m0 = __ldg(mv), m1 = __ldg(mv + nI), m2 = __ldg(mv + 2 * nI), ms = __ldg(mv + 3 * nI);
         const float4 X = __ldg(J.points32 + pt);
         R[0] = m0.x; R[1] = m0.y; R[2] = m0.z; R[3] = m0.w;
         R[4] = m1.x; R[5] = m1.y; R[6] = m1.z; R[7] = m1.w;
@@ -255,30 +255,26 @@ struct MvOp {
         q2 = R[6] * X.x + R[7] * X.y + R[8] * X.z;
         const float pc0 = q0 + m2.y, pc1 = q1 + m2.z, pc2 = q2 + m2.w;
         const bool ok = pc2 > float(kMinDepth);
-        iz = ok ? __frcp_rn(pc2) : 0.0f;  // the correctly rounded 1 / pc2
+        iz = ok ? __fdividef(1.0f, pc2) : 0.0f;  // approximate reciprocal (FP32 Jacobian operator)
         xp = pc0 * iz;
         yp = pc1 * iz;
-        f = c03.x;
-        fy = f;
+        f = ms.x;
+        fy = ms.y;
         d = 1.0f;
         dd2 = 0.0f;
         r2 = xp * xp + yp * yp;
-        float cx = c03.y, cy = c03.z;
-        if constexpr (M == SFMBA_PINHOLE) {
-            fy = c03.y;
-            cx = c03.z;
-            cy = c03.w;
-        } else if constexpr (M == SFMBA_SIMPLE_RADIAL) {
-            d = 1.0f + c03.w * r2;
-            dd2 = 2.0f * c03.w;
+        if constexpr (M == SFMBA_SIMPLE_RADIAL) {
+            d = 1.0f + ms.z * r2;
+            dd2 = 2.0f * ms.z;
         } else if constexpr (M == SFMBA_RADIAL) {
-            d = 1.0f + r2 * (c03.w + c4 * r2);
-            dd2 = 2.0f * (c03.w + 2.0f * c4 * r2);
+            d = 1.0f + r2 * (ms.z + ms.w * r2);
+            dd2 = 2.0f * (ms.z + 2.0f * ms.w * r2);
         }
         s = ok ? 1.0f : 0.0f;
         if (ok && J.loss != SFMBA_LOSS_NONE) {  // sqrt of the robust weight of the FP32 residual
-            const float r0 = f * xp * d + cx - __int_as_float(rc.z);
-            const float r1 = fy * yp * d + cy - __int_as_float(rc.w);
+            const float4 cc = __ldg(mv + 4 * nI);  // cx, cy
+            const float r0 = f * xp * d + cc.x - __int_as_float(rc.z);
+            const float r1 = fy * yp * d + cc.y - __int_as_float(rc.w);
             s = sqrtf(robust_weight<float>(sqrtf(r0 * r0 + r1 * r1), J.loss, J.scale));
         }
     }

@@ -15,13 +15,15 @@ namespace {
 // Inclusive segmented warp scan (segments start at head lanes). The lane
 // `off` places back is added while it lies in the lane's segment, found once
 // from the ballot of heads (the same additions in the same order as carrying
-// a head flag through the levels).
+// a head flag through the levels). Levels whose offset exceeds every lane's
+// distance to its segment start add nothing and are skipped (short tracks:
+// rounds of 32 observations rarely hold a segment longer than 8 or 16).
 template <typename T, int N>
 __device__ __forceinline__ void seg_scan(T (&v)[N], bool head, int lane) {
     const unsigned heads = __ballot_sync(0xffffffffu, head) | 1u;
     const int seg_start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
+    const int reach = (int)__reduce_max_sync(0xffffffffu, (unsigned)(lane - seg_start));
+    for (int off = 1; off <= reach; off <<= 1) {
         T a[N];
 #pragma unroll
         for (int n = 0; n < N; ++n) a[n] = shfl_up(v[n], off);
@@ -37,16 +39,21 @@ __device__ __forceinline__ void seg_scan(T (&v)[N], bool head, int lane) {
 // consume(pt, v) runs on the lane holding a point's complete sum. With
 // ILP = 2 two rounds of 32 observations are taken per step and both rounds'
 // contributions are computed before either round's segmented scan, so their
-// independent loads and arithmetic overlap; the scans (and so the sums) are
-// the same as with ILP = 1.
-template <typename T, int N, int ILP = 2, typename Contrib, typename Consume>
+// independent loads and arithmetic overlap. With PF the records of the next
+// step are loaded while the current step computes (their DRAM latency leaves
+// the dependent chain record -> gathers -> arithmetic). Whether lane 31's
+// point continues past its round is read from the first record of the next
+// round, which is already in registers except for a step's last round
+// without PF. The scans (and so the sums) are the same in every form.
+template <typename T, int N, int ILP = 2, bool PF = false, typename Contrib, typename Consume>
 __device__ __forceinline__ void point_chunk(const int4 *__restrict__ obrec, int cs, int ce, int lane,
                                             Contrib contrib, Consume consume) {
     T carry[N];
 #pragma unroll
     for (int n = 0; n < N; ++n) carry[n] = T(0);
     int carry_pt = -1;
-    auto scan_round = [&](T (&v)[N], int o, bool valid, int pt) {
+    // next31: on lane 31, the point of the observation after this round (-1 past the chunk)
+    auto scan_round = [&](T (&v)[N], bool valid, int pt, int next31) {
         if (valid && lane == 0 && pt == carry_pt) {
 #pragma unroll
             for (int n = 0; n < N; ++n) v[n] += carry[n];
@@ -54,34 +61,55 @@ __device__ __forceinline__ void point_chunk(const int4 *__restrict__ obrec, int 
         const int prev = __shfl_up_sync(0xffffffffu, pt, 1);
         seg_scan<T, N>(v, lane == 0 || pt != prev, lane);
         int next = __shfl_down_sync(0xffffffffu, pt, 1);
-        if (lane == 31) next = (o + 1 < ce) ? __ldg(obrec + o + 1).y : -1;
+        if (lane == 31) next = next31;
         const bool tail = valid && next != pt;
         if (tail) consume(pt, v);
 #pragma unroll
         for (int n = 0; n < N; ++n) carry[n] = __shfl_sync(0xffffffffu, v[n], 31);
         carry_pt = __shfl_sync(0xffffffffu, (valid && !tail) ? pt : -1, 31);
     };
-    for (int base = cs; base < ce; base += 32 * ILP) {
-        int o[ILP];
-        bool va[ILP];
-        int4 rc[ILP];
-        T v[ILP][N];
+    // invalid lanes hold point -1, so "next" past the chunk reads as -1
+    auto load = [&](int base, int4 (&rc)[ILP]) {
 #pragma unroll
         for (int r = 0; r < ILP; ++r) {
-            o[r] = base + 32 * r + lane;
-            va[r] = o[r] < ce;
+            const int o = base + 32 * r + lane;
             rc[r] = make_int4(0, -1, 0, 0);
-            if (va[r]) rc[r] = __ldg(obrec + o[r]);
+            if (o < ce) rc[r] = __ldg(obrec + o);
         }
+    };
+    int4 nx[ILP];
+    if constexpr (PF) load(cs, nx);
+    for (int base = cs; base < ce; base += 32 * ILP) {
+        int4 rc[ILP];
+        if constexpr (PF) {
+#pragma unroll
+            for (int r = 0; r < ILP; ++r) rc[r] = nx[r];
+            load(base + 32 * ILP, nx);
+        } else {
+            load(base, rc);
+        }
+        T v[ILP][N];
 #pragma unroll
         for (int r = 0; r < ILP; ++r) {
 #pragma unroll
             for (int n = 0; n < N; ++n) v[r][n] = T(0);
-            if (va[r]) contrib(o[r], rc[r], v[r]);
+            if (base + 32 * r + lane < ce) contrib(base + 32 * r + lane, rc[r], v[r]);
         }
 #pragma unroll
-        for (int r = 0; r < ILP; ++r)
-            if (base + 32 * r < ce) scan_round(v[r], o[r], va[r], rc[r].y);
+        for (int r = 0; r < ILP; ++r) {
+            if (base + 32 * r >= ce) break;
+            int n31;
+            if (r + 1 < ILP) {
+                n31 = __shfl_sync(0xffffffffu, rc[r + 1 < ILP ? r + 1 : r].y, 0);
+            } else if constexpr (PF) {
+                n31 = __shfl_sync(0xffffffffu, nx[0].y, 0);
+            } else {
+                const int o = base + 32 * r + 31;
+                n31 = (lane == 31 && o + 1 < ce) ? __ldg(obrec + o + 1).y : -1;
+            }
+            const bool valid = base + 32 * r + lane < ce;
+            scan_round(v[r], valid, rc[r].y, n31);
+        }
     }
 }
 
@@ -493,9 +521,12 @@ __device__ __forceinline__ void load_image_vec(const T *__restrict__ v, const T 
 }
 
 template <int V>
-struct PassVariant {  // 0-3: one or two rounds x 3 or 4 blocks/SM; 4, 5: one round, 5 or 6 blocks/SM
-    static constexpr int kILP = (V < 4 && (V & 1)) ? 2 : 1;
-    static constexpr int kMinBlocks = V < 4 ? ((V & 2) ? 4 : 3) : V + 1;
+struct PassVariant {  // 0-3: one or two rounds x 3 or 4 blocks/SM; 4, 5: one round, 5 or 6 blocks/SM;
+                      // 6-9: as 0-3 with the next step's records loaded ahead
+    static constexpr int kBase = V >= 6 ? V - 6 : V;
+    static constexpr int kILP = (kBase < 4 && (kBase & 1)) ? 2 : 1;
+    static constexpr int kMinBlocks = kBase < 4 ? ((kBase & 2) ? 4 : 3) : kBase + 1;
+    static constexpr bool kPF = V >= 6;
 };
 
 // PCG point pass: u_p = C_p^-1 sum_o Jx~^T (Jc~_o p_img(o)).
@@ -508,7 +539,7 @@ __global__ void __launch_bounds__(256, PassVariant<V>::kMinBlocks)
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nchunks) return;
-    point_chunk<T, 3, PassVariant<V>::kILP>(
+    point_chunk<T, 3, PassVariant<V>::kILP, PassVariant<V>::kPF>(
         J.obrec, pchunk[warp], pchunk[warp + 1], lane,
         [&](int o, int4 rc, T (&v)[3]) {
             T pv[D];
@@ -534,8 +565,12 @@ __global__ void __launch_bounds__(256, PassVariant<V>::kMinBlocks)
                 u1 = Ci[1] * v[0] + Ci[3] * v[1] + Ci[4] * v[2];
                 u2 = Ci[2] * v[0] + Ci[4] * v[1] + Ci[5] * v[2];
             }
-            T *uo = u + 4 * (size_t)pt;
-            uo[0] = u0; uo[1] = u1; uo[2] = u2;
+            if constexpr (std::is_same<T, float>::value) {
+                reinterpret_cast<float4 *>(u)[pt] = make_float4(u0, u1, u2, 0.0f);
+            } else {
+                T *uo = u + 4 * (size_t)pt;
+                uo[0] = u0; uo[1] = u1; uo[2] = u2;
+            }
         });
 }
 
@@ -611,23 +646,32 @@ __global__ void __launch_bounds__(256, PassVariant<V>::kMinBlocks)
         }
     };
     // ILP rounds of 32 observations per step, all computed before any is
-    // accumulated (independent work overlaps; the sums are the same).
-    for (long long base = cs; base < ce; base += 32 * ILP) {
-        long long k[ILP];
-        bool va[ILP];
-        int4 rc[ILP];
-        T cv[ILP][D];
+    // accumulated (independent work overlaps; the sums are the same); with
+    // PF the next step's records are loaded while this step computes.
+    auto load = [&](long long base, int4 (&rc)[ILP]) {
 #pragma unroll
         for (int r = 0; r < ILP; ++r) {
-            k[r] = base + 32 * r + lane;
-            va[r] = k[r] < ce;
+            const long long k = base + 32 * r + lane;
             rc[r] = make_int4(0x7fffffff, 0, 0, 0);
-            if (va[r]) rc[r] = __ldg(J.isrec + k[r]);
+            if (k < ce) rc[r] = __ldg(J.isrec + k);
         }
+    };
+    int4 nx[ILP];
+    if constexpr (PassVariant<V>::kPF) load(cs, nx);
+    for (long long base = cs; base < ce; base += 32 * ILP) {
+        int4 rc[ILP];
+        if constexpr (PassVariant<V>::kPF) {
 #pragma unroll
-        for (int r = 0; r < ILP; ++r) contrib(k[r], va[r], rc[r], cv[r]);
+            for (int r = 0; r < ILP; ++r) rc[r] = nx[r];
+            load(base + 32 * ILP, nx);
+        } else {
+            load(base, rc);
+        }
+        T cv[ILP][D];
 #pragma unroll
-        for (int r = 0; r < ILP; ++r) accumulate(va[r], rc[r].x, cv[r]);
+        for (int r = 0; r < ILP; ++r) contrib(base + 32 * r + lane, base + 32 * r + lane < ce, rc[r], cv[r]);
+#pragma unroll
+        for (int r = 0; r < ILP; ++r) accumulate(base + 32 * r + lane < ce, rc[r].x, cv[r]);
     }
     flush(cur);
 }

@@ -7,11 +7,14 @@
 //
 // Per round of 32 pairs, lane t stages pair t: A_t = Jc~_a (2xD) and
 // P_t = M_ab Jc~_b (2xD). S_ij -= sum_t sum_rho A_t[rho]^T P_t[rho] is then a
-// D x D product with inner dimension 2 x 32, register-tiled: the warp is
-// four subgroups of 8 lanes, subgroup g takes pairs t = g (mod 4), and each
-// of its lanes owns a ceil(D/2) x ceil(D/4) tile of the output. Each round's
-// partial sums are added into the running sums with Kahan compensation (for
-// FP32), and the four subgroups' sums are combined in FP64 at the end.
+// D x D product with inner dimension 2 x 32, register-tiled: the warp is SG
+// subgroups of 32/SG lanes, subgroup g takes pairs t = g (mod SG), and its
+// lanes form a (8/SG) x 4 grid over the output, each owning a
+// ceil(D SG/8) x ceil(D/4) tile. Each round's partial sums are added into
+// the running sums with Kahan compensation (for FP32), and the subgroups'
+// sums are combined in FP64 at the end. Fewer subgroups mean smaller tiles
+// (fewer registers per lane, more warps resident) for more shared-memory
+// reads per multiply-add.
 #pragma once
 
 #include <type_traits>
@@ -20,11 +23,14 @@
 
 namespace sfmba {
 
-template <typename T, int D>
+template <typename T, int D, int SG = 4>
 struct SchurTile {
-    static constexpr int RH = (D + 1) / 2;  // output rows per lane
-    static constexpr int CQ = (D + 3) / 4;  // output columns per lane
-    static constexpr int LDS = 2 * D + 1;   // staged row length (odd: fewer bank conflicts)
+    static_assert(SG == 1 || SG == 2 || SG == 4, "subgroups of 32, 16 or 8 lanes");
+    static constexpr int LS = 32 / SG;                   // lanes per subgroup
+    static constexpr int GR = LS / 4;                    // rows of the subgroup's lane grid
+    static constexpr int RH = (D + GR - 1) / GR;         // output rows per lane
+    static constexpr int CQ = (D + 3) / 4;               // output columns per lane
+    static constexpr int LDS = 2 * D + 1;                // staged row length (odd: fewer bank conflicts)
 };
 
 template <typename T>
@@ -66,20 +72,22 @@ __device__ __forceinline__ void load_jc_part(const T *__restrict__ r, T jc[2 * D
     }
 }
 
-// Accumulates the Schur term of pairs [gs, ge) and returns, in lanes 0..7,
-// the lane's output tile in FP64: out[a][b] = -sum (rows r0+a, cols c0+b)
-// with r0 = (lane >> 2) * RH, c0 = (lane & 3) * CQ. sA, sP: this warp's
-// staging rows [32][LDS].
-template <typename T, int D>
+// Accumulates the Schur term of pairs [gs, ge) and returns, in lanes
+// 0..LS-1, the lane's output tile in FP64: out[a][b] = -sum (rows r0+a,
+// cols c0+b) with r0 = (lane >> 2) * RH, c0 = (lane & 3) * CQ. sA, sP: this
+// warp's staging rows [32][LDS].
+template <typename T, int D, int SG = 4>
 __device__ __forceinline__ void schur_group(const T *__restrict__ rec, const int2 *__restrict__ pairs, int gs,
                                             int ge, const int *__restrict__ ob_pt, const T *__restrict__ pt_Cinv,
-                                            const unsigned char *__restrict__ pt_ok, T (*sA)[SchurTile<T, D>::LDS],
-                                            T (*sP)[SchurTile<T, D>::LDS], int lane,
-                                            double out[SchurTile<T, D>::RH][SchurTile<T, D>::CQ]) {
+                                            const unsigned char *__restrict__ pt_ok,
+                                            T (*sA)[SchurTile<T, D, SG>::LDS], T (*sP)[SchurTile<T, D, SG>::LDS],
+                                            int lane,
+                                            double out[SchurTile<T, D, SG>::RH][SchurTile<T, D, SG>::CQ]) {
     constexpr int RS = RecLayout<D>::kStride;
-    constexpr int RH = SchurTile<T, D>::RH, CQ = SchurTile<T, D>::CQ;
-    const int sg = lane >> 3, l8 = lane & 7;
-    const int r0 = (l8 >> 2) * RH, c0 = (l8 & 3) * CQ;
+    using Tile = SchurTile<T, D, SG>;
+    constexpr int RH = Tile::RH, CQ = Tile::CQ, LS = Tile::LS;
+    const int sg = lane / LS, ll = lane % LS;
+    const int r0 = (ll >> 2) * RH, c0 = (ll & 3) * CQ;
     T acc[RH][CQ], comp[RH][CQ];
 #pragma unroll
     for (int a = 0; a < RH; ++a)
@@ -134,8 +142,8 @@ __device__ __forceinline__ void schur_group(const T *__restrict__ rec, const int
 #pragma unroll
             for (int b = 0; b < CQ; ++b) part[a][b] = T(0);
 #pragma unroll 2
-        for (int k = 0; k < 8; ++k) {
-            const int t = sg + 4 * k;
+        for (int k = 0; k < 32 / SG; ++k) {
+            const int t = sg + SG * k;
 #pragma unroll
             for (int rho = 0; rho < 2; ++rho) {
                 T av[RH], pv[CQ];
@@ -160,8 +168,8 @@ __device__ __forceinline__ void schur_group(const T *__restrict__ rec, const int
 #pragma unroll
         for (int b = 0; b < CQ; ++b) {
             double v = (double)acc[a][b] - (double)comp[a][b];
-            v += __shfl_xor_sync(0xffffffffu, v, 8);
-            v += __shfl_xor_sync(0xffffffffu, v, 16);
+#pragma unroll
+            for (int off = LS; off < 32; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
             out[a][b] = -v;
         }
 }

@@ -221,12 +221,14 @@ class Arena {
     bool sizing_ = false;
 };
 
-// Autotuner of the PCG passes' launch variants (ILP depth x minimum blocks
-// per SM, k_matfree.cu): per device, pass, block width and problem size
-// (log2 of the observation count) the variant with the shortest mean of
-// three timed launches on a solve's own buffers, measured once at the first
-// FP32 PCG solve and kept for the process. Every variant computes the same
-// sums in the same order, so the choice never changes results.
+// Autotuner of launch variants: the PCG passes (ILP depth, records loaded
+// ahead, minimum blocks per SM; mf_passes.cuh) and the batched windows'
+// Schur reduction (warps per block, minimum blocks per SM; k_batched.cu).
+// Per device, kernel, block width and problem size (log2 of the
+// observation count) the variant with the shortest mean of three timed
+// launches on a solve's own buffers, measured once at the first use and
+// kept for the process. Every variant computes the same sums in the same
+// order, so the choice never changes results.
 struct TuneEntry {
     int variant = 0;
     int count = 0;  // variants timed
@@ -277,7 +279,11 @@ std::string tune_report() {
         char tmp[256];
         const TuneEntry &e = kv.second;
         std::snprintf(tmp, sizeof(tmp), "%s{\"device\":%d,\"pass\":\"%s\",\"D\":%d,\"log2_obs\":%d,\"variant\":%d,\"us\":[",
-                      first ? "" : ",", std::get<0>(kv.first), std::get<1>(kv.first) == 0 ? "points" : "images",
+                      first ? "" : ",", std::get<0>(kv.first),
+                      std::get<1>(kv.first) == 0   ? "points"
+                      : std::get<1>(kv.first) == 1 ? "images"
+                      : std::get<1>(kv.first) == 2 ? "wb_schur"
+                                                   : "wb_schur_fp64",
                       std::get<2>(kv.first), std::get<3>(kv.first), e.variant);
         js += tmp;
         for (int v = 0; v < e.count; ++v) {
@@ -1391,14 +1397,17 @@ class Solver {
                         vi = tuned_variant(ctx_.device, 1, kImagePassVariants, b, s_,
                                            [&](int v) { launch_mf_images(b, s_, v); });
                     }
-                    for (int it = 0; it < maxit; it += kPcgPollEvery) {
-                        const int m = std::min(kPcgPollEvery, maxit - it);
-                        // it is a multiple of kPcgPollEvery (even): iteration it + k has parity k & 1
+                    // With the phase profiler on, convergence is polled after every
+                    // iteration, so every profiled pass launch does an iteration's work
+                    // (otherwise up to 7 launches per solve return at once).
+                    const int poll = profiler().on ? 1 : kPcgPollEvery;
+                    for (int it = 0; it < maxit; it += poll) {
+                        const int m = std::min(poll, maxit - it);
                         auto chunk = [&] {
                             for (int k = 0; k < m; ++k) {
                                 { SFMBA_PHASE(PH_PCG_POINTS); launch_mf_points(b, s_, vp); }
                                 { SFMBA_PHASE(PH_PCG_IMAGES); launch_mf_images(b, s_, vi); }
-                                { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_iteration_vector(b, s_, k & 1, coarse); }
+                                { SFMBA_PHASE(PH_PCG_VECTOR); launch_pcg_iteration_vector(b, s_, (it + k) & 1, coarse); }
                             }
                         };
                         pcg_chunk_[coarse ? 1 : 0].run(s_, m == kPcgPollEvery && !profiler().on, chunk);
@@ -1505,12 +1514,24 @@ class Solver {
             { SFMBA_PHASE(PH_IMAGE_REDUCE); launch_image_blocks_records(b, s_); launch_diag_fold(b, s_); }
             for (int inner = 0; inner < kMaxDampingRetries; ++inner) {
                 // One retry round of every window, the same launches each round
-                // (the windows taking part are flagged on the device).
+                // (the windows taking part are flagged on the device). The Schur
+                // reduction's launch shape is tuned at the first round of the
+                // process for this block width and size (run eagerly: the round is
+                // captured as a graph only from its second use).
+                int vs = -1;
                 auto round = [&] {
                     { SFMBA_PHASE(PH_LM); launch_wb_begin_retry(w, s_); launch_wb_live(b, w, true, s_); }
                     { SFMBA_PHASE(PH_POINT_INVERSE); launch_wb_point_inverse(b, w, s_); }
                     { SFMBA_PHASE(PH_IMAGE_RHS); launch_image_rhs(b, s_); launch_fold_rhs(b, s_); }
-                    { SFMBA_PHASE(PH_SCHUR); launch_wb_schur(b, w, s_); }
+                    {
+                        SFMBA_PHASE(PH_SCHUR);
+                        if (vs < 0) {
+                            vs = o->kernel_variant > 0 ? (o->kernel_variant - 1) % kWbSchurForced
+                                                       : tuned_variant(ctx_.device, b.mixed ? 2 : 3, kWbSchurVariants,
+                                                                       b, s_, [&](int v) { launch_wb_schur(b, w, s_, v); });
+                        }
+                        launch_wb_schur(b, w, s_, vs);
+                    }
                     { SFMBA_PHASE(PH_FOLD); launch_wb_fold(b, w, s_); }
                     { SFMBA_PHASE(PH_CHOLESKY); launch_wb_cholesky(b, w, s_); }
                     { SFMBA_PHASE(PH_TRSV); launch_wb_solve(b, w, w.rhs_p, b.work2, s_); }
