@@ -400,6 +400,10 @@ def record_traffic(args):
             launches[r["ID"]] += float(r["Metric Value"].replace(",", "")) * scale
     if not launches:
         raise SystemExit("no k_mf_points launch with DRAM byte counters in " + args.record_traffic)
+    # Launches after a PCG solve has converged return at once (a few KB):
+    # only launches that ran an iteration count.
+    top_bytes = max(launches.values())
+    launches = {k: v for k, v in launches.items() if v >= 0.01 * top_bytes}
     per_launch = int(sum(launches.values()) / len(launches))
     data = json.load(open(TRAFFIC_FILE)) if os.path.exists(TRAFFIC_FILE) else {"entries": []}
     key = ("pcg_points", args.workload, float(args.scale))

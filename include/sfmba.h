@@ -111,8 +111,10 @@ typedef struct sfmba_options {
                                      the FP32 path already forms its gradient from
                                      FP64 residuals and stops where FP64 does) */
     int32_t kernel_variant;       /* 0: launch variants of the PCG observation passes
-                                     picked by the autotuner; 1..10: force one (all
-                                     variants give the same results) */
+                                     and of the batched Schur reduction picked by the
+                                     autotuner; k > 0: force variant k - 1 of each
+                                     (modulo their counts, 10 and 3; all variants of
+                                     a kernel give the same results) */
     int32_t pcg_coarse_clusters;  /* PCG solver: clusters of consecutive images in the
                                      coarse correction of the preconditioner (0: 64,
                                      at most 128; < 0: block-Jacobi alone) */

@@ -138,18 +138,18 @@ __global__ void k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_n
 
 // Launch shapes of the batched Schur reduction, picked by the autotuner in
 // solver.cu: warps per block and the minimum resident blocks per SM (the
-// register budget of the 7 x 4 FP32 / FP64 tile sums plus their Kahan
-// terms). Every shape runs one warp per image pair with the same
-// arithmetic, so the sums and results are the same.
+// register budget of the 7 x 4 tile sums and their Kahan terms). Every shape
+// runs one warp per image pair with the same arithmetic, so the sums and
+// results are the same. Measured on the 512-window batch (Schur phase of a
+// whole FP32 batch): no cap 87 ms (157 registers), 5 blocks/SM 101 ms,
+// 6 blocks/SM 123 ms, 8 blocks/SM 198 ms — the spills cost more than the
+// extra warps gain; smaller tiles over 16 or 32 lanes (more warps, other
+// rounding) took 83-157 ms. FP64: 800-818 ms for every cap (FP64-bound).
 template <typename T, int V>
 struct WbSchurShape {
     static constexpr bool kF = sizeof(T) == 4;
-    static constexpr int kW = kF ? ((V == 3 || V == 4) ? 2 : 4) : 2;
-    static constexpr int kMinBlocks = kF ? (V == 0 ? 1 : V == 1 ? 5 : V == 2 ? 6 : V == 3 ? 10 : V == 4 ? 12 :
-                                            V == 5 ? 8 : V == 6 ? 1 : V == 7 ? 6 : V == 8 ? 1 : 8)
-                                         : (V == 0 ? 1 : V == 1 ? 4 : V == 2 ? 6 : V == 3 ? 8 : V == 4 ? 10 :
-                                            V == 5 ? 12 : V == 6 ? 1 : V == 7 ? 6 : V == 8 ? 1 : 8);
-    static constexpr int kSG = V < 6 ? 4 : V < 8 ? 2 : 1;  // subgroups of the tile (schur.cuh)
+    static constexpr int kW = kF ? (V == 2 ? 2 : 4) : 2;
+    static constexpr int kMinBlocks = kF ? (V == 0 ? 1 : V == 1 ? 5 : 10) : (V == 0 ? 1 : V == 1 ? 6 : 8);
 };
 
 // Schur reduction of the image pairs of every retrying window (one warp per
@@ -165,8 +165,7 @@ __global__ void __launch_bounds__(32 * WbSchurShape<T, V>::kW, WbSchurShape<T, V
                      const long long *__restrict__ simg_off, const WinState *__restrict__ ws,
                      double *__restrict__ S_img) {
     constexpr int W = WbSchurShape<T, V>::kW;
-    constexpr int SG = WbSchurShape<T, V>::kSG;
-    using Tile = SchurTile<T, D, SG>;
+    using Tile = SchurTile<T, D>;
     __shared__ T sA[W][32][Tile::LDS];
     __shared__ T sP[W][32][Tile::LDS];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -176,8 +175,8 @@ __global__ void __launch_bounds__(32 * WbSchurShape<T, V>::kW, WbSchurShape<T, V
     const int w = img_win[ij.x];
     if (!ws[w].active) return;
     double out[Tile::RH][Tile::CQ];
-    schur_group<T, D, SG>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl],
-                          lane, out);
+    schur_group<T, D>(rec, pairs, group_start[g], group_start[g + 1], ob_pt, pt_Cinv, pt_ok, sA[wl], sP[wl], lane,
+                      out);
     if (lane >= Tile::LS) return;
     const int li = ij.x - img_base[w], lj = ij.y - img_base[w];
     const int nid = nid_w[w];
@@ -1112,14 +1111,7 @@ void wb_schur_t(const Bufs &b, const WinBufs &w, cudaStream_t s, int variant) {
     switch (variant) {
     case 0: wb_schur_v<T, 0>(b, w, s); break;
     case 1: wb_schur_v<T, 1>(b, w, s); break;
-    case 2: wb_schur_v<T, 2>(b, w, s); break;
-    case 3: wb_schur_v<T, 3>(b, w, s); break;
-    case 4: wb_schur_v<T, 4>(b, w, s); break;
-    case 5: wb_schur_v<T, 5>(b, w, s); break;
-    case 6: wb_schur_v<T, 6>(b, w, s); break;
-    case 7: wb_schur_v<T, 7>(b, w, s); break;
-    case 8: wb_schur_v<T, 8>(b, w, s); break;
-    default: wb_schur_v<T, 9>(b, w, s); break;
+    default: wb_schur_v<T, 2>(b, w, s); break;
     }
 }
 

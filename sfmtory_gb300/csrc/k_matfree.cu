@@ -104,7 +104,8 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s) {
         k_mf_precond_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>((const T *)b.ipart2, b.iachunk_off, b.img_H, b.img_b,
                                                        b.img_active, b.img_pmask, b.state, b.nI, b.img_rhs, (T *)b.pcg_Minv,
                                                        (T *)b.pcg_x, (T *)b.pcg_r, (T *)b.pcg_z, (T *)b.pcg_p,
-                                                       (T *)pcg_p4_of<T>(b), b.pcg_part, D * (D + 1) / 2 + D);
+                                                       (T *)pcg_p4_of<T>(b), b.pcg_part, D * (D + 1) / 2 + D,
+                                                       std::is_same<T, float>::value ? b.img_Hf : nullptr);
         SFMBA_LAUNCH_CHECK();
     });
 }
@@ -129,7 +130,7 @@ void launch_mf_precond_fused(const Bufs &b, cudaStream_t s) {
             k_mf_precond_finish<T, D><<<div_up(b.nI, 4), 128, 0, s>>>(
                 (const T *)b.ipart2 + NV, b.iachunk_off, b.img_H, b.img_b, b.img_active, b.img_pmask, b.state, b.nI, b.img_rhs,
                 (T *)b.pcg_Minv, (T *)b.pcg_x, (T *)b.pcg_r, (T *)b.pcg_z, (T *)b.pcg_p, (T *)pcg_p4_of<T>(b),
-                b.pcg_part, 2 * NV);
+                b.pcg_part, 2 * NV, b.img_Hf);
             SFMBA_LAUNCH_CHECK();
         } else {
             throw Error(SFMBA_ERR_INTERNAL, "the fused image pass is FP32 only");

@@ -9,11 +9,11 @@
 // launches each step costs a launch and a drain of the GPU; here one grid of
 // co-resident blocks runs them all with grid-wide barriers between them
 // (cooperative launch: every block is resident, so the barriers cannot
-// wait on a block that never runs). The arithmetic, its order and the
-// results are those of k_pcg_images_finish, k_sh_qreduce, k_pcg_update,
-// k_coarse_restrict / gemv / z and k_pcg_dir; every reduction that decides
-// whether to stop is computed by every block in the same order, so all
-// blocks take the same branch and reach the same barriers.
+// wait on a block that never runs). The dot products are summed per warp
+// over its images, then per block, and after the barrier every block adds
+// the blocks' partials in block order: each reduction that decides whether
+// to stop is computed by every block in the same order, so all blocks take
+// the same branch and reach the same barriers.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -27,30 +27,32 @@ namespace sfmba {
 
 namespace {
 
+// Sum of v over the block's threads in a fixed order: warp butterflies
+// (every lane ends with the same value), then the warps' sums in warp
+// order. Every block that passes the same values gets the same bits.
 __device__ __forceinline__ double block_sum_c(double v, double *sh) {
-    sh[threadIdx.x] = v;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    __syncthreads();  // sh is free: its previous readers are done
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-        __syncthreads();
-    }
-    const double r = sh[0];
-    __syncthreads();
+    double r = 0.0;
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; ++w) r += sh[w];
     return r;
 }
 
-// v[t] + v[t + B] + ... for thread t of a B-thread block, added in that
-// order, loads issued eight at a time (as in k_pcg.cu).
+// v[t] + v[t + B] + ... for thread t of a B-thread block, added in that order.
 __device__ __forceinline__ double strided_sum_c(const double *__restrict__ v, int n) {
     const int B = blockDim.x;
     double a = 0.0;
     int k = threadIdx.x;
-    for (; k + 7 * B < n; k += 8 * B) {
-        double w[8];
+    for (; k + 3 * B < n; k += 4 * B) {
+        double w[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) w[u] = v[k + u * B];
+        for (int u = 0; u < 4; ++u) w[u] = v[k + u * B];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) a += w[u];
+        for (int u = 0; u < 4; ++u) a += w[u];
     }
     for (; k < n; k += B) a += v[k];
     return a;
@@ -60,12 +62,13 @@ template <typename T>
 struct VecArgs {
     const T *ipart;
     const int *ipart_off;
-    const double *img_H;
+    const double *img_H;  // FP64 path: H_i (damped here)
+    const float *img_Hf;  // FP32 path: H_i + lambda diag H_i
     const int *img_active, *img_pmask, *img_dmask;
     const T *Minv;
     T *p, *q, *x, *r, *z;
     float *p4;
-    double *part;
+    double *blk;  // per-block partial sums [4][gridDim.x]: p.q, p.q of shared cameras, r.z, r.r
     LMState *st;
     int nI, nID, parity;
     // shared cameras (nsh = 0: none)
@@ -85,54 +88,82 @@ struct VecArgs {
     double *zpart;
 };
 
+// Writes this block's sum of its warps' values (warp order) to out[blockIdx.x].
+__device__ __forceinline__ void block_partial(double warp_value, double *sh, double *out) {
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = warp_value;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
+        out[blockIdx.x] = r;
+    }
+}
+
 template <typename T, int D>
 __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
     cg::grid_group grid = cg::this_grid();
-    __shared__ double sh[256];
+    __shared__ double sh[32];
     LMState *st = a.st;
     // Read before any block of this launch writes the state (block 0 writes
     // it only after the first grid barrier), so every block sees one value.
     if (st->pcg_done) return;
     const int nI = a.nI;
+    const int G = gridDim.x;
     const int lane = threadIdx.x & 31;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const double lam = st->lambda;
-    // q_i = (H_i + lambda diag H_i) p_i - sum of the image's partials; p.q over pmask.
-    for (int i = gw; i < nI; i += nw) {
-        const int act = a.img_active[i], pm = a.img_pmask[i];
-        const double *H = a.img_H + (size_t)i * D * D;
-        const T *pv = a.p + (size_t)i * D;
-        double pq = 0.0;
-        if (lane < D) {
-            const int c = lane;
-            double sch = 0.0;
-            const int k1 = a.ipart_off[i + 1];
-            int k = a.ipart_off[i];
-            for (; k + 8 <= k1; k += 8) {
-                T w[8];
+    double *PQ = a.blk, *PQS = a.blk + G, *RZ = a.blk + 2 * G, *RR = a.blk + 3 * G;
+    T *zpart = reinterpret_cast<T *>(a.zpart);  // the fused restriction's per-block sums, kernel precision
+    // q_i = (H_i + lambda diag H_i) p_i - sum of the image's partials; p.q over
+    // pmask, summed per warp over its images, then per block.
+    {
+        double pq_w = 0.0;
+        for (int i = gw; i < nI; i += nw) {
+            const int act = a.img_active[i], pm = a.img_pmask[i];
+            const T *pv = a.p + (size_t)i * D;
+            T pq = T(0);
+            if (lane < D) {
+                const int c = lane;
+                T sch = T(0);
+                const int k1 = a.ipart_off[i + 1];
+                int k = a.ipart_off[i];
+                for (; k + 8 <= k1; k += 8) {
+                    T w[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) w[u] = a.ipart[(size_t)(k + u) * D + c];
+                    for (int u = 0; u < 8; ++u) w[u] = a.ipart[(size_t)(k + u) * D + c];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) sch += (double)w[u];
+                    for (int u = 0; u < 8; ++u) sch += w[u];
+                }
+                for (; k < k1; ++k) sch += a.ipart[(size_t)k * D + c];
+                T hp = T(0);
+                if constexpr (std::is_same<T, float>::value) {
+                    const float *H = a.img_Hf + (size_t)i * D * D;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) hp += H[c * D + d] * pv[d];
+                } else {
+                    const double *H = a.img_H + (size_t)i * D * D;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) hp += H[c * D + d] * pv[d];
+                    hp += lam * H[c * D + c] * pv[c];
+                }
+                const T qc = ((act >> c) & 1) ? hp - sch : T(0);
+                a.q[(size_t)i * D + c] = qc;
+                if ((pm >> c) & 1) pq = pv[c] * qc;
             }
-            for (; k < k1; ++k) sch += (double)a.ipart[(size_t)k * D + c];
-            double hp = 0.0;
 #pragma unroll
-            for (int d = 0; d < D; ++d) hp += H[c * D + d] * (double)pv[d];
-            hp += lam * H[c * D + c] * (double)pv[c];
-            const double qc = ((act >> c) & 1) ? hp - sch : 0.0;
-            a.q[(size_t)i * D + c] = (T)qc;
-            if ((pm >> c) & 1) pq = (double)pv[c] * (double)(T)qc;
+            for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
+            pq_w += (double)pq;
         }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
-        if (lane == 0) a.part[2 * nI + i] = pq;
+        block_partial(pq_w, sh, PQ);
     }
+    const bool shared_cams = D > 6 && a.nsh > 0;
     grid.sync();
     if constexpr (D > 6) {
-        if (a.nsh > 0) {  // shared cameras: q summed over each camera's images, the owner's p.q
+        if (shared_cams) {  // shared cameras: q summed over each camera's images, the owner's p.q
             constexpr int KC = D - 6;
+            double pq_w = 0.0;
             for (int c = gw; c < a.nsh; c += nw) {
                 const int i0 = a.sh_img_start[c], i1 = a.sh_img_start[c + 1];
                 const int owner = a.sh_imgs[i0];
@@ -146,14 +177,16 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
                 }
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, off);
-                if (lane == 0) a.part[2 * nI + owner] += pq;
+                pq_w += pq;
             }
+            block_partial(pq_w, sh, PQS);
             grid.sync();
         }
     }
     // alpha = (r.z) / (p.q); x += alpha p; r -= alpha q; z = M^-1 r; r.z, r.r partials.
     {
-        const double pq = block_sum_c(strided_sum_c(a.part + 2 * nI, nI), sh);
+        double pq = block_sum_c(strided_sum_c(PQ, G), sh);
+        if (shared_cams) pq += block_sum_c(strided_sum_c(PQS, G), sh);
         if (!(pq > 0.0) || !isfinite(pq)) {  // breakdown (every block sees it): keep the iterate
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 st->pcg_done = 1;
@@ -164,40 +197,40 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         }
         const double alpha = st->pcg_rzbuf[a.parity] / pq;
         if (blockIdx.x == 0 && threadIdx.x == 0) st->pcg_alpha = alpha;
-        __shared__ double rs[8][16];  // fused coarse: this block's images' restricted residuals
+        __shared__ T rs[8][16];  // fused coarse: this block's images' restricted residuals
+        const T al = (T)alpha;
+        double rz_w = 0.0, rr_w = 0.0;
         for (int i = gw; i < nI; i += nw) {
             const size_t base = (size_t)i * D;
             T rc = T(0);
             if (lane < D) {
-                a.x[base + lane] = (T)((double)a.x[base + lane] + alpha * (double)a.p[base + lane]);
-                rc = (T)((double)a.r[base + lane] - alpha * (double)a.q[base + lane]);
+                a.x[base + lane] = a.x[base + lane] + al * a.p[base + lane];
+                rc = a.r[base + lane] - al * a.q[base + lane];
                 a.r[base + lane] = rc;
             }
-            double zc = 0.0;
+            T zc = T(0);
             const T *M = a.Minv + (size_t)i * D * D;
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 const T rd = __shfl_sync(0xffffffffu, rc, d);
-                if (lane < D) zc += (double)M[lane * D + d] * (double)rd;
+                if (lane < D) zc += M[lane * D + d] * rd;
             }
-            double rz = 0.0, rr = 0.0;
+            T rz = T(0), rr = T(0);
             if (lane < D) {
-                a.z[base + lane] = (T)zc;
+                a.z[base + lane] = zc;
                 if ((a.img_dmask[i] >> lane) & 1) {
-                    rz = (double)rc * (double)(T)zc;
-                    rr = (double)rc * (double)rc;
+                    rz = rc * zc;
+                    rr = rc * rc;
                 }
-                if (a.fused) rs[threadIdx.x >> 5][lane] = ((a.img_pmask[i] >> lane) & 1) ? (double)rc : 0.0;
+                if (a.fused) rs[threadIdx.x >> 5][lane] = ((a.img_pmask[i] >> lane) & 1) ? rc : T(0);
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
                 rz += __shfl_xor_sync(0xffffffffu, rz, off);
                 rr += __shfl_xor_sync(0xffffffffu, rr, off);
             }
-            if (lane == 0) {
-                a.part[i] = rz;
-                a.part[nI + i] = rr;
-            }
+            rz_w += (double)rz;
+            rr_w += (double)rr;
         }
         if (a.fused) {  // per-block sums of the restriction over the clusters of images [8b, 8b + 8)
             __syncthreads();
@@ -205,11 +238,14 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
             if (i0 < nI && (int)threadIdx.x < 3 * D) {
                 const int s = threadIdx.x / D, d = threadIdx.x - s * D;
                 const int c = a.img_cluster[i0] + s;
-                double v = 0.0;
+                T v = T(0);
                 for (int i = i0; i < i1; ++i)
                     if (a.img_cluster[i] == c) v += rs[i - i0][d];
-                a.zpart[((size_t)blockIdx.x * 3 + s) * D + d] = v;
+                zpart[((size_t)blockIdx.x * 3 + s) * D + d] = v;
             }
+        } else if (a.nc == 0) {  // no coarse correction: these are the iteration's r.z, r.r
+            block_partial(rz_w, sh, RZ);
+            block_partial(rr_w, sh, RR);
         }
     }
     grid.sync();
@@ -217,56 +253,55 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         // zc = Z^T r from the per-block sums (every block rebuilds all of it),
         // cc rows of this block's clusters, z_i += cc[cluster(i)] for its
         // images, r.z / r.r partials.
-        __shared__ double zcs[kMaxCoarseClusters * 14];
-        __shared__ double ccs[3 * 16];
+        __shared__ T zcs[kMaxCoarseClusters * 14];
+        __shared__ T ccs[3 * 16];
         for (int e = threadIdx.x; e < a.Nc; e += blockDim.x) {
             const int c = e / D, d = e - c * D;
             const int b0 = a.clu_start[c] / 8, b1 = (a.clu_start[c + 1] - 1) / 8;
-            double v = 0.0;
-            for (int b = b0; b <= b1; ++b)
-                v += a.zpart[((size_t)b * 3 + (c - a.img_cluster[b * 8])) * D + d];
+            T v = T(0);
+            for (int b = b0; b <= b1; ++b) v += zpart[((size_t)b * 3 + (c - a.img_cluster[b * 8])) * D + d];
             zcs[e] = v;
         }
         __syncthreads();
         const int i0 = blockIdx.x * 8, i1 = min(i0 + 8, nI);
+        double rz = 0.0, rr = 0.0;
         if (i0 < nI) {
             const int c0 = a.img_cluster[i0], nrow = (a.img_cluster[i1 - 1] - c0 + 1) * D;
             const int wl = threadIdx.x >> 5;
             for (int rl = wl; rl < nrow; rl += blockDim.x >> 5) {
                 const float *ar = a.Ainv + (size_t)(c0 * D + rl) * a.Nc;
                 T s = T(0);
-                for (int j = lane; j < a.Nc; j += 32) s += (T)__ldg(ar + j) * (T)zcs[j];
+                for (int j = lane; j < a.Nc; j += 32) s += (T)__ldg(ar + j) * zcs[j];
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-                if (lane == 0) ccs[rl] = (double)s;
+                if (lane == 0) ccs[rl] = s;
             }
             __syncthreads();
             const int i = gw;
             if (i < i1) {
                 const size_t base = (size_t)i * D;
-                double rz = 0.0, rr = 0.0;
+                T rzl = T(0), rrl = T(0);
                 if (lane < D) {
-                    const double rc = (double)a.r[base + lane];
-                    double zc = (double)a.z[base + lane];
+                    const T rc = a.r[base + lane];
+                    T zc = a.z[base + lane];
                     if ((a.img_pmask[i] >> lane) & 1) zc += ccs[(a.img_cluster[i] - c0) * D + lane];
-                    const T zt = (T)zc;
-                    a.z[base + lane] = zt;
+                    a.z[base + lane] = zc;
                     if ((a.img_dmask[i] >> lane) & 1) {
-                        rz = rc * (double)zt;
-                        rr = rc * rc;
+                        rzl = rc * zc;
+                        rrl = rc * rc;
                     }
                 }
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
-                    rz += __shfl_xor_sync(0xffffffffu, rz, off);
-                    rr += __shfl_xor_sync(0xffffffffu, rr, off);
+                    rzl += __shfl_xor_sync(0xffffffffu, rzl, off);
+                    rrl += __shfl_xor_sync(0xffffffffu, rrl, off);
                 }
-                if (lane == 0) {
-                    a.part[i] = rz;
-                    a.part[nI + i] = rr;
-                }
+                rz = (double)rzl;
+                rr = (double)rrl;
             }
         }
+        block_partial(rz, sh, RZ);
+        block_partial(rr, sh, RR);
         grid.sync();
     } else if (a.nc > 0) {
         // zc = Z^T r (per cluster and column, image order, own columns only)
@@ -312,6 +347,7 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         }
         grid.sync();
         // z_i += cc[cluster(i)] on the image's own columns; r.z, r.r partials
+        double rz_w = 0.0, rr_w = 0.0;
         for (int i = gw; i < nI; i += nw) {
             const size_t base = (size_t)i * D;
             double rz = 0.0, rr = 0.0;
@@ -331,17 +367,16 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
                 rz += __shfl_xor_sync(0xffffffffu, rz, off);
                 rr += __shfl_xor_sync(0xffffffffu, rr, off);
             }
-            if (lane == 0) {
-                a.part[i] = rz;
-                a.part[nI + i] = rr;
-            }
+            rz_w += rz;
+            rr_w += rr;
         }
+        block_partial(rz_w, sh, RZ);
+        block_partial(rr_w, sh, RR);
         grid.sync();
     }
     // convergence test, beta, p = z + beta p
-    double rz = strided_sum_c(a.part, nI), rr = strided_sum_c(a.part + nI, nI);
-    rz = block_sum_c(rz, sh);
-    rr = block_sum_c(rr, sh);
+    const double rz = block_sum_c(strided_sum_c(RZ, G), sh);
+    const double rr = block_sum_c(strided_sum_c(RR, G), sh);
     const bool stop = rr <= st->pcg_tol2 * st->pcg_bb || !(rz > 0.0) || !isfinite(rz);
     const double beta = stop ? 0.0 : rz / st->pcg_rzbuf[a.parity];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -358,10 +393,11 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
     }
     if (stop) return;
     const int nthreads = gridDim.x * blockDim.x;
+    const T bt = (T)beta;
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.nID; u += nthreads) {
         const int i = u / D, c = u - i * D;
         const int zu = (a.img_owner && c >= 6) ? a.img_owner[i] * D + c : u;
-        const T pn = (T)((double)a.z[zu] + beta * (double)a.p[u]);
+        const T pn = a.z[zu] + bt * a.p[u];
         a.p[u] = pn;
         if (a.p4) a.p4[plane_index(nI, i, c)] = (float)pn;
     }
@@ -385,6 +421,7 @@ void run_coop(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
     a.ipart = (const T *)b.ipart;
     a.ipart_off = b.ipart_off;
     a.img_H = b.img_H;
+    a.img_Hf = b.img_Hf;
     a.img_active = b.img_active;
     a.img_pmask = b.img_pmask;
     a.img_dmask = b.img_dmask;
@@ -395,7 +432,7 @@ void run_coop(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
     a.r = (T *)b.pcg_r;
     a.z = (T *)b.pcg_z;
     a.p4 = std::is_same<T, float>::value ? b.pcg_p4 : nullptr;
-    a.part = b.pcg_part;
+    a.blk = b.pcg_blk;
     a.st = b.state;
     a.nI = b.nI;
     a.nID = b.nID;
@@ -427,7 +464,7 @@ void run_coop(const Bufs &b, cudaStream_t s, int parity, bool coarse) {
     }
     if (cap < 1) throw Error(SFMBA_ERR_INTERNAL, "the PCG vector kernel cannot be resident");
     const int want = std::max(std::max(std::max(div_up(b.nI, 8), div_up(a.Nc, 8)), div_up(a.nsh, 8)), 1);
-    const int grid = std::min(want, cap);
+    const int grid = std::min(std::min(want, cap), kPcgMaxCoopBlocks);
     // The fused coarse phase needs image i on warp i (block b: images 8b..8b+7).
     a.fused = (coarse && (long long)grid * 8 >= b.nI && D <= 16 && b.co.zpart) ? 1 : 0;
     a.zpart = b.co.zpart;

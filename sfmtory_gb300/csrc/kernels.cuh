@@ -160,7 +160,9 @@ struct Bufs {
     CoarseBufs co;                // coarse correction of the preconditioner
     void *pcg_u = nullptr;        // [nP*4] per-point Cinv E^T p
     void *pcg_Minv = nullptr;     // [nI*D*D] block-Jacobi inverse
+    float *img_Hf = nullptr;      // FP32 PCG: [nI*D*D] H_i + lambda diag H_i (the CG kernel's B p)
     double *pcg_part = nullptr;   // [3*nI] per-image partial dot products
+    double *pcg_blk = nullptr;    // [4*kPcgMaxCoopBlocks] per-block partial sums of the cooperative CG kernel
     double pcg_tol = 1e-6;
     // Work partition of the matrix-free passes (fixed-size observation chunks).
     int *pchunk = nullptr;        // [npchunks+1] point-aligned chunk starts (point-major order)
@@ -238,6 +240,7 @@ constexpr int kCostBlocks = 1024;
 constexpr int kDotSlots = 16;
 constexpr int kCholNB = 64;
 constexpr int kChunkObs = 256;  // observations per warp in the matrix-free passes
+constexpr int kPcgMaxCoopBlocks = 4096;  // grid of the cooperative CG kernel at most
 
 // Inputs/outputs of the per-observation Jacobian probe (original order).
 struct JacProbe {
@@ -469,8 +472,7 @@ void launch_wb_begin_outer(const WinBufs &w, int max_iterations, cudaStream_t s)
 void launch_wb_begin_retry(const WinBufs &w, cudaStream_t s);
 void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s);
 // variant: launch shape (k_batched.cu WbSchurShape), 0 .. kWbSchurVariants - 1; all give the same sums
-constexpr int kWbSchurVariants = 6;
-constexpr int kWbSchurForced = 10;  // shapes reachable by sfmba_options.kernel_variant (6..9: other tilings)
+constexpr int kWbSchurVariants = 3;
 void launch_wb_schur(const Bufs &b, const WinBufs &w, cudaStream_t s, int variant = 0);
 void launch_wb_fold(const Bufs &b, const WinBufs &w, cudaStream_t s);
 void launch_wb_cholesky(const Bufs &b, const WinBufs &w, cudaStream_t s);

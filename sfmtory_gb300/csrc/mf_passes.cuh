@@ -15,15 +15,15 @@ namespace {
 // Inclusive segmented warp scan (segments start at head lanes). The lane
 // `off` places back is added while it lies in the lane's segment, found once
 // from the ballot of heads (the same additions in the same order as carrying
-// a head flag through the levels). Levels whose offset exceeds every lane's
-// distance to its segment start add nothing and are skipped (short tracks:
-// rounds of 32 observations rarely hold a segment longer than 8 or 16).
+// a head flag through the levels). All five levels run unrolled: skipping
+// the levels no segment needs (a warp-wide maximum and a loop) was measured
+// slower on the 2000-camera problem's point pass (86.8 against 82.7 us).
 template <typename T, int N>
 __device__ __forceinline__ void seg_scan(T (&v)[N], bool head, int lane) {
     const unsigned heads = __ballot_sync(0xffffffffu, head) | 1u;
     const int seg_start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-    const int reach = (int)__reduce_max_sync(0xffffffffu, (unsigned)(lane - seg_start));
-    for (int off = 1; off <= reach; off <<= 1) {
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
         T a[N];
 #pragma unroll
         for (int n = 0; n < N; ++n) a[n] = shfl_up(v[n], off);
@@ -363,7 +363,8 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
                                                            double *__restrict__ img_rhs, T *__restrict__ Minv_out,
                                                            T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
                                                            T *__restrict__ p, T *__restrict__ p4,
-                                                           double *__restrict__ dots, int stride) {
+                                                           double *__restrict__ dots, int stride,
+                                                           float *__restrict__ Hf) {
     constexpr int NH = D * (D + 1) / 2;
     constexpr int NV = NH + D;
     constexpr int WPB = 4;
@@ -402,6 +403,14 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
             const double rhs = ((act >> a) & 1) ? -img_b[(size_t)i * D + a] + sum : 0.0;
             rv[a] = rhs;
             img_rhs[(size_t)i * D + a] = rhs;
+        }
+    }
+    if (Hf) {  // FP32 PCG: the damped image block for the CG kernel's (H_i + lambda diag H_i) p_i
+        for (int idx = lane; idx < D * D; idx += 32) {
+            const int a = idx / D, c = idx - a * D;
+            double v = H[idx];
+            if (a == c) v += H[idx] * lam;
+            Hf[(size_t)i * D * D + idx] = (float)v;
         }
     }
     __syncwarp();

@@ -1156,7 +1156,9 @@ class Solver {
                     b.pcg_q = A.take<char>((size_t)nID * tsz);
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
                     b.pcg_Minv = A.take<char>((size_t)nID * D * tsz);
+                    b.img_Hf = mixed ? A.take<float>((size_t)nID * D) : nullptr;
                     b.pcg_part = A.take<double>((size_t)3 * nI);  // r.z, r.r, p.q per image
+                    b.pcg_blk = A.take<double>((size_t)4 * kPcgMaxCoopBlocks);
                     b.pchunk = A.take<int>((size_t)nchunks + 1);
                     b.ipart_off = A.take<int>((size_t)nI + 1);
                     b.ipart = A.take<char>((size_t)(nI + nchunks + 1) * D * tsz);
@@ -1526,7 +1528,7 @@ class Solver {
                     {
                         SFMBA_PHASE(PH_SCHUR);
                         if (vs < 0) {
-                            vs = o->kernel_variant > 0 ? (o->kernel_variant - 1) % kWbSchurForced
+                            vs = o->kernel_variant > 0 ? (o->kernel_variant - 1) % kWbSchurVariants
                                                        : tuned_variant(ctx_.device, b.mixed ? 2 : 3, kWbSchurVariants,
                                                                        b, s_, [&](int v) { launch_wb_schur(b, w, s_, v); });
                         }

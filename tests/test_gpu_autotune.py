@@ -28,7 +28,7 @@ def test_autotune_report_lists_choices():
     assert {e["pass"] for e in rep} >= {"points", "images"}
     for e in rep:
         # launch variants per kernel (kernels.cuh: kPointPassVariants, kImagePassVariants, kWbSchurVariants)
-        n = 6 if e["pass"] == "wb_schur" else 10
+        n = 3 if e["pass"].startswith("wb_schur") else 10
         assert 0 <= e["variant"] < n and len(e["us"]) == n and min(e["us"]) > 0
         assert e["us"][e["variant"]] == min(e["us"])
 
@@ -42,7 +42,7 @@ def test_batched_schur_shapes_are_bit_identical(precision):
     wins = [scenes.local_window(rng, int(rng.integers(8, 24)), int(rng.integers(150, 600))) for _ in range(12)]
     kw = dict(precision=precision, robust_loss=abi.LOSS_HUBER, loss_scale_px=2.0, max_iterations=6)
     ref = native.bundle_adjust_batched_arrays(wins, kernel_variant=1, **kw)
-    for v in (2, 3, 4, 5, 6):
+    for v in (2, 3):
         res = native.bundle_adjust_batched_arrays(wins, kernel_variant=v, **kw)
         for a, b in zip(res, ref):
             assert a.final_cost == b.final_cost and a.iterations_run == b.iterations_run, v
@@ -51,4 +51,4 @@ def test_batched_schur_shapes_are_bit_identical(precision):
     tuned = native.bundle_adjust_batched_arrays(wins, **kw)
     for a, b in zip(tuned, ref):
         assert a.final_cost == b.final_cost
-    assert any(e["pass"] == "wb_schur" for e in native.profile_report()["autotune"])
+    assert any(e["pass"].startswith("wb_schur") for e in native.profile_report()["autotune"])
