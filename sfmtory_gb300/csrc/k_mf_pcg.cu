@@ -1,9 +1,34 @@
 // Launchers of the two observation passes of every PCG iteration (point
 // pass u = C^-1 E^T p, image pass E u), in the launch-shape variants the
-// autotuner picks from.
-#include "mf_passes.cuh"
+// autotuner picks from; the point pass's last variant streams its records
+// by bulk copies (mf_tma.cuh).
+#include "mf_tma.cuh"
 
 namespace sfmba {
+
+namespace {
+
+// The record-streaming point pass where it applies (FP32 recomputed operator
+// of a camera model MvOp serves); false otherwise.
+bool mf_points_tma(const Bufs &b, cudaStream_t s) {
+    if (!b.mixed || !b.pcg_p4 || !b.points32 || !b.img_mv) return false;
+    bool ran = false;
+    dispatch_TDR(b, [&](auto t, auto dc, auto rc, auto mc) {
+        using T = decltype(t);
+        constexpr int D = decltype(dc)::value;
+        constexpr int M = decltype(mc)::value;
+        if constexpr (std::is_same<T, float>::value && decltype(rc)::value && mv_model<M>() && pad4(D) <= 12) {
+            k_mf_points_tma<D, M><<<div_up(b.npchunks, kTmaWarps), 32 * kTmaWarps, 0, s>>>(
+                jac_src<float>(b), b.pchunk, b.npchunks, (const float *)b.pt_Cinv, b.pt_ok, b.pcg_p4, b.state,
+                (float *)b.pcg_u);
+            SFMBA_LAUNCH_CHECK();
+            ran = true;
+        }
+    });
+    return ran;
+}
+
+}  // namespace
 
 template <int V>
 void mf_points_v(const Bufs &b, cudaStream_t s) {
@@ -43,7 +68,10 @@ void launch_mf_points(const Bufs &b, cudaStream_t s, int variant) {
     case 6: mf_points_v<6>(b, s); break;
     case 7: mf_points_v<7>(b, s); break;
     case 8: mf_points_v<8>(b, s); break;
-    default: mf_points_v<9>(b, s); break;
+    case 9: mf_points_v<9>(b, s); break;
+    default:  // records by bulk copy, where it applies; else the same sums by variant 8
+        if (!mf_points_tma(b, s)) mf_points_v<8>(b, s);
+        break;
     }
 }
 

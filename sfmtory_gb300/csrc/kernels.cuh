@@ -324,9 +324,9 @@ void launch_mf_precond(const Bufs &b, cudaStream_t s);          // M^-1, rhs, PC
 void launch_mf_precond_fused(const Bufs &b, cudaStream_t s);
 // The two PCG passes in launch variant 0..k{Point,Image}PassVariants-1
 // (same results; chosen by the autotuner).
-constexpr int kPointPassVariants = 10;
+constexpr int kPointPassVariants = 11;  // the last one streams its records by bulk copies (mf_tma.cuh)
 constexpr int kImagePassVariants = 10;
-constexpr int kPassVariants = kPointPassVariants;  // the most variants of any tuned kernel
+constexpr int kPassVariants = 11;  // the most variants of any tuned kernel
 void launch_mf_points(const Bufs &b, cudaStream_t s, int variant);  // u = C^-1 E^T p
 void launch_mf_images(const Bufs &b, cudaStream_t s, int variant);  // partials of E u
 void launch_mf_backsub(const Bufs &b, const double *delta_slot, cudaStream_t s);

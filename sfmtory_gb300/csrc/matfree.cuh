@@ -247,6 +247,11 @@ struct MvOp {
         const size_t nI = (size_t)J.nI;
         const float4 m0 = __ldg(mv), m1 = __ldg(mv + nI), m2 = __ldg(mv + 2 * nI), ms = __ldg(mv + 3 * nI);
         const float4 X = __ldg(J.points32 + pt);
+        build_from(J, img, m0, m1, m2, ms, X, rc);
+    }
+    // From the image's constants (R, t, {f, fy, k1, k2}) and the point, wherever they were loaded.
+    __device__ __forceinline__ void build_from(const JacSrc<float> &J, int img, float4 m0, float4 m1, float4 m2,
+                                               float4 ms, float4 X, int4 rc) {
         R[0] = m0.x; R[1] = m0.y; R[2] = m0.z; R[3] = m0.w;
         R[4] = m1.x; R[5] = m1.y; R[6] = m1.z; R[7] = m1.w;
         R[8] = m2.x;
@@ -272,7 +277,7 @@ struct MvOp {
         }
         s = ok ? 1.0f : 0.0f;
         if (ok && J.loss != SFMBA_LOSS_NONE) {  // sqrt of the robust weight of the FP32 residual
-            const float4 cc = __ldg(mv + 4 * nI);  // cx, cy
+            const float4 cc = __ldg(J.mv + 4 * (size_t)J.nI + img);  // cx, cy
             const float r0 = f * xp * d + cc.x - __int_as_float(rc.z);
             const float r1 = fy * yp * d + cc.y - __int_as_float(rc.w);
             s = sqrtf(robust_weight<float>(sqrtf(r0 * r0 + r1 * r1), J.loss, J.scale));
