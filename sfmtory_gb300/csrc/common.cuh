@@ -64,18 +64,9 @@ __host__ __device__ constexpr int pad4(int D) { return (D + 3) & ~3; }
 __host__ __device__ __forceinline__ size_t plane_index(int nI, int i, int c) {
     return ((size_t)(c >> 2) * nI + i) * 4 + (c & 3);
 }
-// FP32 PCG: after the planes of the direction vector p (pad4(D) * nI floats)
-// follow the per-image rows that the TMA point pass gathers, one 128-byte
-// row per image: R (9), t (3), the model's scalars {f, fy, k1, k2}, then p
-// from column kRowP (D <= 16), zero-padded.
-constexpr int kRowFloats = 32;
-constexpr int kRowP = 16;
-__host__ __device__ __forceinline__ float *row_table(float *p4, int nI, int D) { return p4 + (size_t)nI * pad4(D); }
-// Entry c of image i of p into both copies.
-__device__ __forceinline__ void store_dir(float *p4, int nI, int D, int i, int c, float v) {
-    p4[plane_index(nI, i, c)] = v;
-    row_table(p4, nI, D)[(size_t)i * kRowFloats + kRowP + c] = v;
-}
+// FP32 PCG: entry c of image i of the direction vector p into its plane copy
+// (the point pass's gathers read p there).
+__device__ __forceinline__ void store_dir(float *p4, int nI, int i, int c, float v) { p4[plane_index(nI, i, c)] = v; }
 
 // Width of the per-image variable block: 6 pose columns + the widest camera.
 __host__ __device__ constexpr int block_width_for(int kmax) {

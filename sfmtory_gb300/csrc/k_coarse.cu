@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(256) k_coarse_z(const T *__restrict__ r, const
         z[base + lane] = zt;
         if (init && own) {
             p[base + lane] = zt;
-            if (p4) store_dir(p4, nI, D, i, lane, (float)zt);
+            if (p4) store_dir(p4, nI, i, lane, (float)zt);
         }
         if ((img_dmask[i] >> lane) & 1) {
             rz = rc * (double)zt;

@@ -36,7 +36,7 @@ __device__ __forceinline__ void quat_to_R(const double *q, double R[9]) {
 template <typename T>
 __global__ void k_prepare_images(const double *poses, const double *cams, const int *cam_of_img,
                                  const int *cam_model, const int *img_active, int nI,
-                                 ImageLin<T> *out, float4 *mv, float *row) {
+                                 ImageLin<T> *out, float4 *mv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nI) return;
     const double *q = poses + 7 * (size_t)i;
@@ -69,13 +69,6 @@ __global__ void k_prepare_images(const double *poses, const double *cams, const 
         const float k2 = im.model == SFMBA_RADIAL ? (float)im.c[4] : 0.f;
         mv[3 * (size_t)nI + i] = make_float4(f, fy, k1, k2);
         mv[4 * (size_t)nI + i] = make_float4(cx, cy, 0.f, 0.f);
-        if (row) {  // the same 16 values at the start of the image's row (TMA point pass)
-            float4 *rw = reinterpret_cast<float4 *>(row + (size_t)i * kRowFloats);
-            rw[0] = m0;
-            rw[1] = m1;
-            rw[2] = m2;
-            rw[3] = make_float4(f, fy, k1, k2);
-        }
     }
 }
 
@@ -660,12 +653,11 @@ void launch_prepare_images(const Bufs &b, cudaStream_t s) {
     if (b.nI == 0) return;
     if (b.mixed)
         k_prepare_images<float><<<div_up(b.nI, 128), 128, 0, s>>>(
-            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin, b.img_mv,
-            b.pcg_p4 ? row_table(b.pcg_p4, b.nI, b.D) : nullptr);
+            b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<float> *)b.img_lin, b.img_mv);
     else
         k_prepare_images<double><<<div_up(b.nI, 128), 128, 0, s>>>(
             b.poses, b.cams, b.cam_of_img, b.cam_model, b.img_active, b.nI, (ImageLin<double> *)b.img_lin,
-            nullptr, nullptr);
+            nullptr);
     SFMBA_LAUNCH_CHECK();
 }
 

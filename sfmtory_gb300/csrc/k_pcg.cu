@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256) k_pcg_dir(const T *z, LMState *st, const 
     p[u] = pn;
     if (p4) {
         const int i = u / D;
-        store_dir(reinterpret_cast<float *>(p4), nI, D, i, u - i * D, (float)pn);
+        store_dir(reinterpret_cast<float *>(p4), nI, i, u - i * D, (float)pn);
     }
 }
 

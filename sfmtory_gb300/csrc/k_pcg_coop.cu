@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         const int zu = (a.img_owner && c >= 6) ? a.img_owner[i] * D + c : u;
         const T pn = a.z[zu] + bt * a.p[u];
         a.p[u] = pn;
-        if (a.p4) store_dir(a.p4, nI, D, i, c, (float)pn);
+        if (a.p4) store_dir(a.p4, nI, i, c, (float)pn);
     }
 }
 

@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(128) k_sh_precond(const double *__restrict__ i
             const int i = sh_imgs[k];
             r[(size_t)i * D + 6 + lane] = rt;
             p[(size_t)i * D + 6 + lane] = zt;
-            if (p4) store_dir(p4, nI, D, i, 6 + lane, (float)zt);
+            if (p4) store_dir(p4, nI, i, 6 + lane, (float)zt);
         }
         z[(size_t)owner * D + 6 + lane] = zt;
         rz = (double)rt * (double)zt;

@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
         r[u] = rt;
         z[u] = zt;
         p[u] = zt;
-        if (p4) store_dir(reinterpret_cast<float *>(p4), nI, D, i, lane, (float)zt);
+        if (p4) store_dir(reinterpret_cast<float *>(p4), nI, i, lane, (float)zt);
         if ((pm >> lane) & 1) {  // a shared camera's entries are counted by launch_shared_precond
             rz = (double)rt * (double)zt;
             rr = (double)rt * (double)rt;

@@ -1151,7 +1151,7 @@ class Solver {
                     b.pcg_r = A.take<char>((size_t)nID * tsz);
                     b.pcg_z = A.take<char>((size_t)nID * tsz);
                     b.pcg_p = A.take<char>((size_t)nID * tsz);
-                    b.pcg_p4 = mixed ? A.take<float>((size_t)nI * (pad4(D) + kRowFloats)) : nullptr;  // planes, rows
+                    b.pcg_p4 = mixed ? A.take<float>((size_t)nI * pad4(D)) : nullptr;
                     b.img_mv = mixed ? A.take<float4>((size_t)5 * nI) : nullptr;
                     b.pcg_q = A.take<char>((size_t)nID * tsz);
                     b.pcg_u = A.take<char>((size_t)nP * 4 * tsz);
@@ -1250,8 +1250,7 @@ class Solver {
             b.n_iachunks = (int)ia.size();
             put_vec(b.iachunk, ia, s_);
             put_vec(b.iachunk_off, ia_off, s_);
-            if (b.pcg_p4)  // planes and rows (the rows' padding is never written by the kernels)
-                SFMBA_CUDA(cudaMemsetAsync(b.pcg_p4, 0, sizeof(float) * (size_t)nI * (pad4(D) + kRowFloats), s_));
+            if (b.pcg_p4) SFMBA_CUDA(cudaMemsetAsync(b.pcg_p4, 0, sizeof(float) * (size_t)nI * pad4(D), s_));
             launch_mf_prepare(b, s_);
         }
         if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
