@@ -113,8 +113,9 @@ typedef struct sfmba_options {
     int32_t kernel_variant;       /* 0: launch variants of the PCG observation passes
                                      and of the batched Schur reduction picked by the
                                      autotuner; k > 0: force variant k - 1 of each
-                                     (modulo their counts, 10 and 3; all variants of
-                                     a kernel give the same results) */
+                                     (point pass min(k, 11), image pass modulo 10,
+                                     batched Schur modulo 3; all variants of a
+                                     kernel give the same results) */
     int32_t pcg_coarse_clusters;  /* PCG solver: clusters of consecutive images in the
                                      coarse correction of the preconditioner (0: 64,
                                      at most 128; < 0: block-Jacobi alone) */
