@@ -303,3 +303,23 @@ def test_mixed_cost_double_float_matches_fp64(oracle_lib, models, loss):
     out = p.copy(poses=g.poses, points=g.points, camera_params=g.camera_params)
     ref1 = oracle_lib.total_cost(out, **kw)
     assert abs(g.final_cost - ref1) <= 1e-10 * ref1, (g.final_cost, ref1)
+
+
+def test_auto_solver_switch_over_point_matches_oracle(oracle_lib):
+    """SOLVER_AUTO picks the dense reduced-camera solve up to dense_max_dim
+    unknowns and the matrix-free PCG above it. At the switch-over point (the
+    problem's own reduced dimension n: dense at dense_max_dim = n, PCG at
+    n - 1) both FP64 solves follow the oracle's LM iterations: the same
+    iteration count and final cost to 1e-6 (PCG solved tightly, so it is an
+    exact linear solve up to its tolerance)."""
+    p = scenes.ring16(seed=9, scale=0.25)
+    n = p.reduced_dim()
+    kw = dict(robust_loss=abi.LOSS_NONE, max_iterations=20)
+    r = oracle_lib.bundle_adjust(p, **kw)
+    dense = native.bundle_adjust_arrays(p, solver=abi.SOLVER_AUTO, dense_max_dim=n, **kw)
+    pcg = native.bundle_adjust_arrays(p, solver=abi.SOLVER_AUTO, dense_max_dim=n - 1, pcg_tolerance=1e-10,
+                                      pcg_max_iterations=2000, **kw)
+    assert dense.solver_used == abi.SOLVER_DENSE and pcg.solver_used == abi.SOLVER_PCG
+    for g in (dense, pcg):
+        assert g.iterations_run == r.iterations_run, (g.solver_used, g.iterations_run, r.iterations_run)
+        assert abs(g.final_cost - r.final_cost) <= 1e-6 * r.final_cost, (g.solver_used, g.final_cost, r.final_cost)
