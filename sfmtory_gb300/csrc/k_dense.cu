@@ -109,13 +109,13 @@ constexpr int NB = kCholNB;
 constexpr int LD = NB + 1;
 
 // Factor the diagonal block k0 (in place, lower) and write the inverse of
-// its factor to Linv. Sets state->factor_failed when a pivot is not > 0
-// (nalgebra Cholesky::new semantics: 0, negative and NaN all fail).
-__global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, double *Linv, LMState *st) {
-    extern __shared__ double sm[];
+// its factor to Linv (sm: two NB x LD tiles, buf: NB + 3). Sets
+// state->factor_failed when a pivot is not > 0 (nalgebra Cholesky::new
+// semantics: 0, negative and NaN all fail).
+__device__ __forceinline__ void chol_diag_body(double *L, int n, int k0, double *Linv, LMState *st, double *sm,
+                                               double *buf) {
     double *A = sm;            // NB x LD
     double *X = sm + NB * LD;  // NB x LD
-    __shared__ double buf[NB + 3];
     static_assert(LD == kBlkLD, "tile stride of chol_block_factor_invert");
     if (st->factor_failed) return;
     const int nb = min(NB, n - k0);
@@ -140,16 +140,22 @@ __global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, dou
     }
 }
 
-// Panel below the diagonal block: A[r, k-block] <- A[r, k-block] Lkk^-T.
-constexpr int PANEL_ROWS = 32;
-__global__ void __launch_bounds__(256) k_chol_panel(double *L, int n, int k0, const double *Linv,
-                                                     const LMState *st) {
+__global__ void __launch_bounds__(256) k_chol_diag(double *L, int n, int k0, double *Linv, LMState *st) {
     extern __shared__ double sm[];
+    __shared__ double buf[NB + 3];
+    chol_diag_body(L, n, k0, Linv, st, sm, buf);
+}
+
+// Panel below the diagonal block: A[r, k-block] <- A[r, k-block] Lkk^-T,
+// rows k0 + nb + blk PANEL_ROWS onwards (sm: NB + PANEL_ROWS rows of LD).
+constexpr int PANEL_ROWS = 32;
+__device__ __forceinline__ void chol_panel_body(double *L, int n, int k0, const double *Linv, const LMState *st,
+                                                int blk, double *sm) {
     double *Li = sm;             // NB x LD
     double *R = sm + NB * LD;    // PANEL_ROWS x LD
     if (st->factor_failed) return;
     const int nb = min(NB, n - k0);
-    const int r0 = k0 + nb + blockIdx.x * PANEL_ROWS;
+    const int r0 = k0 + nb + blk * PANEL_ROWS;
     const int rows = min(PANEL_ROWS, n - r0);
     if (rows <= 0) return;
     const double *inv = Linv + (size_t)(k0 / NB) * NB * NB;
@@ -165,6 +171,12 @@ __global__ void __launch_bounds__(256) k_chol_panel(double *L, int n, int k0, co
         for (int t = 0; t <= c; ++t) s += R[r * LD + t] * Li[c * LD + t];
         L[(size_t)(r0 + r) * n + k0 + c] = s;
     }
+}
+
+__global__ void __launch_bounds__(256) k_chol_panel(double *L, int n, int k0, const double *Linv,
+                                                     const LMState *st) {
+    extern __shared__ double sm[];
+    chol_panel_body(L, n, k0, Linv, st, blockIdx.x, sm);
 }
 
 // Tile (ti, tj), tj <= ti, of block q of a trailing update launch. part 0:
@@ -189,15 +201,13 @@ __device__ __forceinline__ void trailing_tile(long long q, int part, int &ti, in
 
 // Trailing update of the lower triangle: A[I,J] -= P_I P_J^T for the 64x64
 // tiles (I >= J) right of the panel. Each thread owns a 4x4 register tile.
-__global__ void __launch_bounds__(256) k_chol_update(double *L, int n, int k0, int part, const LMState *st) {
-    extern __shared__ double sm[];
+__device__ __forceinline__ void chol_update_body(double *L, int n, int k0, int ti, int tj, const LMState *st,
+                                                 double *sm) {
     double *Pi = sm;            // NB x LD
     double *Pj = sm + NB * LD;  // NB x LD
     if (st->factor_failed) return;
     const int nb = min(NB, n - k0);
     const int t0 = k0 + nb;
-    int ti, tj;
-    trailing_tile(blockIdx.x, part, ti, tj);
     const int ri = t0 + ti * NB, rj = t0 + tj * NB;
     if (ri >= n || rj >= n) return;
     const int mi = min(NB, n - ri), mj = min(NB, n - rj);
@@ -235,6 +245,70 @@ __global__ void __launch_bounds__(256) k_chol_update(double *L, int n, int k0, i
             if (ti == tj && c > r) continue;
             L[(size_t)(ri + r) * n + rj + c] -= acc[a][b];
         }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_chol_update(double *L, int n, int k0, int part, const LMState *st) {
+    extern __shared__ double sm[];
+    int ti, tj;
+    trailing_tile(blockIdx.x, part, ti, tj);
+    chol_update_body(L, n, k0, ti, tj, st, sm);
+}
+
+// The column loop of k_lu_pivot / k_lu_update (below) in one cooperative
+// launch: block 0 pivots, swaps and scales column k, then every block
+// updates its rows of the trailing matrix; two grid barriers per column
+// instead of two launches, the same operations in the same order (the same
+// factors).
+__global__ void __launch_bounds__(256) k_lu_coop(double *A, int n, int *perm, const LMState *st) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double bv[256];
+    __shared__ int bi[256];
+    if (!st->factor_failed || st->solve_failed) return;
+    const int tid = threadIdx.x;
+    for (int k = 0; k < n; ++k) {
+        if (blockIdx.x == 0) {
+            double best = -1.0;
+            int besti = k;
+            for (int r = k + tid; r < n; r += blockDim.x) {
+                const double v = fabs(A[(size_t)r * n + k]);
+                if (v > best) { best = v; besti = r; }
+            }
+            bv[tid] = best;
+            bi[tid] = besti;
+            __syncthreads();
+            for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+                if (tid < h) {
+                    const double o = bv[tid + h];
+                    const int oi = bi[tid + h];
+                    if (o > bv[tid] || (o == bv[tid] && oi < bi[tid])) { bv[tid] = o; bi[tid] = oi; }
+                }
+                __syncthreads();
+            }
+            const int piv = bi[0];
+            const double diag = A[(size_t)piv * n + k];
+            if (diag != 0.0) {
+                if (piv != k)
+                    for (int c = tid; c < n; c += blockDim.x) {
+                        const double t = A[(size_t)k * n + c];
+                        A[(size_t)k * n + c] = A[(size_t)piv * n + c];
+                        A[(size_t)piv * n + c] = t;
+                    }
+                __syncthreads();
+                for (int r = k + 1 + tid; r < n; r += blockDim.x) A[(size_t)r * n + k] /= diag;
+            }
+            if (tid == 0) perm[k] = diag != 0.0 ? piv : -1;  // a zero column is skipped
+            __syncthreads();
+        }
+        grid.sync();
+        if (k + 1 >= n) break;
+        if (((volatile const int *)perm)[k] >= 0)
+            for (int r = k + 1 + blockIdx.x; r < n; r += gridDim.x) {
+                const double lrk = A[(size_t)r * n + k];
+                for (int c = k + 1 + tid; c < n; c += blockDim.x) A[(size_t)r * n + c] -= lrk * A[(size_t)k * n + c];
+            }
+        grid.sync();
     }
 }
 
@@ -471,9 +545,23 @@ __global__ void k_lu_update(double *A, int n, int k, const int *perm, const LMSt
 // Apply the row swaps to rhs, solve unit-lower then upper. A zero diagonal
 // of U fails the solve (lambda then grows); success clears factor_failed so
 // the back-substitution and trial kernels run.
+// Sum of v over the 1024-thread block (warp sums, then the 32 warps' sums
+// by warp 0), valid in every thread; two barriers.
+__device__ __forceinline__ double block_sum_1024(double v, double *red) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = (threadIdx.x & 31) < (blockDim.x >> 5) ? red[threadIdx.x & 31] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    __syncthreads();  // red is reused by the next call
+    return t;
+}
+
 __global__ void __launch_bounds__(1024) k_lu_solve(const double *A, int n, const int *perm,
                                                     const double *rhs, double *x, LMState *st) {
-    __shared__ double red[1024];
+    __shared__ double red[32];
     __shared__ int bad;
     if (!st->factor_failed || st->solve_failed) return;
     if (threadIdx.x == 0) bad = 0;
@@ -490,28 +578,18 @@ __global__ void __launch_bounds__(1024) k_lu_solve(const double *A, int n, const
     for (int i = 0; i < n; ++i) {
         double s = 0.0;
         for (int k = threadIdx.x; k < i; k += blockDim.x) s += A[(size_t)i * n + k] * x[k];
-        red[threadIdx.x] = s;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) x[i] -= red[0];
+        s = block_sum_1024(s, red);
+        if (threadIdx.x == 0) x[i] -= s;
         __syncthreads();
     }
     for (int i = n - 1; i >= 0; --i) {
         double s = 0.0;
         for (int k = i + 1 + threadIdx.x; k < n; k += blockDim.x) s += A[(size_t)i * n + k] * x[k];
-        red[threadIdx.x] = s;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
-        }
+        s = block_sum_1024(s, red);
         if (threadIdx.x == 0) {
             const double d = A[(size_t)i * n + i];
             if (d == 0.0) bad = 1;
-            else x[i] = (x[i] - red[0]) / d;
+            else x[i] = (x[i] - s) / d;
         }
         __syncthreads();
         if (bad) break;
@@ -628,6 +706,37 @@ LookAhead &look_ahead() {
 // diagonal factor is the serial part (one block, FP64-pipe bound), so it
 // hides behind the bulk update. Tensor-core updates read the panel slices of
 // their own step: two slice buffers alternate by step.
+// Cooperative launch of kernel k with `want` blocks of 256 threads at most
+// what the GPU holds at once (cap: co-resident blocks, queried once per
+// device by the caller); false when none can be resident.
+template <typename... Args>
+bool launch_coop(void (*k)(Args...), int cap, int want, size_t smem, cudaStream_t s, Args... args) {
+    if (cap < 1) return false;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)std::max(1, std::min(cap, want)));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SFMBA_CUDA(cudaLaunchKernelEx(&cfg, k, args...));
+    SFMBA_LAUNCH_CHECK();
+    return true;
+}
+
+// Co-resident blocks of a 256-thread kernel with `smem` dynamic shared memory.
+template <typename K>
+int coop_capacity(K k, size_t smem) {
+    int dev = 0, per_sm = 0, sms = 0;
+    SFMBA_CUDA(cudaGetDevice(&dev));
+    SFMBA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
+    SFMBA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return per_sm * sms;
+}
+
 void launch_cholesky(const Bufs &b, cudaStream_t s) {
     set_smem_limits();
     const int n = b.n;
@@ -732,6 +841,18 @@ void launch_refine(const Bufs &b, cudaStream_t s) {
 void launch_lu_factor(const Bufs &b, cudaStream_t s) {
     const int n = b.n;
     SFMBA_CUDA(cudaMemcpyAsync(b.L, b.S, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s));
+    // One block per SM at most: every column costs two grid barriers, whose
+    // cost grows with the blocks taking part, while its update is small.
+    static int cap_dev = -1, cap = 0, sms = 0;
+    int dev = 0;
+    SFMBA_CUDA(cudaGetDevice(&dev));
+    if (cap_dev != dev) {
+        cap = coop_capacity(k_lu_coop, 0);
+        SFMBA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cap_dev = dev;
+    }
+    if (n > 0 && launch_coop(k_lu_coop, cap, std::min(n, sms), 0, s, b.L, n, b.lu_perm, (const LMState *)b.state))
+        return;
     for (int k = 0; k < n; ++k) {
         k_lu_pivot<<<1, 1024, 0, s>>>(b.L, n, k, b.lu_perm, b.state);
         SFMBA_LAUNCH_CHECK();
