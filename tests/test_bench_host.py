@@ -54,3 +54,47 @@ def test_clock_summary_ignores_malformed_lines(tmp_path):
              "0, [N/A], 2070, 1.0, 0x0, Not Active, Not Active, Not Active, Not Active"]
     r = _sampler(tmp_path, lines, skip=0).stop()
     assert r["samples"] == 1 and r["sm_mhz"] == 2070.0
+
+
+def _traffic_csv(path, launches):
+    """An ncu --csv metrics log with the two DRAM counters per launch."""
+    rows = ['"ID","Process ID","Process Name","Host Name","Kernel Name","Context","Stream","Block Size",'
+            '"Grid Size","Device","CC","Section Name","Metric Name","Metric Unit","Metric Value"']
+    for i, (rd, wr) in enumerate(launches):
+        for name, unit, val in (("dram__bytes_read.sum", "Mbyte", rd), ("dram__bytes_write.sum", "Kbyte", wr)):
+            rows.append(f'"{i}","1","python3","h","void k_mf_points<float, 11, 1, 8, 3>(JacSrc<float>)","1","7",'
+                        f'"(256, 1, 1)","(2909, 1, 1)","0","10.3","Command line profiler metrics","{name}",'
+                        f'"{unit}","{val}"')
+    path.write_text("\n".join(rows) + "\n")
+
+
+def test_record_traffic_skips_launches_of_converged_solves(tmp_path, monkeypatch):
+    """Launches after a PCG solve converged return at once (a few KB of DRAM
+    traffic): the per-launch figure is the mean of the launches that ran an
+    iteration, keyed by the pass's sources."""
+    csv = tmp_path / "traffic.csv"
+    _traffic_csv(csv, [(0.011776, 0.0), (140.0, 3000.0), (0.011520, 0.0), (142.0, 5000.0)])
+    out = tmp_path / "ncu_traffic.json"
+    monkeypatch.setattr(bench, "TRAFFIC_FILE", str(out))
+    args = bench.argparse.Namespace(record_traffic=str(csv), workload="radial2000", scale=1.0)
+    bench.record_traffic(args)
+    import json
+
+    e = json.load(open(out))["entries"][0]
+    assert e["launches_captured"] == 2
+    assert e["dram_bytes_per_launch"] == int((140e6 + 3e6 + 142e6 + 5e6) / 2)
+    assert e["sources_sha"] == bench.sources_sha(bench.POINT_PASS_SOURCES)
+    traffic, src = bench.ncu_traffic("pcg_points", "radial2000", 1.0)
+    assert traffic == e["dram_bytes_per_launch"] and "ncu" in src
+
+
+def test_traffic_of_changed_sources_is_not_reported(tmp_path, monkeypatch):
+    import json
+
+    out = tmp_path / "ncu_traffic.json"
+    out.write_text(json.dumps({"entries": [{"phase": "pcg_points", "workload": "radial2000", "scale": 1.0,
+                                            "dram_bytes_per_launch": 1, "sources": bench.POINT_PASS_SOURCES,
+                                            "sources_sha": "0000000000000000"}]}))
+    monkeypatch.setattr(bench, "TRAFFIC_FILE", str(out))
+    traffic, src = bench.ncu_traffic("pcg_points", "radial2000", 1.0)
+    assert traffic is None and "changed" in src
