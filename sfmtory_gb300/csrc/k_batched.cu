@@ -105,35 +105,15 @@ __global__ void k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_n
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nP) return;
     if (!pt_live[p]) return;
-    const double lam = ws[pt_win[p]].lambda;
-    const T *C = pt_C + 6 * (size_t)p;
-    double m00 = C[0], m01 = C[1], m02 = C[2], m11 = C[3], m12 = C[4], m22 = C[5];
-    m00 = m00 + m00 * lam; m11 = m11 + m11 * lam; m22 = m22 + m22 * lam;
-    const double c00 = m11 * m22 - m12 * m12;
-    const double c01 = m12 * m02 - m01 * m22;
-    const double c02 = m01 * m12 - m11 * m02;
-    const double det = m00 * c00 + m01 * c01 + m02 * c02;
-    const bool ok = pt_nfree[p] > 0 && det != 0.0;
     T *Ci = pt_Cinv + 6 * (size_t)p;
     T *h = pt_h + 3 * (size_t)p;
+    const bool ok = point_block_inverse<T>(pt_C + 6 * (size_t)p, pt_g + 3 * (size_t)p, ws[pt_win[p]].lambda,
+                                           pt_nfree[p] > 0, Ci, h);
     if (!ok) {
         for (int k = 0; k < 6; ++k) Ci[k] = T(0);
         h[0] = h[1] = h[2] = T(0);
-        pt_ok[p] = 0;
-        return;
     }
-    const double id = 1.0 / det;
-    const double i00 = c00 * id, i01 = c01 * id, i02 = c02 * id;
-    const double i11 = (m00 * m22 - m02 * m02) * id;
-    const double i12 = (m02 * m01 - m00 * m12) * id;
-    const double i22 = (m00 * m11 - m01 * m01) * id;
-    Ci[0] = (T)i00; Ci[1] = (T)i01; Ci[2] = (T)i02; Ci[3] = (T)i11; Ci[4] = (T)i12; Ci[5] = (T)i22;
-    const T *g = pt_g + 3 * (size_t)p;
-    const double g0 = g[0], g1 = g[1], g2 = g[2];
-    h[0] = (T)(i00 * g0 + i01 * g1 + i02 * g2);
-    h[1] = (T)(i01 * g0 + i11 * g1 + i12 * g2);
-    h[2] = (T)(i02 * g0 + i12 * g1 + i22 * g2);
-    pt_ok[p] = 1;
+    pt_ok[p] = ok ? 1 : 0;
 }
 
 // Launch shapes of the batched Schur reduction, picked by the autotuner in
