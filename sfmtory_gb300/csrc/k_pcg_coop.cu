@@ -27,35 +27,42 @@ namespace sfmba {
 
 namespace {
 
-// Sum of v over the block's threads in a fixed order: warp butterflies
-// (every lane ends with the same value), then the warps' sums in warp
-// order. Every block that passes the same values gets the same bits.
-__device__ __forceinline__ double block_sum_c(double v, double *sh) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+// Sums of the blocks' partials X[0, G) and Y[0, G) (Y may be null), added
+// by the block's first warp in a fixed order (lane l: X[l], X[l + 32], ...,
+// then a butterfly) and handed to every thread: every block that reads the
+// same partials gets the same bits. One warp adds, so the block's other
+// warps do not contend for the FP64 pipe.
+__device__ __forceinline__ double2 grid_sums(const double *X, const double *Y, int G, double *sh) {
     __syncthreads();  // sh is free: its previous readers are done
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double r = 0.0;
-    const int nw = blockDim.x >> 5;
-    for (int w = 0; w < nw; ++w) r += sh[w];
-    return r;
-}
-
-// v[t] + v[t + B] + ... for thread t of a B-thread block, added in that order.
-__device__ __forceinline__ double strided_sum_c(const double *__restrict__ v, int n) {
-    const int B = blockDim.x;
-    double a = 0.0;
-    int k = threadIdx.x;
-    for (; k + 3 * B < n; k += 4 * B) {
-        double w[4];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double sx = 0.0, sy = 0.0;
+        for (int base = 0; base < G; base += 8 * 32) {
+            double wx[8], wy[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) w[u] = v[k + u * B];
+            for (int u = 0; u < 8; ++u) {
+                const int j = base + lane + 32 * u;
+                wx[u] = j < G ? X[j] : 0.0;
+                wy[u] = (Y && j < G) ? Y[j] : 0.0;
+            }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) a += w[u];
+            for (int u = 0; u < 8; ++u) {
+                sx += wx[u];
+                sy += wy[u];
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, off);
+            sy += __shfl_xor_sync(0xffffffffu, sy, off);
+        }
+        if (lane == 0) {
+            sh[0] = sx;
+            sh[1] = sy;
+        }
     }
-    for (; k < n; k += B) a += v[k];
-    return a;
+    __syncthreads();
+    return make_double2(sh[0], sh[1]);
 }
 
 template <typename T>
@@ -185,8 +192,8 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
     }
     // alpha = (r.z) / (p.q); x += alpha p; r -= alpha q; z = M^-1 r; r.z, r.r partials.
     {
-        double pq = block_sum_c(strided_sum_c(PQ, G), sh);
-        if (shared_cams) pq += block_sum_c(strided_sum_c(PQS, G), sh);
+        const double2 pqs = grid_sums(PQ, shared_cams ? PQS : nullptr, G, sh);
+        const double pq = shared_cams ? pqs.x + pqs.y : pqs.x;
         if (!(pq > 0.0) || !isfinite(pq)) {  // breakdown (every block sees it): keep the iterate
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 st->pcg_done = 1;
@@ -255,11 +262,32 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         // images, r.z / r.r partials.
         __shared__ T zcs[kMaxCoarseClusters * 14];
         __shared__ T ccs[3 * 16];
+        __shared__ int cls[kMaxCoarseClusters + 1];  // clu_start
+        __shared__ int cl0[kMaxCoarseClusters];      // cluster of the first image of a cluster's first block
+        for (int c = threadIdx.x; c <= a.nc; c += blockDim.x) {
+            const int st0 = a.clu_start[c];
+            cls[c] = st0;
+            if (c < a.nc) cl0[c] = a.clu_start[c + 1] > st0 ? a.img_cluster[(st0 >> 3) * 8] : 0;  // empty: unused
+        }
+        __syncthreads();
+        // Cluster c spans blocks b0..b1; every block after b0 starts inside c
+        // (its slot 0), block b0 holds c in slot c - cluster(8 b0). Sums in
+        // block order; the loads of a chunk are issued before its adds.
         for (int e = threadIdx.x; e < a.Nc; e += blockDim.x) {
             const int c = e / D, d = e - c * D;
-            const int b0 = a.clu_start[c] / 8, b1 = (a.clu_start[c + 1] - 1) / 8;
+            const int b0 = cls[c] >> 3, b1 = (cls[c + 1] - 1) >> 3;
             T v = T(0);
-            for (int b = b0; b <= b1; ++b) v += zpart[((size_t)b * 3 + (c - a.img_cluster[b * 8])) * D + d];
+            if (b1 >= b0) {
+                v = zpart[((size_t)b0 * 3 + (c - cl0[c])) * D + d];
+                for (int b = b0 + 1; b <= b1; b += 8) {
+                    T w[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) w[u] = b + u <= b1 ? zpart[(size_t)(b + u) * 3 * D + d] : T(0);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        if (b + u <= b1) v += w[u];
+                }
+            }
             zcs[e] = v;
         }
         __syncthreads();
@@ -268,13 +296,44 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         if (i0 < nI) {
             const int c0 = a.img_cluster[i0], nrow = (a.img_cluster[i1 - 1] - c0 + 1) * D;
             const int wl = threadIdx.x >> 5;
-            for (int rl = wl; rl < nrow; rl += blockDim.x >> 5) {
-                const float *ar = a.Ainv + (size_t)(c0 * D + rl) * a.Nc;
-                T s = T(0);
-                for (int j = lane; j < a.Nc; j += 32) s += (T)__ldg(ar + j) * zcs[j];
+            // Rows rl, rl + 8, rl + 16 of A_c^-1 per warp at a time, eight
+            // column loads per row in flight; each lane adds its columns in
+            // column order, then the butterfly.
+            constexpr int RW = 3;
+            for (int rl = wl; rl < nrow; rl += 8 * RW) {
+                const float *ar[RW];
+                T s[RW];
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-                if (lane == 0) ccs[rl] = s;
+                for (int k = 0; k < RW; ++k) {
+                    const int row = min(rl + 8 * k, nrow - 1);
+                    ar[k] = a.Ainv + (size_t)(c0 * D + row) * a.Nc;
+                    s[k] = T(0);
+                }
+                for (int base = 0; base < a.Nc; base += 8 * 32) {
+                    float w[RW][8];
+#pragma unroll
+                    for (int k = 0; k < RW; ++k)
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int j = base + lane + 32 * u;
+                            w[k][u] = j < a.Nc ? __ldg(ar[k] + j) : 0.0f;
+                        }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int j = base + lane + 32 * u;
+                        if (j < a.Nc) {
+                            const T zj = zcs[j];
+#pragma unroll
+                            for (int k = 0; k < RW; ++k) s[k] += (T)w[k][u] * zj;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < RW; ++k) {
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], off);
+                    if (lane == 0 && rl + 8 * k < nrow) ccs[rl + 8 * k] = s[k];
+                }
             }
             __syncthreads();
             const int i = gw;
@@ -375,8 +434,8 @@ __global__ void __launch_bounds__(256) k_pcg_vec_coop(VecArgs<T> a) {
         grid.sync();
     }
     // convergence test, beta, p = z + beta p
-    const double rz = block_sum_c(strided_sum_c(RZ, G), sh);
-    const double rr = block_sum_c(strided_sum_c(RR, G), sh);
+    const double2 rzr = grid_sums(RZ, RR, G, sh);
+    const double rz = rzr.x, rr = rzr.y;
     const bool stop = rr <= st->pcg_tol2 * st->pcg_bb || !(rz > 0.0) || !isfinite(rz);
     const double beta = stop ? 0.0 : rz / st->pcg_rzbuf[a.parity];
     if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -347,6 +347,80 @@ __global__ void __launch_bounds__(128) k_mf_image_finish0(const T *__restrict__ 
     }
 }
 
+// Minimum pivot of the FP32 factorisation of a unit-diagonal block: below
+// it the block is factorised in FP64 instead.
+constexpr float kMinScaledPivot = 1e-3f;
+
+// FP32 inverse of the damped image block L (FP64, symmetric) into Mi: the
+// block scaled to a unit diagonal (s_a = 1/sqrt(L_aa)), factorised by a
+// right-looking Cholesky in FP32, its inverse one column per lane, and
+// Mi = S (S L S)^-1 S. False (Mi untouched) when a diagonal entry is not
+// positive or a scaled pivot falls below kMinScaledPivot: the caller then
+// factorises in FP64. The FP32 path's preconditioner is stored in FP32, and
+// a 1e-3 pivot bounds the FP32 factorisation's error in the inverse to about
+// 1e-3 relative, which leaves the preconditioned iteration unchanged in
+// practice; GB300 runs FP64 at 1/64 of the FP32 rate, and the FP64
+// factorisation's square roots and divisions dominated this kernel.
+template <int D>
+__device__ __forceinline__ bool image_block_inverse_f32(const double (&L)[D][D + 1], double (&Mi)[D][D + 1],
+                                                        float (&A)[D][D + 1], float *sc, float *inv, int lane) {
+    bool pos = true;
+    if (lane < D) {
+        const double dd = L[lane][lane];
+        pos = dd > 0.0 && isfinite(dd);
+        sc[lane] = pos ? rsqrtf((float)dd) : 0.0f;
+    }
+    if (!__all_sync(0xffffffffu, pos)) return false;
+    __syncwarp();
+    for (int idx = lane; idx < D * D; idx += 32) {
+        const int a = idx / D, b = idx - a * D;
+        A[a][b] = (float)L[a][b] * sc[a] * sc[b];
+    }
+    __syncwarp();
+    for (int j = 0; j < D; ++j) {
+        const float d = A[j][j];
+        if (!(d > kMinScaledPivot) || !isfinite(d)) return false;  // every lane read the same d
+        const float sd = sqrtf(d);
+        const float id = 1.0f / sd;
+        __syncwarp();
+        if (lane == 0) {
+            A[j][j] = sd;
+            inv[j] = id;
+        }
+        if (lane > j && lane < D) A[lane][j] *= id;
+        __syncwarp();
+        const int m = D - j - 1;
+        for (int idx = lane; idx < m * m; idx += 32) {
+            const int q = j + 1 + idx / m, c = j + 1 + idx % m;
+            if (c <= q) A[q][c] = fmaf(-A[q][j], A[c][j], A[q][c]);
+        }
+        __syncwarp();
+    }
+    float col[D];
+    if (lane < D) {
+        const int c = lane;
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            float v = q == c ? 1.0f : 0.0f;
+#pragma unroll
+            for (int k = 0; k < q; ++k) v = fmaf(-A[q][k], col[k], v);
+            col[q] = q < c ? 0.0f : v * inv[q];
+        }
+#pragma unroll
+        for (int q = D - 1; q >= 0; --q) {
+            float v = col[q];
+#pragma unroll
+            for (int k = q + 1; k < D; ++k) v = fmaf(-A[k][q], col[k], v);
+            col[q] = v * inv[q];
+        }
+    }
+    __syncwarp();
+    if (lane < D)
+#pragma unroll
+        for (int q = 0; q < D; ++q) Mi[q][lane] = (double)(sc[q] * col[q] * sc[lane]);
+    return true;
+}
+
 // Block-Jacobi preconditioner (exact image diagonal block of the Schur
 // complement, Cholesky-inverted), reduced rhs and the PCG start vectors
 // (x = 0, r = rhs, p = z = M^-1 r) of image i, from its MODE-1 partials.
@@ -414,9 +488,15 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
         }
     }
     __syncwarp();
-    // Right-looking Cholesky of the D x D block, lower triangle in place.
-    bool ok = true;
-    for (int j = 0; j < D; ++j) {
+    bool done = false;  // FP32 path: Mi from the FP32 factorisation of the scaled block
+    if constexpr (std::is_same<T, float>::value) {
+        __shared__ float As[WPB][D][D + 1];
+        __shared__ float scs[WPB][D], invs[WPB][D];
+        done = image_block_inverse_f32<D>(L, Mi, As[wl], scs[wl], invs[wl], lane);
+    }
+    // Right-looking Cholesky of the D x D block in FP64, lower triangle in place.
+    bool ok = !done;  // the FP64 factorisation ran and succeeded
+    for (int j = 0; j < D && ok; ++j) {
         const double d = L[j][j];
         if (!(d > 0.0)) { ok = false; break; }
         const double sd = sqrt(d);
@@ -456,8 +536,8 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
         if (lane < D)
 #pragma unroll
             for (int q = 0; q < D; ++q) Mi[q][lane] = col[q];
-    } else {
-        // Not SPD in the kernel precision: Jacobi on the block's diagonal.
+    } else if (!done) {
+        // Not SPD in FP64: Jacobi on the block's diagonal.
         double dl = 0.0;
         if (lane < D) dl = Mi[lane][lane];
         __syncwarp();
