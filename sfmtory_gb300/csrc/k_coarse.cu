@@ -61,7 +61,8 @@ __global__ void k_coarse_count(const int *pt_start, const int *ob_img, const int
 }
 
 __global__ void k_coarse_emit(const int *pt_start, const int *ob_img, const int *img_cluster, int nP, int nc,
-                              const long long *off, const long long *inc_off, int *key, int *val, int *inc_cl) {
+                              const long long *off, const long long *inc_off, int *key, int *val, int *inc_cl,
+                              int *inc_pt) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nP) return;
     int cl[kMaxCoarseClusters];
@@ -69,6 +70,7 @@ __global__ void k_coarse_emit(const int *pt_start, const int *ob_img, const int 
     long long w = off[p];
     for (int a = 0; a < k; ++a) {
         inc_cl[inc_off[p] + a] = cl[a];
+        inc_pt[inc_off[p] + a] = p;
         for (int b = a; b < k; ++b) {
             key[w] = cl[a] * nc + cl[b];
             val[w] = p;
@@ -132,22 +134,15 @@ template <typename T, int D, bool RC, int M>
 __global__ void __launch_bounds__(128) k_coarse_y(JacSrc<T> J, const int *__restrict__ pt_start,
                                                   const int *__restrict__ img_cluster,
                                                   const int *__restrict__ img_pmask,
-                                                  const long long *__restrict__ inc_off,
-                                                  const int *__restrict__ inc_cl,
-                                                  const int *__restrict__ inc_order, int nP, long long ninc,
+                                                  const int *__restrict__ inc_pt, const int *__restrict__ inc_cl,
+                                                  const int *__restrict__ inc_order, long long ninc,
                                                   const unsigned char *__restrict__ pt_ok, T *__restrict__ Y) {
     // Threads take the incidences in track-length order, so a warp's
     // threads walk tracks of similar length.
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= ninc) return;
     const long long j = inc_order[t];
-    int lo = 0, hi = nP - 1;  // the point of incidence j: last p with inc_off[p] <= j
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (inc_off[mid] <= j) lo = mid;
-        else hi = mid - 1;
-    }
-    const int p = lo, c = inc_cl[j];
+    const int p = inc_pt[j], c = inc_cl[j];
     T y[3][D];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -667,7 +662,7 @@ void launch_coarse_group(const Bufs &b, const long long *off, long long npairs, 
                          int *val_sorted, int *key_counts, void *temp, size_t temp_bytes, cudaStream_t s) {
     const int nc = b.co.nc;
     k_coarse_emit<<<div_up(b.nP, 128), 128, 0, s>>>(b.pt_start, b.ob_img, b.co.img_cluster, b.nP, nc, off,
-                                                    b.co.inc_off, key, val, b.co.inc_cl);
+                                                    b.co.inc_off, key, val, b.co.inc_cl, b.co.inc_pt);
     SFMBA_LAUNCH_CHECK();
     size_t tb = temp_bytes;
     int bits = 1;
@@ -695,22 +690,21 @@ void launch_coarse_assemble(const Bufs &b, cudaStream_t s) {
     k_coarse_diag<<<co.nc, 128, 0, s>>>(b.img_H, b.img_pmask, co.clu_start, co.nc, D, b.state, co.A);
     SFMBA_LAUNCH_CHECK();
     if (co.nchunks > 0) {
+        const unsigned yb = (unsigned)div_up(co.ninc, 128);
+        dispatch_TDR(b, [&](auto t, auto dc, auto rc, auto mc) {  // Y with the camera model compiled in
+            using T = decltype(t);
+            k_coarse_y<T, decltype(dc)::value, decltype(rc)::value, decltype(mc)::value><<<yb, 128, 0, s>>>(
+                jac_src<T>(b), b.pt_start, co.img_cluster, b.img_pmask, co.inc_pt, co.inc_cl, co.inc_order, co.ninc,
+                b.pt_ok, (T *)co.ybuf);
+        });
+        SFMBA_LAUNCH_CHECK();
         dispatch_D(D, [&](auto dc) {
             constexpr int DD = decltype(dc)::value;
-            const unsigned yb = (unsigned)div_up(co.ninc, 128);
             if (b.mixed) {
-                k_coarse_y<float, DD, true, -1><<<yb, 128, 0, s>>>(jac_src<float>(b), b.pt_start, co.img_cluster,
-                                                                   b.img_pmask, co.inc_off, co.inc_cl, co.inc_order, b.nP,
-                                                                   co.ninc, b.pt_ok, (float *)co.ybuf);
-                SFMBA_LAUNCH_CHECK();
                 k_coarse_pairs<float, DD><<<div_up(co.nchunks, 4), 128, 0, s>>>(
                     (const float *)co.ybuf, co.inc_off, co.inc_cl, co.chunk, co.nchunks, co.pair_pt, co.group_cc,
                     (const float *)b.pt_Cinv, b.pt_ok, co.chunk_part);
             } else {
-                k_coarse_y<double, DD, false, -1><<<yb, 128, 0, s>>>(jac_src<double>(b), b.pt_start, co.img_cluster,
-                                                                     b.img_pmask, co.inc_off, co.inc_cl, co.inc_order, b.nP,
-                                                                     co.ninc, b.pt_ok, (double *)co.ybuf);
-                SFMBA_LAUNCH_CHECK();
                 k_coarse_pairs<double, DD><<<div_up(co.nchunks, 2), 64, 0, s>>>(
                     (const double *)co.ybuf, co.inc_off, co.inc_cl, co.chunk, co.nchunks, co.pair_pt, co.group_cc,
                     (const double *)b.pt_Cinv, b.pt_ok, co.chunk_part);

@@ -22,6 +22,7 @@ struct CoarseBufs {
     long long *inc_off = nullptr;     // [nP+1] first incidence of each point
     int *inc_cl = nullptr;            // [ninc] cluster of each incidence, increasing within a point
     int *inc_order = nullptr;         // [ninc] incidences by their point's track length (k_coarse_y's thread order)
+    int *inc_pt = nullptr;            // [ninc] point of each incidence
     void *ybuf = nullptr;             // [ninc][3*D] Y_c of each incidence, element type of the linearisation
     int ngroups = 0;
     int2 *group_cc = nullptr;         // [ngroups] (c, c'), c <= c'

@@ -334,7 +334,16 @@ __global__ void __launch_bounds__(128) k_mf_image_finish0(const T *__restrict__ 
     if (img_live && !img_live[i]) return;
     for (int e = lane; e < NV; e += 32) {
         double s = 0.0;
-        for (int k = ipart_off[i]; k < ipart_off[i + 1]; ++k) s += (double)part[(size_t)k * stride + e];
+        const int k1 = ipart_off[i + 1];
+        int k = ipart_off[i];
+        for (; k + 8 <= k1; k += 8) {  // eight loads in flight, added in partial order
+            T w[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) w[u] = part[(size_t)(k + u) * stride + e];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += (double)w[u];
+        }
+        for (; k < k1; ++k) s += (double)part[(size_t)k * stride + e];
         if (e < NH) {
             int t = e, a = 0;
             while (t >= D - a) { t -= D - a; ++a; }
@@ -460,7 +469,15 @@ __global__ void __launch_bounds__(128) k_mf_precond_finish(const T *__restrict__
     const int p0 = ipart_off[i], p1 = ipart_off[i + 1];
     for (int e = lane; e < NV; e += 32) {
         double sum = 0.0;
-        for (int k = p0; k < p1; ++k) sum += (double)part[(size_t)k * stride + e];
+        int k = p0;
+        for (; k + 8 <= p1; k += 8) {  // eight loads in flight, added in partial order
+            T w[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) w[u] = part[(size_t)(k + u) * stride + e];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) sum += (double)w[u];
+        }
+        for (; k < p1; ++k) sum += (double)part[(size_t)k * stride + e];
         if (e < NH) {
             int t = e, a = 0;
             while (t >= D - a) { t -= D - a; ++a; }

@@ -825,6 +825,7 @@ class Solver {
             co.chunk_part = P.take<double>((size_t)max_chunks * D * D);
             co.inc_cl = P.take<int>(ninc);
             co.inc_order = P.take<int>(ninc);
+            co.inc_pt = P.take<int>(ninc);
             co.ybuf = P.take<double>((size_t)ninc * 3 * D);  // FP64-sized: an FP64 polish reuses it
         }
         co.ninc = ninc;
