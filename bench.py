@@ -937,6 +937,8 @@ def run_ours(args):
         "phase_ms_profiled_step": {k: round(v["ms"], 3) for k, v in prof.items()
                                    if isinstance(v, dict) and v.get("launches")},
         "counts_profiled_step": prof.get("counts", {}),
+        "setup_host_ms_profiled_step": {k: round(v, 3) for k, v in prof.get("host_ms", {}).items()
+                                        if k.startswith("setup_")},
         "autotune_us": prof.get("autotune"),
     }
     if not args.skip_side and world == 1:

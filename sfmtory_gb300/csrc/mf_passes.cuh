@@ -113,6 +113,15 @@ __device__ __forceinline__ void point_chunk(const int4 *__restrict__ obrec, int 
     }
 }
 
+// Step shape of the once-per-retry point-major passes (point reduction,
+// back-substitution): in FP32 one round per step with the next step's
+// records loaded ahead, the shape the PCG point pass measured fastest; in
+// FP64 two rounds per step. The sums are the same either way.
+template <typename T>
+constexpr int kPtPassILP = sizeof(T) == 4 ? 1 : 2;
+template <typename T>
+constexpr bool kPtPassPF = sizeof(T) == 4;
+
 // C_p = sum Jx~^T Jx~, g_p = sum Jx~^T r~, free-block count (lib.rs:863-864, :870-879).
 template <typename T, int D, bool RC, int M>
 __global__ void __launch_bounds__(256) k_mf_point_reduce(JacSrc<T> J, const unsigned char *__restrict__ ob_valid,
@@ -123,7 +132,7 @@ __global__ void __launch_bounds__(256) k_mf_point_reduce(JacSrc<T> J, const unsi
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nchunks) return;
-    point_chunk<T, 10>(
+    point_chunk<T, 10, kPtPassILP<T>, kPtPassPF<T>>(
         J.obrec, pchunk[warp], pchunk[warp + 1], lane,
         [&](int o, int4 rc, T (&v)[10]) {
             ObsOp<T, D, RC, M> op;
@@ -794,7 +803,7 @@ __global__ void __launch_bounds__(256) k_mf_backsub(JacSrc<T> J, const int *__re
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nchunks) return;
-    point_chunk<T, 3>(
+    point_chunk<T, 3, kPtPassILP<T>, kPtPassPF<T>>(
         J.obrec, pchunk[warp], pchunk[warp + 1], lane,
         [&](int o, int4 rc, T (&v)[3]) {
             ObsOp<T, D, RC, M> op;

@@ -110,6 +110,23 @@ Profiler &profiler() {
     return p;
 }
 
+// Wall time of the set-up's stages under the profiler: mark(name) waits for
+// the stream and charges the time since the previous mark to name (host
+// work, host-device copies and the stage's kernels), so the stages add up
+// to the set-up phase. Does nothing when profiling is off.
+struct StageClock {
+    cudaStream_t s;
+    double t;
+    explicit StageClock(cudaStream_t stream) : s(stream), t(now_s()) {}
+    void mark(const char *name) {
+        if (!profiler().on) return;
+        SFMBA_CUDA(cudaStreamSynchronize(s));
+        const double u = now_s();
+        profiler().host(name, u - t);
+        t = u;
+    }
+};
+
 // Brackets the launches of one phase with events when profiling is on.
 struct PhaseScope {
     Profiler &p;
@@ -380,7 +397,10 @@ Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> 
         for (int k = 0; k < model_dof(model[c]); ++k)
             if (fixed_cp[(size_t)c * 8 + k]) L.slot_masked[L.cam_slot[c] + k] = 1;
     }
-    std::vector<std::vector<int>> pre(n);
+    // (slot, image block entry) of every image entry that maps to a slot, in
+    // image order; grouped by slot below (stable), one allocation for all.
+    std::vector<std::pair<int, int>> pre;
+    pre.reserve((size_t)n);
     std::vector<int> cam_users(nC, 0);
     for (int i = 0; i < nI; ++i) {
         const int c = cam_of_img[i];
@@ -388,7 +408,7 @@ Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> 
         if (L.pose_slot[i] >= 0)
             for (int r = 0; r < 6; ++r) {
                 L.img_slot[(size_t)i * D + r] = L.pose_slot[i] + r;
-                pre[L.pose_slot[i] + r].push_back(i * D + r);
+                pre.emplace_back(L.pose_slot[i] + r, i * D + r);
                 act |= 1 << r;
             }
         if (L.cam_slot[c] >= 0) {
@@ -397,7 +417,7 @@ Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> 
                 const int slot = L.cam_slot[c] + k;
                 if (L.slot_masked[slot]) continue;
                 L.img_slot[(size_t)i * D + 6 + k] = slot;
-                pre[slot].push_back(i * D + 6 + k);
+                pre.emplace_back(slot, i * D + 6 + k);
                 act |= 1 << (6 + k);
             }
         }
@@ -436,9 +456,13 @@ Layout make_layout(int nI, int nC, int nP, long long nO, const std::vector<int> 
             if (L.img_shcam[i] >= 0) L.sh_imgs[fill[L.img_shcam[i]]++] = i;
     }
     L.slot_pre_start.assign(n + 1, 0);
-    for (int a = 0; a < n; ++a) L.slot_pre_start[a + 1] = L.slot_pre_start[a] + (int)pre[a].size();
-    L.slot_pre.reserve(L.slot_pre_start[n]);
-    for (int a = 0; a < n; ++a) L.slot_pre.insert(L.slot_pre.end(), pre[a].begin(), pre[a].end());
+    for (const auto &e : pre) L.slot_pre_start[e.first + 1] += 1;
+    for (int a = 0; a < n; ++a) L.slot_pre_start[a + 1] += L.slot_pre_start[a];
+    L.slot_pre.assign(L.slot_pre_start[n], 0);
+    {
+        std::vector<int> fill(L.slot_pre_start.begin(), L.slot_pre_start.end() - 1);
+        for (const auto &e : pre) L.slot_pre[fill[e.first]++] = e.second;
+    }
     return L;
 }
 
@@ -952,6 +976,7 @@ class Solver {
                const Batch *batch = nullptr) {
         const int nI = (int)p->num_images, nC = (int)p->num_cameras, nP = (int)p->num_points;
         const long long nO = p->num_observations;
+        StageClock clk(s_);
         std::vector<int> cam_of_img = fetch(p->camera_of_image, nI, device, s_);
         std::vector<int> model = fetch(p->camera_model, nC, device, s_);
         for (int c = 0; c < nC; ++c)
@@ -1181,6 +1206,7 @@ class Solver {
             v2 = A.take<int>(nO);
         }
         Bufs &b = b_;
+        clk.mark("setup_layout");
         // Problem arrays.
         put(const_cast<int *>(b.cam_model), p->camera_model, nC, device, s_);
         put(const_cast<int *>(b.cam_of_img), p->camera_of_image, nI, device, s_);
@@ -1212,6 +1238,7 @@ class Solver {
         put_vec(b.slot_pre_start, lay_.slot_pre_start, s_);
         put_vec(b.slot_pre, lay_.slot_pre, s_);
         put_vec(b.slot_masked, lay_.slot_masked, s_);
+        clk.mark("setup_upload");
         if (need_system) {
             // Solver point order: by first observing image (see order_points).
             order_points(src_pt, src_img, nO, nP, nI, pkey, pkey2, piota, b.pt_perm, b.pt_old2new, obs_pt_new,
@@ -1223,6 +1250,7 @@ class Solver {
         sort_observations(src_pt, src_img, src_xy, nO, nP, nI, b, sort_temp, sort_tmp, k1, v1, k2, v2, s_);
         launch_split_xy_df(b, s_);
         SFMBA_CUDA(cudaMemsetAsync(b.state, 0, sizeof(LMState), s_));
+        clk.mark("setup_sort");
         if (need_system) {
             std::vector<int> img_start = fetch(b.img_start, (size_t)nI + 1, true, s_);
             if (solver_ == SFMBA_SOLVER_PCG) {
@@ -1235,7 +1263,9 @@ class Solver {
                 }
                 b.nparts = off[nI];
                 put_vec(b.ipart_off, off, s_);
+                clk.mark("setup_partition");
                 setup_coarse(o->pcg_coarse_clusters);
+                clk.mark("setup_coarse");
                 b.sh = SharedBufs();
                 if (lay_.sh_img_start.size() > 1) setup_shared(tsz);
             }
@@ -1253,6 +1283,7 @@ class Solver {
             put_vec(b.iachunk_off, ia_off, s_);
             if (b.pcg_p4) SFMBA_CUDA(cudaMemsetAsync(b.pcg_p4, 0, sizeof(float) * (size_t)nI * pad4(D), s_));
             launch_mf_prepare(b, s_);
+            clk.mark("setup_chunks");
         }
         if (need_system && solver_ == SFMBA_SOLVER_DENSE && n > 0) {
             // pair count scan uses the sort temp (cub scan needs little)
@@ -1303,6 +1334,7 @@ class Solver {
             launch_wb_window_of_points(win_in, b.pt_perm, nP, w.pt_win, s_);
         }
         if (mixed) launch_refresh_points32(b, s_);
+        clk.mark("setup_rest");
     }
 
     SolveOutput run(const sfmba_options *o) {
