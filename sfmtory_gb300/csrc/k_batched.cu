@@ -99,21 +99,11 @@ __global__ void k_wb_begin_retry(WinState *ws, int W) {
 
 // Damped point inverses with the damping of the point's window.
 template <typename T>
-__global__ void k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_nfree, const int *pt_win,
-                                   const WinState *ws, int nP, T *pt_Cinv, T *pt_h, unsigned char *pt_ok,
-                                   const unsigned char *pt_live) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nP) return;
-    if (!pt_live[p]) return;
-    T *Ci = pt_Cinv + 6 * (size_t)p;
-    T *h = pt_h + 3 * (size_t)p;
-    const bool ok = point_block_inverse<T>(pt_C + 6 * (size_t)p, pt_g + 3 * (size_t)p, ws[pt_win[p]].lambda,
-                                           pt_nfree[p] > 0, Ci, h);
-    if (!ok) {
-        for (int k = 0; k < 6; ++k) Ci[k] = T(0);
-        h[0] = h[1] = h[2] = T(0);
-    }
-    pt_ok[p] = ok ? 1 : 0;
+__global__ void __launch_bounds__(kPointInvBlock)
+    k_wb_point_inverse(const T *pt_C, const T *pt_g, const int *pt_nfree, const int *pt_win, const WinState *ws,
+                       int nP, T *pt_Cinv, T *pt_h, unsigned char *pt_ok, const unsigned char *pt_live) {
+    point_inverse_block<T>(pt_C, pt_g, pt_nfree, nP, [&](int q) { return ws[pt_win[q]].lambda; },
+                           [&](int q) { return pt_live[q] != 0; }, pt_Cinv, pt_h, pt_ok);
 }
 
 // Launch shapes of the batched Schur reduction, picked by the autotuner in
@@ -1063,12 +1053,12 @@ void launch_wb_begin_retry(const WinBufs &w, cudaStream_t s) {
 void launch_wb_point_inverse(const Bufs &b, const WinBufs &w, cudaStream_t s) {
     if (b.nP == 0) return;
     if (b.mixed)
-        k_wb_point_inverse<float><<<div_up(b.nP, 256), 256, 0, s>>>((const float *)b.pt_C, (const float *)b.pt_g,
+        k_wb_point_inverse<float><<<div_up(b.nP, kPointInvBlock), kPointInvBlock, 0, s>>>((const float *)b.pt_C, (const float *)b.pt_g,
                                                                     b.pt_nfree, w.pt_win, w.ws, b.nP,
                                                                     (float *)b.pt_Cinv, (float *)b.pt_h, b.pt_ok,
                                                                     b.pt_live);
     else
-        k_wb_point_inverse<double><<<div_up(b.nP, 256), 256, 0, s>>>((const double *)b.pt_C, (const double *)b.pt_g,
+        k_wb_point_inverse<double><<<div_up(b.nP, kPointInvBlock), kPointInvBlock, 0, s>>>((const double *)b.pt_C, (const double *)b.pt_g,
                                                                      b.pt_nfree, w.pt_win, w.ws, b.nP,
                                                                      (double *)b.pt_Cinv, (double *)b.pt_h, b.pt_ok,
                                                                      b.pt_live);

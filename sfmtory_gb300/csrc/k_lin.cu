@@ -173,23 +173,15 @@ __global__ void k_diag_fold(const double *img_H, const int *slot_pre_start, cons
 
 // (C_p + lambda diag C_p)^-1 for points with a free block (lib.rs:958-965),
 // adjugate over determinant (None iff det == 0), and h_p = C^-1 g_p
-// (point_block_inverse: FP64, or FP32 for well-conditioned blocks on the
+// (point_inverse_block: FP64, or FP32 for well-conditioned blocks on the
 // FP32 path).
 template <typename T>
-__global__ void k_point_inverse(const T *pt_C, const T *pt_g, const int *pt_nfree,
-                                const LMState *state, int nP, T *pt_Cinv, T *pt_h,
-                                unsigned char *pt_ok) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nP) return;
-    T *Ci = pt_Cinv + 6 * (size_t)p;
-    T *h = pt_h + 3 * (size_t)p;
-    const bool ok = point_block_inverse<T>(pt_C + 6 * (size_t)p, pt_g + 3 * (size_t)p, state->lambda,
-                                           pt_nfree[p] > 0, Ci, h);
-    if (!ok) {
-        for (int k = 0; k < 6; ++k) Ci[k] = T(0);
-        h[0] = h[1] = h[2] = T(0);
-    }
-    pt_ok[p] = ok ? 1 : 0;
+__global__ void __launch_bounds__(kPointInvBlock) k_point_inverse(const T *pt_C, const T *pt_g, const int *pt_nfree,
+                                                                  const LMState *state, int nP, T *pt_Cinv, T *pt_h,
+                                                                  unsigned char *pt_ok) {
+    const double lam = state->lambda;
+    point_inverse_block<T>(pt_C, pt_g, pt_nfree, nP, [&](int) { return lam; }, [](int) { return true; }, pt_Cinv,
+                           pt_h, pt_ok);
 }
 
 // rhs_i = -b_i + sum_o Jc~_o^T (Jx~_o h_p): the reduced right-hand side
@@ -685,11 +677,11 @@ void launch_diag_fold(const Bufs &b, cudaStream_t s) {
 void launch_point_inverse(const Bufs &b, cudaStream_t s) {
     if (b.nP == 0) return;
     if (b.mixed)
-        k_point_inverse<float><<<div_up(b.nP, 256), 256, 0, s>>>(
+        k_point_inverse<float><<<div_up(b.nP, kPointInvBlock), kPointInvBlock, 0, s>>>(
             (const float *)b.pt_C, (const float *)b.pt_g, b.pt_nfree, b.state, b.nP,
             (float *)b.pt_Cinv, (float *)b.pt_h, b.pt_ok);
     else
-        k_point_inverse<double><<<div_up(b.nP, 256), 256, 0, s>>>(
+        k_point_inverse<double><<<div_up(b.nP, kPointInvBlock), kPointInvBlock, 0, s>>>(
             (const double *)b.pt_C, (const double *)b.pt_g, b.pt_nfree, b.state, b.nP,
             (double *)b.pt_Cinv, (double *)b.pt_h, b.pt_ok);
     SFMBA_LAUNCH_CHECK();

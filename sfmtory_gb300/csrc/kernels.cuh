@@ -468,64 +468,122 @@ void launch_filter_keep(const int *orig, long long m, unsigned char *keep, long 
 // where the block is well conditioned (|det| > 1e-4 of the product of its
 // diagonal, which bounds det for a positive semi-definite block); a
 // near-singular block and the det == 0 decision fall back to FP64 from the
-// same FP32 entries, whose products FP64 holds exactly.
-template <typename T>
-__device__ __forceinline__ bool point_block_inverse(const T *C, const T *g, double lam, bool has_free, T *Ci, T *h) {
-    if constexpr (std::is_same<T, float>::value) {
-        const float l = (float)lam;
-        const float m00 = fmaf(C[0], l, C[0]), m11 = fmaf(C[3], l, C[3]), m22 = fmaf(C[5], l, C[5]);
-        const float m01 = C[1], m02 = C[2], m12 = C[4];
-        const float c00 = fmaf(m11, m22, -m12 * m12);
-        const float c01 = fmaf(m12, m02, -m01 * m22);
-        const float c02 = fmaf(m01, m12, -m11 * m02);
-        const float det = fmaf(m00, c00, fmaf(m01, c01, m02 * c02));
-        if (has_free && fabsf(det) > 1e-4f * fabsf(m00 * m11 * m22) && isfinite(det)) {
-            const float id = 1.0f / det;
-            const float i00 = c00 * id, i01 = c01 * id, i02 = c02 * id;
-            const float i11 = fmaf(m00, m22, -m02 * m02) * id;
-            const float i12 = fmaf(m02, m01, -m00 * m12) * id;
-            const float i22 = fmaf(m00, m11, -m01 * m01) * id;
-            Ci[0] = i00; Ci[1] = i01; Ci[2] = i02; Ci[3] = i11; Ci[4] = i12; Ci[5] = i22;
-            h[0] = fmaf(i00, g[0], fmaf(i01, g[1], i02 * g[2]));
-            h[1] = fmaf(i01, g[0], fmaf(i11, g[1], i12 * g[2]));
-            h[2] = fmaf(i02, g[0], fmaf(i12, g[1], i22 * g[2]));
-            return true;
+// same FP32 entries, whose products FP64 holds exactly. The FP32 stage and
+// the FP64 stage are separate functions so a block of threads can run the
+// second for its points side by side (point_inverse_block).
+__device__ __forceinline__ bool point_block_inverse_fast(const float *C, const float *g, double lam, bool has_free,
+                                                         float *Ci, float *h) {
+    const float l = (float)lam;
+    const float m00 = fmaf(C[0], l, C[0]), m11 = fmaf(C[3], l, C[3]), m22 = fmaf(C[5], l, C[5]);
+    const float m01 = C[1], m02 = C[2], m12 = C[4];
+    const float c00 = fmaf(m11, m22, -m12 * m12);
+    const float c01 = fmaf(m12, m02, -m01 * m22);
+    const float c02 = fmaf(m01, m12, -m11 * m02);
+    const float det = fmaf(m00, c00, fmaf(m01, c01, m02 * c02));
+    if (!(has_free && fabsf(det) > 1e-4f * fabsf(m00 * m11 * m22) && isfinite(det))) return false;
+    const float id = 1.0f / det;
+    const float i00 = c00 * id, i01 = c01 * id, i02 = c02 * id;
+    const float i11 = fmaf(m00, m22, -m02 * m02) * id;
+    const float i12 = fmaf(m02, m01, -m00 * m12) * id;
+    const float i22 = fmaf(m00, m11, -m01 * m01) * id;
+    Ci[0] = i00; Ci[1] = i01; Ci[2] = i02; Ci[3] = i11; Ci[4] = i12; Ci[5] = i22;
+    h[0] = fmaf(i00, g[0], fmaf(i01, g[1], i02 * g[2]));
+    h[1] = fmaf(i01, g[0], fmaf(i11, g[1], i12 * g[2]));
+    h[2] = fmaf(i02, g[0], fmaf(i12, g[1], i22 * g[2]));
+    return true;
+}
+// The FP64 stage of the FP32 path (a block the FP32 stage declined).
+__device__ __forceinline__ bool point_block_inverse_slow(const float *C, const float *g, double lam, bool has_free,
+                                                         float *Ci, float *h) {
+    if (!has_free) return false;
+    const float l = (float)lam;
+    const double d00 = fmaf(C[0], l, C[0]), d11 = fmaf(C[3], l, C[3]), d22 = fmaf(C[5], l, C[5]);
+    const double d01 = C[1], d02 = C[2], d12 = C[4];
+    const double e00 = d11 * d22 - d12 * d12, e01 = d12 * d02 - d01 * d22, e02 = d01 * d12 - d11 * d02;
+    const double dd = d00 * e00 + d01 * e01 + d02 * e02;
+    if (dd == 0.0) return false;
+    const double id = 1.0 / dd;
+    const double i00 = e00 * id, i01 = e01 * id, i02 = e02 * id;
+    const double i11 = (d00 * d22 - d02 * d02) * id, i12 = (d02 * d01 - d00 * d12) * id;
+    const double i22 = (d00 * d11 - d01 * d01) * id;
+    Ci[0] = (float)i00; Ci[1] = (float)i01; Ci[2] = (float)i02;
+    Ci[3] = (float)i11; Ci[4] = (float)i12; Ci[5] = (float)i22;
+    const double g0 = g[0], g1 = g[1], g2 = g[2];
+    h[0] = (float)(i00 * g0 + i01 * g1 + i02 * g2);
+    h[1] = (float)(i01 * g0 + i11 * g1 + i12 * g2);
+    h[2] = (float)(i02 * g0 + i12 * g1 + i22 * g2);
+    return true;
+}
+__device__ __forceinline__ bool point_block_inverse_fp64(const double *C, const double *g, double lam, bool has_free,
+                                                         double *Ci, double *h) {
+    double m00 = C[0], m01 = C[1], m02 = C[2], m11 = C[3], m12 = C[4], m22 = C[5];
+    m00 = m00 + m00 * lam; m11 = m11 + m11 * lam; m22 = m22 + m22 * lam;
+    const double c00 = m11 * m22 - m12 * m12;
+    const double c01 = m12 * m02 - m01 * m22;
+    const double c02 = m01 * m12 - m11 * m02;
+    const double det = m00 * c00 + m01 * c01 + m02 * c02;
+    if (!has_free || det == 0.0) return false;
+    const double id = 1.0 / det;
+    const double i00 = c00 * id, i01 = c01 * id, i02 = c02 * id;
+    const double i11 = (m00 * m22 - m02 * m02) * id;
+    const double i12 = (m02 * m01 - m00 * m12) * id;
+    const double i22 = (m00 * m11 - m01 * m01) * id;
+    Ci[0] = i00; Ci[1] = i01; Ci[2] = i02; Ci[3] = i11; Ci[4] = i12; Ci[5] = i22;
+    const double g0 = g[0], g1 = g[1], g2 = g[2];
+    h[0] = i00 * g0 + i01 * g1 + i02 * g2;
+    h[1] = i01 * g0 + i11 * g1 + i12 * g2;
+    h[2] = i02 * g0 + i12 * g1 + i22 * g2;
+    return true;
+}
+
+// Threads per block of the point-inverse kernels.
+constexpr int kPointInvBlock = 256;
+
+// The damped inverses of a block's points (one thread each; lam_of(p) the
+// point's damping, live(p) whether it takes part), None written as zeros
+// with pt_ok = 0. On the FP32 path the points the FP32 stage declines are
+// collected in shared memory and taken by the block's threads side by side
+// in the FP64 stage, so a near-singular point costs one lane's FP64 work
+// instead of its whole warp's (GB300 runs FP64 at 1/64 of the FP32 rate);
+// every point's result is the same as inverting it alone. Called by every
+// thread of a block of kPointInvBlock threads.
+template <typename T, typename Lam, typename Live>
+__device__ __forceinline__ void point_inverse_block(const T *pt_C, const T *pt_g, const int *pt_nfree, int nP,
+                                                    Lam lam_of, Live live, T *pt_Cinv, T *pt_h,
+                                                    unsigned char *pt_ok) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    auto finish = [&](int q, bool ok) {
+        if (!ok) {
+            T *Ci = pt_Cinv + 6 * (size_t)q;
+            T *h = pt_h + 3 * (size_t)q;
+            for (int k = 0; k < 6; ++k) Ci[k] = T(0);
+            h[0] = h[1] = h[2] = T(0);
         }
-        // near-singular (or no free block): FP64 from the same FP32 entries
-        const double d00 = m00, d01 = m01, d02 = m02, d11 = m11, d12 = m12, d22 = m22;
-        const double e00 = d11 * d22 - d12 * d12, e01 = d12 * d02 - d01 * d22, e02 = d01 * d12 - d11 * d02;
-        const double dd = d00 * e00 + d01 * e01 + d02 * e02;
-        if (!has_free || dd == 0.0) return false;
-        const double id = 1.0 / dd;
-        const double i00 = e00 * id, i01 = e01 * id, i02 = e02 * id;
-        const double i11 = (d00 * d22 - d02 * d02) * id, i12 = (d02 * d01 - d00 * d12) * id;
-        const double i22 = (d00 * d11 - d01 * d01) * id;
-        Ci[0] = (float)i00; Ci[1] = (float)i01; Ci[2] = (float)i02;
-        Ci[3] = (float)i11; Ci[4] = (float)i12; Ci[5] = (float)i22;
-        const double g0 = g[0], g1 = g[1], g2 = g[2];
-        h[0] = (float)(i00 * g0 + i01 * g1 + i02 * g2);
-        h[1] = (float)(i01 * g0 + i11 * g1 + i12 * g2);
-        h[2] = (float)(i02 * g0 + i12 * g1 + i22 * g2);
-        return true;
+        pt_ok[q] = ok ? 1 : 0;
+    };
+    if constexpr (std::is_same<T, float>::value) {
+        __shared__ int slow[kPointInvBlock];
+        __shared__ int nslow;
+        if (threadIdx.x == 0) nslow = 0;
+        __syncthreads();
+        if (p < nP && live(p)) {
+            if (point_block_inverse_fast(pt_C + 6 * (size_t)p, pt_g + 3 * (size_t)p, lam_of(p), pt_nfree[p] > 0,
+                                         pt_Cinv + 6 * (size_t)p, pt_h + 3 * (size_t)p))
+                pt_ok[p] = 1;
+            else
+                slow[atomicAdd(&nslow, 1)] = p;
+        }
+        __syncthreads();
+        const int n = nslow;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const int q = slow[k];
+            finish(q, point_block_inverse_slow(pt_C + 6 * (size_t)q, pt_g + 3 * (size_t)q, lam_of(q),
+                                               pt_nfree[q] > 0, pt_Cinv + 6 * (size_t)q, pt_h + 3 * (size_t)q));
+        }
     } else {
-        double m00 = C[0], m01 = C[1], m02 = C[2], m11 = C[3], m12 = C[4], m22 = C[5];
-        m00 = m00 + m00 * lam; m11 = m11 + m11 * lam; m22 = m22 + m22 * lam;
-        const double c00 = m11 * m22 - m12 * m12;
-        const double c01 = m12 * m02 - m01 * m22;
-        const double c02 = m01 * m12 - m11 * m02;
-        const double det = m00 * c00 + m01 * c01 + m02 * c02;
-        if (!has_free || det == 0.0) return false;
-        const double id = 1.0 / det;
-        const double i00 = c00 * id, i01 = c01 * id, i02 = c02 * id;
-        const double i11 = (m00 * m22 - m02 * m02) * id;
-        const double i12 = (m02 * m01 - m00 * m12) * id;
-        const double i22 = (m00 * m11 - m01 * m01) * id;
-        Ci[0] = i00; Ci[1] = i01; Ci[2] = i02; Ci[3] = i11; Ci[4] = i12; Ci[5] = i22;
-        const double g0 = g[0], g1 = g[1], g2 = g[2];
-        h[0] = i00 * g0 + i01 * g1 + i02 * g2;
-        h[1] = i01 * g0 + i11 * g1 + i12 * g2;
-        h[2] = i02 * g0 + i12 * g1 + i22 * g2;
-        return true;
+        if (p >= nP || !live(p)) return;
+        finish(p, point_block_inverse_fp64(pt_C + 6 * (size_t)p, pt_g + 3 * (size_t)p, lam_of(p), pt_nfree[p] > 0,
+                                           pt_Cinv + 6 * (size_t)p, pt_h + 3 * (size_t)p));
     }
 }
 
