@@ -416,7 +416,12 @@ int sfmba_dense_cholesky(int64_t n, const double *A, double *L, int32_t tensor_u
 int sfmba_profile_enable(int32_t on);
 
 /* JSON object {phase: {"ms": total device ms, "launches": n}} of the
- * profiled phases since the last sfmba_profile_enable, into buf[len]. */
+ * profiled phases since the last sfmba_profile_enable, into buf[len], with
+ * "kernel_launches", "host_ms" (wall ms of host-side stages: the batched
+ * entry's batch building and copies, and the set-up's stages "setup_layout",
+ * "setup_upload", "setup_sort", "setup_partition", "setup_coarse",
+ * "setup_chunks", "setup_rest", each waited for on the stream while
+ * profiling), "counts", "lm_trace" and "autotune". */
 int sfmba_profile_report(char *buf, int64_t len);
 
 /* Message of the last failed call on this thread ("" if none). */
